@@ -1,0 +1,330 @@
+#!/usr/bin/env python3
+"""Benchmark: multigrid cell-updates/s to a 1e-10 relative residual on one
+GB300, mixed precision (FP32 cycles inside FP64 defect correction) against
+the plain FP64 path, for the 2D 512x512 variable-coefficient projection
+Poisson problem div(Pi grad p) = f.
+
+Workload (synthetic, seeded): porosity chi = Gaussian-filtered white noise
+(correlation length 32 cells) mapped to [0.05, 1]; Kozeny-Carman permeability
+Pi = chi^3/(1-chi)^2 capped at 1e4; faces by geometric mean; f = div of a
+seeded random FP64 face velocity, mean removed; periodic in x, Neumann in y.
+
+One step = one complete solve from a zero initial guess to |r| <= 1e-10 |r0|
+(max norm).  `value` is device-timed with inputs resident in HBM; between
+steps a 512 MiB buffer is written to flush the 129 MB L2.  `e2e` times the
+same solve through the public C ABI with the step's rhs copied from pinned
+host memory and the solution copied back, every step.
+
+--impl reference times the CPU restatement of the reference algorithm
+(oracle, FP64, all host cores) on the same problem.
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "mushy-layer_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "tests"))
+
+import numpy as np  # noqa: E402
+
+N = 512
+SEED = 1
+TOL = 1e-10
+METRIC = "FAS V-cycle cell-updates/s on 1 GB300: mixed vs FP64 at 1e-10 rel residual"
+PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
+
+
+def make_problem(n=N, seed=SEED):
+    from problems import projection_problem
+    from oracle import oracle as O
+    g, chi, perm, u = projection_problem((n, n), seed, sigma=32.0)
+    faces = O.face_geomean(g, perm)
+    b = [-f for f in faces]
+    f = O.mac_divergence(g, u)
+    f -= f.mean()
+    return g, b, f
+
+
+def options(abi, ops, mixed):
+    o = ops.default_options(False)
+    o.tolerance, o.hang, o.max_iter = TOL, 1e-15, 300
+    o.precision = abi.PREC_MIXED if mixed else abi.PREC_F64
+    o.use_graph = 1
+    return o
+
+
+class Clocks:
+    """Samples nvidia-smi during the timed region."""
+
+    def __init__(self):
+        self.samples, self.stop = [], threading.Event()
+        self.t = None
+
+    def _run(self):
+        q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        while not self.stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0],
+                                      "--query-gpu=" + q, "--format=csv,noheader,nounits"],
+                                     capture_output=True, text=True, timeout=5).stdout.strip()
+                if out:
+                    self.samples.append([x.strip() for x in out.split(",")])
+            except Exception:
+                pass
+            self.stop.wait(0.2)
+
+    def __enter__(self):
+        self.t = threading.Thread(target=self._run, daemon=True)
+        self.t.start()
+        return self
+
+    def __exit__(self, *a):
+        self.stop.set()
+        self.t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4)
+                          if len(s) > 2 + i and s[2 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.samples)}
+
+
+def peaks():
+    try:
+        d = json.load(open(PEAKS))
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def run_gpu(args):
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    from mushy_gb300 import abi, ops
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    g, b, f = make_problem()
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    db = [dev(x) for x in b]
+    df = dev(f)
+    op = ops.ProjectionOp(g, abi.make_bc(), 0.0, 1.0, None, db)
+    solvers = {"mixed": ops.AMRMultiGrid(op, options(abi, ops, True)),
+               "fp64": ops.AMRMultiGrid(op, options(abi, ops, False))}
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    ncell = g.n[0] * g.n[1]
+    stream = torch.cuda.current_stream()
+
+    def timed(name, steps, warmup):
+        S = solvers[name]
+        phi = torch.zeros_like(df)
+        for _ in range(warmup):
+            phi.zero_()
+            st, rc = S.solve(phi, df)
+            assert rc == 0, "solve failed rc=%d" % rc
+        tot_ms, upd, last = 0.0, 0.0, None
+        for _ in range(steps):
+            phi.zero_()
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            if world > 1:
+                torch.distributed.barrier()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            st, rc = S.solve(phi, df)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            assert rc == 0, "solve failed rc=%d" % rc
+            tot_ms += e0.elapsed_time(e1)
+            upd += st.cell_updates
+            last = st
+        if world > 1:
+            t = torch.tensor([tot_ms], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            tot_ms = float(t.item())
+        return tot_ms, upd, last, phi
+
+    with Clocks() as clk:
+        ms_mixed, upd_mixed, st_mixed, phi_mixed = timed("mixed", args.steps, args.warmup)
+        ms_f64, upd_f64, st_f64, phi_f64 = timed("fp64", args.steps, args.warmup)
+
+    # error of the mixed solution against the FP64 solution (null space removed)
+    a = phi_f64.cpu().numpy()
+    m = phi_mixed.cpu().numpy()
+    err = float(np.abs((a - a.mean()) - (m - m.mean())).max() / np.abs(a - a.mean()).max())
+
+    # end to end through the C ABI: pinned host rhs -> device -> solve -> host
+    h_rhs = torch.from_numpy(f.copy()).pin_memory()
+    h_out = torch.empty_like(h_rhs).pin_memory()
+    d_rhs = torch.empty_like(df)
+    phi = torch.zeros_like(df)
+    S = solvers["mixed"]
+    for _ in range(args.warmup):
+        d_rhs.copy_(h_rhs, non_blocking=True)
+        phi.zero_()
+        S.solve(phi, d_rhs)
+        h_out.copy_(phi, non_blocking=True)
+    torch.cuda.synchronize()
+    e2e_ms, e2e_upd = 0.0, 0.0
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        d_rhs.copy_(h_rhs, non_blocking=True)
+        phi.zero_()
+        st, rc = S.solve(phi, d_rhs)
+        h_out.copy_(phi, non_blocking=True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        e2e_ms += e0.elapsed_time(e1)
+        e2e_upd += st.cell_updates
+
+    # dominant kernel: finest-level FP32 red/black half sweep, timed alone
+    op32 = ops.ProjectionOp(g, abi.make_bc(), 0.0, 1.0, None, [x.float() for x in db])
+    e32 = torch.zeros(df.shape, dtype=torch.float32, device="cuda")
+    r32 = df.float()
+    for _ in range(10):
+        op32.levelGSRBPass(e32, r32, 0)
+    reps = 200
+    k0, k1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    k0.record(stream)
+    for i in range(reps):
+        op32.levelGSRBPass(e32, r32, i & 1)
+    k1.record(stream)
+    torch.cuda.synchronize()
+    k_ms = k0.elapsed_time(k1) / reps
+    alg_bytes = 4 * (3 + 2) * ncell / 2.0   # one half of a full sweep's arrays (FP32, 2D)
+    hbm, kind = peaks()
+    achieved = alg_bytes / (k_ms * 1e-3) / 1e9
+
+    clocks = clk.summary()
+    value = upd_mixed / (ms_mixed * 1e-3) * world
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "cell-updates/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_mixed / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32-inner/f64-outer",
+        "data": "synthetic (seeded Kozeny-Carman permeability of a Gaussian-filtered porosity)",
+        "config": {"workload": "projection Poisson div(Pi grad p)=div u*, 2D 512x512, "
+                               "periodic x / Neumann y, to 1e-10 max-norm rel residual",
+                   "cells": ncell, "levels": st_mixed.levels, "l2": "flushed (512 MiB write) between steps",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "fp64": {"value": upd_f64 / (ms_f64 * 1e-3) * world, "ms_per_step": ms_f64 / args.steps,
+                 "iterations": st_f64.iterations, "cycles": st_f64.cycles},
+        "mixed": {"iterations": st_mixed.iterations, "cycles": st_mixed.cycles,
+                  "final_rel_residual": st_mixed.final_norm / st_mixed.initial_norm,
+                  "rel_err_vs_fp64_solution": err},
+        "time_to_solution_ratio_fp64_over_mixed": ms_f64 / ms_mixed,
+        "e2e": {"value": e2e_upd / (e2e_ms * 1e-3) * world, "unit": "cell-updates/s",
+                "h2d_bytes_per_step": int(ncell * 8), "d2h_bytes_per_step": int(ncell * 8)},
+        "roofline": {"bound": "hbm", "kernel": "vc_gsrb_kernel<float,2> (finest level)",
+                     "achieved": achieved, "peak": hbm, "peak_kind": kind, "unit": "GB/s",
+                     "frac": achieved / hbm, "traffic": None, "launch_us": k_ms * 1e3,
+                     "alg_bytes_per_launch": alg_bytes},
+        "clocks": clocks,
+        "gpu_launches": None,
+    }
+    if rank == 0:
+        line["cpu_baseline"] = cpu_baseline(args) if not args.no_cpu else None
+        print(json.dumps(line))
+
+
+def cpu_baseline(args, seconds=12.0):
+    from oracle import oracle as O
+    from mushy_gb300 import abi
+    g, b, f = make_problem()
+    ref = O.VCOpHost(g, abi.make_bc(), 0.0, 1.0, None, b)
+    o = O.default_options(0)
+    o.tolerance, o.hang, o.max_iter = TOL, 1e-15, 300
+    t0 = time.time()
+    upd, solves = 0.0, 0
+    while time.time() - t0 < seconds or solves == 0:
+        _, st, rc = O.vc_solve(ref, o, np.zeros_like(f), f)
+        upd += st.cell_updates
+        solves += 1
+    el = time.time() - t0
+    return {"value": upd / el, "unit": "cell-updates/s", "cores": os.cpu_count(),
+            "kind": "port", "sample": "%d full FP64 solves of the 512x512 problem (%.1f s)"
+                                      % (solves, el)}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    from mushy_gb300 import abi
+    g, b, f = make_problem()
+    ref = O.VCOpHost(g, abi.make_bc(), 0.0, 1.0, None, b)
+    o = O.default_options(0)
+    o.tolerance, o.hang, o.max_iter = TOL, 1e-15, 300
+    for _ in range(args.warmup):
+        O.vc_solve(ref, o, np.zeros_like(f), f)
+    t0 = time.time()
+    upd = 0.0
+    for _ in range(args.steps):
+        _, st, rc = O.vc_solve(ref, o, np.zeros_like(f), f)
+        upd += st.cell_updates
+    el = time.time() - t0
+    v = upd / el
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "cell-updates/s",
+        "n_gpus": int(os.environ.get("WORLD_SIZE", "1")), "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": el * 1e3 / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (same seeded problem)",
+        "config": {"workload": "projection Poisson div(Pi grad p)=div u*, 2D 512x512, "
+                               "periodic x / Neumann y, to 1e-10 max-norm rel residual"},
+        "cpu_baseline": {"value": v, "unit": "cell-updates/s", "cores": os.cpu_count(),
+                         "kind": "port", "sample": "%d full solves" % args.steps},
+        "e2e": {"value": v, "unit": "cell-updates/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0}}))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,311 @@
+/*
+ * mlgpu.h -- C ABI of the GB300 (sm_103a) elliptic/closure hot path of the
+ * mushy-layer solidification code.
+ *
+ * Everything here is plain C: device pointers, extents, POD parameter structs
+ * and a cudaStream_t passed as `void*`.  No allocation happens inside any
+ * entry point except where a function says so; multigrid hierarchies live in
+ * a caller-provided workspace.
+ *
+ * Data layout (one uniform box per level, no ghost cells stored):
+ *   cell field  [comp][k][j][i]            i fastest, n[0] x n[1] x n[2] cells
+ *   face field  b_d[comp][k][j][i]         direction d has n[d]+1 faces,
+ *                                          the other directions n cells
+ * Ghost values required by the 5/7-point stencils are produced in registers
+ * from the adjacent interior cell according to `mlgpu_bc` (first-order
+ * Dirichlet: ghost = 2v - interior; Neumann: ghost = interior + s*dx*g) or by
+ * periodic wrap.  That is exactly what a one-ghost-cell fill followed by the
+ * stencil computes in the reference, without the fill pass.
+ *
+ * Return codes: every entry point returns MLGPU_OK (0) or one of the codes
+ * below; nothing aborts the process and no kernel traps.
+ */
+#ifndef MLGPU_H_
+#define MLGPU_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+#define MLGPU_OK 0
+#define MLGPU_ERR_ARG 1           /* bad extents, null pointer, unsupported option */
+#define MLGPU_ERR_CUDA 2          /* a CUDA runtime call failed */
+#define MLGPU_ERR_NAN 3           /* NaN or Inf found by a fused norm */
+#define MLGPU_ERR_NOT_CONVERGED 4 /* iteration limit reached above tolerance */
+#define MLGPU_ERR_WORKSPACE 5     /* workspace too small or misaligned */
+#define MLGPU_ERR_HANG 6          /* solver stopped reducing the residual */
+#define MLGPU_ERR_SCRATCH 7       /* request exceeds a fixed-size scratch area */
+
+/* ---------------------------------------------------------------- types */
+enum { MLGPU_F64 = 0, MLGPU_F32 = 1 };
+enum { MLGPU_BC_NEUMANN = 0, MLGPU_BC_DIRICHLET = 1 };
+enum { MLGPU_RELAX_GSRB = 1, MLGPU_RELAX_JACOBI = 4 };     /* reference s_relaxMode */
+enum { MLGPU_PROLONG_CONSTANT = 0, MLGPU_PROLONG_LINEAR = 1 };
+enum { MLGPU_BOTTOM_RELAX = 0, MLGPU_BOTTOM_BICGSTAB = 1 };
+enum { MLGPU_PREC_F64 = 0, MLGPU_PREC_MIXED = 1 };
+enum { MLGPU_NORM_MAX = 0, MLGPU_NORM_L1 = 1, MLGPU_NORM_L2 = 2 };
+
+/* One uniform box: the reference's ProblemDomain + single-box layout. */
+typedef struct mlgpu_grid {
+  int dim;          /* 2 or 3 */
+  int n[3];         /* cells per direction; n[2] == 1 when dim == 2 */
+  double dx;        /* isotropic cell size */
+  int periodic[3];  /* ProblemDomain::isPeriodic(dir) */
+} mlgpu_grid;
+
+/* Physical boundary conditions per [dir][side][comp] for up to 2 components.
+ * side 0 = low, 1 = high.  Ignored in periodic directions. */
+typedef struct mlgpu_bc {
+  int type[3][2][2];
+  double value[3][2][2];
+} mlgpu_bc;
+
+/* MushyLayerParams fields used by the path (src/MushyLayerParams.h). */
+typedef struct mlgpu_params {
+  double compositionRatio;       /* CR */
+  double waterDistributionCoeff; /* k (partition coefficient) */
+  double specificHeatRatio;      /* cp */
+  double stefan;                 /* St */
+  double thetaEutectic;          /* theta_e */
+  double ThetaEutectic;          /* Theta_e */
+  double heatConductivityRatio;  /* k_T */
+  double heatDiffusionCoeff;     /* D_H */
+  double saltDiffusionCoeff;     /* D_C */
+  double darcyCoeff;
+  double viscosityCoeff;
+} mlgpu_params;
+
+/* Nonlinear enthalpy/bulk-concentration operator
+ *   L(phi) = alpha a phi - beta div(b grad f(phi)),  phi = (H, C), f = (T, C_l)
+ * (AMRNonLinearMultiCompOp).  Coefficient pointers are device pointers in the
+ * precision named by `dtype`; aCoef may be NULL meaning aCoef == 1. */
+typedef struct mlgpu_nlop {
+  mlgpu_grid grid;
+  mlgpu_params params;
+  mlgpu_bc phi_bc;       /* BC on (H, C): noFluxBC in the reference */
+  mlgpu_bc derived_bc;   /* BC on (T, C_l): temperatureLiquidSalinityBC */
+  int apply_derived_bc;  /* m_apply_bcs_to_diagnostic_var (default 1) */
+  double alpha, beta;
+  const void *aCoef;     /* [2][cells] or NULL */
+  const void *bCoef[3];  /* [2][faces_d] per direction */
+  int dtype;
+} mlgpu_nlop;
+
+/* Linear variable-coefficient operator for one component
+ *   L(phi) = alpha a phi - beta c phi - beta div(b grad phi)
+ * with c == NULL giving the VCAMRPoissonOp2/AMRProjectionOp operator and
+ * c != NULL the DarcyBrinkmanOp operator. */
+typedef struct mlgpu_vcop {
+  mlgpu_grid grid;
+  mlgpu_bc bc;           /* comp 0 only */
+  double alpha, beta;
+  const void *aCoef;     /* [cells] or NULL (== 1) */
+  const void *cCoef;     /* [cells] or NULL (== 0) */
+  const void *bCoef[3];  /* [faces_d] */
+  int dtype;
+} mlgpu_vcop;
+
+/* Multigrid / FAS solver settings (AMRMultiGrid::setSolverParameters). */
+typedef struct mlgpu_mg_options {
+  int num_smooth_down;   /* pre-smoothing sweeps */
+  int num_smooth_up;     /* post-smoothing sweeps */
+  int num_mg;            /* coarse-grid visits per level: 1 = V, 2 = W */
+  int max_iter;          /* outer iterations */
+  double tolerance;      /* stop when |r| <= tolerance * |r0| */
+  double hang;           /* stop when |r| > (1 - hang) * |r_prev| */
+  double norm_thresh;    /* stop when |r0| <= norm_thresh */
+  int relax_mode;        /* MLGPU_RELAX_GSRB or MLGPU_RELAX_JACOBI */
+  int bottom_solver;     /* MLGPU_BOTTOM_RELAX or MLGPU_BOTTOM_BICGSTAB */
+  int bottom_max_iter;   /* m_imax of the bottom solver */
+  int max_coarse;        /* s_maxCoarse: coarsen while coarsenable(2^d * max_coarse) */
+  int prolong;           /* MLGPU_PROLONG_* */
+  int precision;         /* MLGPU_PREC_F64 or MLGPU_PREC_MIXED */
+  int inner_cycles;      /* mixed: FP32 cycles per FP64 defect-correction step */
+  int norm_type;         /* MLGPU_NORM_MAX (reference default) or L2 */
+  int use_graph;         /* capture one cycle in a CUDA graph and replay it */
+} mlgpu_mg_options;
+
+typedef struct mlgpu_solve_stats {
+  int exit_status;       /* 0 converged, 2 hang, 4 max_iter, 8 NaN, ... */
+  int iterations;        /* outer iterations done */
+  int cycles;            /* V-cycles done (all precisions) */
+  int levels;            /* multigrid depth used */
+  double initial_norm;
+  double final_norm;
+  double cell_updates;   /* smoothing sweeps + residual/operator evaluations, in cells */
+  double norm_history[64];
+} mlgpu_solve_stats;
+
+typedef struct mlgpu_solver mlgpu_solver;  /* opaque */
+
+/* ------------------------------------------------------------ utilities */
+const char *mlgpu_status_string(int status);
+int mlgpu_version(void);
+
+/* ------------------------------------------------ closure (a1-a5) -------
+ * Full enthalpy closure H, C -> T, porosity, C_l, C_s and the bounding
+ * energies, FP64 on every cell.  Replaces updateEnthalpyVariables
+ * (src/phaseDiagram.cpp:92-177) and the Fortran CALCULATE_BOUNDING_ENERGY /
+ * CALCULATEPOROSITY / CALCULATECL / CALCULATECS / CALCULATET
+ * (src/EnthalpyVariablesF.ChF:13-284, :657-698).
+ * HC = [2][cells]; any output pointer may be NULL. */
+int mlgpu_closure(const mlgpu_grid *grid, const mlgpu_params *p,
+                  const double *HC, double *T, double *porosity, double *Cl,
+                  double *Cs, double *Hs, double *He, double *Hl, void *stream);
+
+/* (T, C_l) = f(H, C) on every cell: CALCULATE_T_CL
+ * (src/EnthalpyVariablesF.ChF:419-467) preceded by CALCULATE_BOUNDING_ENERGY,
+ * i.e. AMRNonLinearMultiCompOp::computeDiffusedVar on valid cells
+ * (src/AMRNonLinearMultiCompOp.cpp:57-98). */
+int mlgpu_closure_tcl(const mlgpu_grid *grid, const mlgpu_params *p,
+                      const double *HC, double *TCl, void *stream);
+
+/* ---------------------------------------- nonlinear operator (a6-a12) --- */
+/* Bytes of device scratch the fused norms need (norm_type >= 0 below). */
+size_t mlgpu_norm_workspace_bytes(void);
+
+/* res = rhs - L(phi); with norm_type >= 0 also the norm of res (MLGPU_NORM_*)
+ * into *norm (host, the call then synchronises `stream`), using `ws` of at
+ * least mlgpu_norm_workspace_bytes() bytes.  norm_type < 0: no norm, ws may
+ * be NULL.
+ * AMRNonLinearMultiCompOp::residualI (src/AMRNonLinearMultiCompOp.cpp:100-166)
+ * -> NLVCCOMPUTERES (src/AMRNonLinearMultiCompOpF.ChF:350-434). */
+int mlgpu_nl_residual(const mlgpu_nlop *op, void *res, const void *phi,
+                      const void *rhs, int norm_type, double *norm, void *ws,
+                      size_t ws_bytes, void *stream);
+
+/* lhs = L(phi): applyOpI / applyOpNoBoundary2 (:208-352) -> NLVCCOMPUTEOP
+ * (src/AMRNonLinearMultiCompOpF.ChF:233-313). */
+int mlgpu_nl_apply(const mlgpu_nlop *op, void *lhs, const void *phi,
+                   void *stream);
+
+/* One red (pass 0) or black (pass 1) nonlinear Gauss-Seidel half sweep:
+ * levelGSRB (:815-949) -> NONLINEARSMOOTHING (F.ChF:50-198), lambda from
+ * resetLambda/SUMFACESNLVC (:540-573, F.ChF:598-625) recomputed inline. */
+int mlgpu_nl_gsrb_pass(const mlgpu_nlop *op, void *phi, const void *rhs,
+                       int pass, void *stream);
+
+/* n full red+black sweeps (levelGSRB called n times, AMRPoissonOp::relax). */
+int mlgpu_nl_relax(const mlgpu_nlop *op, void *phi, const void *rhs,
+                   int n_sweeps, void *stream);
+
+/* Weighted Jacobi: phi += 0.5 lambda (rhs - L phi): levelJacobi (:1077-1101).
+ * `tmp` is caller scratch of the size of phi. */
+int mlgpu_nl_jacobi(const mlgpu_nlop *op, void *phi, const void *rhs,
+                    void *tmp, void *stream);
+
+/* lambda = 1 / diag(L): resetLambda (:540-573) as an explicit field. */
+int mlgpu_nl_lambda(const mlgpu_nlop *op, void *lambda, void *stream);
+
+/* FAS residual restriction: res_c = avg_{2^D}(rhs - L phi), with res_c fully
+ * overwritten.  restrictResidual (:373-451) -> RESTRICTRESNLVC (F.ChF:465-542). */
+int mlgpu_nl_restrict_residual(const mlgpu_nlop *op, void *res_coarse,
+                               const void *phi, const void *rhs, void *stream);
+
+/* -------------------------------------------- transfers (a12-a15, a18) -- */
+/* phi_c = avg_{2^D} phi_f for ncomp components (restrictR :492-514 ->
+ * RESTRICT F.ChF:555-585; also CoarseAverage for cell coefficients). */
+int mlgpu_restrict_average(const mlgpu_grid *fine, int ncomp, int dtype,
+                           void *coarse, const void *fine_data, void *stream);
+
+/* phi_f += P e_c.  MLGPU_PROLONG_LINEAR follows the stencil of PROLONG_JP
+ * (src/AMRProjectionOpF.ChF:15-78), MLGPU_PROLONG_CONSTANT is piecewise
+ * constant injection.  Coarse ghosts use the homogeneous form of `bc`. */
+int mlgpu_prolong_increment(const mlgpu_grid *fine, const mlgpu_bc *bc,
+                            int ncomp, int dtype, int kind, void *fine_data,
+                            const void *coarse, void *stream);
+
+/* Face coefficient coarsening (CoarseAverageFace, arithmetic): each coarse
+ * face is the mean of the 2^(D-1) fine faces it covers. */
+int mlgpu_coarsen_faces(const mlgpu_grid *fine, int ncomp, int dtype, int dir,
+                        void *coarse_faces, const void *fine_faces,
+                        void *stream);
+
+/* Geometric-mean face average sqrt(|c_lo c_hi|) (CELLTOEDGEGEOMETRIC,
+ * src/CellToEdge2F.ChF) of a cell field; boundary faces of non-periodic
+ * directions use a zero-gradient ghost (face = |c|). FP64. */
+int mlgpu_face_geomean(const mlgpu_grid *grid, const double *cell,
+                       double *faces[3], void *stream);
+
+/* ----------------------------------- linear operators (a16, a17, a19) -- */
+/* res = rhs - L(phi) for the projection (c == NULL) or Darcy-Brinkman op:
+ * VCCOMPUTERES / DBCOMPUTERES (src/DarcyBrinkmanOpF.ChF:299-396). */
+int mlgpu_vc_residual(const mlgpu_vcop *op, void *res, const void *phi,
+                      const void *rhs, int homogeneous, int norm_type,
+                      double *norm, void *ws, size_t ws_bytes, void *stream);
+int mlgpu_vc_apply(const mlgpu_vcop *op, void *lhs, const void *phi,
+                   int homogeneous, void *stream);
+/* GSRB half sweep (GSRBHELMHOLTZDB, F.ChF:46-159; homogeneous BCs as in
+ * DarcyBrinkmanOp::levelGSRB :503-576). */
+int mlgpu_vc_gsrb_pass(const mlgpu_vcop *op, void *phi, const void *rhs,
+                       int pass, void *stream);
+int mlgpu_vc_relax(const mlgpu_vcop *op, void *phi, const void *rhs,
+                   int n_sweeps, void *stream);
+int mlgpu_vc_jacobi(const mlgpu_vcop *op, void *phi, const void *rhs,
+                    void *tmp, void *stream);
+int mlgpu_vc_lambda(const mlgpu_vcop *op, void *lambda, void *stream);
+/* RESTRICTRESDB (F.ChF:427-505), homogeneous BCs. */
+int mlgpu_vc_restrict_residual(const mlgpu_vcop *op, void *res_coarse,
+                               const void *phi, const void *rhs, void *stream);
+
+/* ------------------------------------ MAC projection pieces (8f row 1) -- */
+/* div = sum_d (u_d[i+e_d] - u_d[i]) / dx  (DIVERGENCE, util/DivergenceF.ChF) */
+int mlgpu_mac_divergence(const mlgpu_grid *grid, double *div,
+                         const double *u[3], void *stream);
+/* u_d -= scale_d * (phi[i] - phi[i-e_d]) / dx on every face, ghosts of phi
+ * from `bc` (inhomogeneous): levelGradientMAC + the correction loop of
+ * Projector::levelMacProject (srcSubcycle/Projector.cpp:942-968).
+ * scale may be NULL (scale == 1). */
+int mlgpu_mac_correct(const mlgpu_grid *grid, const mlgpu_bc *bc,
+                      const double *phi, const double *scale[3], double *u[3],
+                      void *stream);
+
+/* ---------------------------------------------- elementwise utilities -- */
+/* y = a x + b y on n elements (LinearOp::axby / incr). */
+int mlgpu_axpby(size_t n, int dtype, double a, const void *x, double b,
+                void *y, void *stream);
+/* norm of n elements into *out (host), MLGPU_NORM_*; FP64 accumulation;
+ * `ws` as for mlgpu_nl_residual. */
+int mlgpu_norm(size_t n, int dtype, const void *x, int norm_type, double *out,
+               void *ws, size_t ws_bytes, void *stream);
+/* dst (dtype_dst) = src (dtype_src) elementwise conversion. */
+int mlgpu_convert(size_t n, int dtype_dst, void *dst, int dtype_src,
+                  const void *src, void *stream);
+
+/* ---------------------------------------------------- solvers (E1-E4) -- */
+void mlgpu_mg_default_options(mlgpu_mg_options *opt, int hc_defaults);
+
+/* Bytes of device workspace a solver needs (coarse levels, coefficients,
+ * reduction scratch).  The caller allocates it (256-byte aligned). */
+int mlgpu_hc_solver_workspace(const mlgpu_nlop *op, const mlgpu_mg_options *o,
+                              size_t *bytes);
+int mlgpu_vc_solver_workspace(const mlgpu_vcop *op, const mlgpu_mg_options *o,
+                              size_t *bytes);
+
+/* FAS multigrid for the nonlinear H-C operator (AMRFASMultiGrid driving
+ * AMRNonLinearMultiCompOp; MGnewOp coarsening :1285-1501).  `op` must be FP64;
+ * the mixed precision variant builds FP32 copies inside the workspace. */
+int mlgpu_hc_solver_create(const mlgpu_nlop *op, const mlgpu_mg_options *o,
+                           void *workspace, size_t bytes, void *stream,
+                           mlgpu_solver **out);
+/* Linear multigrid for the projection / Darcy-Brinkman operator
+ * (AMRMultiGrid + VCAMRPoissonOp2 / DarcyBrinkmanOp). FP64 `op`. */
+int mlgpu_vc_solver_create(const mlgpu_vcop *op, const mlgpu_mg_options *o,
+                           void *workspace, size_t bytes, void *stream,
+                           mlgpu_solver **out);
+/* Solve L(phi) = rhs in place (phi holds the initial guess), FP64 arrays. */
+int mlgpu_solver_solve(mlgpu_solver *s, double *phi, const double *rhs,
+                       mlgpu_solve_stats *stats);
+/* Re-read alpha/beta (setAlphaAndBeta) and rebuild coarse coefficients. */
+int mlgpu_solver_set_alpha_beta(mlgpu_solver *s, double alpha, double beta);
+int mlgpu_solver_destroy(mlgpu_solver *s);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MLGPU_H_ */

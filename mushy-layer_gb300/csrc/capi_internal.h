@@ -1,0 +1,28 @@
+// capi_internal.h -- declarations shared by the C-ABI units (capi.cu,
+// solver.cu): descriptor conversion and the FP64-only launchers.
+#pragma once
+#include "launch.h"
+#include "nl_kernels.cuh"
+#include "vc_kernels.cuh"
+
+namespace mlgpu {
+
+bool valid_grid(const mlgpu_grid *g);
+template <class T> NLArgs<T> make_nl_args(const mlgpu_nlop &op);
+template <class T> VCArgs<T> make_vc_args(const mlgpu_vcop &op);
+int status_of(cudaError_t e);
+int finish_norm(int norm_type, double *part, int nparts, double *host_out, cudaStream_t s);
+
+cudaError_t launch_closure_full(long long n, const ClosureParams &p, const double *HC, double *T,
+                                double *por, double *Cl, double *Cs, double *Hs, double *He,
+                                double *Hl, cudaStream_t s);
+cudaError_t launch_closure_tcl(long long n, const ClosureParams &p, const double *HC, double *TCl,
+                               cudaStream_t s);
+cudaError_t launch_face_geomean(const Geom &G, int d, const double *cell, double *face,
+                                cudaStream_t s);
+cudaError_t launch_mac_div(const Geom &G, const double *u0, const double *u1, const double *u2,
+                           double *div, cudaStream_t s);
+cudaError_t launch_mac_correct(const Geom &G, const BCD &bc, int d, const double *phi,
+                               const double *scale, double *u, cudaStream_t s);
+
+}  // namespace mlgpu

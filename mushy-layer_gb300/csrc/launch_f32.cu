@@ -1,0 +1,42 @@
+// launch_f32.cu -- FP32 instantiations of the kernel launchers (inner
+// multigrid cycles of the mixed-precision solvers).  FMA contraction is left
+// on; the nonlinear closure inside these kernels still runs in FP64.
+#include "launch_impl.cuh"
+
+namespace mlgpu {
+
+template cudaError_t launch_nl_op<float>(const NLArgs<float> &, int, int, const float *,
+                                         const float *, float *, float *, double *, cudaStream_t);
+template cudaError_t launch_nl_gsrb<float>(const NLArgs<float> &, float *, const float *, int,
+                                           cudaStream_t);
+template cudaError_t launch_nl_relax_block<float>(const NLArgs<float> &, float *, const float *,
+                                                  int, cudaStream_t);
+template cudaError_t launch_nl_restrict<float>(const NLArgs<float> &, const Geom &, const float *,
+                                               const float *, float *, float *, cudaStream_t);
+template cudaError_t launch_nl_lambda<float>(const NLArgs<float> &, float *, cudaStream_t);
+template cudaError_t launch_vc_op<float>(const VCArgs<float> &, int, int, const float *,
+                                         const float *, float *, int, double *, cudaStream_t);
+template cudaError_t launch_vc_gsrb<float>(const VCArgs<float> &, float *, const float *, int,
+                                           cudaStream_t);
+template cudaError_t launch_vc_gsrb_zero<float>(const VCArgs<float> &, float *, const float *,
+                                                cudaStream_t);
+template cudaError_t launch_vc_relax_block<float>(const VCArgs<float> &, float *, const float *,
+                                                  int, int, cudaStream_t);
+template cudaError_t launch_vc_restrict<float>(const VCArgs<float> &, const Geom &, const float *,
+                                               const float *, float *, float *, cudaStream_t);
+template cudaError_t launch_vc_lambda<float>(const VCArgs<float> &, float *, cudaStream_t);
+template cudaError_t launch_restrict_avg<float>(const Geom &, int, const float *, float *,
+                                                cudaStream_t);
+template cudaError_t launch_prolong<float>(const Geom &, const BCD &, int, int, float *,
+                                           const float *, const float *, cudaStream_t);
+template cudaError_t launch_coarsen_faces<float>(const Geom &, int, int, const float *, float *,
+                                                 cudaStream_t);
+template cudaError_t launch_axpby<float>(long long, float, const float *, float, float *,
+                                         cudaStream_t);
+template cudaError_t launch_norm_partial<float>(long long, const float *, int, double *,
+                                                cudaStream_t);
+template cudaError_t launch_convert<float, double>(long long, float *, const double *,
+                                                  cudaStream_t);
+template cudaError_t launch_convert<float, float>(long long, float *, const float *, cudaStream_t);
+
+}  // namespace mlgpu

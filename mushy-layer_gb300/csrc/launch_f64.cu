@@ -1,0 +1,100 @@
+// launch_f64.cu -- FP64 instantiations of the kernel launchers.  Built with
+// --fmad=false: every FP64 product and sum is rounded separately, as in the
+// reference's Fortran, so FP64 results match the CPU restatement bit for bit.
+#define MLGPU_FP64_UNIT 1
+#include "launch_impl.cuh"
+
+namespace mlgpu {
+
+template cudaError_t launch_nl_op<double>(const NLArgs<double> &, int, int, const double *,
+                                          const double *, double *, double *, double *,
+                                          cudaStream_t);
+template cudaError_t launch_nl_gsrb<double>(const NLArgs<double> &, double *, const double *, int,
+                                            cudaStream_t);
+template cudaError_t launch_nl_relax_block<double>(const NLArgs<double> &, double *,
+                                                   const double *, int, cudaStream_t);
+template cudaError_t launch_nl_restrict<double>(const NLArgs<double> &, const Geom &,
+                                                const double *, const double *, double *,
+                                                double *, cudaStream_t);
+template cudaError_t launch_nl_lambda<double>(const NLArgs<double> &, double *, cudaStream_t);
+template cudaError_t launch_vc_op<double>(const VCArgs<double> &, int, int, const double *,
+                                          const double *, double *, int, double *, cudaStream_t);
+template cudaError_t launch_vc_update_residual<double, double>(const VCArgs<double> &, int,
+                                                               const double *, const double *,
+                                                               const double *, double *,
+                                                               double *, double *, double *,
+                                                               cudaStream_t);
+template cudaError_t launch_vc_update_residual<double, float>(const VCArgs<double> &, int,
+                                                              const double *, const float *,
+                                                              const double *, double *, double *,
+                                                              float *, double *, cudaStream_t);
+template cudaError_t launch_vc_gsrb<double>(const VCArgs<double> &, double *, const double *, int,
+                                            cudaStream_t);
+template cudaError_t launch_vc_gsrb_zero<double>(const VCArgs<double> &, double *, const double *,
+                                                 cudaStream_t);
+template cudaError_t launch_vc_relax_block<double>(const VCArgs<double> &, double *,
+                                                   const double *, int, int, cudaStream_t);
+template cudaError_t launch_vc_restrict<double>(const VCArgs<double> &, const Geom &,
+                                                const double *, const double *, double *,
+                                                double *, cudaStream_t);
+template cudaError_t launch_vc_lambda<double>(const VCArgs<double> &, double *, cudaStream_t);
+template cudaError_t launch_restrict_avg<double>(const Geom &, int, const double *, double *,
+                                                 cudaStream_t);
+template cudaError_t launch_prolong<double>(const Geom &, const BCD &, int, int, double *,
+                                            const double *, const double *, cudaStream_t);
+template cudaError_t launch_coarsen_faces<double>(const Geom &, int, int, const double *, double *,
+                                                  cudaStream_t);
+template cudaError_t launch_axpby<double>(long long, double, const double *, double, double *,
+                                          cudaStream_t);
+template cudaError_t launch_norm_partial<double>(long long, const double *, int, double *,
+                                                 cudaStream_t);
+template cudaError_t launch_convert<double, float>(long long, double *, const float *,
+                                                   cudaStream_t);
+template cudaError_t launch_convert<double, double>(long long, double *, const double *,
+                                                    cudaStream_t);
+
+cudaError_t launch_finalize_norm(int norm, const double *part, int nparts, double *out,
+                                 cudaStream_t s) {
+  switch (norm) {
+    case MLGPU_NORM_L1:
+      finalize_norm_kernel<MLGPU_NORM_L1><<<1, 1024, 0, s>>>(part, nparts, out);
+      break;
+    case MLGPU_NORM_L2:
+      finalize_norm_kernel<MLGPU_NORM_L2><<<1, 1024, 0, s>>>(part, nparts, out);
+      break;
+    default:
+      finalize_norm_kernel<MLGPU_NORM_MAX><<<1, 1024, 0, s>>>(part, nparts, out);
+      break;
+  }
+  return cudaGetLastError();
+}
+
+// full closure / MAC helpers are FP64-only and live in this unit too
+cudaError_t launch_closure_full(long long n, const ClosureParams &p, const double *HC, double *T,
+                                double *por, double *Cl, double *Cs, double *Hs, double *He,
+                                double *Hl, cudaStream_t s) {
+  closure_full_kernel<<<blocks_for(n), kBlock, 0, s>>>(n, p, HC, T, por, Cl, Cs, Hs, He, Hl);
+  return cudaGetLastError();
+}
+cudaError_t launch_closure_tcl(long long n, const ClosureParams &p, const double *HC, double *TCl,
+                               cudaStream_t s) {
+  closure_tcl_kernel<<<blocks_for(n), kBlock, 0, s>>>(n, p, HC, TCl);
+  return cudaGetLastError();
+}
+cudaError_t launch_face_geomean(const Geom &G, int d, const double *cell, double *face,
+                                cudaStream_t s) {
+  face_geomean_kernel<<<blocks_for(G.nface(d)), kBlock, 0, s>>>(G, d, cell, face);
+  return cudaGetLastError();
+}
+cudaError_t launch_mac_div(const Geom &G, const double *u0, const double *u1, const double *u2,
+                           double *div, cudaStream_t s) {
+  mac_div_kernel<<<blocks_for(G.ncell), kBlock, 0, s>>>(G, u0, u1, u2, div);
+  return cudaGetLastError();
+}
+cudaError_t launch_mac_correct(const Geom &G, const BCD &bc, int d, const double *phi,
+                               const double *scale, double *u, cudaStream_t s) {
+  mac_correct_kernel<<<blocks_for(G.nface(d)), kBlock, 0, s>>>(G, bc, d, phi, scale, u);
+  return cudaGetLastError();
+}
+
+}  // namespace mlgpu

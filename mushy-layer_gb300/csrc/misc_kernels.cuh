@@ -1,0 +1,291 @@
+// misc_kernels.cuh -- multigrid transfers, coefficient coarsening, the full
+// closure, MAC divergence/gradient correction and elementwise helpers.
+#pragma once
+#include "common.cuh"
+#include "reduce.cuh"
+
+namespace mlgpu {
+
+// ---------------------------------------------------------------- restrict
+// phi_c = avg_{2^D} phi_f, accumulated as in RESTRICT (F.ChF:555-585).
+template <class T, int DIM>
+__global__ void __launch_bounds__(kBlock) restrict_avg_kernel(Geom F, Geom C, int ncomp,
+                                                              const T *__restrict__ fine,
+                                                              T *__restrict__ coarse) {
+  const T denom = DIM == 3 ? T(8) : T(4);
+  long long total = C.ncell * ncomp;
+  for (long long t = gtid(); t < total; t += gstride()) {
+    int c = (int)(t / C.ncell);
+    long long Q = t % C.ncell;
+    int I, J, K;
+    cell_ijk(C, Q, I, J, K);
+    T acc = T(0);
+#pragma unroll
+    for (int kk = 0; kk < (DIM == 3 ? 2 : 1); kk++)
+#pragma unroll
+      for (int jj = 0; jj < 2; jj++)
+#pragma unroll
+        for (int ii = 0; ii < 2; ii++) {
+          int k = DIM == 3 ? 2 * K + kk : 0;
+          acc = acc + fine[c * F.ncell + F.cell(2 * I + ii, 2 * J + jj, k)] / denom;
+        }
+    coarse[t] = acc;
+  }
+}
+
+// ---------------------------------------------------------------- prolong
+// Coarse value with the homogeneous ghost rule applied per direction:
+// periodic wrap, else clamp to the boundary cell and negate for Dirichlet.
+template <class T>
+__device__ __forceinline__ T coarse_at(const Geom &C, const BCD &bc, int comp,
+                                       const T *__restrict__ a, const T *__restrict__ b,
+                                       int I, int J, int K) {
+  int idx[3] = {I, J, K};
+  T sign = T(1);
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    if (d >= C.dim) break;
+    int m = C.n(d);
+    if (idx[d] < 0 || idx[d] >= m) {
+      int side = idx[d] < 0 ? 0 : 1;
+      if (C.per(d)) {
+        idx[d] = idx[d] < 0 ? m - 1 : 0;
+      } else {
+        idx[d] = idx[d] < 0 ? 0 : m - 1;
+        if (bc.type[d][side][comp] == MLGPU_BC_DIRICHLET) sign = -sign;
+      }
+    }
+  }
+  long long q = comp * C.ncell + C.cell(idx[0], idx[1], idx[2]);
+  T v = b ? (a[q] - b[q]) : a[q];
+  return sign * v;
+}
+
+// phi_f += P (a - b) (b may be null): KIND 0 piecewise constant (Chombo
+// FORT_PROLONG), KIND 1 the linear stencil of PROLONG_JP
+// (src/AMRProjectionOpF.ChF:15-78).  The FAS correction u_c - u_c,old is
+// formed on the fly from its two operands.
+template <class T, int DIM, int KIND>
+__global__ void __launch_bounds__(kBlock) prolong_kernel(Geom F, Geom C, BCD bc, int ncomp,
+                                                         T *__restrict__ fine,
+                                                         const T *__restrict__ a,
+                                                         const T *__restrict__ b) {
+  long long total = F.ncell * ncomp;
+  const T den = T(1) / (DIM == 3 ? T(64) : T(16));
+  const T fx1 = T(3) * den, fx2 = T(9) * den, fx3 = T(27) * den, f0 = T(1) * den;
+  for (long long t = gtid(); t < total; t += gstride()) {
+    int c = (int)(t / F.ncell);
+    long long q = t % F.ncell;
+    int i, j, k;
+    cell_ijk(F, q, i, j, k);
+    int ic = i / 2, jc = j / 2, kc = DIM == 3 ? k / 2 : 0;
+    T p = fine[t];
+    if (KIND == MLGPU_PROLONG_CONSTANT) {
+      p = p + coarse_at(C, bc, c, a, b, ic, jc, kc);
+    } else {
+      int o1 = 2 * (i % 2) - 1, o2 = 2 * (j % 2) - 1, o3 = DIM == 3 ? 2 * (k % 2) - 1 : 0;
+      if (DIM == 2) {
+        p = p + fx2 * coarse_at(C, bc, c, a, b, ic, jc, kc) +
+            f0 * coarse_at(C, bc, c, a, b, ic + o1, jc + o2, kc);
+        p = p + fx1 * (coarse_at(C, bc, c, a, b, ic + o1, jc, kc) +
+                       coarse_at(C, bc, c, a, b, ic, jc + o2, kc));
+      } else {
+        p = p + fx3 * coarse_at(C, bc, c, a, b, ic, jc, kc) +
+            f0 * coarse_at(C, bc, c, a, b, ic + o1, jc + o2, kc + o3);
+        p = p + fx2 * (coarse_at(C, bc, c, a, b, ic + o1, jc, kc) +
+                       coarse_at(C, bc, c, a, b, ic, jc + o2, kc) +
+                       coarse_at(C, bc, c, a, b, ic, jc, kc + o3));
+        p = p + fx1 * (coarse_at(C, bc, c, a, b, ic + o1, jc + o2, kc) +
+                       coarse_at(C, bc, c, a, b, ic, jc + o2, kc + o3) +
+                       coarse_at(C, bc, c, a, b, ic + o1, jc, kc + o3));
+      }
+    }
+    fine[t] = p;
+  }
+}
+
+// ------------------------------------------------------- face coarsening
+// CoarseAverageFace (arithmetic): mean of the 2^(D-1) covered fine faces.
+template <class T, int DIM>
+__global__ void __launch_bounds__(kBlock) coarsen_faces_kernel(Geom F, Geom C, int ncomp, int d,
+                                                               const T *__restrict__ ff,
+                                                               T *__restrict__ cf) {
+  long long nfc = C.nface(d), nff = F.nface(d);
+  long long total = nfc * ncomp;
+  const T refScale = DIM == 3 ? T(0.25) : T(0.5);
+  int m0 = C.n0 + (d == 0), m1 = C.n1 + (d == 1);
+  for (long long t = gtid(); t < total; t += gstride()) {
+    int c = (int)(t / nfc);
+    long long r = t % nfc;
+    int I = (int)(r % m0);
+    long long rr = r / m0;
+    int J = (int)(rr % m1);
+    int K = (int)(rr / m1);
+    int rk = (DIM == 3 && d != 2) ? 2 : 1, rj = d != 1 ? 2 : 1, ri = d != 0 ? 2 : 1;
+    T sum = T(0);
+    for (int kk = 0; kk < rk; kk++)
+      for (int jj = 0; jj < rj; jj++)
+        for (int ii = 0; ii < ri; ii++) {
+          int fi = 2 * I + ii, fj = 2 * J + jj, fk = DIM == 3 ? 2 * K + kk : 0;
+          sum = sum + ff[c * nff + F.face(d, fi, fj, fk)];
+        }
+    cf[t] = sum * refScale;
+  }
+}
+
+#ifdef MLGPU_FP64_UNIT  // FP64-only kernels: compiled in launch_f64.cu alone
+// ------------------------------------------------------------ full closure
+// updateEnthalpyVariables (src/phaseDiagram.cpp:92-177) for one cell:
+// CALCULATEPOROSITY/CL/CS/T with the bounding energies.
+__global__ void __launch_bounds__(kBlock) closure_full_kernel(long long n, ClosureParams p,
+                                                              const double *__restrict__ HC,
+                                                              double *T, double *por, double *Cl,
+                                                              double *Cs, double *Hs,
+                                                              double *He, double *Hl) {
+  for (long long q = gtid(); q < n; q += gstride()) {
+    double H = HC[q], C = HC[q + n];
+    double hs, he, hl;
+    bounding_energy(C, p, hs, he, hl);
+    double t, po, cl, cs;
+    if (H <= hs) {
+      po = 0;
+      cl = p.Te;
+      cs = C;
+      t = H / p.cp;
+    } else if (H > hs && H <= he) {
+      po = (H - p.te * p.cp) / (p.St + p.te * (1 - p.cp));
+      cl = p.Te;
+      double pm = porosity_mush(C, H, p);  // CALCULATECS uses the mush root here
+      cs = C / (1 - pm);
+      t = p.te;
+    } else if (H > he && H < hl) {
+      double pm = porosity_mush(C, H, p);
+      po = pm;
+      cl = (C + p.CR * (1 - pm)) / (pm + p.k * (1 - pm));
+      cs = (C * p.k - p.CR * pm) / (pm + p.k * (1 - pm));
+      t = -(C + p.CR * (1 - pm)) / (pm + p.k * (1 - pm));
+    } else if (H >= hl) {
+      po = 1;
+      cl = C;
+      cs = 0;
+      t = H - p.St;
+    } else {
+      po = H; cl = H; cs = H; t = H;
+    }
+    if (T) T[q] = t;
+    if (por) por[q] = po;
+    if (Cl) Cl[q] = cl;
+    if (Cs) Cs[q] = cs;
+    if (Hs) Hs[q] = hs;
+    if (He) He[q] = he;
+    if (Hl) Hl[q] = hl;
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) closure_tcl_kernel(long long n, ClosureParams p,
+                                                             const double *__restrict__ HC,
+                                                             double *__restrict__ TCl) {
+  for (long long q = gtid(); q < n; q += gstride()) t_cl(HC[q], HC[q + n], p, TCl[q], TCl[q + n]);
+}
+
+// ---------------------------------------------------- face geometric mean
+// CELLTOEDGEGEOMETRIC: sqrt(|c_lo c_hi|); non-periodic boundary faces see a
+// zero-gradient ghost (face = |c|).
+__global__ void __launch_bounds__(kBlock) face_geomean_kernel(Geom G, int d,
+                                                              const double *__restrict__ cell,
+                                                              double *__restrict__ face) {
+  long long nf = G.nface(d);
+  int m0 = G.n0 + (d == 0), m1 = G.n1 + (d == 1);
+  for (long long t = gtid(); t < nf; t += gstride()) {
+    int i = (int)(t % m0);
+    long long r = t / m0;
+    int j = (int)(r % m1);
+    int k = (int)(r / m1);
+    int hi[3] = {i, j, k}, lo[3] = {i, j, k};
+    lo[d] -= 1;
+    int m = G.n(d);
+    if (hi[d] >= m) hi[d] = G.per(d) ? 0 : m - 1;
+    if (lo[d] < 0) lo[d] = G.per(d) ? m - 1 : 0;
+    double a = cell[G.cell(lo[0], lo[1], lo[2])], b = cell[G.cell(hi[0], hi[1], hi[2])];
+    face[t] = sqrt(fabs(a * b));
+  }
+}
+
+// ----------------------------------------------------- MAC div / correct
+__global__ void __launch_bounds__(kBlock) mac_div_kernel(Geom G, const double *__restrict__ u0,
+                                                         const double *__restrict__ u1,
+                                                         const double *__restrict__ u2,
+                                                         double *__restrict__ div) {
+  double one_on_dx = 1.0 / G.dx;
+  for (long long q = gtid(); q < G.ncell; q += gstride()) {
+    int i, j, k;
+    cell_ijk(G, q, i, j, k);
+    double v = 0.0;
+    v = v + one_on_dx * (u0[G.face(0, i + 1, j, k)] - u0[G.face(0, i, j, k)]);
+    v = v + one_on_dx * (u1[G.face(1, i, j + 1, k)] - u1[G.face(1, i, j, k)]);
+    if (G.dim == 3) v = v + one_on_dx * (u2[G.face(2, i, j, k + 1)] - u2[G.face(2, i, j, k)]);
+    div[q] = v;
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) mac_correct_kernel(Geom G, BCD bc, int d,
+                                                             const double *__restrict__ phi,
+                                                             const double *__restrict__ scale,
+                                                             double *__restrict__ u) {
+  long long nf = G.nface(d);
+  int m0 = G.n0 + (d == 0), m1 = G.n1 + (d == 1);
+  int m = G.n(d);
+  for (long long t = gtid(); t < nf; t += gstride()) {
+    int i = (int)(t % m0);
+    long long r = t / m0;
+    int j = (int)(r % m1);
+    int k = (int)(r / m1);
+    int hi[3] = {i, j, k}, lo[3] = {i, j, k};
+    lo[d] -= 1;
+    double ph, pl;
+    if (hi[d] < m && lo[d] >= 0) {
+      ph = phi[G.cell(hi[0], hi[1], hi[2])];
+      pl = phi[G.cell(lo[0], lo[1], lo[2])];
+    } else if (G.per(d)) {
+      if (hi[d] >= m) hi[d] = 0;
+      if (lo[d] < 0) lo[d] = m - 1;
+      ph = phi[G.cell(hi[0], hi[1], hi[2])];
+      pl = phi[G.cell(lo[0], lo[1], lo[2])];
+    } else if (lo[d] < 0) {
+      ph = phi[G.cell(hi[0], hi[1], hi[2])];
+      pl = ghost_value<double>(bc, d, 0, 0, ph, G.dx, false);
+    } else {
+      pl = phi[G.cell(lo[0], lo[1], lo[2])];
+      ph = ghost_value<double>(bc, d, 1, 0, pl, G.dx, false);
+    }
+    double grad = (ph - pl) / G.dx;
+    if (scale) grad = grad * scale[t];
+    u[t] = u[t] - grad;
+  }
+}
+#endif  // MLGPU_FP64_UNIT
+
+// ------------------------------------------------------------ elementwise
+template <class T>
+__global__ void __launch_bounds__(kBlock) axpby_kernel(long long n, T a, const T *__restrict__ x,
+                                                       T b, T *__restrict__ y) {
+  for (long long q = gtid(); q < n; q += gstride()) y[q] = a * x[q] + b * y[q];
+}
+
+template <class D, class S>
+__global__ void __launch_bounds__(kBlock) convert_kernel(long long n, D *__restrict__ dst,
+                                                         const S *__restrict__ src) {
+  for (long long q = gtid(); q < n; q += gstride()) dst[q] = (D)src[q];
+}
+
+template <class T, int NORM>
+__global__ void __launch_bounds__(kBlock) norm_partial_kernel(long long n,
+                                                              const T *__restrict__ x,
+                                                              double *__restrict__ part) {
+  double acc = 0.0;
+  for (long long q = gtid(); q < n; q += gstride()) acc = norm_accum<NORM>(acc, (double)x[q]);
+  double r = block_reduce<NORM>(acc);
+  if (threadIdx.x == 0) part[blockIdx.x] = r;
+}
+
+}  // namespace mlgpu

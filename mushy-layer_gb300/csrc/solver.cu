@@ -1,0 +1,720 @@
+// solver.cu -- host-side multigrid drivers over the sm_103a kernels.
+//
+//  * VCSolver: correction-scheme multigrid for the projection and
+//    Darcy-Brinkman operators, restating Chombo's AMRMultiGrid::solveNoInit
+//    on one level + MultiGrid::cycle (relax, restrictResidual, coarse cycle,
+//    prolongIncrement, relax) with the bottom solve done by relaxation.
+//    MLGPU_PREC_MIXED runs the inner cycles in FP32 inside an FP64
+//    defect-correction loop (FP64 residual, FP64 update, FP64 norm).
+//  * HCSolver: FAS multigrid for AMRNonLinearMultiCompOp (the role of
+//    Chombo's AMRFASMultiGrid): relax, restrictR + restrictResidual, coarse
+//    rhs = N_c(R u) + R r, coarse cycle, prolong (u_c - R u), relax.
+//
+// All device memory comes from the caller's workspace.  One outer iteration
+// (cycle + residual + norm + norm read-back) is captured once in a CUDA graph
+// and replayed, so a solve costs one graph launch and one host wait per outer
+// iteration.
+#include <cstring>
+#include <cmath>
+#include <vector>
+#include "capi_internal.h"
+
+using namespace mlgpu;
+
+struct mlgpu_solver {
+  virtual ~mlgpu_solver() {}
+  virtual int solve(double *phi, const double *rhs, mlgpu_solve_stats *st) = 0;
+  virtual int set_alpha_beta(double a, double b) = 0;
+};
+
+namespace {
+
+struct Arena {
+  char *base = nullptr;
+  size_t off = 0;
+  template <class T>
+  T *get(size_t n) {
+    off = (off + 255) & ~(size_t)255;
+    T *p = base ? (T *)(base + off) : nullptr;
+    off += n * sizeof(T);
+    return p;
+  }
+};
+
+int mg_depth(const mlgpu_grid &g, int max_coarse) {
+  if (max_coarse < 1) max_coarse = 1;
+  int depth = 0;
+  while (true) {
+    long long c = (1LL << (depth + 1)) * max_coarse;
+    bool ok = true;
+    for (int d = 0; d < g.dim; d++)
+      if (g.n[d] % c != 0) ok = false;
+    if (!ok || depth > 40) break;
+    depth++;
+  }
+  return depth;
+}
+
+mlgpu_grid coarsen_grid(const mlgpu_grid &f) {
+  mlgpu_grid c = f;
+  for (int d = 0; d < f.dim; d++) c.n[d] = f.n[d] / 2;
+  c.dx = f.dx * 2;
+  return c;
+}
+
+size_t nfaces(const mlgpu_grid &g, int d) {
+  size_t m = 1;
+  for (int e = 0; e < 3; e++) m *= (size_t)(g.n[e] + (e == d ? 1 : 0));
+  return m;
+}
+size_t ncells(const mlgpu_grid &g) { return (size_t)g.n[0] * g.n[1] * g.n[2]; }
+
+#define CK(...)                                   \
+  do {                                            \
+    cudaError_t e_ = (__VA_ARGS__);               \
+    if (e_ != cudaSuccess) return MLGPU_ERR_CUDA; \
+  } while (0)
+
+// Per-level coefficient storage in one precision.
+template <class T>
+struct Coefs {
+  T *a = nullptr, *c = nullptr, *b[3] = {nullptr, nullptr, nullptr};
+};
+
+// outer convergence bookkeeping (AMRMultiGrid::solveNoInit semantics)
+struct Outer {
+  double norm0 = 0, norm = 0, prev = 0;
+  int iter = 0, status = 0;
+};
+
+void stats_begin(mlgpu_solve_stats *st, int levels, double norm0) {
+  memset(st, 0, sizeof(*st));
+  st->levels = levels;
+  st->initial_norm = norm0;
+  st->norm_history[0] = norm0;
+}
+
+// returns true when iterating should continue
+bool outer_continue(const mlgpu_mg_options &o, Outer &S) {
+  return S.norm > o.tolerance * S.norm0 && S.norm0 > o.norm_thresh && S.iter < o.max_iter &&
+         S.status == 0;
+}
+
+void outer_after(const mlgpu_mg_options &o, Outer &S, mlgpu_solve_stats *st) {
+  S.iter++;
+  if (S.iter < 64) st->norm_history[S.iter] = S.norm;
+  if (!std::isfinite(S.norm)) {
+    S.status = 8;
+    return;
+  }
+  if (S.norm > (1.0 - o.hang) * S.prev && S.norm > o.tolerance * S.norm0) {
+    S.status = 2;
+    return;
+  }
+  S.prev = S.norm;
+}
+
+int outer_finish(const mlgpu_mg_options &o, Outer &S, mlgpu_solve_stats *st) {
+  st->iterations = S.iter;
+  st->final_norm = S.norm;
+  if (S.status == 0 && S.norm > o.tolerance * S.norm0 && S.norm0 > o.norm_thresh) S.status = 4;
+  st->exit_status = S.status;
+  if (S.status == 8) return MLGPU_ERR_NAN;
+  if (S.status == 2) return MLGPU_ERR_HANG;
+  if (S.status == 4) return MLGPU_ERR_NOT_CONVERGED;
+  return MLGPU_OK;
+}
+
+// ====================================================================== VC
+struct VCLevel {
+  mlgpu_grid grid;
+  Geom G;
+  Coefs<double> c64;
+  Coefs<float> c32;
+  void *e = nullptr, *r = nullptr, *t = nullptr;  // inner precision
+};
+
+class VCSolver : public mlgpu_solver {
+ public:
+  mlgpu_vcop op;
+  mlgpu_mg_options o;
+  std::vector<VCLevel> L;
+  double *phi[2] = {nullptr, nullptr};
+  double *rhs = nullptr, *part = nullptr;
+  double *host_norm = nullptr;
+  cudaStream_t s = nullptr;
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  bool mixed = false;
+  double updates_per_iter = 0;
+
+  ~VCSolver() override {
+    for (auto &g : graph)
+      if (g) cudaGraphExecDestroy(g);
+    if (host_norm) cudaFreeHost(host_norm);
+  }
+
+  // lay out (or size, when base is null) the workspace
+  size_t layout(char *base) {
+    Arena A;
+    A.base = base;
+    int depth = mg_depth(op.grid, o.max_coarse);
+    L.assign(depth + 1, VCLevel());
+    mlgpu_grid g = op.grid;
+    for (int l = 0; l <= depth; l++) {
+      L[l].grid = g;
+      L[l].G = make_geom(g);
+      size_t n = ncells(g);
+      if (l == 0) {
+        L[l].c64.a = (double *)op.aCoef;
+        L[l].c64.c = (double *)op.cCoef;
+        for (int d = 0; d < 3; d++) L[l].c64.b[d] = (double *)op.bCoef[d];
+      } else {
+        if (op.aCoef) L[l].c64.a = A.get<double>(n);
+        if (op.cCoef) L[l].c64.c = A.get<double>(n);
+        for (int d = 0; d < g.dim; d++) L[l].c64.b[d] = A.get<double>(nfaces(g, d));
+      }
+      if (mixed) {
+        if (op.aCoef) L[l].c32.a = A.get<float>(n);
+        if (op.cCoef) L[l].c32.c = A.get<float>(n);
+        for (int d = 0; d < g.dim; d++) L[l].c32.b[d] = A.get<float>(nfaces(g, d));
+        L[l].e = A.get<float>(n);
+        L[l].r = A.get<float>(n);
+        L[l].t = A.get<float>(n);
+      } else {
+        L[l].e = A.get<double>(n);
+        L[l].r = A.get<double>(n);
+        L[l].t = A.get<double>(n);
+      }
+      g = coarsen_grid(g);
+    }
+    size_t n0 = ncells(op.grid);
+    phi[0] = A.get<double>(n0);
+    phi[1] = A.get<double>(n0);
+    rhs = A.get<double>(n0);
+    part = A.get<double>(kNormScratchDoubles);
+    return A.off + 256;
+  }
+
+  int build_coefs() {
+    for (size_t l = 1; l < L.size(); l++) {
+      Geom F = L[l - 1].G;
+      if (op.aCoef) CK(launch_restrict_avg<double>(F, 1, L[l - 1].c64.a, L[l].c64.a, s));
+      if (op.cCoef) CK(launch_restrict_avg<double>(F, 1, L[l - 1].c64.c, L[l].c64.c, s));
+      for (int d = 0; d < F.dim; d++)
+        CK(launch_coarsen_faces<double>(F, 1, d, L[l - 1].c64.b[d], L[l].c64.b[d], s));
+    }
+    if (mixed) {
+      for (auto &lv : L) {
+        long long n = lv.G.ncell;
+        if (op.aCoef) CK(launch_convert<float, double>(n, lv.c32.a, lv.c64.a, s));
+        if (op.cCoef) CK(launch_convert<float, double>(n, lv.c32.c, lv.c64.c, s));
+        for (int d = 0; d < lv.G.dim; d++)
+          CK(launch_convert<float, double>(lv.G.nface(d), lv.c32.b[d], lv.c64.b[d], s));
+      }
+    }
+    // cell updates per outer iteration (same accounting as the CPU oracle)
+    double u = 0;
+    int last = (int)L.size() - 1;
+    std::vector<double> visits(L.size(), 0);
+    visits[0] = std::max(1, o.inner_cycles);
+    for (int l = 1; l <= last; l++) visits[l] = visits[l - 1] * o.num_mg;
+    for (int l = 0; l <= last; l++) {
+      double n = (double)L[l].G.ncell;
+      if (l == last)
+        u += visits[l] * o.bottom_max_iter * n;
+      else
+        u += visits[l] * ((o.num_smooth_down + o.num_smooth_up) * n + n);
+    }
+    updates_per_iter = u + (double)L[0].G.ncell;  // + outer residual
+    return MLGPU_OK;
+  }
+
+  template <class T>
+  VCArgs<T> args(int l) {
+    mlgpu_vcop lop = op;
+    lop.grid = L[l].grid;
+    VCArgs<T> A = make_vc_args<T>(lop);
+    if (sizeof(T) == 8) {
+      A.a = (const T *)L[l].c64.a;
+      A.c = (const T *)L[l].c64.c;
+      for (int d = 0; d < 3; d++) A.b[d] = (const T *)L[l].c64.b[d];
+    } else {
+      A.a = (const T *)L[l].c32.a;
+      A.c = (const T *)L[l].c32.c;
+      for (int d = 0; d < 3; d++) A.b[d] = (const T *)L[l].c32.b[d];
+    }
+    return A;
+  }
+
+  template <class T>
+  int relax(int l, int n, bool zero_init) {
+    VCArgs<T> A = args<T>(l);
+    T *e = (T *)L[l].e;
+    const T *r = (const T *)L[l].r;
+    if (o.relax_mode == MLGPU_RELAX_JACOBI) {
+      if (zero_init) CK(cudaMemsetAsync(e, 0, sizeof(T) * L[l].G.ncell, s));
+      for (int i = 0; i < n; i++) {
+        CK(launch_vc_op<T>(A, VC_JACOBI, -1, e, r, (T *)L[l].t, 1, nullptr, s));
+        CK(cudaMemcpyAsync(e, L[l].t, sizeof(T) * L[l].G.ncell, cudaMemcpyDeviceToDevice, s));
+      }
+      return MLGPU_OK;
+    }
+    if (zero_init) {
+      if (n == 0) {
+        CK(cudaMemsetAsync(e, 0, sizeof(T) * L[l].G.ncell, s));
+        return MLGPU_OK;
+      }
+      CK(launch_vc_gsrb_zero<T>(A, e, r, s));
+      CK(launch_vc_gsrb<T>(A, e, r, 1, s));
+      n--;
+    }
+    for (int i = 0; i < n; i++) {
+      CK(launch_vc_gsrb<T>(A, e, r, 0, s));
+      CK(launch_vc_gsrb<T>(A, e, r, 1, s));
+    }
+    return MLGPU_OK;
+  }
+
+  template <class T>
+  int cycle(int l, bool zero_init) {
+    int last = (int)L.size() - 1;
+    VCArgs<T> A = args<T>(l);
+    if (l == last) {
+      if (o.relax_mode == MLGPU_RELAX_JACOBI) return relax<T>(l, o.bottom_max_iter, zero_init);
+      CK(launch_vc_relax_block<T>(A, (T *)L[l].e, (const T *)L[l].r, o.bottom_max_iter,
+                                  zero_init ? 1 : 0, s));
+      return MLGPU_OK;
+    }
+    int rc = relax<T>(l, o.num_smooth_down, zero_init);
+    if (rc) return rc;
+    CK(launch_vc_restrict<T>(A, L[l + 1].G, (const T *)L[l].e, (const T *)L[l].r,
+                             (T *)L[l + 1].r, nullptr, s));
+    for (int m = 0; m < o.num_mg; m++) {
+      rc = cycle<T>(l + 1, m == 0);
+      if (rc) return rc;
+    }
+    CK(launch_prolong<T>(L[l].G, make_bcd(op.bc), 1, o.prolong, (T *)L[l].e,
+                         (const T *)L[l + 1].e, nullptr, s));
+    return relax<T>(l, o.num_smooth_up, false);
+  }
+
+  // one outer iteration: inner cycles on (e0, r0), then phi_out = phi_in + e0
+  // and the new residual (r0 in inner precision) with its norm
+  int iteration(int from) {
+    int rc;
+    int cycles = std::max(1, o.inner_cycles);
+    for (int c = 0; c < cycles; c++) {
+      rc = mixed ? cycle<float>(0, c == 0) : cycle<double>(0, c == 0);
+      if (rc) return rc;
+    }
+    VCArgs<double> A = args<double>(0);
+    A.a = (const double *)op.aCoef;
+    A.c = (const double *)op.cCoef;
+    for (int d = 0; d < 3; d++) A.b[d] = (const double *)op.bCoef[d];
+    if (mixed)
+      CK((launch_vc_update_residual<double, float>(A, o.norm_type, phi[from], (const float *)L[0].e,
+                                                   rhs, phi[1 - from], nullptr, (float *)L[0].r,
+                                                   part, s)));
+    else
+      CK((launch_vc_update_residual<double, double>(A, o.norm_type, phi[from],
+                                                    (const double *)L[0].e, rhs, phi[1 - from],
+                                                    nullptr, (double *)L[0].r, part, s)));
+    CK(launch_finalize_norm(o.norm_type, part, norm_parts(L[0].G.ncell), part + kMaxBlocks, s));
+    CK(cudaMemcpyAsync(host_norm, part + kMaxBlocks, sizeof(double), cudaMemcpyDeviceToHost, s));
+    return MLGPU_OK;
+  }
+
+  int run_iteration(int from) {
+    if (!o.use_graph) return iteration(from);
+    if (!graph[from]) {
+      cudaGraph_t g;
+      CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+      int rc = iteration(from);
+      cudaError_t e = cudaStreamEndCapture(s, &g);
+      if (rc) return rc;
+      CK(e);
+      e = cudaGraphInstantiate(&graph[from], g, 0);
+      cudaGraphDestroy(g);
+      CK(e);
+    }
+    CK(cudaGraphLaunch(graph[from], s));
+    return MLGPU_OK;
+  }
+
+  int solve(double *user_phi, const double *user_rhs, mlgpu_solve_stats *st) override {
+    if (!user_phi || !user_rhs || !st) return MLGPU_ERR_ARG;
+    size_t bytes = sizeof(double) * L[0].G.ncell;
+    CK(cudaMemcpyAsync(phi[0], user_phi, bytes, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(rhs, user_rhs, bytes, cudaMemcpyDeviceToDevice, s));
+    // initial residual (no update)
+    VCArgs<double> A = args<double>(0);
+    A.a = (const double *)op.aCoef;
+    A.c = (const double *)op.cCoef;
+    for (int d = 0; d < 3; d++) A.b[d] = (const double *)op.bCoef[d];
+    if (mixed)
+      CK((launch_vc_update_residual<double, float>(A, o.norm_type, phi[0], nullptr, rhs, nullptr,
+                                                   nullptr, (float *)L[0].r, part, s)));
+    else
+      CK((launch_vc_update_residual<double, double>(A, o.norm_type, phi[0], nullptr, rhs, nullptr,
+                                                    nullptr, (double *)L[0].r, part, s)));
+    CK(launch_finalize_norm(o.norm_type, part, norm_parts(L[0].G.ncell), part + kMaxBlocks, s));
+    CK(cudaMemcpyAsync(host_norm, part + kMaxBlocks, sizeof(double), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    Outer S;
+    S.norm0 = S.norm = S.prev = *host_norm;
+    stats_begin(st, (int)L.size(), S.norm0);
+    st->cell_updates = (double)L[0].G.ncell;
+    if (!std::isfinite(S.norm0)) S.status = 8;
+    int cur = 0;
+    while (outer_continue(o, S)) {
+      int rc = run_iteration(cur);
+      if (rc) return rc;
+      CK(cudaStreamSynchronize(s));
+      cur = 1 - cur;
+      S.norm = *host_norm;
+      st->cycles += std::max(1, o.inner_cycles);
+      st->cell_updates += updates_per_iter;
+      outer_after(o, S, st);
+    }
+    CK(cudaMemcpyAsync(user_phi, phi[cur], bytes, cudaMemcpyDeviceToDevice, s));
+    CK(cudaStreamSynchronize(s));
+    return outer_finish(o, S, st);
+  }
+
+  int set_alpha_beta(double a, double b) override {
+    op.alpha = a;
+    op.beta = b;
+    for (auto &g : graph)
+      if (g) {
+        cudaGraphExecDestroy(g);
+        g = nullptr;
+      }
+    return MLGPU_OK;
+  }
+};
+
+// ====================================================================== HC
+struct HCLevel {
+  mlgpu_grid grid;
+  Geom G;
+  Coefs<double> c64;
+  double *u = nullptr, *f = nullptr, *r = nullptr, *uold = nullptr, *t = nullptr;
+};
+
+class HCSolver : public mlgpu_solver {
+ public:
+  mlgpu_nlop op;
+  mlgpu_mg_options o;
+  std::vector<HCLevel> L;
+  double *part = nullptr, *host_norm = nullptr;
+  cudaStream_t s = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  double updates_per_iter = 0;
+
+  ~HCSolver() override {
+    if (graph) cudaGraphExecDestroy(graph);
+    if (host_norm) cudaFreeHost(host_norm);
+  }
+
+  size_t layout(char *base) {
+    Arena A;
+    A.base = base;
+    int depth = mg_depth(op.grid, o.max_coarse);
+    L.assign(depth + 1, HCLevel());
+    mlgpu_grid g = op.grid;
+    for (int l = 0; l <= depth; l++) {
+      L[l].grid = g;
+      L[l].G = make_geom(g);
+      size_t n = 2 * ncells(g);
+      if (l == 0) {
+        L[l].c64.a = (double *)op.aCoef;
+        for (int d = 0; d < 3; d++) L[l].c64.b[d] = (double *)op.bCoef[d];
+      } else {
+        if (op.aCoef) L[l].c64.a = A.get<double>(n);
+        for (int d = 0; d < g.dim; d++) L[l].c64.b[d] = A.get<double>(2 * nfaces(g, d));
+      }
+      L[l].u = A.get<double>(n);
+      L[l].f = A.get<double>(n);
+      L[l].r = A.get<double>(n);
+      L[l].uold = A.get<double>(n);
+      L[l].t = A.get<double>(n);
+      g = coarsen_grid(g);
+    }
+    part = A.get<double>(kNormScratchDoubles);
+    return A.off + 256;
+  }
+
+  int build_coefs() {
+    for (size_t l = 1; l < L.size(); l++) {
+      Geom F = L[l - 1].G;
+      if (op.aCoef) CK(launch_restrict_avg<double>(F, 2, L[l - 1].c64.a, L[l].c64.a, s));
+      for (int d = 0; d < F.dim; d++)
+        CK(launch_coarsen_faces<double>(F, 2, d, L[l - 1].c64.b[d], L[l].c64.b[d], s));
+    }
+    double u = 0;
+    int last = (int)L.size() - 1;
+    std::vector<double> visits(L.size(), 0);
+    visits[0] = 1;
+    for (int l = 1; l <= last; l++) visits[l] = visits[l - 1] * o.num_mg;
+    for (int l = 0; l <= last; l++) {
+      double n = (double)L[l].G.ncell;
+      if (l == last)
+        u += visits[l] * o.bottom_max_iter * n;
+      else
+        u += visits[l] * ((o.num_smooth_down + o.num_smooth_up) * n + n +
+                          (double)L[l + 1].G.ncell);
+    }
+    updates_per_iter = u + (double)L[0].G.ncell;
+    return MLGPU_OK;
+  }
+
+  NLArgs<double> args(int l) {
+    mlgpu_nlop lop = op;
+    lop.grid = L[l].grid;
+    NLArgs<double> A = make_nl_args<double>(lop);
+    A.a = L[l].c64.a;
+    for (int d = 0; d < 3; d++) A.b[d] = L[l].c64.b[d];
+    return A;
+  }
+
+  int relax(int l, int n) {
+    NLArgs<double> A = args(l);
+    for (int i = 0; i < n; i++) {
+      if (o.relax_mode == MLGPU_RELAX_JACOBI) {
+        CK(launch_nl_op<double>(A, NL_JACOBI, -1, L[l].u, L[l].f, L[l].t, nullptr, nullptr, s));
+        CK(cudaMemcpyAsync(L[l].u, L[l].t, sizeof(double) * 2 * L[l].G.ncell,
+                           cudaMemcpyDeviceToDevice, s));
+      } else {
+        CK(launch_nl_gsrb<double>(A, L[l].u, L[l].f, 0, s));
+        CK(launch_nl_gsrb<double>(A, L[l].u, L[l].f, 1, s));
+      }
+    }
+    return MLGPU_OK;
+  }
+
+  int cycle(int l) {
+    int last = (int)L.size() - 1;
+    NLArgs<double> A = args(l);
+    if (l == last) {
+      if (o.relax_mode == MLGPU_RELAX_JACOBI) return relax(l, o.bottom_max_iter);
+      CK(launch_nl_relax_block<double>(A, L[l].u, L[l].f, o.bottom_max_iter, s));
+      return MLGPU_OK;
+    }
+    int rc = relax(l, o.num_smooth_down);
+    if (rc) return rc;
+    HCLevel &C = L[l + 1];
+    CK(launch_nl_restrict<double>(A, C.G, L[l].u, L[l].f, C.r, C.u, s));
+    CK(launch_nl_op<double>(args(l + 1), NL_APPLY_PLUS, -1, C.u, C.r, C.f, C.uold, nullptr, s));
+    for (int m = 0; m < o.num_mg; m++) {
+      rc = cycle(l + 1);
+      if (rc) return rc;
+    }
+    CK(launch_prolong<double>(L[l].G, make_bcd(op.phi_bc), 2, o.prolong, L[l].u, C.u, C.uold, s));
+    return relax(l, o.num_smooth_up);
+  }
+
+  int residual_norm() {
+    CK(launch_nl_op<double>(args(0), NL_RESIDUAL, o.norm_type, L[0].u, L[0].f, L[0].r, nullptr,
+                            part, s));
+    CK(launch_finalize_norm(o.norm_type, part, norm_parts(L[0].G.ncell), part + kMaxBlocks, s));
+    CK(cudaMemcpyAsync(host_norm, part + kMaxBlocks, sizeof(double), cudaMemcpyDeviceToHost, s));
+    return MLGPU_OK;
+  }
+
+  int iteration() {
+    int rc = cycle(0);
+    if (rc) return rc;
+    return residual_norm();
+  }
+
+  int run_iteration() {
+    if (!o.use_graph) return iteration();
+    if (!graph) {
+      cudaGraph_t g;
+      CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+      int rc = iteration();
+      cudaError_t e = cudaStreamEndCapture(s, &g);
+      if (rc) return rc;
+      CK(e);
+      e = cudaGraphInstantiate(&graph, g, 0);
+      cudaGraphDestroy(g);
+      CK(e);
+    }
+    CK(cudaGraphLaunch(graph, s));
+    return MLGPU_OK;
+  }
+
+  int solve(double *user_phi, const double *user_rhs, mlgpu_solve_stats *st) override {
+    if (!user_phi || !user_rhs || !st) return MLGPU_ERR_ARG;
+    size_t bytes = sizeof(double) * 2 * L[0].G.ncell;
+    CK(cudaMemcpyAsync(L[0].u, user_phi, bytes, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(L[0].f, user_rhs, bytes, cudaMemcpyDeviceToDevice, s));
+    int rc = residual_norm();
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(s));
+    Outer S;
+    S.norm0 = S.norm = S.prev = *host_norm;
+    stats_begin(st, (int)L.size(), S.norm0);
+    st->cell_updates = (double)L[0].G.ncell;
+    if (!std::isfinite(S.norm0)) S.status = 8;
+    while (outer_continue(o, S)) {
+      rc = run_iteration();
+      if (rc) return rc;
+      CK(cudaStreamSynchronize(s));
+      S.norm = *host_norm;
+      st->cycles += 1;
+      st->cell_updates += updates_per_iter;
+      outer_after(o, S, st);
+    }
+    CK(cudaMemcpyAsync(user_phi, L[0].u, bytes, cudaMemcpyDeviceToDevice, s));
+    CK(cudaStreamSynchronize(s));
+    return outer_finish(o, S, st);
+  }
+
+  int set_alpha_beta(double a, double b) override {
+    op.alpha = a;
+    op.beta = b;
+    if (graph) {
+      cudaGraphExecDestroy(graph);
+      graph = nullptr;
+    }
+    return MLGPU_OK;
+  }
+};
+
+bool valid_options(const mlgpu_mg_options *o) {
+  if (!o) return false;
+  if (o->num_smooth_down < 0 || o->num_smooth_up < 0 || o->num_mg < 1 || o->max_iter < 0)
+    return false;
+  if (o->relax_mode != MLGPU_RELAX_GSRB && o->relax_mode != MLGPU_RELAX_JACOBI) return false;
+  if (o->bottom_max_iter < 0 || o->max_coarse < 1) return false;
+  if (o->prolong != MLGPU_PROLONG_CONSTANT && o->prolong != MLGPU_PROLONG_LINEAR) return false;
+  if (o->precision != MLGPU_PREC_F64 && o->precision != MLGPU_PREC_MIXED) return false;
+  if (o->norm_type < MLGPU_NORM_MAX || o->norm_type > MLGPU_NORM_L2) return false;
+  return true;
+}
+
+}  // namespace
+
+extern "C" {
+
+void mlgpu_mg_default_options(mlgpu_mg_options *o, int hc) {
+  if (!o) return;
+  memset(o, 0, sizeof(*o));
+  // HCMultigrid defaults (srcSubcycle/MushyLayerSubcycleUtils.cpp:668-678)
+  // or projection defaults (srcSubcycle/Projector.cpp:44-64)
+  o->num_smooth_down = hc ? 1 : 2;
+  o->num_smooth_up = 4;
+  o->num_mg = 1;
+  o->max_iter = hc ? 10 : 20;
+  o->tolerance = hc ? 1e-10 : 1e-15;
+  o->hang = hc ? 1e-10 : 1e-15;
+  o->norm_thresh = hc ? 1e-10 : 1e-30;
+  o->relax_mode = MLGPU_RELAX_GSRB;
+  o->bottom_solver = MLGPU_BOTTOM_RELAX;
+  o->bottom_max_iter = hc ? 40 : 20;
+  o->max_coarse = 2;
+  o->prolong = hc ? MLGPU_PROLONG_LINEAR : MLGPU_PROLONG_CONSTANT;
+  o->precision = MLGPU_PREC_F64;
+  o->inner_cycles = 1;
+  o->norm_type = MLGPU_NORM_MAX;
+  o->use_graph = 1;
+}
+
+int mlgpu_vc_solver_workspace(const mlgpu_vcop *op, const mlgpu_mg_options *o, size_t *bytes) {
+  if (!op || !valid_grid(&op->grid) || !valid_options(o) || !bytes) return MLGPU_ERR_ARG;
+  VCSolver S;
+  S.op = *op;
+  S.o = *o;
+  S.mixed = o->precision == MLGPU_PREC_MIXED;
+  *bytes = S.layout(nullptr);
+  return MLGPU_OK;
+}
+
+int mlgpu_vc_solver_create(const mlgpu_vcop *op, const mlgpu_mg_options *o, void *ws,
+                           size_t bytes, void *stream, mlgpu_solver **out) {
+  if (!op || !valid_grid(&op->grid) || !valid_options(o) || !ws || !out) return MLGPU_ERR_ARG;
+  if (op->dtype != MLGPU_F64) return MLGPU_ERR_ARG;
+  for (int d = 0; d < op->grid.dim; d++)
+    if (!op->bCoef[d]) return MLGPU_ERR_ARG;
+  if (((uintptr_t)ws) & 255) return MLGPU_ERR_WORKSPACE;
+  VCSolver *S = new VCSolver;
+  S->op = *op;
+  S->o = *o;
+  S->mixed = o->precision == MLGPU_PREC_MIXED;
+  S->s = (cudaStream_t)stream;
+  size_t need = S->layout(nullptr);
+  if (bytes < need) {
+    delete S;
+    return MLGPU_ERR_WORKSPACE;
+  }
+  S->layout((char *)ws);
+  if (cudaHostAlloc((void **)&S->host_norm, sizeof(double), cudaHostAllocDefault) != cudaSuccess) {
+    delete S;
+    return MLGPU_ERR_CUDA;
+  }
+  int rc = S->build_coefs();
+  if (rc) {
+    delete S;
+    return rc;
+  }
+  *out = S;
+  return MLGPU_OK;
+}
+
+int mlgpu_hc_solver_workspace(const mlgpu_nlop *op, const mlgpu_mg_options *o, size_t *bytes) {
+  if (!op || !valid_grid(&op->grid) || !valid_options(o) || !bytes) return MLGPU_ERR_ARG;
+  HCSolver S;
+  S.op = *op;
+  S.o = *o;
+  *bytes = S.layout(nullptr);
+  return MLGPU_OK;
+}
+
+int mlgpu_hc_solver_create(const mlgpu_nlop *op, const mlgpu_mg_options *o, void *ws,
+                           size_t bytes, void *stream, mlgpu_solver **out) {
+  if (!op || !valid_grid(&op->grid) || !valid_options(o) || !ws || !out) return MLGPU_ERR_ARG;
+  if (op->dtype != MLGPU_F64) return MLGPU_ERR_ARG;
+  if (o->precision != MLGPU_PREC_F64) return MLGPU_ERR_ARG;
+  for (int d = 0; d < op->grid.dim; d++)
+    if (!op->bCoef[d]) return MLGPU_ERR_ARG;
+  if (((uintptr_t)ws) & 255) return MLGPU_ERR_WORKSPACE;
+  HCSolver *S = new HCSolver;
+  S->op = *op;
+  S->o = *o;
+  S->s = (cudaStream_t)stream;
+  size_t need = S->layout(nullptr);
+  if (bytes < need) {
+    delete S;
+    return MLGPU_ERR_WORKSPACE;
+  }
+  S->layout((char *)ws);
+  if (cudaHostAlloc((void **)&S->host_norm, sizeof(double), cudaHostAllocDefault) != cudaSuccess) {
+    delete S;
+    return MLGPU_ERR_CUDA;
+  }
+  int rc = S->build_coefs();
+  if (rc) {
+    delete S;
+    return rc;
+  }
+  *out = S;
+  return MLGPU_OK;
+}
+
+int mlgpu_solver_solve(mlgpu_solver *s, double *phi, const double *rhs, mlgpu_solve_stats *st) {
+  if (!s) return MLGPU_ERR_ARG;
+  return s->solve(phi, rhs, st);
+}
+
+int mlgpu_solver_set_alpha_beta(mlgpu_solver *s, double a, double b) {
+  if (!s) return MLGPU_ERR_ARG;
+  return s->set_alpha_beta(a, b);
+}
+
+int mlgpu_solver_destroy(mlgpu_solver *s) {
+  delete s;
+  return MLGPU_OK;
+}
+
+}  // extern "C"

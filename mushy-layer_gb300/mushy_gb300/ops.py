@@ -1,0 +1,309 @@
+"""Python mirror of the reference's level-operator surface over the C ABI.
+
+Class and method names follow Chombo's LinearOp / MGLevelOp / AMRLevelOp as
+overridden by the reference (src/AMRNonLinearMultiCompOp.H:51-352,
+src/DarcyBrinkmanOp.H:49-256, src/AMRProjectionOp.h:32-36): residual,
+applyOp, relax, levelGSRB, levelJacobi, restrictResidual, restrictR,
+prolongIncrement, createCoarser, resetLambda/computeLambda, norm.  Fields are
+torch CUDA tensors ([comp][k][j][i], no ghosts); every call goes through
+libmlgpu.so on the current torch stream.  Errors raise RuntimeError with the
+library's status string (the reference aborts through MayDay instead).
+"""
+import ctypes as C
+
+import torch
+
+from . import abi
+
+
+def _stream():
+    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _ptr(t):
+    if t is None:
+        return None
+    if not t.is_cuda or not t.is_contiguous():
+        raise RuntimeError("fields must be contiguous CUDA tensors")
+    return C.c_void_p(t.data_ptr())
+
+
+def _dtype_code(t):
+    if t.dtype == torch.float64:
+        return abi.F64
+    if t.dtype == torch.float32:
+        return abi.F32
+    raise RuntimeError("unsupported dtype %s" % t.dtype)
+
+
+def coarse_grid(g):
+    return abi.make_grid([g.n[d] // 2 for d in range(g.dim)], g.dx * 2,
+                         [g.periodic[d] for d in range(3)])
+
+
+def cell_tensor(g, ncomp, dtype=torch.float64, device="cuda"):
+    return torch.zeros((ncomp,) + abi.cell_shape(g), dtype=dtype, device=device)
+
+
+def face_tensor(g, d, ncomp, dtype=torch.float64, device="cuda"):
+    return torch.zeros((ncomp,) + abi.face_shape(g, d), dtype=dtype, device=device)
+
+
+class _NormScratch:
+    _t = None
+
+    @classmethod
+    def get(cls):
+        if cls._t is None:
+            n = abi.load().mlgpu_norm_workspace_bytes()
+            cls._t = torch.empty(n // 8 + 1, dtype=torch.float64, device="cuda")
+        return cls._t
+
+
+def norm(x, kind=abi.NORM_MAX):
+    ws = _NormScratch.get()
+    out = C.c_double()
+    abi.check(abi.load().mlgpu_norm(x.numel(), _dtype_code(x), _ptr(x), kind, C.byref(out),
+                                    _ptr(ws), ws.numel() * 8, _stream()), "mlgpu_norm")
+    return out.value
+
+
+class NLMultiCompOp:
+    """AMRNonLinearMultiCompOp on one uniform box (H, C) -> (T, C_l)."""
+
+    ncomp = 2
+
+    def __init__(self, grid, params, phi_bc, derived_bc, alpha, beta, aCoef, bCoef,
+                 apply_derived_bc=True):
+        self.grid, self.params = grid, params
+        self.phi_bc, self.derived_bc = phi_bc, derived_bc
+        self.alpha, self.beta = float(alpha), float(beta)
+        self.aCoef, self.bCoef = aCoef, list(bCoef)
+        self.apply_derived_bc = int(apply_derived_bc)
+        self.dtype = bCoef[0].dtype
+
+    def desc(self):
+        op = abi.NLOp()
+        op.grid, op.params = self.grid, self.params
+        op.phi_bc, op.derived_bc = self.phi_bc, self.derived_bc
+        op.apply_derived_bc = self.apply_derived_bc
+        op.alpha, op.beta = self.alpha, self.beta
+        op.aCoef = _ptr(self.aCoef)
+        for d in range(3):
+            op.bCoef[d] = _ptr(self.bCoef[d]) if d < self.grid.dim else None
+        op.dtype = _dtype_code(self.bCoef[0])
+        return op
+
+    def setAlphaAndBeta(self, alpha, beta):
+        self.alpha, self.beta = float(alpha), float(beta)
+
+    def create(self, like=None):
+        return cell_tensor(self.grid, 2, self.dtype)
+
+    def residual(self, lhs, phi, rhs, homogeneous=False, norm_type=-1):
+        ws = _NormScratch.get()
+        out = C.c_double()
+        abi.check(abi.load().mlgpu_nl_residual(C.byref(self.desc()), _ptr(lhs), _ptr(phi),
+                                               _ptr(rhs), norm_type, C.byref(out), _ptr(ws),
+                                               ws.numel() * 8, _stream()), "residual")
+        return out.value if norm_type >= 0 else lhs
+
+    def applyOp(self, lhs, phi, homogeneous=False):
+        abi.check(abi.load().mlgpu_nl_apply(C.byref(self.desc()), _ptr(lhs), _ptr(phi),
+                                            _stream()), "applyOp")
+        return lhs
+
+    def levelGSRBPass(self, phi, rhs, pass_):
+        abi.check(abi.load().mlgpu_nl_gsrb_pass(C.byref(self.desc()), _ptr(phi), _ptr(rhs),
+                                                pass_, _stream()), "levelGSRB")
+
+    def levelGSRB(self, phi, rhs):
+        self.levelGSRBPass(phi, rhs, 0)
+        self.levelGSRBPass(phi, rhs, 1)
+
+    def relax(self, phi, rhs, n):
+        abi.check(abi.load().mlgpu_nl_relax(C.byref(self.desc()), _ptr(phi), _ptr(rhs), n,
+                                            _stream()), "relax")
+
+    def levelJacobi(self, phi, rhs):
+        tmp = torch.empty_like(phi)
+        abi.check(abi.load().mlgpu_nl_jacobi(C.byref(self.desc()), _ptr(phi), _ptr(rhs),
+                                             _ptr(tmp), _stream()), "levelJacobi")
+
+    def computeLambda(self):
+        lam = cell_tensor(self.grid, 2, self.dtype)
+        abi.check(abi.load().mlgpu_nl_lambda(C.byref(self.desc()), _ptr(lam), _stream()),
+                  "computeLambda")
+        return lam
+
+    def restrictResidual(self, resCoarse, phiFine, rhsFine):
+        abi.check(abi.load().mlgpu_nl_restrict_residual(C.byref(self.desc()), _ptr(resCoarse),
+                                                        _ptr(phiFine), _ptr(rhsFine), _stream()),
+                  "restrictResidual")
+        return resCoarse
+
+    def restrictR(self, phiCoarse, phiFine):
+        abi.check(abi.load().mlgpu_restrict_average(C.byref(self.grid), 2, _dtype_code(phiFine),
+                                                    _ptr(phiCoarse), _ptr(phiFine), _stream()),
+                  "restrictR")
+        return phiCoarse
+
+    def prolongIncrement(self, phiThisLevel, correctCoarse, kind=abi.PROLONG_LINEAR):
+        abi.check(abi.load().mlgpu_prolong_increment(C.byref(self.grid), C.byref(self.phi_bc), 2,
+                                                     _dtype_code(phiThisLevel), kind,
+                                                     _ptr(phiThisLevel), _ptr(correctCoarse),
+                                                     _stream()), "prolongIncrement")
+        return phiThisLevel
+
+    def createCoarser(self):
+        return cell_tensor(coarse_grid(self.grid), 2, self.dtype)
+
+
+class VCOp:
+    """alpha a phi - beta c phi - beta div(b grad phi) on one component."""
+
+    prolong_kind = abi.PROLONG_CONSTANT
+
+    def __init__(self, grid, bc, alpha, beta, aCoef, bCoef, cCoef=None):
+        self.grid, self.bc = grid, bc
+        self.alpha, self.beta = float(alpha), float(beta)
+        self.aCoef, self.cCoef, self.bCoef = aCoef, cCoef, list(bCoef)
+        self.dtype = bCoef[0].dtype
+
+    def desc(self):
+        op = abi.VCOp()
+        op.grid, op.bc = self.grid, self.bc
+        op.alpha, op.beta = self.alpha, self.beta
+        op.aCoef, op.cCoef = _ptr(self.aCoef), _ptr(self.cCoef)
+        for d in range(3):
+            op.bCoef[d] = _ptr(self.bCoef[d]) if d < self.grid.dim else None
+        op.dtype = _dtype_code(self.bCoef[0])
+        return op
+
+    def setAlphaAndBeta(self, alpha, beta):
+        self.alpha, self.beta = float(alpha), float(beta)
+
+    def create(self):
+        return cell_tensor(self.grid, 1, self.dtype)
+
+    def residual(self, lhs, phi, rhs, homogeneous=False, norm_type=-1):
+        ws = _NormScratch.get()
+        out = C.c_double()
+        abi.check(abi.load().mlgpu_vc_residual(C.byref(self.desc()), _ptr(lhs), _ptr(phi),
+                                               _ptr(rhs), int(homogeneous), norm_type,
+                                               C.byref(out), _ptr(ws), ws.numel() * 8,
+                                               _stream()), "residual")
+        return out.value if norm_type >= 0 else lhs
+
+    def applyOp(self, lhs, phi, homogeneous=False):
+        abi.check(abi.load().mlgpu_vc_apply(C.byref(self.desc()), _ptr(lhs), _ptr(phi),
+                                            int(homogeneous), _stream()), "applyOp")
+        return lhs
+
+    def levelGSRBPass(self, phi, rhs, pass_):
+        abi.check(abi.load().mlgpu_vc_gsrb_pass(C.byref(self.desc()), _ptr(phi), _ptr(rhs),
+                                                pass_, _stream()), "levelGSRB")
+
+    def levelGSRB(self, phi, rhs):
+        self.levelGSRBPass(phi, rhs, 0)
+        self.levelGSRBPass(phi, rhs, 1)
+
+    def relax(self, phi, rhs, n):
+        abi.check(abi.load().mlgpu_vc_relax(C.byref(self.desc()), _ptr(phi), _ptr(rhs), n,
+                                            _stream()), "relax")
+
+    def levelJacobi(self, phi, rhs):
+        tmp = torch.empty_like(phi)
+        abi.check(abi.load().mlgpu_vc_jacobi(C.byref(self.desc()), _ptr(phi), _ptr(rhs),
+                                             _ptr(tmp), _stream()), "levelJacobi")
+
+    def computeLambda(self):
+        lam = cell_tensor(self.grid, 1, self.dtype)
+        abi.check(abi.load().mlgpu_vc_lambda(C.byref(self.desc()), _ptr(lam), _stream()),
+                  "computeLambda")
+        return lam
+
+    def restrictResidual(self, resCoarse, phiFine, rhsFine):
+        abi.check(abi.load().mlgpu_vc_restrict_residual(C.byref(self.desc()), _ptr(resCoarse),
+                                                        _ptr(phiFine), _ptr(rhsFine), _stream()),
+                  "restrictResidual")
+        return resCoarse
+
+    def prolongIncrement(self, phiThisLevel, correctCoarse, kind=None):
+        kind = self.prolong_kind if kind is None else kind
+        abi.check(abi.load().mlgpu_prolong_increment(C.byref(self.grid), C.byref(self.bc), 1,
+                                                     _dtype_code(phiThisLevel), kind,
+                                                     _ptr(phiThisLevel), _ptr(correctCoarse),
+                                                     _stream()), "prolongIncrement")
+        return phiThisLevel
+
+    def createCoarser(self):
+        return cell_tensor(coarse_grid(self.grid), 1, self.dtype)
+
+
+class ProjectionOp(VCOp):
+    """AMRProjectionOp: alpha = 0, bCoef = -Pi_face, beta = 1
+    (srcSubcycle/Projector.cpp:2942-2973); piecewise-constant prolongation
+    (src/AMRProjectionOp.cpp:67-98)."""
+
+
+class DarcyBrinkmanOp(VCOp):
+    """DarcyBrinkmanOp: (alpha a - beta c - beta div b grad) u = rho."""
+
+
+def default_options(hc):
+    o = abi.MGOptions()
+    abi.load().mlgpu_mg_default_options(C.byref(o), int(hc))
+    return o
+
+
+class _Solver:
+    def __init__(self, op, opts, kind):
+        self.op, self.opts = op, opts
+        lib = abi.load()
+        self.desc = op.desc()
+        nbytes = C.c_size_t()
+        fn_ws = lib.mlgpu_hc_solver_workspace if kind == "hc" else lib.mlgpu_vc_solver_workspace
+        fn_cr = lib.mlgpu_hc_solver_create if kind == "hc" else lib.mlgpu_vc_solver_create
+        abi.check(fn_ws(C.byref(self.desc), C.byref(opts), C.byref(nbytes)), "workspace")
+        self.ws = torch.empty(nbytes.value // 8 + 64, dtype=torch.float64, device="cuda")
+        base = self.ws.data_ptr()
+        aligned = (base + 255) & ~255
+        self.h = C.c_void_p()
+        abi.check(fn_cr(C.byref(self.desc), C.byref(opts), C.c_void_p(aligned),
+                        self.ws.numel() * 8 - (aligned - base), _stream(), C.byref(self.h)),
+                  "solver create")
+
+    def solve(self, phi, rhs, check=False):
+        st = abi.SolveStats()
+        rc = abi.load().mlgpu_solver_solve(self.h, _ptr(phi), _ptr(rhs), C.byref(st))
+        if check:
+            abi.check(rc, "solve")
+        elif rc not in (abi.OK, abi.ERR_NOT_CONVERGED, abi.ERR_HANG):
+            abi.check(rc, "solve")
+        return st, rc
+
+    def setAlphaAndBeta(self, a, b):
+        abi.check(abi.load().mlgpu_solver_set_alpha_beta(self.h, a, b), "setAlphaAndBeta")
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            try:
+                abi.load().mlgpu_solver_destroy(self.h)
+            except Exception:
+                pass
+            self.h = None
+
+
+class AMRFASMultiGrid(_Solver):
+    """FAS multigrid driving NLMultiCompOp (AMRFASMultiGrid's role)."""
+
+    def __init__(self, op, opts=None):
+        super().__init__(op, opts or default_options(True), "hc")
+
+
+class AMRMultiGrid(_Solver):
+    """Linear multigrid driving ProjectionOp / DarcyBrinkmanOp."""
+
+    def __init__(self, op, opts=None):
+        super().__init__(op, opts or default_options(False), "vc")

@@ -1,0 +1,1111 @@
+// oracle.cpp -- CPU FP64 restatement of mushy-layer's elliptic/closure hot
+// path.  TEST INFRASTRUCTURE ONLY: the CUDA product never links, loads or
+// calls this file; tests and the CPU-baseline leg of the benchmark use it as
+// the checker.
+//
+// It follows the reference's data model literally: every field is a FAB with
+// one ghost layer; operators fill ghosts (periodic exchange, then physical BC
+// functions), compute the closure over the ghosted box, apply the derived
+// variable BC and then run the Fortran loop nests.  Expressions keep the
+// Fortran evaluation order (left to right, no contraction; build with
+// -ffp-contract=off) so that FP64 results can be compared bit for bit.
+//
+// Reference files restated (paths inside the mushy-layer project):
+//   src/EnthalpyVariablesF.ChF        closure kernels
+//   src/phaseDiagram.cpp              closure driver
+//   src/AMRNonLinearMultiCompOpF.ChF  nonlinear op kernels
+//   src/AMRNonLinearMultiCompOp.cpp   op call sequence, lambda, MGnewOp
+//   src/DarcyBrinkmanOpF.ChF / .cpp   linear op with c term
+//   src/AMRProjectionOp.cpp, AMRProjectionOpF.ChF   projection op, prolong
+//   src/CellToEdge2F.ChF, util/DivergenceF.ChF, util/Gradient.cpp
+//   BCutil/BCFuncF.ChF, BCutil/BCFunctions.cpp, BCutil/PhysBCUtil.cpp
+// The multigrid drivers restate Chombo's AMRMultiGrid / AMRFASMultiGrid /
+// RelaxSolver (Chombo fork c00e7b62, not in the reference tree); parity at
+// the driver level is unpinned.
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+#include <algorithm>
+
+#include "../include/mlgpu.h"
+
+namespace {
+
+// ------------------------------------------------------------------ FAB
+struct Fab {
+  int nc = 0;
+  int n[3] = {1, 1, 1};
+  int g[3] = {0, 0, 0};
+  int s[3] = {0, 0, 0};  // strides of the ghosted box
+  std::vector<double> v;
+  Fab() {}
+  Fab(const mlgpu_grid &gr, int ncomp) { define(gr, ncomp); }
+  void define(const mlgpu_grid &gr, int ncomp) {
+    nc = ncomp;
+    for (int d = 0; d < 3; d++) {
+      n[d] = gr.n[d];
+      g[d] = (d < gr.dim) ? 1 : 0;
+    }
+    s[0] = 1;
+    s[1] = n[0] + 2 * g[0];
+    s[2] = s[1] * (n[1] + 2 * g[1]);
+    v.assign((size_t)nc * s[2] * (n[2] + 2 * g[2]), 0.0);
+  }
+  size_t plane() const { return (size_t)s[2] * (n[2] + 2 * g[2]); }
+  double &operator()(int i, int j, int k, int c) {
+    return v[(size_t)c * plane() + (size_t)(i + g[0]) + (size_t)(j + g[1]) * s[1] +
+             (size_t)(k + g[2]) * s[2]];
+  }
+  double operator()(int i, int j, int k, int c) const {
+    return v[(size_t)c * plane() + (size_t)(i + g[0]) + (size_t)(j + g[1]) * s[1] +
+             (size_t)(k + g[2]) * s[2]];
+  }
+  void load(const double *dense) {
+    for (int c = 0; c < nc; c++)
+      for (int k = 0; k < n[2]; k++)
+        for (int j = 0; j < n[1]; j++)
+          for (int i = 0; i < n[0]; i++)
+            (*this)(i, j, k, c) = dense[(((size_t)c * n[2] + k) * n[1] + j) * n[0] + i];
+  }
+  void store(double *dense) const {
+    for (int c = 0; c < nc; c++)
+      for (int k = 0; k < n[2]; k++)
+        for (int j = 0; j < n[1]; j++)
+          for (int i = 0; i < n[0]; i++)
+            dense[(((size_t)c * n[2] + k) * n[1] + j) * n[0] + i] = (*this)(i, j, k, c);
+  }
+};
+
+inline size_t ncells(const mlgpu_grid &g) { return (size_t)g.n[0] * g.n[1] * g.n[2]; }
+inline size_t nfaces(const mlgpu_grid &g, int d) {
+  size_t m = 1;
+  for (int e = 0; e < 3; e++) m *= (size_t)(g.n[e] + (e == d ? 1 : 0));
+  return m;
+}
+// face index of face (i,j,k) in direction d (face i sits between cells i-1, i)
+inline size_t fidx(const mlgpu_grid &g, int d, int i, int j, int k, int c) {
+  int m0 = g.n[0] + (d == 0), m1 = g.n[1] + (d == 1), m2 = g.n[2] + (d == 2);
+  return (((size_t)c * m2 + k) * m1 + j) * m0 + i;
+}
+
+mlgpu_grid coarsen_grid(const mlgpu_grid &f) {
+  mlgpu_grid c = f;
+  for (int d = 0; d < f.dim; d++) c.n[d] = f.n[d] / 2;
+  c.dx = f.dx * 2;
+  return c;
+}
+
+// ------------------------------------------------------ BC functions
+// Periodic exchange of the face ghosts (trimmed-edge copier: corners are
+// not exchanged).
+void exchange(Fab &f, const mlgpu_grid &gr) {
+  for (int d = 0; d < gr.dim; d++) {
+    if (!gr.periodic[d]) continue;
+    int lo[3] = {0, 0, 0}, hi[3] = {f.n[0] - 1, f.n[1] - 1, f.n[2] - 1};
+    for (int c = 0; c < f.nc; c++)
+      for (int k = lo[2]; k <= hi[2]; k++)
+        for (int j = lo[1]; j <= hi[1]; j++)
+          for (int i = lo[0]; i <= hi[0]; i++) {
+            int idx[3] = {i, j, k};
+            if (idx[d] != 0 && idx[d] != f.n[d] - 1) continue;
+            if (idx[d] == f.n[d] - 1) {
+              int t[3] = {i, j, k};
+              t[d] = -1;
+              f(t[0], t[1], t[2], c) = f(i, j, k, c);
+            }
+            if (idx[d] == 0) {
+              int t[3] = {i, j, k};
+              t[d] = f.n[d];
+              f(t[0], t[1], t[2], c) = f(i, j, k, c);
+            }
+          }
+  }
+}
+
+// DIRIBC order 1 (BCutil/BCFuncF.ChF:14-57) and NEUMBC (:63-95) on the ghost
+// row adjacent to the valid box (adjCellBox, BCFunctions.cpp:101-161).
+void physbc(Fab &f, const mlgpu_grid &gr, const mlgpu_bc &bc, bool homogeneous) {
+  for (int d = 0; d < gr.dim; d++) {
+    if (gr.periodic[d]) continue;
+    for (int side = 0; side < 2; side++) {
+      int isign = side == 0 ? -1 : 1;
+      for (int c = 0; c < f.nc; c++) {
+        int type = bc.type[d][side][c];
+        double val = homogeneous ? 0.0 : bc.value[d][side][c];
+        int lo[3] = {0, 0, 0}, hi[3] = {f.n[0] - 1, f.n[1] - 1, f.n[2] - 1};
+        lo[d] = hi[d] = (side == 0) ? -1 : f.n[d];
+        for (int k = lo[2]; k <= hi[2]; k++)
+          for (int j = lo[1]; j <= hi[1]; j++)
+            for (int i = lo[0]; i <= hi[0]; i++) {
+              int t[3] = {i, j, k};
+              t[d] -= isign;
+              double phi1 = f(t[0], t[1], t[2], c);
+              if (type == MLGPU_BC_DIRICHLET)
+                f(i, j, k, c) = 2 * val - phi1;
+              else
+                f(i, j, k, c) = phi1 + (isign * gr.dx) * val;
+            }
+      }
+    }
+  }
+}
+
+void fill_ghosts(Fab &f, const mlgpu_grid &gr, const mlgpu_bc &bc, bool homogeneous) {
+  exchange(f, gr);
+  physbc(f, gr, bc, homogeneous);
+}
+
+// Homogeneous ghost fill including edges and corners, direction by
+// direction over the already-extended ranges; used for the coarse correction
+// read by the prolongation.
+void fill_ghosts_full_homog(Fab &f, const mlgpu_grid &gr, const mlgpu_bc &bc) {
+  for (int d = 0; d < gr.dim; d++) {
+    int lo[3], hi[3];
+    for (int e = 0; e < 3; e++) {
+      lo[e] = (e < d) ? -f.g[e] : 0;
+      hi[e] = (e < d) ? f.n[e] - 1 + f.g[e] : f.n[e] - 1;
+    }
+    for (int side = 0; side < 2; side++) {
+      int gl[3] = {lo[0], lo[1], lo[2]}, gh[3] = {hi[0], hi[1], hi[2]};
+      gl[d] = gh[d] = (side == 0) ? -1 : f.n[d];
+      for (int c = 0; c < f.nc; c++)
+        for (int k = gl[2]; k <= gh[2]; k++)
+          for (int j = gl[1]; j <= gh[1]; j++)
+            for (int i = gl[0]; i <= gh[0]; i++) {
+              int t[3] = {i, j, k};
+              if (gr.periodic[d]) {
+                t[d] = (side == 0) ? f.n[d] - 1 : 0;
+                f(i, j, k, c) = f(t[0], t[1], t[2], c);
+              } else {
+                t[d] = (side == 0) ? 0 : f.n[d] - 1;
+                double v = f(t[0], t[1], t[2], c);
+                f(i, j, k, c) = (bc.type[d][side][c] == MLGPU_BC_DIRICHLET) ? -v : v;
+              }
+            }
+    }
+  }
+}
+
+// ------------------------------------------------------------ closure
+// CALCULATE_BOUNDING_ENERGY (src/EnthalpyVariablesF.ChF:657-698)
+inline void bounding_energy(double C, const mlgpu_params &p, double &Hs, double &He,
+                            double &Hl) {
+  const double CR = p.compositionRatio, k = p.waterDistributionCoeff,
+               cp = p.specificHeatRatio, St = p.stefan, te = p.thetaEutectic,
+               Te = p.ThetaEutectic;
+  if (C < -CR)
+    Hs = 0.0;
+  else
+    Hs = cp * ((-C - CR) / k);
+  if (Hs < 0.0) Hs = 0.0;
+  Hs = Hs + te * cp;
+  double pe = (CR + C) / (CR + Te);
+  He = pe * (St + te * (1 - cp)) + cp * te;
+  Hl = St - C + te + Te;
+}
+
+// CALCULATEPOROSITYMUSH (src/EnthalpyVariablesF.ChF:103-150), clamps C >= -CR.
+inline double porosity_mush(double C, double H, const mlgpu_params &p) {
+  const double CR = p.compositionRatio, k = p.waterDistributionCoeff,
+               cp = p.specificHeatRatio, St = p.stefan;
+  double validC = (C >= -CR) ? C : -CR;
+  if (St == 0) return 1;
+  double a = CR * (cp - 1) + St * (k - 1);
+  double b = CR * (1 - 2 * cp) + H * (1 - k) - validC * (cp - 1) - k * St;
+  double c = (CR + validC) * cp + k * H;
+  return (-b - std::sqrt(b * b - 4 * a * c)) / (2 * a);
+}
+
+// CALCULATE_T_CL (src/EnthalpyVariablesF.ChF:419-467)
+inline void t_cl(double H, double C, const mlgpu_params &p, double &T, double &Cl) {
+  double Hs, He, Hl;
+  bounding_energy(C, p, Hs, He, Hl);
+  const double CR = p.compositionRatio, k = p.waterDistributionCoeff;
+  if (H <= Hs) {
+    T = H / p.specificHeatRatio;
+    Cl = p.ThetaEutectic;
+  } else if (H > Hs && H <= He) {
+    T = p.thetaEutectic;
+    Cl = p.ThetaEutectic;
+  } else if (H > He && H < Hl) {
+    double por = porosity_mush(C, H, p);
+    T = -(C + CR * (1 - por)) / (por + k * (1 - por));
+    Cl = (C + CR * (1 - por)) / (por + k * (1 - por));
+  } else if (H >= Hl) {
+    T = H - p.stefan;
+    Cl = C;
+  } else {  // NaN input: no branch taken in the Fortran either
+    T = H;
+    Cl = C;
+  }
+}
+
+// CALCULATEPOROSITY/CL/CS/T (src/EnthalpyVariablesF.ChF:13-284) for one cell.
+inline void full_closure(double H, double C, const mlgpu_params &p, double &T,
+                         double &por, double &Cl, double &Cs, double &Hs, double &He,
+                         double &Hl) {
+  bounding_energy(C, p, Hs, He, Hl);
+  const double CR = p.compositionRatio, k = p.waterDistributionCoeff,
+               cp = p.specificHeatRatio, St = p.stefan, te = p.thetaEutectic,
+               Te = p.ThetaEutectic;
+  if (H <= Hs) {
+    por = 0;
+    Cl = Te;
+    Cs = C;
+    T = H / cp;
+  } else if (H > Hs && H <= He) {
+    por = (H - te * cp) / (St + te * (1 - cp));
+    Cl = Te;
+    double pm = porosity_mush(C, H, p);  // CALCULATECS uses the mush root here
+    Cs = C / (1 - pm);
+    T = te;
+  } else if (H > He && H < Hl) {
+    double pm = porosity_mush(C, H, p);
+    por = pm;
+    Cl = (C + CR * (1 - pm)) / (pm + k * (1 - pm));
+    Cs = (C * k - CR * pm) / (pm + k * (1 - pm));
+    T = -(C + CR * (1 - pm)) / (pm + k * (1 - pm));
+  } else if (H >= Hl) {
+    por = 1;
+    Cl = C;
+    Cs = 0;
+    T = H - St;
+  } else {
+    por = H; Cl = H; Cs = H; T = H;
+  }
+}
+
+// computeDiffusedVar (src/AMRNonLinearMultiCompOp.cpp:57-98): closure over
+// the whole ghosted box, then the derived-variable BC.
+void diffused_var(Fab &out, const Fab &phi, const mlgpu_nlop &op) {
+  out.define(op.grid, 2);
+  int lo[3], hi[3];
+  for (int d = 0; d < 3; d++) {
+    lo[d] = -phi.g[d];
+    hi[d] = phi.n[d] - 1 + phi.g[d];
+  }
+  for (int k = lo[2]; k <= hi[2]; k++)
+    for (int j = lo[1]; j <= hi[1]; j++)
+      for (int i = lo[0]; i <= hi[0]; i++) {
+        double T, Cl;
+        t_cl(phi(i, j, k, 0), phi(i, j, k, 1), op.params, T, Cl);
+        out(i, j, k, 0) = T;
+        out(i, j, k, 1) = Cl;
+      }
+  if (op.apply_derived_bc) physbc(out, op.grid, op.derived_bc, false);
+}
+
+// --------------------------------------------------- face coefficients
+struct Faces {
+  const double *b[3] = {nullptr, nullptr, nullptr};
+  mlgpu_grid g;
+  double operator()(int d, int i, int j, int k, int c) const {
+    return b[d][fidx(g, d, i, j, k, c)];
+  }
+};
+
+// Flat Fortran sum over directions:
+// b0(i+1)(p(i+1)-p0) - b0(i)(p0-p(i-1)) + b1(j+1)(..) - b1(j)(..) [+ b2 ..]
+inline double flux_sum(const Faces &B, const Fab &pl, int i, int j, int k, int c,
+                       int dim) {
+  double p0 = pl(i, j, k, c);
+  double s = B(0, i + 1, j, k, c) * (pl(i + 1, j, k, c) - p0) -
+             B(0, i, j, k, c) * (p0 - pl(i - 1, j, k, c));
+  s = s + B(1, i, j + 1, k, c) * (pl(i, j + 1, k, c) - p0);
+  s = s - B(1, i, j, k, c) * (p0 - pl(i, j - 1, k, c));
+  if (dim == 3) {
+    s = s + B(2, i, j, k + 1, c) * (pl(i, j, k + 1, c) - p0);
+    s = s - B(2, i, j, k, c) * (p0 - pl(i, j, k - 1, c));
+  }
+  return s;
+}
+
+// resetLambda (AMRNonLinearMultiCompOp.cpp:540-573 / DarcyBrinkmanOp.cpp:
+// 265-296): lambda = a*alpha [+ (-beta) c] + sum_d scale*beta*(b_hi + b_lo),
+// then 1/lambda.
+inline double lambda_at(const Faces &B, const double *a, const double *cc,
+                        double alpha, double beta, double scale, size_t cell, int i,
+                        int j, int k, int c, int dim) {
+  double l = (a ? a[cell] : 1.0) * alpha;
+  if (cc) l = l + (-beta) * cc[cell];
+  for (int d = 0; d < dim; d++) {
+    int ip = i + (d == 0), jp = j + (d == 1), kp = k + (d == 2);
+    double sumVal = B(d, ip, jp, kp, c) + B(d, i, j, k, c);
+    l = l + scale * beta * sumVal;
+  }
+  return 1.0 / l;
+}
+
+inline size_t cidx(const mlgpu_grid &g, int i, int j, int k, int c) {
+  return (((size_t)c * g.n[2] + k) * g.n[1] + j) * g.n[0] + i;
+}
+
+Faces make_faces(const mlgpu_grid &g, const void *const b[3]) {
+  Faces F;
+  F.g = g;
+  for (int d = 0; d < 3; d++) F.b[d] = (const double *)b[d];
+  return F;
+}
+
+// -------------------------------------------------- nonlinear operator
+struct NLCtx {
+  const mlgpu_nlop &op;
+  Faces B;
+  const double *a;
+  double dxinv, scale;
+  int nc = 2;
+  explicit NLCtx(const mlgpu_nlop &o) : op(o) {
+    B = make_faces(o.grid, o.bCoef);
+    a = (const double *)o.aCoef;
+    dxinv = 1.0 / (o.grid.dx * o.grid.dx);
+    scale = 1.0 / (o.grid.dx * o.grid.dx);
+  }
+  // L(phi) at a cell given phi and the diffused variable (NLVCCOMPUTEOP)
+  double lofphi(const Fab &phi, const Fab &pl, int i, int j, int k, int c) const {
+    size_t cell = cidx(op.grid, i, j, k, c);
+    double av = a ? a[cell] : 1.0;
+    return op.alpha * av * phi(i, j, k, c) -
+           op.beta * flux_sum(B, pl, i, j, k, c, op.grid.dim) * dxinv;
+  }
+};
+
+void nl_prepare(Fab &phi, Fab &pl, const mlgpu_nlop &op, const double *phid) {
+  phi.define(op.grid, 2);
+  phi.load(phid);
+  fill_ghosts(phi, op.grid, op.phi_bc, false);
+  diffused_var(pl, phi, op);
+}
+
+template <class F>
+void for_cells(const mlgpu_grid &g, F f) {
+#pragma omp parallel for collapse(2) schedule(static)
+  for (int k = 0; k < g.n[2]; k++)
+    for (int j = 0; j < g.n[1]; j++)
+      for (int i = 0; i < g.n[0]; i++) f(i, j, k);
+}
+
+// one red/black pass: NONLINEARSMOOTHING (F.ChF:50-198) with lambda inline
+void nl_gsrb_pass_fab(Fab &phi, const double *rhs, const mlgpu_nlop &op, int pass) {
+  NLCtx X(op);
+  fill_ghosts(phi, op.grid, op.phi_bc, false);
+  Fab pl;
+  diffused_var(pl, phi, op);
+  const mlgpu_grid &g = op.grid;
+  for (int c = 0; c < 2; c++) {
+#pragma omp parallel for collapse(2) schedule(static)
+    for (int k = 0; k < g.n[2]; k++)
+      for (int j = 0; j < g.n[1]; j++) {
+        int imin = std::abs((j + k + pass) % 2);
+        for (int i = imin; i < g.n[0]; i += 2) {
+          size_t cell = cidx(g, i, j, k, c);
+          double lam = lambda_at(X.B, X.a, nullptr, op.alpha, op.beta, X.scale, cell,
+                                 i, j, k, c, g.dim);
+          double lof = X.lofphi(phi, pl, i, j, k, c);
+          phi(i, j, k, c) = phi(i, j, k, c) - lam * (lof - rhs[cell]);
+        }
+      }
+  }
+}
+
+// ------------------------------------------------------ linear operator
+struct VCCtx {
+  const mlgpu_vcop &op;
+  Faces B;
+  const double *a, *cc;
+  double dxinv, scale;
+  explicit VCCtx(const mlgpu_vcop &o) : op(o) {
+    B = make_faces(o.grid, o.bCoef);
+    a = (const double *)o.aCoef;
+    cc = (const double *)o.cCoef;
+    dxinv = 1.0 / (o.grid.dx * o.grid.dx);
+    scale = 1.0 / (o.grid.dx * o.grid.dx);
+  }
+  // DBCOMPUTEOP (F.ChF:182-274); without c it is the VC Poisson operator
+  double lofphi(const Fab &phi, int i, int j, int k) const {
+    size_t cell = cidx(op.grid, i, j, k, 0);
+    double av = a ? a[cell] : 1.0;
+    double v = op.alpha * av * phi(i, j, k, 0);
+    if (cc) v = v - op.beta * cc[cell] * phi(i, j, k, 0);
+    return v - op.beta * flux_sum(B, phi, i, j, k, 0, op.grid.dim) * dxinv;
+  }
+};
+
+void vc_gsrb_pass_fab(Fab &phi, const double *rhs, const mlgpu_vcop &op, int pass) {
+  VCCtx X(op);
+  fill_ghosts(phi, op.grid, op.bc, true);  // levelGSRB: homogeneous BCs
+  const mlgpu_grid &g = op.grid;
+#pragma omp parallel for collapse(2) schedule(static)
+  for (int k = 0; k < g.n[2]; k++)
+    for (int j = 0; j < g.n[1]; j++) {
+      int imin = std::abs((j + k + pass) % 2);
+      for (int i = imin; i < g.n[0]; i += 2) {
+        size_t cell = cidx(g, i, j, k, 0);
+        double lam = lambda_at(X.B, X.a, X.cc, op.alpha, op.beta, X.scale, cell, i, j,
+                               k, 0, g.dim);
+        double lof = X.lofphi(phi, i, j, k);
+        phi(i, j, k, 0) = phi(i, j, k, 0) - lam * (lof - rhs[cell]);
+      }
+    }
+}
+
+// ------------------------------------------------------------ transfers
+// RESTRICT / RESTRICTRESNLVC accumulation order: fine cells of a coarse cell
+// in Fortran loop order (k, j outer; i fastest), each scaled by 1/2^D.
+template <class F>
+void restrict_loop(const mlgpu_grid &fg, int ncomp, double *coarse, F fine_val) {
+  mlgpu_grid cg = coarsen_grid(fg);
+  double denom = fg.dim == 3 ? 8.0 : 4.0;
+  int r2 = fg.dim == 3 ? 2 : 1;
+  for (int c = 0; c < ncomp; c++) {
+#pragma omp parallel for collapse(2) schedule(static)
+    for (int K = 0; K < cg.n[2]; K++)
+      for (int J = 0; J < cg.n[1]; J++)
+        for (int I = 0; I < cg.n[0]; I++) {
+          double acc = 0.0;
+          for (int kk = 0; kk < r2; kk++)
+            for (int jj = 0; jj < 2; jj++)
+              for (int ii = 0; ii < 2; ii++)
+                acc = acc + fine_val(2 * I + ii, 2 * J + jj, r2 == 2 ? 2 * K + kk : 0, c) / denom;
+          coarse[cidx(cg, I, J, K, c)] = acc;
+        }
+  }
+}
+
+void prolong_fab(const mlgpu_grid &fg, const mlgpu_bc &bc, int ncomp, int kind,
+                 double *fine, const double *coarse) {
+  mlgpu_grid cg = coarsen_grid(fg);
+  Fab C(cg, ncomp);
+  C.load(coarse);
+  fill_ghosts_full_homog(C, cg, bc);
+  int dim = fg.dim;
+  double den = 1.0 / (dim == 3 ? 64.0 : 16.0);
+  double fx1 = 3.0 * den, fx2 = 9.0 * den, fx3 = 27.0 * den, f0 = 1.0 * den;
+  for (int c = 0; c < ncomp; c++) {
+#pragma omp parallel for collapse(2) schedule(static)
+    for (int k = 0; k < fg.n[2]; k++)
+      for (int j = 0; j < fg.n[1]; j++)
+        for (int i = 0; i < fg.n[0]; i++) {
+          int ic = i / 2, jc = j / 2, kc = (dim == 3) ? k / 2 : 0;
+          double &p = fine[cidx(fg, i, j, k, c)];
+          if (kind == MLGPU_PROLONG_CONSTANT) {
+            p = p + C(ic, jc, kc, c);
+            continue;
+          }
+          int o1 = 2 * (i % 2) - 1, o2 = 2 * (j % 2) - 1, o3 = (dim == 3) ? 2 * (k % 2) - 1 : 0;
+          if (dim == 2) {
+            p = p + fx2 * C(ic, jc, kc, c) + f0 * C(ic + o1, jc + o2, kc, c);
+            p = p + fx1 * (C(ic + o1, jc, kc, c) + C(ic, jc + o2, kc, c));
+          } else {
+            p = p + fx3 * C(ic, jc, kc, c) + f0 * C(ic + o1, jc + o2, kc + o3, c);
+            p = p + fx2 * (C(ic + o1, jc, kc, c) + C(ic, jc + o2, kc, c) + C(ic, jc, kc + o3, c));
+            p = p + fx1 * (C(ic + o1, jc + o2, kc, c) + C(ic, jc + o2, kc + o3, c) +
+                           C(ic + o1, jc, kc + o3, c));
+          }
+        }
+  }
+}
+
+// CoarseAverageFace (arithmetic): sum of the 2^(D-1) covered fine faces in
+// Fortran order, times 1/2^(D-1).
+void coarsen_faces(const mlgpu_grid &fg, int ncomp, int d, double *cf, const double *ff) {
+  mlgpu_grid cg = coarsen_grid(fg);
+  int dim = fg.dim;
+  double refScale = dim == 3 ? 0.25 : 0.5;
+  int m[3];
+  for (int e = 0; e < 3; e++) m[e] = cg.n[e] + (e == d);
+  for (int c = 0; c < ncomp; c++)
+    for (int K = 0; K < m[2]; K++)
+      for (int J = 0; J < m[1]; J++)
+        for (int I = 0; I < m[0]; I++) {
+          int r[3] = {2, 2, dim == 3 ? 2 : 1};
+          r[d] = 1;
+          double sum = 0.0;
+          for (int kk = 0; kk < r[2]; kk++)
+            for (int jj = 0; jj < r[1]; jj++)
+              for (int ii = 0; ii < r[0]; ii++) {
+                int fi = 2 * I + ii, fj = 2 * J + jj, fk = (dim == 3) ? 2 * K + kk : 0;
+                sum = sum + ff[fidx(fg, d, fi, fj, fk, c)];
+              }
+          cf[fidx(cg, d, I, J, K, c)] = sum * refScale;
+        }
+}
+
+double norm_of(const double *x, size_t n, int type) {
+  double r = 0;
+  if (type == MLGPU_NORM_MAX) {
+    for (size_t i = 0; i < n; i++) r = std::max(r, std::fabs(x[i]));
+    return r;
+  }
+  if (type == MLGPU_NORM_L1) {
+    for (size_t i = 0; i < n; i++) r += std::fabs(x[i]);
+    return r;
+  }
+  for (size_t i = 0; i < n; i++) r += x[i] * x[i];
+  return std::sqrt(r);
+}
+
+bool has_nan(const double *x, size_t n) {
+  for (size_t i = 0; i < n; i++)
+    if (!std::isfinite(x[i])) return true;
+  return false;
+}
+
+}  // namespace
+
+// ====================================================================== C ABI
+extern "C" {
+
+int orc_closure(const mlgpu_grid *g, const mlgpu_params *p, const double *HC, double *T,
+                double *por, double *Cl, double *Cs, double *Hs, double *He,
+                double *Hl) {
+  size_t n = ncells(*g);
+#pragma omp parallel for schedule(static)
+  for (size_t q = 0; q < n; q++) {
+    double t, po, cl, cs, hs, he, hl;
+    full_closure(HC[q], HC[n + q], *p, t, po, cl, cs, hs, he, hl);
+    if (T) T[q] = t;
+    if (por) por[q] = po;
+    if (Cl) Cl[q] = cl;
+    if (Cs) Cs[q] = cs;
+    if (Hs) Hs[q] = hs;
+    if (He) He[q] = he;
+    if (Hl) Hl[q] = hl;
+  }
+  return 0;
+}
+
+int orc_closure_tcl(const mlgpu_grid *g, const mlgpu_params *p, const double *HC,
+                    double *TCl) {
+  size_t n = ncells(*g);
+#pragma omp parallel for schedule(static)
+  for (size_t q = 0; q < n; q++) t_cl(HC[q], HC[n + q], *p, TCl[q], TCl[n + q]);
+  return 0;
+}
+
+int orc_nl_residual(const mlgpu_nlop *op, double *res, const double *phid,
+                    const double *rhs) {
+  Fab phi, pl;
+  nl_prepare(phi, pl, *op, phid);
+  NLCtx X(*op);
+  for (int c = 0; c < 2; c++)
+    for_cells(op->grid, [&](int i, int j, int k) {
+      size_t cell = cidx(op->grid, i, j, k, c);
+      res[cell] = rhs[cell] - X.lofphi(phi, pl, i, j, k, c);
+    });
+  return 0;
+}
+
+int orc_nl_apply(const mlgpu_nlop *op, double *lhs, const double *phid) {
+  Fab phi, pl;
+  nl_prepare(phi, pl, *op, phid);
+  NLCtx X(*op);
+  for (int c = 0; c < 2; c++)
+    for_cells(op->grid, [&](int i, int j, int k) {
+      lhs[cidx(op->grid, i, j, k, c)] = X.lofphi(phi, pl, i, j, k, c);
+    });
+  return 0;
+}
+
+int orc_nl_gsrb_pass(const mlgpu_nlop *op, double *phid, const double *rhs, int pass) {
+  Fab phi(op->grid, 2);
+  phi.load(phid);
+  nl_gsrb_pass_fab(phi, rhs, *op, pass);
+  phi.store(phid);
+  return 0;
+}
+
+int orc_nl_relax(const mlgpu_nlop *op, double *phid, const double *rhs, int n) {
+  Fab phi(op->grid, 2);
+  phi.load(phid);
+  for (int s = 0; s < n; s++) {
+    nl_gsrb_pass_fab(phi, rhs, *op, 0);
+    nl_gsrb_pass_fab(phi, rhs, *op, 1);
+  }
+  phi.store(phid);
+  return 0;
+}
+
+int orc_nl_lambda(const mlgpu_nlop *op, double *lam) {
+  NLCtx X(*op);
+  for (int c = 0; c < 2; c++)
+    for_cells(op->grid, [&](int i, int j, int k) {
+      size_t cell = cidx(op->grid, i, j, k, c);
+      lam[cell] = lambda_at(X.B, X.a, nullptr, op->alpha, op->beta, X.scale, cell, i, j,
+                            k, c, op->grid.dim);
+    });
+  return 0;
+}
+
+// levelJacobi (AMRNonLinearMultiCompOp.cpp:1077-1101): phi + 0.5*(r*lambda)
+int orc_nl_jacobi(const mlgpu_nlop *op, double *phid, const double *rhs) {
+  size_t n = 2 * ncells(op->grid);
+  std::vector<double> r(n), lam(n);
+  orc_nl_residual(op, r.data(), phid, rhs);
+  orc_nl_lambda(op, lam.data());
+  for (size_t q = 0; q < n; q++) phid[q] = phid[q] + 0.5 * (r[q] * lam[q]);
+  return 0;
+}
+
+int orc_nl_restrict_residual(const mlgpu_nlop *op, double *resc, const double *phid,
+                             const double *rhs) {
+  Fab phi, pl;
+  nl_prepare(phi, pl, *op, phid);
+  NLCtx X(*op);
+  restrict_loop(op->grid, 2, resc, [&](int i, int j, int k, int c) {
+    return rhs[cidx(op->grid, i, j, k, c)] - X.lofphi(phi, pl, i, j, k, c);
+  });
+  return 0;
+}
+
+int orc_restrict_average(const mlgpu_grid *g, int ncomp, double *coarse,
+                         const double *fine) {
+  restrict_loop(*g, ncomp, coarse, [&](int i, int j, int k, int c) {
+    return fine[cidx(*g, i, j, k, c)];
+  });
+  return 0;
+}
+
+int orc_prolong_increment(const mlgpu_grid *g, const mlgpu_bc *bc, int ncomp, int kind,
+                          double *fine, const double *coarse) {
+  prolong_fab(*g, *bc, ncomp, kind, fine, coarse);
+  return 0;
+}
+
+int orc_coarsen_faces(const mlgpu_grid *g, int ncomp, int dir, double *cf,
+                      const double *ff) {
+  coarsen_faces(*g, ncomp, dir, cf, ff);
+  return 0;
+}
+
+// CELLTOEDGEGEOMETRIC (src/CellToEdge2F.ChF): edge = sqrt(|c(i-1) c(i)|);
+// cell ghosts: periodic wrap, else zero-gradient copy.
+int orc_face_geomean(const mlgpu_grid *g, const double *cell, double *faces[3]) {
+  Fab c(*g, 1);
+  c.load(cell);
+  mlgpu_bc bc;
+  memset(&bc, 0, sizeof(bc));
+  fill_ghosts(c, *g, bc, true);
+  for (int d = 0; d < g->dim; d++) {
+    int m[3];
+    for (int e = 0; e < 3; e++) m[e] = g->n[e] + (e == d);
+    for (int k = 0; k < m[2]; k++)
+      for (int j = 0; j < m[1]; j++)
+        for (int i = 0; i < m[0]; i++) {
+          int ii = i - (d == 0), jj = j - (d == 1), kk = k - (d == 2);
+          faces[d][fidx(*g, d, i, j, k, 0)] =
+              std::sqrt(std::fabs(c(ii, jj, kk, 0) * c(i, j, k, 0)));
+        }
+  }
+  return 0;
+}
+
+int orc_vc_residual(const mlgpu_vcop *op, double *res, const double *phid,
+                    const double *rhs, int homogeneous) {
+  Fab phi(op->grid, 1);
+  phi.load(phid);
+  fill_ghosts(phi, op->grid, op->bc, homogeneous != 0);
+  VCCtx X(*op);
+  for_cells(op->grid, [&](int i, int j, int k) {
+    size_t cell = cidx(op->grid, i, j, k, 0);
+    res[cell] = rhs[cell] - X.lofphi(phi, i, j, k);
+  });
+  return 0;
+}
+
+int orc_vc_apply(const mlgpu_vcop *op, double *lhs, const double *phid, int homogeneous) {
+  Fab phi(op->grid, 1);
+  phi.load(phid);
+  fill_ghosts(phi, op->grid, op->bc, homogeneous != 0);
+  VCCtx X(*op);
+  for_cells(op->grid, [&](int i, int j, int k) {
+    lhs[cidx(op->grid, i, j, k, 0)] = X.lofphi(phi, i, j, k);
+  });
+  return 0;
+}
+
+int orc_vc_gsrb_pass(const mlgpu_vcop *op, double *phid, const double *rhs, int pass) {
+  Fab phi(op->grid, 1);
+  phi.load(phid);
+  vc_gsrb_pass_fab(phi, rhs, *op, pass);
+  phi.store(phid);
+  return 0;
+}
+
+int orc_vc_relax(const mlgpu_vcop *op, double *phid, const double *rhs, int n) {
+  Fab phi(op->grid, 1);
+  phi.load(phid);
+  for (int s = 0; s < n; s++) {
+    vc_gsrb_pass_fab(phi, rhs, *op, 0);
+    vc_gsrb_pass_fab(phi, rhs, *op, 1);
+  }
+  phi.store(phid);
+  return 0;
+}
+
+int orc_vc_lambda(const mlgpu_vcop *op, double *lam) {
+  VCCtx X(*op);
+  for_cells(op->grid, [&](int i, int j, int k) {
+    size_t cell = cidx(op->grid, i, j, k, 0);
+    lam[cell] = lambda_at(X.B, X.a, X.cc, op->alpha, op->beta, X.scale, cell, i, j, k, 0,
+                          op->grid.dim);
+  });
+  return 0;
+}
+
+// DarcyBrinkmanOp::levelJacobi (DarcyBrinkmanOp.cpp:699-720): homogeneous residual
+int orc_vc_jacobi(const mlgpu_vcop *op, double *phid, const double *rhs) {
+  size_t n = ncells(op->grid);
+  std::vector<double> r(n), lam(n);
+  orc_vc_residual(op, r.data(), phid, rhs, 1);
+  orc_vc_lambda(op, lam.data());
+  for (size_t q = 0; q < n; q++) phid[q] = phid[q] + 0.5 * (r[q] * lam[q]);
+  return 0;
+}
+
+int orc_vc_restrict_residual(const mlgpu_vcop *op, double *resc, const double *phid,
+                             const double *rhs) {
+  Fab phi(op->grid, 1);
+  phi.load(phid);
+  fill_ghosts(phi, op->grid, op->bc, true);
+  VCCtx X(*op);
+  restrict_loop(op->grid, 1, resc, [&](int i, int j, int k, int) {
+    return rhs[cidx(op->grid, i, j, k, 0)] - X.lofphi(phi, i, j, k);
+  });
+  return 0;
+}
+
+// DIVERGENCE (util/DivergenceF.ChF): div += (u(i+e_d) - u(i)) / dx per dir
+int orc_mac_divergence(const mlgpu_grid *g, double *div, const double *u[3]) {
+  double one_on_dx = 1.0 / g->dx;
+  for_cells(*g, [&](int i, int j, int k) {
+    double v = 0.0;
+    for (int d = 0; d < g->dim; d++) {
+      int ip = i + (d == 0), jp = j + (d == 1), kp = k + (d == 2);
+      v = v + one_on_dx * (u[d][fidx(*g, d, ip, jp, kp, 0)] - u[d][fidx(*g, d, i, j, k, 0)]);
+    }
+    div[cidx(*g, i, j, k, 0)] = v;
+  });
+  return 0;
+}
+
+// levelGradientMAC + correction loop (srcSubcycle/Projector.cpp:942-968):
+// grad = (phi(i) - phi(i-e_d)) / dx on faces, u -= scale * grad
+int orc_mac_correct(const mlgpu_grid *g, const mlgpu_bc *bc, const double *phid,
+                    const double *scale[3], double *u[3]) {
+  Fab phi(*g, 1);
+  phi.load(phid);
+  fill_ghosts(phi, *g, *bc, false);
+  for (int d = 0; d < g->dim; d++) {
+    int m[3];
+    for (int e = 0; e < 3; e++) m[e] = g->n[e] + (e == d);
+    for (int k = 0; k < m[2]; k++)
+      for (int j = 0; j < m[1]; j++)
+        for (int i = 0; i < m[0]; i++) {
+          int ii = i - (d == 0), jj = j - (d == 1), kk = k - (d == 2);
+          size_t f = fidx(*g, d, i, j, k, 0);
+          double grad = (phi(i, j, k, 0) - phi(ii, jj, kk, 0)) / g->dx;
+          if (scale && scale[d]) grad = grad * scale[d][f];
+          u[d][f] = u[d][f] - grad;
+        }
+  }
+  return 0;
+}
+
+double orc_norm(size_t n, const double *x, int type) { return norm_of(x, n, type); }
+
+}  // extern "C"
+
+// ========================================================== solver drivers
+namespace {
+
+struct Level {
+  mlgpu_grid g;
+  std::vector<double> a, c, b[3];
+  std::vector<double> u, f, r, e, uold;  // scratch
+};
+
+int mg_depth(const mlgpu_grid &g, int max_coarse) {
+  // MGnewOp returns nullptr when !coarsenable(2^depth * s_maxCoarse)
+  int depth = 0;
+  while (true) {
+    long c = (long)(1L << (depth + 1)) * max_coarse;
+    bool ok = true;
+    for (int d = 0; d < g.dim; d++)
+      if (g.n[d] % c != 0) ok = false;
+    if (!ok) break;
+    depth++;
+  }
+  return depth;  // number of coarser levels
+}
+
+void build_levels(std::vector<Level> &L, const mlgpu_grid &g0, int ncomp, const double *a0,
+                  const double *c0, const void *const b0[3], int max_coarse) {
+  int depth = mg_depth(g0, max_coarse);
+  L.resize(depth + 1);
+  L[0].g = g0;
+  size_t n0 = ncells(g0) * ncomp;
+  if (a0) L[0].a.assign(a0, a0 + n0);
+  if (c0) L[0].c.assign(c0, c0 + n0);
+  for (int d = 0; d < g0.dim; d++) {
+    const double *bb = (const double *)b0[d];
+    L[0].b[d].assign(bb, bb + nfaces(g0, d) * ncomp);
+  }
+  for (int l = 1; l <= depth; l++) {
+    L[l].g = coarsen_grid(L[l - 1].g);
+    size_t nc = ncells(L[l].g) * ncomp;
+    if (a0) {
+      L[l].a.assign(nc, 0);
+      orc_restrict_average(&L[l - 1].g, ncomp, L[l].a.data(), L[l - 1].a.data());
+    }
+    if (c0) {
+      L[l].c.assign(nc, 0);
+      orc_restrict_average(&L[l - 1].g, ncomp, L[l].c.data(), L[l - 1].c.data());
+    }
+    for (int d = 0; d < g0.dim; d++) {
+      L[l].b[d].assign(nfaces(L[l].g, d) * ncomp, 0);
+      coarsen_faces(L[l - 1].g, ncomp, d, L[l].b[d].data(), L[l - 1].b[d].data());
+    }
+  }
+  for (auto &lv : L) {
+    size_t n = ncells(lv.g) * ncomp;
+    lv.u.assign(n, 0);
+    lv.f.assign(n, 0);
+    lv.r.assign(n, 0);
+    lv.e.assign(n, 0);
+    lv.uold.assign(n, 0);
+  }
+}
+
+void vec_axpy(std::vector<double> &y, double a, const std::vector<double> &x) {
+  for (size_t q = 0; q < y.size(); q++) y[q] = y[q] + a * x[q];
+}
+
+// ---- nonlinear FAS
+struct HCSolver {
+  mlgpu_nlop op0;
+  mlgpu_mg_options o;
+  std::vector<Level> L;
+  double updates = 0;
+
+  mlgpu_nlop op_at(int l) {
+    mlgpu_nlop op = op0;
+    op.grid = L[l].g;
+    op.aCoef = L[l].a.empty() ? nullptr : L[l].a.data();
+    for (int d = 0; d < 3; d++) op.bCoef[d] = d < op.grid.dim ? L[l].b[d].data() : nullptr;
+    return op;
+  }
+  size_t cells(int l) { return ncells(L[l].g); }
+
+  void relax(int l, double *u, const double *f, int n) {
+    mlgpu_nlop op = op_at(l);
+    for (int s = 0; s < n; s++) {
+      if (o.relax_mode == MLGPU_RELAX_JACOBI)
+        orc_nl_jacobi(&op, u, f);
+      else {
+        orc_nl_gsrb_pass(&op, u, f, 0);
+        orc_nl_gsrb_pass(&op, u, f, 1);
+      }
+      updates += cells(l);
+    }
+  }
+
+  // FAS V-cycle on level l (restated AMRFASMultiGrid cycle)
+  void cycle(int l, double *u, const double *f) {
+    int last = (int)L.size() - 1;
+    if (l == last) {
+      relax(l, u, f, o.bottom_max_iter);
+      return;
+    }
+    relax(l, u, f, o.num_smooth_down);
+    mlgpu_nlop op = op_at(l), opc = op_at(l + 1);
+    Level &C = L[l + 1];
+    orc_restrict_average(&L[l].g, 2, C.u.data(), u);          // restrictR
+    orc_nl_restrict_residual(&op, C.r.data(), u, f);           // restrictResidual
+    updates += cells(l);
+    orc_nl_apply(&opc, C.f.data(), C.u.data());                // N_c(R u)
+    updates += cells(l + 1);
+    for (size_t q = 0; q < C.f.size(); q++) C.f[q] = C.f[q] + C.r[q];
+    C.uold = C.u;
+    for (int m = 0; m < o.num_mg; m++) cycle(l + 1, C.u.data(), C.f.data());
+    for (size_t q = 0; q < C.e.size(); q++) C.e[q] = C.u[q] - C.uold[q];
+    orc_prolong_increment(&L[l].g, &op0.phi_bc, 2, o.prolong, u, C.e.data());
+    relax(l, u, f, o.num_smooth_up);
+  }
+};
+
+struct VCSolver {
+  mlgpu_vcop op0;
+  mlgpu_mg_options o;
+  std::vector<Level> L;
+  double updates = 0;
+  mlgpu_vcop op_at(int l) {
+    mlgpu_vcop op = op0;
+    op.grid = L[l].g;
+    op.aCoef = L[l].a.empty() ? nullptr : L[l].a.data();
+    op.cCoef = L[l].c.empty() ? nullptr : L[l].c.data();
+    for (int d = 0; d < 3; d++) op.bCoef[d] = d < op.grid.dim ? L[l].b[d].data() : nullptr;
+    return op;
+  }
+  size_t cells(int l) { return ncells(L[l].g); }
+  void relax(int l, double *e, const double *r, int n) {
+    mlgpu_vcop op = op_at(l);
+    for (int s = 0; s < n; s++) {
+      if (o.relax_mode == MLGPU_RELAX_JACOBI)
+        orc_vc_jacobi(&op, e, r);
+      else {
+        orc_vc_gsrb_pass(&op, e, r, 0);
+        orc_vc_gsrb_pass(&op, e, r, 1);
+      }
+      updates += cells(l);
+    }
+  }
+  // MultiGrid::cycle (homogeneous correction form)
+  void cycle(int l, double *e, const double *r) {
+    int last = (int)L.size() - 1;
+    if (l == last) {
+      relax(l, e, r, o.bottom_max_iter);
+      return;
+    }
+    relax(l, e, r, o.num_smooth_down);
+    mlgpu_vcop op = op_at(l);
+    Level &C = L[l + 1];
+    orc_vc_restrict_residual(&op, C.r.data(), e, r);
+    updates += cells(l);
+    std::fill(C.e.begin(), C.e.end(), 0.0);
+    for (int m = 0; m < o.num_mg; m++) cycle(l + 1, C.e.data(), C.r.data());
+    orc_prolong_increment(&L[l].g, &op0.bc, 1, o.prolong, e, C.e.data());
+    relax(l, e, r, o.num_smooth_up);
+  }
+};
+
+// outer loop shared by both solvers (AMRMultiGrid::solveNoInit semantics)
+template <class Res, class Iter>
+int outer_loop(const mlgpu_mg_options &o, mlgpu_solve_stats *st, Res residual_norm,
+               Iter iterate) {
+  double norm0 = residual_norm();
+  st->initial_norm = norm0;
+  st->norm_history[0] = norm0;
+  st->iterations = 0;
+  st->cycles = 0;
+  st->exit_status = 0;
+  if (!std::isfinite(norm0)) {
+    st->exit_status = 8;
+    st->final_norm = norm0;
+    return MLGPU_ERR_NAN;
+  }
+  double norm = norm0, prev = norm0;
+  int iter = 0;
+  while (norm > o.tolerance * norm0 && norm0 > o.norm_thresh && iter < o.max_iter) {
+    iterate();
+    iter++;
+    norm = residual_norm();
+    if (iter < 64) st->norm_history[iter] = norm;
+    if (!std::isfinite(norm)) {
+      st->exit_status = 8;
+      break;
+    }
+    if (norm > (1.0 - o.hang) * prev && norm > o.tolerance * norm0) {
+      st->exit_status = 2;
+      break;
+    }
+    prev = norm;
+  }
+  st->iterations = iter;
+  st->final_norm = norm;
+  if (st->exit_status == 0 && norm > o.tolerance * norm0 && norm0 > o.norm_thresh)
+    st->exit_status = 4;
+  if (st->exit_status == 8) return MLGPU_ERR_NAN;
+  if (st->exit_status == 2) return MLGPU_ERR_HANG;
+  if (st->exit_status == 4) return MLGPU_ERR_NOT_CONVERGED;
+  return MLGPU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void orc_mg_default_options(mlgpu_mg_options *o, int hc) {
+  memset(o, 0, sizeof(*o));
+  // HCMultigrid defaults (srcSubcycle/MushyLayerSubcycleUtils.cpp:668-678)
+  // or projection defaults (srcSubcycle/Projector.cpp:44-64)
+  o->num_smooth_down = hc ? 1 : 2;
+  o->num_smooth_up = 4;
+  o->num_mg = 1;
+  o->max_iter = hc ? 10 : 20;
+  o->tolerance = hc ? 1e-10 : 1e-15;
+  o->hang = hc ? 1e-10 : 1e-15;
+  o->norm_thresh = hc ? 1e-10 : 1e-30;
+  o->relax_mode = MLGPU_RELAX_GSRB;
+  o->bottom_solver = MLGPU_BOTTOM_RELAX;
+  o->bottom_max_iter = hc ? 40 : 20;
+  o->max_coarse = 2;
+  o->prolong = hc ? MLGPU_PROLONG_LINEAR : MLGPU_PROLONG_CONSTANT;
+  o->precision = MLGPU_PREC_F64;
+  o->inner_cycles = 1;
+  o->norm_type = MLGPU_NORM_MAX;
+  o->use_graph = 0;
+}
+
+int orc_mg_depth(const mlgpu_grid *g, int max_coarse) { return mg_depth(*g, max_coarse); }
+
+int orc_hc_solve(const mlgpu_nlop *op, const mlgpu_mg_options *o, double *phi,
+                 const double *rhs, mlgpu_solve_stats *st) {
+  HCSolver S;
+  S.op0 = *op;
+  S.o = *o;
+  build_levels(S.L, op->grid, 2, (const double *)op->aCoef, nullptr, op->bCoef,
+               o->max_coarse);
+  memset(st, 0, sizeof(*st));
+  st->levels = (int)S.L.size();
+  size_t n = 2 * ncells(op->grid);
+  std::vector<double> r(n);
+  auto resnorm = [&]() {
+    orc_nl_residual(op, r.data(), phi, rhs);
+    S.updates += ncells(op->grid);
+    return norm_of(r.data(), n, o->norm_type);
+  };
+  int cycles = 0;
+  auto iterate = [&]() {
+    S.cycle(0, phi, rhs);
+    cycles++;
+  };
+  int rc = outer_loop(*o, st, resnorm, iterate);
+  st->cycles = cycles;
+  st->cell_updates = S.updates;
+  return rc;
+}
+
+int orc_vc_solve(const mlgpu_vcop *op, const mlgpu_mg_options *o, double *phi,
+                 const double *rhs, mlgpu_solve_stats *st) {
+  VCSolver S;
+  S.op0 = *op;
+  S.o = *o;
+  build_levels(S.L, op->grid, 1, (const double *)op->aCoef, (const double *)op->cCoef,
+               op->bCoef, o->max_coarse);
+  memset(st, 0, sizeof(*st));
+  st->levels = (int)S.L.size();
+  size_t n = ncells(op->grid);
+  std::vector<double> r(n), e(n);
+  auto resnorm = [&]() {
+    orc_vc_residual(op, r.data(), phi, rhs, 0);
+    S.updates += n;
+    return norm_of(r.data(), n, o->norm_type);
+  };
+  int cycles = 0;
+  auto iterate = [&]() {
+    std::fill(e.begin(), e.end(), 0.0);
+    for (int m = 0; m < std::max(1, o->inner_cycles); m++) {
+      S.cycle(0, e.data(), r.data());
+      cycles++;
+    }
+    for (size_t q = 0; q < n; q++) phi[q] = phi[q] + e[q];
+  };
+  int rc = outer_loop(*o, st, resnorm, iterate);
+  st->cycles = cycles;
+  st->cell_updates = S.updates;
+  return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,379 @@
+"""GPU parity: every sm_103a kernel against the CPU oracle on seeded inputs.
+
+FP64 kernels are required to be bitwise equal to the oracle (both evaluate
+the reference's Fortran expressions in the same order without contraction).
+FP32 kernels (inner cycles of the mixed solver) are checked against the
+FP64 oracle with a relative tolerance of 1e-5 of the field scale.
+"""
+import numpy as np
+import pytest
+
+import problems as P
+from mushy_gb300 import abi
+from oracle import oracle as O
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib():
+    import __graft_entry__
+    __graft_entry__.build()
+    from mushy_gb300 import ops  # noqa: F401
+    yield
+
+
+def dev(a, dtype=None):
+    t = torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    return t.to(dtype) if dtype is not None else t
+
+
+def host(t):
+    torch.cuda.synchronize()
+    return t.double().cpu().numpy()
+
+
+def exact(a, b):
+    assert a.shape == b.shape
+    if not np.array_equal(a, b):
+        d = np.abs(a - b)
+        raise AssertionError("not bitwise equal: max diff %g at %s (%r vs %r)"
+                             % (d.max(), np.unravel_index(d.argmax(), d.shape),
+                                a.flat[d.argmax()], b.flat[d.argmax()]))
+
+
+def close32(gpu, ref, rtol=1e-5):
+    scale = max(np.abs(ref).max(), 1e-30)
+    err = np.abs(gpu - ref).max() / scale
+    assert err < rtol, "FP32 relative error %g >= %g" % (err, rtol)
+
+
+CASES_2D = [((16, 12), (0, 0, 0)), ((18, 10), (1, 0, 0)), ((8, 8), (1, 1, 0))]
+CASES_3D = [((8, 6, 4), (0, 0, 0)), ((6, 4, 8), (0, 1, 1))]
+ALL = CASES_2D + CASES_3D
+
+
+def nl_setup(n, per, seed, a=True, dbc=True, kind="mixed"):
+    from mushy_gb300 import ops
+    rng = np.random.default_rng(seed)
+    g = P.grid(n, per)
+    p = P.mushy_params()
+    phi_bc, der = P.hc_bcs(kind)
+    phi = P.hc_state(g, rng)
+    rhs = phi + 0.1 * rng.standard_normal(phi.shape)
+    b = P.faces(g, rng, 2)
+    aC = rng.uniform(0.5, 1.5, phi.shape) if a else None
+    alpha, beta = 1.0, -2e-3
+    ref = O.NLOpHost(g, p, phi_bc, der, alpha, beta, aC, b, apply_derived_bc=int(dbc))
+    op = ops.NLMultiCompOp(g, p, phi_bc, der, alpha, beta, None if aC is None else dev(aC),
+                           [dev(x) for x in b], apply_derived_bc=dbc)
+    return g, p, ref, op, phi, rhs
+
+
+# ------------------------------------------------------------------ closure
+@pytest.mark.parametrize("seed", [0, 1])
+def test_closure_full_bitwise(seed):
+    from mushy_gb300 import ops
+    import ctypes as C
+    rng = np.random.default_rng(seed)
+    g = P.grid((33, 17))
+    for params in (P.mushy_params(), P.mushy_params(specificHeatRatio=1.3, thetaEutectic=0.2,
+                                                    ThetaEutectic=0.1, waterDistributionCoeff=0.05)):
+        HC = P.hc_state(g, rng)
+        ref = O.closure(g, params, HC)
+        d = dev(HC)
+        outs = {k: torch.empty(abi.ncells(g), dtype=torch.float64, device="cuda")
+                for k in ("T", "porosity", "Cl", "Cs", "Hs", "He", "Hl")}
+        abi.check(abi.load().mlgpu_closure(C.byref(g), C.byref(params), ops._ptr(d),
+                                           *[ops._ptr(outs[k]) for k in
+                                             ("T", "porosity", "Cl", "Cs", "Hs", "He", "Hl")],
+                                           ops._stream()))
+        for k in outs:
+            exact(host(outs[k]), ref[k])
+
+
+def test_closure_tcl_bitwise():
+    from mushy_gb300 import ops
+    import ctypes as C
+    rng = np.random.default_rng(3)
+    g = P.grid((40, 9))
+    p = P.mushy_params()
+    HC = P.hc_state(g, rng)
+    ref = O.closure_tcl(g, p, HC)
+    d = dev(HC)
+    out = torch.empty_like(d)
+    abi.check(abi.load().mlgpu_closure_tcl(C.byref(g), C.byref(p), ops._ptr(d), ops._ptr(out),
+                                           ops._stream()))
+    exact(host(out), ref)
+
+
+# ------------------------------------------------------ nonlinear operator
+@pytest.mark.parametrize("n,per", ALL)
+@pytest.mark.parametrize("dbc", [True, False])
+def test_nl_residual_apply_bitwise(n, per, dbc):
+    g, p, ref, op, phi, rhs = nl_setup(n, per, 11, dbc=dbc)
+    d_phi, d_rhs = dev(phi), dev(rhs)
+    res = torch.empty_like(d_phi)
+    nrm = op.residual(res, d_phi, d_rhs, norm_type=abi.NORM_MAX)
+    r_ref = O.nl_residual(ref, phi, rhs)
+    exact(host(res), r_ref)
+    assert nrm == np.abs(r_ref).max()
+    lhs = torch.empty_like(d_phi)
+    op.applyOp(lhs, d_phi)
+    exact(host(lhs), O.nl_apply(ref, phi))
+    nrm2 = op.residual(res, d_phi, d_rhs, norm_type=abi.NORM_L2)
+    assert abs(nrm2 - np.sqrt((r_ref ** 2).sum())) <= 1e-12 * nrm2
+
+
+@pytest.mark.parametrize("n,per", ALL)
+def test_nl_gsrb_bitwise(n, per):
+    g, p, ref, op, phi, rhs = nl_setup(n, per, 12)
+    d_phi, d_rhs = dev(phi), dev(rhs)
+    op.levelGSRBPass(d_phi, d_rhs, 0)
+    exact(host(d_phi), O.nl_gsrb_pass(ref, phi, rhs, 0))
+    op.relax(d_phi, d_rhs, 3)
+    r = O.nl_gsrb_pass(ref, phi, rhs, 0)
+    r = O.nl_relax(ref, r, rhs, 3)
+    exact(host(d_phi), r)
+
+
+@pytest.mark.parametrize("n,per", CASES_2D[:2] + CASES_3D[:1])
+def test_nl_jacobi_lambda_bitwise(n, per):
+    g, p, ref, op, phi, rhs = nl_setup(n, per, 13)
+    d_phi, d_rhs = dev(phi), dev(rhs)
+    exact(host(op.computeLambda()), O.nl_lambda(ref))
+    op.levelJacobi(d_phi, d_rhs)
+    exact(host(d_phi), O.nl_jacobi(ref, phi, rhs))
+
+
+@pytest.mark.parametrize("n,per", ALL)
+def test_nl_restrict_residual_bitwise(n, per):
+    g, p, ref, op, phi, rhs = nl_setup(n, per, 14)
+    d_phi, d_rhs = dev(phi), dev(rhs)
+    rc = op.createCoarser()
+    op.restrictResidual(rc, d_phi, d_rhs)
+    exact(host(rc), O.nl_restrict_residual(ref, phi, rhs))
+    pc = op.createCoarser()
+    op.restrictR(pc, d_phi)
+    exact(host(pc), O.restrict_average(g, 2, phi))
+
+
+def test_nl_fp32_kernels_close():
+    from mushy_gb300 import ops
+    g, p, ref, op64, phi, rhs = nl_setup((20, 16), (1, 0, 0), 15, kind="mixed")
+    rng = np.random.default_rng(15)
+    op = ops.NLMultiCompOp(g, p, op64.phi_bc, op64.derived_bc, op64.alpha, op64.beta,
+                           op64.aCoef.float(), [b.float() for b in op64.bCoef])
+    d_phi, d_rhs = dev(phi, torch.float32), dev(rhs, torch.float32)
+    res = torch.empty_like(d_phi)
+    op.residual(res, d_phi, d_rhs)
+    close32(host(res), O.nl_residual(ref, host(d_phi), host(d_rhs)), 1e-4)
+    op.levelGSRB(d_phi, d_rhs)
+    close32(host(d_phi), O.nl_relax(ref, phi, rhs, 1), 1e-5)
+
+
+# ---------------------------------------------------------------- transfers
+@pytest.mark.parametrize("n,per", ALL)
+@pytest.mark.parametrize("kind", [abi.PROLONG_CONSTANT, abi.PROLONG_LINEAR])
+def test_prolong_bitwise(n, per, kind):
+    import ctypes as C
+    from mushy_gb300 import ops
+    rng = np.random.default_rng(20)
+    g = P.grid(n, per)
+    bc = P.vc_bc("mixed")
+    for ncomp in (1, 2):
+        fine = rng.standard_normal((ncomp,) + abi.cell_shape(g))
+        coarse = rng.standard_normal(O.coarse_shape(g, ncomp))
+        ref = O.prolong_increment(g, bc, ncomp, kind, fine, coarse)
+        df, dc = dev(fine), dev(coarse)
+        abi.check(abi.load().mlgpu_prolong_increment(C.byref(g), C.byref(bc), ncomp, abi.F64,
+                                                     kind, ops._ptr(df), ops._ptr(dc),
+                                                     ops._stream()))
+        exact(host(df), ref)
+
+
+@pytest.mark.parametrize("n,per", ALL)
+def test_coarsen_coefficients_bitwise(n, per):
+    import ctypes as C
+    from mushy_gb300 import ops
+    rng = np.random.default_rng(21)
+    g = P.grid(n, per)
+    for d in range(g.dim):
+        ff = rng.uniform(0.1, 2.0, (2,) + abi.face_shape(g, d))
+        ref = O.coarsen_faces(g, 2, d, ff)
+        out = torch.empty(ref.shape, dtype=torch.float64, device="cuda")
+        abi.check(abi.load().mlgpu_coarsen_faces(C.byref(g), 2, abi.F64, d, ops._ptr(out),
+                                                 ops._ptr(dev(ff)), ops._stream()))
+        exact(host(out), ref)
+
+
+@pytest.mark.parametrize("n,per", CASES_2D + CASES_3D[:1])
+def test_face_geomean_and_mac_bitwise(n, per):
+    import ctypes as C
+    from mushy_gb300 import ops
+    rng = np.random.default_rng(22)
+    g = P.grid(n, per)
+    cell = rng.uniform(0.05, 1.0, abi.cell_shape(g))
+    ref = O.face_geomean(g, cell)
+    outs = [torch.empty(abi.face_shape(g, d), dtype=torch.float64, device="cuda")
+            for d in range(g.dim)]
+    arr = (C.c_void_p * 3)(*([o.data_ptr() for o in outs] + [None] * (3 - g.dim)))
+    abi.check(abi.load().mlgpu_face_geomean(C.byref(g), ops._ptr(dev(cell)), arr, ops._stream()))
+    for d in range(g.dim):
+        exact(host(outs[d]), ref[d])
+    # MAC divergence and gradient correction
+    u = [rng.standard_normal(abi.face_shape(g, d)) for d in range(g.dim)]
+    du = [dev(x) for x in u]
+    div = torch.empty(abi.cell_shape(g), dtype=torch.float64, device="cuda")
+    uarr = (C.c_void_p * 3)(*([x.data_ptr() for x in du] + [None] * (3 - g.dim)))
+    abi.check(abi.load().mlgpu_mac_divergence(C.byref(g), ops._ptr(div), uarr, ops._stream()))
+    exact(host(div), O.mac_divergence(g, u))
+    bc = P.vc_bc("mixed")
+    phi = rng.standard_normal(abi.cell_shape(g))
+    scale = [rng.uniform(0.1, 1, abi.face_shape(g, d)) for d in range(g.dim)]
+    dsc = [dev(x) for x in scale]
+    sarr = (C.c_void_p * 3)(*([x.data_ptr() for x in dsc] + [None] * (3 - g.dim)))
+    abi.check(abi.load().mlgpu_mac_correct(C.byref(g), C.byref(bc), ops._ptr(dev(phi)), sarr,
+                                           uarr, ops._stream()))
+    ref_u = O.mac_correct(g, bc, phi, u, scale)
+    for d in range(g.dim):
+        exact(host(du[d]), ref_u[d])
+
+
+# ------------------------------------------------------- linear operators
+def vc_setup(n, per, seed, with_c, with_a, dtype=torch.float64):
+    from mushy_gb300 import ops
+    rng = np.random.default_rng(seed)
+    g = P.grid(n, per)
+    bc = P.vc_bc("mixed")
+    b = P.faces(g, rng, 1)
+    b = [x[0] for x in b]
+    aC = rng.uniform(0.5, 1.5, abi.cell_shape(g)) if with_a else None
+    cC = rng.uniform(0.1, 3.0, abi.cell_shape(g)) if with_c else None
+    alpha, beta = (0.7, -0.9) if with_c else (0.0, 1.0)
+    ref = O.VCOpHost(g, bc, alpha, beta, aC, b, cC)
+    cls = ops.DarcyBrinkmanOp if with_c else ops.ProjectionOp
+    op = cls(g, bc, alpha, beta, None if aC is None else dev(aC, dtype),
+             [dev(x, dtype) for x in b], None if cC is None else dev(cC, dtype))
+    phi = rng.standard_normal(abi.cell_shape(g))
+    rhs = rng.standard_normal(abi.cell_shape(g))
+    return g, ref, op, phi, rhs
+
+
+@pytest.mark.parametrize("n,per", ALL)
+@pytest.mark.parametrize("with_c", [False, True])
+def test_vc_ops_bitwise(n, per, with_c):
+    g, ref, op, phi, rhs = vc_setup(n, per, 30, with_c, with_c)
+    d_phi, d_rhs = dev(phi), dev(rhs)
+    res = torch.empty_like(d_phi)
+    for hom in (0, 1):
+        nrm = op.residual(res, d_phi, d_rhs, homogeneous=hom, norm_type=abi.NORM_MAX)
+        r = O.vc_residual(ref, phi, rhs, hom)
+        exact(host(res), r)
+        assert nrm == np.abs(r).max()
+        op.applyOp(res, d_phi, homogeneous=hom)
+        exact(host(res), O.vc_apply(ref, phi, hom))
+    exact(host(op.computeLambda()), O.vc_lambda(ref))
+    rc = op.createCoarser()
+    op.restrictResidual(rc, d_phi, d_rhs)
+    exact(host(rc), O.vc_restrict_residual(ref, phi, rhs))
+    op.levelGSRBPass(d_phi, d_rhs, 0)
+    r1 = O.vc_gsrb_pass(ref, phi, rhs, 0)
+    exact(host(d_phi), r1)
+    op.relax(d_phi, d_rhs, 2)
+    exact(host(d_phi), O.vc_relax(ref, r1, rhs, 2))
+    op.levelJacobi(d_phi, d_rhs)
+    exact(host(d_phi), O.vc_jacobi(ref, O.vc_relax(ref, r1, rhs, 2), rhs))
+
+
+def test_vc_fp32_close():
+    g, ref, op, phi, rhs = vc_setup((24, 16), (1, 0, 0), 31, True, True, torch.float32)
+    d_phi, d_rhs = dev(phi, torch.float32), dev(rhs, torch.float32)
+    res = torch.empty_like(d_phi)
+    op.residual(res, d_phi, d_rhs)
+    close32(host(res), O.vc_residual(ref, host(d_phi), host(d_rhs)), 1e-5)
+    op.relax(d_phi, d_rhs, 2)
+    close32(host(d_phi), O.vc_relax(ref, phi, rhs, 2), 1e-5)
+
+
+# -------------------------------------------------------------------- solvers
+def test_vc_solver_fp64_matches_oracle():
+    from mushy_gb300 import ops
+    g, chi, perm, u = P.projection_problem((64, 64), 5, sigma=8.0)
+    faces = O.face_geomean(g, perm)
+    b = [-f for f in faces]
+    f = O.mac_divergence(g, u)
+    f -= f.mean()
+    bc = abi.make_bc()
+    ref = O.VCOpHost(g, bc, 0.0, 1.0, None, b)
+    opts = O.default_options(0)
+    opts.tolerance, opts.hang, opts.max_iter = 1e-10, 1e-15, 30
+    sol_ref, st_ref, rc_ref = O.vc_solve(ref, opts, np.zeros_like(f), f)
+    assert rc_ref == 0
+    op = ops.ProjectionOp(g, bc, 0.0, 1.0, None, [dev(x) for x in b])
+    for graph in (0, 1):
+        o = ops.default_options(False)
+        o.tolerance, o.hang, o.max_iter, o.use_graph = 1e-10, 1e-15, 30, graph
+        S = ops.AMRMultiGrid(op, o)
+        d_phi = torch.zeros_like(dev(f))
+        st, rc = S.solve(d_phi, dev(f))
+        assert rc == 0 and st.iterations == st_ref.iterations
+        exact(host(d_phi), sol_ref)
+        assert st.cell_updates == st_ref.cell_updates
+
+
+def test_vc_solver_mixed_converges():
+    from mushy_gb300 import ops
+    g, chi, perm, u = P.projection_problem((128, 128), 6, sigma=16.0)
+    faces = O.face_geomean(g, perm)
+    b = [-f for f in faces]
+    f = O.mac_divergence(g, u)
+    f -= f.mean()
+    bc = abi.make_bc()
+    op = ops.ProjectionOp(g, bc, 0.0, 1.0, None, [dev(x) for x in b])
+    o64 = ops.default_options(False)
+    o64.tolerance, o64.hang, o64.max_iter = 1e-10, 1e-15, 40
+    om = ops.default_options(False)
+    om.tolerance, om.hang, om.max_iter, om.precision = 1e-10, 1e-15, 40, abi.PREC_MIXED
+    p64 = torch.zeros_like(dev(f))
+    st64, rc64 = ops.AMRMultiGrid(op, o64).solve(p64, dev(f))
+    pm = torch.zeros_like(dev(f))
+    stm, rcm = ops.AMRMultiGrid(op, om).solve(pm, dev(f))
+    assert rc64 == 0 and rcm == 0
+    assert stm.final_norm <= 1e-10 * stm.initial_norm
+    # FP64-checked residual of the mixed solution
+    ref = O.VCOpHost(g, bc, 0.0, 1.0, None, b)
+    r = O.vc_residual(ref, host(pm), f)
+    assert np.abs(r).max() <= 1e-10 * np.abs(f).max() * 1.0001
+    # solutions agree up to the null-space constant
+    a, m = host(p64), host(pm)
+    diff = (a - a.mean()) - (m - m.mean())
+    assert np.abs(diff).max() <= 1e-8 * np.abs(a - a.mean()).max()
+
+
+def test_hc_solver_fp64_matches_oracle():
+    from mushy_gb300 import ops
+    n = 32
+    g = P.grid((n, n))
+    p = P.mushy_params()
+    phi_bc, der = P.hc_bcs("mixed")
+    rng = np.random.default_rng(40)
+    phi = P.hc_state(g, rng, regimes=False)
+    dt = 1e-3
+    b = [np.stack([-np.ones(abi.face_shape(g, d)), -0.01 * np.ones(abi.face_shape(g, d))])
+         for d in range(2)]
+    ref = O.NLOpHost(g, p, phi_bc, der, 1.0, -dt, None, b)
+    opts = O.default_options(1)
+    opts.max_iter = 6
+    sol_ref, st_ref, rc_ref = O.hc_solve(ref, opts, phi, phi.copy())
+    op = ops.NLMultiCompOp(g, p, phi_bc, der, 1.0, -dt, None, [dev(x) for x in b])
+    for graph in (0, 1):
+        o = ops.default_options(True)
+        o.max_iter, o.use_graph = 6, graph
+        S = ops.AMRFASMultiGrid(op, o)
+        d_phi = dev(phi)
+        st, rc = S.solve(d_phi, dev(phi))
+        assert rc == rc_ref and st.iterations == st_ref.iterations
+        exact(host(d_phi), sol_ref)
+        assert st.cell_updates == st_ref.cell_updates

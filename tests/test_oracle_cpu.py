@@ -1,0 +1,244 @@
+"""CPU tests of the oracle (the checker) and of the host-side library surface.
+
+* closure identities and known answers from the reference's phase diagram
+  (src/EnthalpyVariablesF.ChF, src/phaseDiagram.cpp);
+* an independent pure-numpy restatement of the nonlinear residual and one
+  GSRB pass with explicit ghost cells, compared with the C++ oracle;
+* manufactured-solution checks of the linear operator and multigrid solver;
+* the C-ABI library exports every entry point declared in include/mlgpu.h.
+"""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+import problems as P
+from mushy_gb300 import abi
+from oracle import oracle as O
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+# ------------------------------------------------------------ closure
+def test_closure_regimes_known_answers():
+    g = P.grid((4, 1))
+    p = P.mushy_params()  # St=5, CR=5, k=1e-3, cp=1, theta_e=Theta_e=0
+    HC = np.zeros((2, 1, 1, 4))
+    HC[0, 0, 0] = [6.0, 5.0, 0.5, -0.5]   # liquid, mush, eutectic, solid
+    HC[1, 0, 0] = [-1.0, -1.0, -4.0, -4.0]
+    out = O.closure(g, p, HC)
+    T, chi, Cl = out["T"], out["porosity"], out["Cl"]
+    # liquid: T = H - St, C_l = C, chi = 1
+    assert T[0] == 1.0 and Cl[0] == -1.0 and chi[0] == 1.0
+    # mush: T = -C_l, chi in (0,1), H = chi*St + T (cp = 1), C = chi*C_l + (1-chi)*C_s
+    assert T[1] == -Cl[1] and 0 < chi[1] < 1
+    assert abs(chi[1] * 5.0 + T[1] - 5.0) < 1e-12
+    assert abs(chi[1] * Cl[1] + (1 - chi[1]) * out["Cs"][1] - (-1.0)) < 1e-12
+    # eutectic (H_s < H <= H_e): T = theta_e = 0, C_l = Theta_e = 0
+    assert T[2] == 0.0 and Cl[2] == 0.0 and abs(chi[2] - 0.5 / 5.0) < 1e-15
+    # solid: T = H / cp, porosity 0
+    assert T[3] == -0.5 and chi[3] == 0.0
+    # bounding energies: H_l = St - C, H_e = chi_e St with chi_e = (CR + C)/CR
+    assert out["Hl"][0] == 6.0 and abs(out["He"][0] - 4.0) < 1e-15 and out["Hs"][0] == 0.0
+
+
+def test_closure_continuous_at_liquidus():
+    g = P.grid((2, 1))
+    p = P.mushy_params()
+    C = -1.3
+    Hl = 5.0 - C
+    HC = np.array([[[[Hl - 1e-9, Hl + 1e-9]]], [[[C, C]]]])
+    out = O.closure(g, p, HC)
+    assert abs(out["porosity"][0] - 1.0) < 1e-6
+    assert abs(out["T"][0] - out["T"][1]) < 1e-6
+
+
+def test_closure_tcl_matches_full_closure():
+    rng = np.random.default_rng(0)
+    g = P.grid((16, 8))
+    p = P.mushy_params(specificHeatRatio=1.2, waterDistributionCoeff=0.02)
+    HC = P.hc_state(g, rng)
+    full = O.closure(g, p, HC)
+    tcl = O.closure_tcl(g, p, HC).reshape(2, -1)
+    assert np.array_equal(tcl[0], full["T"]) and np.array_equal(tcl[1], full["Cl"])
+
+
+def test_porosity_clamps_c_below_minus_cr():
+    # CALCULATEPOROSITYMUSH uses max(C, -CR); the scalar C++ version does not
+    g = P.grid((1, 1))
+    p = P.mushy_params()
+    HC = np.array([[[[4.0]]], [[[-5.5]]]])
+    out = O.closure(g, p, HC)
+    assert np.isfinite(out["porosity"]).all()
+
+
+# --------------------------------------- independent numpy restatement
+def _np_closure_tcl(H, C, p):
+    CR, k, cp, St = (p.compositionRatio, p.waterDistributionCoeff, p.specificHeatRatio,
+                     p.stefan)
+    Hs = np.where(C < -CR, 0.0, cp * ((-C - CR) / k))
+    Hs = np.where(Hs < 0, 0.0, Hs)
+    He = (CR + C) / CR * St
+    Hl = St - C
+    T = np.empty_like(H)
+    Cl = np.empty_like(H)
+    vC = np.where(C >= -CR, C, -CR)
+    a = CR * (cp - 1) + St * (k - 1)
+    b = CR * (1 - 2 * cp) + H * (1 - k) - vC * (cp - 1) - k * St
+    c = (CR + vC) * cp + k * H
+    with np.errstate(invalid="ignore"):
+        chi = (-b - np.sqrt(b * b - 4 * a * c)) / (2 * a)
+    solid, eut = H <= Hs, (H > Hs) & (H <= He)
+    mush, liq = (H > He) & (H < Hl), H >= Hl
+    T[solid], Cl[solid] = H[solid] / cp, 0.0
+    T[eut], Cl[eut] = 0.0, 0.0
+    cl = (C + CR * (1 - chi)) / (chi + k * (1 - chi))
+    T[mush], Cl[mush] = -cl[mush], cl[mush]
+    T[liq], Cl[liq] = H[liq] - St, C[liq]
+    return T, Cl
+
+
+def test_oracle_nl_residual_against_numpy_ghost_fill():
+    rng = np.random.default_rng(5)
+    nx, ny = 10, 6
+    g = P.grid((nx, ny), (1, 0, 0))
+    p = P.mushy_params()
+    phi_bc, der = P.hc_bcs("mixed")
+    phi = P.hc_state(g, rng)
+    rhs = rng.standard_normal(phi.shape)
+    bx, by = P.faces(g, rng, 2)
+    alpha, beta, dx = 1.0, -3e-3, g.dx
+    ref = O.NLOpHost(g, p, phi_bc, der, alpha, beta, None, [bx, by])
+    res = O.nl_residual(ref, phi, rhs)
+    # numpy: closure on interior, periodic x ghosts, derived BC rows in y
+    T, Cl = _np_closure_tcl(phi[0, 0], phi[1, 0], p)
+    pl = np.zeros((2, ny + 2, nx + 2))
+    pl[0, 1:-1, 1:-1], pl[1, 1:-1, 1:-1] = T, Cl
+    pl[:, 1:-1, 0], pl[:, 1:-1, -1] = pl[:, 1:-1, -2], pl[:, 1:-1, 1]
+    for c, (vlo, vhi) in enumerate([(-1.0, 0.5), (-1.0, -1.0)]):
+        pl[c, 0, 1:-1] = 2 * vlo - pl[c, 1, 1:-1]
+        pl[c, -1, 1:-1] = 2 * vhi - pl[c, -2, 1:-1]
+    mine = np.empty_like(phi)
+    for c in range(2):
+        q = pl[c]
+        p0 = q[1:-1, 1:-1]
+        s = (bx[c, 0, :, 1:] * (q[1:-1, 2:] - p0) - bx[c, 0, :, :-1] * (p0 - q[1:-1, :-2]))
+        s = s + by[c, 0, 1:, :] * (q[2:, 1:-1] - p0)
+        s = s - by[c, 0, :-1, :] * (p0 - q[:-2, 1:-1])
+        mine[c, 0] = rhs[c, 0] - (alpha * phi[c, 0] - beta * s * (1.0 / (dx * dx)))
+    assert np.allclose(mine, res, rtol=1e-13, atol=1e-13)
+
+
+def test_oracle_gsrb_colours_and_fixed_point():
+    rng = np.random.default_rng(6)
+    g = P.grid((8, 6))
+    p = P.mushy_params()
+    phi_bc, der = P.hc_bcs("mixed")
+    phi = P.hc_state(g, rng)
+    rhs = phi.copy()
+    b = P.faces(g, rng, 2)
+    ref = O.NLOpHost(g, p, phi_bc, der, 1.0, -1e-3, None, b)
+    red = O.nl_gsrb_pass(ref, phi, rhs, 0)
+    changed = red != phi
+    ii, jj = np.meshgrid(np.arange(8), np.arange(6))
+    black = ((ii + jj) % 2 == 1)[None, None]
+    assert not changed[:, :, black[0, 0]].any()  # black cells untouched by red pass
+    # at a converged solution a sweep is a fixed point
+    sol, st, rc = O.hc_solve(ref, _opts(hc=True, tol=1e-13, iters=60), phi, rhs)
+    again = O.nl_relax(ref, sol, rhs, 1)
+    assert np.abs(again - sol).max() < 1e-9
+
+
+def _opts(hc, tol, iters):
+    o = O.default_options(hc)
+    o.tolerance, o.max_iter, o.hang = tol, iters, 0.0
+    return o
+
+
+# ------------------------------------------------ linear operator / solver
+def test_vc_operator_exact_on_quadratic():
+    # div(grad x^2) = 2 with b = -1, alpha=0, beta=1: L = div grad
+    n = 16
+    g = abi.make_grid([n, n], 1.0 / n, (0, 0, 0))
+    x = (np.arange(n) + 0.5) / n
+    X, Y = np.meshgrid(x, x)
+    phi = (X ** 2 + 2 * Y ** 2)[None]
+    b = [np.ones(abi.face_shape(g, d)) for d in range(2)]
+    ref = O.VCOpHost(g, abi.make_bc(), 0.0, -1.0, None, b)
+    lhs = O.vc_apply(ref, phi, 0)
+    # interior cells only (ghosts from Neumann 0 spoil the boundary rows)
+    assert np.allclose(lhs[0, 1:-1, 1:-1], 6.0, atol=1e-9)
+
+
+def test_vc_multigrid_solves_manufactured_problem():
+    n = 64
+    g = abi.make_grid([n, n], 1.0 / n, (1, 0, 0))
+    rng = np.random.default_rng(7)
+    sol = rng.standard_normal((1, n, n))
+    b = [-rng.uniform(0.5, 2.0, abi.face_shape(g, d)) for d in range(2)]
+    bc = abi.make_bc({(1, 0, 0): (abi.BC_DIRICHLET, 0.3), (1, 1, 0): (abi.BC_NEUMANN, 0.7)})
+    ref = O.VCOpHost(g, bc, 0.0, 1.0, None, b)
+    f = O.vc_apply(ref, sol, 0)
+    out, st, rc = O.vc_solve(ref, _opts(False, 1e-12, 60), np.zeros_like(sol), f)
+    assert rc == 0
+    assert np.abs(out - sol).max() < 1e-8
+
+
+def test_mg_depth_follows_max_coarse():
+    assert O.mg_depth(P.grid((64, 64)), 2) == 5        # 64 -> 2
+    assert O.mg_depth(P.grid((512, 512)), 2) == 8      # 512 -> 2
+    assert O.mg_depth(P.grid((96, 64)), 2) == 4        # limited by 96 = 3 * 32
+    assert O.mg_depth(P.grid((256, 256, 256)), 2) == 7
+
+
+def test_restriction_prolongation_adjoint_scaling():
+    # constant prolongation of a restricted constant field reproduces it
+    g = P.grid((8, 8))
+    fine = np.full((1, 1, 8, 8), 3.25)
+    c = O.restrict_average(g, 1, fine)
+    assert np.all(c == 3.25)
+    back = O.prolong_increment(g, abi.make_bc(), 1, abi.PROLONG_CONSTANT, np.zeros_like(fine), c)
+    assert np.all(back == 3.25)
+    lin = O.prolong_increment(g, abi.make_bc(), 1, abi.PROLONG_LINEAR, np.zeros_like(fine), c)
+    assert np.allclose(lin, 3.25, rtol=0, atol=1e-15)
+
+
+# ------------------------------------------------------ ABI surface
+def _header_symbols():
+    txt = open(os.path.join(ROOT, "include", "mlgpu.h")).read()
+    return sorted(set(re.findall(r"\b(mlgpu_[a-z0-9_]+)\s*\(", txt)))
+
+
+def test_python_binding_declares_every_header_symbol():
+    assert abi.declared_symbols() == _header_symbols()
+
+
+def test_library_exports_every_symbol():
+    import __graft_entry__
+    __graft_entry__.build()
+    lib = C.CDLL(abi.LIB_PATH)
+    for name in _header_symbols():
+        assert hasattr(lib, name), name
+    lib2 = abi.load()
+    assert lib2.mlgpu_version() >= 1
+    assert lib2.mlgpu_status_string(abi.ERR_ARG) == b"invalid argument"
+
+
+def test_argument_validation_without_gpu():
+    lib = abi.load()
+    bad = abi.make_grid([8, 8])
+    bad.dim = 4
+    p = abi.make_params()
+    assert lib.mlgpu_closure(C.byref(bad), C.byref(p), None, None, None, None, None, None,
+                             None, None, None) == abi.ERR_ARG
+    nbytes = C.c_size_t()
+    op = abi.VCOp()
+    op.grid = abi.make_grid([64, 64])
+    opts = abi.MGOptions()
+    lib.mlgpu_mg_default_options(C.byref(opts), 0)
+    assert lib.mlgpu_vc_solver_workspace(C.byref(op), C.byref(opts), C.byref(nbytes)) == 0
+    assert nbytes.value > 64 * 64 * 8 * 3
+    opts.relax_mode = 7
+    assert lib.mlgpu_vc_solver_workspace(C.byref(op), C.byref(opts), C.byref(nbytes)) == abi.ERR_ARG
