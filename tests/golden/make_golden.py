@@ -1,0 +1,50 @@
+"""Generates tests/golden/closure_plt000100.npz from the reference's own data.
+
+Source: test/unit/data/plt000100.2d.hdf5 of the mushy-layer project, a
+3-level AMR plotfile written by the reference (AMRLevelMushyLayer plot
+output; components 0-4 are Enthalpy, Bulk concentration, Temperature,
+Porosity, Liquid concentration, the last three produced by
+updateEnthalpyVariables, src/phaseDiagram.cpp:92-177).  The phase-diagram
+parameters are the file's root attributes (C = compositionRatio,
+S = stefan, cp = specificHeatRatio, pc = waterDistributionCoeff).
+
+The reference tree is only present where the fixture is generated; the GPU
+box and the tests read the committed .npz.  Run:
+    python tests/golden/make_golden.py /path/to/mushy-layer
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(HERE, "..", "..", "mushy-layer_gb300"))
+from mushy_gb300 import chombo_hdf5  # noqa: E402
+
+
+def main(ref_root):
+    path = os.path.join(ref_root, "test", "unit", "data", "plt000100.2d.hdf5")
+    pf = chombo_hdf5.read_plotfile(path)
+    a = pf["attrs"]
+    assert pf["components"][:5] == ["Enthalpy", "Bulk concentration", "Temperature",
+                                    "Porosity", "Liquid concentration"]
+    cols = [[] for _ in range(5)]
+    level = []
+    for lev_i, lev in enumerate(pf["levels"]):
+        for b in lev["boxes"]:
+            for c in range(5):
+                cols[c].append(b["data"][c].ravel())
+            level.append(np.full(b["data"][0].size, lev_i, dtype=np.int8))
+    H, C, T, chi, Cl = [np.concatenate(x) for x in cols]
+    out = os.path.join(HERE, "closure_plt000100.npz")
+    np.savez_compressed(
+        out, H=H, C=C, T=T, porosity=chi, Cl=Cl, level=np.concatenate(level),
+        compositionRatio=float(a["C"]), stefan=float(a["S"]),
+        specificHeatRatio=float(a["cp"]), waterDistributionCoeff=float(a["pc"]),
+        max_enthalpy_level0=max(b["data"][0].max() for b in pf["levels"][0]["boxes"]),
+        max_enthalpy_level2=max(b["data"][0].max() for b in pf["levels"][2]["boxes"]))
+    print("wrote", out, H.size, "cells")
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
