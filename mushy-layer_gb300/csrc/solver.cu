@@ -21,8 +21,34 @@
 
 using namespace mlgpu;
 
+// A solver runs on its own non-blocking stream (graph capture is not allowed
+// on the legacy default stream a caller may pass); it is ordered after the
+// caller's stream on entry and the caller's stream waits for it on exit.
 struct mlgpu_solver {
-  virtual ~mlgpu_solver() {}
+  cudaStream_t user = nullptr, s = nullptr;
+  cudaEvent_t ev_in = nullptr, ev_out = nullptr;
+  virtual ~mlgpu_solver() {
+    if (ev_in) cudaEventDestroy(ev_in);
+    if (ev_out) cudaEventDestroy(ev_out);
+    if (s) cudaStreamDestroy(s);
+  }
+  int init_streams(cudaStream_t caller) {
+    user = caller;
+    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return MLGPU_ERR_CUDA;
+    if (cudaEventCreateWithFlags(&ev_in, cudaEventDisableTiming) != cudaSuccess) return MLGPU_ERR_CUDA;
+    if (cudaEventCreateWithFlags(&ev_out, cudaEventDisableTiming) != cudaSuccess) return MLGPU_ERR_CUDA;
+    return MLGPU_OK;
+  }
+  int enter() {
+    if (cudaEventRecord(ev_in, user) != cudaSuccess) return MLGPU_ERR_CUDA;
+    if (cudaStreamWaitEvent(s, ev_in, 0) != cudaSuccess) return MLGPU_ERR_CUDA;
+    return MLGPU_OK;
+  }
+  int leave() {
+    if (cudaEventRecord(ev_out, s) != cudaSuccess) return MLGPU_ERR_CUDA;
+    if (cudaStreamWaitEvent(user, ev_out, 0) != cudaSuccess) return MLGPU_ERR_CUDA;
+    return MLGPU_OK;
+  }
   virtual int solve(double *phi, const double *rhs, mlgpu_solve_stats *st) = 0;
   virtual int set_alpha_beta(double a, double b) = 0;
 };
@@ -142,7 +168,6 @@ class VCSolver : public mlgpu_solver {
   double *phi[2] = {nullptr, nullptr};
   double *rhs = nullptr, *part = nullptr;
   double *host_norm = nullptr;
-  cudaStream_t s = nullptr;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
   bool mixed = false;
   double updates_per_iter = 0;
@@ -344,6 +369,8 @@ class VCSolver : public mlgpu_solver {
   int solve(double *user_phi, const double *user_rhs, mlgpu_solve_stats *st) override {
     if (!user_phi || !user_rhs || !st) return MLGPU_ERR_ARG;
     size_t bytes = sizeof(double) * L[0].G.ncell;
+    cudaGetLastError();  // clear any stale error of an earlier call
+    if (enter()) return MLGPU_ERR_CUDA;
     CK(cudaMemcpyAsync(phi[0], user_phi, bytes, cudaMemcpyDeviceToDevice, s));
     CK(cudaMemcpyAsync(rhs, user_rhs, bytes, cudaMemcpyDeviceToDevice, s));
     // initial residual (no update)
@@ -378,6 +405,7 @@ class VCSolver : public mlgpu_solver {
     }
     CK(cudaMemcpyAsync(user_phi, phi[cur], bytes, cudaMemcpyDeviceToDevice, s));
     CK(cudaStreamSynchronize(s));
+    if (leave()) return MLGPU_ERR_CUDA;
     return outer_finish(o, S, st);
   }
 
@@ -407,7 +435,6 @@ class HCSolver : public mlgpu_solver {
   mlgpu_mg_options o;
   std::vector<HCLevel> L;
   double *part = nullptr, *host_norm = nullptr;
-  cudaStream_t s = nullptr;
   cudaGraphExec_t graph = nullptr;
   double updates_per_iter = 0;
 
@@ -547,6 +574,8 @@ class HCSolver : public mlgpu_solver {
   int solve(double *user_phi, const double *user_rhs, mlgpu_solve_stats *st) override {
     if (!user_phi || !user_rhs || !st) return MLGPU_ERR_ARG;
     size_t bytes = sizeof(double) * 2 * L[0].G.ncell;
+    cudaGetLastError();  // clear any stale error of an earlier call
+    if (enter()) return MLGPU_ERR_CUDA;
     CK(cudaMemcpyAsync(L[0].u, user_phi, bytes, cudaMemcpyDeviceToDevice, s));
     CK(cudaMemcpyAsync(L[0].f, user_rhs, bytes, cudaMemcpyDeviceToDevice, s));
     int rc = residual_norm();
@@ -568,6 +597,7 @@ class HCSolver : public mlgpu_solver {
     }
     CK(cudaMemcpyAsync(user_phi, L[0].u, bytes, cudaMemcpyDeviceToDevice, s));
     CK(cudaStreamSynchronize(s));
+    if (leave()) return MLGPU_ERR_CUDA;
     return outer_finish(o, S, st);
   }
 
@@ -642,7 +672,11 @@ int mlgpu_vc_solver_create(const mlgpu_vcop *op, const mlgpu_mg_options *o, void
   S->op = *op;
   S->o = *o;
   S->mixed = o->precision == MLGPU_PREC_MIXED;
-  S->s = (cudaStream_t)stream;
+  cudaGetLastError();
+  if (S->init_streams((cudaStream_t)stream)) {
+    delete S;
+    return MLGPU_ERR_CUDA;
+  }
   size_t need = S->layout(nullptr);
   if (bytes < need) {
     delete S;
@@ -653,7 +687,9 @@ int mlgpu_vc_solver_create(const mlgpu_vcop *op, const mlgpu_mg_options *o, void
     delete S;
     return MLGPU_ERR_CUDA;
   }
-  int rc = S->build_coefs();
+  int rc = S->enter();
+  if (!rc) rc = S->build_coefs();
+  if (!rc) rc = S->leave();
   if (rc) {
     delete S;
     return rc;
@@ -682,7 +718,11 @@ int mlgpu_hc_solver_create(const mlgpu_nlop *op, const mlgpu_mg_options *o, void
   HCSolver *S = new HCSolver;
   S->op = *op;
   S->o = *o;
-  S->s = (cudaStream_t)stream;
+  cudaGetLastError();
+  if (S->init_streams((cudaStream_t)stream)) {
+    delete S;
+    return MLGPU_ERR_CUDA;
+  }
   size_t need = S->layout(nullptr);
   if (bytes < need) {
     delete S;
@@ -693,7 +733,9 @@ int mlgpu_hc_solver_create(const mlgpu_nlop *op, const mlgpu_mg_options *o, void
     delete S;
     return MLGPU_ERR_CUDA;
   }
-  int rc = S->build_coefs();
+  int rc = S->enter();
+  if (!rc) rc = S->build_coefs();
+  if (!rc) rc = S->leave();
   if (rc) {
     delete S;
     return rc;
