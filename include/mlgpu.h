@@ -304,6 +304,28 @@ int mlgpu_solver_solve(mlgpu_solver *s, double *phi, const double *rhs,
 int mlgpu_solver_set_alpha_beta(mlgpu_solver *s, double alpha, double beta);
 int mlgpu_solver_destroy(mlgpu_solver *s);
 
+/* MAC projection of a face velocity, the sequence of
+ * Projector::levelMacProject (srcSubcycle/Projector.cpp:858-982):
+ * rhs = div u (DIVERGENCE, util/DivergenceF.ChF), solve div(Pi grad phi) = rhs
+ * with `S` (a projection solver built with bCoef = -Pi_face, alpha = 0,
+ * beta = 1), then u_d -= Pi_d (phi[i] - phi[i-e_d]) / dx on every face
+ * (levelGradientMAC + the correction loop), ghosts of phi from `phi_bc`.
+ * phi: initial guess in, pressure correction out.  `scratch`: one cell field.
+ * pi_face may be NULL (unit scaling).  Runs on the solver's stream. */
+int mlgpu_mac_project(mlgpu_solver *S, const mlgpu_grid *grid, const mlgpu_bc *phi_bc,
+                      double *u[3], const double *pi_face[3], double *phi, double *scratch,
+                      mlgpu_solve_stats *stats);
+
+/* One backward-Euler step of the enthalpy/bulk-concentration equations, as
+ * LevelBackwardEuler::updateSoln drives the FAS solve
+ * (srcSubcycle/AMRLevelMushyLayer.cpp:1766-1779): rhs = phi_old * a + dt src
+ * (aCoef NULL: a == 1; src NULL: no source), alpha = 1, beta = -dt, then the
+ * solve of `S` (an HC solver) for phi_new, whose content is the initial guess.
+ * `rhs_scratch` has the size of phi. */
+int mlgpu_hc_backward_euler(mlgpu_solver *S, double *phi_new, const double *phi_old,
+                            const double *src, const double *aCoef, double dt,
+                            double *rhs_scratch, mlgpu_solve_stats *stats);
+
 #ifdef __cplusplus
 }
 #endif

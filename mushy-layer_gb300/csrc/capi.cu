@@ -50,6 +50,7 @@ VCArgs<T> make_vc_args(const mlgpu_vcop &op) {
   A.a = (const T *)op.aCoef;
   A.c = (const T *)op.cCoef;
   for (int d = 0; d < 3; d++) A.b[d] = (const T *)op.bCoef[d];
+  A.lam = nullptr;
   return A;
 }
 template VCArgs<double> make_vc_args<double>(const mlgpu_vcop &);

@@ -4,6 +4,7 @@
 #include "launch.h"
 #include "nl_kernels.cuh"
 #include "vc_kernels.cuh"
+#include "cycle_kernels.cuh"
 
 namespace mlgpu {
 
@@ -24,5 +25,7 @@ cudaError_t launch_mac_div(const Geom &G, const double *u0, const double *u1, co
                            double *div, cudaStream_t s);
 cudaError_t launch_mac_correct(const Geom &G, const BCD &bc, int d, const double *phi,
                                const double *scale, double *u, cudaStream_t s);
+cudaError_t launch_be_rhs(long long n, const double *phi_old, const double *a, const double *src,
+                          double dt, double *rhs, cudaStream_t s);
 
 }  // namespace mlgpu

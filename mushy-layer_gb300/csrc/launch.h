@@ -57,6 +57,11 @@ cudaError_t launch_vc_restrict(const VCArgs<T> &A, const Geom &C, const T *phi, 
                                T *res_c, T *zero_c, cudaStream_t s);
 template <class T>
 cudaError_t launch_vc_lambda(const VCArgs<T> &A, T *lam, cudaStream_t s);
+template <class T> struct VCBlockCycle;
+template <class T>
+cudaError_t launch_vc_block_cycle(const VCBlockCycle<T> &P, cudaStream_t s);
+// levels at or below this many cells run inside one thread block
+constexpr long long kBlockCycleCells = 4096;
 
 template <class T>
 cudaError_t launch_restrict_avg(const Geom &F, int ncomp, const T *fine, T *coarse, cudaStream_t s);

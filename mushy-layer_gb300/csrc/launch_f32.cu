@@ -40,3 +40,7 @@ template cudaError_t launch_convert<float, double>(long long, float *, const dou
 template cudaError_t launch_convert<float, float>(long long, float *, const float *, cudaStream_t);
 
 }  // namespace mlgpu
+
+namespace mlgpu {
+template cudaError_t launch_vc_block_cycle<float>(const VCBlockCycle<float> &, cudaStream_t);
+}

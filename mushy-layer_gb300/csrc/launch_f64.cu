@@ -96,5 +96,14 @@ cudaError_t launch_mac_correct(const Geom &G, const BCD &bc, int d, const double
   mac_correct_kernel<<<blocks_for(G.nface(d)), kBlock, 0, s>>>(G, bc, d, phi, scale, u);
   return cudaGetLastError();
 }
+cudaError_t launch_be_rhs(long long n, const double *phi_old, const double *a, const double *src,
+                          double dt, double *rhs, cudaStream_t s) {
+  be_rhs_kernel<<<blocks_for(n), kBlock, 0, s>>>(n, phi_old, a, src, dt, rhs);
+  return cudaGetLastError();
+}
 
 }  // namespace mlgpu
+
+namespace mlgpu {
+template cudaError_t launch_vc_block_cycle<double>(const VCBlockCycle<double> &, cudaStream_t);
+}

@@ -5,6 +5,7 @@
 #include "nl_kernels.cuh"
 #include "vc_kernels.cuh"
 #include "misc_kernels.cuh"
+#include "cycle_kernels.cuh"
 
 namespace mlgpu {
 
@@ -168,6 +169,16 @@ template <class T>
 cudaError_t launch_vc_lambda(const VCArgs<T> &A, T *lam, cudaStream_t s) {
   int nb = blocks_for(A.G.ncell);
   MLGPU_DIM_SWITCH(A.G.dim, (vc_lambda_kernel<T, DIM><<<nb, kBlock, 0, s>>>(A, lam)));
+  return cudaGetLastError();
+}
+
+template <class T>
+cudaError_t launch_vc_block_cycle(const VCBlockCycle<T> &P, cudaStream_t s) {
+  long long nt = colour_threads(P.A[0].G);
+  int threads = (int)((nt + 31) / 32 * 32);
+  if (threads > 1024) threads = 1024;
+  if (threads < 64) threads = 64;
+  MLGPU_DIM_SWITCH(P.A[0].G.dim, (vc_block_cycle_kernel<T, DIM><<<1, threads, 0, s>>>(P)));
   return cudaGetLastError();
 }
 

@@ -65,43 +65,50 @@ __device__ __forceinline__ T coarse_at(const Geom &C, const BCD &bc, int comp,
 // FORT_PROLONG), KIND 1 the linear stencil of PROLONG_JP
 // (src/AMRProjectionOpF.ChF:15-78).  The FAS correction u_c - u_c,old is
 // formed on the fly from its two operands.
+// One fine value t (component-major index) of the prolongation.
+template <class T, int DIM, int KIND>
+__device__ __forceinline__ void prolong_one(const Geom &F, const Geom &C, const BCD &bc,
+                                            long long t, T *__restrict__ fine,
+                                            const T *__restrict__ a, const T *__restrict__ b) {
+  const T den = T(1) / (DIM == 3 ? T(64) : T(16));
+  const T fx1 = T(3) * den, fx2 = T(9) * den, fx3 = T(27) * den, f0 = T(1) * den;
+  int c = (int)(t / F.ncell);
+  long long q = t % F.ncell;
+  int i, j, k;
+  cell_ijk(F, q, i, j, k);
+  int ic = i / 2, jc = j / 2, kc = DIM == 3 ? k / 2 : 0;
+  T p = fine[t];
+  if (KIND == MLGPU_PROLONG_CONSTANT) {
+    p = p + coarse_at(C, bc, c, a, b, ic, jc, kc);
+  } else {
+    int o1 = 2 * (i % 2) - 1, o2 = 2 * (j % 2) - 1, o3 = DIM == 3 ? 2 * (k % 2) - 1 : 0;
+    if (DIM == 2) {
+      p = p + fx2 * coarse_at(C, bc, c, a, b, ic, jc, kc) +
+          f0 * coarse_at(C, bc, c, a, b, ic + o1, jc + o2, kc);
+      p = p + fx1 * (coarse_at(C, bc, c, a, b, ic + o1, jc, kc) +
+                     coarse_at(C, bc, c, a, b, ic, jc + o2, kc));
+    } else {
+      p = p + fx3 * coarse_at(C, bc, c, a, b, ic, jc, kc) +
+          f0 * coarse_at(C, bc, c, a, b, ic + o1, jc + o2, kc + o3);
+      p = p + fx2 * (coarse_at(C, bc, c, a, b, ic + o1, jc, kc) +
+                     coarse_at(C, bc, c, a, b, ic, jc + o2, kc) +
+                     coarse_at(C, bc, c, a, b, ic, jc, kc + o3));
+      p = p + fx1 * (coarse_at(C, bc, c, a, b, ic + o1, jc + o2, kc) +
+                     coarse_at(C, bc, c, a, b, ic, jc + o2, kc + o3) +
+                     coarse_at(C, bc, c, a, b, ic + o1, jc, kc + o3));
+    }
+  }
+  fine[t] = p;
+}
+
 template <class T, int DIM, int KIND>
 __global__ void __launch_bounds__(kBlock) prolong_kernel(Geom F, Geom C, BCD bc, int ncomp,
                                                          T *__restrict__ fine,
                                                          const T *__restrict__ a,
                                                          const T *__restrict__ b) {
   long long total = F.ncell * ncomp;
-  const T den = T(1) / (DIM == 3 ? T(64) : T(16));
-  const T fx1 = T(3) * den, fx2 = T(9) * den, fx3 = T(27) * den, f0 = T(1) * den;
-  for (long long t = gtid(); t < total; t += gstride()) {
-    int c = (int)(t / F.ncell);
-    long long q = t % F.ncell;
-    int i, j, k;
-    cell_ijk(F, q, i, j, k);
-    int ic = i / 2, jc = j / 2, kc = DIM == 3 ? k / 2 : 0;
-    T p = fine[t];
-    if (KIND == MLGPU_PROLONG_CONSTANT) {
-      p = p + coarse_at(C, bc, c, a, b, ic, jc, kc);
-    } else {
-      int o1 = 2 * (i % 2) - 1, o2 = 2 * (j % 2) - 1, o3 = DIM == 3 ? 2 * (k % 2) - 1 : 0;
-      if (DIM == 2) {
-        p = p + fx2 * coarse_at(C, bc, c, a, b, ic, jc, kc) +
-            f0 * coarse_at(C, bc, c, a, b, ic + o1, jc + o2, kc);
-        p = p + fx1 * (coarse_at(C, bc, c, a, b, ic + o1, jc, kc) +
-                       coarse_at(C, bc, c, a, b, ic, jc + o2, kc));
-      } else {
-        p = p + fx3 * coarse_at(C, bc, c, a, b, ic, jc, kc) +
-            f0 * coarse_at(C, bc, c, a, b, ic + o1, jc + o2, kc + o3);
-        p = p + fx2 * (coarse_at(C, bc, c, a, b, ic + o1, jc, kc) +
-                       coarse_at(C, bc, c, a, b, ic, jc + o2, kc) +
-                       coarse_at(C, bc, c, a, b, ic, jc, kc + o3));
-        p = p + fx1 * (coarse_at(C, bc, c, a, b, ic + o1, jc + o2, kc) +
-                       coarse_at(C, bc, c, a, b, ic, jc + o2, kc + o3) +
-                       coarse_at(C, bc, c, a, b, ic + o1, jc, kc + o3));
-      }
-    }
-    fine[t] = p;
-  }
+  for (long long t = gtid(); t < total; t += gstride())
+    prolong_one<T, DIM, KIND>(F, C, bc, t, fine, a, b);
 }
 
 // ------------------------------------------------------- face coarsening
@@ -261,6 +268,18 @@ __global__ void __launch_bounds__(kBlock) mac_correct_kernel(Geom G, BCD bc, int
     double grad = (ph - pl) / G.dx;
     if (scale) grad = grad * scale[t];
     u[t] = u[t] - grad;
+  }
+}
+// Backward-Euler right-hand side (LevelBackwardEuler::updateSoln):
+// rhs = phi_old * a + dt * src; a == null means a == 1, src == null no source.
+__global__ void __launch_bounds__(kBlock) be_rhs_kernel(long long n, const double *__restrict__ phi_old,
+                                                        const double *__restrict__ a,
+                                                        const double *__restrict__ src, double dt,
+                                                        double *__restrict__ rhs) {
+  for (long long q = gtid(); q < n; q += gstride()) {
+    double v = a ? phi_old[q] * a[q] : phi_old[q];
+    if (src) v = v + dt * src[q];
+    rhs[q] = v;
   }
 }
 #endif  // MLGPU_FP64_UNIT

@@ -158,6 +158,7 @@ struct VCLevel {
   Coefs<double> c64;
   Coefs<float> c32;
   void *e = nullptr, *r = nullptr, *t = nullptr;  // inner precision
+  double *lam64 = nullptr;  // stored 1/diag for FP64 inner cycles
 };
 
 class VCSolver : public mlgpu_solver {
@@ -170,6 +171,7 @@ class VCSolver : public mlgpu_solver {
   double *host_norm = nullptr;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
   bool mixed = false;
+  bool use_block_cycle = true;
   double updates_per_iter = 0;
 
   ~VCSolver() override {
@@ -209,9 +211,13 @@ class VCSolver : public mlgpu_solver {
         L[l].e = A.get<double>(n);
         L[l].r = A.get<double>(n);
         L[l].t = A.get<double>(n);
+        // FP64 has 1/57 of the FP32 rate on GB300: store 1/diag instead of a
+        // division per cell per half sweep (the reference stores it too)
+        L[l].lam64 = A.get<double>(n);
       }
       g = coarsen_grid(g);
     }
+    use_block_cycle = o.relax_mode == MLGPU_RELAX_GSRB && o.num_mg == 1;
     size_t n0 = ncells(op.grid);
     phi[0] = A.get<double>(n0);
     phi[1] = A.get<double>(n0);
@@ -236,6 +242,9 @@ class VCSolver : public mlgpu_solver {
         for (int d = 0; d < lv.G.dim; d++)
           CK(launch_convert<float, double>(lv.G.nface(d), lv.c32.b[d], lv.c64.b[d], s));
       }
+    } else {
+      int rc = build_lambda();
+      if (rc) return rc;
     }
     // cell updates per outer iteration (same accounting as the CPU oracle)
     double u = 0;
@@ -254,6 +263,15 @@ class VCSolver : public mlgpu_solver {
     return MLGPU_OK;
   }
 
+  int build_lambda() {
+    for (size_t l = 0; l < L.size(); l++) {
+      VCArgs<double> A = args<double>((int)l);
+      A.lam = nullptr;
+      CK(launch_vc_lambda<double>(A, L[l].lam64, s));
+    }
+    return MLGPU_OK;
+  }
+
   template <class T>
   VCArgs<T> args(int l) {
     mlgpu_vcop lop = op;
@@ -263,6 +281,7 @@ class VCSolver : public mlgpu_solver {
       A.a = (const T *)L[l].c64.a;
       A.c = (const T *)L[l].c64.c;
       for (int d = 0; d < 3; d++) A.b[d] = (const T *)L[l].c64.b[d];
+      A.lam = (const T *)L[l].lam64;
     } else {
       A.a = (const T *)L[l].c32.a;
       A.c = (const T *)L[l].c32.c;
@@ -304,6 +323,25 @@ class VCSolver : public mlgpu_solver {
   int cycle(int l, bool zero_init) {
     int last = (int)L.size() - 1;
     VCArgs<T> A = args<T>(l);
+    if (use_block_cycle && L[l].G.ncell <= kBlockCycleCells && last - l + 1 <= kMaxBlockLevels &&
+        last > l) {
+      // this level and every coarser one inside one thread block
+      VCBlockCycle<T> P;
+      P.nlev = last - l + 1;
+      P.pre = o.num_smooth_down;
+      P.post = o.num_smooth_up;
+      P.bottom = o.bottom_max_iter;
+      P.prolong = o.prolong;
+      P.zero_init = zero_init ? 1 : 0;
+      P.bc = make_bcd(op.bc);
+      for (int m = 0; m < P.nlev; m++) {
+        P.A[m] = args<T>(l + m);
+        P.e[m] = (T *)L[l + m].e;
+        P.r[m] = (T *)L[l + m].r;
+      }
+      CK(launch_vc_block_cycle<T>(P, s));
+      return MLGPU_OK;
+    }
     if (l == last) {
       if (o.relax_mode == MLGPU_RELAX_JACOBI) return relax<T>(l, o.bottom_max_iter, zero_init);
       CK(launch_vc_relax_block<T>(A, (T *)L[l].e, (const T *)L[l].r, o.bottom_max_iter,
@@ -417,7 +455,11 @@ class VCSolver : public mlgpu_solver {
         cudaGraphExecDestroy(g);
         g = nullptr;
       }
-    return MLGPU_OK;
+    if (mixed) return MLGPU_OK;
+    if (enter()) return MLGPU_ERR_CUDA;
+    int rc = build_lambda();
+    if (!rc) rc = leave();
+    return rc;
   }
 };
 
@@ -752,6 +794,47 @@ int mlgpu_solver_solve(mlgpu_solver *s, double *phi, const double *rhs, mlgpu_so
 int mlgpu_solver_set_alpha_beta(mlgpu_solver *s, double a, double b) {
   if (!s) return MLGPU_ERR_ARG;
   return s->set_alpha_beta(a, b);
+}
+
+int mlgpu_mac_project(mlgpu_solver *S, const mlgpu_grid *grid, const mlgpu_bc *phi_bc,
+                      double *u[3], const double *pi_face[3], double *phi, double *scratch,
+                      mlgpu_solve_stats *stats) {
+  if (!S || !valid_grid(grid) || !phi_bc || !u || !phi || !scratch || !stats)
+    return MLGPU_ERR_ARG;
+  VCSolver *V = dynamic_cast<VCSolver *>(S);
+  if (!V) return MLGPU_ERR_ARG;
+  for (int d = 0; d < 3; d++)
+    if (grid->n[d] != V->op.grid.n[d]) return MLGPU_ERR_ARG;
+  for (int d = 0; d < grid->dim; d++)
+    if (!u[d]) return MLGPU_ERR_ARG;
+  Geom G = make_geom(*grid);
+  cudaGetLastError();
+  if (S->enter()) return MLGPU_ERR_CUDA;
+  CK(launch_mac_div(G, u[0], u[1], grid->dim == 3 ? u[2] : nullptr, scratch, S->s));
+  int rc = S->solve(phi, scratch, stats);
+  if (rc != MLGPU_OK && rc != MLGPU_ERR_NOT_CONVERGED && rc != MLGPU_ERR_HANG) return rc;
+  BCD b = make_bcd(*phi_bc);
+  for (int d = 0; d < grid->dim; d++)
+    CK(launch_mac_correct(G, b, d, phi, pi_face ? pi_face[d] : nullptr, u[d], S->s));
+  if (S->leave()) return MLGPU_ERR_CUDA;
+  return rc;
+}
+
+int mlgpu_hc_backward_euler(mlgpu_solver *S, double *phi_new, const double *phi_old,
+                            const double *src, const double *aCoef, double dt,
+                            double *rhs_scratch, mlgpu_solve_stats *stats) {
+  if (!S || !phi_new || !phi_old || !rhs_scratch || !stats || !(dt > 0)) return MLGPU_ERR_ARG;
+  HCSolver *H = dynamic_cast<HCSolver *>(S);
+  if (!H) return MLGPU_ERR_ARG;
+  long long n = 2 * H->L[0].G.ncell;
+  if (H->op.alpha != 1.0 || H->op.beta != -dt) {
+    int rc = S->set_alpha_beta(1.0, -dt);
+    if (rc) return rc;
+  }
+  cudaGetLastError();
+  if (S->enter()) return MLGPU_ERR_CUDA;
+  CK(launch_be_rhs(n, phi_old, aCoef, src, dt, rhs_scratch, S->s));
+  return S->solve(phi_new, rhs_scratch, stats);
 }
 
 int mlgpu_solver_destroy(mlgpu_solver *s) {

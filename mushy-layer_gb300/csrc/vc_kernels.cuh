@@ -19,7 +19,23 @@ struct VCArgs {
   const T *a;     // [cells] or null (a == 1)
   const T *c;     // [cells] or null (c == 0)
   const T *b[3];  // [faces_d]
+  const T *lam;   // stored 1/diag (resetLambda) or null: computed inline
 };
+
+// 1/diag(L) at cell q in resetLambda order (DarcyBrinkmanOp.cpp:265-296):
+// a*alpha, + (-beta) c, + sum_d scale*beta*(b_hi + b_lo), then 1/x.
+template <class T, int DIM>
+__device__ __forceinline__ T vc_lambda_at(const VCArgs<T> &A, long long q, T bxh, T bxl, T byh,
+                                          T byl, T bzh, T bzl) {
+  if (A.lam) return A.lam[q];
+  T av = A.a ? A.a[q] : T(1);
+  T l = av * A.alpha;
+  if (A.c) l = l + (-A.beta) * A.c[q];
+  l = l + A.dxinv * A.beta * (bxh + bxl);
+  l = l + A.dxinv * A.beta * (byh + byl);
+  if (DIM == 3) l = l + A.dxinv * A.beta * (bzh + bzl);
+  return T(1) / l;
+}
 
 // Reads phi at a cell; the "update" form returns phi + e (FP64 phi, any e)
 // so an outer defect-correction step can apply its correction on the fly.
@@ -82,14 +98,7 @@ __device__ __forceinline__ T vc_lofphi(const VCArgs<T> &A, const R &rd, int i, i
   T v = A.alpha * av * p0;
   if (A.c) v = v - A.beta * A.c[q] * p0;
   v = v - A.beta * s * A.dxinv;
-  if (WANT_LAMBDA) {
-    T l = av * A.alpha;
-    if (A.c) l = l + (-A.beta) * A.c[q];
-    l = l + A.dxinv * A.beta * (bxh + bxl);
-    l = l + A.dxinv * A.beta * (byh + byl);
-    if (DIM == 3) l = l + A.dxinv * A.beta * (bzh + bzl);
-    lam = T(1) / l;
-  }
+  if (WANT_LAMBDA) lam = vc_lambda_at<T, DIM>(A, q, bxh, bxl, byh, byl, bzh, bzl);
   return v;
 }
 
@@ -179,7 +188,29 @@ __global__ void __launch_bounds__(kBlock) vc_gsrb_kernel(VCArgs<T> A, T *phi,
 
 // First red pass from a zero initial guess: e = 0 everywhere, so the red
 // update is lambda * rhs and black cells are written as zero.  Equal to
-// "zero the field, then vc_gsrb_kernel(pass 0)" without the extra pass.
+// "zero the field, then vc_gsrb_kernel(pass 0)" without the extra pass:
+// L(0) with homogeneous BCs is exactly 0 in every term, so
+// phi = 0 - lambda * (0 - rhs) reproduces the general update bit for bit.
+template <class T, int DIM>
+__device__ __forceinline__ void vc_gsrb_zero_cell(const VCArgs<T> &A, T *__restrict__ phi,
+                                                  const T *__restrict__ rhs, long long q, int i,
+                                                  int j, int k) {
+  if (((i + j + k) & 1) == 0) {
+    T z = T(0);
+    T bzh = T(0), bzl = T(0);
+    if (DIM == 3) {
+      bzh = vface(A, 2, i, j, k + 1);
+      bzl = vface(A, 2, i, j, k);
+    }
+    T lam = vc_lambda_at<T, DIM>(A, q, vface(A, 0, i + 1, j, k), vface(A, 0, i, j, k),
+                                 vface(A, 1, i, j + 1, k), vface(A, 1, i, j, k), bzh, bzl);
+    T lof = z;
+    phi[q] = z - lam * (lof - rhs[q]);
+  } else {
+    phi[q] = T(0);
+  }
+}
+
 template <class T, int DIM>
 __global__ void __launch_bounds__(kBlock) vc_gsrb_zero_kernel(VCArgs<T> A, T *__restrict__ phi,
                                                               const T *__restrict__ rhs) {
@@ -187,22 +218,7 @@ __global__ void __launch_bounds__(kBlock) vc_gsrb_zero_kernel(VCArgs<T> A, T *__
   for (long long q = gtid(); q < G.ncell; q += gstride()) {
     int i, j, k;
     cell_ijk(G, q, i, j, k);
-    if (((i + j + k) & 1) == 0) {
-      T z = T(0);
-      // L(0) with homogeneous BC is exactly 0 in every term, so
-      // phi = 0 - lambda * (0 - rhs) reproduces the general update.
-      T av = A.a ? A.a[q] : T(1);
-      T l = av * A.alpha;
-      if (A.c) l = l + (-A.beta) * A.c[q];
-      l = l + A.dxinv * A.beta * (vface(A, 0, i + 1, j, k) + vface(A, 0, i, j, k));
-      l = l + A.dxinv * A.beta * (vface(A, 1, i, j + 1, k) + vface(A, 1, i, j, k));
-      if (DIM == 3) l = l + A.dxinv * A.beta * (vface(A, 2, i, j, k + 1) + vface(A, 2, i, j, k));
-      T lam = T(1) / l;
-      T lof = z;
-      phi[q] = z - lam * (lof - rhs[q]);
-    } else {
-      phi[q] = T(0);
-    }
+    vc_gsrb_zero_cell<T, DIM>(A, phi, rhs, q, i, j, k);
   }
 }
 

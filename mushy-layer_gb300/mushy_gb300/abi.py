@@ -173,6 +173,8 @@ def _declare(lib):
         "mlgpu_solver_solve": (i, [vp, vp, vp, P(SolveStats)]),
         "mlgpu_solver_set_alpha_beta": (i, [vp, d, d]),
         "mlgpu_solver_destroy": (i, [vp]),
+        "mlgpu_mac_project": (i, [vp, P(Grid), P(BC), vp * 3, vp * 3, vp, vp, P(SolveStats)]),
+        "mlgpu_hc_backward_euler": (i, [vp, vp, vp, vp, vp, d, vp, P(SolveStats)]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

@@ -295,11 +295,29 @@ class _Solver:
             self.h = None
 
 
+def _faces3(ts):
+    arr = (C.c_void_p * 3)()
+    for d, t in enumerate(ts):
+        arr[d] = t.data_ptr() if t is not None else None
+    return arr
+
+
 class AMRFASMultiGrid(_Solver):
     """FAS multigrid driving NLMultiCompOp (AMRFASMultiGrid's role)."""
 
     def __init__(self, op, opts=None):
         super().__init__(op, opts or default_options(True), "hc")
+
+    def backwardEuler(self, phi_new, phi_old, dt, src=None, aCoef=None):
+        """LevelBackwardEuler::updateSoln: solve (a - dt L) phi_new = a phi_old + dt src."""
+        scratch = torch.empty_like(phi_old)
+        st = abi.SolveStats()
+        rc = abi.load().mlgpu_hc_backward_euler(self.h, _ptr(phi_new), _ptr(phi_old), _ptr(src),
+                                                _ptr(aCoef), float(dt), _ptr(scratch),
+                                                C.byref(st))
+        if rc not in (abi.OK, abi.ERR_NOT_CONVERGED, abi.ERR_HANG):
+            abi.check(rc, "backwardEuler")
+        return st, rc
 
 
 class AMRMultiGrid(_Solver):
@@ -307,3 +325,18 @@ class AMRMultiGrid(_Solver):
 
     def __init__(self, op, opts=None):
         super().__init__(op, opts or default_options(False), "vc")
+
+    def levelMacProject(self, u, pi_face, phi, phi_bc=None):
+        """Projector::levelMacProject: u <- u - Pi grad(phi), div(Pi grad phi) = div u."""
+        g = self.op.grid
+        scratch = cell_tensor(g, 1, torch.float64)
+        st = abi.SolveStats()
+        bc = phi_bc if phi_bc is not None else self.op.bc
+        rc = abi.load().mlgpu_mac_project(self.h, C.byref(g), C.byref(bc),
+                                          _faces3(list(u) + [None] * (3 - len(u))),
+                                          _faces3(list(pi_face) + [None] * (3 - len(pi_face)))
+                                          if pi_face is not None else None,
+                                          _ptr(phi), _ptr(scratch), C.byref(st))
+        if rc not in (abi.OK, abi.ERR_NOT_CONVERGED, abi.ERR_HANG):
+            abi.check(rc, "levelMacProject")
+        return st, rc

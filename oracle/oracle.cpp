@@ -1078,6 +1078,41 @@ int orc_hc_solve(const mlgpu_nlop *op, const mlgpu_mg_options *o, double *phi,
 }
 
 int orc_vc_solve(const mlgpu_vcop *op, const mlgpu_mg_options *o, double *phi,
+                 const double *rhs, mlgpu_solve_stats *st);
+
+// Projector::levelMacProject (srcSubcycle/Projector.cpp:858-982):
+// div -> solve div(Pi grad phi) = div u -> u -= Pi grad phi
+int orc_mac_project(const mlgpu_vcop *op, const mlgpu_mg_options *o, const mlgpu_bc *phi_bc,
+                    double *u[3], const double *pi[3], double *phi, mlgpu_solve_stats *st) {
+  std::vector<double> rhs(ncells(op->grid));
+  const double *uc[3] = {u[0], u[1], u[2]};
+  orc_mac_divergence(&op->grid, rhs.data(), uc);
+  int rc = orc_vc_solve(op, o, phi, rhs.data(), st);
+  orc_mac_correct(&op->grid, phi_bc, phi, pi, u);
+  return rc;
+}
+
+// LevelBackwardEuler::updateSoln: rhs = phi_old * a + dt * src, alpha = 1,
+// beta = -dt, FAS solve for phi_new
+int orc_hc_solve(const mlgpu_nlop *op, const mlgpu_mg_options *o, double *phi,
+                 const double *rhs, mlgpu_solve_stats *st);
+int orc_hc_backward_euler(const mlgpu_nlop *op, const mlgpu_mg_options *o, double *phi_new,
+                          const double *phi_old, const double *src, const double *a, double dt,
+                          mlgpu_solve_stats *st) {
+  size_t n = 2 * ncells(op->grid);
+  std::vector<double> rhs(n);
+  for (size_t q = 0; q < n; q++) {
+    double v = a ? phi_old[q] * a[q] : phi_old[q];
+    if (src) v = v + dt * src[q];
+    rhs[q] = v;
+  }
+  mlgpu_nlop be = *op;
+  be.alpha = 1.0;
+  be.beta = -dt;
+  return orc_hc_solve(&be, o, phi_new, rhs.data(), st);
+}
+
+int orc_vc_solve(const mlgpu_vcop *op, const mlgpu_mg_options *o, double *phi,
                  const double *rhs, mlgpu_solve_stats *st) {
   VCSolver S;
   S.op0 = *op;

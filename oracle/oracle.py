@@ -54,6 +54,10 @@ def lib():
             "orc_mg_depth": (i, [P(abi.Grid), i]),
             "orc_hc_solve": (i, [P(abi.NLOp), P(abi.MGOptions), vp, vp, P(abi.SolveStats)]),
             "orc_vc_solve": (i, [P(abi.VCOp), P(abi.MGOptions), vp, vp, P(abi.SolveStats)]),
+            "orc_mac_project": (i, [P(abi.VCOp), P(abi.MGOptions), P(abi.BC), vp * 3, vp * 3,
+                                    vp, P(abi.SolveStats)]),
+            "orc_hc_backward_euler": (i, [P(abi.NLOp), P(abi.MGOptions), vp, vp, vp, vp, d,
+                                          P(abi.SolveStats)]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -279,3 +283,21 @@ def vc_solve(o, opts, phi, rhs):
     st = abi.SolveStats()
     rc = lib().orc_vc_solve(C.byref(o.op), C.byref(opts), _p(phi), _p(rhs), C.byref(st))
     return phi, st, rc
+
+
+def mac_project(o, opts, phi_bc, u, pi, phi):
+    u = [x.copy() for x in u]
+    phi = phi.copy()
+    st = abi.SolveStats()
+    rc = lib().orc_mac_project(C.byref(o.op), C.byref(opts), C.byref(phi_bc),
+                               _faces3(u + [None] * (3 - len(u))),
+                               _faces3(list(pi) + [None] * (3 - len(pi))), _p(phi), C.byref(st))
+    return u, phi, st, rc
+
+
+def hc_backward_euler(o, opts, phi_new, phi_old, dt, src=None, a=None):
+    phi_new = phi_new.copy()
+    st = abi.SolveStats()
+    rc = lib().orc_hc_backward_euler(C.byref(o.op), C.byref(opts), _p(phi_new), _p(phi_old),
+                                     _p(src), _p(a), float(dt), C.byref(st))
+    return phi_new, st, rc

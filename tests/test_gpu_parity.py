@@ -379,3 +379,55 @@ def test_hc_solver_fp64_matches_oracle():
         assert rc == rc_ref and st.iterations == st_ref.iterations
         exact(host(d_phi), sol_ref)
         assert st.cell_updates == st_ref.cell_updates
+
+
+# ------------------------------------------------- composed "next" rows
+def test_mac_project_bitwise_and_divergence_free():
+    from mushy_gb300 import ops
+    g, chi, perm, u = P.projection_problem((64, 32), 8, sigma=6.0)
+    pi = O.face_geomean(g, perm)
+    b = [-x for x in pi]
+    bc = abi.make_bc()
+    ref = O.VCOpHost(g, bc, 0.0, 1.0, None, b)
+    opts = O.default_options(0)
+    opts.tolerance, opts.hang, opts.max_iter = 1e-12, 0.0, 400
+    u_ref, phi_ref, st_ref, rc_ref = O.mac_project(ref, opts, bc, u, pi, np.zeros(abi.cell_shape(g)))
+    div0 = np.abs(O.mac_divergence(g, u)).max()
+    assert np.abs(O.mac_divergence(g, u_ref)).max() <= 1e-10 * div0
+    op = ops.ProjectionOp(g, bc, 0.0, 1.0, None, [dev(x) for x in b])
+    o = ops.default_options(False)
+    o.tolerance, o.hang, o.max_iter = 1e-12, 0.0, 400
+    S = ops.AMRMultiGrid(op, o)
+    du = [dev(x) for x in u]
+    d_phi = torch.zeros(abi.cell_shape(g), dtype=torch.float64, device="cuda")
+    st, rc = S.levelMacProject(du, [dev(x) for x in pi], d_phi)
+    assert rc == rc_ref and st.iterations == st_ref.iterations
+    exact(host(d_phi), phi_ref)
+    for d in range(2):
+        exact(host(du[d]), u_ref[d])
+
+
+def test_backward_euler_steps_bitwise():
+    from mushy_gb300 import ops
+    n, dt = 32, 1e-3
+    g = P.grid((n, n))
+    p = P.mushy_params()
+    phi_bc, der = P.hc_bcs("mixed")
+    rng = np.random.default_rng(41)
+    phi = P.hc_state(g, rng, regimes=False)
+    b = [np.stack([-np.ones(abi.face_shape(g, d)), -0.02 * np.ones(abi.face_shape(g, d))])
+         for d in range(2)]
+    src = 0.1 * rng.standard_normal(phi.shape)
+    ref = O.NLOpHost(g, p, phi_bc, der, 1.0, 1.0, None, b)
+    opts = O.default_options(1)
+    op = ops.NLMultiCompOp(g, p, phi_bc, der, 1.0, 1.0, None, [dev(x) for x in b])
+    S = ops.AMRFASMultiGrid(op, ops.default_options(True))
+    h_phi, d_phi = phi.copy(), dev(phi)
+    d_src = dev(src)
+    for step in range(3):
+        new_ref, st_ref, rc_ref = O.hc_backward_euler(ref, opts, h_phi, h_phi, dt, src)
+        d_new = d_phi.clone()
+        st, rc = S.backwardEuler(d_new, d_phi, dt, src=d_src)
+        assert rc == rc_ref and st.iterations == st_ref.iterations
+        exact(host(d_new), new_ref)
+        h_phi, d_phi = new_ref, d_new
