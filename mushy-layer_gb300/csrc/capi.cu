@@ -14,6 +14,12 @@ bool valid_grid(const mlgpu_grid *g) {
     if (g->n[d] < 1) return false;
   if (g->dim == 2 && g->n[2] != 1) return false;
   if (!(g->dx > 0)) return false;
+  // 32-bit index arithmetic in the kernels: two components of the box plus
+  // one face layer must stay below 2^31 entries
+  long long cells = (long long)g->n[0] * g->n[1] * g->n[2];
+  if (2 * (cells + (long long)g->n[0] * g->n[1] + (long long)g->n[1] * g->n[2] +
+           (long long)g->n[0] * g->n[2]) >= (1LL << 31))
+    return false;
   return true;
 }
 

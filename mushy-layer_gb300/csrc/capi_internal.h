@@ -5,6 +5,7 @@
 #include "nl_kernels.cuh"
 #include "vc_kernels.cuh"
 #include "cycle_kernels.cuh"
+#include "tile_kernels.cuh"
 
 namespace mlgpu {
 

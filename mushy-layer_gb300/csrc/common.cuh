@@ -50,7 +50,7 @@ inline Geom make_geom(const mlgpu_grid &g) {
   return G;
 }
 
-inline Geom coarsen_geom(const Geom &f) {
+__host__ __device__ inline Geom coarsen_geom(const Geom &f) {
   Geom c = f;
   c.n0 = f.n0 / 2;
   c.n1 = f.n1 / 2;
@@ -158,11 +158,16 @@ __device__ __forceinline__ long long gtid() {
 }
 __device__ __forceinline__ long long gstride() { return (long long)gridDim.x * blockDim.x; }
 
+// Index decode in 32-bit unsigned arithmetic (a box holds fewer than 2^31
+// cells per component; the library rejects larger boxes): a 64-bit division
+// costs ~4x the instructions and dominated the small stencil kernels.
 __device__ __forceinline__ void cell_ijk(const Geom &G, long long q, int &i, int &j, int &k) {
-  i = (int)(q % G.n0);
-  long long t = q / G.n0;
-  j = (int)(t % G.n1);
-  k = (int)(t / G.n1);
+  unsigned u = (unsigned)q, n0 = (unsigned)G.n0, n1 = (unsigned)G.n1;
+  unsigned t = u / n0;
+  i = (int)(u - t * n0);
+  unsigned kk = t / n1;
+  j = (int)(t - kk * n1);
+  k = (int)kk;
 }
 
 // Active cells of a red (pass 0) / black (pass 1) half sweep.  The
@@ -170,11 +175,13 @@ __device__ __forceinline__ void cell_ijk(const Geom &G, long long q, int &i, int
 // selects cells with (i + j + k) % 2 == pass.
 __device__ __forceinline__ bool colour_cell(const Geom &G, int pass, long long t, int &i, int &j,
                                             int &k) {
-  int half = (G.n0 + 1) / 2;
-  long long row = t / half;
-  int h = (int)(t % half);
-  j = (int)(row % G.n1);
-  k = (int)(row / G.n1);
+  unsigned half = (unsigned)(G.n0 + 1) / 2u, n1 = (unsigned)G.n1;
+  unsigned u = (unsigned)t;
+  unsigned row = u / half;
+  int h = (int)(u - row * half);
+  unsigned kk = row / n1;
+  j = (int)(row - kk * n1);
+  k = (int)kk;
   int imin = (j + k + pass) & 1;
   i = imin + 2 * h;
   return i < G.n0 && k < G.n2;

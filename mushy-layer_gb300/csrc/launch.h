@@ -62,6 +62,11 @@ template <class T>
 cudaError_t launch_vc_block_cycle(const VCBlockCycle<T> &P, cudaStream_t s);
 // levels at or below this many cells run inside one thread block
 constexpr long long kBlockCycleCells = 4096;
+template <class T> struct TileSmooth;
+template <class T>
+cudaError_t launch_vc_tile_smooth(const TileSmooth<T> &P, cudaStream_t s);
+// largest halo a tile launch may use for element size `elem` (shared memory)
+int tile_max_halo(size_t elem);
 
 template <class T>
 cudaError_t launch_restrict_avg(const Geom &F, int ncomp, const T *fine, T *coarse, cudaStream_t s);

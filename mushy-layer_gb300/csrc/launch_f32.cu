@@ -43,4 +43,5 @@ template cudaError_t launch_convert<float, float>(long long, float *, const floa
 
 namespace mlgpu {
 template cudaError_t launch_vc_block_cycle<float>(const VCBlockCycle<float> &, cudaStream_t);
+template cudaError_t launch_vc_tile_smooth<float>(const TileSmooth<float> &, cudaStream_t);
 }

@@ -106,4 +106,11 @@ cudaError_t launch_be_rhs(long long n, const double *phi_old, const double *a, c
 
 namespace mlgpu {
 template cudaError_t launch_vc_block_cycle<double>(const VCBlockCycle<double> &, cudaStream_t);
+template cudaError_t launch_vc_tile_smooth<double>(const TileSmooth<double> &, cudaStream_t);
+
+int tile_max_halo(size_t elem) {
+  int h = 0;
+  while (tile_smem_bytes(h + 1, elem) <= kMaxDynSmem) h++;
+  return h;
+}
 }

@@ -6,8 +6,29 @@
 #include "vc_kernels.cuh"
 #include "misc_kernels.cuh"
 #include "cycle_kernels.cuh"
+#include "tile_kernels.cuh"
 
 namespace mlgpu {
+
+constexpr size_t kMaxDynSmem = 227 * 1024;
+
+template <class T>
+cudaError_t launch_vc_tile_smooth(const TileSmooth<T> &P, cudaStream_t s) {
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(vc_tile_smooth_kernel<T>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)kMaxDynSmem);
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
+  size_t bytes = tile_smem_bytes(P.halo, sizeof(T));
+  if (bytes > kMaxDynSmem) return cudaErrorInvalidValue;
+  const Geom &G = P.A.G;
+  dim3 grid((G.n0 + kTileX - 1) / kTileX, (G.n1 + kTileY - 1) / kTileY);
+  vc_tile_smooth_kernel<T><<<grid, kTileThreads, bytes, s>>>(P);
+  return cudaGetLastError();
+}
 
 #define MLGPU_DIM_SWITCH(dim, ...) \
   do {                              \

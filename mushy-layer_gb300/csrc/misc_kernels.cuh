@@ -65,40 +65,45 @@ __device__ __forceinline__ T coarse_at(const Geom &C, const BCD &bc, int comp,
 // FORT_PROLONG), KIND 1 the linear stencil of PROLONG_JP
 // (src/AMRProjectionOpF.ChF:15-78).  The FAS correction u_c - u_c,old is
 // formed on the fly from its two operands.
+// p + (P (a - b))(i, j, k) for component c: the prolongation increment of one
+// fine cell, arithmetic identical to prolong_one below.
+template <class T, int DIM, int KIND>
+__device__ __forceinline__ T prolong_add(const Geom &C, const BCD &bc, int c, int i, int j, int k,
+                                         T p, const T *__restrict__ a, const T *__restrict__ b) {
+  const T den = T(1) / (DIM == 3 ? T(64) : T(16));
+  const T fx1 = T(3) * den, fx2 = T(9) * den, fx3 = T(27) * den, f0 = T(1) * den;
+  int ic = i >> 1, jc = j >> 1, kc = DIM == 3 ? k >> 1 : 0;
+  if (KIND == MLGPU_PROLONG_CONSTANT) return p + coarse_at(C, bc, c, a, b, ic, jc, kc);
+  int o1 = 2 * (i & 1) - 1, o2 = 2 * (j & 1) - 1, o3 = DIM == 3 ? 2 * (k & 1) - 1 : 0;
+  if (DIM == 2) {
+    p = p + fx2 * coarse_at(C, bc, c, a, b, ic, jc, kc) +
+        f0 * coarse_at(C, bc, c, a, b, ic + o1, jc + o2, kc);
+    p = p + fx1 * (coarse_at(C, bc, c, a, b, ic + o1, jc, kc) +
+                   coarse_at(C, bc, c, a, b, ic, jc + o2, kc));
+  } else {
+    p = p + fx3 * coarse_at(C, bc, c, a, b, ic, jc, kc) +
+        f0 * coarse_at(C, bc, c, a, b, ic + o1, jc + o2, kc + o3);
+    p = p + fx2 * (coarse_at(C, bc, c, a, b, ic + o1, jc, kc) +
+                   coarse_at(C, bc, c, a, b, ic, jc + o2, kc) +
+                   coarse_at(C, bc, c, a, b, ic, jc, kc + o3));
+    p = p + fx1 * (coarse_at(C, bc, c, a, b, ic + o1, jc + o2, kc) +
+                   coarse_at(C, bc, c, a, b, ic, jc + o2, kc + o3) +
+                   coarse_at(C, bc, c, a, b, ic + o1, jc, kc + o3));
+  }
+  return p;
+}
+
 // One fine value t (component-major index) of the prolongation.
 template <class T, int DIM, int KIND>
 __device__ __forceinline__ void prolong_one(const Geom &F, const Geom &C, const BCD &bc,
                                             long long t, T *__restrict__ fine,
                                             const T *__restrict__ a, const T *__restrict__ b) {
-  const T den = T(1) / (DIM == 3 ? T(64) : T(16));
-  const T fx1 = T(3) * den, fx2 = T(9) * den, fx3 = T(27) * den, f0 = T(1) * den;
-  int c = (int)(t / F.ncell);
-  long long q = t % F.ncell;
+  unsigned nc = (unsigned)F.ncell;
+  int c = (int)((unsigned)t / nc);
+  long long q = (unsigned)t - (unsigned)c * nc;
   int i, j, k;
   cell_ijk(F, q, i, j, k);
-  int ic = i / 2, jc = j / 2, kc = DIM == 3 ? k / 2 : 0;
-  T p = fine[t];
-  if (KIND == MLGPU_PROLONG_CONSTANT) {
-    p = p + coarse_at(C, bc, c, a, b, ic, jc, kc);
-  } else {
-    int o1 = 2 * (i % 2) - 1, o2 = 2 * (j % 2) - 1, o3 = DIM == 3 ? 2 * (k % 2) - 1 : 0;
-    if (DIM == 2) {
-      p = p + fx2 * coarse_at(C, bc, c, a, b, ic, jc, kc) +
-          f0 * coarse_at(C, bc, c, a, b, ic + o1, jc + o2, kc);
-      p = p + fx1 * (coarse_at(C, bc, c, a, b, ic + o1, jc, kc) +
-                     coarse_at(C, bc, c, a, b, ic, jc + o2, kc));
-    } else {
-      p = p + fx3 * coarse_at(C, bc, c, a, b, ic, jc, kc) +
-          f0 * coarse_at(C, bc, c, a, b, ic + o1, jc + o2, kc + o3);
-      p = p + fx2 * (coarse_at(C, bc, c, a, b, ic + o1, jc, kc) +
-                     coarse_at(C, bc, c, a, b, ic, jc + o2, kc) +
-                     coarse_at(C, bc, c, a, b, ic, jc, kc + o3));
-      p = p + fx1 * (coarse_at(C, bc, c, a, b, ic + o1, jc + o2, kc) +
-                     coarse_at(C, bc, c, a, b, ic, jc + o2, kc + o3) +
-                     coarse_at(C, bc, c, a, b, ic + o1, jc, kc + o3));
-    }
-  }
-  fine[t] = p;
+  fine[t] = prolong_add<T, DIM, KIND>(C, bc, c, i, j, k, fine[t], a, b);
 }
 
 template <class T, int DIM, int KIND>

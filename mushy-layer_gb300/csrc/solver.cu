@@ -172,6 +172,7 @@ class VCSolver : public mlgpu_solver {
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
   bool mixed = false;
   bool use_block_cycle = true;
+  bool use_tiles = true;
   double updates_per_iter = 0;
 
   ~VCSolver() override {
@@ -218,6 +219,7 @@ class VCSolver : public mlgpu_solver {
       g = coarsen_grid(g);
     }
     use_block_cycle = o.relax_mode == MLGPU_RELAX_GSRB && o.num_mg == 1;
+    use_tiles = use_block_cycle;
     size_t n0 = ncells(op.grid);
     phi[0] = A.get<double>(n0);
     phi[1] = A.get<double>(n0);
@@ -319,10 +321,46 @@ class VCSolver : public mlgpu_solver {
     return MLGPU_OK;
   }
 
+  // nh red/black half sweeps on level l in shared-memory tiles (2D), with an
+  // optional zero start, prolongation before and residual restriction after;
+  // split into several launches when the halo would not fit in shared memory
+  template <class T>
+  int tile_sweeps(int l, int nh, bool zero, bool with_restrict, bool with_prolong) {
+    const int hmax = tile_max_halo(sizeof(T));
+    int done = 0;
+    bool first = true;
+    do {
+      int chunk = std::min(nh - done, hmax - 1);
+      bool is_last = done + chunk == nh;
+      TileSmooth<T> P;
+      P.A = args<T>(l);
+      P.e = (T *)L[l].e;
+      P.r = (const T *)L[l].r;
+      P.zero_init = (first && zero) ? 1 : 0;
+      P.n_half = chunk;
+      P.pass0 = done & 1;
+      P.rc = (is_last && with_restrict) ? (T *)L[l + 1].r : nullptr;
+      P.halo = chunk + (P.rc ? 1 : 0);
+      P.prolong = (first && with_prolong) ? o.prolong : -1;
+      P.ec = with_prolong ? (const T *)L[l + 1].e : nullptr;
+      CK(launch_vc_tile_smooth<T>(P, s));
+      first = false;
+      done += chunk;
+    } while (done < nh);
+    return MLGPU_OK;
+  }
+
   template <class T>
   int cycle(int l, bool zero_init) {
     int last = (int)L.size() - 1;
     VCArgs<T> A = args<T>(l);
+    if (use_tiles && l < last && L[l].G.dim == 2 && L[l].G.ncell > kBlockCycleCells) {
+      int rc = tile_sweeps<T>(l, 2 * o.num_smooth_down, zero_init, true, false);
+      if (rc) return rc;
+      rc = cycle<T>(l + 1, true);
+      if (rc) return rc;
+      return tile_sweeps<T>(l, 2 * o.num_smooth_up, false, false, true);
+    }
     if (use_block_cycle && L[l].G.ncell <= kBlockCycleCells && last - l + 1 <= kMaxBlockLevels &&
         last > l) {
       // this level and every coarser one inside one thread block

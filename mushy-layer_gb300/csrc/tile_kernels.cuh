@@ -1,0 +1,194 @@
+// tile_kernels.cuh -- temporal blocking of the red/black smoother on 2D
+// levels.  One launch performs, for a TX x TY tile of the level:
+//   [zero-init | load e] -> [e += P e_coarse] -> n red/black half sweeps ->
+//   [residual restricted to the coarse level]
+// with the tile and a halo of H >= n (+1 with the restriction) cells held in
+// shared memory.  After half sweep h only cells at least h+1 cells inside the
+// loaded halo are valid, so the tile interior ends exact.  Halo cells are
+// recomputed by every tile that loads them with the same operands, hence
+// with the same bits: results equal the per-level kernels launched one
+// after another (relax, restrictResidual, prolongIncrement, relax).
+#pragma once
+#include "vc_kernels.cuh"
+#include "misc_kernels.cuh"
+
+namespace mlgpu {
+
+template <class T>
+struct TileSmooth {
+  VCArgs<T> A;        // level operator; A.lam null: 1/diag computed at load
+  T *e;               // level correction (in/out)
+  const T *r;         // level right-hand side
+  int zero_init;      // e starts at zero instead of being loaded
+  int n_half;         // red/black half sweeps
+  int pass0;          // colour of the first half sweep (0 red, 1 black)
+  int halo;           // loaded halo width H
+  T *rc;              // restricted residual output (coarse level) or null
+  int prolong;        // -1: none, else MLGPU_PROLONG_* from ec
+  const T *ec;        // coarse correction for the prolongation
+};
+
+constexpr int kTileX = 64, kTileY = 32, kTileThreads = 512;
+
+inline size_t tile_smem_bytes(int halo, size_t elem) {
+  size_t lx = kTileX + 2 * halo, ly = kTileY + 2 * halo;
+  return elem * (3 * lx * ly + (lx + 1) * ly + lx * (ly + 1));
+}
+
+template <class T>
+__global__ void __launch_bounds__(kTileThreads) vc_tile_smooth_kernel(TileSmooth<T> P) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const VCArgs<T> &A = P.A;
+  const Geom &G = A.G;
+  const int H = P.halo;
+  const int LX = kTileX + 2 * H, LY = kTileY + 2 * H;
+  T *se = (T *)smem_raw;
+  T *sr = se + LX * LY;
+  T *sl = sr + LX * LY;
+  T *sbx = sl + LX * LY;           // (LX+1) x LY, face lx between local cells lx-1, lx
+  T *sby = sbx + (LX + 1) * LY;    // LX x (LY+1)
+  const int x0 = blockIdx.x * kTileX, y0 = blockIdx.y * kTileY;
+  const int gx0 = x0 - H, gy0 = y0 - H;
+  const int n0 = G.n0, n1 = G.n1;
+  const bool px = G.per0 != 0, py = G.per1 != 0;
+  const int tid = threadIdx.x, nth = blockDim.x;
+
+  // wrapped global coordinate, or -1 when outside a non-periodic domain
+  auto gxw = [&](int gx) -> int {
+    if (gx >= 0 && gx < n0) return gx;
+    if (!px) return -1;
+    return ((gx % n0) + n0) % n0;
+  };
+  auto gyw = [&](int gy) -> int {
+    if (gy >= 0 && gy < n1) return gy;
+    if (!py) return -1;
+    return ((gy % n1) + n1) % n1;
+  };
+
+  // ---- load faces, then cells (e, r, 1/diag)
+  for (int q = tid; q < (LX + 1) * LY; q += nth) {
+    int ly = q / (LX + 1), lx = q - ly * (LX + 1);
+    int gx = gx0 + lx, gy = gyw(gy0 + ly);
+    T v = T(0);
+    if (gy >= 0) {
+      int fx = gx;
+      if (fx < 0 || fx > n0) fx = px ? ((fx % n0) + n0) % n0 : -1;
+      if (fx >= 0) v = A.b[0][(long long)gy * (n0 + 1) + fx];
+    }
+    sbx[q] = v;
+  }
+  for (int q = tid; q < LX * (LY + 1); q += nth) {
+    int ly = q / LX, lx = q - ly * LX;
+    int gx = gxw(gx0 + lx), gy = gy0 + ly;
+    T v = T(0);
+    if (gx >= 0) {
+      int fy = gy;
+      if (fy < 0 || fy > n1) fy = py ? ((fy % n1) + n1) % n1 : -1;
+      if (fy >= 0) v = A.b[1][(long long)fy * n0 + gx];
+    }
+    sby[q] = v;
+  }
+  __syncthreads();
+  for (int q = tid; q < LX * LY; q += nth) {
+    int ly = q / LX, lx = q - ly * LX;
+    int gx = gxw(gx0 + lx), gy = gyw(gy0 + ly);
+    T ev = T(0), rv = T(0), lv = T(0);
+    if (gx >= 0 && gy >= 0) {
+      long long gq = (long long)gy * n0 + gx;
+      if (!P.zero_init) ev = P.e[gq];
+      rv = P.r[gq];
+      if (A.lam) {
+        lv = A.lam[gq];
+      } else {
+        lv = vc_lambda_at<T, 2>(A, gq, sbx[ly * (LX + 1) + lx + 1], sbx[ly * (LX + 1) + lx],
+                                sby[(ly + 1) * LX + lx], sby[ly * LX + lx], T(0), T(0));
+      }
+      if (P.prolong >= 0) {
+        Geom Cg = coarsen_geom(G);
+        if (P.prolong == MLGPU_PROLONG_LINEAR)
+          ev = prolong_add<T, 2, MLGPU_PROLONG_LINEAR>(Cg, A.bc, 0, gx, gy, 0, ev, P.ec, nullptr);
+        else
+          ev = prolong_add<T, 2, MLGPU_PROLONG_CONSTANT>(Cg, A.bc, 0, gx, gy, 0, ev, P.ec, nullptr);
+      }
+    }
+    se[q] = ev;
+    sr[q] = rv;
+    sl[q] = lv;
+  }
+  __syncthreads();
+
+  // L(e) at local (lx, ly), global (gx, gy) (both valid), homogeneous BCs;
+  // same operation order as vc_lofphi
+  auto lofphi = [&](int lx, int ly, int gx, int gy, T &p0) -> T {
+    int c = ly * LX + lx;
+    p0 = se[c];
+    T lo0 = (gx0 + lx - 1 < 0 && !px) ? ghost_value<T>(A.bc, 0, 0, 0, p0, A.dx, true) : se[c - 1];
+    T hi0 = (gx0 + lx + 1 >= n0 && !px) ? ghost_value<T>(A.bc, 0, 1, 0, p0, A.dx, true) : se[c + 1];
+    T lo1 = (gy0 + ly - 1 < 0 && !py) ? ghost_value<T>(A.bc, 1, 0, 0, p0, A.dx, true) : se[c - LX];
+    T hi1 = (gy0 + ly + 1 >= n1 && !py) ? ghost_value<T>(A.bc, 1, 1, 0, p0, A.dx, true) : se[c + LX];
+    T bxh = sbx[ly * (LX + 1) + lx + 1], bxl = sbx[ly * (LX + 1) + lx];
+    T byh = sby[(ly + 1) * LX + lx], byl = sby[ly * LX + lx];
+    T s = bxh * (hi0 - p0) - bxl * (p0 - lo0);
+    s = s + byh * (hi1 - p0);
+    s = s - byl * (p0 - lo1);
+    long long gq = (long long)gy * n0 + gx;
+    T av = A.a ? A.a[gq] : T(1);
+    T v = A.alpha * av * p0;
+    if (A.c) v = v - A.beta * A.c[gq] * p0;
+    v = v - A.beta * s * A.dxinv;
+    return v;
+  };
+
+  // ---- red/black half sweeps over the shrinking valid region
+  for (int h = 0; h < P.n_half; h++) {
+    const int pass = (P.pass0 + h) & 1;
+    const int lo = h + 1, hx = LX - 2 - h, hy = LY - 2 - h;
+    const int w = hx - lo + 1, hgt = hy - lo + 1;
+    const int halfw = (w + 1) >> 1;
+    for (int t = tid; t < halfw * hgt; t += nth) {
+      int row = t / halfw, hh = t - row * halfw;
+      int ly = lo + row;
+      int gy = gy0 + ly;
+      // first local x in [lo, hx] whose global parity matches the pass
+      int lx = lo + (((gx0 + lo + gy + pass) & 1) ? 1 : 0) + 2 * hh;
+      if (lx > hx) continue;
+      int gxv = gxw(gx0 + lx), gyv = gyw(gy);
+      if (gxv < 0 || gyv < 0) continue;
+      T p0;
+      T lof = lofphi(lx, ly, gxv, gyv, p0);
+      int c = ly * LX + lx;
+      se[c] = p0 - sl[c] * (lof - sr[c]);
+    }
+    __syncthreads();
+  }
+
+  // ---- write the interior back
+  for (int q = tid; q < kTileX * kTileY; q += nth) {
+    int iy = q / kTileX, ix = q - iy * kTileX;
+    int gx = x0 + ix, gy = y0 + iy;
+    if (gx < n0 && gy < n1) P.e[(long long)gy * n0 + gx] = se[(iy + H) * LX + ix + H];
+  }
+
+  // ---- residual of the interior, restricted to the coarse level
+  if (P.rc) {
+    const T denom = T(4);
+    const int cn0 = n0 >> 1, cn1 = n1 >> 1;
+    for (int q = tid; q < (kTileX / 2) * (kTileY / 2); q += nth) {
+      int J = q / (kTileX / 2), I = q - J * (kTileX / 2);
+      int CI = (x0 >> 1) + I, CJ = (y0 >> 1) + J;
+      if (CI >= cn0 || CJ >= cn1) continue;
+      T acc = T(0);
+      for (int jj = 0; jj < 2; jj++)
+        for (int ii = 0; ii < 2; ii++) {
+          int gx = 2 * CI + ii, gy = 2 * CJ + jj;
+          int lx = gx - gx0, ly = gy - gy0;
+          T p0;
+          T lof = lofphi(lx, ly, gx, gy, p0);
+          acc = acc + (sr[ly * LX + lx] - lof) / denom;
+        }
+      P.rc[(long long)CJ * cn0 + CI] = acc;
+    }
+  }
+}
+
+}  // namespace mlgpu

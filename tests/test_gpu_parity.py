@@ -325,6 +325,53 @@ def test_vc_solver_fp64_matches_oracle():
         assert st.cell_updates == st_ref.cell_updates
 
 
+@pytest.mark.parametrize("n,per,with_c,bckind,pre,post", [
+    ((256, 128), (1, 0, 0), False, "neumann", 2, 4),
+    ((192, 128), (0, 0, 0), True, "mixed", 1, 3),
+    ((128, 256), (0, 1, 0), False, "mixed", 2, 8),
+    ((256, 96), (1, 1, 0), True, "neumann", 3, 2),
+])
+def test_vc_solver_tiled_levels_bitwise(n, per, with_c, bckind, pre, post):
+    """Levels above 4096 cells run the shared-memory tile smoother (temporal
+    blocking of pre-smoothing + restriction and prolongation +
+    post-smoothing); the result must equal the per-level oracle bit for bit."""
+    from mushy_gb300 import ops
+    rng = np.random.default_rng(50)
+    g = P.grid(n, per)
+    bc = P.vc_bc(bckind)
+    b = [-rng.uniform(0.2, 3.0, abi.face_shape(g, d)) for d in range(2)]
+    aC = rng.uniform(0.5, 1.5, abi.cell_shape(g)) if with_c else None
+    cC = rng.uniform(0.1, 2.0, abi.cell_shape(g)) if with_c else None
+    alpha, beta = (1.0, -0.5) if with_c else (0.0, 1.0)
+    f = rng.standard_normal(abi.cell_shape(g))
+    if not with_c and bckind == "neumann":
+        f -= f.mean()
+    ref = O.VCOpHost(g, bc, alpha, beta, aC, b, cC)
+    opts = O.default_options(0)
+    opts.tolerance, opts.hang, opts.max_iter = 1e-30, 0.0, 5
+    opts.num_smooth_down, opts.num_smooth_up = pre, post
+    sol_ref, st_ref, rc_ref = O.vc_solve(ref, opts, np.zeros_like(f), f)
+    cls = ops.DarcyBrinkmanOp if with_c else ops.ProjectionOp
+    op = cls(g, bc, alpha, beta, None if aC is None else dev(aC), [dev(x) for x in b],
+             None if cC is None else dev(cC))
+    o = ops.default_options(False)
+    o.tolerance, o.hang, o.max_iter = 1e-30, 0.0, 5
+    o.num_smooth_down, o.num_smooth_up = pre, post
+    S = ops.AMRMultiGrid(op, o)
+    d_phi = torch.zeros_like(dev(f))
+    st, rc = S.solve(d_phi, dev(f))
+    assert st.iterations == st_ref.iterations == 5
+    exact(host(d_phi), sol_ref)
+    assert [st.norm_history[i] for i in range(6)] == [st_ref.norm_history[i] for i in range(6)]
+    # mixed precision on the same tiled path converges like the FP64 one
+    om = ops.default_options(False)
+    om.tolerance, om.hang, om.max_iter, om.precision = 1e-30, 0.0, 5, abi.PREC_MIXED
+    om.num_smooth_down, om.num_smooth_up = pre, post
+    pm = torch.zeros_like(dev(f))
+    stm, rcm = ops.AMRMultiGrid(op, om).solve(pm, dev(f))
+    assert stm.final_norm <= 1.5 * st.final_norm + 1e-12 * st.initial_norm
+
+
 def test_vc_solver_mixed_converges():
     from mushy_gb300 import ops
     g, chi, perm, u = P.projection_problem((128, 128), 6, sigma=16.0)
