@@ -126,7 +126,10 @@ typedef struct mlgpu_mg_options {
   int precision;         /* MLGPU_PREC_F64 or MLGPU_PREC_MIXED */
   int inner_cycles;      /* mixed: FP32 cycles per FP64 defect-correction step */
   int norm_type;         /* MLGPU_NORM_MAX (reference default) or L2 */
-  int use_graph;         /* capture one cycle in a CUDA graph and replay it */
+  int use_graph;         /* 0: plain launches; 1: one outer iteration captured in a
+                            CUDA graph and replayed; 2 (default): the whole outer
+                            loop as a graph WHILE node, decided on the device
+                            (linear solvers; the FAS solver treats 2 as 1) */
 } mlgpu_mg_options;
 
 typedef struct mlgpu_solve_stats {

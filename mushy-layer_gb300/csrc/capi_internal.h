@@ -6,6 +6,7 @@
 #include "vc_kernels.cuh"
 #include "cycle_kernels.cuh"
 #include "tile_kernels.cuh"
+#include "outer_kernels.cuh"
 
 namespace mlgpu {
 
@@ -28,5 +29,7 @@ cudaError_t launch_mac_correct(const Geom &G, const BCD &bc, int d, const double
                                const double *scale, double *u, cudaStream_t s);
 cudaError_t launch_be_rhs(long long n, const double *phi_old, const double *a, const double *src,
                           double dt, double *rhs, cudaStream_t s);
+cudaError_t launch_outer_decide(OuterDev *st, const double *norm, const OuterCfg &c,
+                                cudaGraphConditionalHandle h, cudaStream_t s);
 
 }  // namespace mlgpu

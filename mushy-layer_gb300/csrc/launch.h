@@ -44,7 +44,7 @@ cudaError_t launch_vc_op(const VCArgs<T> &A, int mode, int norm, const T *phi, c
 template <class T, class E>
 cudaError_t launch_vc_update_residual(const VCArgs<T> &A, int norm, const T *phi, const E *e,
                                       const T *rhs, T *out_phi, T *res, E *res_inner,
-                                      double *part, cudaStream_t s);
+                                      double *part, cudaStream_t s, const int *par = nullptr);
 template <class T>
 cudaError_t launch_vc_gsrb(const VCArgs<T> &A, T *phi, const T *rhs, int pass, cudaStream_t s);
 template <class T>

@@ -23,11 +23,18 @@ template cudaError_t launch_vc_update_residual<double, double>(const VCArgs<doub
                                                                const double *, const double *,
                                                                const double *, double *,
                                                                double *, double *, double *,
-                                                               cudaStream_t);
+                                                               cudaStream_t, const int *);
 template cudaError_t launch_vc_update_residual<double, float>(const VCArgs<double> &, int,
                                                               const double *, const float *,
                                                               const double *, double *, double *,
-                                                              float *, double *, cudaStream_t);
+                                                              float *, double *, cudaStream_t,
+                                                              const int *);
+
+cudaError_t launch_outer_decide(OuterDev *st, const double *norm, const OuterCfg &c,
+                                cudaGraphConditionalHandle h, cudaStream_t s) {
+  outer_decide_kernel<<<1, 1, 0, s>>>(st, norm, c, h);
+  return cudaGetLastError();
+}
 template cudaError_t launch_vc_gsrb<double>(const VCArgs<double> &, double *, const double *, int,
                                             cudaStream_t);
 template cudaError_t launch_vc_gsrb_zero<double>(const VCArgs<double> &, double *, const double *,

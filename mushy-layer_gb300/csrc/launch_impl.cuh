@@ -7,6 +7,7 @@
 #include "misc_kernels.cuh"
 #include "cycle_kernels.cuh"
 #include "tile_kernels.cuh"
+#include "outer_kernels.cuh"
 
 namespace mlgpu {
 
@@ -142,13 +143,13 @@ cudaError_t launch_vc_op(const VCArgs<T> &A, int mode, int norm, const T *phi, c
 template <class T, class E>
 cudaError_t launch_vc_update_residual(const VCArgs<T> &A, int norm, const T *phi, const E *e,
                                       const T *rhs, T *out_phi, T *res, E *res_inner,
-                                      double *part, cudaStream_t s) {
+                                      double *part, cudaStream_t s, const int *par) {
   int nb = blocks_for(A.G.ncell);
   if (norm < 0) norm = MLGPU_NORM_MAX;
   MLGPU_DIM_SWITCH(A.G.dim, MLGPU_NORM_SWITCH(norm, {
     if (NORM >= 0)
       vc_update_residual_kernel<T, E, DIM, (NORM < 0 ? 0 : NORM)>
-          <<<nb, kBlock, 0, s>>>(A, phi, e, rhs, out_phi, res, res_inner, part);
+          <<<nb, kBlock, 0, s>>>(A, phi, e, rhs, out_phi, res, res_inner, part, par);
   }));
   return cudaGetLastError();
 }

@@ -170,6 +170,9 @@ class VCSolver : public mlgpu_solver {
   double *rhs = nullptr, *part = nullptr;
   double *host_norm = nullptr;
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  cudaGraphExec_t loop_exec = nullptr;
+  bool loop_failed = false;
+  OuterDev *dev_state = nullptr, *host_state = nullptr;
   bool mixed = false;
   bool use_block_cycle = true;
   bool use_tiles = true;
@@ -178,7 +181,21 @@ class VCSolver : public mlgpu_solver {
   ~VCSolver() override {
     for (auto &g : graph)
       if (g) cudaGraphExecDestroy(g);
+    if (loop_exec) cudaGraphExecDestroy(loop_exec);
     if (host_norm) cudaFreeHost(host_norm);
+    if (host_state) cudaFreeHost(host_state);
+  }
+
+  void drop_graphs() {
+    for (auto &g : graph)
+      if (g) {
+        cudaGraphExecDestroy(g);
+        g = nullptr;
+      }
+    if (loop_exec) {
+      cudaGraphExecDestroy(loop_exec);
+      loop_exec = nullptr;
+    }
   }
 
   // lay out (or size, when base is null) the workspace
@@ -225,6 +242,7 @@ class VCSolver : public mlgpu_solver {
     phi[1] = A.get<double>(n0);
     rhs = A.get<double>(n0);
     part = A.get<double>(kNormScratchDoubles);
+    dev_state = A.get<OuterDev>(1);
     return A.off + 256;
   }
 
@@ -401,7 +419,9 @@ class VCSolver : public mlgpu_solver {
 
   // one outer iteration: inner cycles on (e0, r0), then phi_out = phi_in + e0
   // and the new residual (r0 in inner precision) with its norm
-  int iteration(int from) {
+  // one outer iteration; `par` (device) selects the ping-pong direction when
+  // the loop runs on the device, and then the decision kernel ends the body
+  int iteration(int from, const int *par = nullptr, cudaGraphConditionalHandle h = 0) {
     int rc;
     int cycles = std::max(1, o.inner_cycles);
     for (int c = 0; c < cycles; c++) {
@@ -415,14 +435,47 @@ class VCSolver : public mlgpu_solver {
     if (mixed)
       CK((launch_vc_update_residual<double, float>(A, o.norm_type, phi[from], (const float *)L[0].e,
                                                    rhs, phi[1 - from], nullptr, (float *)L[0].r,
-                                                   part, s)));
+                                                   part, s, par)));
     else
       CK((launch_vc_update_residual<double, double>(A, o.norm_type, phi[from],
                                                     (const double *)L[0].e, rhs, phi[1 - from],
-                                                    nullptr, (double *)L[0].r, part, s)));
+                                                    nullptr, (double *)L[0].r, part, s, par)));
     CK(launch_finalize_norm(o.norm_type, part, norm_parts(L[0].G.ncell), part + kMaxBlocks, s));
-    CK(cudaMemcpyAsync(host_norm, part + kMaxBlocks, sizeof(double), cudaMemcpyDeviceToHost, s));
+    if (par) {
+      OuterCfg cfg{o.tolerance, o.hang, o.norm_thresh, o.max_iter};
+      CK(launch_outer_decide(dev_state, part + kMaxBlocks, cfg, h, s));
+    } else {
+      CK(cudaMemcpyAsync(host_norm, part + kMaxBlocks, sizeof(double), cudaMemcpyDeviceToHost, s));
+    }
     return MLGPU_OK;
+  }
+
+  // whole outer loop as a graph WHILE node (one launch per solve)
+  int build_loop() {
+    cudaGraph_t g;
+    CK(cudaGraphCreate(&g, 0));
+    cudaGraphConditionalHandle h;
+    cudaError_t e = cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault);
+    cudaGraphNodeParams np = {cudaGraphNodeTypeConditional};
+    np.conditional.handle = h;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t node;
+    if (e == cudaSuccess) e = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &np);
+    if (e == cudaSuccess)
+      e = cudaStreamBeginCaptureToGraph(s, np.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                        cudaStreamCaptureModeThreadLocal);
+    int rc = MLGPU_OK;
+    if (e == cudaSuccess) {
+      rc = iteration(0, &dev_state->parity, h);
+      cudaGraph_t body;
+      e = cudaStreamEndCapture(s, &body);
+    }
+    if (e == cudaSuccess && rc == MLGPU_OK) e = cudaGraphInstantiate(&loop_exec, g, 0);
+    cudaGraphDestroy(g);
+    cudaGetLastError();
+    if (rc) return rc;
+    return e == cudaSuccess ? MLGPU_OK : MLGPU_ERR_CUDA;
   }
 
   int run_iteration(int from) {
@@ -469,6 +522,25 @@ class VCSolver : public mlgpu_solver {
     st->cell_updates = (double)L[0].G.ncell;
     if (!std::isfinite(S.norm0)) S.status = 8;
     int cur = 0;
+    if (o.use_graph >= 2 && !loop_failed && outer_continue(o, S)) {
+      if (!loop_exec && build_loop() != MLGPU_OK) loop_failed = true;
+      if (!loop_failed) {
+        memset(host_state, 0, sizeof(OuterDev));
+        host_state->norm0 = host_state->norm = host_state->prev = S.norm0;
+        CK(cudaMemcpyAsync(dev_state, host_state, sizeof(OuterDev), cudaMemcpyHostToDevice, s));
+        CK(cudaGraphLaunch(loop_exec, s));
+        CK(cudaMemcpyAsync(host_state, dev_state, sizeof(OuterDev), cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        S.iter = host_state->iter;
+        S.norm = host_state->norm;
+        S.prev = host_state->prev;
+        S.status = host_state->status;
+        for (int i = 1; i <= S.iter && i < 64; i++) st->norm_history[i] = host_state->hist[i];
+        cur = host_state->parity;
+        st->cycles = S.iter * std::max(1, o.inner_cycles);
+        st->cell_updates += S.iter * updates_per_iter;
+      }
+    }
     while (outer_continue(o, S)) {
       int rc = run_iteration(cur);
       if (rc) return rc;
@@ -488,11 +560,7 @@ class VCSolver : public mlgpu_solver {
   int set_alpha_beta(double a, double b) override {
     op.alpha = a;
     op.beta = b;
-    for (auto &g : graph)
-      if (g) {
-        cudaGraphExecDestroy(g);
-        g = nullptr;
-      }
+    drop_graphs();
     if (mixed) return MLGPU_OK;
     if (enter()) return MLGPU_ERR_CUDA;
     int rc = build_lambda();
@@ -728,7 +796,7 @@ void mlgpu_mg_default_options(mlgpu_mg_options *o, int hc) {
   o->precision = MLGPU_PREC_F64;
   o->inner_cycles = 1;
   o->norm_type = MLGPU_NORM_MAX;
-  o->use_graph = 1;
+  o->use_graph = 2;
 }
 
 int mlgpu_vc_solver_workspace(const mlgpu_vcop *op, const mlgpu_mg_options *o, size_t *bytes) {
@@ -763,7 +831,8 @@ int mlgpu_vc_solver_create(const mlgpu_vcop *op, const mlgpu_mg_options *o, void
     return MLGPU_ERR_WORKSPACE;
   }
   S->layout((char *)ws);
-  if (cudaHostAlloc((void **)&S->host_norm, sizeof(double), cudaHostAllocDefault) != cudaSuccess) {
+  if (cudaHostAlloc((void **)&S->host_norm, sizeof(double), cudaHostAllocDefault) != cudaSuccess ||
+      cudaHostAlloc((void **)&S->host_state, sizeof(OuterDev), cudaHostAllocDefault) != cudaSuccess) {
     delete S;
     return MLGPU_ERR_CUDA;
   }

@@ -65,6 +65,25 @@ __global__ void __launch_bounds__(kTileThreads) vc_tile_smooth_kernel(TileSmooth
     return ((gy % n1) + n1) % n1;
   };
 
+  // Faces of the cell at local (lx, ly) with wrapped global (gx, gy).  The
+  // shared arrays are positional; in a periodic direction the box keeps two
+  // entries for the seam face (face 0 for cell 0, face n for cell n-1), so the
+  // seam cells read their own entry from global memory, exactly as the
+  // per-level kernels index faces by the cell's own coordinates.
+  auto fxl = [&](int lx, int ly, int gx, int gy) -> T {
+    return (px && gx == 0) ? A.b[0][(long long)gy * (n0 + 1)] : sbx[ly * (LX + 1) + lx];
+  };
+  auto fxh = [&](int lx, int ly, int gx, int gy) -> T {
+    return (px && gx == n0 - 1) ? A.b[0][(long long)gy * (n0 + 1) + n0]
+                                : sbx[ly * (LX + 1) + lx + 1];
+  };
+  auto fyl = [&](int lx, int ly, int gx, int gy) -> T {
+    return (py && gy == 0) ? A.b[1][gx] : sby[ly * LX + lx];
+  };
+  auto fyh = [&](int lx, int ly, int gx, int gy) -> T {
+    return (py && gy == n1 - 1) ? A.b[1][(long long)n1 * n0 + gx] : sby[(ly + 1) * LX + lx];
+  };
+
   // ---- load faces, then cells (e, r, 1/diag)
   for (int q = tid; q < (LX + 1) * LY; q += nth) {
     int ly = q / (LX + 1), lx = q - ly * (LX + 1);
@@ -100,8 +119,8 @@ __global__ void __launch_bounds__(kTileThreads) vc_tile_smooth_kernel(TileSmooth
       if (A.lam) {
         lv = A.lam[gq];
       } else {
-        lv = vc_lambda_at<T, 2>(A, gq, sbx[ly * (LX + 1) + lx + 1], sbx[ly * (LX + 1) + lx],
-                                sby[(ly + 1) * LX + lx], sby[ly * LX + lx], T(0), T(0));
+        lv = vc_lambda_at<T, 2>(A, gq, fxh(lx, ly, gx, gy), fxl(lx, ly, gx, gy),
+                                fyh(lx, ly, gx, gy), fyl(lx, ly, gx, gy), T(0), T(0));
       }
       if (P.prolong >= 0) {
         Geom Cg = coarsen_geom(G);
@@ -126,8 +145,8 @@ __global__ void __launch_bounds__(kTileThreads) vc_tile_smooth_kernel(TileSmooth
     T hi0 = (gx0 + lx + 1 >= n0 && !px) ? ghost_value<T>(A.bc, 0, 1, 0, p0, A.dx, true) : se[c + 1];
     T lo1 = (gy0 + ly - 1 < 0 && !py) ? ghost_value<T>(A.bc, 1, 0, 0, p0, A.dx, true) : se[c - LX];
     T hi1 = (gy0 + ly + 1 >= n1 && !py) ? ghost_value<T>(A.bc, 1, 1, 0, p0, A.dx, true) : se[c + LX];
-    T bxh = sbx[ly * (LX + 1) + lx + 1], bxl = sbx[ly * (LX + 1) + lx];
-    T byh = sby[(ly + 1) * LX + lx], byl = sby[ly * LX + lx];
+    T bxh = fxh(lx, ly, gx, gy), bxl = fxl(lx, ly, gx, gy);
+    T byh = fyh(lx, ly, gx, gy), byl = fyl(lx, ly, gx, gy);
     T s = bxh * (hi0 - p0) - bxl * (p0 - lo0);
     s = s + byh * (hi1 - p0);
     s = s - byl * (p0 - lo1);

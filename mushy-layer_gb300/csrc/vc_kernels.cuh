@@ -138,11 +138,19 @@ __global__ void __launch_bounds__(kBlock) vc_op_kernel(VCArgs<T> A, const T *__r
 // fused norm.  Neighbours apply their own correction in registers, so the
 // update and the residual need one pass over memory.  out_phi must not alias
 // phi (other threads still read the old value); it is unused when e is null.
+// With `par` non-null the two solution buffers swap roles when *par == 1
+// (ping-pong selected on the device by the outer-loop decision kernel).
 template <class T, class E, int DIM, int NORM>
 __global__ void __launch_bounds__(kBlock) vc_update_residual_kernel(
     VCArgs<T> A, const T *phi, const E *__restrict__ e, const T *__restrict__ rhs,
-    T *out_phi, T *__restrict__ res, E *__restrict__ res_inner, double *__restrict__ part) {
+    T *out_phi, T *__restrict__ res, E *__restrict__ res_inner, double *__restrict__ part,
+    const int *__restrict__ par) {
   const Geom &G = A.G;
+  if (par && *par) {
+    T *t = out_phi;
+    out_phi = (T *)phi;
+    phi = t;
+  }
   double acc = 0.0;
   for (long long q = gtid(); q < G.ncell; q += gstride()) {
     int i, j, k;

@@ -19,7 +19,8 @@ REPO = os.path.dirname(PKG_ROOT)
 LIB = os.path.join(BUILD, "libmlgpu.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-COMMON = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-lineinfo",
+COMMON = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+          "-lineinfo",
           "-I" + os.path.join(REPO, "include")]
 UNITS = {
     "launch_f64.cu": ["--fmad=false"],

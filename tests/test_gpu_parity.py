@@ -313,7 +313,7 @@ def test_vc_solver_fp64_matches_oracle():
     sol_ref, st_ref, rc_ref = O.vc_solve(ref, opts, np.zeros_like(f), f)
     assert st_ref.iterations == 12
     op = ops.ProjectionOp(g, bc, 0.0, 1.0, None, [dev(x) for x in b])
-    for graph in (0, 1):
+    for graph in (0, 1, 2):
         o = ops.default_options(False)
         o.tolerance, o.hang, o.max_iter, o.use_graph = 1e-30, 0.0, 12, graph
         S = ops.AMRMultiGrid(op, o)
@@ -417,7 +417,7 @@ def test_hc_solver_fp64_matches_oracle():
     opts.max_iter = 6
     sol_ref, st_ref, rc_ref = O.hc_solve(ref, opts, phi, phi.copy())
     op = ops.NLMultiCompOp(g, p, phi_bc, der, 1.0, -dt, None, [dev(x) for x in b])
-    for graph in (0, 1):
+    for graph in (0, 1, 2):
         o = ops.default_options(True)
         o.max_iter, o.use_graph = 6, graph
         S = ops.AMRFASMultiGrid(op, o)
@@ -432,6 +432,10 @@ def test_hc_solver_fp64_matches_oracle():
 def test_mac_project_bitwise_and_divergence_free():
     from mushy_gb300 import ops
     g, chi, perm, u = P.projection_problem((64, 32), 8, sigma=6.0)
+    # a compatible u*: periodic in x (seam faces equal), solid walls in y
+    u[0][..., -1] = u[0][..., 0]
+    u[1][:, 0, :] = 0.0
+    u[1][:, -1, :] = 0.0
     pi = O.face_geomean(g, perm)
     b = [-x for x in pi]
     bc = abi.make_bc()
