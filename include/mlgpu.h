@@ -130,6 +130,10 @@ typedef struct mlgpu_mg_options {
                             CUDA graph and replayed; 2 (default): the whole outer
                             loop as a graph WHILE node, decided on the device
                             (linear solvers; the FAS solver treats 2 as 1) */
+  int fuse_levels;       /* 1 (default): 2D levels above 256 cells run shared-memory
+                            tiles (smoothing fused with restriction / prolongation)
+                            and the coarser levels one single-CTA cycle; 0: one
+                            launch per smoothing pass / transfer (same FP64 bits) */
 } mlgpu_mg_options;
 
 typedef struct mlgpu_solve_stats {

@@ -1,10 +1,11 @@
 // cycle_kernels.cuh -- the coarse end of a multigrid V-cycle in ONE thread
-// block.  Below a few thousand cells a level's work is far smaller than a
+// block.  Below a few hundred cells a level's work is far smaller than a
 // kernel launch, so every level from `A[0]` down to the bottom runs inside a
-// single CTA: relax, restrict, bottom relaxation, prolong, relax, separated
-// by __syncthreads().  Each cell update calls the same device functions as
-// the per-level kernels, so the results are bit-identical to launching the
-// per-level kernels one after another.
+// single CTA: relax, restrict, bottom relaxation, prolong, relax.  Levels of
+// at most 64 cells (and the bottom) are finished by warp 0 alone with warp
+// barriers, the larger ones by the whole block with block barriers.  Each
+// cell update calls the same device functions as the per-level kernels, so
+// results are bit-identical to launching the per-level kernels in sequence.
 #pragma once
 #include "vc_kernels.cuh"
 #include "misc_kernels.cuh"
@@ -12,6 +13,7 @@
 namespace mlgpu {
 
 constexpr int kMaxBlockLevels = 12;
+constexpr long long kWarpLevelCells = 64;
 
 template <class T>
 struct VCBlockCycle {
@@ -24,80 +26,133 @@ struct VCBlockCycle {
   T *r[kMaxBlockLevels];
 };
 
-template <class T, int DIM>
+// WARP: the phase is run by warp 0 only (32 lanes, __syncwarp); otherwise by
+// the whole block (__syncthreads).
+template <bool WARP>
+__device__ __forceinline__ void cyc_sync() {
+  if (WARP)
+    __syncwarp();
+  else
+    __syncthreads();
+}
+template <bool WARP>
+__device__ __forceinline__ int cyc_nthreads() {
+  return WARP ? 32 : (int)blockDim.x;
+}
+
+template <class T, int DIM, bool WARP>
 __device__ __forceinline__ void blk_half_sweep(const VCArgs<T> &A, T *e, const T *r, int pass) {
   long long nt = colour_threads(A.G);
-  for (long long t = threadIdx.x; t < nt; t += blockDim.x) {
+  for (long long t = threadIdx.x; t < nt; t += cyc_nthreads<WARP>()) {
     int i, j, k;
     if (colour_cell(A.G, pass, t, i, j, k)) vc_gsrb_cell<T, DIM>(A, e, r, i, j, k);
   }
-  __syncthreads();
+  cyc_sync<WARP>();
 }
 
-// VCSolver::relax for GSRB, inside the block
-template <class T, int DIM>
+// VCSolver::relax for GSRB, inside the block (or warp)
+template <class T, int DIM, bool WARP>
 __device__ void blk_relax(const VCArgs<T> &A, T *e, const T *r, int n, bool zero_init) {
+  const int nth = cyc_nthreads<WARP>();
   if (zero_init) {
     if (n == 0) {
-      for (long long q = threadIdx.x; q < A.G.ncell; q += blockDim.x) e[q] = T(0);
-      __syncthreads();
+      for (long long q = threadIdx.x; q < A.G.ncell; q += nth) e[q] = T(0);
+      cyc_sync<WARP>();
       return;
     }
-    for (long long q = threadIdx.x; q < A.G.ncell; q += blockDim.x) {
+    for (long long q = threadIdx.x; q < A.G.ncell; q += nth) {
       int i, j, k;
       cell_ijk(A.G, q, i, j, k);
       vc_gsrb_zero_cell<T, DIM>(A, e, r, q, i, j, k);
     }
-    __syncthreads();
-    blk_half_sweep<T, DIM>(A, e, r, 1);
+    cyc_sync<WARP>();
+    blk_half_sweep<T, DIM, WARP>(A, e, r, 1);
     n--;
   }
   for (int s = 0; s < n; s++) {
-    blk_half_sweep<T, DIM>(A, e, r, 0);
-    blk_half_sweep<T, DIM>(A, e, r, 1);
+    blk_half_sweep<T, DIM, WARP>(A, e, r, 0);
+    blk_half_sweep<T, DIM, WARP>(A, e, r, 1);
+  }
+}
+
+template <class T, int DIM, bool WARP>
+__device__ void blk_restrict(const VCBlockCycle<T> &P, int l) {
+  const VCArgs<T> &A = P.A[l];
+  const T denom = DIM == 3 ? T(8) : T(4);
+  const Geom &C = P.A[l + 1].G;
+  PlainRead<T> rd{P.e[l]};
+  for (long long Q = threadIdx.x; Q < C.ncell; Q += cyc_nthreads<WARP>()) {
+    int I, J, K;
+    cell_ijk(C, Q, I, J, K);
+    T acc = T(0);
+    for (int kk = 0; kk < (DIM == 3 ? 2 : 1); kk++)
+      for (int jj = 0; jj < 2; jj++)
+        for (int ii = 0; ii < 2; ii++) {
+          int i = 2 * I + ii, j = 2 * J + jj, k = DIM == 3 ? 2 * K + kk : 0;
+          T p0, lam;
+          T lof = vc_lofphi<T, DIM, false>(A, rd, i, j, k, true, p0, lam);
+          acc = acc + (P.r[l][A.G.cell(i, j, k)] - lof) / denom;
+        }
+    P.r[l + 1][Q] = acc;
+  }
+  cyc_sync<WARP>();
+}
+
+template <class T, int DIM, bool WARP>
+__device__ void blk_prolong(const VCBlockCycle<T> &P, int l) {
+  const Geom &F = P.A[l].G, &C = P.A[l + 1].G;
+  for (long long t = threadIdx.x; t < F.ncell; t += cyc_nthreads<WARP>()) {
+    if (P.prolong == MLGPU_PROLONG_LINEAR)
+      prolong_one<T, DIM, MLGPU_PROLONG_LINEAR>(F, C, P.bc, t, P.e[l], P.e[l + 1], nullptr);
+    else
+      prolong_one<T, DIM, MLGPU_PROLONG_CONSTANT>(F, C, P.bc, t, P.e[l], P.e[l + 1], nullptr);
+  }
+  cyc_sync<WARP>();
+}
+
+// levels [l0, last] with the bottom, by the block (WARP false) or warp 0
+template <class T, int DIM, bool WARP>
+__device__ void blk_cycle_range(const VCBlockCycle<T> &P, int l0, int l1, bool zero_top) {
+  // down over [l0, l1): pre-smooth and restrict; l1 is handled by the caller
+  for (int l = l0; l < l1; l++) {
+    blk_relax<T, DIM, WARP>(P.A[l], P.e[l], P.r[l], P.pre, l > l0 || zero_top);
+    blk_restrict<T, DIM, WARP>(P, l);
+  }
+}
+template <class T, int DIM, bool WARP>
+__device__ void blk_cycle_up(const VCBlockCycle<T> &P, int l0, int l1) {
+  // up over (l0 .. l1] reversed: prolong into l, post-smooth l
+  for (int l = l1 - 1; l >= l0; l--) {
+    blk_prolong<T, DIM, WARP>(P, l);
+    blk_relax<T, DIM, WARP>(P.A[l], P.e[l], P.r[l], P.post, false);
   }
 }
 
 template <class T, int DIM>
 __global__ void __launch_bounds__(1024) vc_block_cycle_kernel(VCBlockCycle<T> P) {
   const int last = P.nlev - 1;
-  const T denom = DIM == 3 ? T(8) : T(4);
-  // down: pre-smooth, restrict the residual
-  for (int l = 0; l < last; l++) {
-    const VCArgs<T> &A = P.A[l];
-    blk_relax<T, DIM>(A, P.e[l], P.r[l], P.pre, l > 0 || P.zero_init);
-    const Geom &C = P.A[l + 1].G;
-    PlainRead<T> rd{P.e[l]};
-    for (long long Q = threadIdx.x; Q < C.ncell; Q += blockDim.x) {
-      int I, J, K;
-      cell_ijk(C, Q, I, J, K);
-      T acc = T(0);
-      for (int kk = 0; kk < (DIM == 3 ? 2 : 1); kk++)
-        for (int jj = 0; jj < 2; jj++)
-          for (int ii = 0; ii < 2; ii++) {
-            int i = 2 * I + ii, j = 2 * J + jj, k = DIM == 3 ? 2 * K + kk : 0;
-            T p0, lam;
-            T lof = vc_lofphi<T, DIM, false>(A, rd, i, j, k, true, p0, lam);
-            acc = acc + (P.r[l][A.G.cell(i, j, k)] - lof) / denom;
-          }
-      P.r[l + 1][Q] = acc;
+  // first level small enough for warp 0 alone (the bottom at the latest)
+  int lw = last;
+  for (int l = 0; l < last; l++)
+    if (P.A[l].G.ncell <= kWarpLevelCells) {
+      lw = l;
+      break;
+    }
+  const bool warp_bottom = P.A[last].G.ncell <= kWarpLevelCells;
+  // block part, down
+  blk_cycle_range<T, DIM, false>(P, 0, lw, P.zero_init != 0);
+  if (warp_bottom) {
+    if (threadIdx.x < 32) {
+      blk_cycle_range<T, DIM, true>(P, lw, last, lw > 0 || P.zero_init != 0);
+      blk_relax<T, DIM, true>(P.A[last], P.e[last], P.r[last], P.bottom, true);
+      blk_cycle_up<T, DIM, true>(P, lw, last);
     }
     __syncthreads();
+  } else {
+    blk_relax<T, DIM, false>(P.A[last], P.e[last], P.r[last], P.bottom, true);
   }
-  // bottom: zero, then relaxation sweeps (RelaxSolver role)
-  blk_relax<T, DIM>(P.A[last], P.e[last], P.r[last], P.bottom, true);
-  // up: prolong the correction, post-smooth
-  for (int l = last - 1; l >= 0; l--) {
-    const Geom &F = P.A[l].G, &C = P.A[l + 1].G;
-    for (long long t = threadIdx.x; t < F.ncell; t += blockDim.x) {
-      if (P.prolong == MLGPU_PROLONG_LINEAR)
-        prolong_one<T, DIM, MLGPU_PROLONG_LINEAR>(F, C, P.bc, t, P.e[l], P.e[l + 1], nullptr);
-      else
-        prolong_one<T, DIM, MLGPU_PROLONG_CONSTANT>(F, C, P.bc, t, P.e[l], P.e[l + 1], nullptr);
-    }
-    __syncthreads();
-    blk_relax<T, DIM>(P.A[l], P.e[l], P.r[l], P.post, false);
-  }
+  // block part, up
+  blk_cycle_up<T, DIM, false>(P, 0, lw);
 }
 
 }  // namespace mlgpu

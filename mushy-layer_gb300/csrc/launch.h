@@ -61,7 +61,7 @@ template <class T> struct VCBlockCycle;
 template <class T>
 cudaError_t launch_vc_block_cycle(const VCBlockCycle<T> &P, cudaStream_t s);
 // levels at or below this many cells run inside one thread block
-constexpr long long kBlockCycleCells = 4096;
+constexpr long long kBlockCycleCells = 256;
 template <class T> struct TileSmooth;
 template <class T>
 cudaError_t launch_vc_tile_smooth(const TileSmooth<T> &P, cudaStream_t s);

@@ -158,6 +158,7 @@ struct VCLevel {
   Coefs<double> c64;
   Coefs<float> c32;
   void *e = nullptr, *r = nullptr, *t = nullptr;  // inner precision
+  void *ecur = nullptr;  // which of e / t holds the correction after the last pass
   double *lam64 = nullptr;  // stored 1/diag for FP64 inner cycles
 };
 
@@ -235,7 +236,7 @@ class VCSolver : public mlgpu_solver {
       }
       g = coarsen_grid(g);
     }
-    use_block_cycle = o.relax_mode == MLGPU_RELAX_GSRB && o.num_mg == 1;
+    use_block_cycle = o.relax_mode == MLGPU_RELAX_GSRB && o.num_mg == 1 && o.fuse_levels;
     use_tiles = use_block_cycle;
     size_t n0 = ncells(op.grid);
     phi[0] = A.get<double>(n0);
@@ -352,7 +353,15 @@ class VCSolver : public mlgpu_solver {
       bool is_last = done + chunk == nh;
       TileSmooth<T> P;
       P.A = args<T>(l);
-      P.e = (T *)L[l].e;
+      // ping-pong: read the current buffer, write the other one
+      if (first && zero) {
+        P.e_in = nullptr;
+        P.e_out = (T *)L[l].e;
+      } else {
+        P.e_in = (const T *)L[l].ecur;
+        P.e_out = (T *)(L[l].ecur == L[l].e ? L[l].t : L[l].e);
+      }
+      L[l].ecur = P.e_out;
       P.r = (const T *)L[l].r;
       P.zero_init = (first && zero) ? 1 : 0;
       P.n_half = chunk;
@@ -360,7 +369,7 @@ class VCSolver : public mlgpu_solver {
       P.rc = (is_last && with_restrict) ? (T *)L[l + 1].r : nullptr;
       P.halo = chunk + (P.rc ? 1 : 0);
       P.prolong = (first && with_prolong) ? o.prolong : -1;
-      P.ec = with_prolong ? (const T *)L[l + 1].e : nullptr;
+      P.ec = with_prolong ? (const T *)L[l + 1].ecur : nullptr;
       CK(launch_vc_tile_smooth<T>(P, s));
       first = false;
       done += chunk;
@@ -372,6 +381,9 @@ class VCSolver : public mlgpu_solver {
   int cycle(int l, bool zero_init) {
     int last = (int)L.size() - 1;
     VCArgs<T> A = args<T>(l);
+    // a fresh correction starts in e; a continued one stays where the last
+    // pass left it (the tile path alternates e / t, the other paths work in e)
+    if (zero_init || !L[l].ecur) L[l].ecur = L[l].e;
     if (use_tiles && l < last && L[l].G.dim == 2 && L[l].G.ncell > kBlockCycleCells) {
       int rc = tile_sweeps<T>(l, 2 * o.num_smooth_down, zero_init, true, false);
       if (rc) return rc;
@@ -413,7 +425,7 @@ class VCSolver : public mlgpu_solver {
       if (rc) return rc;
     }
     CK(launch_prolong<T>(L[l].G, make_bcd(op.bc), 1, o.prolong, (T *)L[l].e,
-                         (const T *)L[l + 1].e, nullptr, s));
+                         (const T *)L[l + 1].ecur, nullptr, s));
     return relax<T>(l, o.num_smooth_up, false);
   }
 
@@ -433,12 +445,12 @@ class VCSolver : public mlgpu_solver {
     A.c = (const double *)op.cCoef;
     for (int d = 0; d < 3; d++) A.b[d] = (const double *)op.bCoef[d];
     if (mixed)
-      CK((launch_vc_update_residual<double, float>(A, o.norm_type, phi[from], (const float *)L[0].e,
-                                                   rhs, phi[1 - from], nullptr, (float *)L[0].r,
-                                                   part, s, par)));
+      CK((launch_vc_update_residual<double, float>(A, o.norm_type, phi[from],
+                                                   (const float *)L[0].ecur, rhs, phi[1 - from],
+                                                   nullptr, (float *)L[0].r, part, s, par)));
     else
       CK((launch_vc_update_residual<double, double>(A, o.norm_type, phi[from],
-                                                    (const double *)L[0].e, rhs, phi[1 - from],
+                                                    (const double *)L[0].ecur, rhs, phi[1 - from],
                                                     nullptr, (double *)L[0].r, part, s, par)));
     CK(launch_finalize_norm(o.norm_type, part, norm_parts(L[0].G.ncell), part + kMaxBlocks, s));
     if (par) {
@@ -797,6 +809,7 @@ void mlgpu_mg_default_options(mlgpu_mg_options *o, int hc) {
   o->inner_cycles = 1;
   o->norm_type = MLGPU_NORM_MAX;
   o->use_graph = 2;
+  o->fuse_levels = 1;
 }
 
 int mlgpu_vc_solver_workspace(const mlgpu_vcop *op, const mlgpu_mg_options *o, size_t *bytes) {

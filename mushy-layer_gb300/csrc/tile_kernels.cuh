@@ -14,10 +14,14 @@
 
 namespace mlgpu {
 
+// The correction is read from `e_in` and written to `e_out`, never the same
+// buffer: a block loads its halo from cells other blocks own and write back,
+// so an in-place update would race with blocks of a later wave.
 template <class T>
 struct TileSmooth {
   VCArgs<T> A;        // level operator; A.lam null: 1/diag computed at load
-  T *e;               // level correction (in/out)
+  const T *e_in;      // level correction before (unused with zero_init)
+  T *e_out;           // level correction after (interior cells of every tile)
   const T *r;         // level right-hand side
   int zero_init;      // e starts at zero instead of being loaded
   int n_half;         // red/black half sweeps
@@ -28,7 +32,10 @@ struct TileSmooth {
   const T *ec;        // coarse correction for the prolongation
 };
 
-constexpr int kTileX = 64, kTileY = 32, kTileThreads = 512;
+// Small interior tiles with a wide halo: every level gets many blocks and each
+// thread updates one or two cells per half sweep; the redundant halo work is
+// cheap next to the latency it removes.
+constexpr int kTileX = 16, kTileY = 16, kTileThreads = 512;
 
 inline size_t tile_smem_bytes(int halo, size_t elem) {
   size_t lx = kTileX + 2 * halo, ly = kTileY + 2 * halo;
@@ -114,7 +121,7 @@ __global__ void __launch_bounds__(kTileThreads) vc_tile_smooth_kernel(TileSmooth
     T ev = T(0), rv = T(0), lv = T(0);
     if (gx >= 0 && gy >= 0) {
       long long gq = (long long)gy * n0 + gx;
-      if (!P.zero_init) ev = P.e[gq];
+      if (!P.zero_init) ev = P.e_in[gq];
       rv = P.r[gq];
       if (A.lam) {
         lv = A.lam[gq];
@@ -185,7 +192,7 @@ __global__ void __launch_bounds__(kTileThreads) vc_tile_smooth_kernel(TileSmooth
   for (int q = tid; q < kTileX * kTileY; q += nth) {
     int iy = q / kTileX, ix = q - iy * kTileX;
     int gx = x0 + ix, gy = y0 + iy;
-    if (gx < n0 && gy < n1) P.e[(long long)gy * n0 + gx] = se[(iy + H) * LX + ix + H];
+    if (gx < n0 && gy < n1) P.e_out[(long long)gy * n0 + gx] = se[(iy + H) * LX + ix + H];
   }
 
   // ---- residual of the interior, restricted to the coarse level

@@ -70,7 +70,7 @@ class MGOptions(C.Structure):
                 ("bottom_solver", C.c_int), ("bottom_max_iter", C.c_int),
                 ("max_coarse", C.c_int), ("prolong", C.c_int),
                 ("precision", C.c_int), ("inner_cycles", C.c_int),
-                ("norm_type", C.c_int), ("use_graph", C.c_int)]
+                ("norm_type", C.c_int), ("use_graph", C.c_int), ("fuse_levels", C.c_int)]
 
 
 class SolveStats(C.Structure):

@@ -1046,6 +1046,7 @@ void orc_mg_default_options(mlgpu_mg_options *o, int hc) {
   o->inner_cycles = 1;
   o->norm_type = MLGPU_NORM_MAX;
   o->use_graph = 0;
+  o->fuse_levels = 1;
 }
 
 int orc_mg_depth(const mlgpu_grid *g, int max_coarse) { return mg_depth(*g, max_coarse); }

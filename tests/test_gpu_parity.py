@@ -372,6 +372,34 @@ def test_vc_solver_tiled_levels_bitwise(n, per, with_c, bckind, pre, post):
     assert stm.final_norm <= 1.5 * st.final_norm + 1e-12 * st.initial_norm
 
 
+@pytest.mark.parametrize("mixed", [False, True])
+def test_vc_fused_levels_match_unfused_multiwave(mixed):
+    """1024x768 puts thousands of tiles in flight (several waves), where a
+    tile reading halo cells that another tile already rewrote would show up.
+    FP64: fused == per-level launches bit for bit; mixed: same convergence."""
+    from mushy_gb300 import ops
+    g, chi, perm, u = P.projection_problem((1024, 768), 9, sigma=24.0)
+    faces = O.face_geomean(g, perm)
+    b = [-x for x in faces]
+    f = O.mac_divergence(g, u)
+    f -= f.mean()
+    op = ops.ProjectionOp(g, abi.make_bc(), 0.0, 1.0, None, [dev(x) for x in b])
+    out = {}
+    for fuse in (0, 1):
+        o = ops.default_options(False)
+        o.tolerance, o.hang, o.max_iter, o.fuse_levels = 1e-30, 0.0, 6, fuse
+        o.precision = abi.PREC_MIXED if mixed else abi.PREC_F64
+        d_phi = torch.zeros_like(dev(f))
+        st, rc = ops.AMRMultiGrid(op, o).solve(d_phi, dev(f))
+        out[fuse] = (host(d_phi), [st.norm_history[i] for i in range(7)])
+    if not mixed:
+        exact(out[1][0], out[0][0])
+        assert out[1][1] == out[0][1]
+    else:
+        h0, h1 = np.array(out[0][1]), np.array(out[1][1])
+        assert np.all(np.abs(h1 - h0) <= 1e-3 * h0), (h0, h1)
+
+
 def test_vc_solver_mixed_converges():
     from mushy_gb300 import ops
     g, chi, perm, u = P.projection_problem((128, 128), 6, sigma=16.0)
