@@ -130,10 +130,12 @@ typedef struct mlgpu_mg_options {
                             CUDA graph and replayed; 2 (default): the whole outer
                             loop as a graph WHILE node, decided on the device
                             (linear solvers; the FAS solver treats 2 as 1) */
-  int fuse_levels;       /* 1 (default): 2D levels above 256 cells run shared-memory
-                            tiles (smoothing fused with restriction / prolongation)
-                            and the coarser levels one single-CTA cycle; 0: one
-                            launch per smoothing pass / transfer (same FP64 bits) */
+  int fuse_levels;       /* 1 (default): levels of at most 256 cells run one
+                            single-CTA cycle and, in mixed precision, 2D levels
+                            above that run FP32 shared-memory tiles (smoothing fused
+                            with restriction / prolongation); 2: FP64 cycles use
+                            the tiles too; 0: one launch per smoothing pass /
+                            transfer.  FP64 results are the same bits for 0, 1, 2 */
 } mlgpu_mg_options;
 
 typedef struct mlgpu_solve_stats {

@@ -6,6 +6,7 @@
 #include "vc_kernels.cuh"
 #include "cycle_kernels.cuh"
 #include "tile_kernels.cuh"
+#include "tile_fast_kernels.cuh"
 #include "outer_kernels.cuh"
 
 namespace mlgpu {

@@ -41,7 +41,7 @@ __device__ __forceinline__ int cyc_nthreads() {
 }
 
 template <class T, int DIM, bool WARP>
-__device__ __forceinline__ void blk_half_sweep(const VCArgs<T> &A, T *e, const T *r, int pass) {
+__device__ __noinline__ void blk_half_sweep(const VCArgs<T> &A, T *e, const T *r, int pass) {
   long long nt = colour_threads(A.G);
   for (long long t = threadIdx.x; t < nt; t += cyc_nthreads<WARP>()) {
     int i, j, k;
@@ -52,7 +52,7 @@ __device__ __forceinline__ void blk_half_sweep(const VCArgs<T> &A, T *e, const T
 
 // VCSolver::relax for GSRB, inside the block (or warp)
 template <class T, int DIM, bool WARP>
-__device__ void blk_relax(const VCArgs<T> &A, T *e, const T *r, int n, bool zero_init) {
+__device__ __noinline__ void blk_relax(const VCArgs<T> &A, T *e, const T *r, int n, bool zero_init) {
   const int nth = cyc_nthreads<WARP>();
   if (zero_init) {
     if (n == 0) {
@@ -76,7 +76,7 @@ __device__ void blk_relax(const VCArgs<T> &A, T *e, const T *r, int n, bool zero
 }
 
 template <class T, int DIM, bool WARP>
-__device__ void blk_restrict(const VCBlockCycle<T> &P, int l) {
+__device__ __noinline__ void blk_restrict(const VCBlockCycle<T> &P, int l) {
   const VCArgs<T> &A = P.A[l];
   const T denom = DIM == 3 ? T(8) : T(4);
   const Geom &C = P.A[l + 1].G;
@@ -99,7 +99,7 @@ __device__ void blk_restrict(const VCBlockCycle<T> &P, int l) {
 }
 
 template <class T, int DIM, bool WARP>
-__device__ void blk_prolong(const VCBlockCycle<T> &P, int l) {
+__device__ __noinline__ void blk_prolong(const VCBlockCycle<T> &P, int l) {
   const Geom &F = P.A[l].G, &C = P.A[l + 1].G;
   for (long long t = threadIdx.x; t < F.ncell; t += cyc_nthreads<WARP>()) {
     if (P.prolong == MLGPU_PROLONG_LINEAR)
@@ -128,8 +128,86 @@ __device__ void blk_cycle_up(const VCBlockCycle<T> &P, int l0, int l1) {
   }
 }
 
+// Shared-memory image of every level of the cycle: the descriptor itself and,
+// per level, e, r, 1/diag and the faces.  The cell-update code reads them
+// through the descriptor's pointers, so the arithmetic is unchanged; only the
+// latency of each of the ~80 barrier-separated phases drops from L2 round
+// trips to shared-memory accesses.
+template <class T>
+__host__ __device__ inline size_t block_cycle_smem_elems(const VCBlockCycle<T> &P) {
+  size_t n = 0;
+  for (int m = 0; m < P.nlev; m++) {
+    const Geom &G = P.A[m].G;
+    n += 3 * (size_t)G.ncell;
+    for (int d = 0; d < G.dim; d++) n += (size_t)G.nface(d);
+  }
+  return n;
+}
+template <class T>
+inline size_t block_cycle_smem_bytes(const VCBlockCycle<T> &P) {
+  return ((sizeof(VCBlockCycle<T>) + 15) & ~(size_t)15) + sizeof(T) * block_cycle_smem_elems(P);
+}
+
 template <class T, int DIM>
-__global__ void __launch_bounds__(1024) vc_block_cycle_kernel(VCBlockCycle<T> P) {
+__global__ void __launch_bounds__(256) vc_block_cycle_kernel(VCBlockCycle<T> Pg) {
+  extern __shared__ __align__(16) unsigned char cyc_smem[];
+  VCBlockCycle<T> &P = *reinterpret_cast<VCBlockCycle<T> *>(cyc_smem);
+  T *pool = reinterpret_cast<T *>(cyc_smem + ((sizeof(VCBlockCycle<T>) + 15) & ~(size_t)15));
+  T *top_e = Pg.e[0];
+  if (threadIdx.x == 0) {
+    P = Pg;
+    size_t off = 0;
+    for (int m = 0; m < Pg.nlev; m++) {
+      const Geom &G = Pg.A[m].G;
+      P.e[m] = pool + off;
+      off += G.ncell;
+      P.r[m] = pool + off;
+      off += G.ncell;
+      P.A[m].lam = pool + off;
+      off += G.ncell;
+      for (int d = 0; d < G.dim; d++) {
+        P.A[m].b[d] = pool + off;
+        off += G.nface(d);
+      }
+    }
+  }
+  __syncthreads();
+  // stage faces, the top level's right-hand side and correction
+  for (int m = 0; m < Pg.nlev; m++) {
+    const Geom &G = Pg.A[m].G;
+    for (int d = 0; d < G.dim; d++)
+      for (long long q = threadIdx.x; q < G.nface(d); q += blockDim.x)
+        const_cast<T *>(P.A[m].b[d])[q] = Pg.A[m].b[d][q];
+  }
+  for (long long q = threadIdx.x; q < Pg.A[0].G.ncell; q += blockDim.x) {
+    P.r[0][q] = Pg.r[0][q];
+    if (!Pg.zero_init) P.e[0][q] = top_e[q];
+  }
+  __syncthreads();
+  // 1/diag per level, from the stored array or in resetLambda order
+  for (int m = 0; m < Pg.nlev; m++) {
+    const VCArgs<T> &A = P.A[m];
+    for (long long q = threadIdx.x; q < A.G.ncell; q += blockDim.x) {
+      T lv;
+      if (Pg.A[m].lam) {
+        lv = Pg.A[m].lam[q];
+      } else {
+        int i, j, k;
+        cell_ijk(A.G, q, i, j, k);
+        T bzh = T(0), bzl = T(0);
+        if (DIM == 3) {
+          bzh = vface(A, 2, i, j, k + 1);
+          bzl = vface(A, 2, i, j, k);
+        }
+        VCArgs<T> Ai = A;
+        Ai.lam = nullptr;
+        lv = vc_lambda_at<T, DIM>(Ai, q, vface(A, 0, i + 1, j, k), vface(A, 0, i, j, k),
+                                  vface(A, 1, i, j + 1, k), vface(A, 1, i, j, k), bzh, bzl);
+      }
+      const_cast<T *>(A.lam)[q] = lv;
+    }
+  }
+  __syncthreads();
   const int last = P.nlev - 1;
   // first level small enough for warp 0 alone (the bottom at the latest)
   int lw = last;
@@ -153,6 +231,8 @@ __global__ void __launch_bounds__(1024) vc_block_cycle_kernel(VCBlockCycle<T> P)
   }
   // block part, up
   blk_cycle_up<T, DIM, false>(P, 0, lw);
+  // the top level's correction is what the caller prolongs from
+  for (long long q = threadIdx.x; q < Pg.A[0].G.ncell; q += blockDim.x) top_e[q] = P.e[0][q];
 }
 
 }  // namespace mlgpu

@@ -67,6 +67,10 @@ template <class T>
 cudaError_t launch_vc_tile_smooth(const TileSmooth<T> &P, cudaStream_t s);
 // largest halo a tile launch may use for element size `elem` (shared memory)
 int tile_max_halo(size_t elem);
+struct TileFast;
+cudaError_t launch_vc_tile_fast(const TileFast &P, cudaStream_t s);
+cudaError_t launch_fast_coefs(const VCArgs<double> &A, float *cx, float *cy, float *lam,
+                              float *diag, cudaStream_t s);
 
 template <class T>
 cudaError_t launch_restrict_avg(const Geom &F, int ncomp, const T *fine, T *coarse, cudaStream_t s);

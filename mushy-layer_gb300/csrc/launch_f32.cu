@@ -1,7 +1,9 @@
 // launch_f32.cu -- FP32 instantiations of the kernel launchers (inner
 // multigrid cycles of the mixed-precision solvers).  FMA contraction is left
 // on; the nonlinear closure inside these kernels still runs in FP64.
+#define MLGPU_FP32_UNIT 1
 #include "launch_impl.cuh"
+#include "tile_fast_kernels.cuh"
 
 namespace mlgpu {
 
@@ -44,4 +46,29 @@ template cudaError_t launch_convert<float, float>(long long, float *, const floa
 namespace mlgpu {
 template cudaError_t launch_vc_block_cycle<float>(const VCBlockCycle<float> &, cudaStream_t);
 template cudaError_t launch_vc_tile_smooth<float>(const TileSmooth<float> &, cudaStream_t);
+
+cudaError_t launch_vc_tile_fast(const TileFast &P, cudaStream_t s) {
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaError_t e = cudaFuncSetAttribute(vc_tile_fast_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)kMaxDynSmem);
+    if (e != cudaSuccess) return e;
+    attr_set = true;
+  }
+  size_t bytes = tile_fast_smem_bytes(P.halo);
+  if (bytes > kMaxDynSmem) return cudaErrorInvalidValue;
+  dim3 grid((P.G.n0 + kTileX - 1) / kTileX, (P.G.n1 + kTileY - 1) / kTileY);
+  vc_tile_fast_kernel<<<grid, dim3(kTileTX, kTileTY), bytes, s>>>(P);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fast_coefs(const VCArgs<double> &A, float *cx, float *cy, float *lam,
+                              float *diag, cudaStream_t s) {
+  if (A.G.dim != 2) return cudaErrorInvalidValue;
+  long long n = A.G.nface(0) > A.G.ncell ? A.G.nface(0) : A.G.ncell;
+  if (A.G.nface(1) > n) n = A.G.nface(1);
+  fast_coefs_kernel<2><<<blocks_for(n), kBlock, 0, s>>>(A, cx, cy, lam, diag);
+  return cudaGetLastError();
+}
 }

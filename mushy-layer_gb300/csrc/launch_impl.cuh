@@ -27,7 +27,7 @@ cudaError_t launch_vc_tile_smooth(const TileSmooth<T> &P, cudaStream_t s) {
   if (bytes > kMaxDynSmem) return cudaErrorInvalidValue;
   const Geom &G = P.A.G;
   dim3 grid((G.n0 + kTileX - 1) / kTileX, (G.n1 + kTileY - 1) / kTileY);
-  vc_tile_smooth_kernel<T><<<grid, kTileThreads, bytes, s>>>(P);
+  vc_tile_smooth_kernel<T><<<grid, dim3(kTileTX, kTileTY), bytes, s>>>(P);
   return cudaGetLastError();
 }
 
@@ -198,9 +198,11 @@ template <class T>
 cudaError_t launch_vc_block_cycle(const VCBlockCycle<T> &P, cudaStream_t s) {
   long long nt = colour_threads(P.A[0].G);
   int threads = (int)((nt + 31) / 32 * 32);
-  if (threads > 1024) threads = 1024;
+  if (threads > 256) threads = 256;  // __launch_bounds__ of the kernel
   if (threads < 64) threads = 64;
-  MLGPU_DIM_SWITCH(P.A[0].G.dim, (vc_block_cycle_kernel<T, DIM><<<1, threads, 0, s>>>(P)));
+  size_t bytes = block_cycle_smem_bytes(P);
+  if (bytes > 48 * 1024) return cudaErrorInvalidValue;  // levels above kBlockCycleCells
+  MLGPU_DIM_SWITCH(P.A[0].G.dim, (vc_block_cycle_kernel<T, DIM><<<1, threads, bytes, s>>>(P)));
   return cudaGetLastError();
 }
 

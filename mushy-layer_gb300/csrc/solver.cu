@@ -160,6 +160,7 @@ struct VCLevel {
   void *e = nullptr, *r = nullptr, *t = nullptr;  // inner precision
   void *ecur = nullptr;  // which of e / t holds the correction after the last pass
   double *lam64 = nullptr;  // stored 1/diag for FP64 inner cycles
+  float *fcx = nullptr, *fcy = nullptr, *flam = nullptr, *fdiag = nullptr;  // lean FP32 tiles
 };
 
 class VCSolver : public mlgpu_solver {
@@ -226,6 +227,12 @@ class VCSolver : public mlgpu_solver {
         L[l].e = A.get<float>(n);
         L[l].r = A.get<float>(n);
         L[l].t = A.get<float>(n);
+        if (g.dim == 2) {
+          L[l].fcx = A.get<float>(nfaces(g, 0));
+          L[l].fcy = A.get<float>(nfaces(g, 1));
+          L[l].flam = A.get<float>(n);
+          L[l].fdiag = A.get<float>(n);
+        }
       } else {
         L[l].e = A.get<double>(n);
         L[l].r = A.get<double>(n);
@@ -237,7 +244,9 @@ class VCSolver : public mlgpu_solver {
       g = coarsen_grid(g);
     }
     use_block_cycle = o.relax_mode == MLGPU_RELAX_GSRB && o.num_mg == 1 && o.fuse_levels;
-    use_tiles = use_block_cycle;
+    // FP32 tiles pay for their halo recomputation; FP64 tiles (4 extra half
+    // sweeps of redundant FP64 work per tile) only when asked for explicitly
+    use_tiles = use_block_cycle && (mixed || o.fuse_levels >= 2);
     size_t n0 = ncells(op.grid);
     phi[0] = A.get<double>(n0);
     phi[1] = A.get<double>(n0);
@@ -263,6 +272,8 @@ class VCSolver : public mlgpu_solver {
         for (int d = 0; d < lv.G.dim; d++)
           CK(launch_convert<float, double>(lv.G.nface(d), lv.c32.b[d], lv.c64.b[d], s));
       }
+      int rc = build_fast();
+      if (rc) return rc;
     } else {
       int rc = build_lambda();
       if (rc) return rc;
@@ -281,6 +292,17 @@ class VCSolver : public mlgpu_solver {
         u += visits[l] * ((o.num_smooth_down + o.num_smooth_up) * n + n);
     }
     updates_per_iter = u + (double)L[0].G.ncell;  // + outer residual
+    return MLGPU_OK;
+  }
+
+  // FP32 coefficients of the lean tile smoother (2D mixed precision)
+  int build_fast() {
+    for (size_t l = 0; l < L.size(); l++) {
+      if (!L[l].fcx) continue;
+      VCArgs<double> A = args<double>((int)l);
+      A.lam = nullptr;
+      CK(launch_fast_coefs(A, L[l].fcx, L[l].fcy, L[l].flam, L[l].fdiag, s));
+    }
     return MLGPU_OK;
   }
 
@@ -370,6 +392,29 @@ class VCSolver : public mlgpu_solver {
       P.halo = chunk + (P.rc ? 1 : 0);
       P.prolong = (first && with_prolong) ? o.prolong : -1;
       P.ec = with_prolong ? (const T *)L[l + 1].ecur : nullptr;
+      if constexpr (sizeof(T) == 4) {
+        if (L[l].fcx) {
+          // lean FP32 form with precomputed face weights and 1/diag
+          TileFast F;
+          F.G = P.A.G;
+          F.bc = P.A.bc;
+          F.K = FastCoefs{L[l].fcx, L[l].fcy, L[l].flam, L[l].fdiag};
+          F.e_in = P.e_in;
+          F.e_out = P.e_out;
+          F.r = P.r;
+          F.zero_init = P.zero_init;
+          F.n_half = P.n_half;
+          F.pass0 = P.pass0;
+          F.halo = P.halo;
+          F.rc = P.rc;
+          F.prolong = P.prolong;
+          F.ec = P.ec;
+          CK(launch_vc_tile_fast(F, s));
+          first = false;
+          done += chunk;
+          continue;
+        }
+      }
       CK(launch_vc_tile_smooth<T>(P, s));
       first = false;
       done += chunk;
@@ -573,9 +618,8 @@ class VCSolver : public mlgpu_solver {
     op.alpha = a;
     op.beta = b;
     drop_graphs();
-    if (mixed) return MLGPU_OK;
     if (enter()) return MLGPU_ERR_CUDA;
-    int rc = build_lambda();
+    int rc = mixed ? build_fast() : build_lambda();
     if (!rc) rc = leave();
     return rc;
   }
