@@ -256,6 +256,16 @@ int mlgpu_vc_relax(const mlgpu_vcop *op, void *phi, const void *rhs,
                    int n_sweeps, void *stream);
 int mlgpu_vc_jacobi(const mlgpu_vcop *op, void *phi, const void *rhs,
                     void *tmp, void *stream);
+/* mlgpu_vc_jacobi without the caller's `tmp`: the temporary field lives in a
+   fixed 8 MiB device array of the library, so the call allocates nothing.  No
+   counterpart in the reference (its levelJacobi builds a temporary LevelData
+   per call); it serves hosts that cannot allocate device memory.  At most
+   1,048,576 FP64 / 2,097,152 FP32 cells (else MLGPU_ERR_SCRATCH, nothing
+   launched).  One scratch per device: calls that may overlap in time on one
+   device race.  The first call on a device looks the scratch up and should
+   come before any stream capture. */
+int mlgpu_vc_jacobi_noalloc(const mlgpu_vcop *op, void *phi, const void *rhs,
+                            void *stream);
 int mlgpu_vc_lambda(const mlgpu_vcop *op, void *lambda, void *stream);
 /* RESTRICTRESDB (F.ChF:427-505), homogeneous BCs. */
 int mlgpu_vc_restrict_residual(const mlgpu_vcop *op, void *res_coarse,

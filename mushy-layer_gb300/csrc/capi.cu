@@ -72,7 +72,7 @@ static bool valid_nlop(const mlgpu_nlop *op) {
   return true;
 }
 
-static bool valid_vcop(const mlgpu_vcop *op) {
+bool valid_vcop(const mlgpu_vcop *op) {
   if (!op || !valid_grid(&op->grid)) return false;
   if (op->dtype != MLGPU_F64 && op->dtype != MLGPU_F32) return false;
   for (int d = 0; d < op->grid.dim; d++)

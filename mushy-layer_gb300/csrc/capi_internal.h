@@ -12,6 +12,7 @@
 namespace mlgpu {
 
 bool valid_grid(const mlgpu_grid *g);
+bool valid_vcop(const mlgpu_vcop *op);
 template <class T> NLArgs<T> make_nl_args(const mlgpu_nlop &op);
 template <class T> VCArgs<T> make_vc_args(const mlgpu_vcop &op);
 int status_of(cudaError_t e);

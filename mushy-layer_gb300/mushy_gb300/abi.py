@@ -158,6 +158,7 @@ def _declare(lib):
         "mlgpu_vc_gsrb_pass": (i, [P(VCOp), vp, vp, i, vp]),
         "mlgpu_vc_relax": (i, [P(VCOp), vp, vp, i, vp]),
         "mlgpu_vc_jacobi": (i, [P(VCOp), vp, vp, vp, vp]),
+        "mlgpu_vc_jacobi_noalloc": (i, [P(VCOp), vp, vp, vp]),
         "mlgpu_vc_lambda": (i, [P(VCOp), vp, vp]),
         "mlgpu_vc_restrict_residual": (i, [P(VCOp), vp, vp, vp, vp]),
         "mlgpu_mac_divergence": (i, [P(Grid), vp, vp * 3, vp]),

@@ -27,6 +27,7 @@ UNITS = {
     "launch_f32.cu": [],
     "capi.cu": ["--fmad=false"],
     "solver.cu": ["--fmad=false"],
+    "capi_noalloc.cu": ["--fmad=false"],
 }
 
 
