@@ -7,6 +7,7 @@
 #include "cycle_kernels.cuh"
 #include "tile_kernels.cuh"
 #include "tile_fast_kernels.cuh"
+#include "cycle_fast_kernels.cuh"
 #include "outer_kernels.cuh"
 
 namespace mlgpu {

@@ -4,6 +4,7 @@
 #define MLGPU_FP32_UNIT 1
 #include "launch_impl.cuh"
 #include "tile_fast_kernels.cuh"
+#include "cycle_fast_kernels.cuh"
 
 namespace mlgpu {
 
@@ -48,18 +49,20 @@ template cudaError_t launch_vc_block_cycle<float>(const VCBlockCycle<float> &, c
 template cudaError_t launch_vc_tile_smooth<float>(const TileSmooth<float> &, cudaStream_t);
 
 cudaError_t launch_vc_tile_fast(const TileFast &P, cudaStream_t s) {
-  static bool attr_set = false;
-  if (!attr_set) {
-    cudaError_t e = cudaFuncSetAttribute(vc_tile_fast_kernel,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)kMaxDynSmem);
-    if (e != cudaSuccess) return e;
-    attr_set = true;
-  }
-  size_t bytes = tile_fast_smem_bytes(P.halo);
-  if (bytes > kMaxDynSmem) return cudaErrorInvalidValue;
-  dim3 grid((P.G.n0 + kTileX - 1) / kTileX, (P.G.n1 + kTileY - 1) / kTileY);
-  vc_tile_fast_kernel<<<grid, dim3(kTileTX, kTileTY), bytes, s>>>(P);
+  if (P.G.dim != 2 || P.halo < 1 || P.halo > kTFMaxHalo) return cudaErrorInvalidValue;
+  if (P.halo < P.n_half + (P.rc ? 1 : 0)) return cudaErrorInvalidValue;
+  const int te = tile_fast_edge(P.halo);
+  dim3 grid((P.G.n0 + te - 1) / te, (P.G.n1 + te - 1) / te);
+  vc_tile_fast_kernel<<<grid, dim3(kTFThreadsX, kTFThreadsY), 0, s>>>(P);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_vc_cycle_fast(const CycFast &P, cudaStream_t s) {
+  if (P.nlev < 2 || P.nlev > kFastCycLevels || P.G[0].dim != 2) return cudaErrorInvalidValue;
+  if ((P.G[0].n0 / 2) * (P.G[0].n1 / 2) > kFastCycThreads) return cudaErrorInvalidValue;
+  size_t bytes = cyc_fast_smem_bytes(P);
+  if (bytes > 48 * 1024) return cudaErrorInvalidValue;
+  vc_cycle_fast_kernel<<<1, kFastCycThreads, bytes, s>>>(P);
   return cudaGetLastError();
 }
 

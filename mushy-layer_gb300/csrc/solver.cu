@@ -367,7 +367,7 @@ class VCSolver : public mlgpu_solver {
   // split into several launches when the halo would not fit in shared memory
   template <class T>
   int tile_sweeps(int l, int nh, bool zero, bool with_restrict, bool with_prolong) {
-    const int hmax = tile_max_halo(sizeof(T));
+    const int hmax = (sizeof(T) == 4 && L[l].fcx) ? kTFMaxHalo : tile_max_halo(sizeof(T));
     int done = 0;
     bool first = true;
     do {
@@ -439,6 +439,29 @@ class VCSolver : public mlgpu_solver {
     if (use_block_cycle && L[l].G.ncell <= kBlockCycleCells && last - l + 1 <= kMaxBlockLevels &&
         last > l) {
       // this level and every coarser one inside one thread block
+      if constexpr (sizeof(T) == 4) {
+        const Geom &G0 = L[l].G;
+        if (L[l].fcx && last - l + 1 <= kFastCycLevels &&
+            (G0.n0 / 2) * (G0.n1 / 2) <= kFastCycThreads) {
+          // lean FP32 form with the precomputed face weights and 1/diag
+          CycFast F;
+          F.nlev = last - l + 1;
+          F.pre = o.num_smooth_down;
+          F.post = o.num_smooth_up;
+          F.bottom = o.bottom_max_iter;
+          F.prolong = o.prolong;
+          F.zero_init = zero_init ? 1 : 0;
+          F.bc = make_bcd(op.bc);
+          for (int m = 0; m < F.nlev; m++) {
+            F.G[m] = L[l + m].G;
+            F.K[m] = FastCoefs{L[l + m].fcx, L[l + m].fcy, L[l + m].flam, L[l + m].fdiag};
+          }
+          F.e0 = (float *)L[l].e;
+          F.r0 = (const float *)L[l].r;
+          CK(launch_vc_cycle_fast(F, s));
+          return MLGPU_OK;
+        }
+      }
       VCBlockCycle<T> P;
       P.nlev = last - l + 1;
       P.pre = o.num_smooth_down;

@@ -5,11 +5,20 @@
 // and diag = alpha a - beta c + sum_f c_f (resetLambda's diagonal), the
 // Gauss-Seidel update e - lambda (L e - r) with lambda = 1/diag is, in exact
 // arithmetic, lambda (r + sum_f c_f e_nb(f)); a homogeneous boundary ghost
-// s e (s = -1 Dirichlet, +1 Neumann) contributes c_f s e.  That form needs
-// four fused multiply-adds per update instead of the reference expression's
+// g e (g = -1 Dirichlet, +1 Neumann) contributes c_f g e.  That form needs
+// five fused multiply-adds per update instead of the reference expression's
 // dozen operations.  It is used only inside FP32 cycles, whose result the
 // FP64 defect correction re-checks; FP64 cycles keep the reference's exact
 // expression (tile_kernels.cuh) and its bits.
+//
+// Block layout: a 32 x 32 cell region in shared memory (correction only) =
+// a (32 - 2H)^2 interior tile + a halo of H cells, H >= the number of half
+// sweeps (+1 when the launch also restricts the residual).  Thread (tx, ty)
+// owns the horizontal pair of cells (2tx, 2tx+1) of row ty: exactly one of the
+// two has the colour of any given pass, so every thread updates one cell per
+// half sweep.  Each cell's right-hand side, 1/diag, face weights and its
+// boundary-ghost weight stay in registers for the whole launch; a half sweep
+// is five shared-memory loads, five FMAs and one store per thread.
 #pragma once
 #include "tile_kernels.cuh"
 
@@ -36,10 +45,11 @@ struct TileFast {
   const float *ec;
 };
 
-inline size_t tile_fast_smem_bytes(int halo) {
-  size_t lx = kTileX + 2 * halo, ly = kTileY + 2 * halo;
-  return sizeof(float) * (3 * lx * ly + (lx + 1) * ly + lx * (ly + 1));
-}
+constexpr int kTF = 32;                     // shared region edge (cells)
+constexpr int kTFThreadsX = kTF / 2, kTFThreadsY = kTF;
+constexpr int kTFMaxHalo = 12;              // interior edge >= 8
+// interior edge of a tile with halo h
+__host__ __device__ inline int tile_fast_edge(int h) { return kTF - 2 * h; }
 
 // homogeneous ghost factor of side s of direction d (comp 0)
 __device__ __forceinline__ float ghost_factor(const BCD &bc, int d, int s) {
@@ -47,151 +57,151 @@ __device__ __forceinline__ float ghost_factor(const BCD &bc, int d, int s) {
 }
 
 #ifdef MLGPU_FP32_UNIT  // kernels compiled in launch_f32.cu only
-__global__ void __launch_bounds__(kTileThreads) vc_tile_fast_kernel(TileFast P) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
+struct TFCell {
+  int c, lx;        // shared-memory index, local x
+  bool valid;       // maps to a domain cell (after periodic wrap)
+  float e, r, lam, diag;
+  float kself, ke, kw, kn, ks;  // ghost weight on e itself; neighbour weights
+};
+
+__device__ __forceinline__ void tf_setup(const TileFast &P, int lx, int ly, int gx0, int gy0,
+                                         bool inside, float *se, TFCell &k) {
   const Geom &G = P.G;
-  const int H = P.halo;
-  const int LX = kTileX + 2 * H, LY = kTileY + 2 * H;
-  float *se = (float *)smem_raw;
-  float *sr = se + LX * LY;
-  float *sl = sr + LX * LY;
-  float *scx = sl + LX * LY;         // (LX+1) x LY
-  float *scy = scx + (LX + 1) * LY;  // LX x (LY+1)
-  const int x0 = blockIdx.x * kTileX, y0 = blockIdx.y * kTileY;
+  const int n0 = G.n0, n1 = G.n1;
+  int gx = gx0 + lx, gy = gy0 + ly;
+  k.c = ly * kTF + lx;
+  k.lx = lx;
+  k.valid = true;
+  if (!inside) {
+    if (gx < 0 || gx >= n0) {
+      if (G.per0)
+        gx = ((gx % n0) + n0) % n0;
+      else
+        k.valid = false;
+    }
+    if (gy < 0 || gy >= n1) {
+      if (G.per1)
+        gy = ((gy % n1) + n1) % n1;
+      else
+        k.valid = false;
+    }
+  }
+  float ev = 0.f;
+  k.r = k.lam = k.diag = 0.f;
+  k.kself = k.ke = k.kw = k.kn = k.ks = 0.f;
+  if (k.valid) {
+    const long long q = (long long)gy * n0 + gx;
+    if (!P.zero_init) ev = P.e_in[q];
+    k.r = P.r[q];
+    k.lam = P.K.lam[q];
+    if (P.rc) k.diag = P.K.diag[q];
+    if (P.prolong == MLGPU_PROLONG_LINEAR)
+      ev = prolong_add<float, 2, MLGPU_PROLONG_LINEAR>(coarsen_geom(G), P.bc, 0, gx, gy, 0, ev,
+                                                        P.ec, nullptr);
+    else if (P.prolong == MLGPU_PROLONG_CONSTANT)
+      ev = ev + P.ec[(long long)(gy >> 1) * (n0 >> 1) + (gx >> 1)];
+    // the cell's own faces (periodic seams included)
+    const long long fx = (long long)gy * (n0 + 1) + gx;
+    k.ke = P.K.cx[fx + 1];
+    k.kw = P.K.cx[fx];
+    k.kn = P.K.cy[q + n0];
+    k.ks = P.K.cy[q];
+    // a non-periodic boundary face: the ghost is g e of this cell
+    if (!inside) {
+      if (!G.per0 && gx == n0 - 1) {
+        k.kself += ghost_factor(P.bc, 0, 1) * k.ke;
+        k.ke = 0.f;
+      }
+      if (!G.per0 && gx == 0) {
+        k.kself += ghost_factor(P.bc, 0, 0) * k.kw;
+        k.kw = 0.f;
+      }
+      if (!G.per1 && gy == n1 - 1) {
+        k.kself += ghost_factor(P.bc, 1, 1) * k.kn;
+        k.kn = 0.f;
+      }
+      if (!G.per1 && gy == 0) {
+        k.kself += ghost_factor(P.bc, 1, 0) * k.ks;
+        k.ks = 0.f;
+      }
+    }
+  }
+  k.e = ev;
+  se[k.c] = ev;
+}
+
+// sum_f c_f e_nb(f), ghosts included
+__device__ __forceinline__ float tf_nbsum(const TFCell &k, const float *se) {
+  float s = k.kself * k.e;
+  s = fmaf(k.ke, se[k.c + 1], s);
+  s = fmaf(k.kw, se[k.c - 1], s);
+  s = fmaf(k.kn, se[k.c + kTF], s);
+  s = fmaf(k.ks, se[k.c - kTF], s);
+  return s;
+}
+
+// half sweep h updates the cells of [h+1, kTF-2-h]^2 that exist
+__device__ __forceinline__ void tf_update(TFCell &k, int ly, int h, float *se) {
+  const int lo = h + 1, hi = kTF - 2 - h;
+  if (k.valid && k.lx >= lo && k.lx <= hi && ly >= lo && ly <= hi) {
+    k.e = k.lam * (k.r + tf_nbsum(k, se));
+    se[k.c] = k.e;
+  }
+}
+
+__global__ void __launch_bounds__(kTFThreadsX *kTFThreadsY) vc_tile_fast_kernel(TileFast P) {
+  __shared__ float se[kTF * kTF];
+  __shared__ float sres[kTF * kTF];
+  const Geom &G = P.G;
+  const int H = P.halo, TE = tile_fast_edge(H);
+  const int x0 = blockIdx.x * TE, y0 = blockIdx.y * TE;
   const int gx0 = x0 - H, gy0 = y0 - H;
   const int n0 = G.n0, n1 = G.n1;
-  const bool px = G.per0 != 0, py = G.per1 != 0;
-  const int tx = threadIdx.x, ty = threadIdx.y;
-  const bool inside = gx0 >= 0 && gx0 + LX <= n0 && gy0 >= 0 && gy0 + LY <= n1;
-  const float *cxg = P.K.cx, *cyg = P.K.cy;
-
-  auto gxw = [&](int gx) -> int {
-    if (gx >= 0 && gx < n0) return gx;
-    if (!px) return -1;
-    return ((gx % n0) + n0) % n0;
-  };
-  auto gyw = [&](int gy) -> int {
-    if (gy >= 0 && gy < n1) return gy;
-    if (!py) return -1;
-    return ((gy % n1) + n1) % n1;
-  };
-
-  // ---- load scaled faces, then cells
-  for (int ly = ty; ly < LY; ly += kTileTY)
-    for (int lx = tx; lx <= LX; lx += kTileTX) {
-      float v = 0.f;
-      int gy = inside ? gy0 + ly : gyw(gy0 + ly);
-      if (gy >= 0) {
-        int fx = gx0 + lx;
-        if (fx < 0 || fx > n0) fx = px ? ((fx % n0) + n0) % n0 : -1;
-        if (fx >= 0) v = cxg[(long long)gy * (n0 + 1) + fx];
-      }
-      scx[ly * (LX + 1) + lx] = v;
-    }
-  for (int ly = ty; ly <= LY; ly += kTileTY)
-    for (int lx = tx; lx < LX; lx += kTileTX) {
-      float v = 0.f;
-      int gx = inside ? gx0 + lx : gxw(gx0 + lx);
-      if (gx >= 0) {
-        int fy = gy0 + ly;
-        if (fy < 0 || fy > n1) fy = py ? ((fy % n1) + n1) % n1 : -1;
-        if (fy >= 0) v = cyg[(long long)fy * n0 + gx];
-      }
-      scy[ly * LX + lx] = v;
-    }
-  const Geom Cg = coarsen_geom(G);
-  for (int ly = ty; ly < LY; ly += kTileTY)
-    for (int lx = tx; lx < LX; lx += kTileTX) {
-      int q = ly * LX + lx;
-      int gx = inside ? gx0 + lx : gxw(gx0 + lx), gy = inside ? gy0 + ly : gyw(gy0 + ly);
-      float ev = 0.f, rv = 0.f, lv = 0.f;
-      if (gx >= 0 && gy >= 0) {
-        long long gq = (long long)gy * n0 + gx;
-        if (!P.zero_init) ev = P.e_in[gq];
-        rv = P.r[gq];
-        lv = P.K.lam[gq];
-        if (P.prolong == MLGPU_PROLONG_LINEAR)
-          ev = prolong_add<float, 2, MLGPU_PROLONG_LINEAR>(Cg, P.bc, 0, gx, gy, 0, ev, P.ec, nullptr);
-        else if (P.prolong == MLGPU_PROLONG_CONSTANT)
-          ev = prolong_add<float, 2, MLGPU_PROLONG_CONSTANT>(Cg, P.bc, 0, gx, gy, 0, ev, P.ec, nullptr);
-      }
-      se[q] = ev;
-      sr[q] = rv;
-      sl[q] = lv;
-    }
+  const bool inside = gx0 >= 0 && gx0 + kTF <= n0 && gy0 >= 0 && gy0 + kTF <= n1;
+  const int ly = threadIdx.y;
+  // A: the cell of the pair with the colour of pass0, B: the other one
+  const int odd = (gx0 + gy0 + ly + P.pass0) & 1;
+  TFCell A, B;
+  tf_setup(P, 2 * threadIdx.x + odd, ly, gx0, gy0, inside, se, A);
+  tf_setup(P, 2 * threadIdx.x + 1 - odd, ly, gx0, gy0, inside, se, B);
   __syncthreads();
 
-  // sum_f c_f e_nb(f) at local (lx, ly), global wrapped (gx, gy)
-  auto nbsum = [&](int lx, int ly, int gx, int gy) -> float {
-    int c = ly * LX + lx, fc = ly * (LX + 1) + lx;
-    if (inside) {
-      float s = scx[fc + 1] * se[c + 1];
-      s = fmaf(scx[fc], se[c - 1], s);
-      s = fmaf(scy[c + LX], se[c + LX], s);
-      s = fmaf(scy[c], se[c - LX], s);
-      return s;
-    }
-    float p0 = se[c];
-    // seam faces of periodic directions come from the cell's own entries
-    float cxh = (px && gx == n0 - 1) ? cxg[(long long)gy * (n0 + 1) + n0] : scx[fc + 1];
-    float cxl = (px && gx == 0) ? cxg[(long long)gy * (n0 + 1)] : scx[fc];
-    float cyh = (py && gy == n1 - 1) ? cyg[(long long)n1 * n0 + gx] : scy[c + LX];
-    float cyl = (py && gy == 0) ? cyg[gx] : scy[c];
-    float hi0 = (gx0 + lx + 1 >= n0 && !px) ? ghost_factor(P.bc, 0, 1) * p0 : se[c + 1];
-    float lo0 = (gx0 + lx - 1 < 0 && !px) ? ghost_factor(P.bc, 0, 0) * p0 : se[c - 1];
-    float hi1 = (gy0 + ly + 1 >= n1 && !py) ? ghost_factor(P.bc, 1, 1) * p0 : se[c + LX];
-    float lo1 = (gy0 + ly - 1 < 0 && !py) ? ghost_factor(P.bc, 1, 0) * p0 : se[c - LX];
-    float s = cxh * hi0;
-    s = fmaf(cxl, lo0, s);
-    s = fmaf(cyh, hi1, s);
-    s = fmaf(cyl, lo1, s);
-    return s;
-  };
-
-  for (int h = 0; h < P.n_half; h++) {
-    const int pass = (P.pass0 + h) & 1;
-    const int lo = h + 1, hx = LX - 2 - h, hy = LY - 2 - h;
-    for (int ly = lo + ty; ly <= hy; ly += kTileTY) {
-      const int gy = gy0 + ly;
-      const int xs = lo + ((gx0 + lo + gy + pass) & 1);
-      for (int lx = xs + 2 * tx; lx <= hx; lx += 2 * kTileTX) {
-        const int c = ly * LX + lx;
-        int gxv = gx0 + lx, gyv = gy;
-        if (!inside) {
-          gxv = gxw(gxv);
-          gyv = gyw(gyv);
-          if (gxv < 0 || gyv < 0) continue;
-        }
-        se[c] = sl[c] * (sr[c] + nbsum(lx, ly, gxv, gyv));
-      }
-    }
+  for (int h = 0; h < P.n_half; h += 2) {
+    tf_update(A, ly, h, se);
     __syncthreads();
+    if (h + 1 < P.n_half) {
+      tf_update(B, ly, h + 1, se);
+      __syncthreads();
+    }
   }
 
-  for (int iy = ty; iy < kTileY; iy += kTileTY)
-    for (int ix = tx; ix < kTileX; ix += kTileTX) {
-      int gx = x0 + ix, gy = y0 + iy;
-      if (gx < n0 && gy < n1) P.e_out[(long long)gy * n0 + gx] = se[(iy + H) * LX + ix + H];
-    }
-
-  // residual r - diag e + sum c e_nb, averaged onto the coarse cell
+  // interior cells: store; residual r - diag e + sum c e_nb for the restriction
+  const bool row_in = ly >= H && ly < H + TE && gy0 + ly < n1;
+  const bool a_in = row_in && A.lx >= H && A.lx < H + TE && gx0 + A.lx < n0;
+  const bool b_in = row_in && B.lx >= H && B.lx < H + TE && gx0 + B.lx < n0;
+  const long long grow = (long long)(gy0 + ly) * n0 + gx0;
+  if (a_in) P.e_out[grow + A.lx] = A.e;
+  if (b_in) P.e_out[grow + B.lx] = B.e;
   if (P.rc) {
-    const int cn0 = n0 >> 1, cn1 = n1 >> 1;
-    for (int J = ty; J < kTileY / 2; J += kTileTY)
-      for (int I = tx; I < kTileX / 2; I += kTileTX) {
-        int CI = (x0 >> 1) + I, CJ = (y0 >> 1) + J;
-        if (CI >= cn0 || CJ >= cn1) continue;
+    if (a_in) sres[A.c] = (A.r + tf_nbsum(A, se)) - A.diag * A.e;
+    if (b_in) sres[B.c] = (B.r + tf_nbsum(B, se)) - B.diag * B.e;
+    __syncthreads();
+    const int half = TE / 2;
+    const int t = threadIdx.y * kTFThreadsX + threadIdx.x;
+    if (t < half * half) {
+      const int I = t % half, J = t / half;
+      const int CI = (x0 >> 1) + I, CJ = (y0 >> 1) + J;
+      const int cn0 = n0 >> 1, cn1 = n1 >> 1;
+      if (CI < cn0 && CJ < cn1) {
         float acc = 0.f;
         for (int jj = 0; jj < 2; jj++)
           for (int ii = 0; ii < 2; ii++) {
-            int gx = 2 * CI + ii, gy = 2 * CJ + jj;
-            int lx = gx - gx0, ly = gy - gy0;
-            int c = ly * LX + lx;
-            float res = sr[c] - P.K.diag[(long long)gy * n0 + gx] * se[c] + nbsum(lx, ly, gx, gy);
+            float res = sres[(H + 2 * J + jj) * kTF + H + 2 * I + ii];
             acc = acc + res * 0.25f;
           }
         P.rc[(long long)CJ * cn0 + CI] = acc;
       }
+    }
   }
 }
 
