@@ -9,6 +9,7 @@
 #include "tile_fast_kernels.cuh"
 #include "cycle_fast_kernels.cuh"
 #include "outer_kernels.cuh"
+#include "outer_fast_kernels.cuh"
 
 namespace mlgpu {
 
@@ -32,6 +33,9 @@ cudaError_t launch_mac_correct(const Geom &G, const BCD &bc, int d, const double
                                const double *scale, double *u, cudaStream_t s);
 cudaError_t launch_be_rhs(long long n, const double *phi_old, const double *a, const double *src,
                           double dt, double *rhs, cudaStream_t s);
+cudaError_t launch_vc_outer_fast(const OuterFast &P, int norm, cudaStream_t s);
+cudaError_t launch_outer_coefs(const VCArgs<double> &A, double *cx, double *cy, double *diag,
+                               cudaStream_t s);
 cudaError_t launch_outer_decide(OuterDev *st, const double *norm, const OuterCfg &c,
                                 cudaGraphConditionalHandle h, cudaStream_t s);
 

@@ -3,6 +3,7 @@
 // reference's Fortran, so FP64 results match the CPU restatement bit for bit.
 #define MLGPU_FP64_UNIT 1
 #include "launch_impl.cuh"
+#include "outer_fast_kernels.cuh"
 
 namespace mlgpu {
 
@@ -29,6 +30,23 @@ template cudaError_t launch_vc_update_residual<double, float>(const VCArgs<doubl
                                                               const double *, double *, double *,
                                                               float *, double *, cudaStream_t,
                                                               const int *);
+
+cudaError_t launch_vc_outer_fast(const OuterFast &P, int norm, cudaStream_t s) {
+  if (P.G.dim != 2 || !P.count || !P.part || !P.res_inner) return cudaErrorInvalidValue;
+  long long tiles = (long long)((P.G.n0 + kOTX - 1) / kOTX) * ((P.G.n1 + kOTY - 1) / kOTY);
+  int grid = (int)(tiles < kMaxBlocks ? tiles : kMaxBlocks);
+  MLGPU_NORM_SWITCH(norm, (vc_outer_fast_kernel<NORM><<<grid, kOTThreads, 0, s>>>(P)));
+  return cudaGetLastError();
+}
+
+cudaError_t launch_outer_coefs(const VCArgs<double> &A, double *cx, double *cy, double *diag,
+                               cudaStream_t s) {
+  if (A.G.dim != 2) return cudaErrorInvalidValue;
+  long long n = A.G.nface(0) > A.G.ncell ? A.G.nface(0) : A.G.ncell;
+  if (A.G.nface(1) > n) n = A.G.nface(1);
+  outer_coefs_kernel<<<blocks_for(n), kBlock, 0, s>>>(A, cx, cy, diag);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_outer_decide(OuterDev *st, const double *norm, const OuterCfg &c,
                                 cudaGraphConditionalHandle h, cudaStream_t s) {

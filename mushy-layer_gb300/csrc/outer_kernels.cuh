@@ -22,9 +22,9 @@ struct OuterCfg {
 };
 
 #ifdef MLGPU_FP64_UNIT  // defined once, in launch_f64.cu
-__global__ void outer_decide_kernel(OuterDev *st, const double *__restrict__ norm_in, OuterCfg c,
-                                    cudaGraphConditionalHandle h) {
-  double norm = norm_in[0];
+// the host loop's tests after one outer iteration with residual norm `norm`
+__device__ __forceinline__ void outer_decide_step(OuterDev *st, double norm, const OuterCfg &c,
+                                                  cudaGraphConditionalHandle h) {
   int iter = st->iter + 1;
   st->iter = iter;
   st->norm = norm;
@@ -43,6 +43,11 @@ __global__ void outer_decide_kernel(OuterDev *st, const double *__restrict__ nor
              status == 0;
   st->cont = cont;
   cudaGraphSetConditional(h, cont ? 1u : 0u);
+}
+
+__global__ void outer_decide_kernel(OuterDev *st, const double *__restrict__ norm_in, OuterCfg c,
+                                    cudaGraphConditionalHandle h) {
+  outer_decide_step(st, norm_in[0], c, h);
 }
 #endif
 

@@ -161,6 +161,7 @@ struct VCLevel {
   void *ecur = nullptr;  // which of e / t holds the correction after the last pass
   double *lam64 = nullptr;  // stored 1/diag for FP64 inner cycles
   float *fcx = nullptr, *fcy = nullptr, *flam = nullptr, *fdiag = nullptr;  // lean FP32 tiles
+  double *ocx = nullptr, *ocy = nullptr, *odiag = nullptr;  // FP64 outer step (level 0, mixed)
 };
 
 class VCSolver : public mlgpu_solver {
@@ -227,6 +228,11 @@ class VCSolver : public mlgpu_solver {
         L[l].e = A.get<float>(n);
         L[l].r = A.get<float>(n);
         L[l].t = A.get<float>(n);
+        if (g.dim == 2 && l == 0) {
+          L[l].ocx = A.get<double>(nfaces(g, 0));
+          L[l].ocy = A.get<double>(nfaces(g, 1));
+          L[l].odiag = A.get<double>(n);
+        }
         if (g.dim == 2) {
           L[l].fcx = A.get<float>(nfaces(g, 0));
           L[l].fcy = A.get<float>(nfaces(g, 1));
@@ -295,8 +301,10 @@ class VCSolver : public mlgpu_solver {
     return MLGPU_OK;
   }
 
-  // FP32 coefficients of the lean tile smoother (2D mixed precision)
+  // FP32 coefficients of the lean tile smoother and FP64 ones of the outer
+  // step (2D mixed precision)
   int build_fast() {
+    if (L[0].ocx) CK(launch_outer_coefs(outer_args(), L[0].ocx, L[0].ocy, L[0].odiag, s));
     for (size_t l = 0; l < L.size(); l++) {
       if (!L[l].fcx) continue;
       VCArgs<double> A = args<double>((int)l);
@@ -312,6 +320,40 @@ class VCSolver : public mlgpu_solver {
       A.lam = nullptr;
       CK(launch_vc_lambda<double>(A, L[l].lam64, s));
     }
+    return MLGPU_OK;
+  }
+
+  // level-0 FP64 operator on the caller's coefficient arrays
+  VCArgs<double> outer_args() {
+    VCArgs<double> A = args<double>(0);
+    A.a = (const double *)op.aCoef;
+    A.c = (const double *)op.cCoef;
+    for (int d = 0; d < 3; d++) A.b[d] = (const double *)op.bCoef[d];
+    A.lam = nullptr;
+    return A;
+  }
+
+  // mixed 2D: phi_out = phi_in + e, FP64 residual, FP32 copy, norm (and, with
+  // `st`, the outer-loop decision) in one launch; the norm lands in
+  // part[kMaxBlocks]
+  int outer_fast(const double *phi_in, const float *e, double *phi_out, const int *par,
+                 OuterDev *st, cudaGraphConditionalHandle h) {
+    OuterFast P;
+    P.G = L[0].G;
+    P.bc = make_bcd(op.bc);
+    P.K = OuterCoefs{L[0].ocx, L[0].ocy, L[0].odiag};
+    P.phi = phi_in;
+    P.e = e;
+    P.rhs = rhs;
+    P.out_phi = phi_out;
+    P.res_inner = (float *)L[0].r;
+    P.part = part;
+    P.count = (unsigned *)(part + kMaxBlocks + 1);
+    P.par = par;
+    P.st = st;
+    P.cfg = OuterCfg{o.tolerance, o.hang, o.norm_thresh, o.max_iter};
+    P.h = h;
+    CK(launch_vc_outer_fast(P, o.norm_type, s));
     return MLGPU_OK;
   }
 
@@ -508,6 +550,14 @@ class VCSolver : public mlgpu_solver {
       rc = mixed ? cycle<float>(0, c == 0) : cycle<double>(0, c == 0);
       if (rc) return rc;
     }
+    if (L[0].ocx) {
+      int rc2 = outer_fast(phi[from], (const float *)L[0].ecur, phi[1 - from], par,
+                           par ? dev_state : nullptr, h);
+      if (rc2) return rc2;
+      if (!par)
+        CK(cudaMemcpyAsync(host_norm, part + kMaxBlocks, sizeof(double), cudaMemcpyDeviceToHost, s));
+      return MLGPU_OK;
+    }
     VCArgs<double> A = args<double>(0);
     A.a = (const double *)op.aCoef;
     A.c = (const double *)op.cCoef;
@@ -587,13 +637,18 @@ class VCSolver : public mlgpu_solver {
     A.a = (const double *)op.aCoef;
     A.c = (const double *)op.cCoef;
     for (int d = 0; d < 3; d++) A.b[d] = (const double *)op.bCoef[d];
-    if (mixed)
-      CK((launch_vc_update_residual<double, float>(A, o.norm_type, phi[0], nullptr, rhs, nullptr,
-                                                   nullptr, (float *)L[0].r, part, s)));
-    else
-      CK((launch_vc_update_residual<double, double>(A, o.norm_type, phi[0], nullptr, rhs, nullptr,
-                                                    nullptr, (double *)L[0].r, part, s)));
-    CK(launch_finalize_norm(o.norm_type, part, norm_parts(L[0].G.ncell), part + kMaxBlocks, s));
+    if (L[0].ocx) {
+      int rc0 = outer_fast(phi[0], nullptr, nullptr, nullptr, nullptr, 0);
+      if (rc0) return rc0;
+    } else {
+      if (mixed)
+        CK((launch_vc_update_residual<double, float>(A, o.norm_type, phi[0], nullptr, rhs, nullptr,
+                                                     nullptr, (float *)L[0].r, part, s)));
+      else
+        CK((launch_vc_update_residual<double, double>(A, o.norm_type, phi[0], nullptr, rhs, nullptr,
+                                                      nullptr, (double *)L[0].r, part, s)));
+      CK(launch_finalize_norm(o.norm_type, part, norm_parts(L[0].G.ncell), part + kMaxBlocks, s));
+    }
     CK(cudaMemcpyAsync(host_norm, part + kMaxBlocks, sizeof(double), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     Outer S;
@@ -917,6 +972,9 @@ int mlgpu_vc_solver_create(const mlgpu_vcop *op, const mlgpu_mg_options *o, void
     return MLGPU_ERR_CUDA;
   }
   int rc = S->enter();
+  // norm partials and the finished-block counter of the fused outer step
+  if (!rc && cudaMemsetAsync(S->part, 0, kNormScratchDoubles * sizeof(double), S->s) != cudaSuccess)
+    rc = MLGPU_ERR_CUDA;
   if (!rc) rc = S->build_coefs();
   if (!rc) rc = S->leave();
   if (rc) {
