@@ -59,10 +59,13 @@ cudaError_t launch_vc_tile_fast(const TileFast &P, cudaStream_t s) {
 
 cudaError_t launch_vc_cycle_fast(const CycFast &P, cudaStream_t s) {
   if (P.nlev < 2 || P.nlev > kFastCycLevels || P.G[0].dim != 2) return cudaErrorInvalidValue;
-  if ((P.G[0].n0 / 2) * (P.G[0].n1 / 2) > kFastCycThreads) return cudaErrorInvalidValue;
+  const int quads = (P.G[0].n0 / 2) * (P.G[0].n1 / 2);
+  if (quads > kFastCycThreads) return cudaErrorInvalidValue;
   size_t bytes = cyc_fast_smem_bytes(P);
   if (bytes > 48 * 1024) return cudaErrorInvalidValue;
-  vc_cycle_fast_kernel<<<1, kFastCycThreads, bytes, s>>>(P);
+  int threads = (quads + 31) / 32 * 32;
+  if (threads < 64) threads = 64;
+  vc_cycle_fast_kernel<<<1, threads, bytes, s>>>(P);
   return cudaGetLastError();
 }
 

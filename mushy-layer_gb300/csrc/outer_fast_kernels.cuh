@@ -44,7 +44,7 @@ struct OuterFast {
   cudaGraphConditionalHandle h;
 };
 
-constexpr int kOTX = 32, kOTY = 16, kOTThreads = 256;
+constexpr int kOTX = 32, kOTY = 32, kOTThreads = 256;
 constexpr int kOTLX = kOTX + 2, kOTLY = kOTY + 2;
 
 #ifdef MLGPU_FP64_UNIT  // kernels compiled in launch_f64.cu only
@@ -63,6 +63,7 @@ __global__ void __launch_bounds__(kOTThreads) vc_outer_fast_kernel(OuterFast P) 
   const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
   const int ntx = (n0 + kOTX - 1) / kOTX, nty = (n1 + kOTY - 1) / kOTY;
   double acc = 0.0;
+  bool bad = false;
   for (int tile = blockIdx.x; tile < ntx * nty; tile += gridDim.x) {
     const int x0 = (tile % ntx) * kOTX, y0 = (tile / ntx) * kOTY;
     for (int q = tid; q < kOTLX * kOTLY; q += kOTThreads) {
@@ -81,6 +82,9 @@ __global__ void __launch_bounds__(kOTThreads) vc_outer_fast_kernel(OuterFast P) 
       sp[q] = v;
     }
     __syncthreads();
+    // tiles away from non-periodic boundaries need no ghost values
+    const bool plain = (G.per0 || (x0 > 0 && x0 + kOTX < n0)) &&
+                       (G.per1 || (y0 > 0 && y0 + kOTY < n1));
 #pragma unroll
     for (int m = 0; m < kOTY / 8; m++) {
       const int gx = x0 + tx, gy = y0 + ty + 8 * m;
@@ -88,22 +92,35 @@ __global__ void __launch_bounds__(kOTThreads) vc_outer_fast_kernel(OuterFast P) 
       const int c = (ty + 8 * m + 1) * kOTLX + tx + 1;
       const long long g = (long long)gy * n0 + gx;
       const double p0 = sp[c];
-      const double ve = (gx + 1 < n0 || G.per0) ? sp[c + 1] : ghost_value<double>(P.bc, 0, 1, 0, p0, G.dx, false);
-      const double vw = (gx > 0 || G.per0) ? sp[c - 1] : ghost_value<double>(P.bc, 0, 0, 0, p0, G.dx, false);
-      const double vn = (gy + 1 < n1 || G.per1) ? sp[c + kOTLX] : ghost_value<double>(P.bc, 1, 1, 0, p0, G.dx, false);
-      const double vs = (gy > 0 || G.per1) ? sp[c - kOTLX] : ghost_value<double>(P.bc, 1, 0, 0, p0, G.dx, false);
+      double ve = sp[c + 1], vw = sp[c - 1], vn = sp[c + kOTLX], vs = sp[c - kOTLX];
+      if (!plain) {
+        if (gx + 1 >= n0 && !G.per0) ve = ghost_value<double>(P.bc, 0, 1, 0, p0, G.dx, false);
+        if (gx == 0 && !G.per0) vw = ghost_value<double>(P.bc, 0, 0, 0, p0, G.dx, false);
+        if (gy + 1 >= n1 && !G.per1) vn = ghost_value<double>(P.bc, 1, 1, 0, p0, G.dx, false);
+        if (gy == 0 && !G.per1) vs = ghost_value<double>(P.bc, 1, 0, 0, p0, G.dx, false);
+      }
       const long long fx = (long long)gy * (n0 + 1) + gx;
       double r = fma(-P.K.diag[g], p0, P.rhs[g]);
       r = fma(P.K.cx[fx + 1], ve, r);
       r = fma(P.K.cx[fx], vw, r);
       r = fma(P.K.cy[g + n0], vn, r);
       r = fma(P.K.cy[g], vs, r);
-      P.res_inner[g] = (float)r;
+      const float rf = (float)r;
+      P.res_inner[g] = rf;
       if (P.e) out[g] = p0;
-      acc = norm_accum<NORM>(acc, r);
+      if (NORM == MLGPU_NORM_MAX) {
+        // NaN / Inf: all exponent bits set (integer test); the FP64 max is
+        // then one operation
+        bad |= (__double2hiint(r) & 0x7ff00000) == 0x7ff00000;
+        acc = fmax(acc, fabs(r));
+      } else {
+        acc = norm_accum<NORM>(acc, r);
+      }
     }
     __syncthreads();
   }
+  if (NORM == MLGPU_NORM_MAX && __syncthreads_or(bad))
+    acc = __longlong_as_double(0x7ff8000000000000LL);
   double r = block_reduce<NORM>(acc);
   if (tid == 0) {
     P.part[blockIdx.x] = r;

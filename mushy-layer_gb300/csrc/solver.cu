@@ -471,14 +471,16 @@ class VCSolver : public mlgpu_solver {
     // a fresh correction starts in e; a continued one stays where the last
     // pass left it (the tile path alternates e / t, the other paths work in e)
     if (zero_init || !L[l].ecur) L[l].ecur = L[l].e;
-    if (use_tiles && l < last && L[l].G.dim == 2 && L[l].G.ncell > kBlockCycleCells) {
+    // the lean FP32 single-CTA cycle takes levels up to 1024 cells
+    const long long block_cells = (sizeof(T) == 4 && L[l].fcx) ? kFastCycCells : kBlockCycleCells;
+    if (use_tiles && l < last && L[l].G.dim == 2 && L[l].G.ncell > block_cells) {
       int rc = tile_sweeps<T>(l, 2 * o.num_smooth_down, zero_init, true, false);
       if (rc) return rc;
       rc = cycle<T>(l + 1, true);
       if (rc) return rc;
       return tile_sweeps<T>(l, 2 * o.num_smooth_up, false, false, true);
     }
-    if (use_block_cycle && L[l].G.ncell <= kBlockCycleCells && last - l + 1 <= kMaxBlockLevels &&
+    if (use_block_cycle && L[l].G.ncell <= block_cells && last - l + 1 <= kMaxBlockLevels &&
         last > l) {
       // this level and every coarser one inside one thread block
       if constexpr (sizeof(T) == 4) {
