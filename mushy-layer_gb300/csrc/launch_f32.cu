@@ -49,7 +49,7 @@ template cudaError_t launch_vc_block_cycle<float>(const VCBlockCycle<float> &, c
 template cudaError_t launch_vc_tile_smooth<float>(const TileSmooth<float> &, cudaStream_t);
 
 cudaError_t launch_vc_tile_fast(const TileFast &P, cudaStream_t s) {
-  if (P.G.dim != 2 || P.halo < 1 || P.halo > kTFMaxHalo) return cudaErrorInvalidValue;
+  if (P.G.dim != 2 || P.halo < 0 || P.halo > kTFMaxHalo) return cudaErrorInvalidValue;
   if (P.halo < P.n_half + (P.rc ? 1 : 0)) return cudaErrorInvalidValue;
   const int te = tile_fast_edge(P.halo);
   dim3 grid((P.G.n0 + te - 1) / te, (P.G.n1 + te - 1) / te);

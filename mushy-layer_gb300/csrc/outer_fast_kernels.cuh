@@ -18,6 +18,7 @@
 // order) and, inside the device-resident outer loop, applies the
 // convergence tests and sets the loop's condition.
 #pragma once
+#include "launch.h"
 #include "vc_kernels.cuh"
 #include "outer_kernels.cuh"
 

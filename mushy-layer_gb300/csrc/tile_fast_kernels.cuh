@@ -149,7 +149,9 @@ __device__ __forceinline__ void tf_update(TFCell &k, int ly, int h, float *se) {
   }
 }
 
-__global__ void __launch_bounds__(kTFThreadsX *kTFThreadsY) vc_tile_fast_kernel(TileFast P) {
+// three 512-thread blocks per SM (40 registers) so a 512^2 level runs in
+// fewer waves
+__global__ void __launch_bounds__(kTFThreadsX *kTFThreadsY, 3) vc_tile_fast_kernel(TileFast P) {
   __shared__ float se[kTF * kTF];
   __shared__ float sres[kTF * kTF];
   const Geom &G = P.G;

@@ -373,6 +373,32 @@ def test_vc_solver_tiled_levels_bitwise(n, per, with_c, bckind, pre, post):
     one_cycle_agrees(op, f)
 
 
+@pytest.mark.parametrize("pre,post", [(0, 3), (2, 0)])
+def test_vc_solver_zero_sweeps(pre, post):
+    """No pre- or no post-smoothing: the fused paths still restrict,
+    prolong and cycle exactly like the per-level oracle (FP64 bits) and like
+    the per-level FP32 path (mixed)."""
+    from mushy_gb300 import ops
+    rng = np.random.default_rng(60 + pre)
+    g = P.grid((256, 128), (1, 0, 0))
+    bc = P.vc_bc("mixed")
+    b = [-rng.uniform(0.2, 3.0, abi.face_shape(g, d)) for d in range(2)]
+    f = rng.standard_normal(abi.cell_shape(g))
+    ref = O.VCOpHost(g, bc, 0.0, 1.0, None, b)
+    opts = O.default_options(0)
+    opts.tolerance, opts.hang, opts.max_iter = 1e-30, 0.0, 4
+    opts.num_smooth_down, opts.num_smooth_up = pre, post
+    sol_ref, st_ref, rc_ref = O.vc_solve(ref, opts, np.zeros_like(f), f)
+    op = ops.ProjectionOp(g, bc, 0.0, 1.0, None, [dev(x) for x in b])
+    o = ops.default_options(False)
+    o.tolerance, o.hang, o.max_iter, o.fuse_levels = 1e-30, 0.0, 4, 2
+    o.num_smooth_down, o.num_smooth_up = pre, post
+    d_phi = torch.zeros_like(dev(f))
+    st, rc = ops.AMRMultiGrid(op, o).solve(d_phi, dev(f))
+    exact(host(d_phi), sol_ref)
+    one_cycle_agrees(op, f, pre=pre, post=post)
+
+
 @pytest.mark.parametrize("mixed", [False, True])
 def test_vc_fused_levels_match_unfused_multiwave(mixed):
     """1024x768 puts thousands of tiles in flight (several waves), where a
@@ -405,7 +431,7 @@ def test_vc_fused_levels_match_unfused_multiwave(mixed):
         one_cycle_agrees(op, f)
 
 
-def one_cycle_agrees(op, f, rel=2e-5):
+def one_cycle_agrees(op, f, rel=2e-5, pre=None, post=None):
     """One FP32 V-cycle from zero (one outer iteration) is the same linear
     map of the right-hand side whether it runs per level or fused in tiles
     (lean FP32 form); its results must agree to FP32 rounding."""
@@ -415,6 +441,8 @@ def one_cycle_agrees(op, f, rel=2e-5):
         o = ops.default_options(False)
         o.tolerance, o.hang, o.max_iter, o.fuse_levels = 1e-30, 0.0, 1, fuse
         o.precision = abi.PREC_MIXED
+        if pre is not None:
+            o.num_smooth_down, o.num_smooth_up = pre, post
         d_phi = torch.zeros_like(dev(f))
         ops.AMRMultiGrid(op, o).solve(d_phi, dev(f))
         sol[fuse] = host(d_phi)
