@@ -36,6 +36,12 @@ import numpy as np  # noqa: E402
 
 N = 512
 SEED = 1
+# DRAM bytes (read + write) of one outer iteration of the mixed solve, summed
+# over its kernels from an ncu capture of warm-L2 launches (--profile mixed;
+# profiles/vc_solve_mixed_512x512_launch_list.md): the ~25 MB working set
+# stays in the 129 MB L2 between iterations, so DRAM sees ~1% of the
+# algorithmic bytes
+ITERATION_DRAM_BYTES = 389120
 TOL = 1e-10
 METRIC = "FAS V-cycle cell-updates/s on 1 GB300: mixed vs FP64 at 1e-10 rel residual"
 PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
@@ -53,11 +59,32 @@ def make_problem(n=N, seed=SEED):
 
 
 def options(abi, ops, mixed):
+    # library defaults: whole outer loop as one device-resident graph, fused
+    # levels; only the stopping rule and the precision are set here
     o = ops.default_options(False)
     o.tolerance, o.hang, o.max_iter = TOL, 1e-15, 300
     o.precision = abi.PREC_MIXED if mixed else abi.PREC_F64
-    o.use_graph = 1
     return o
+
+
+# Algorithmic bytes of one mixed-precision outer iteration (2D): the FP64
+# outer step reads phi, rhs, diag (8 B each), two face weights (16 B), the
+# FP32 correction (4 B) and writes phi (8 B) and the FP32 residual (4 B):
+# 56 B per finest cell.  Every level above the single-CTA coarse cycle runs
+# two lean tile launches: pre-smoothing (r, 1/diag, diag, two FP32 face
+# weights in, correction and a quarter-cell restricted residual out: 25 B per
+# cell) and post-smoothing (correction, r, 1/diag, face weights and a
+# quarter-cell coarse correction in, correction out: 25 B per cell).  The
+# coarse cycle (at most 1024-cell top) moves under 1% of that and is left out.
+OUTER_BYTES_PER_CELL = 56
+TILE_BYTES_PER_CELL = 50
+COARSE_CYCLE_CELLS = 1024
+
+
+def iteration_bytes(n0, n1, levels):
+    cells = [(n0 >> l) * (n1 >> l) for l in range(levels)]
+    tiled = sum(c for l, c in enumerate(cells) if c > COARSE_CYCLE_CELLS and l < levels - 1)
+    return OUTER_BYTES_PER_CELL * cells[0] + TILE_BYTES_PER_CELL * tiled
 
 
 class Clocks:
@@ -161,7 +188,7 @@ def run_gpu(args):
             phi.zero_()
             st, rc = S.solve(phi, df)
             assert rc == 0, "solve failed rc=%d" % rc
-        tot_ms, upd, last = 0.0, 0.0, None
+        tot_ms, upd, last, launches, iters = 0.0, 0.0, None, 0.0, 0
         for _ in range(steps):
             phi.zero_()
             flush.fill_(1.0)
@@ -176,13 +203,16 @@ def run_gpu(args):
             assert rc == 0, "solve failed rc=%d" % rc
             tot_ms += e0.elapsed_time(e1)
             upd += st.cell_updates
+            launches += st.kernel_launches
+            iters += st.iterations
             last = st
         tot_ms = aggregate_max(tot_ms, world, "cuda")
-        return tot_ms, upd, last, phi
+        return tot_ms, upd, last, phi, launches, iters
 
     with Clocks() as clk:
-        ms_mixed, upd_mixed, st_mixed, phi_mixed = timed("mixed", args.steps, args.warmup)
-        ms_f64, upd_f64, st_f64, phi_f64 = timed("fp64", args.steps, args.warmup)
+        ms_mixed, upd_mixed, st_mixed, phi_mixed, nl_mixed, it_mixed = timed("mixed", args.steps,
+                                                                             args.warmup)
+        ms_f64, upd_f64, st_f64, phi_f64, nl_f64, it_f64 = timed("fp64", args.steps, args.warmup)
 
     # error of the mixed solution against the FP64 solution (null space removed)
     a = phi_f64.cpu().numpy()
@@ -216,32 +246,13 @@ def run_gpu(args):
         e2e_ms += e0.elapsed_time(e1)
         e2e_upd += st.cell_updates
 
-    # dominant kernel: finest-level FP32 red/black half sweep, timed alone
-    op32 = ops.ProjectionOp(g, abi.make_bc(), 0.0, 1.0, None, [x.float() for x in db])
-    e32 = torch.zeros(df.shape, dtype=torch.float32, device="cuda")
-    r32 = df.float()
-    for _ in range(10):
-        op32.levelGSRBPass(e32, r32, 0)
-    # launches captured in a CUDA graph so the host's ctypes overhead does not
-    # pace them; the replay time / launches bounds the kernel duration from above
-    reps = 200
-    cg = torch.cuda.CUDAGraph()
-    torch.cuda.synchronize()
-    with torch.cuda.graph(cg):
-        for i in range(reps):
-            op32.levelGSRBPass(e32, r32, i & 1)
-    cg.replay()
-    torch.cuda.synchronize()
-    k0, k1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    k0.record(stream)
-    cg.replay()
-    k1.record(stream)
-    torch.cuda.synchronize()
-    k_ms = k0.elapsed_time(k1) / reps
-    alg_bytes = 4 * (3 + 2) * ncell / 2.0   # one half of a full sweep's arrays (FP32, 2D)
+    # roofline of the timed unit the events see: one outer iteration of the
+    # mixed solve (its ~10 kernels run back to back inside the device-resident
+    # graph loop; their individual shares come from the ncu launch list)
     hbm, kind = peaks()
-    achieved = alg_bytes / (k_ms * 1e-3) / 1e9
-
+    it_us = ms_mixed * 1e3 / max(it_mixed, 1)
+    alg_bytes = iteration_bytes(g.n[0], g.n[1], st_mixed.levels)
+    achieved = alg_bytes / (it_us * 1e-6) / 1e9
     clocks = clk.summary()
     value = upd_mixed / (ms_mixed * 1e-3) * world
     line = {
@@ -262,19 +273,21 @@ def run_gpu(args):
                    "cells": ncell, "levels": st_mixed.levels, "l2": "flushed (512 MiB write) between steps",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "fp64": {"value": upd_f64 / (ms_f64 * 1e-3) * world, "ms_per_step": ms_f64 / args.steps,
-                 "iterations": st_f64.iterations, "cycles": st_f64.cycles},
+                 "iterations": st_f64.iterations, "cycles": st_f64.cycles,
+                 "gpu_launches": int(nl_f64)},
         "mixed": {"iterations": st_mixed.iterations, "cycles": st_mixed.cycles,
                   "final_rel_residual": st_mixed.final_norm / st_mixed.initial_norm,
                   "rel_err_vs_fp64_solution": err},
         "time_to_solution_ratio_fp64_over_mixed": ms_f64 / ms_mixed,
         "e2e": {"value": e2e_upd / (e2e_ms * 1e-3) * world, "unit": "cell-updates/s",
                 "h2d_bytes_per_step": int(ncell * 8), "d2h_bytes_per_step": int(ncell * 8)},
-        "roofline": {"bound": "hbm", "kernel": "vc_gsrb_kernel<float,2> (finest level)",
+        "roofline": {"bound": "hbm", "kernel": "one mixed outer iteration (graph body: FP64 outer "
+                                               "step, lean FP32 tiles, single-CTA coarse cycle)",
                      "achieved": achieved, "peak": hbm, "peak_kind": kind, "unit": "GB/s",
-                     "frac": achieved / hbm, "traffic": None, "launch_us": k_ms * 1e3,
-                     "alg_bytes_per_launch": alg_bytes},
+                     "frac": achieved / hbm, "traffic": ITERATION_DRAM_BYTES,
+                     "iteration_us": it_us, "alg_bytes_per_iteration": alg_bytes},
         "clocks": clocks,
-        "gpu_launches": None,
+        "gpu_launches": int(nl_mixed),
     }
     if rank == 0:
         line["cpu_baseline"] = cpu_baseline(args) if not args.no_cpu else None
@@ -333,6 +346,30 @@ def run_reference(args):
                 "d2h_bytes_per_step": 0}}))
 
 
+def run_profile(args):
+    """One warm-up solve and one solve of 3 outer iterations of the bench
+    problem (mixed or fp64), for ncu launch lists and captures."""
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    from mushy_gb300 import abi, ops
+    g, b, f = make_problem()
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    op = ops.ProjectionOp(g, abi.make_bc(), 0.0, 1.0, None, [dev(x) for x in b])
+    o = options(abi, ops, args.profile == "mixed")
+    o.max_iter = 3
+    # same kernels as the timed solve, launched one by one: profilers do not
+    # see kernel nodes inside a graph with a conditional (WHILE) node
+    o.use_graph = 0
+    S = ops.AMRMultiGrid(op, o)
+    for _ in range(2):
+        phi = torch.zeros_like(dev(f))
+        st, rc = S.solve(phi, dev(f))
+    torch.cuda.synchronize()
+    print(json.dumps({"profile": args.profile, "iterations": st.iterations,
+                      "kernel_launches": st.kernel_launches}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -340,8 +377,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--profile", choices=["mixed", "fp64"],
+                    help="run one short solve for a profiler and exit")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.profile:
+        run_profile(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gpu(args)

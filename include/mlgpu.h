@@ -130,12 +130,13 @@ typedef struct mlgpu_mg_options {
                             CUDA graph and replayed; 2 (default): the whole outer
                             loop as a graph WHILE node, decided on the device
                             (linear solvers; the FAS solver treats 2 as 1) */
-  int fuse_levels;       /* 1 (default): levels of at most 256 cells run one
-                            single-CTA cycle and, in mixed precision, 2D levels
-                            above that run FP32 shared-memory tiles (smoothing fused
-                            with restriction / prolongation); 2: FP64 cycles use
-                            the tiles too; 0: one launch per smoothing pass /
-                            transfer.  FP64 results are the same bits for 0, 1, 2 */
+  int fuse_levels;       /* 1 (default): the coarse levels run one single-CTA cycle
+                            (levels of at most 256 cells; in 2D mixed precision
+                            1024) and, in mixed precision, 2D levels above that run
+                            FP32 shared-memory tiles (smoothing fused with
+                            restriction / prolongation); 2: FP64 cycles use the
+                            tiles too; 0: one launch per smoothing pass / transfer.
+                            FP64 results are the same bits for 0, 1, 2 */
 } mlgpu_mg_options;
 
 typedef struct mlgpu_solve_stats {
@@ -147,6 +148,8 @@ typedef struct mlgpu_solve_stats {
   double final_norm;
   double cell_updates;   /* smoothing sweeps + residual/operator evaluations, in cells */
   double norm_history[64];
+  double kernel_launches; /* sm_103a kernels this solve launched (counted from the
+                             captured iteration graph; -1 per piece not counted) */
 } mlgpu_solve_stats;
 
 typedef struct mlgpu_solver mlgpu_solver;  /* opaque */

@@ -51,6 +51,36 @@ struct mlgpu_solver {
   }
   virtual int solve(double *phi, const double *rhs, mlgpu_solve_stats *st) = 0;
   virtual int set_alpha_beta(double a, double b) = 0;
+
+  // kernels a piece of host code launches: captured once into a graph that
+  // is never run, and its kernel nodes counted (-1 if the capture failed)
+  template <class F>
+  int count_kernels(F &&f) {
+    cudaGraph_t g = nullptr;
+    if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return -1;
+    int rc = f();
+    cudaError_t e = cudaStreamEndCapture(s, &g);
+    cudaGetLastError();
+    if (rc || e != cudaSuccess || !g) {
+      if (g) cudaGraphDestroy(g);
+      return -1;
+    }
+    int n = kernel_nodes(g);
+    cudaGraphDestroy(g);
+    return n;
+  }
+  static int kernel_nodes(cudaGraph_t g) {
+    size_t n = 0;
+    if (cudaGraphGetNodes(g, nullptr, &n) != cudaSuccess) return -1;
+    std::vector<cudaGraphNode_t> nodes(n);
+    if (n && cudaGraphGetNodes(g, nodes.data(), &n) != cudaSuccess) return -1;
+    int k = 0;
+    for (auto nd : nodes) {
+      cudaGraphNodeType t;
+      if (cudaGraphNodeGetType(nd, &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) k++;
+    }
+    return k;
+  }
 };
 
 namespace {
@@ -180,6 +210,7 @@ class VCSolver : public mlgpu_solver {
   bool use_block_cycle = true;
   bool use_tiles = true;
   double updates_per_iter = 0;
+  int kern_init = -1, kern_iter = -1, kern_loop = -1;  // kernels per piece (counted)
 
   ~VCSolver() override {
     for (auto &g : graph)
@@ -602,6 +633,7 @@ class VCSolver : public mlgpu_solver {
       rc = iteration(0, &dev_state->parity, h);
       cudaGraph_t body;
       e = cudaStreamEndCapture(s, &body);
+      if (e == cudaSuccess) kern_loop = kernel_nodes(body);
     }
     if (e == cudaSuccess && rc == MLGPU_OK) e = cudaGraphInstantiate(&loop_exec, g, 0);
     cudaGraphDestroy(g);
@@ -627,14 +659,8 @@ class VCSolver : public mlgpu_solver {
     return MLGPU_OK;
   }
 
-  int solve(double *user_phi, const double *user_rhs, mlgpu_solve_stats *st) override {
-    if (!user_phi || !user_rhs || !st) return MLGPU_ERR_ARG;
-    size_t bytes = sizeof(double) * L[0].G.ncell;
-    cudaGetLastError();  // clear any stale error of an earlier call
-    if (enter()) return MLGPU_ERR_CUDA;
-    CK(cudaMemcpyAsync(phi[0], user_phi, bytes, cudaMemcpyDeviceToDevice, s));
-    CK(cudaMemcpyAsync(rhs, user_rhs, bytes, cudaMemcpyDeviceToDevice, s));
-    // initial residual (no update)
+  // residual and norm of the starting field (no update); norm in part[kMaxBlocks]
+  int initial_residual() {
     VCArgs<double> A = args<double>(0);
     A.a = (const double *)op.aCoef;
     A.c = (const double *)op.cCoef;
@@ -651,12 +677,30 @@ class VCSolver : public mlgpu_solver {
                                                       nullptr, (double *)L[0].r, part, s)));
       CK(launch_finalize_norm(o.norm_type, part, norm_parts(L[0].G.ncell), part + kMaxBlocks, s));
     }
+    return MLGPU_OK;
+  }
+
+  int solve(double *user_phi, const double *user_rhs, mlgpu_solve_stats *st) override {
+    if (!user_phi || !user_rhs || !st) return MLGPU_ERR_ARG;
+    size_t bytes = sizeof(double) * L[0].G.ncell;
+    cudaGetLastError();  // clear any stale error of an earlier call
+    if (enter()) return MLGPU_ERR_CUDA;
+    CK(cudaMemcpyAsync(phi[0], user_phi, bytes, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(rhs, user_rhs, bytes, cudaMemcpyDeviceToDevice, s));
+    // initial residual (no update)
+    if (kern_init < 0) {
+      kern_init = count_kernels([&] { return initial_residual(); });
+      kern_iter = count_kernels([&] { return iteration(0); });
+    }
+    int rc_init = initial_residual();
+    if (rc_init) return rc_init;
     CK(cudaMemcpyAsync(host_norm, part + kMaxBlocks, sizeof(double), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     Outer S;
     S.norm0 = S.norm = S.prev = *host_norm;
     stats_begin(st, (int)L.size(), S.norm0);
     st->cell_updates = (double)L[0].G.ncell;
+    st->kernel_launches = kern_init;
     if (!std::isfinite(S.norm0)) S.status = 8;
     int cur = 0;
     if (o.use_graph >= 2 && !loop_failed && outer_continue(o, S)) {
@@ -676,6 +720,7 @@ class VCSolver : public mlgpu_solver {
         cur = host_state->parity;
         st->cycles = S.iter * std::max(1, o.inner_cycles);
         st->cell_updates += S.iter * updates_per_iter;
+        st->kernel_launches += (double)S.iter * kern_loop;
       }
     }
     while (outer_continue(o, S)) {
@@ -686,6 +731,7 @@ class VCSolver : public mlgpu_solver {
       S.norm = *host_norm;
       st->cycles += std::max(1, o.inner_cycles);
       st->cell_updates += updates_per_iter;
+      st->kernel_launches += kern_iter;
       outer_after(o, S, st);
     }
     CK(cudaMemcpyAsync(user_phi, phi[cur], bytes, cudaMemcpyDeviceToDevice, s));
@@ -719,6 +765,7 @@ class HCSolver : public mlgpu_solver {
   mlgpu_mg_options o;
   std::vector<HCLevel> L;
   double *part = nullptr, *host_norm = nullptr;
+  int kern_init = -1, kern_iter = -1;  // kernels per piece (counted)
   cudaGraphExec_t graph = nullptr;
   double updates_per_iter = 0;
 
@@ -862,6 +909,10 @@ class HCSolver : public mlgpu_solver {
     if (enter()) return MLGPU_ERR_CUDA;
     CK(cudaMemcpyAsync(L[0].u, user_phi, bytes, cudaMemcpyDeviceToDevice, s));
     CK(cudaMemcpyAsync(L[0].f, user_rhs, bytes, cudaMemcpyDeviceToDevice, s));
+    if (kern_init < 0) {
+      kern_init = count_kernels([&] { return residual_norm(); });
+      kern_iter = count_kernels([&] { return iteration(); });
+    }
     int rc = residual_norm();
     if (rc) return rc;
     CK(cudaStreamSynchronize(s));
@@ -869,6 +920,7 @@ class HCSolver : public mlgpu_solver {
     S.norm0 = S.norm = S.prev = *host_norm;
     stats_begin(st, (int)L.size(), S.norm0);
     st->cell_updates = (double)L[0].G.ncell;
+    st->kernel_launches = kern_init;
     if (!std::isfinite(S.norm0)) S.status = 8;
     while (outer_continue(o, S)) {
       rc = run_iteration();
@@ -877,6 +929,7 @@ class HCSolver : public mlgpu_solver {
       S.norm = *host_norm;
       st->cycles += 1;
       st->cell_updates += updates_per_iter;
+      st->kernel_launches += kern_iter;
       outer_after(o, S, st);
     }
     CK(cudaMemcpyAsync(user_phi, L[0].u, bytes, cudaMemcpyDeviceToDevice, s));

@@ -78,7 +78,8 @@ class SolveStats(C.Structure):
                 ("cycles", C.c_int), ("levels", C.c_int),
                 ("initial_norm", C.c_double), ("final_norm", C.c_double),
                 ("cell_updates", C.c_double),
-                ("norm_history", C.c_double * 64)]
+                ("norm_history", C.c_double * 64),
+                ("kernel_launches", C.c_double)]
 
 
 def make_grid(n, dx=None, periodic=(0, 0, 0)):
