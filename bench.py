@@ -346,6 +346,215 @@ def run_reference(args):
                 "d2h_bytes_per_step": 0}}))
 
 
+def _events_ms(fn):
+    """Device time of fn() on the current stream (CUDA events, synchronised)."""
+    import torch
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    out = fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1), out
+
+
+def _compatible_u(u):
+    """MAC velocity with zero net flux: periodic x seam faces equal, zero
+    normal velocity on the non-periodic walls (y, and z in 3D)."""
+    u[0][..., -1] = u[0][..., 0]
+    u[1][..., 0, :] = 0.0
+    u[1][..., -1, :] = 0.0
+    if len(u) == 3:
+        u[2][0] = 0.0
+        u[2][-1] = 0.0
+    return u
+
+
+def config1(args, torch, abi, ops, O, P):
+    """64x64 diffusive solidification, no flow: ten backward-Euler steps of the
+    nonlinear (H, C) system, each solved by FAS multigrid to 1e-10 (FP64).
+    Checked against the CPU restatement step by step."""
+    n, dt, steps = 64, 1e-3, 10
+    g = P.grid((n, n))
+    prm = abi.make_params(stefan=5.0, compositionRatio=5.0, waterDistributionCoeff=1e-3,
+                          specificHeatRatio=1.0, heatConductivityRatio=1.0)
+    phi_bc = abi.make_bc()
+    der = abi.make_bc({(1, 0, 0): (abi.BC_DIRICHLET, -1.0), (1, 1, 0): (abi.BC_DIRICHLET, 0.5),
+                       (1, 0, 1): (abi.BC_DIRICHLET, -1.0), (1, 1, 1): (abi.BC_DIRICHLET, -1.0)})
+    phi0 = np.empty((2,) + abi.cell_shape(g))
+    phi0[0], phi0[1] = 6.0, -1.0
+    b = [np.stack([-np.ones(abi.face_shape(g, d)), np.zeros(abi.face_shape(g, d))])
+         for d in range(2)]
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    op = ops.NLMultiCompOp(g, prm, phi_bc, der, 1.0, 1.0, None, [dev(x) for x in b])
+    S = ops.AMRFASMultiGrid(op, ops.default_options(True))
+
+    def march():
+        cur, upd, its, rcs = dev(phi0), 0.0, 0, []
+        for _ in range(steps):
+            new = cur.clone()
+            st, rc = S.backwardEuler(new, cur, dt)
+            upd, its, cur = upd + st.cell_updates, its + st.iterations, new
+            rcs.append(rc)
+        return cur, upd, its, rcs
+
+    march()
+    ms, (cur, upd, its, rcs) = _events_ms(march)
+    ref = O.NLOpHost(g, prm, phi_bc, der, 1.0, 1.0, None, b)
+    oo = O.default_options(1)
+    t0 = time.time()
+    h = phi0.copy()
+    for _ in range(steps):
+        h, st_ref, rc_ref = O.hc_backward_euler(ref, oo, h, h, dt)
+    cpu_s = time.time() - t0
+    diff = float(np.abs(cur.cpu().numpy() - h).max())
+    return {"metric": "backward-Euler steps/s (FAS to 1e-10, FP64)", "value": steps / (ms * 1e-3),
+            "unit": "steps/s", "higher_is_better": True, "ms_per_step": ms / steps,
+            "cell_updates_per_s": upd / (ms * 1e-3), "fas_iterations": its, "status": rcs,
+            "config": {"workload": "64x64 diffusive solidification, St=5, CR=5, k=1e-3, "
+                                   "T=-1 bottom / 0.5 top, C_l=-1, 10 steps dt=1e-3"},
+            "parity": {"max_abs_diff_vs_oracle": diff, "oracle_s": cpu_s},
+            "note": "latency bound (4096 cells): report only"}
+
+
+def config3(args, torch, abi, ops, O, P):
+    """1024x1024 mushy-layer step: (H, C) backward-Euler FAS solve, the two
+    Darcy-Brinkman velocity solves and the MAC projection, FP64 against mixed
+    precision for the linear solves (the FAS solve is FP64 in both)."""
+    n = 1024
+    g, chi, perm, u = P.projection_problem((n, n), 3, sigma=32.0)
+    u = _compatible_u(u)
+    rng = np.random.default_rng(3)
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    # (H, C): liquid plus 1e-3 noise, cold bottom
+    prm = abi.make_params(stefan=5.0, compositionRatio=25.0, waterDistributionCoeff=1e-3,
+                          specificHeatRatio=1.0, heatConductivityRatio=1.0)
+    phi_bc = abi.make_bc()
+    der = abi.make_bc({(1, 0, 0): (abi.BC_DIRICHLET, -1.0), (1, 0, 1): (abi.BC_DIRICHLET, -1.0)})
+    phi0 = np.empty((2,) + abi.cell_shape(g))
+    phi0[0] = 6.0 + 1e-3 * rng.standard_normal(abi.cell_shape(g))
+    phi0[1] = -1.0 + 1e-3 * rng.standard_normal(abi.cell_shape(g))
+    bh = [np.stack([-np.ones(abi.face_shape(g, d)), -np.full(abi.face_shape(g, d), 1.0 / 200)])
+          for d in range(2)]
+    hop = ops.NLMultiCompOp(g, prm, phi_bc, der, 1.0, 1.0, None, [dev(x) for x in bh])
+    HS = ops.AMRFASMultiGrid(hop, ops.default_options(True))
+    d_phi0 = dev(phi0)
+    # Darcy-Brinkman: (Da^-1 chi/Pi) u - visc lap u = rho per component
+    cC = dev(chi / (1e-3 * perm))
+    bdb = [dev(-np.ones(abi.face_shape(g, d))) for d in range(2)]
+    noslip = abi.make_bc({(d, s, 0): (abi.BC_DIRICHLET, 0.0) for d in range(2) for s in range(2)})
+    dbop = ops.DarcyBrinkmanOp(g, noslip, 0.0, -1.0, None, bdb, cC)
+    rho = [dev(1e-3 * rng.standard_normal(abi.cell_shape(g))) for _ in range(2)]
+    pif = O.face_geomean(g, perm)
+    pop = ops.ProjectionOp(g, abi.make_bc(), 0.0, 1.0, None, [dev(-x) for x in pif])
+    d_pif = [dev(x) for x in pif]
+    out = {}
+    for prec in ("fp64", "mixed"):
+        o = ops.default_options(False)
+        o.tolerance, o.hang, o.max_iter = TOL, 1e-15, 300
+        o.precision = abi.PREC_MIXED if prec == "mixed" else abi.PREC_F64
+        DS, PS = ops.AMRMultiGrid(dbop, o), ops.AMRMultiGrid(pop, o)
+
+        def step():
+            new = d_phi0.clone()
+            st_h, rc_h = HS.backwardEuler(new, d_phi0, 1e-4)
+            vel = []
+            its = [st_h.iterations]
+            for c in range(2):
+                v = torch.zeros_like(rho[c])
+                st_v, rc_v = DS.solve(v, rho[c])
+                vel.append(v)
+                its.append(st_v.iterations)
+            du = [dev(x) for x in u]
+            p = torch.zeros(abi.cell_shape(g), dtype=torch.float64, device="cuda")
+            st_p, rc_p = PS.levelMacProject(du, d_pif, p)
+            its.append(st_p.iterations)
+            return new, vel, du, its
+
+        step()
+        ms, res = _events_ms(step)
+        out[prec] = (ms, res)
+    ms64, (h64, v64, u64, it64) = out["fp64"]
+    msm, (hm, vm, um, itm) = out["mixed"]
+    rel = lambda a, b: float((a - b).abs().max() / b.abs().max())
+    return {"metric": "mushy-layer step time, 1024^2 (HC FAS + 2 Darcy-Brinkman + MAC projection)",
+            "value": msm, "unit": "ms/step (mixed)", "higher_is_better": False,
+            "fp64_ms": ms64, "ratio_fp64_over_mixed": ms64 / msm,
+            "iterations": {"fp64": it64, "mixed": itm},
+            "mixed_vs_fp64": {"velocity_rel": max(rel(vm[c], v64[c]) for c in range(2)),
+                              "mac_u_rel": max(rel(um[d], u64[d]) for d in range(2))},
+            "config": {"workload": "2D 1024x1024, Kozeny-Carman Pi of a smooth porosity, "
+                                   "Da=1e-3, CR=25, Le=200, liquid + 1e-3 noise, dt=1e-4; "
+                                   "linear solves to 1e-10"}}
+
+
+def config4(args, torch, abi, ops, O, P):
+    """3D 256^3 projection solve (mixed vs FP64) and one (H, C) FAS step."""
+    n = 256
+    g, chi, perm, u = P.projection_problem((n, n, n), 4, sigma=32.0)
+    u = _compatible_u(u)
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    pif = O.face_geomean(g, perm)
+    f = O.mac_divergence(g, u)
+    f -= f.mean()
+    pop = ops.ProjectionOp(g, abi.make_bc(), 0.0, 1.0, None, [dev(-x) for x in pif])
+    df = dev(f)
+    res = {}
+    for prec in ("fp64", "mixed"):
+        o = ops.default_options(False)
+        o.tolerance, o.hang, o.max_iter = TOL, 1e-15, 300
+        o.precision = abi.PREC_MIXED if prec == "mixed" else abi.PREC_F64
+        S = ops.AMRMultiGrid(pop, o)
+        phi = torch.zeros_like(df)
+        S.solve(phi, df)
+        phi.zero_()
+        ms, (st, rc) = _events_ms(lambda: S.solve(phi, df))
+        res[prec] = (ms, st, rc, phi.clone())
+    a, m = res["fp64"][3], res["mixed"][3]
+    err = float(((a - a.mean()) - (m - m.mean())).abs().max() / (a - a.mean()).abs().max())
+    # one (H, C) backward-Euler FAS step on the same grid, FP64
+    rng = np.random.default_rng(4)
+    prm = abi.make_params(stefan=5.0, compositionRatio=5.0, waterDistributionCoeff=1e-3,
+                          specificHeatRatio=1.0, heatConductivityRatio=1.0)
+    der = abi.make_bc({(2, 0, 0): (abi.BC_DIRICHLET, -1.0), (2, 0, 1): (abi.BC_DIRICHLET, -1.0)})
+    phi0 = np.empty((2,) + abi.cell_shape(g))
+    phi0[0] = 6.0 - 4.0 * np.linspace(1, 0, n)[:, None, None] * (1 + 1e-2 * rng.standard_normal((n, n, n)))
+    phi0[1] = -1.0
+    bh = [np.stack([-np.ones(abi.face_shape(g, d)), -np.full(abi.face_shape(g, d), 1e-2)])
+          for d in range(3)]
+    hop = ops.NLMultiCompOp(g, prm, abi.make_bc(), der, 1.0, 1.0, None, [dev(x) for x in bh])
+    HS = ops.AMRFASMultiGrid(hop, ops.default_options(True))
+    d0 = dev(phi0)
+    new = d0.clone()
+    ms_hc, (st_h, rc_h) = _events_ms(lambda: HS.backwardEuler(new, d0, 1e-4))
+    cells = n ** 3
+    return {"metric": "3D 256^3 projection solve cell-updates/s: mixed vs FP64 at 1e-10",
+            "value": res["mixed"][1].cell_updates / (res["mixed"][0] * 1e-3),
+            "unit": "cell-updates/s", "higher_is_better": True,
+            "mixed_ms": res["mixed"][0], "fp64_ms": res["fp64"][0],
+            "fp64_value": res["fp64"][1].cell_updates / (res["fp64"][0] * 1e-3),
+            "iterations": {"fp64": res["fp64"][1].iterations, "mixed": res["mixed"][1].iterations},
+            "rel_err_mixed_vs_fp64": err,
+            "hc_fas_step": {"ms": ms_hc, "iterations": st_h.iterations, "rc": rc_h,
+                            "cell_updates_per_s": st_h.cell_updates / (ms_hc * 1e-3)},
+            "config": {"workload": "3D 256^3 (16.8M cells) Kozeny-Carman projection Poisson, "
+                                   "periodic x, Neumann y/z; (H, C) BE step dt=1e-4", "cells": cells}}
+
+
+def run_config(args):
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    from mushy_gb300 import abi, ops
+    from oracle import oracle as O
+    import problems as P
+    fn = {1: config1, 3: config3, 4: config4}[args.config]
+    line = fn(args, torch, abi, ops, O, P)
+    line.update({"n_gpus": 1, "data": "synthetic (seeded)", "config_index": args.config})
+    print(json.dumps(line))
+
+
 def run_profile(args):
     """One warm-up solve and one solve of 3 outer iterations of the bench
     problem (mixed or fp64), for ncu launch lists and captures."""
@@ -379,9 +588,13 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--profile", choices=["mixed", "fp64"],
                     help="run one short solve for a profiler and exit")
+    ap.add_argument("--config", type=int, choices=[1, 3, 4],
+                    help="measure another configuration (one JSON line) and exit")
     args = ap.parse_args()
     if args.profile:
         run_profile(args)
+    elif args.config:
+        run_config(args)
     elif args.impl == "reference":
         run_reference(args)
     else:
