@@ -371,11 +371,10 @@ def _compatible_u(u):
     return u
 
 
-def config1(args, torch, abi, ops, O, P):
-    """64x64 diffusive solidification, no flow: ten backward-Euler steps of the
-    nonlinear (H, C) system, each solved by FAS multigrid to 1e-10 (FP64).
-    Checked against the CPU restatement step by step."""
-    n, dt, steps = 64, 1e-3, 10
+def _c1_setup(torch, abi, ops, P, n):
+    """(H, C) problem of the 64x64 diffusive-solidification configuration:
+    liquid H = 1 + St, C = -1; T = -1 at the bottom, 0.5 at the top, C_l = -1
+    on both; side walls Neumann; k_T = 1, D_C = 0 (Le infinite)."""
     g = P.grid((n, n))
     prm = abi.make_params(stefan=5.0, compositionRatio=5.0, waterDistributionCoeff=1e-3,
                           specificHeatRatio=1.0, heatConductivityRatio=1.0)
@@ -388,6 +387,15 @@ def config1(args, torch, abi, ops, O, P):
          for d in range(2)]
     dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
     op = ops.NLMultiCompOp(g, prm, phi_bc, der, 1.0, 1.0, None, [dev(x) for x in b])
+    return g, prm, phi_bc, der, phi0, b, dev, op
+
+
+def config1(args, torch, abi, ops, O, P):
+    """64x64 diffusive solidification, no flow: ten backward-Euler steps of the
+    nonlinear (H, C) system, each solved by FAS multigrid to 1e-10 (FP64).
+    Checked against the CPU restatement step by step."""
+    n, dt, steps = 64, 1e-3, 10
+    g, prm, phi_bc, der, phi0, b, dev, op = _c1_setup(torch, abi, ops, P, n)
     S = ops.AMRFASMultiGrid(op, ops.default_options(True))
 
     def march():
@@ -562,6 +570,22 @@ def run_profile(args):
     import __graft_entry__
     __graft_entry__.build()
     from mushy_gb300 import abi, ops
+    if args.profile == "hc":
+        # two backward-Euler FAS steps of the 64x64 solidification problem
+        import problems as P
+        g, prm, phi_bc, der, phi0, b, dev, op = _c1_setup(torch, abi, ops, P, 64)
+        o = ops.default_options(True)
+        o.use_graph = 0
+        S = ops.AMRFASMultiGrid(op, o)
+        cur = dev(phi0)
+        for _ in range(2):
+            new = cur.clone()
+            st, rc = S.backwardEuler(new, cur, 1e-3)
+            cur = new
+        torch.cuda.synchronize()
+        print(json.dumps({"profile": "hc", "iterations": st.iterations,
+                          "kernel_launches": st.kernel_launches}))
+        return
     g, b, f = make_problem()
     dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
     op = ops.ProjectionOp(g, abi.make_bc(), 0.0, 1.0, None, [dev(x) for x in b])
@@ -586,7 +610,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--profile", choices=["mixed", "fp64"],
+    ap.add_argument("--profile", choices=["mixed", "fp64", "hc"],
                     help="run one short solve for a profiler and exit")
     ap.add_argument("--config", type=int, choices=[1, 3, 4],
                     help="measure another configuration (one JSON line) and exit")

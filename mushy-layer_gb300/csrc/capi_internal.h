@@ -10,6 +10,7 @@
 #include "cycle_fast_kernels.cuh"
 #include "outer_kernels.cuh"
 #include "outer_fast_kernels.cuh"
+#include "nl_cached_kernels.cuh"
 
 namespace mlgpu {
 
@@ -36,6 +37,20 @@ cudaError_t launch_be_rhs(long long n, const double *phi_old, const double *a, c
 cudaError_t launch_vc_outer_fast(const OuterFast &P, int norm, cudaStream_t s);
 cudaError_t launch_outer_coefs(const VCArgs<double> &A, double *cx, double *cy, double *diag,
                                cudaStream_t s);
+// FP64 nonlinear kernels over the per-level (T, C_l) cache
+cudaError_t launch_nlc_closure(const NLArgs<double> &A, const double *phi, double *tcl,
+                               cudaStream_t s);
+cudaError_t launch_nlc_gsrb(const NLArgs<double> &A, double *phi, const double *rhs, double *tcl,
+                            const double *lam, int pass, cudaStream_t s);
+cudaError_t launch_nlc_relax_block(const NLArgs<double> &A, double *phi, const double *rhs,
+                                   double *tcl, const double *lam, int sweeps, int init,
+                                   cudaStream_t s);
+cudaError_t launch_nlc_op(const NLArgs<double> &A, int mode, int norm, const double *phi,
+                          const double *tcl, const double *rhs, double *out, double *copy,
+                          double *part, cudaStream_t s);
+cudaError_t launch_nlc_restrict(const NLArgs<double> &A, const Geom &C, const double *phi,
+                                const double *tcl, const double *rhs, double *res_c,
+                                double *phi_c, cudaStream_t s);
 cudaError_t launch_outer_decide(OuterDev *st, const double *norm, const OuterCfg &c,
                                 cudaGraphConditionalHandle h, cudaStream_t s);
 

@@ -141,8 +141,10 @@ __device__ __forceinline__ void t_cl(double H, double C, const ClosureParams &p,
     Cl = p.Te;
   } else if (H > He && H < Hl) {
     double por = porosity_mush(C, H, p);
-    T = -(C + p.CR * (1 - por)) / (por + p.k * (1 - por));
+    // T = -(x) / d and C_l = x / d: IEEE division is symmetric in the sign of
+    // the numerator, so T is exactly -C_l (one FP64 division instead of two)
     Cl = (C + p.CR * (1 - por)) / (por + p.k * (1 - por));
+    T = -Cl;
   } else if (H >= Hl) {
     T = H - p.St;
     Cl = C;

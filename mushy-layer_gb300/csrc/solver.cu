@@ -757,6 +757,8 @@ struct HCLevel {
   Geom G;
   Coefs<double> c64;
   double *u = nullptr, *f = nullptr, *r = nullptr, *uold = nullptr, *t = nullptr;
+  double *tcl = nullptr;  // (T, C_l) of u, valid while tcl_ok says so
+  double *lam = nullptr;  // stored 1/diag (resetLambda)
 };
 
 class HCSolver : public mlgpu_solver {
@@ -766,6 +768,9 @@ class HCSolver : public mlgpu_solver {
   std::vector<HCLevel> L;
   double *part = nullptr, *host_norm = nullptr;
   int kern_init = -1, kern_iter = -1;  // kernels per piece (counted)
+  // per level: does tcl hold the closure of the current u?  Tracked on the
+  // host along the launch sequence (the same sequence every iteration)
+  std::vector<char> tcl_ok;
   cudaGraphExec_t graph = nullptr;
   double updates_per_iter = 0;
 
@@ -796,8 +801,11 @@ class HCSolver : public mlgpu_solver {
       L[l].r = A.get<double>(n);
       L[l].uold = A.get<double>(n);
       L[l].t = A.get<double>(n);
+      L[l].tcl = A.get<double>(n);
+      L[l].lam = A.get<double>(n);
       g = coarsen_grid(g);
     }
+    tcl_ok.assign(L.size(), 0);
     part = A.get<double>(kNormScratchDoubles);
     return A.off + 256;
   }
@@ -809,6 +817,8 @@ class HCSolver : public mlgpu_solver {
       for (int d = 0; d < F.dim; d++)
         CK(launch_coarsen_faces<double>(F, 2, d, L[l - 1].c64.b[d], L[l].c64.b[d], s));
     }
+    int rc = build_lambda();
+    if (rc) return rc;
     double u = 0;
     int last = (int)L.size() - 1;
     std::vector<double> visits(L.size(), 0);
@@ -823,6 +833,20 @@ class HCSolver : public mlgpu_solver {
                           (double)L[l + 1].G.ncell);
     }
     updates_per_iter = u + (double)L[0].G.ncell;
+    return MLGPU_OK;
+  }
+
+  // stored 1/diag of every level (bitwise the inline resetLambda value)
+  int build_lambda() {
+    for (size_t l = 0; l < L.size(); l++)
+      CK(launch_nl_lambda<double>(args((int)l), L[l].lam, s));
+    return MLGPU_OK;
+  }
+
+  // make tcl of level l the closure of its u
+  int ensure_tcl(int l) {
+    if (!tcl_ok[l]) CK(launch_nlc_closure(args(l), L[l].u, L[l].tcl, s));
+    tcl_ok[l] = 1;
     return MLGPU_OK;
   }
 
@@ -842,9 +866,12 @@ class HCSolver : public mlgpu_solver {
         CK(launch_nl_op<double>(A, NL_JACOBI, -1, L[l].u, L[l].f, L[l].t, nullptr, nullptr, s));
         CK(cudaMemcpyAsync(L[l].u, L[l].t, sizeof(double) * 2 * L[l].G.ncell,
                            cudaMemcpyDeviceToDevice, s));
+        tcl_ok[l] = 0;
       } else {
-        CK(launch_nl_gsrb<double>(A, L[l].u, L[l].f, 0, s));
-        CK(launch_nl_gsrb<double>(A, L[l].u, L[l].f, 1, s));
+        int rc = ensure_tcl(l);
+        if (rc) return rc;
+        CK(launch_nlc_gsrb(A, L[l].u, L[l].f, L[l].tcl, L[l].lam, 0, s));
+        CK(launch_nlc_gsrb(A, L[l].u, L[l].f, L[l].tcl, L[l].lam, 1, s));
       }
     }
     return MLGPU_OK;
@@ -855,31 +882,44 @@ class HCSolver : public mlgpu_solver {
     NLArgs<double> A = args(l);
     if (l == last) {
       if (o.relax_mode == MLGPU_RELAX_JACOBI) return relax(l, o.bottom_max_iter);
-      CK(launch_nl_relax_block<double>(A, L[l].u, L[l].f, o.bottom_max_iter, s));
+      CK(launch_nlc_relax_block(A, L[l].u, L[l].f, L[l].tcl, L[l].lam, o.bottom_max_iter,
+                                tcl_ok[l] ? 0 : 1, s));
+      tcl_ok[l] = 1;
       return MLGPU_OK;
     }
     int rc = relax(l, o.num_smooth_down);
     if (rc) return rc;
     HCLevel &C = L[l + 1];
-    CK(launch_nl_restrict<double>(A, C.G, L[l].u, L[l].f, C.r, C.u, s));
-    CK(launch_nl_op<double>(args(l + 1), NL_APPLY_PLUS, -1, C.u, C.r, C.f, C.uold, nullptr, s));
+    rc = ensure_tcl(l);
+    if (rc) return rc;
+    CK(launch_nlc_restrict(A, C.G, L[l].u, L[l].tcl, L[l].f, C.r, C.u, s));
+    tcl_ok[l + 1] = 0;
+    rc = ensure_tcl(l + 1);
+    if (rc) return rc;
+    CK(launch_nlc_op(args(l + 1), NL_APPLY_PLUS, -1, C.u, C.tcl, C.r, C.f, C.uold, nullptr, s));
     for (int m = 0; m < o.num_mg; m++) {
       rc = cycle(l + 1);
       if (rc) return rc;
     }
     CK(launch_prolong<double>(L[l].G, make_bcd(op.phi_bc), 2, o.prolong, L[l].u, C.u, C.uold, s));
+    tcl_ok[l] = 0;
     return relax(l, o.num_smooth_up);
   }
 
   int residual_norm() {
-    CK(launch_nl_op<double>(args(0), NL_RESIDUAL, o.norm_type, L[0].u, L[0].f, L[0].r, nullptr,
-                            part, s));
+    int rc = ensure_tcl(0);
+    if (rc) return rc;
+    CK(launch_nlc_op(args(0), NL_RESIDUAL, o.norm_type, L[0].u, L[0].tcl, L[0].f, L[0].r, nullptr,
+                     part, s));
     CK(launch_finalize_norm(o.norm_type, part, norm_parts(L[0].G.ncell), part + kMaxBlocks, s));
     CK(cudaMemcpyAsync(host_norm, part + kMaxBlocks, sizeof(double), cudaMemcpyDeviceToHost, s));
     return MLGPU_OK;
   }
 
+  // one FAS iteration; on entry tcl of level 0 is valid (the residual norm
+  // that ended the previous iteration, or the initial one, left it so)
   int iteration() {
+    tcl_ok[0] = 1;
     int rc = cycle(0);
     if (rc) return rc;
     return residual_norm();
@@ -909,9 +949,11 @@ class HCSolver : public mlgpu_solver {
     if (enter()) return MLGPU_ERR_CUDA;
     CK(cudaMemcpyAsync(L[0].u, user_phi, bytes, cudaMemcpyDeviceToDevice, s));
     CK(cudaMemcpyAsync(L[0].f, user_rhs, bytes, cudaMemcpyDeviceToDevice, s));
+    tcl_ok.assign(L.size(), 0);  // u of level 0 was just replaced
     if (kern_init < 0) {
       kern_init = count_kernels([&] { return residual_norm(); });
       kern_iter = count_kernels([&] { return iteration(); });
+      tcl_ok.assign(L.size(), 0);  // the counting captures launched nothing
     }
     int rc = residual_norm();
     if (rc) return rc;
@@ -945,7 +987,11 @@ class HCSolver : public mlgpu_solver {
       cudaGraphExecDestroy(graph);
       graph = nullptr;
     }
-    return MLGPU_OK;
+    // 1/diag depends on alpha and beta
+    if (enter()) return MLGPU_ERR_CUDA;
+    int rc = build_lambda();
+    if (!rc) rc = leave();
+    return rc;
   }
 };
 
