@@ -11,6 +11,7 @@
 #include "outer_kernels.cuh"
 #include "outer_fast_kernels.cuh"
 #include "nl_cached_kernels.cuh"
+#include "hcm_kernels.cuh"
 
 namespace mlgpu {
 
@@ -37,6 +38,10 @@ cudaError_t launch_be_rhs(long long n, const double *phi_old, const double *a, c
 cudaError_t launch_vc_outer_fast(const OuterFast &P, int norm, cudaStream_t s);
 cudaError_t launch_outer_coefs(const VCArgs<double> &A, double *cx, double *cy, double *diag,
                                cudaStream_t s);
+// mixed-precision nonlinear solve: FP64 closure Jacobian (stored FP32), u += e
+cudaError_t launch_hcm_jac(const Geom &G, const ClosureParams &cp, const double *u, float *J,
+                           cudaStream_t s);
+cudaError_t launch_hcm_update(long long n, double *u, const float *e, cudaStream_t s);
 // FP64 nonlinear kernels over the per-level (T, C_l) cache
 cudaError_t launch_nlc_closure(const NLArgs<double> &A, const double *phi, double *tcl,
                                cudaStream_t s);

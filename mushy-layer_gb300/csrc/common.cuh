@@ -154,6 +154,47 @@ __device__ __forceinline__ void t_cl(double H, double C, const ClosureParams &p,
   }
 }
 
+// Derivative of t_cl: J = {dT/dH, dT/dC, dC_l/dH, dC_l/dC}, regime by regime
+// (solid T = H/cp; eutectic constant; mush through the porosity root
+// a por^2 + b por + c = 0, differentiated implicitly, with C clamped at -CR
+// as CALCULATEPOROSITYMUSH does; liquid T = H - St, C_l = C).  Used by the
+// linearised inner cycles of the mixed-precision nonlinear solve; it has no
+// counterpart in the reference, which only evaluates the closure.
+__device__ __forceinline__ void t_cl_jac(double H, double C, const ClosureParams &p, double J[4]) {
+  double Hs, He, Hl;
+  bounding_energy(C, p, Hs, He, Hl);
+  J[0] = J[1] = J[2] = J[3] = 0.0;
+  if (H <= Hs) {
+    J[0] = 1.0 / p.cp;
+  } else if (H > Hs && H <= He) {
+    // eutectic: T and C_l fixed
+  } else if (H > He && H < Hl) {
+    double por = 1.0, dpH = 0.0, dpC = 0.0;
+    if (p.St != 0) {
+      const bool clamp = !(C >= -p.CR);
+      const double validC = clamp ? -p.CR : C;
+      const double a = p.CR * (p.cp - 1) + p.St * (p.k - 1);
+      const double b = p.CR * (1 - 2 * p.cp) + H * (1 - p.k) - validC * (p.cp - 1) - p.k * p.St;
+      const double c = (p.CR + validC) * p.cp + p.k * H;
+      const double sD = sqrt(b * b - 4 * a * c);
+      por = (-b - sD) / (2 * a);
+      const double dbH = 1 - p.k, dbC = clamp ? 0.0 : -(p.cp - 1);
+      const double dcH = p.k, dcC = clamp ? 0.0 : p.cp;
+      dpH = (-dbH - (b * dbH - 2 * a * dcH) / sD) / (2 * a);
+      dpC = (-dbC - (b * dbC - 2 * a * dcC) / sD) / (2 * a);
+    }
+    const double num = C + p.CR * (1 - por), den = por + p.k * (1 - por);
+    const double dCl_dpor = (-p.CR * den - num * (1 - p.k)) / (den * den);
+    J[2] = dCl_dpor * dpH;
+    J[3] = 1.0 / den + dCl_dpor * dpC;
+    J[0] = -J[2];
+    J[1] = -J[3];
+  } else if (H >= Hl) {
+    J[0] = 1.0;
+    J[3] = 1.0;
+  }
+}
+
 // ------------------------------------------------------------ thread helpers
 __device__ __forceinline__ long long gtid() {
   return (long long)blockIdx.x * blockDim.x + threadIdx.x;

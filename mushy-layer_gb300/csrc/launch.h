@@ -69,6 +69,12 @@ cudaError_t launch_vc_tile_smooth(const TileSmooth<T> &P, cudaStream_t s);
 int tile_max_halo(size_t elem);
 struct TileFast;
 cudaError_t launch_vc_tile_fast(const TileFast &P, cudaStream_t s);
+struct HCMArgs;
+cudaError_t launch_hcm_gsrb(const HCMArgs &A, float *e, const float *r, int pass, cudaStream_t s);
+cudaError_t launch_hcm_relax_block(const HCMArgs &A, float *e, const float *r, int sweeps,
+                                   cudaStream_t s);
+cudaError_t launch_hcm_restrict(const HCMArgs &A, const Geom &C, const float *e, const float *r,
+                                float *rc, cudaStream_t s);
 struct CycFast;
 cudaError_t launch_vc_cycle_fast(const CycFast &P, cudaStream_t s);
 cudaError_t launch_fast_coefs(const VCArgs<double> &A, float *cx, float *cy, float *lam,

@@ -5,6 +5,7 @@
 #include "launch_impl.cuh"
 #include "tile_fast_kernels.cuh"
 #include "cycle_fast_kernels.cuh"
+#include "hcm_kernels.cuh"
 
 namespace mlgpu {
 
@@ -66,6 +67,29 @@ cudaError_t launch_vc_cycle_fast(const CycFast &P, cudaStream_t s) {
   int threads = (quads + 31) / 32 * 32;
   if (threads < 64) threads = 64;
   vc_cycle_fast_kernel<<<1, threads, bytes, s>>>(P);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_hcm_gsrb(const HCMArgs &A, float *e, const float *r, int pass,
+                            cudaStream_t s) {
+  const int nb = blocks_for(colour_threads(A.G));
+  MLGPU_DIM_SWITCH(A.G.dim, (hcm_gsrb_kernel<DIM><<<nb, kBlock, 0, s>>>(A, e, r, pass)));
+  return cudaGetLastError();
+}
+
+cudaError_t launch_hcm_relax_block(const HCMArgs &A, float *e, const float *r, int sweeps,
+                                   cudaStream_t s) {
+  long long nt = colour_threads(A.G);
+  int threads = (int)((nt + 31) / 32 * 32);
+  if (threads > 1024) threads = 1024;
+  if (threads < 64) threads = 64;
+  MLGPU_DIM_SWITCH(A.G.dim, (hcm_relax_block_kernel<DIM><<<1, threads, 0, s>>>(A, e, r, sweeps)));
+  return cudaGetLastError();
+}
+
+cudaError_t launch_hcm_restrict(const HCMArgs &A, const Geom &C, const float *e, const float *r,
+                                float *rc, cudaStream_t s) {
+  MLGPU_DIM_SWITCH(A.G.dim, (hcm_restrict_kernel<DIM><<<blocks_for(C.ncell), kBlock, 0, s>>>(A, C, e, r, rc)));
   return cudaGetLastError();
 }
 

@@ -5,6 +5,7 @@
 #include "launch_impl.cuh"
 #include "outer_fast_kernels.cuh"
 #include "nl_cached_kernels.cuh"
+#include "hcm_kernels.cuh"
 
 namespace mlgpu {
 
@@ -81,6 +82,17 @@ cudaError_t launch_nlc_restrict(const NLArgs<double> &A, const Geom &C, const do
                                 const double *tcl, const double *rhs, double *res_c,
                                 double *phi_c, cudaStream_t s) {
   MLGPU_DIM_SWITCH(A.G.dim, (nlc_restrict_kernel<DIM><<<nlc_blocks(C.ncell), kNLCBlock, 0, s>>>(A, C, phi, tcl, rhs, res_c, phi_c)));
+  return cudaGetLastError();
+}
+
+cudaError_t launch_hcm_jac(const Geom &G, const ClosureParams &cp, const double *u, float *J,
+                           cudaStream_t s) {
+  hcm_jac_kernel<<<blocks_for(G.ncell), kBlock, 0, s>>>(G, cp, u, J);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_hcm_update(long long n, double *u, const float *e, cudaStream_t s) {
+  hcm_update_kernel<<<blocks_for(n), kBlock, 0, s>>>(n, u, e);
   return cudaGetLastError();
 }
 

@@ -759,6 +759,9 @@ struct HCLevel {
   double *u = nullptr, *f = nullptr, *r = nullptr, *uold = nullptr, *t = nullptr;
   double *tcl = nullptr;  // (T, C_l) of u, valid while tcl_ok says so
   double *lam = nullptr;  // stored 1/diag (resetLambda)
+  // mixed precision: FP32 correction, residual, closure Jacobian, 1/diag, coefficients
+  float *e32 = nullptr, *r32 = nullptr, *J32 = nullptr, *lam32 = nullptr;
+  float *a32 = nullptr, *b32[3] = {nullptr, nullptr, nullptr};
 };
 
 class HCSolver : public mlgpu_solver {
@@ -768,6 +771,18 @@ class HCSolver : public mlgpu_solver {
   std::vector<HCLevel> L;
   double *part = nullptr, *host_norm = nullptr;
   int kern_init = -1, kern_iter = -1;  // kernels per piece (counted)
+  bool mixed = false;  // FP32 linearised inner cycles in FP64 defect correction
+  // within a mixed solve: take linearised steps now?  The solve starts with
+  // FP64 FAS cycles (a linearisation at a state far from the solution
+  // overshoots across closure regime boundaries) and switches to the FP32
+  // linearised cycles once a FAS iteration has at least halved the residual;
+  // a linearised step that fails to reduce the residual goes back to FAS, and
+  // after two such failures the solve stays with FAS
+  bool lin = false;
+  int lin_fail = 0;
+  cudaGraphExec_t graph_m = nullptr;
+  int kern_iter_fas = -1;
+  double upd_fas = 0, upd_lin = 0;
   // per level: does tcl hold the closure of the current u?  Tracked on the
   // host along the launch sequence (the same sequence every iteration)
   std::vector<char> tcl_ok;
@@ -776,6 +791,7 @@ class HCSolver : public mlgpu_solver {
 
   ~HCSolver() override {
     if (graph) cudaGraphExecDestroy(graph);
+    if (graph_m) cudaGraphExecDestroy(graph_m);
     if (host_norm) cudaFreeHost(host_norm);
   }
 
@@ -803,6 +819,14 @@ class HCSolver : public mlgpu_solver {
       L[l].t = A.get<double>(n);
       L[l].tcl = A.get<double>(n);
       L[l].lam = A.get<double>(n);
+      if (mixed) {
+        L[l].e32 = A.get<float>(n);
+        L[l].r32 = A.get<float>(n);
+        L[l].J32 = A.get<float>(2 * n);
+        L[l].lam32 = A.get<float>(n);
+        if (op.aCoef) L[l].a32 = A.get<float>(n);
+        for (int d = 0; d < g.dim; d++) L[l].b32[d] = A.get<float>(2 * nfaces(g, d));
+      }
       g = coarsen_grid(g);
     }
     tcl_ok.assign(L.size(), 0);
@@ -819,28 +843,99 @@ class HCSolver : public mlgpu_solver {
     }
     int rc = build_lambda();
     if (rc) return rc;
-    double u = 0;
+    if (mixed) {
+      for (auto &lv : L) {
+        long long n = 2 * lv.G.ncell;
+        if (lv.a32) CK(launch_convert<float, double>(n, lv.a32, lv.c64.a, s));
+        for (int d = 0; d < lv.G.dim; d++)
+          CK(launch_convert<float, double>(2 * lv.G.nface(d), lv.b32[d], lv.c64.b[d], s));
+      }
+    }
     int last = (int)L.size() - 1;
     std::vector<double> visits(L.size(), 0);
     visits[0] = 1;
     for (int l = 1; l <= last; l++) visits[l] = visits[l - 1] * o.num_mg;
-    for (int l = 0; l <= last; l++) {
-      double n = (double)L[l].G.ncell;
-      if (l == last)
-        u += visits[l] * o.bottom_max_iter * n;
-      else
-        u += visits[l] * ((o.num_smooth_down + o.num_smooth_up) * n + n +
-                          (double)L[l + 1].G.ncell);
+    for (int lin_cycle = 0; lin_cycle < 2; lin_cycle++) {
+      double u = 0;
+      for (int l = 0; l <= last; l++) {
+        double n = (double)L[l].G.ncell;
+        if (l == last)
+          u += visits[l] * o.bottom_max_iter * n;
+        else  // the FAS cycle also applies the coarse operator once per visit
+          u += visits[l] * ((o.num_smooth_down + o.num_smooth_up) * n + n +
+                            (lin_cycle ? 0.0 : (double)L[l + 1].G.ncell));
+      }
+      (lin_cycle ? upd_lin : upd_fas) = u + (double)L[0].G.ncell;
     }
-    updates_per_iter = u + (double)L[0].G.ncell;
+    updates_per_iter = mixed ? upd_lin : upd_fas;
     return MLGPU_OK;
   }
 
   // stored 1/diag of every level (bitwise the inline resetLambda value)
   int build_lambda() {
-    for (size_t l = 0; l < L.size(); l++)
+    for (size_t l = 0; l < L.size(); l++) {
       CK(launch_nl_lambda<double>(args((int)l), L[l].lam, s));
+      if (L[l].lam32)
+        CK(launch_convert<float, double>(2 * L[l].G.ncell, L[l].lam32, L[l].lam, s));
+    }
     return MLGPU_OK;
+  }
+
+  // ---- mixed precision: FP32 cycles on the problem linearised at u
+  HCMArgs margs(int l) {
+    NLArgs<double> D = args(l);
+    HCMArgs M;
+    M.G = D.G;
+    M.phi_bc = D.phi_bc;
+    M.dbc = D.dbc;
+    M.apply_dbc = D.apply_dbc;
+    M.alpha = (float)D.alpha;
+    M.beta = (float)D.beta;
+    M.dxinv = (float)D.dxinv;
+    M.a = L[l].a32;
+    for (int d = 0; d < 3; d++) M.b[d] = L[l].b32[d];
+    M.J = L[l].J32;
+    M.lam = L[l].lam32;
+    return M;
+  }
+
+  // correction-scheme V-cycle on level l (e starts at zero)
+  int mcycle(int l) {
+    const int last = (int)L.size() - 1;
+    HCMArgs M = margs(l);
+    if (l == last) {
+      CK(launch_hcm_relax_block(M, L[l].e32, L[l].r32, o.bottom_max_iter, s));
+      return MLGPU_OK;
+    }
+    CK(cudaMemsetAsync(L[l].e32, 0, sizeof(float) * 2 * L[l].G.ncell, s));
+    for (int i = 0; i < o.num_smooth_down; i++)
+      for (int pass = 0; pass < 2; pass++) CK(launch_hcm_gsrb(M, L[l].e32, L[l].r32, pass, s));
+    CK(launch_hcm_restrict(M, L[l + 1].G, L[l].e32, L[l].r32, L[l + 1].r32, s));
+    for (int m = 0; m < o.num_mg; m++) {
+      int rc = mcycle(l + 1);
+      if (rc) return rc;
+    }
+    CK(launch_prolong<float>(L[l].G, make_bcd(op.phi_bc), 2, o.prolong, L[l].e32, L[l + 1].e32,
+                             nullptr, s));
+    for (int i = 0; i < o.num_smooth_up; i++)
+      for (int pass = 0; pass < 2; pass++) CK(launch_hcm_gsrb(M, L[l].e32, L[l].r32, pass, s));
+    return MLGPU_OK;
+  }
+
+  // one defect-correction step: J at the current state on every level (the
+  // state restricted by averaging), FP32 cycle on r = f - N(u) (left in
+  // L[0].r by the previous residual), u += e, FP64 residual and norm
+  int iteration_mixed() {
+    for (size_t l = 1; l < L.size(); l++)
+      CK(launch_restrict_avg<double>(L[l - 1].G, 2, L[l - 1].u, L[l].u, s));
+    for (size_t l = 0; l < L.size(); l++)
+      CK(launch_hcm_jac(L[l].G, args((int)l).cp, L[l].u, L[l].J32, s));
+    CK(launch_convert<float, double>(2 * L[0].G.ncell, L[0].r32, L[0].r, s));
+    int rc = mcycle(0);
+    if (rc) return rc;
+    CK(launch_hcm_update(2 * L[0].G.ncell, L[0].u, L[0].e32, s));
+    tcl_ok[0] = 0;
+    return residual_norm();
   }
 
   // make tcl of level l the closure of its u
@@ -920,6 +1015,7 @@ class HCSolver : public mlgpu_solver {
   // that ended the previous iteration, or the initial one, left it so)
   int iteration() {
     tcl_ok[0] = 1;
+    if (mixed && lin) return iteration_mixed();
     int rc = cycle(0);
     if (rc) return rc;
     return residual_norm();
@@ -927,18 +1023,19 @@ class HCSolver : public mlgpu_solver {
 
   int run_iteration() {
     if (!o.use_graph) return iteration();
-    if (!graph) {
+    cudaGraphExec_t &gx = (mixed && lin) ? graph_m : graph;
+    if (!gx) {
       cudaGraph_t g;
       CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
       int rc = iteration();
       cudaError_t e = cudaStreamEndCapture(s, &g);
       if (rc) return rc;
       CK(e);
-      e = cudaGraphInstantiate(&graph, g, 0);
+      e = cudaGraphInstantiate(&gx, g, 0);
       cudaGraphDestroy(g);
       CK(e);
     }
-    CK(cudaGraphLaunch(graph, s));
+    CK(cudaGraphLaunch(gx, s));
     return MLGPU_OK;
   }
 
@@ -952,9 +1049,14 @@ class HCSolver : public mlgpu_solver {
     tcl_ok.assign(L.size(), 0);  // u of level 0 was just replaced
     if (kern_init < 0) {
       kern_init = count_kernels([&] { return residual_norm(); });
+      lin = mixed;
       kern_iter = count_kernels([&] { return iteration(); });
+      lin = false;
+      kern_iter_fas = count_kernels([&] { return iteration(); });
       tcl_ok.assign(L.size(), 0);  // the counting captures launched nothing
     }
+    lin = false;
+    lin_fail = 0;
     int rc = residual_norm();
     if (rc) return rc;
     CK(cudaStreamSynchronize(s));
@@ -965,13 +1067,27 @@ class HCSolver : public mlgpu_solver {
     st->kernel_launches = kern_init;
     if (!std::isfinite(S.norm0)) S.status = 8;
     while (outer_continue(o, S)) {
+      const bool was_lin = mixed && lin;
       rc = run_iteration();
       if (rc) return rc;
       CK(cudaStreamSynchronize(s));
       S.norm = *host_norm;
       st->cycles += 1;
-      st->cell_updates += updates_per_iter;
-      st->kernel_launches += kern_iter;
+      st->cell_updates += was_lin ? upd_lin : upd_fas;
+      st->kernel_launches += was_lin ? kern_iter : kern_iter_fas;
+      if (was_lin && std::isfinite(S.norm) && S.norm > (1.0 - o.hang) * S.prev &&
+          S.norm > o.tolerance * S.norm0) {
+        // the linearised step did not reduce the FP64 residual: back to FP64
+        // FAS cycles (the state and its FP64 residual stay valid)
+        lin = false;
+        lin_fail++;
+        S.iter++;
+        if (S.iter < 64) st->norm_history[S.iter] = S.norm;
+        S.prev = S.norm;
+        continue;
+      }
+      if (mixed && !was_lin && lin_fail < 2 && std::isfinite(S.norm) && S.norm < 0.5 * S.prev)
+        lin = true;
       outer_after(o, S, st);
     }
     CK(cudaMemcpyAsync(user_phi, L[0].u, bytes, cudaMemcpyDeviceToDevice, s));
@@ -983,10 +1099,11 @@ class HCSolver : public mlgpu_solver {
   int set_alpha_beta(double a, double b) override {
     op.alpha = a;
     op.beta = b;
-    if (graph) {
-      cudaGraphExecDestroy(graph);
-      graph = nullptr;
-    }
+    for (auto *gp : {&graph, &graph_m})
+      if (*gp) {
+        cudaGraphExecDestroy(*gp);
+        *gp = nullptr;
+      }
     // 1/diag depends on alpha and beta
     if (enter()) return MLGPU_ERR_CUDA;
     int rc = build_lambda();
@@ -1091,6 +1208,7 @@ int mlgpu_hc_solver_workspace(const mlgpu_nlop *op, const mlgpu_mg_options *o, s
   HCSolver S;
   S.op = *op;
   S.o = *o;
+  S.mixed = o->precision == MLGPU_PREC_MIXED;
   *bytes = S.layout(nullptr);
   return MLGPU_OK;
 }
@@ -1099,13 +1217,15 @@ int mlgpu_hc_solver_create(const mlgpu_nlop *op, const mlgpu_mg_options *o, void
                            size_t bytes, void *stream, mlgpu_solver **out) {
   if (!op || !valid_grid(&op->grid) || !valid_options(o) || !ws || !out) return MLGPU_ERR_ARG;
   if (op->dtype != MLGPU_F64) return MLGPU_ERR_ARG;
-  if (o->precision != MLGPU_PREC_F64) return MLGPU_ERR_ARG;
+  // mixed precision needs red/black smoothing (the linearised cycles)
+  if (o->precision == MLGPU_PREC_MIXED && o->relax_mode != MLGPU_RELAX_GSRB) return MLGPU_ERR_ARG;
   for (int d = 0; d < op->grid.dim; d++)
     if (!op->bCoef[d]) return MLGPU_ERR_ARG;
   if (((uintptr_t)ws) & 255) return MLGPU_ERR_WORKSPACE;
   HCSolver *S = new HCSolver;
   S->op = *op;
   S->o = *o;
+  S->mixed = o->precision == MLGPU_PREC_MIXED;
   cudaGetLastError();
   if (S->init_streams((cudaStream_t)stream)) {
     delete S;

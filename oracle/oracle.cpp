@@ -242,6 +242,45 @@ inline void t_cl(double H, double C, const mlgpu_params &p, double &T, double &C
   }
 }
 
+// Derivative of t_cl, J = {dT/dH, dT/dC, dC_l/dH, dC_l/dC} (no counterpart in
+// the reference: the linearisation used by the mixed-precision nonlinear
+// solve).  Regimes as t_cl; in the mush the porosity root of
+// a por^2 + b por + c = 0 is differentiated implicitly, C clamped at -CR.
+inline void t_cl_jac(double H, double C, const mlgpu_params &p, double J[4]) {
+  double Hs, He, Hl;
+  bounding_energy(C, p, Hs, He, Hl);
+  const double CR = p.compositionRatio, k = p.waterDistributionCoeff,
+               cp = p.specificHeatRatio, St = p.stefan;
+  J[0] = J[1] = J[2] = J[3] = 0.0;
+  if (H <= Hs) {
+    J[0] = 1.0 / cp;
+  } else if (H > Hs && H <= He) {
+  } else if (H > He && H < Hl) {
+    double por = 1.0, dpH = 0.0, dpC = 0.0;
+    if (St != 0) {
+      const bool clamp = !(C >= -CR);
+      const double vC = clamp ? -CR : C;
+      const double a = CR * (cp - 1) + St * (k - 1);
+      const double b = CR * (1 - 2 * cp) + H * (1 - k) - vC * (cp - 1) - k * St;
+      const double c = (CR + vC) * cp + k * H;
+      const double sD = std::sqrt(b * b - 4 * a * c);
+      por = (-b - sD) / (2 * a);
+      const double dbH = 1 - k, dbC = clamp ? 0.0 : -(cp - 1), dcH = k, dcC = clamp ? 0.0 : cp;
+      dpH = (-dbH - (b * dbH - 2 * a * dcH) / sD) / (2 * a);
+      dpC = (-dbC - (b * dbC - 2 * a * dcC) / sD) / (2 * a);
+    }
+    const double num = C + CR * (1 - por), den = por + k * (1 - por);
+    const double dcl = (-CR * den - num * (1 - k)) / (den * den);
+    J[2] = dcl * dpH;
+    J[3] = 1.0 / den + dcl * dpC;
+    J[0] = -J[2];
+    J[1] = -J[3];
+  } else if (H >= Hl) {
+    J[0] = 1.0;
+    J[3] = 1.0;
+  }
+}
+
 // CALCULATEPOROSITY/CL/CS/T (src/EnthalpyVariablesF.ChF:13-284) for one cell.
 inline void full_closure(double H, double C, const mlgpu_params &p, double &T,
                          double &por, double &Cl, double &Cs, double &Hs, double &He,
@@ -581,6 +620,18 @@ int orc_closure_tcl(const mlgpu_grid *g, const mlgpu_params *p, const double *HC
   size_t n = ncells(*g);
 #pragma omp parallel for schedule(static)
   for (size_t q = 0; q < n; q++) t_cl(HC[q], HC[n + q], *p, TCl[q], TCl[n + q]);
+  return 0;
+}
+
+// J[4][cells] = d(T, C_l)/d(H, C) of every cell
+int orc_closure_jac(const mlgpu_grid *g, const mlgpu_params *p, const double *HC, double *J) {
+  size_t n = ncells(*g);
+#pragma omp parallel for schedule(static)
+  for (size_t q = 0; q < n; q++) {
+    double j4[4];
+    t_cl_jac(HC[q], HC[n + q], *p, j4);
+    for (int m = 0; m < 4; m++) J[m * n + q] = j4[m];
+  }
   return 0;
 }
 

@@ -29,6 +29,7 @@ def lib():
         sig = {
             "orc_closure": (i, [P(abi.Grid), P(abi.Params)] + [vp] * 8),
             "orc_closure_tcl": (i, [P(abi.Grid), P(abi.Params), vp, vp]),
+            "orc_closure_jac": (i, [P(abi.Grid), P(abi.Params), vp, vp]),
             "orc_nl_residual": (i, [P(abi.NLOp), vp, vp, vp]),
             "orc_nl_apply": (i, [P(abi.NLOp), vp, vp]),
             "orc_nl_gsrb_pass": (i, [P(abi.NLOp), vp, vp, i]),
@@ -93,6 +94,14 @@ def closure(g, p, HC):
 def closure_tcl(g, p, HC):
     out = np.zeros_like(HC)
     lib().orc_closure_tcl(C.byref(g), C.byref(p), _p(HC), _p(out))
+    return out
+
+
+def closure_jac(g, p, HC):
+    """d(T, C_l)/d(H, C) per cell: array [4][cells] = dT/dH, dT/dC, dCl/dH, dCl/dC."""
+    n = HC.size // 2
+    out = np.zeros((4,) + HC.shape[1:])
+    lib().orc_closure_jac(C.byref(g), C.byref(p), _p(HC), _p(out))
     return out
 
 

@@ -537,6 +537,71 @@ def test_hc_solver_fp64_matches_oracle():
         assert st.cell_updates == st_ref.cell_updates
 
 
+@pytest.mark.parametrize("n,dt", [((48, 32), 1e-3), ((64, 64), 1e-3)])
+def test_hc_solver_mixed_converges_to_fp64_solution(n, dt):
+    """Mixed precision for the nonlinear (H, C) solve: FP32 cycles on the
+    problem linearised with the FP64 closure Jacobian, inside an FP64
+    defect-correction loop (switching to FP64 FAS cycles if a linearised step
+    fails to reduce the residual: the 64x64 case needs it).  It reaches 1e-10
+    under the oracle's own FP64 residual and agrees with the FP64 FAS
+    solution to 1e-8."""
+    from mushy_gb300 import ops
+    g = P.grid(n)
+    p = P.mushy_params()
+    phi_bc, der = P.hc_bcs("mixed")
+    rng = np.random.default_rng(44)
+    phi = P.hc_state(g, rng, regimes=False)  # straddles the liquidus (mush + liquid)
+    b = [np.stack([-np.ones(abi.face_shape(g, d)), -0.01 * np.ones(abi.face_shape(g, d))])
+         for d in range(2)]
+    rhs = phi.copy()
+    ref = O.NLOpHost(g, p, phi_bc, der, 1.0, -dt, None, b)
+    op = ops.NLMultiCompOp(g, p, phi_bc, der, 1.0, -dt, None, [dev(x) for x in b])
+    sols = {}
+    for prec in (abi.PREC_F64, abi.PREC_MIXED):
+        o = ops.default_options(True)
+        o.max_iter, o.tolerance, o.hang, o.precision = 60, 1e-10, 1e-15, prec
+        d_phi = dev(phi)
+        st, rc = ops.AMRFASMultiGrid(op, o).solve(d_phi, dev(rhs))
+        sols[prec] = (host(d_phi), st, rc)
+    um, stm, rcm = sols[abi.PREC_MIXED]
+    assert rcm == 0 and stm.final_norm <= 1e-10 * stm.initial_norm
+    r0 = np.abs(O.nl_residual(ref, phi, rhs)).max()
+    assert np.abs(O.nl_residual(ref, um, rhs)).max() <= 1.05e-10 * r0
+    u64, st64, rc64 = sols[abi.PREC_F64]
+    if rc64 == 0:
+        assert np.abs(um - u64).max() <= 1e-8 * np.abs(u64).max()
+
+
+def test_hc_backward_euler_mixed_matches_fp64():
+    """Three backward-Euler steps with the mixed nonlinear solve against the
+    FP64 FAS, both iterated to 1e-10."""
+    from mushy_gb300 import ops
+    n, dt = 32, 1e-3
+    g = P.grid((n, n))
+    p = P.mushy_params()
+    phi_bc, der = P.hc_bcs("mixed")
+    rng = np.random.default_rng(45)
+    phi = P.hc_state(g, rng, regimes=False)
+    b = [np.stack([-np.ones(abi.face_shape(g, d)), -0.02 * np.ones(abi.face_shape(g, d))])
+         for d in range(2)]
+    src = dev(0.1 * rng.standard_normal(phi.shape))
+    op = ops.NLMultiCompOp(g, p, phi_bc, der, 1.0, 1.0, None, [dev(x) for x in b])
+    out = {}
+    for prec in (abi.PREC_F64, abi.PREC_MIXED):
+        o = ops.default_options(True)
+        o.max_iter, o.tolerance, o.hang, o.precision = 60, 1e-10, 1e-15, prec
+        S = ops.AMRFASMultiGrid(op, o)
+        cur = dev(phi)
+        for _ in range(3):
+            new = cur.clone()
+            st, rc = S.backwardEuler(new, cur, dt, src=src)
+            assert rc == 0, (prec, rc, st.iterations)
+            cur = new
+        out[prec] = host(cur)
+    scale = np.abs(out[abi.PREC_F64]).max()
+    assert np.abs(out[abi.PREC_MIXED] - out[abi.PREC_F64]).max() <= 1e-8 * scale
+
+
 # ------------------------------------------------- composed "next" rows
 def test_mac_project_bitwise_and_divergence_free():
     from mushy_gb300 import ops

@@ -65,6 +65,38 @@ def test_closure_tcl_matches_full_closure():
     assert np.array_equal(tcl[0], full["T"]) and np.array_equal(tcl[1], full["Cl"])
 
 
+def test_closure_jacobian_matches_finite_differences():
+    """d(T, C_l)/d(H, C) of the closure (linearised inner cycles of the mixed
+    nonlinear solve) against central differences, away from regime edges."""
+    rng = np.random.default_rng(3)
+    g = P.grid((64, 32))
+    p = P.mushy_params(specificHeatRatio=1.2, waterDistributionCoeff=0.02)
+    HC = P.hc_state(g, rng)
+    J = O.closure_jac(g, p, HC).reshape(4, -1)
+    h = 1e-6
+    fd = np.empty_like(J)
+    for col in range(2):
+        dp, dm = HC.copy(), HC.copy()
+        dp[col] += h
+        dm[col] -= h
+        tp = O.closure_tcl(g, p, dp).reshape(2, -1)
+        tm = O.closure_tcl(g, p, dm).reshape(2, -1)
+        fd[0 + col] = (tp[0] - tm[0]) / (2 * h)
+        fd[2 + col] = (tp[1] - tm[1]) / (2 * h)
+    # cells whose regime is the same at +-h (the closure is piecewise smooth)
+    reg = lambda x: O.closure(g, p, x)["porosity"].reshape(-1)
+    same = np.ones(J.shape[1], bool)
+    for col in range(2):
+        for sgn in (1, -1):
+            d = HC.copy()
+            d[col] += sgn * 2 * h
+            pr, p0 = reg(d), reg(HC)
+            same &= ((pr < 1) == (p0 < 1)) & ((pr > 0) == (p0 > 0))
+    assert same.sum() > 0.9 * same.size
+    err = np.abs(J[:, same] - fd[:, same])
+    assert np.all(err <= 1e-6 * (1 + np.abs(fd[:, same]))), err.max()
+
+
 def test_porosity_clamps_c_below_minus_cr():
     # CALCULATEPOROSITYMUSH uses max(C, -CR); the scalar C++ version does not
     g = P.grid((1, 1))
