@@ -309,8 +309,12 @@ int mlgpu_vc_solver_workspace(const mlgpu_vcop *op, const mlgpu_mg_options *o,
                               size_t *bytes);
 
 /* FAS multigrid for the nonlinear H-C operator (AMRFASMultiGrid driving
- * AMRNonLinearMultiCompOp; MGnewOp coarsening :1285-1501).  `op` must be FP64;
- * the mixed precision variant builds FP32 copies inside the workspace. */
+ * AMRNonLinearMultiCompOp; MGnewOp coarsening :1285-1501).  `op` must be FP64.
+ * MLGPU_PREC_MIXED (GSRB smoothing only) keeps the FP64 nonlinear residual and
+ * takes FP32 cycles on the problem linearised with the closure Jacobian once a
+ * FAS iteration has at least halved the residual, going back to FAS cycles
+ * when a linearised step does not reduce it (no counterpart in the
+ * reference); the FP32 copies live inside the workspace. */
 int mlgpu_hc_solver_create(const mlgpu_nlop *op, const mlgpu_mg_options *o,
                            void *workspace, size_t bytes, void *stream,
                            mlgpu_solver **out);
