@@ -140,7 +140,8 @@ typedef struct mlgpu_mg_options {
 } mlgpu_mg_options;
 
 typedef struct mlgpu_solve_stats {
-  int exit_status;       /* 0 converged, 2 hang, 4 max_iter, 8 NaN, ... */
+  int exit_status;       /* 0 converged, 2 hang, 4 max_iter, 8 NaN, 16 a device-side
+                            wait ran past its bound (solve returns MLGPU_ERR_CUDA) */
   int iterations;        /* outer iterations done */
   int cycles;            /* V-cycles done (all precisions) */
   int levels;            /* multigrid depth used */

@@ -77,6 +77,9 @@ cudaError_t launch_hcm_restrict(const HCMArgs &A, const Geom &C, const float *e,
                                 float *rc, cudaStream_t s);
 struct CycFast;
 cudaError_t launch_vc_cycle_fast(const CycFast &P, cudaStream_t s);
+struct FastCoefs;
+cudaError_t launch_cyc_pack(const Geom &G, const BCD &bc, const FastCoefs &K, float *level,
+                            cudaStream_t s);
 cudaError_t launch_fast_coefs(const VCArgs<double> &A, float *cx, float *cy, float *lam,
                               float *diag, cudaStream_t s);
 

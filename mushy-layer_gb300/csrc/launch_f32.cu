@@ -59,14 +59,32 @@ cudaError_t launch_vc_tile_fast(const TileFast &P, cudaStream_t s) {
 }
 
 cudaError_t launch_vc_cycle_fast(const CycFast &P, cudaStream_t s) {
-  if (P.nlev < 2 || P.nlev > kFastCycLevels || P.G[0].dim != 2) return cudaErrorInvalidValue;
+  if (P.nlev < 2 || P.nlev > kFastCycLevels || P.G[0].dim != 2 || !P.pack) return cudaErrorInvalidValue;
+  if (P.G[0].ncell > kFastCycCells || (P.off[P.nlev] & 3)) return cudaErrorInvalidValue;
   const int quads = (P.G[0].n0 / 2) * (P.G[0].n1 / 2);
   if (quads > kFastCycThreads) return cudaErrorInvalidValue;
   size_t bytes = cyc_fast_smem_bytes(P);
-  if (bytes > 48 * 1024) return cudaErrorInvalidValue;
+  if (bytes > kMaxDynSmem) return cudaErrorInvalidValue;
+  // raise the dynamic shared-memory limit only as far as needed: the kernel
+  // also has static shared memory (level table, barrier), and static +
+  // dynamic must stay within the per-block opt-in maximum
+  static size_t attr_bytes = 48 * 1024;
+  if (bytes > attr_bytes) {
+    cudaError_t e = cudaFuncSetAttribute(vc_cycle_fast_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e != cudaSuccess) return e;
+    attr_bytes = bytes;
+  }
   int threads = (quads + 31) / 32 * 32;
   if (threads < 64) threads = 64;
   vc_cycle_fast_kernel<<<1, threads, bytes, s>>>(P);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_cyc_pack(const Geom &G, const BCD &bc, const FastCoefs &K, float *level,
+                            cudaStream_t s) {
+  if (G.dim != 2 || G.ncell > 65535) return cudaErrorInvalidValue;
+  cyc_pack_kernel<<<blocks_for(cyc_pad((int)G.ncell)), kBlock, 0, s>>>(G, bc, K, level);
   return cudaGetLastError();
 }
 

@@ -13,8 +13,12 @@ namespace mlgpu {
 struct OuterDev {
   double norm0, norm, prev;
   int iter, status, parity, cont;
+  int fault;  // set by a kernel whose bounded wait ran out; ends the loop
   double hist[64];
 };
+
+// exit status of a solve that a device-side wait timeout ended
+constexpr int kStatusDeviceFault = 16;
 
 struct OuterCfg {
   double tolerance, hang, norm_thresh;
@@ -31,7 +35,9 @@ __device__ __forceinline__ void outer_decide_step(OuterDev *st, double norm, con
   if (iter < 64) st->hist[iter] = norm;
   st->parity ^= 1;
   int status = 0;
-  if (!isfinite(norm)) {
+  if (st->fault) {
+    status = kStatusDeviceFault;
+  } else if (!isfinite(norm)) {
     status = 8;
   } else if (norm > (1.0 - c.hang) * st->prev && norm > c.tolerance * st->norm0) {
     status = 2;

@@ -175,6 +175,7 @@ int outer_finish(const mlgpu_mg_options &o, Outer &S, mlgpu_solve_stats *st) {
   st->final_norm = S.norm;
   if (S.status == 0 && S.norm > o.tolerance * S.norm0 && S.norm0 > o.norm_thresh) S.status = 4;
   st->exit_status = S.status;
+  if (S.status == kStatusDeviceFault) return MLGPU_ERR_CUDA;
   if (S.status == 8) return MLGPU_ERR_NAN;
   if (S.status == 2) return MLGPU_ERR_HANG;
   if (S.status == 4) return MLGPU_ERR_NOT_CONVERGED;
@@ -211,6 +212,10 @@ class VCSolver : public mlgpu_solver {
   bool use_tiles = true;
   double updates_per_iter = 0;
   int kern_init = -1, kern_iter = -1, kern_loop = -1;  // kernels per piece (counted)
+  // level pack of the lean FP32 coarse cycle (mixed 2D): levels cyc_top..last
+  float *cyc_pack = nullptr;
+  int cyc_top = -1;
+  std::vector<int> cyc_off;
 
   ~VCSolver() override {
     for (auto &g : graph)
@@ -281,6 +286,25 @@ class VCSolver : public mlgpu_solver {
       g = coarsen_grid(g);
     }
     use_block_cycle = o.relax_mode == MLGPU_RELAX_GSRB && o.num_mg == 1 && o.fuse_levels;
+    // the lean coarse cycle starts at the first level of at most kFastCycCells
+    cyc_top = -1;
+    cyc_off.clear();
+    if (mixed && op.grid.dim == 2) {
+      for (int l = 0; l < depth; l++)
+        if (L[l].G.ncell <= kFastCycCells && depth - l + 1 <= kFastCycLevels) {
+          cyc_top = l;
+          break;
+        }
+      if (cyc_top >= 0) {
+        int o2 = 0;
+        for (int l = cyc_top; l <= depth; l++) {
+          cyc_off.push_back(o2);
+          o2 += cyc_pack_level_floats((int)L[l].G.ncell);
+        }
+        cyc_off.push_back(o2);
+        cyc_pack = A.get<float>(o2);
+      }
+    }
     // FP32 tiles pay for their halo recomputation; FP64 tiles (4 extra half
     // sweeps of redundant FP64 work per tile) only when asked for explicitly
     use_tiles = use_block_cycle && (mixed || o.fuse_levels >= 2);
@@ -342,6 +366,11 @@ class VCSolver : public mlgpu_solver {
       A.lam = nullptr;
       CK(launch_fast_coefs(A, L[l].fcx, L[l].fcy, L[l].flam, L[l].fdiag, s));
     }
+    if (cyc_top >= 0)
+      for (int l = cyc_top; l < (int)L.size(); l++)
+        CK(launch_cyc_pack(L[l].G, make_bcd(op.bc),
+                           FastCoefs{L[l].fcx, L[l].fcy, L[l].flam, L[l].fdiag},
+                           cyc_pack + cyc_off[l - cyc_top], s));
     return MLGPU_OK;
   }
 
@@ -516,7 +545,7 @@ class VCSolver : public mlgpu_solver {
       // this level and every coarser one inside one thread block
       if constexpr (sizeof(T) == 4) {
         const Geom &G0 = L[l].G;
-        if (L[l].fcx && last - l + 1 <= kFastCycLevels &&
+        if (L[l].fcx && l == cyc_top && last - l + 1 <= kFastCycLevels &&
             (G0.n0 / 2) * (G0.n1 / 2) <= kFastCycThreads) {
           // lean FP32 form with the precomputed face weights and 1/diag
           CycFast F;
@@ -527,12 +556,12 @@ class VCSolver : public mlgpu_solver {
           F.prolong = o.prolong;
           F.zero_init = zero_init ? 1 : 0;
           F.bc = make_bcd(op.bc);
-          for (int m = 0; m < F.nlev; m++) {
-            F.G[m] = L[l + m].G;
-            F.K[m] = FastCoefs{L[l + m].fcx, L[l + m].fcy, L[l + m].flam, L[l + m].fdiag};
-          }
+          for (int m = 0; m < F.nlev; m++) F.G[m] = L[l + m].G;
+          for (int m = 0; m <= F.nlev; m++) F.off[m] = cyc_off[m];
+          F.pack = reinterpret_cast<const float4 *>(cyc_pack);
           F.e0 = (float *)L[l].e;
           F.r0 = (const float *)L[l].r;
+          F.fault = &dev_state->fault;
           CK(launch_vc_cycle_fast(F, s));
           return MLGPU_OK;
         }
@@ -687,6 +716,7 @@ class VCSolver : public mlgpu_solver {
     if (enter()) return MLGPU_ERR_CUDA;
     CK(cudaMemcpyAsync(phi[0], user_phi, bytes, cudaMemcpyDeviceToDevice, s));
     CK(cudaMemcpyAsync(rhs, user_rhs, bytes, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemsetAsync(&dev_state->fault, 0, sizeof(int), s));
     // initial residual (no update)
     if (kern_init < 0) {
       kern_init = count_kernels([&] { return initial_residual(); });
@@ -735,7 +765,10 @@ class VCSolver : public mlgpu_solver {
       outer_after(o, S, st);
     }
     CK(cudaMemcpyAsync(user_phi, phi[cur], bytes, cudaMemcpyDeviceToDevice, s));
+    // a kernel whose bounded wait ran out leaves its mark in the device state
+    CK(cudaMemcpyAsync(&host_state->fault, &dev_state->fault, sizeof(int), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
+    if (host_state->fault) S.status = kStatusDeviceFault;
     if (leave()) return MLGPU_ERR_CUDA;
     return outer_finish(o, S, st);
   }
