@@ -43,6 +43,20 @@ extern "C" {
 /* ---------------------------------------------------------------- types */
 enum { MLGPU_F64 = 0, MLGPU_F32 = 1 };
 enum { MLGPU_BC_NEUMANN = 0, MLGPU_BC_DIRICHLET = 1 };
+/* Temperature conditions applied to the enthalpy ghost cells of the (H, C)
+ * operator (PhysBCUtil::FixedTemperature, TemperatureFlux,
+ * TemperatureFluxRadiation; BCutil/PhysBCUtil.cpp:590-722): the ghost
+ * enthalpy is solved so that the ghost temperature meets the Robin condition
+ * a (T_g - T_i)/dx = F + b (T_b - T_ref), T_b = (T_g + T_i)/2, on each side
+ * (NonlinearTemperatureBCRobin's predicted ghost temperature; see mlgpu_nlbc).  Only phi_bc comp 0 (H) of a
+ * nonlinear operator may use them (the reference stops with "Can't apply
+ * temperature bcs to bulk concentration"); elsewhere they are MLGPU_ERR_ARG. */
+enum {
+  MLGPU_BC_FIXED_TEMPERATURE = 2,         /* value = T on the boundary */
+  MLGPU_BC_TEMPERATURE_FLUX = 3,          /* value = F (a = 1, b = 0) */
+  MLGPU_BC_TEMPERATURE_FLUX_RADIATION = 4 /* value = F, a, b, T_ref from mlgpu_nlbc */
+};
+enum { MLGPU_NLBC_PICARD = 0, MLGPU_NLBC_NEWTON = 1 };
 enum { MLGPU_RELAX_GSRB = 1, MLGPU_RELAX_JACOBI = 4 };     /* reference s_relaxMode */
 enum { MLGPU_PROLONG_CONSTANT = 0, MLGPU_PROLONG_LINEAR = 1 };
 enum { MLGPU_BOTTOM_RELAX = 0, MLGPU_BOTTOM_BICGSTAB = 1 };
@@ -79,6 +93,22 @@ typedef struct mlgpu_params {
   double viscosityCoeff;
 } mlgpu_params;
 
+/* Parameters of the nonlinear temperature conditions (BCutil/NonlinearBC.H:
+ * NonlinearTemperatureBCRobin residual, Picard / Newton ghost solvers;
+ * MushyLayerParams max_bc_iter 2, max_bc_residual 1e-5, bc_relax_coeff 0.5). */
+typedef struct mlgpu_nlbc {
+  double a[3][2], b[3][2], T_ref[3][2];  /* radiation coefficients per [dir][side] */
+  double no_flux_limit[3][2];  /* below this position (cell centre along the next
+                                  direction) the ghost enthalpy is the interior one */
+  int method;                  /* MLGPU_NLBC_PICARD or MLGPU_NLBC_NEWTON */
+  int max_iter;                /* max_bc_iter */
+  double max_residual;         /* max_bc_residual */
+  double relax_coeff;          /* bc_relax_coeff (Picard) */
+  double dx;                   /* spacing the condition is built with (PhysBCUtil
+                                  m_dx: the AMR level's spacing, also on the
+                                  coarser multigrid levels); 0 = the grid's dx */
+} mlgpu_nlbc;
+
 /* Nonlinear enthalpy/bulk-concentration operator
  *   L(phi) = alpha a phi - beta div(b grad f(phi)),  phi = (H, C), f = (T, C_l)
  * (AMRNonLinearMultiCompOp).  Coefficient pointers are device pointers in the
@@ -93,6 +123,7 @@ typedef struct mlgpu_nlop {
   const void *aCoef;     /* [2][cells] or NULL */
   const void *bCoef[3];  /* [2][faces_d] per direction */
   int dtype;
+  mlgpu_nlbc nlbc;       /* used where phi_bc comp 0 has a temperature type */
 } mlgpu_nlop;
 
 /* Linear variable-coefficient operator for one component

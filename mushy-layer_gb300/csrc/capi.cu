@@ -30,6 +30,7 @@ NLArgs<T> make_nl_args(const mlgpu_nlop &op) {
   A.cp = make_cp(op.params);
   A.phi_bc = make_bcd(op.phi_bc);
   A.dbc = make_bcd(op.derived_bc);
+  A.nlbc = make_nlbcd(op.phi_bc, op.nlbc, op.grid.dx);
   A.apply_dbc = op.apply_derived_bc;
   double dxinv = 1.0 / (op.grid.dx * op.grid.dx);
   A.alpha = (T)op.alpha;
@@ -64,8 +65,39 @@ template VCArgs<float> make_vc_args<float>(const mlgpu_vcop &);
 
 int status_of(cudaError_t e) { return e == cudaSuccess ? MLGPU_OK : MLGPU_ERR_CUDA; }
 
+// BC types: Neumann/Dirichlet everywhere, temperature conditions only on
+// component 0 of a nonlinear operator's (H, C) condition
+bool valid_bc(const mlgpu_bc &b, int dim, bool temperature_h) {
+  for (int d = 0; d < dim; d++)
+    for (int s = 0; s < 2; s++)
+      for (int c = 0; c < 2; c++) {
+        const int t = b.type[d][s][c];
+        if (t == MLGPU_BC_NEUMANN || t == MLGPU_BC_DIRICHLET) continue;
+        if (temperature_h && c == 0 && is_temperature_bc(t)) continue;
+        return false;
+      }
+  return true;
+}
+
+bool valid_nl_bcs(const mlgpu_nlop &op) {
+  if (!valid_bc(op.phi_bc, op.grid.dim, true) || !valid_bc(op.derived_bc, op.grid.dim, false))
+    return false;
+  const mlgpu_nlbc &n = op.nlbc;
+  if (n.method != MLGPU_NLBC_PICARD && n.method != MLGPU_NLBC_NEWTON) return false;
+  if (n.max_iter < 0 || !(n.dx >= 0)) return false;
+  // a Robin denominator a/dx - b/2 of zero has no ghost value
+  for (int d = 0; d < op.grid.dim; d++)
+    for (int s = 0; s < 2; s++)
+      if (op.phi_bc.type[d][s][0] == MLGPU_BC_TEMPERATURE_FLUX_RADIATION) {
+        const double dxb = n.dx > 0 ? n.dx : op.grid.dx;
+        if (!(n.a[d][s] / dxb - n.b[d][s] / 2 != 0)) return false;
+      }
+  return true;
+}
+
 static bool valid_nlop(const mlgpu_nlop *op) {
   if (!op || !valid_grid(&op->grid)) return false;
+  if (!valid_nl_bcs(*op)) return false;
   if (op->dtype != MLGPU_F64 && op->dtype != MLGPU_F32) return false;
   for (int d = 0; d < op->grid.dim; d++)
     if (!op->bCoef[d]) return false;
@@ -74,6 +106,7 @@ static bool valid_nlop(const mlgpu_nlop *op) {
 
 bool valid_vcop(const mlgpu_vcop *op) {
   if (!op || !valid_grid(&op->grid)) return false;
+  if (!valid_bc(op->bc, op->grid.dim, false)) return false;
   if (op->dtype != MLGPU_F64 && op->dtype != MLGPU_F32) return false;
   for (int d = 0; d < op->grid.dim; d++)
     if (!op->bCoef[d]) return false;

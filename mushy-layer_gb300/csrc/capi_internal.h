@@ -17,6 +17,8 @@ namespace mlgpu {
 
 bool valid_grid(const mlgpu_grid *g);
 bool valid_vcop(const mlgpu_vcop *op);
+bool valid_bc(const mlgpu_bc &b, int dim, bool temperature_h);
+bool valid_nl_bcs(const mlgpu_nlop &op);
 template <class T> NLArgs<T> make_nl_args(const mlgpu_nlop &op);
 template <class T> VCArgs<T> make_vc_args(const mlgpu_vcop &op);
 int status_of(cudaError_t e);

@@ -195,6 +195,133 @@ __device__ __forceinline__ void t_cl_jac(double H, double C, const ClosureParams
   }
 }
 
+// ------------------------------------------- nonlinear temperature conditions
+// computeTemperature of the scalar phase diagram (src/phaseDiagram.cpp:225-258
+// with computeBoundingEnergy :326-341 and computePorosityMushyLayer :298-324),
+// the form MushyLayerParams::computeTemperature (src/MushyLayerParams.cpp:
+// 1312-1321) hands to the temperature conditions.  It differs from t_cl in
+// rounding: H_s is cp (te + max(0, (-C - CR)/k)), the porosity root has no
+// clamp on C, and a NaN enthalpy takes the liquid branch.
+__device__ __forceinline__ double temperature_pd(double H, double C, const ClosureParams &p) {
+  const double zero = 0.0;
+  const double x = (-C - p.CR) / p.k;
+  const double Hs = p.cp * (p.te + ((zero < x) ? x : zero));  // std::max(zero, x)
+  const double chi = (p.CR + C) / (p.Te + p.CR);
+  const double He = chi * (p.St + p.te * (1 - p.cp)) + p.cp * p.te;
+  const double Hl = p.St - C + p.te + p.Te;
+  if (H <= Hs) return H / p.cp;
+  if (H > Hs && H <= He) return p.te;
+  if (H > He && H < Hl) {
+    double por;
+    if (p.St == 0) {
+      por = 1;
+    } else {
+      const double a = p.CR * (p.cp - 1) + p.St * (p.k - 1);
+      const double b = p.CR * (1 - 2 * p.cp) + H * (1 - p.k) - C * (p.cp - 1) - p.k * p.St;
+      const double c = (C + p.CR) * p.cp + p.k * H;
+      por = (-b - sqrt(b * b - 4 * a * c)) / (2 * a);
+    }
+    return -(C + p.CR * (1 - por)) / (por + p.k * (1 - por));
+  }
+  return H - p.St;
+}
+
+// Resolved temperature conditions: per [dir][side] the Robin coefficients
+// (FixedTemperature a = 0, b = 1, T_ref = value; TemperatureFlux a = 1,
+// F = value; TemperatureFluxRadiation a, b, T_ref given, F = value;
+// BCutil/PhysBCUtil.cpp:614-640) and the solver settings.
+struct NLBCD {
+  double a[3][2], b[3][2], F[3][2], Tref[3][2], lim[3][2];
+  double dx, max_resid, relax;
+  int method, max_iter;
+};
+
+inline bool is_temperature_bc(int type) {
+  return type == MLGPU_BC_FIXED_TEMPERATURE || type == MLGPU_BC_TEMPERATURE_FLUX ||
+         type == MLGPU_BC_TEMPERATURE_FLUX_RADIATION;
+}
+
+inline NLBCD make_nlbcd(const mlgpu_bc &phi_bc, const mlgpu_nlbc &nb, double grid_dx) {
+  NLBCD r;
+  for (int d = 0; d < 3; d++)
+    for (int s = 0; s < 2; s++) {
+      const int type = phi_bc.type[d][s][0];
+      const double v = phi_bc.value[d][s][0];
+      double a = 0.0, b = 0.0, F = 0.0, T = 0.0;
+      if (type == MLGPU_BC_FIXED_TEMPERATURE) {
+        b = 1.0;
+        T = v;
+      } else if (type == MLGPU_BC_TEMPERATURE_FLUX) {
+        a = 1.0;
+        F = v;
+      } else if (type == MLGPU_BC_TEMPERATURE_FLUX_RADIATION) {
+        a = nb.a[d][s];
+        b = nb.b[d][s];
+        F = v;
+        T = nb.T_ref[d][s];
+      }
+      r.a[d][s] = a;
+      r.b[d][s] = b;
+      r.F[d][s] = F;
+      r.Tref[d][s] = T;
+      r.lim[d][s] = nb.no_flux_limit[d][s];
+    }
+  r.dx = nb.dx > 0 ? nb.dx : grid_dx;
+  r.max_resid = nb.max_residual;
+  r.relax = nb.relax_coeff;
+  r.method = nb.method;
+  r.max_iter = nb.max_iter;
+  return r;
+}
+
+// NonlinearTemperatureBCRobin::computeResidual (BCutil/NonlinearBC.H:88-116):
+// predicted ghost temperature minus T(H_g, C_g), zeroed beyond 10
+__device__ __forceinline__ double nlbc_residual(double pred, double Hg, double Cg,
+                                                const ClosureParams &p) {
+  double r = pred - temperature_pd(Hg, Cg, p);
+  if (fabs(r) > 10.0) r = 0.0;
+  return r;
+}
+
+// Ghost enthalpy on side s of direction d next to interior cell iv (H_i, C_i)
+// (BCutil/PhysBCUtil.cpp:690-722): the interior enthalpy below the no-flux
+// limit, else the Picard (NonlinearBC.H:194-233) or Newton (:259-301) root of
+// the Robin residual started from H_i, with the ghost concentration taken as
+// C_i.  Both loops stop after max_iter further steps.
+__device__ __forceinline__ double nlbc_ghost_enthalpy(const NLBCD &B, const ClosureParams &p,
+                                                      int dim, int d, int s, const int iv[3],
+                                                      double Hi, double Ci) {
+  const int perp = (d == dim - 1) ? 0 : d + 1;
+  const double face_pos = B.dx * (iv[perp] + 0.5);
+  if (face_pos < B.lim[d][s]) return Hi;
+  const double Ti = temperature_pd(Hi, Ci, p);
+  const double a = B.a[d][s], b = B.b[d][s];
+  const double pred = (Ti * a / B.dx + B.F[d][s] + b * Ti / 2 - B.Tref[d][s] * b) / (a / B.dx - b / 2);
+  double Hg = Hi;
+  if (B.method == MLGPU_NLBC_NEWTON) {
+    double dH = 0.01;
+    double r_old = B.max_resid * 10;
+    for (int it = 0; fabs(r_old) > B.max_resid && it < B.max_iter; it++) {
+      r_old = nlbc_residual(pred, Hg, Ci, p);
+      const double r_new = nlbc_residual(pred, Hg + dH, Ci, p);
+      if (fabs(r_new - r_old) < B.max_resid) {
+        Hg = Hg + r_old;
+        dH = 2 * dH;
+      } else {
+        Hg = Hg - r_old * dH / (r_new - r_old);
+      }
+    }
+  } else {
+    double r = nlbc_residual(pred, Hg, Ci, p);
+    Hg = Hg + B.relax * r;
+    for (int it = 0; fabs(r) > B.max_resid && it < B.max_iter; it++) {
+      r = nlbc_residual(pred, Hg, Ci, p);
+      Hg = Hg + B.relax * r;
+    }
+  }
+  return Hg;
+}
+
 // ------------------------------------------------------------ thread helpers
 __device__ __forceinline__ long long gtid() {
   return (long long)blockIdx.x * blockDim.x + threadIdx.x;

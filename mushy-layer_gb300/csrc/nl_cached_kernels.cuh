@@ -44,7 +44,7 @@ __device__ __forceinline__ void nlc_dv_nb(const NLArgs<double> &A, const double 
       cl = ghost_value<double>(A.dbc, d, side, 1, l0, A.dx, false);
       return;
     } else {
-      double hg = ghost_value<double>(A.phi_bc, d, side, 0, h0, A.dx, false);
+      double hg = nl_ghost_h(A, i, j, k, d, side, h0, c0);
       double cg = ghost_value<double>(A.phi_bc, d, side, 1, c0, A.dx, false);
       t_cl(hg, cg, A.cp, t, cl);
       return;

@@ -21,11 +21,25 @@ struct NLArgs {
   Geom G;
   ClosureParams cp;
   BCD phi_bc, dbc;
+  NLBCD nlbc;       // temperature conditions on H (phi_bc comp 0 types 2-4)
   int apply_dbc;
   T alpha, beta, dxinv, dx;
   const T *a;       // [2][cells] or null (a == 1)
   const T *b[3];    // [2][faces_d]
 };
+
+// Enthalpy ghost value across face (d, side) of interior cell (i,j,k):
+// the temperature condition's root where phi_bc comp 0 has one, else the
+// linear rule.
+template <class T>
+__device__ __forceinline__ double nl_ghost_h(const NLArgs<T> &A, int i, int j, int k, int d,
+                                             int side, double h0, double c0) {
+  if (A.phi_bc.type[d][side][0] >= MLGPU_BC_FIXED_TEMPERATURE) {
+    const int iv[3] = {i, j, k};
+    return nlbc_ghost_enthalpy(A.nlbc, A.cp, A.G.dim, d, side, iv, h0, c0);
+  }
+  return ghost_value<double>(A.phi_bc, d, side, 0, h0, (double)A.dx, false);
+}
 
 // Diffused variable (T, C_l) of cell (i,j,k), which must be interior.
 template <class T>
@@ -61,7 +75,9 @@ __device__ __forceinline__ void nl_dv_nb(const NLArgs<T> &A, const T *phi, int i
     cl = ghost_value<T>(A.dbc, d, side, 1, l0, A.dx, false);
     return;
   }
-  T hg = ghost_value<T>(A.phi_bc, d, side, 0, h0, A.dx, false);
+  T hg = A.phi_bc.type[d][side][0] >= MLGPU_BC_FIXED_TEMPERATURE
+             ? (T)nl_ghost_h(A, i, j, k, d, side, (double)h0, (double)c0)
+             : ghost_value<T>(A.phi_bc, d, side, 0, h0, A.dx, false);
   T cg = ghost_value<T>(A.phi_bc, d, side, 1, c0, A.dx, false);
   double Td, Cd;
   t_cl((double)hg, (double)cg, A.cp, Td, Cd);

@@ -1187,6 +1187,7 @@ void mlgpu_mg_default_options(mlgpu_mg_options *o, int hc) {
 
 int mlgpu_vc_solver_workspace(const mlgpu_vcop *op, const mlgpu_mg_options *o, size_t *bytes) {
   if (!op || !valid_grid(&op->grid) || !valid_options(o) || !bytes) return MLGPU_ERR_ARG;
+  if (!valid_bc(op->bc, op->grid.dim, false)) return MLGPU_ERR_ARG;
   VCSolver S;
   S.op = *op;
   S.o = *o;
@@ -1198,7 +1199,7 @@ int mlgpu_vc_solver_workspace(const mlgpu_vcop *op, const mlgpu_mg_options *o, s
 int mlgpu_vc_solver_create(const mlgpu_vcop *op, const mlgpu_mg_options *o, void *ws,
                            size_t bytes, void *stream, mlgpu_solver **out) {
   if (!op || !valid_grid(&op->grid) || !valid_options(o) || !ws || !out) return MLGPU_ERR_ARG;
-  if (op->dtype != MLGPU_F64) return MLGPU_ERR_ARG;
+  if (op->dtype != MLGPU_F64 || !valid_bc(op->bc, op->grid.dim, false)) return MLGPU_ERR_ARG;
   for (int d = 0; d < op->grid.dim; d++)
     if (!op->bCoef[d]) return MLGPU_ERR_ARG;
   if (((uintptr_t)ws) & 255) return MLGPU_ERR_WORKSPACE;
@@ -1238,6 +1239,7 @@ int mlgpu_vc_solver_create(const mlgpu_vcop *op, const mlgpu_mg_options *o, void
 
 int mlgpu_hc_solver_workspace(const mlgpu_nlop *op, const mlgpu_mg_options *o, size_t *bytes) {
   if (!op || !valid_grid(&op->grid) || !valid_options(o) || !bytes) return MLGPU_ERR_ARG;
+  if (!valid_nl_bcs(*op)) return MLGPU_ERR_ARG;
   HCSolver S;
   S.op = *op;
   S.o = *o;
@@ -1249,7 +1251,7 @@ int mlgpu_hc_solver_workspace(const mlgpu_nlop *op, const mlgpu_mg_options *o, s
 int mlgpu_hc_solver_create(const mlgpu_nlop *op, const mlgpu_mg_options *o, void *ws,
                            size_t bytes, void *stream, mlgpu_solver **out) {
   if (!op || !valid_grid(&op->grid) || !valid_options(o) || !ws || !out) return MLGPU_ERR_ARG;
-  if (op->dtype != MLGPU_F64) return MLGPU_ERR_ARG;
+  if (op->dtype != MLGPU_F64 || !valid_nl_bcs(*op)) return MLGPU_ERR_ARG;
   // mixed precision needs red/black smoothing (the linearised cycles)
   if (o->precision == MLGPU_PREC_MIXED && o->relax_mode != MLGPU_RELAX_GSRB) return MLGPU_ERR_ARG;
   for (int d = 0; d < op->grid.dim; d++)
@@ -1257,6 +1259,8 @@ int mlgpu_hc_solver_create(const mlgpu_nlop *op, const mlgpu_mg_options *o, void
   if (((uintptr_t)ws) & 255) return MLGPU_ERR_WORKSPACE;
   HCSolver *S = new HCSolver;
   S->op = *op;
+  // the temperature conditions keep the finest spacing on every level
+  if (!(S->op.nlbc.dx > 0)) S->op.nlbc.dx = op->grid.dx;
   S->o = *o;
   S->mixed = o->precision == MLGPU_PREC_MIXED;
   cudaGetLastError();
@@ -1300,6 +1304,7 @@ int mlgpu_mac_project(mlgpu_solver *S, const mlgpu_grid *grid, const mlgpu_bc *p
                       mlgpu_solve_stats *stats) {
   if (!S || !valid_grid(grid) || !phi_bc || !u || !phi || !scratch || !stats)
     return MLGPU_ERR_ARG;
+  if (!valid_bc(*phi_bc, grid->dim, false)) return MLGPU_ERR_ARG;
   VCSolver *V = dynamic_cast<VCSolver *>(S);
   if (!V) return MLGPU_ERR_ARG;
   for (int d = 0; d < 3; d++)

@@ -22,6 +22,8 @@ ERR_SCRATCH = 7
 
 F64, F32 = 0, 1
 BC_NEUMANN, BC_DIRICHLET = 0, 1
+BC_FIXED_TEMPERATURE, BC_TEMPERATURE_FLUX, BC_TEMPERATURE_FLUX_RADIATION = 2, 3, 4
+NLBC_PICARD, NLBC_NEWTON = 0, 1
 RELAX_GSRB, RELAX_JACOBI = 1, 4
 PROLONG_CONSTANT, PROLONG_LINEAR = 0, 1
 BOTTOM_RELAX, BOTTOM_BICGSTAB = 0, 1
@@ -47,12 +49,20 @@ class Params(C.Structure):
         "viscosityCoeff")]
 
 
+class NLBC(C.Structure):
+    _fields_ = [("a", (C.c_double * 2) * 3), ("b", (C.c_double * 2) * 3),
+                ("T_ref", (C.c_double * 2) * 3), ("no_flux_limit", (C.c_double * 2) * 3),
+                ("method", C.c_int), ("max_iter", C.c_int),
+                ("max_residual", C.c_double), ("relax_coeff", C.c_double),
+                ("dx", C.c_double)]
+
+
 class NLOp(C.Structure):
     _fields_ = [("grid", Grid), ("params", Params), ("phi_bc", BC),
                 ("derived_bc", BC), ("apply_derived_bc", C.c_int),
                 ("alpha", C.c_double), ("beta", C.c_double),
                 ("aCoef", C.c_void_p), ("bCoef", C.c_void_p * 3),
-                ("dtype", C.c_int)]
+                ("dtype", C.c_int), ("nlbc", NLBC)]
 
 
 class VCOp(C.Structure):
@@ -101,6 +111,22 @@ def make_bc(spec=None):
         b.type[d][s][c] = int(t)
         b.value[d][s][c] = float(v)
     return b
+
+
+def make_nlbc(radiation=None, no_flux_limit=None, method=0, max_iter=2,
+              max_residual=1e-5, relax_coeff=0.5, dx=0.0):
+    """Nonlinear temperature-BC parameters (reference defaults: Picard, 2
+    iterations, residual 1e-5, relaxation 0.5).  radiation: {(dir, side):
+    (a, b, T_ref)}; no_flux_limit: {(dir, side): position}."""
+    n = NLBC()
+    for (d, s), (a, b, t) in (radiation or {}).items():
+        n.a[d][s], n.b[d][s], n.T_ref[d][s] = float(a), float(b), float(t)
+    for (d, s), v in (no_flux_limit or {}).items():
+        n.no_flux_limit[d][s] = float(v)
+    n.method, n.max_iter = int(method), int(max_iter)
+    n.max_residual, n.relax_coeff = float(max_residual), float(relax_coeff)
+    n.dx = float(dx)
+    return n
 
 
 def make_params(**kw):

@@ -74,9 +74,11 @@ class NLMultiCompOp:
     ncomp = 2
 
     def __init__(self, grid, params, phi_bc, derived_bc, alpha, beta, aCoef, bCoef,
-                 apply_derived_bc=True):
+                 apply_derived_bc=True, nlbc=None):
         self.grid, self.params = grid, params
         self.phi_bc, self.derived_bc = phi_bc, derived_bc
+        # temperature-condition settings (reference defaults when not given)
+        self.nlbc = nlbc if nlbc is not None else abi.make_nlbc()
         self.alpha, self.beta = float(alpha), float(beta)
         self.aCoef, self.bCoef = aCoef, list(bCoef)
         self.apply_derived_bc = int(apply_derived_bc)
@@ -86,6 +88,7 @@ class NLMultiCompOp:
         op = abi.NLOp()
         op.grid, op.params = self.grid, self.params
         op.phi_bc, op.derived_bc = self.phi_bc, self.derived_bc
+        op.nlbc = self.nlbc
         op.apply_derived_bc = self.apply_derived_bc
         op.alpha, op.beta = self.alpha, self.beta
         op.aCoef = _ptr(self.aCoef)

@@ -281,6 +281,138 @@ inline void t_cl_jac(double H, double C, const mlgpu_params &p, double J[4]) {
   }
 }
 
+// ------------------------------------ nonlinear temperature conditions
+// computeTemperature (src/phaseDiagram.cpp:225-258) as called by
+// MushyLayerParams::computeTemperature (src/MushyLayerParams.cpp:1312-1321):
+// bounding energies of computeBoundingEnergy (:326-341, H_s with
+// std::max(0, (-C - CR)/k)) and the unclamped root of
+// computePorosityMushyLayer (:298-324).
+double pd_temperature(double H, double C, const mlgpu_params &p) {
+  const double CR = p.compositionRatio, k = p.waterDistributionCoeff,
+               cp = p.specificHeatRatio, St = p.stefan, te = p.thetaEutectic,
+               Te = p.ThetaEutectic;
+  const double zero = 0.0;
+  const double H_s = cp * (te + std::max(zero, (-C - CR) / k));
+  const double chi_e = (CR + C) / (Te + CR);
+  const double H_e = chi_e * (St + te * (1 - cp)) + cp * te;
+  const double H_l = St - C + te + Te;
+  if (H <= H_s) return H / cp;
+  if (H > H_s && H <= H_e) return te;
+  if (H > H_e && H < H_l) {
+    double por;
+    if (St == 0) {
+      por = 1;
+    } else {
+      double a = CR * (cp - 1) + St * (k - 1);
+      double b = CR * (1 - 2 * cp) + H * (1 - k) - C * (cp - 1) - k * St;
+      double c = (C + CR) * cp + k * H;
+      por = (-b - std::sqrt(b * b - 4 * a * c)) / (2 * a);
+    }
+    return -(C + CR * (1 - por)) / (por + k * (1 - por));
+  }
+  return H - St;
+}
+
+// NonlinearTemperatureBCRobin (BCutil/NonlinearBC.H:63-122)
+struct RobinTemperatureBC {
+  mlgpu_params params;
+  double dx, a, b, F, T_ref;
+  // computeResidual (:88-116)
+  double residual(double H_ghost, double C_ghost, double T_interior) const {
+    double T_ghost = pd_temperature(H_ghost, C_ghost, params);
+    double predicted = (T_interior * a / dx + F + b * T_interior / 2 - T_ref * b) / (a / dx - b / 2);
+    double r = predicted - T_ghost;
+    if (std::fabs(r) > 10.0) r = 0.0;
+    return r;
+  }
+};
+
+// NonlinearBCSolverPicard::solve (BCutil/NonlinearBC.H:194-233)
+void solve_picard(const RobinTemperatureBC &R, const mlgpu_nlbc &nb, double &H_ghost,
+                  double T_interior, double C_ghost) {
+  double r = R.residual(H_ghost, C_ghost, T_interior);
+  H_ghost = H_ghost + nb.relax_coeff * r;
+  int iter = 0;
+  while (std::fabs(r) > nb.max_residual && iter < nb.max_iter) {
+    r = R.residual(H_ghost, C_ghost, T_interior);
+    H_ghost = H_ghost + nb.relax_coeff * r;
+    iter++;
+  }
+}
+
+// NonlinearBCSolverNewton::solve (BCutil/NonlinearBC.H:259-301)
+void solve_newton(const RobinTemperatureBC &R, const mlgpu_nlbc &nb, double &H_ghost,
+                  double T_interior, double C_ghost) {
+  double dH = 0.01;
+  double r_old = nb.max_residual * 10, r_new = nb.max_residual * 10;
+  int iter = 0;
+  while (std::fabs(r_old) > nb.max_residual && iter < nb.max_iter) {
+    r_old = R.residual(H_ghost, C_ghost, T_interior);
+    r_new = R.residual(H_ghost + dH, C_ghost, T_interior);
+    if (std::fabs(r_new - r_old) < nb.max_residual) {
+      H_ghost = H_ghost + r_old;
+      dH = 2 * dH;
+    } else {
+      H_ghost = H_ghost - r_old * (dH) / (r_new - r_old);
+    }
+    iter++;
+  }
+}
+
+// AdvectDiffuseScalarBC temperature branch for the enthalpy component
+// (BCutil/PhysBCUtil.cpp:590-722): Robin coefficients by condition type,
+// then per ghost cell of the face row either the interior enthalpy (below the
+// no-flux limit along the next direction) or the solved ghost enthalpy, with
+// the interior concentration as ghost concentration.  The spacing is the one
+// the condition object was built with (PhysBCUtil m_dx).
+void temperature_bc(Fab &f, const mlgpu_nlop &op, int d, int side) {
+  const int type = op.phi_bc.type[d][side][0];
+  const double value = op.phi_bc.value[d][side][0];
+  const mlgpu_nlbc &nb = op.nlbc;
+  RobinTemperatureBC R;
+  R.params = op.params;
+  R.dx = nb.dx > 0 ? nb.dx : op.grid.dx;
+  R.a = 0.0;
+  R.b = 0.0;
+  R.F = 0.0;
+  R.T_ref = 0.0;
+  if (type == MLGPU_BC_FIXED_TEMPERATURE) {
+    R.T_ref = value;
+    R.b = 1.0;
+  } else if (type == MLGPU_BC_TEMPERATURE_FLUX) {
+    R.F = value;
+    R.a = 1.0;
+  } else {
+    R.a = nb.a[d][side];
+    R.b = nb.b[d][side];
+    R.F = value;
+    R.T_ref = nb.T_ref[d][side];
+  }
+  const int isign = side == 0 ? -1 : 1;
+  const int perp = (d == op.grid.dim - 1) ? 0 : d + 1;
+  int lo[3] = {0, 0, 0}, hi[3] = {f.n[0] - 1, f.n[1] - 1, f.n[2] - 1};
+  lo[d] = hi[d] = (side == 0) ? -1 : f.n[d];
+  for (int k = lo[2]; k <= hi[2]; k++)
+    for (int j = lo[1]; j <= hi[1]; j++)
+      for (int i = lo[0]; i <= hi[0]; i++) {
+        int iv[3] = {i, j, k};
+        iv[d] -= isign;
+        const double H_i = f(iv[0], iv[1], iv[2], 0), C_i = f(iv[0], iv[1], iv[2], 1);
+        const double face_pos = R.dx * (iv[perp] + 0.5);
+        if (face_pos < nb.no_flux_limit[d][side]) {
+          f(i, j, k, 0) = H_i;
+          continue;
+        }
+        const double T_i = pd_temperature(H_i, C_i, op.params);
+        double H_g = H_i;
+        if (nb.method == MLGPU_NLBC_NEWTON)
+          solve_newton(R, nb, H_g, T_i, C_i);
+        else
+          solve_picard(R, nb, H_g, T_i, C_i);
+        f(i, j, k, 0) = H_g;
+      }
+}
+
 // CALCULATEPOROSITY/CL/CS/T (src/EnthalpyVariablesF.ChF:13-284) for one cell.
 inline void full_closure(double H, double C, const mlgpu_params &p, double &T,
                          double &por, double &Cl, double &Cs, double &Hs, double &He,
@@ -410,10 +542,25 @@ struct NLCtx {
   }
 };
 
+// (H, C) ghosts: exchange, the linear conditions, then the temperature
+// conditions on H where phi_bc comp 0 names one (they read interior cells only)
+void nl_fill_ghosts(Fab &phi, const mlgpu_nlop &op) {
+  fill_ghosts(phi, op.grid, op.phi_bc, false);
+  for (int d = 0; d < op.grid.dim; d++) {
+    if (op.grid.periodic[d]) continue;
+    for (int side = 0; side < 2; side++) {
+      int t = op.phi_bc.type[d][side][0];
+      if (t == MLGPU_BC_FIXED_TEMPERATURE || t == MLGPU_BC_TEMPERATURE_FLUX ||
+          t == MLGPU_BC_TEMPERATURE_FLUX_RADIATION)
+        temperature_bc(phi, op, d, side);
+    }
+  }
+}
+
 void nl_prepare(Fab &phi, Fab &pl, const mlgpu_nlop &op, const double *phid) {
   phi.define(op.grid, 2);
   phi.load(phid);
-  fill_ghosts(phi, op.grid, op.phi_bc, false);
+  nl_fill_ghosts(phi, op);
   diffused_var(pl, phi, op);
 }
 
@@ -428,7 +575,7 @@ void for_cells(const mlgpu_grid &g, F f) {
 // one red/black pass: NONLINEARSMOOTHING (F.ChF:50-198) with lambda inline
 void nl_gsrb_pass_fab(Fab &phi, const double *rhs, const mlgpu_nlop &op, int pass) {
   NLCtx X(op);
-  fill_ghosts(phi, op.grid, op.phi_bc, false);
+  nl_fill_ghosts(phi, op);
   Fab pl;
   diffused_var(pl, phi, op);
   const mlgpu_grid &g = op.grid;
@@ -1102,10 +1249,17 @@ void orc_mg_default_options(mlgpu_mg_options *o, int hc) {
 
 int orc_mg_depth(const mlgpu_grid *g, int max_coarse) { return mg_depth(*g, max_coarse); }
 
+double orc_pd_temperature(double H, double C, const mlgpu_params *p) {
+  return pd_temperature(H, C, *p);
+}
+
 int orc_hc_solve(const mlgpu_nlop *op, const mlgpu_mg_options *o, double *phi,
                  const double *rhs, mlgpu_solve_stats *st) {
   HCSolver S;
   S.op0 = *op;
+  // the temperature condition object keeps the level's spacing on the
+  // coarser multigrid levels (PhysBCUtil m_dx)
+  if (!(S.op0.nlbc.dx > 0)) S.op0.nlbc.dx = op->grid.dx;
   S.o = *o;
   build_levels(S.L, op->grid, 2, (const double *)op->aCoef, nullptr, op->bCoef,
                o->max_coarse);

@@ -53,6 +53,7 @@ def lib():
             "orc_norm": (d, [sz, vp, i]),
             "orc_mg_default_options": (None, [P(abi.MGOptions), i]),
             "orc_mg_depth": (i, [P(abi.Grid), i]),
+            "orc_pd_temperature": (d, [d, d, P(abi.Params)]),
             "orc_hc_solve": (i, [P(abi.NLOp), P(abi.MGOptions), vp, vp, P(abi.SolveStats)]),
             "orc_vc_solve": (i, [P(abi.VCOp), P(abi.MGOptions), vp, vp, P(abi.SolveStats)]),
             "orc_mac_project": (i, [P(abi.VCOp), P(abi.MGOptions), P(abi.BC), vp * 3, vp * 3,
@@ -97,6 +98,11 @@ def closure_tcl(g, p, HC):
     return out
 
 
+def pd_temperature(p, H, C_):
+    """Scalar phase-diagram temperature (computeTemperature) of one (H, C)."""
+    return lib().orc_pd_temperature(float(H), float(C_), C.byref(p))
+
+
 def closure_jac(g, p, HC):
     """d(T, C_l)/d(H, C) per cell: array [4][cells] = dT/dH, dT/dC, dCl/dH, dCl/dC."""
     n = HC.size // 2
@@ -110,10 +116,11 @@ class NLOpHost:
     """Holds numpy coefficient arrays alive and exposes an NLOp struct."""
 
     def __init__(self, g, p, phi_bc, derived_bc, alpha, beta, aCoef, bCoef,
-                 apply_derived_bc=1):
+                 apply_derived_bc=1, nlbc=None):
         self.g, self.keep = g, [aCoef] + list(bCoef)
         op = abi.NLOp()
         op.grid, op.params, op.phi_bc, op.derived_bc = g, p, phi_bc, derived_bc
+        op.nlbc = nlbc if nlbc is not None else abi.make_nlbc()
         op.apply_derived_bc = apply_derived_bc
         op.alpha, op.beta = alpha, beta
         op.aCoef = _p(aCoef)

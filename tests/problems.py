@@ -48,6 +48,21 @@ def hc_bcs(kind="mixed"):
     return phi_bc, abi.make_bc(spec)
 
 
+def temperature_bcs(method=0, max_iter=2, limit=0.0, dim=2):
+    """Temperature conditions on H (C no flux), derived BC unused:
+    x lo fixed temperature, x hi temperature flux, y lo radiation (with a
+    no-flux limit along x), y hi no flux; z lo fixed temperature in 3D."""
+    spec = {(0, 0, 0): (abi.BC_FIXED_TEMPERATURE, -0.4),
+            (0, 1, 0): (abi.BC_TEMPERATURE_FLUX, 0.8),
+            (1, 0, 0): (abi.BC_TEMPERATURE_FLUX_RADIATION, -0.3),
+            (1, 1, 0): (abi.BC_NEUMANN, 0.0)}
+    if dim == 3:
+        spec[(2, 0, 0)] = (abi.BC_FIXED_TEMPERATURE, 0.6)
+    nlbc = abi.make_nlbc(radiation={(1, 0): (0.7, 1.3, -1.2)},
+                         no_flux_limit={(1, 0): limit}, method=method, max_iter=max_iter)
+    return abi.make_bc(spec), abi.make_bc(), nlbc
+
+
 def vc_bc(kind="mixed"):
     if kind == "neumann":
         return abi.make_bc()

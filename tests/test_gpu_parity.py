@@ -656,3 +656,106 @@ def test_backward_euler_steps_bitwise():
         assert rc == rc_ref and st.iterations == st_ref.iterations
         exact(host(d_new), new_ref)
         h_phi, d_phi = new_ref, d_new
+
+
+# ----------------------------------- nonlinear temperature conditions on H
+def nl_setup_temperature(n, per, seed, method, limit):
+    from mushy_gb300 import ops
+    rng = np.random.default_rng(seed)
+    g = P.grid(n, per)
+    p = P.mushy_params()
+    phi_bc, der, nlbc = P.temperature_bcs(method, limit=limit, dim=len(n))
+    phi = P.hc_state(g, rng)
+    rhs = phi + 0.1 * rng.standard_normal(phi.shape)
+    b = P.faces(g, rng, 2)
+    aC = rng.uniform(0.5, 1.5, phi.shape)
+    alpha, beta = 1.0, -2e-3
+    ref = O.NLOpHost(g, p, phi_bc, der, alpha, beta, aC, b, apply_derived_bc=0, nlbc=nlbc)
+    op = ops.NLMultiCompOp(g, p, phi_bc, der, alpha, beta, dev(aC), [dev(x) for x in b],
+                           apply_derived_bc=False, nlbc=nlbc)
+    return g, ref, op, phi, rhs
+
+
+@pytest.mark.parametrize("n,per", [CASES_2D[0], CASES_2D[1], CASES_3D[0], CASES_3D[1]])
+@pytest.mark.parametrize("method", [abi.NLBC_PICARD, abi.NLBC_NEWTON])
+@pytest.mark.parametrize("limit", [0.0, 0.3])
+def test_nl_temperature_bc_bitwise(n, per, method, limit):
+    """Fixed-temperature, temperature-flux and radiation conditions on H
+    (ghost enthalpy solved per boundary cell, every closure regime next to
+    the walls, no-flux limit on part of one wall): residual, apply, red/black
+    passes and FAS restriction bitwise equal to the oracle."""
+    g, ref, op, phi, rhs = nl_setup_temperature(n, per, 60, method, limit)
+    d_phi, d_rhs = dev(phi), dev(rhs)
+    res = torch.empty_like(d_phi)
+    op.residual(res, d_phi, d_rhs)
+    exact(host(res), O.nl_residual(ref, phi, rhs))
+    lhs = torch.empty_like(d_phi)
+    op.applyOp(lhs, d_phi)
+    exact(host(lhs), O.nl_apply(ref, phi))
+    rc = op.createCoarser()
+    op.restrictResidual(rc, d_phi, d_rhs)
+    exact(host(rc), O.nl_restrict_residual(ref, phi, rhs))
+    op.levelGSRBPass(d_phi, d_rhs, 1)
+    r = O.nl_gsrb_pass(ref, phi, rhs, 1)
+    exact(host(d_phi), r)
+    op.relax(d_phi, d_rhs, 2)
+    exact(host(d_phi), O.nl_relax(ref, r, rhs, 2))
+
+
+def _temperature_solve_problem(n, seed, method=abi.NLBC_PICARD):
+    from mushy_gb300 import ops
+    g = P.grid(n)
+    p = P.mushy_params()
+    phi_bc, der, nlbc = P.temperature_bcs(method, limit=0.3)
+    rng = np.random.default_rng(seed)
+    phi = P.hc_state(g, rng, regimes=False)
+    b = [np.stack([-np.ones(abi.face_shape(g, d)), -0.01 * np.ones(abi.face_shape(g, d))])
+         for d in range(2)]
+    dt = 1e-3
+    ref = O.NLOpHost(g, p, phi_bc, der, 1.0, -dt, None, b, apply_derived_bc=0, nlbc=nlbc)
+    op = ops.NLMultiCompOp(g, p, phi_bc, der, 1.0, -dt, None, [dev(x) for x in b],
+                           apply_derived_bc=False, nlbc=nlbc)
+    return g, ref, op, phi
+
+
+@pytest.mark.parametrize("method", [abi.NLBC_PICARD, abi.NLBC_NEWTON])
+def test_hc_solver_temperature_bc_matches_oracle(method):
+    """FAS solve with temperature conditions on H: the coarse levels keep the
+    condition built at the finest spacing; iterations, statistics and the
+    solution bitwise equal to the oracle's driver."""
+    from mushy_gb300 import ops
+    g, ref, op, phi = _temperature_solve_problem((32, 32), 61, method)
+    opts = O.default_options(1)
+    opts.max_iter = 6
+    sol_ref, st_ref, rc_ref = O.hc_solve(ref, opts, phi, phi.copy())
+    assert st_ref.final_norm < st_ref.initial_norm
+    for graph in (0, 2):
+        o = ops.default_options(True)
+        o.max_iter, o.use_graph = 6, graph
+        d_phi = dev(phi)
+        st, rc = ops.AMRFASMultiGrid(op, o).solve(d_phi, dev(phi))
+        assert rc == rc_ref and st.iterations == st_ref.iterations
+        exact(host(d_phi), sol_ref)
+
+
+def test_hc_solver_mixed_with_temperature_bc():
+    """The mixed nonlinear solve (FP32 linearised cycles, whose ghosts use the
+    homogeneous form of the condition: e_H ghost = interior) still reaches
+    1e-10 under the FP64 residual that carries the temperature conditions."""
+    from mushy_gb300 import ops
+    g, ref, op, phi = _temperature_solve_problem((48, 32), 62)
+    rhs = phi.copy()
+    sols = {}
+    for prec in (abi.PREC_F64, abi.PREC_MIXED):
+        o = ops.default_options(True)
+        o.max_iter, o.tolerance, o.hang, o.precision = 80, 1e-10, 1e-15, prec
+        d_phi = dev(phi)
+        st, rc = ops.AMRFASMultiGrid(op, o).solve(d_phi, dev(rhs))
+        sols[prec] = (host(d_phi), st, rc)
+    um, stm, rcm = sols[abi.PREC_MIXED]
+    assert rcm == 0 and stm.final_norm <= 1e-10 * stm.initial_norm
+    r0 = np.abs(O.nl_residual(ref, phi, rhs)).max()
+    assert np.abs(O.nl_residual(ref, um, rhs)).max() <= 1.05e-10 * r0
+    u64, st64, rc64 = sols[abi.PREC_F64]
+    if rc64 == 0:
+        assert np.abs(um - u64).max() <= 1e-8 * np.abs(u64).max()

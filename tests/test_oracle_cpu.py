@@ -274,3 +274,122 @@ def test_argument_validation_without_gpu():
     assert nbytes.value > 64 * 64 * 8 * 3
     opts.relax_mode = 7
     assert lib.mlgpu_vc_solver_workspace(C.byref(op), C.byref(opts), C.byref(nbytes)) == abi.ERR_ARG
+
+
+# ------------------------------------------- nonlinear temperature conditions
+def test_pd_temperature_matches_closure():
+    """The scalar phase diagram used by the temperature conditions agrees with
+    the Fortran closure (exactly outside the mush, to rounding inside it)."""
+    rng = np.random.default_rng(21)
+    g = P.grid((40, 10))
+    p = P.mushy_params()
+    HC = P.hc_state(g, rng)
+    tcl = O.closure_tcl(g, p, HC)
+    H, Cc = HC[0].ravel(), HC[1].ravel()
+    T = np.array([O.pd_temperature(p, h, c) for h, c in zip(H, Cc)])
+    ref = tcl[0].ravel()
+    assert np.allclose(T, ref, rtol=1e-12, atol=1e-12)
+    liquid = H >= 5.0 - Cc
+    assert np.array_equal(T[liquid], H[liquid] - 5.0)
+
+
+def _ghost_temperature(nlbc, spec, state, cell, face):
+    """Ghost temperature across `face` = (dir, side) of `cell` in a uniform
+    (H, C) field: with alpha = 0, beta = -1 and unit face coefficients the
+    operator there is (T_g - T_0)/dx^2 (the other faces see T_0)."""
+    g = P.grid((8, 6))
+    p = P.mushy_params()
+    phi = np.empty((2,) + abi.cell_shape(g))
+    phi[0], phi[1] = state
+    b = [np.ones((2,) + abi.face_shape(g, d)) for d in range(2)]
+    ref = O.NLOpHost(g, p, abi.make_bc(spec), abi.make_bc(), 0.0, -1.0, None, b,
+                     apply_derived_bc=0, nlbc=nlbc)
+    L = O.nl_apply(ref, phi)
+    i, j = cell
+    T0 = O.pd_temperature(p, *state)
+    return T0 + L[0, 0, j, i] * g.dx * g.dx, T0, g.dx
+
+
+LIQUID = (6.5, -1.0)  # T = H - St = 1.5, ghost stays liquid
+
+
+def test_fixed_temperature_known_answers():
+    spec = {(0, 0, 0): (abi.BC_FIXED_TEMPERATURE, 1.4)}
+    # Newton: residual linear in the liquid, exact after one step
+    Tg, T0, _ = _ghost_temperature(abi.make_nlbc(method=abi.NLBC_NEWTON), spec, LIQUID,
+                                   (0, 3), (0, 0))
+    assert abs(Tg - (2 * 1.4 - T0)) < 1e-12
+    # Picard, max_bc_iter 2, relaxation 0.5: three relaxed steps, r halving
+    Tg, T0, _ = _ghost_temperature(abi.make_nlbc(), spec, LIQUID, (0, 3), (0, 0))
+    r0 = (2 * 1.4 - T0) - T0
+    assert abs(Tg - (T0 + 0.875 * r0)) < 1e-12
+    # Picard run to convergence
+    Tg, T0, _ = _ghost_temperature(abi.make_nlbc(max_iter=80, max_residual=1e-15), spec,
+                                   LIQUID, (0, 3), (0, 0))
+    assert abs(Tg - (2 * 1.4 - T0)) < 1e-12
+
+
+def test_temperature_flux_and_radiation_known_answers():
+    F = 0.8
+    spec = {(0, 1, 0): (abi.BC_TEMPERATURE_FLUX, F)}
+    Tg, T0, dx = _ghost_temperature(abi.make_nlbc(method=abi.NLBC_NEWTON), spec, LIQUID,
+                                    (7, 2), (0, 1))
+    assert abs((Tg - T0) / dx - F) < 1e-9
+    a, bb, Tref, F = 0.7, 1.3, 1.2, -0.3
+    spec = {(1, 0, 0): (abi.BC_TEMPERATURE_FLUX_RADIATION, F)}
+    nl = abi.make_nlbc(radiation={(1, 0): (a, bb, Tref)}, method=abi.NLBC_NEWTON)
+    Tg, T0, dx = _ghost_temperature(nl, spec, LIQUID, (3, 0), (1, 0))
+    assert abs(a * (Tg - T0) / dx - (F + bb * ((Tg + T0) / 2 - Tref))) < 1e-9
+    # below the no-flux limit (cell centres along x) the ghost is the interior
+    nl = abi.make_nlbc(radiation={(1, 0): (a, bb, Tref)}, no_flux_limit={(1, 0): 0.5},
+                       method=abi.NLBC_NEWTON)
+    Tg, T0, _ = _ghost_temperature(nl, spec, LIQUID, (3, 0), (1, 0))  # x = 0.4375 < 0.5
+    assert Tg == T0
+    Tg, T0, dx = _ghost_temperature(nl, spec, LIQUID, (4, 0), (1, 0))  # x = 0.5625
+    assert abs(a * (Tg - T0) / dx - (F + bb * ((Tg + T0) / 2 - Tref))) < 1e-9
+
+
+def test_temperature_condition_in_the_mush_converges():
+    """Newton in the mush (nonlinear T(H)) reaches the condition with enough
+    iterations; the converged ghost stays in the mush."""
+    p = P.mushy_params()
+    state = (5.0, -1.0)  # mush: T = 0.528
+    T0 = O.pd_temperature(p, *state)
+    spec = {(0, 0, 0): (abi.BC_FIXED_TEMPERATURE, T0 - 0.05)}
+    nl = abi.make_nlbc(method=abi.NLBC_NEWTON, max_iter=30, max_residual=1e-13)
+    Tg, T0b, _ = _ghost_temperature(nl, spec, state, (0, 3), (0, 0))
+    assert T0b == T0 and abs(Tg - (2 * (T0 - 0.05) - T0)) < 1e-10
+
+
+def test_temperature_conditions_rejected_off_enthalpy():
+    """Temperature conditions only apply to H of the nonlinear operator; on C
+    (the reference stops there) or on a linear operator the call is refused
+    before any device work."""
+    lib = abi.load()
+    g = P.grid((8, 8))
+    nl = abi.NLOp()
+    nl.grid, nl.params, nl.dtype = g, P.mushy_params(), abi.F64
+    nl.nlbc = abi.make_nlbc()
+    opts = abi.MGOptions()
+    lib.mlgpu_mg_default_options(C.byref(opts), 1)
+    nbytes = C.c_size_t()
+
+    def ws():  # host-only sizing call: validates the operator, no device work
+        return lib.mlgpu_hc_solver_workspace(C.byref(nl), C.byref(opts), C.byref(nbytes))
+
+    nl.phi_bc, _, nl.nlbc = P.temperature_bcs()
+    assert ws() == 0
+    nl.phi_bc = abi.make_bc({(0, 0, 1): (abi.BC_FIXED_TEMPERATURE, 0.0)})
+    assert ws() == abi.ERR_ARG
+    nl.phi_bc = abi.make_bc({(0, 0, 0): (7, 0.0)})
+    assert ws() == abi.ERR_ARG
+    nl.phi_bc = abi.make_bc({(0, 0, 0): (abi.BC_TEMPERATURE_FLUX_RADIATION, 0.0)})
+    nl.nlbc = abi.make_nlbc(radiation={(0, 0): (0.0, 0.0, 0.0)})  # a/dx - b/2 == 0
+    assert ws() == abi.ERR_ARG
+    nl.nlbc = abi.make_nlbc(radiation={(0, 0): (0.0, 1.0, 0.0)})
+    assert ws() == 0
+    vc = abi.VCOp()
+    vc.grid = g
+    vc.bc = abi.make_bc({(1, 1, 0): (abi.BC_FIXED_TEMPERATURE, 0.0)})
+    lib.mlgpu_mg_default_options(C.byref(opts), 0)
+    assert lib.mlgpu_vc_solver_workspace(C.byref(vc), C.byref(opts), C.byref(nbytes)) == abi.ERR_ARG
