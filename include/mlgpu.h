@@ -384,6 +384,72 @@ int mlgpu_hc_backward_euler(mlgpu_solver *S, double *phi_new, const double *phi_
                             const double *src, const double *aCoef, double dt,
                             double *rhs_scratch, mlgpu_solve_stats *stats);
 
+/* ------------------------------------------------------------ adjoint
+ * Discrete adjoint of the path (no counterpart in the reference, which has
+ * no derivatives): the transpose of the Jacobian of the nonlinear operator
+ * N(phi) = alpha a phi - beta div(b grad f(phi)),
+ *   A = dN/dphi = alpha a - beta div(b grad (J .)),  J = d(T, C_l)/d(H, C)
+ * (the closure's derivative, including the porosity root's), with the
+ * ghost rule of N differentiated at the walls.  FP64 throughout.  The
+ * temperature conditions (phi_bc comp 0 types 2-4) are refused
+ * (MLGPU_ERR_ARG). */
+
+/* J of every cell: [4][cells] = dT/dH, dT/dC, dC_l/dH, dC_l/dC. */
+int mlgpu_closure_jacobian(const mlgpu_grid *g, const mlgpu_params *p, const double *HC,
+                           double *J, void *stream);
+/* out = A^T y (g NULL) or g - A^T y, A at state phi whose Jacobian is J
+ * (mlgpu_closure_jacobian of phi); op FP64. */
+int mlgpu_hc_adjoint_apply(const mlgpu_nlop *op, const double *phi, const double *J,
+                           const double *y, const double *g, double *out, void *stream);
+/* One red/black pass (0 red, 1 black) of block Gauss-Seidel on A^T y = g:
+ * each cell of the colour solves its own two rows exactly. */
+int mlgpu_hc_adjoint_gsrb_pass(const mlgpu_nlop *op, const double *phi, const double *J,
+                               double *y, const double *g, int pass, void *stream);
+/* gc = 2^D average of g - A^T y on the grid coarsened by 2. */
+int mlgpu_hc_adjoint_restrict(const mlgpu_nlop *op, const double *phi, const double *J,
+                              const double *y, const double *g, double *gc, void *stream);
+
+/* Multigrid solver of A^T y = g (correction-scheme V-cycles of the block
+ * smoother on the operator rediscretised per level at the averaged state,
+ * coefficients coarsened as the FAS hierarchy does; options as for the FAS
+ * solver: smoothing counts, bottom sweeps, tolerance, max_iter, norm).
+ * Workspace/creation as mlgpu_hc_solver_*; alpha/beta via
+ * mlgpu_solver_set_alpha_beta. */
+int mlgpu_hc_adjoint_workspace(const mlgpu_nlop *op, const mlgpu_mg_options *o,
+                               size_t *bytes);
+int mlgpu_hc_adjoint_create(const mlgpu_nlop *op, const mlgpu_mg_options *o, void *workspace,
+                            size_t bytes, void *stream, mlgpu_solver **out);
+/* Solve A^T y = g with A the Jacobian at state phi; y: initial guess in,
+ * solution out. */
+int mlgpu_hc_adjoint_solve(mlgpu_solver *S, const double *phi, const double *g, double *y,
+                           mlgpu_solve_stats *stats);
+/* grad[(d * 2 + side) * 2 + comp] = -y^T dN/dv for every boundary value v of
+ * the condition N applies at the walls (derived_bc when apply_derived_bc,
+ * else phi_bc), at the state of the last mlgpu_hc_adjoint_solve; 0 on
+ * periodic or absent sides.  grad: 12 host doubles. */
+int mlgpu_hc_adjoint_bc_gradient(mlgpu_solver *S, const double *y, double grad[12]);
+/* Adjoint of mlgpu_hc_backward_euler: given phi_new (the converged step)
+ * and phi_new_bar = dJ/dphi_new, solve A^T mu = phi_new_bar (alpha 1,
+ * beta -dt; mu: initial guess in, solution out), then phi_old_bar = a mu,
+ * src_bar = dt mu and bc_grad (12 host doubles) as
+ * mlgpu_hc_adjoint_bc_gradient; each output may be NULL. */
+int mlgpu_hc_backward_euler_adjoint(mlgpu_solver *S, const double *phi_new,
+                                    const double *phi_new_bar, const double *aCoef, double dt,
+                                    double *mu, double *phi_old_bar, double *src_bar,
+                                    double bc_grad[12], mlgpu_solve_stats *stats);
+/* Adjoint of mlgpu_mac_project.  Forward: u = u* - Pi G p, D Pi G p = D u*.
+ * Given ubar = dJ/du: solve D Pi G q = G^T (Pi ubar) with `S` (q: initial
+ * guess in, solution out), ustar_bar = ubar - D^T q and, if pi_bar is not
+ * NULL, pi_bar = -ustar_bar * (G p) with p the forward pressure (so that
+ * dJ/dPi_face = pi_bar).  G^T, D^T are the exact transposes of the face
+ * arrays as mlgpu_mac_project indexes them.  Across a periodic seam the
+ * forward needs equal coefficients on faces 0 and n, so only the sum of the
+ * two pi_bar entries there is a derivative.  `scratch`: one cell field. */
+int mlgpu_mac_project_adjoint(mlgpu_solver *S, const mlgpu_grid *grid, const mlgpu_bc *phi_bc,
+                              const double *ubar[3], const double *pi_face[3],
+                              const double *p, double *ustar_bar[3], double *pi_bar[3],
+                              double *q, double *scratch, mlgpu_solve_stats *stats);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,350 @@
+// adjoint_kernels.cuh -- discrete adjoint of the nonlinear (H, C) operator.
+//
+// N(phi) = alpha a phi - beta div(b grad f(phi)), f = (T, C_l) = closure(H, C)
+// (nl_kernels.cuh).  Its Jacobian at a state phi is
+//   A x = alpha a x - beta dxinv sum_faces b_f (J_nb x_nb - J x),
+// J = d(T, C_l)/d(H, C) per cell (t_cl_jac: the porosity root differentiated
+// implicitly), with the ghost of J x taken from the boundary rule of N:
+// the derived-variable condition (Dirichlet s = -1, Neumann s = +1 on the
+// centre's J x) when it is applied, else the (H, C) condition mapped through
+// the ghost state's Jacobian J_g.  The transpose, per cell j, is
+//   (A^T y)_j = alpha a_j y_j - beta dxinv (J_j^T w_j + e_j),
+//   w_j = sum_interior b_f (y_nb - y_j) + sum_derived b_f (s y_j - y_j)
+//         - sum_(H,C)-condition b_f y_j,
+//   e_j = sum_(H,C)-condition faces S J_g^T (b_f y_j),   S = diag(s_H, s_C),
+// which is what these kernels evaluate: the apply / residual (fused norm),
+// a red/black block Gauss-Seidel (the 2x2 diagonal block of A^T inverted per
+// cell), the single-CTA bottom relaxation, the restriction of g - A^T y by
+// 2^D averaging, and the gradient of -y^T N with respect to the boundary
+// values.  The reference has no adjoint: the transposition is of its
+// discrete operator, term by term, so A^T is the exact transpose of the
+// linearisation of the kernels that compute N.  Temperature conditions on H
+// (types 2-4) are not differentiated (the entry points refuse them).
+#pragma once
+#include "nl_kernels.cuh"
+#include "reduce.cuh"
+
+namespace mlgpu {
+
+template <class T>
+struct AdjArgs {
+  Geom G;
+  ClosureParams cp;
+  BCD phi_bc, dbc;
+  int apply_dbc;
+  T alpha, beta, dxinv, dx;
+  const T *a;           // [2][cells] or null (a == 1)
+  const T *b[3];        // [2][faces_d]
+  const T *J;           // [4][cells]: dT/dH, dT/dC, dC_l/dH, dC_l/dC
+  const double *u;      // [2][cells] state (ghost Jacobians of the (H, C) condition)
+};
+
+// Jacobian of the closure at the (H, C)-condition ghost of cell q across
+// face (d, side): the ghost state by the linear rule, then t_cl_jac
+template <class T>
+__device__ __forceinline__ void adj_ghost_jac(const AdjArgs<T> &A, long long q, int d, int side,
+                                              double Jg[4]) {
+  const long long n = A.G.ncell;
+  const double hg = ghost_value<double>(A.phi_bc, d, side, 0, A.u[q], A.G.dx, false);
+  const double cg = ghost_value<double>(A.phi_bc, d, side, 1, A.u[q + n], A.G.dx, false);
+  t_cl_jac(hg, cg, A.cp, Jg);
+}
+
+// (A^T y) at interior cell (i,j,k); with WANT_M also the 2x2 diagonal block
+// M (row-major, M[2c + c'] = d(A^T y)_c / d y_c') of that cell
+template <class T, int DIM, bool WANT_M>
+__device__ __forceinline__ void adj_cell(const AdjArgs<T> &A, const T *y, int i, int j, int k,
+                                         T out[2], T y0[2], T M[4]) {
+  const Geom &G = A.G;
+  const long long q = G.cell(i, j, k), n = G.ncell;
+  y0[0] = y[q];
+  y0[1] = y[q + n];
+  T w[2], P[2], ex[2] = {T(0), T(0)}, X[4] = {T(0), T(0), T(0), T(0)};
+  bool any_phi = false;
+#pragma unroll
+  for (int c = 0; c < 2; c++) {
+    T s = T(0), p = T(0);
+#pragma unroll
+    for (int d = 0; d < DIM; d++) {
+      const int idx[3] = {i, j, k};
+      const int m = G.n(d);
+      const long long nf = G.nface(d);
+#pragma unroll
+      for (int side = 1; side >= 0; side--) {  // high face first, as the forward sum
+        int nb[3] = {idx[0], idx[1], idx[2]};
+        nb[d] += side ? 1 : -1;
+        int fi[3] = {idx[0], idx[1], idx[2]};
+        if (side) fi[d] += 1;
+        const T bf = A.b[d][c * nf + G.face(d, fi[0], fi[1], fi[2])];
+        // t: this face's part of w, b_nb y_nb - b y0 (high side) or
+        // b y0 - b_nb y_nb (low side, subtracted), b_nb the coefficient the
+        // neighbour's own row uses for the face (different only across a
+        // periodic seam, where the forward reads face n for cell n-1 and
+        // face 0 for cell 0)
+        T t;
+        T dp;  // contribution of this face to P_c
+        if (nb[d] >= 0 && nb[d] < m) {
+          const T yn = y[c * n + G.cell(nb[0], nb[1], nb[2])];
+          t = side ? bf * (yn - y0[c]) : bf * (y0[c] - yn);
+          dp = bf;
+        } else if (G.per(d)) {
+          nb[d] = nb[d] < 0 ? m - 1 : 0;
+          const long long qn = G.cell(nb[0], nb[1], nb[2]);
+          int fs[3] = {idx[0], idx[1], idx[2]};
+          fs[d] = side ? 0 : m;
+          const T bn = A.b[d][c * nf + G.face(d, fs[0], fs[1], fs[2])];
+          const T yn = y[c * n + qn];
+          if (qn == q)
+            t = T(0);
+          else
+            t = side ? bn * yn - bf * y0[c] : bf * y0[c] - bn * yn;
+          dp = qn == q ? T(0) : bf;
+        } else if (A.apply_dbc) {
+          const T yn = ghost_value<T>(A.dbc, d, side, c, y0[c], A.dx, true);
+          t = side ? bf * (yn - y0[c]) : bf * (y0[c] - yn);
+          dp = A.dbc.type[d][side][c] == MLGPU_BC_DIRICHLET ? T(2) * bf : T(0);
+        } else {
+          t = side ? bf * (T(0) - y0[c]) : bf * (y0[c] - T(0));
+          dp = bf;
+          any_phi = true;
+        }
+        // forward order: + b_hi (y_hi - y0), then - b_lo (y0 - y_lo)
+        if (side)
+          s = (d == 0) ? t : s + t;
+        else
+          s = s - t;
+        if (WANT_M) p = p + dp;
+      }
+    }
+    w[c] = s;
+    P[c] = p;
+  }
+  if (any_phi) {
+    // e_c = sum over (H, C)-condition faces of s_c (J_g^T (b_f y0))_c
+#pragma unroll
+    for (int d = 0; d < DIM; d++) {
+      if (G.per(d)) continue;
+      const int idx[3] = {i, j, k};
+      const int m = G.n(d);
+      const long long nf = G.nface(d);
+#pragma unroll
+      for (int side = 0; side < 2; side++) {
+        if (side ? idx[d] != m - 1 : idx[d] != 0) continue;
+        int fi[3] = {idx[0], idx[1], idx[2]};
+        if (side) fi[d] += 1;
+        const long long f = G.face(d, fi[0], fi[1], fi[2]);
+        const T b0 = A.b[d][f], b1 = A.b[d][nf + f];
+        double Jg[4];
+        adj_ghost_jac(A, q, d, side, Jg);
+#pragma unroll
+        for (int c = 0; c < 2; c++) {
+          const T sc = A.phi_bc.type[d][side][c] == MLGPU_BC_DIRICHLET ? T(-1) : T(1);
+          const T g0 = (T)Jg[c], g1 = (T)Jg[2 + c];  // J_g(0, c), J_g(1, c)
+          ex[c] = ex[c] + sc * (g0 * (b0 * y0[0]) + g1 * (b1 * y0[1]));
+          if (WANT_M) {
+            X[2 * c + 0] = X[2 * c + 0] + sc * (g0 * b0);
+            X[2 * c + 1] = X[2 * c + 1] + sc * (g1 * b1);
+          }
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < 2; c++) {
+    // (J^T w)_c = J(0, c) w_0 + J(1, c) w_1
+    const T j0 = A.J[c * n + q], j1 = A.J[(2 + c) * n + q];
+    T t = j0 * w[0] + j1 * w[1];
+    if (any_phi) t = t + ex[c];
+    const T av = A.a ? A.a[q + c * n] : T(1);
+    out[c] = A.alpha * av * y0[c] - A.beta * t * A.dxinv;
+    if (WANT_M) {
+      // d out_c / d y_c' = delta alpha a_c + beta dxinv (J(c', c) P_c' - X(c, c'))
+#pragma unroll
+      for (int cp = 0; cp < 2; cp++) {
+        const T jcc = A.J[(2 * cp + c) * n + q];
+        T v = A.beta * A.dxinv * (jcc * P[cp] - X[2 * c + cp]);
+        if (cp == c) v = A.alpha * av + v;
+        M[2 * c + cp] = v;
+      }
+    }
+  }
+}
+
+// y_j += M^-1 (g_j - (A^T y)_j): the exact solve of cell j's two rows
+template <class T, int DIM>
+__device__ __forceinline__ void adj_gs_cell(const AdjArgs<T> &A, T *y, const T *g, int i, int j,
+                                            int k) {
+  T out[2], y0[2], M[4];
+  adj_cell<T, DIM, true>(A, y, i, j, k, out, y0, M);
+  const long long q = A.G.cell(i, j, k), n = A.G.ncell;
+  const T r0 = g[q] - out[0], r1 = g[q + n] - out[1];
+  const T det = M[0] * M[3] - M[1] * M[2];
+  y[q] = y0[0] + (M[3] * r0 - M[1] * r1) / det;
+  y[q + n] = y0[1] + (M[0] * r1 - M[2] * r0) / det;
+}
+
+enum { ADJ_APPLY = 0, ADJ_RESIDUAL = 1 };
+
+#if defined(MLGPU_FP64_UNIT) || defined(MLGPU_FP32_UNIT)
+// closure Jacobian of every cell in the kernels' precision
+template <class T>
+__global__ void __launch_bounds__(kBlock) adj_jac_kernel(Geom G, ClosureParams cp,
+                                                         const double *__restrict__ u,
+                                                         T *__restrict__ J) {
+  const long long n = G.ncell;
+  for (long long q = gtid(); q < n; q += gstride()) {
+    double j4[4];
+    t_cl_jac(u[q], u[q + n], cp, j4);
+#pragma unroll
+    for (int m = 0; m < 4; m++) J[q + m * n] = (T)j4[m];
+  }
+}
+
+// out = A^T y (ADJ_APPLY) or g - A^T y with a fused norm (ADJ_RESIDUAL)
+template <class T, int DIM, int MODE, int NORM>
+__global__ void __launch_bounds__(kBlock) adj_op_kernel(AdjArgs<T> A, const T *__restrict__ y,
+                                                        const T *__restrict__ g,
+                                                        T *__restrict__ out,
+                                                        double *__restrict__ part) {
+  const Geom &G = A.G;
+  double acc = 0.0;
+  for (long long q = gtid(); q < G.ncell; q += gstride()) {
+    int i, j, k;
+    cell_ijk(G, q, i, j, k);
+    T o[2], y0[2];
+    adj_cell<T, DIM, false>(A, y, i, j, k, o, y0, nullptr);
+#pragma unroll
+    for (int c = 0; c < 2; c++) {
+      const long long qc = q + c * G.ncell;
+      const T v = MODE == ADJ_RESIDUAL ? g[qc] - o[c] : o[c];
+      out[qc] = v;
+      if (NORM >= 0) acc = norm_accum<NORM < 0 ? 0 : NORM>(acc, (double)v);
+    }
+  }
+  if (NORM >= 0) {
+    double r = block_reduce<NORM < 0 ? 0 : NORM>(acc);
+    if (threadIdx.x == 0) part[blockIdx.x] = r;
+  }
+}
+
+template <class T, int DIM>
+__global__ void __launch_bounds__(kBlock) adj_gsrb_kernel(AdjArgs<T> A, T *y,
+                                                          const T *__restrict__ g, int pass) {
+  const long long nt = colour_threads(A.G);
+  for (long long t = gtid(); t < nt; t += gstride()) {
+    int i, j, k;
+    if (colour_cell(A.G, pass, t, i, j, k)) adj_gs_cell<T, DIM>(A, y, g, i, j, k);
+  }
+}
+
+// bottom: y = 0 (if zero), then `sweeps` red/black sweeps in one block
+template <class T, int DIM>
+__global__ void __launch_bounds__(1024) adj_relax_block_kernel(AdjArgs<T> A, T *y,
+                                                               const T *__restrict__ g,
+                                                               int sweeps, int zero) {
+  const long long n = A.G.ncell;
+  if (zero) {
+    for (long long q = threadIdx.x; q < 2 * n; q += blockDim.x) y[q] = T(0);
+    __syncthreads();
+  }
+  const long long nt = colour_threads(A.G);
+  for (int s = 0; s < sweeps; s++)
+    for (int pass = 0; pass < 2; pass++) {
+      for (long long t = threadIdx.x; t < nt; t += blockDim.x) {
+        int i, j, k;
+        if (colour_cell(A.G, pass, t, i, j, k)) adj_gs_cell<T, DIM>(A, y, g, i, j, k);
+      }
+      __syncthreads();
+    }
+}
+
+// coarse right-hand side: the 2^D average of g - A^T y
+template <class T, int DIM>
+__global__ void __launch_bounds__(kBlock) adj_restrict_kernel(AdjArgs<T> A, Geom C,
+                                                              const T *__restrict__ y,
+                                                              const T *__restrict__ g,
+                                                              T *__restrict__ gc) {
+  const Geom &G = A.G;
+  const T denom = DIM == 3 ? T(8) : T(4);
+  for (long long Q = gtid(); Q < C.ncell; Q += gstride()) {
+    int I, J, K;
+    cell_ijk(C, Q, I, J, K);
+    T acc[2] = {T(0), T(0)};
+#pragma unroll
+    for (int kk = 0; kk < (DIM == 3 ? 2 : 1); kk++)
+#pragma unroll
+      for (int jj = 0; jj < 2; jj++)
+#pragma unroll
+        for (int ii = 0; ii < 2; ii++) {
+          const int i = 2 * I + ii, j = 2 * J + jj, k = DIM == 3 ? 2 * K + kk : 0;
+          T o[2], y0[2];
+          adj_cell<T, DIM, false>(A, y, i, j, k, o, y0, nullptr);
+          const long long q = G.cell(i, j, k);
+#pragma unroll
+          for (int c = 0; c < 2; c++) acc[c] = acc[c] + (g[q + c * G.ncell] - o[c]) / denom;
+        }
+    gc[Q] = acc[0];
+    gc[Q + C.ncell] = acc[1];
+  }
+}
+
+// Gradient of -y^T N with respect to the boundary values: one block per
+// (direction, side), out[(d * 2 + side) * 2 + c].  Derived condition applied:
+// d f_g,c / d v_c = 2 (Dirichlet) or s dx (Neumann), so the entry is
+// beta dxinv sum y_c b_c df; otherwise the (H, C) condition's value moves
+// phi_g,c and f_g through J_g: beta dxinv dphi sum_c' y_c' b_c' J_g(c', c).
+template <class T, int DIM>
+__global__ void __launch_bounds__(kBlock) adj_bc_grad_kernel(AdjArgs<T> A,
+                                                             const T *__restrict__ y,
+                                                             double *__restrict__ out) {
+  const Geom &G = A.G;
+  const int d = blockIdx.x >> 1, side = blockIdx.x & 1;
+  double acc[2] = {0.0, 0.0};
+  if (d < DIM && !G.per(d)) {
+    const int m0 = d == 0 ? G.n1 : G.n0;
+    const int m1 = d == 2 ? G.n1 : G.n2;
+    const long long nf = G.nface(d), n = G.ncell;
+    const long long tot = (long long)m0 * m1;
+    for (long long t = threadIdx.x; t < tot; t += blockDim.x) {
+      const int a0 = (int)(t % m0), a1 = (int)(t / m0);
+      int idx[3];
+      idx[d] = side ? G.n(d) - 1 : 0;
+      if (d == 0) { idx[1] = a0; idx[2] = a1; }
+      if (d == 1) { idx[0] = a0; idx[2] = a1; }
+      if (d == 2) { idx[0] = a0; idx[1] = a1; }
+      const long long q = G.cell(idx[0], idx[1], idx[2]);
+      int fi[3] = {idx[0], idx[1], idx[2]};
+      if (side) fi[d] += 1;
+      const long long f = G.face(d, fi[0], fi[1], fi[2]);
+      const double yb0 = (double)y[q] * (double)A.b[d][f];
+      const double yb1 = (double)y[q + n] * (double)A.b[d][nf + f];
+      if (A.apply_dbc) {
+        acc[0] += yb0;
+        acc[1] += yb1;
+      } else {
+        double Jg[4];
+        adj_ghost_jac(A, q, d, side, Jg);
+        acc[0] += yb0 * Jg[0] + yb1 * Jg[2];
+        acc[1] += yb0 * Jg[1] + yb1 * Jg[3];
+      }
+    }
+  }
+  const double s0 = block_reduce<2>(acc[0]);
+  __syncthreads();
+  const double s1 = block_reduce<2>(acc[1]);
+  if (threadIdx.x == 0) {
+    const BCD &bc = A.apply_dbc ? A.dbc : A.phi_bc;
+    const double isign = side ? 1.0 : -1.0;
+    for (int c = 0; c < 2; c++) {
+      double v = 0.0;
+      if (d < DIM && !G.per(d)) {
+        const double df = bc.type[d][side][c] == MLGPU_BC_DIRICHLET ? 2.0 : isign * (double)A.dx;
+        v = (double)A.beta * (double)A.dxinv * df * (c == 0 ? s0 : s1);
+      }
+      out[blockIdx.x * 2 + c] = v;
+    }
+  }
+}
+#endif
+
+}  // namespace mlgpu

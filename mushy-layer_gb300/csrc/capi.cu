@@ -113,6 +113,34 @@ bool valid_vcop(const mlgpu_vcop *op) {
   return true;
 }
 
+// the adjoint differentiates the linear wall rules only
+bool valid_adjoint_op(const mlgpu_nlop *op) {
+  if (!valid_nlop(op) || op->dtype != MLGPU_F64) return false;
+  for (int d = 0; d < 3; d++)
+    for (int s = 0; s < 2; s++)
+      if (is_temperature_bc(op->phi_bc.type[d][s][0])) return false;
+  return true;
+}
+
+AdjArgs<double> make_adj_args(const mlgpu_nlop &op, const double *phi, const double *J) {
+  NLArgs<double> N = make_nl_args<double>(op);
+  AdjArgs<double> A;
+  A.G = N.G;
+  A.cp = N.cp;
+  A.phi_bc = N.phi_bc;
+  A.dbc = N.dbc;
+  A.apply_dbc = N.apply_dbc;
+  A.alpha = N.alpha;
+  A.beta = N.beta;
+  A.dxinv = N.dxinv;
+  A.dx = N.dx;
+  A.a = N.a;
+  for (int d = 0; d < 3; d++) A.b[d] = N.b[d];
+  A.J = J;
+  A.u = phi;
+  return A;
+}
+
 static bool coarsenable(const mlgpu_grid &g) {
   for (int d = 0; d < g.dim; d++)
     if (g.n[d] % 2) return false;
@@ -168,6 +196,37 @@ int mlgpu_closure_tcl(const mlgpu_grid *g, const mlgpu_params *p, const double *
   if (!valid_grid(g) || !p || !HC || !TCl) return MLGPU_ERR_ARG;
   Geom G = make_geom(*g);
   return status_of(launch_closure_tcl(G.ncell, make_cp(*p), HC, TCl, (cudaStream_t)stream));
+}
+
+int mlgpu_closure_jacobian(const mlgpu_grid *g, const mlgpu_params *p, const double *HC,
+                           double *J, void *stream) {
+  if (!valid_grid(g) || !p || !HC || !J) return MLGPU_ERR_ARG;
+  return status_of(launch_adj_jac(make_geom(*g), make_cp(*p), HC, J, (cudaStream_t)stream));
+}
+
+int mlgpu_hc_adjoint_apply(const mlgpu_nlop *op, const double *phi, const double *J,
+                           const double *y, const double *g, double *out, void *stream) {
+  if (!valid_adjoint_op(op) || !phi || !J || !y || !out) return MLGPU_ERR_ARG;
+  return status_of(launch_adj_op(make_adj_args(*op, phi, J), g ? ADJ_RESIDUAL : ADJ_APPLY, -1,
+                                 y, g, out, nullptr, (cudaStream_t)stream));
+}
+
+int mlgpu_hc_adjoint_gsrb_pass(const mlgpu_nlop *op, const double *phi, const double *J,
+                               double *y, const double *g, int pass, void *stream) {
+  if (!valid_adjoint_op(op) || !phi || !J || !y || !g || (pass != 0 && pass != 1))
+    return MLGPU_ERR_ARG;
+  return status_of(launch_adj_gsrb(make_adj_args(*op, phi, J), y, g, pass, (cudaStream_t)stream));
+}
+
+int mlgpu_hc_adjoint_restrict(const mlgpu_nlop *op, const double *phi, const double *J,
+                              const double *y, const double *g, double *gc, void *stream) {
+  if (!valid_adjoint_op(op) || !phi || !J || !y || !g || !gc || !coarsenable(op->grid))
+    return MLGPU_ERR_ARG;
+  mlgpu_grid cg = op->grid;
+  for (int d = 0; d < cg.dim; d++) cg.n[d] /= 2;
+  cg.dx *= 2;
+  return status_of(launch_adj_restrict(make_adj_args(*op, phi, J), make_geom(cg), y, g, gc,
+                                       (cudaStream_t)stream));
 }
 
 int mlgpu_nl_residual(const mlgpu_nlop *op, void *res, const void *phi, const void *rhs,

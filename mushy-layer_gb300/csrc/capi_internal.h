@@ -12,6 +12,7 @@
 #include "outer_fast_kernels.cuh"
 #include "nl_cached_kernels.cuh"
 #include "hcm_kernels.cuh"
+#include "adjoint_kernels.cuh"
 
 namespace mlgpu {
 
@@ -19,6 +20,8 @@ bool valid_grid(const mlgpu_grid *g);
 bool valid_vcop(const mlgpu_vcop *op);
 bool valid_bc(const mlgpu_bc &b, int dim, bool temperature_h);
 bool valid_nl_bcs(const mlgpu_nlop &op);
+bool valid_adjoint_op(const mlgpu_nlop *op);
+AdjArgs<double> make_adj_args(const mlgpu_nlop &op, const double *phi, const double *J);
 template <class T> NLArgs<T> make_nl_args(const mlgpu_nlop &op);
 template <class T> VCArgs<T> make_vc_args(const mlgpu_vcop &op);
 int status_of(cudaError_t e);
@@ -38,6 +41,27 @@ cudaError_t launch_mac_correct(const Geom &G, const BCD &bc, int d, const double
 cudaError_t launch_be_rhs(long long n, const double *phi_old, const double *a, const double *src,
                           double dt, double *rhs, cudaStream_t s);
 cudaError_t launch_vc_outer_fast(const OuterFast &P, int norm, cudaStream_t s);
+// adjoint (adjoint_kernels.cuh, misc_kernels.cuh)
+cudaError_t launch_mac_grad_t(const Geom &G, const BCD &bc, const double *const y[3],
+                              const double *const scale[3], double *r, cudaStream_t s);
+cudaError_t launch_mac_div_t(const Geom &G, int d, const double *q, const double *ubar,
+                             double *out, cudaStream_t s);
+cudaError_t launch_mac_pi_bar(const Geom &G, const BCD &bc, int d, const double *phi,
+                              const double *usb, double *pib, cudaStream_t s);
+cudaError_t launch_be_adj(long long n, const double *mu, const double *a, double dt,
+                          double *old_bar, double *src_bar, cudaStream_t s);
+cudaError_t launch_adj_jac(const Geom &G, const ClosureParams &cp, const double *u, double *J,
+                           cudaStream_t s);
+cudaError_t launch_adj_op(const AdjArgs<double> &A, int mode, int norm, const double *y,
+                          const double *g, double *out, double *part, cudaStream_t s);
+cudaError_t launch_adj_gsrb(const AdjArgs<double> &A, double *y, const double *g, int pass,
+                            cudaStream_t s);
+cudaError_t launch_adj_relax_block(const AdjArgs<double> &A, double *y, const double *g,
+                                   int sweeps, int zero, cudaStream_t s);
+cudaError_t launch_adj_restrict(const AdjArgs<double> &A, const Geom &C, const double *y,
+                                const double *g, double *gc, cudaStream_t s);
+cudaError_t launch_adj_bc_grad(const AdjArgs<double> &A, const double *y, double *out,
+                               cudaStream_t s);
 cudaError_t launch_outer_coefs(const VCArgs<double> &A, double *cx, double *cy, double *diag,
                                cudaStream_t s);
 // mixed-precision nonlinear solve: FP64 closure Jacobian (stored FP32), u += e

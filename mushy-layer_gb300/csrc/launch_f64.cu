@@ -6,6 +6,7 @@
 #include "outer_fast_kernels.cuh"
 #include "nl_cached_kernels.cuh"
 #include "hcm_kernels.cuh"
+#include "adjoint_kernels.cuh"
 
 namespace mlgpu {
 
@@ -181,6 +182,67 @@ cudaError_t launch_mac_correct(const Geom &G, const BCD &bc, int d, const double
 cudaError_t launch_be_rhs(long long n, const double *phi_old, const double *a, const double *src,
                           double dt, double *rhs, cudaStream_t s) {
   be_rhs_kernel<<<blocks_for(n), kBlock, 0, s>>>(n, phi_old, a, src, dt, rhs);
+  return cudaGetLastError();
+}
+
+// ---- adjoint
+cudaError_t launch_mac_grad_t(const Geom &G, const BCD &bc, const double *const y[3],
+                              const double *const scale[3], double *r, cudaStream_t s) {
+  mac_grad_t_kernel<<<blocks_for(G.ncell), kBlock, 0, s>>>(G, bc, y[0], y[1], y[2], scale[0],
+                                                           scale[1], scale[2], r);
+  return cudaGetLastError();
+}
+cudaError_t launch_mac_div_t(const Geom &G, int d, const double *q, const double *ubar,
+                             double *out, cudaStream_t s) {
+  mac_div_t_kernel<<<blocks_for(G.nface(d)), kBlock, 0, s>>>(G, d, q, ubar, out);
+  return cudaGetLastError();
+}
+cudaError_t launch_mac_pi_bar(const Geom &G, const BCD &bc, int d, const double *phi,
+                              const double *usb, double *pib, cudaStream_t s) {
+  mac_pi_bar_kernel<<<blocks_for(G.nface(d)), kBlock, 0, s>>>(G, bc, d, phi, usb, pib);
+  return cudaGetLastError();
+}
+cudaError_t launch_be_adj(long long n, const double *mu, const double *a, double dt,
+                          double *old_bar, double *src_bar, cudaStream_t s) {
+  be_adj_kernel<<<blocks_for(n), kBlock, 0, s>>>(n, mu, a, dt, old_bar, src_bar);
+  return cudaGetLastError();
+}
+cudaError_t launch_adj_jac(const Geom &G, const ClosureParams &cp, const double *u, double *J,
+                           cudaStream_t s) {
+  adj_jac_kernel<double><<<blocks_for(G.ncell), kBlock, 0, s>>>(G, cp, u, J);
+  return cudaGetLastError();
+}
+cudaError_t launch_adj_op(const AdjArgs<double> &A, int mode, int norm, const double *y,
+                          const double *g, double *out, double *part, cudaStream_t s) {
+  const int nb = blocks_for(A.G.ncell);
+  if (mode == ADJ_RESIDUAL && norm >= 0) {
+    if (!part) return cudaErrorInvalidValue;
+    MLGPU_DIM_SWITCH(A.G.dim, MLGPU_NORM_SWITCH(norm, (adj_op_kernel<double, DIM, ADJ_RESIDUAL, NORM><<<nb, kBlock, 0, s>>>(A, y, g, out, part))));
+  } else if (mode == ADJ_RESIDUAL) {
+    MLGPU_DIM_SWITCH(A.G.dim, (adj_op_kernel<double, DIM, ADJ_RESIDUAL, -1><<<nb, kBlock, 0, s>>>(A, y, g, out, part)));
+  } else {
+    MLGPU_DIM_SWITCH(A.G.dim, (adj_op_kernel<double, DIM, ADJ_APPLY, -1><<<nb, kBlock, 0, s>>>(A, y, g, out, part)));
+  }
+  return cudaGetLastError();
+}
+cudaError_t launch_adj_gsrb(const AdjArgs<double> &A, double *y, const double *g, int pass,
+                            cudaStream_t s) {
+  MLGPU_DIM_SWITCH(A.G.dim, (adj_gsrb_kernel<double, DIM><<<blocks_for(colour_threads(A.G)), kBlock, 0, s>>>(A, y, g, pass)));
+  return cudaGetLastError();
+}
+cudaError_t launch_adj_relax_block(const AdjArgs<double> &A, double *y, const double *g,
+                                   int sweeps, int zero, cudaStream_t s) {
+  MLGPU_DIM_SWITCH(A.G.dim, (adj_relax_block_kernel<double, DIM><<<1, 1024, 0, s>>>(A, y, g, sweeps, zero)));
+  return cudaGetLastError();
+}
+cudaError_t launch_adj_restrict(const AdjArgs<double> &A, const Geom &C, const double *y,
+                                const double *g, double *gc, cudaStream_t s) {
+  MLGPU_DIM_SWITCH(A.G.dim, (adj_restrict_kernel<double, DIM><<<blocks_for(C.ncell), kBlock, 0, s>>>(A, C, y, g, gc)));
+  return cudaGetLastError();
+}
+cudaError_t launch_adj_bc_grad(const AdjArgs<double> &A, const double *y, double *out,
+                               cudaStream_t s) {
+  MLGPU_DIM_SWITCH(A.G.dim, (adj_bc_grad_kernel<double, DIM><<<6, kBlock, 0, s>>>(A, y, out)));
   return cudaGetLastError();
 }
 

@@ -275,6 +275,142 @@ __global__ void __launch_bounds__(kBlock) mac_correct_kernel(Geom G, BCD bc, int
     u[t] = u[t] - grad;
   }
 }
+// --------------------------------------------- MAC projection adjoint
+// The projection u = u* - Pi G p, D Pi G p = D u* (mac_div_kernel,
+// mac_correct_kernel, the projection operator) transposes to
+//   q: D Pi G q = G^T (Pi ubar),  ustar_bar = ubar - D^T q,
+//   pi_bar = -ustar_bar * (G p)   (G p the corrected gradient, all faces),
+// with G^T and D^T the exact transposes of the face arrays as the forward
+// kernels index them: on a periodic seam faces 0 and n both carry the
+// gradient (p_0 - p_(n-1))/dx; at a wall the ghost rule's derivative
+// (Dirichlet -1, Neumann +1) enters.
+
+// r = G^T (scale * y) at every cell (scale == null: 1)
+__global__ void __launch_bounds__(kBlock) mac_grad_t_kernel(Geom G, BCD bc,
+                                                            const double *__restrict__ y0,
+                                                            const double *__restrict__ y1,
+                                                            const double *__restrict__ y2,
+                                                            const double *__restrict__ s0,
+                                                            const double *__restrict__ s1,
+                                                            const double *__restrict__ s2,
+                                                            double *__restrict__ r) {
+  for (long long q = gtid(); q < G.ncell; q += gstride()) {
+    int idx[3];
+    cell_ijk(G, q, idx[0], idx[1], idx[2]);
+    double v = 0.0;
+    for (int d = 0; d < G.dim; d++) {
+      const double *y = d == 0 ? y0 : (d == 1 ? y1 : y2);
+      const double *sc = d == 0 ? s0 : (d == 1 ? s1 : s2);
+      const int m = G.n(d), a = idx[d];
+      int f[3] = {idx[0], idx[1], idx[2]};
+      const long long flo = G.face(d, f[0], f[1], f[2]);
+      f[d] += 1;
+      const long long fhi = G.face(d, f[0], f[1], f[2]);
+      const double ylo = sc ? y[flo] * sc[flo] : y[flo];
+      const double yhi = sc ? y[fhi] * sc[fhi] : y[fhi];
+      // d(grad at the low face)/d p_a, d(grad at the high face)/d p_a
+      double clo = 1.0, chi = -1.0;
+      if (!G.per(d)) {
+        if (a == 0) clo = bc.type[d][0][0] == MLGPU_BC_DIRICHLET ? 2.0 : 0.0;
+        if (a == m - 1) chi = bc.type[d][1][0] == MLGPU_BC_DIRICHLET ? -2.0 : 0.0;
+      }
+      double t = clo * ylo + chi * yhi;
+      if (G.per(d)) {
+        // the seam's other face: face n holds the gradient of cell 0 as its
+        // high neighbour, face 0 that of cell n-1 as its low neighbour
+        if (a == 0) {
+          f[d] = m;
+          const long long fs = G.face(d, f[0], f[1], f[2]);
+          t = t + (sc ? y[fs] * sc[fs] : y[fs]);
+        }
+        if (a == m - 1) {
+          f[d] = 0;
+          const long long fs = G.face(d, f[0], f[1], f[2]);
+          t = t - (sc ? y[fs] * sc[fs] : y[fs]);
+        }
+      }
+      v = v + t / G.dx;
+    }
+    r[q] = v;
+  }
+}
+
+// out = ubar - D^T q on every face of direction d
+__global__ void __launch_bounds__(kBlock) mac_div_t_kernel(Geom G, int d,
+                                                           const double *__restrict__ q,
+                                                           const double *__restrict__ ubar,
+                                                           double *__restrict__ out) {
+  const double one_on_dx = 1.0 / G.dx;
+  const long long nf = G.nface(d);
+  const int m0 = G.n0 + (d == 0), m1 = G.n1 + (d == 1);
+  const int m = G.n(d);
+  for (long long t = gtid(); t < nf; t += gstride()) {
+    int f[3];
+    f[0] = (int)(t % m0);
+    long long rr = t / m0;
+    f[1] = (int)(rr % m1);
+    f[2] = (int)(rr / m1);
+    const int b = f[d];
+    double dt = 0.0;
+    if (b >= 1) {
+      int c[3] = {f[0], f[1], f[2]};
+      c[d] = b - 1;
+      dt = dt + one_on_dx * q[G.cell(c[0], c[1], c[2])];
+    }
+    if (b <= m - 1) dt = dt - one_on_dx * q[G.cell(f[0], f[1], f[2])];
+    out[t] = ubar[t] - dt;
+  }
+}
+
+// pi_bar = -ustar_bar * (corrected gradient of p) on every face of direction d
+__global__ void __launch_bounds__(kBlock) mac_pi_bar_kernel(Geom G, BCD bc, int d,
+                                                            const double *__restrict__ phi,
+                                                            const double *__restrict__ usb,
+                                                            double *__restrict__ pib) {
+  long long nf = G.nface(d);
+  int m0 = G.n0 + (d == 0), m1 = G.n1 + (d == 1);
+  int m = G.n(d);
+  for (long long t = gtid(); t < nf; t += gstride()) {
+    int i = (int)(t % m0);
+    long long r = t / m0;
+    int j = (int)(r % m1);
+    int k = (int)(r / m1);
+    int hi[3] = {i, j, k}, lo[3] = {i, j, k};
+    lo[d] -= 1;
+    double ph, pl;
+    if (hi[d] < m && lo[d] >= 0) {
+      ph = phi[G.cell(hi[0], hi[1], hi[2])];
+      pl = phi[G.cell(lo[0], lo[1], lo[2])];
+    } else if (G.per(d)) {
+      if (hi[d] >= m) hi[d] = 0;
+      if (lo[d] < 0) lo[d] = m - 1;
+      ph = phi[G.cell(hi[0], hi[1], hi[2])];
+      pl = phi[G.cell(lo[0], lo[1], lo[2])];
+    } else if (lo[d] < 0) {
+      ph = phi[G.cell(hi[0], hi[1], hi[2])];
+      pl = ghost_value<double>(bc, d, 0, 0, ph, G.dx, false);
+    } else {
+      pl = phi[G.cell(lo[0], lo[1], lo[2])];
+      ph = ghost_value<double>(bc, d, 1, 0, pl, G.dx, false);
+    }
+    const double grad = (ph - pl) / G.dx;
+    pib[t] = -(usb[t] * grad);
+  }
+}
+
+// Backward-Euler step adjoint: phi_old_bar = a mu (a == null: mu),
+// src_bar = dt mu (either output may be null)
+__global__ void __launch_bounds__(kBlock) be_adj_kernel(long long n, const double *__restrict__ mu,
+                                                        const double *__restrict__ a, double dt,
+                                                        double *__restrict__ old_bar,
+                                                        double *__restrict__ src_bar) {
+  for (long long q = gtid(); q < n; q += gstride()) {
+    const double m = mu[q];
+    if (old_bar) old_bar[q] = a ? a[q] * m : m;
+    if (src_bar) src_bar[q] = dt * m;
+  }
+}
+
 // Backward-Euler right-hand side (LevelBackwardEuler::updateSoln):
 // rhs = phi_old * a + dt * src; a == null means a == 1, src == null no source.
 __global__ void __launch_bounds__(kBlock) be_rhs_kernel(long long n, const double *__restrict__ phi_old,

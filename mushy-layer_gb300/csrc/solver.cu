@@ -1145,6 +1145,235 @@ class HCSolver : public mlgpu_solver {
   }
 };
 
+// ================================================================ adjoint
+// Multigrid for A^T y = g, A = dN/dphi at a given state (adjoint_kernels.cuh).
+// The hierarchy is the FAS solver's: coefficients coarsened the same way,
+// the state averaged down, J per level from its state; correction-scheme
+// V-cycles (block red/black smoothing, 2^D residual averaging, the solver's
+// prolongation with the adjoint variable's wall rule, single-CTA bottom
+// relaxation) inside an FP64 residual loop.
+struct AdjLevel {
+  mlgpu_grid grid;
+  Geom G;
+  Coefs<double> c64;
+  double *u = nullptr, *J = nullptr, *y = nullptr, *g = nullptr, *r = nullptr;
+};
+
+class HCAdjSolver : public mlgpu_solver {
+ public:
+  mlgpu_nlop op;
+  mlgpu_mg_options o;
+  std::vector<AdjLevel> L;
+  double *part = nullptr, *host_norm = nullptr, *bcg = nullptr;
+  double updates_per_iter = 0;
+  int kern_iter = -1, kern_init = -1;
+  cudaGraphExec_t graph = nullptr;
+
+  ~HCAdjSolver() override {
+    if (graph) cudaGraphExecDestroy(graph);
+    if (host_norm) cudaFreeHost(host_norm);
+  }
+
+  size_t layout(char *base) {
+    Arena A;
+    A.base = base;
+    int depth = mg_depth(op.grid, o.max_coarse);
+    L.assign(depth + 1, AdjLevel());
+    mlgpu_grid g = op.grid;
+    for (int l = 0; l <= depth; l++) {
+      L[l].grid = g;
+      L[l].G = make_geom(g);
+      size_t n = 2 * ncells(g);
+      if (l == 0) {
+        L[l].c64.a = (double *)op.aCoef;
+        for (int d = 0; d < 3; d++) L[l].c64.b[d] = (double *)op.bCoef[d];
+      } else {
+        if (op.aCoef) L[l].c64.a = A.get<double>(n);
+        for (int d = 0; d < g.dim; d++) L[l].c64.b[d] = A.get<double>(2 * nfaces(g, d));
+      }
+      L[l].u = A.get<double>(n);
+      L[l].J = A.get<double>(2 * n);
+      L[l].y = A.get<double>(n);
+      L[l].g = A.get<double>(n);
+      L[l].r = A.get<double>(n);
+      g = coarsen_grid(g);
+    }
+    part = A.get<double>(kNormScratchDoubles);
+    bcg = A.get<double>(16);
+    return A.off + 256;
+  }
+
+  int build_coefs() {
+    for (size_t l = 1; l < L.size(); l++) {
+      Geom F = L[l - 1].G;
+      if (op.aCoef) CK(launch_restrict_avg<double>(F, 2, L[l - 1].c64.a, L[l].c64.a, s));
+      for (int d = 0; d < F.dim; d++)
+        CK(launch_coarsen_faces<double>(F, 2, d, L[l - 1].c64.b[d], L[l].c64.b[d], s));
+    }
+    const int last = (int)L.size() - 1;
+    double u = 0;
+    for (int l = 0; l <= last; l++) {
+      double n = (double)L[l].G.ncell;
+      u += l == last ? o.bottom_max_iter * n : (o.num_smooth_down + o.num_smooth_up + 1) * n;
+    }
+    updates_per_iter = u + (double)L[0].G.ncell;
+    return MLGPU_OK;
+  }
+
+  AdjArgs<double> args(int l) {
+    mlgpu_nlop lop = op;
+    lop.grid = L[l].grid;
+    lop.aCoef = L[l].c64.a;
+    for (int d = 0; d < 3; d++) lop.bCoef[d] = L[l].c64.b[d];
+    return make_adj_args(lop, L[l].u, L[l].J);
+  }
+
+  // the wall rule of the adjoint variable in the prolongation
+  BCD ybc() const { return make_bcd(op.apply_derived_bc ? op.derived_bc : op.phi_bc); }
+
+  // state on every level and its Jacobians
+  int set_state(const double *phi) {
+    CK(cudaMemcpyAsync(L[0].u, phi, sizeof(double) * 2 * L[0].G.ncell, cudaMemcpyDeviceToDevice,
+                       s));
+    for (size_t l = 1; l < L.size(); l++)
+      CK(launch_restrict_avg<double>(L[l - 1].G, 2, L[l - 1].u, L[l].u, s));
+    const ClosureParams cp = make_cp(op.params);
+    for (auto &lv : L) CK(launch_adj_jac(lv.G, cp, lv.u, lv.J, s));
+    return MLGPU_OK;
+  }
+
+  int smooth(int l, int n) {
+    AdjArgs<double> A = args(l);
+    for (int i = 0; i < n; i++)
+      for (int pass = 0; pass < 2; pass++) CK(launch_adj_gsrb(A, L[l].y, L[l].g, pass, s));
+    return MLGPU_OK;
+  }
+
+  // V-cycle on level l; coarse levels start from zero
+  int cycle(int l) {
+    const int last = (int)L.size() - 1;
+    AdjArgs<double> A = args(l);
+    if (l == last) {
+      CK(launch_adj_relax_block(A, L[l].y, L[l].g, o.bottom_max_iter, l > 0 ? 1 : 0, s));
+      return MLGPU_OK;
+    }
+    if (l > 0) CK(cudaMemsetAsync(L[l].y, 0, sizeof(double) * 2 * L[l].G.ncell, s));
+    int rc = smooth(l, o.num_smooth_down);
+    if (rc) return rc;
+    CK(launch_adj_restrict(A, L[l + 1].G, L[l].y, L[l].g, L[l + 1].g, s));
+    for (int m = 0; m < o.num_mg; m++) {
+      rc = cycle(l + 1);
+      if (rc) return rc;
+    }
+    CK(launch_prolong<double>(L[l].G, ybc(), 2, o.prolong, L[l].y, L[l + 1].y, nullptr, s));
+    return smooth(l, o.num_smooth_up);
+  }
+
+  int residual_norm() {
+    CK(launch_adj_op(args(0), ADJ_RESIDUAL, o.norm_type, L[0].y, L[0].g, L[0].r, part, s));
+    CK(launch_finalize_norm(o.norm_type, part, norm_parts(L[0].G.ncell), part + kMaxBlocks, s));
+    CK(cudaMemcpyAsync(host_norm, part + kMaxBlocks, sizeof(double), cudaMemcpyDeviceToHost, s));
+    return MLGPU_OK;
+  }
+
+  int iteration() {
+    int rc = cycle(0);
+    if (rc) return rc;
+    return residual_norm();
+  }
+
+  int run_iteration() {
+    if (!o.use_graph) return iteration();
+    if (!graph) {
+      cudaGraph_t g;
+      CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+      int rc = iteration();
+      cudaError_t e = cudaStreamEndCapture(s, &g);
+      if (rc) return rc;
+      CK(e);
+      e = cudaGraphInstantiate(&graph, g, 0);
+      cudaGraphDestroy(g);
+      CK(e);
+    }
+    CK(cudaGraphLaunch(graph, s));
+    return MLGPU_OK;
+  }
+
+  // A^T y = g at the state already set; y, g device arrays of the caller
+  int solve_at_state(double *user_y, const double *user_g, mlgpu_solve_stats *st) {
+    size_t bytes = sizeof(double) * 2 * L[0].G.ncell;
+    CK(cudaMemcpyAsync(L[0].y, user_y, bytes, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(L[0].g, user_g, bytes, cudaMemcpyDeviceToDevice, s));
+    if (kern_iter < 0) {
+      kern_init = count_kernels([&] { return residual_norm(); });
+      kern_iter = count_kernels([&] { return iteration(); });
+    }
+    int rc = residual_norm();
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(s));
+    Outer S;
+    S.norm0 = S.norm = S.prev = *host_norm;
+    stats_begin(st, (int)L.size(), S.norm0);
+    st->cell_updates = (double)L[0].G.ncell;
+    st->kernel_launches = kern_init;
+    if (!std::isfinite(S.norm0)) S.status = 8;
+    while (outer_continue(o, S)) {
+      rc = run_iteration();
+      if (rc) return rc;
+      CK(cudaStreamSynchronize(s));
+      S.norm = *host_norm;
+      st->cycles += 1;
+      st->cell_updates += updates_per_iter;
+      st->kernel_launches += kern_iter;
+      outer_after(o, S, st);
+    }
+    CK(cudaMemcpyAsync(user_y, L[0].y, bytes, cudaMemcpyDeviceToDevice, s));
+    CK(cudaStreamSynchronize(s));
+    return outer_finish(o, S, st);
+  }
+
+  int adjoint_solve(const double *phi, const double *g, double *y, mlgpu_solve_stats *st) {
+    cudaGetLastError();
+    if (enter()) return MLGPU_ERR_CUDA;
+    int rc = set_state(phi);
+    if (rc) return rc;
+    rc = solve_at_state(y, g, st);
+    if (leave()) return MLGPU_ERR_CUDA;
+    return rc;
+  }
+
+  // gradient of -y^T N with respect to the wall values at the current state
+  int bc_gradient(const double *y, double grad[12]) {
+    cudaGetLastError();
+    if (enter()) return MLGPU_ERR_CUDA;
+    CK(launch_adj_bc_grad(args(0), y, bcg, s));
+    CK(cudaMemcpyAsync(grad, bcg, 12 * sizeof(double), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (leave()) return MLGPU_ERR_CUDA;
+    return MLGPU_OK;
+  }
+
+  // the base-class solve: A^T y = g at the state of the last adjoint solve
+  int solve(double *y, const double *g, mlgpu_solve_stats *st) override {
+    if (!y || !g || !st) return MLGPU_ERR_ARG;
+    cudaGetLastError();
+    if (enter()) return MLGPU_ERR_CUDA;
+    int rc = solve_at_state(y, g, st);
+    if (leave()) return MLGPU_ERR_CUDA;
+    return rc;
+  }
+
+  int set_alpha_beta(double a, double b) override {
+    op.alpha = a;
+    op.beta = b;
+    if (graph) {
+      cudaGraphExecDestroy(graph);
+      graph = nullptr;
+    }
+    return MLGPU_OK;
+  }
+};
+
 bool valid_options(const mlgpu_mg_options *o) {
   if (!o) return false;
   if (o->num_smooth_down < 0 || o->num_smooth_up < 0 || o->num_mg < 1 || o->max_iter < 0)
@@ -1339,6 +1568,116 @@ int mlgpu_hc_backward_euler(mlgpu_solver *S, double *phi_new, const double *phi_
   if (S->enter()) return MLGPU_ERR_CUDA;
   CK(launch_be_rhs(n, phi_old, aCoef, src, dt, rhs_scratch, S->s));
   return S->solve(phi_new, rhs_scratch, stats);
+}
+
+int mlgpu_hc_adjoint_workspace(const mlgpu_nlop *op, const mlgpu_mg_options *o,
+                               size_t *bytes) {
+  if (!valid_adjoint_op(op) || !valid_options(o) || !bytes) return MLGPU_ERR_ARG;
+  HCAdjSolver S;
+  S.op = *op;
+  S.o = *o;
+  *bytes = S.layout(nullptr);
+  return MLGPU_OK;
+}
+
+int mlgpu_hc_adjoint_create(const mlgpu_nlop *op, const mlgpu_mg_options *o, void *ws,
+                            size_t bytes, void *stream, mlgpu_solver **out) {
+  if (!valid_adjoint_op(op) || !valid_options(o) || !ws || !out) return MLGPU_ERR_ARG;
+  if (((uintptr_t)ws) & 255) return MLGPU_ERR_WORKSPACE;
+  HCAdjSolver *S = new HCAdjSolver;
+  S->op = *op;
+  S->o = *o;
+  cudaGetLastError();
+  if (S->init_streams((cudaStream_t)stream)) {
+    delete S;
+    return MLGPU_ERR_CUDA;
+  }
+  size_t need = S->layout(nullptr);
+  if (bytes < need) {
+    delete S;
+    return MLGPU_ERR_WORKSPACE;
+  }
+  S->layout((char *)ws);
+  if (cudaHostAlloc((void **)&S->host_norm, sizeof(double), cudaHostAllocDefault) != cudaSuccess) {
+    delete S;
+    return MLGPU_ERR_CUDA;
+  }
+  int rc = S->enter();
+  if (!rc) rc = S->build_coefs();
+  if (!rc) rc = S->leave();
+  if (rc) {
+    delete S;
+    return rc;
+  }
+  *out = S;
+  return MLGPU_OK;
+}
+
+int mlgpu_hc_adjoint_solve(mlgpu_solver *S, const double *phi, const double *g, double *y,
+                           mlgpu_solve_stats *stats) {
+  HCAdjSolver *A = dynamic_cast<HCAdjSolver *>(S);
+  if (!A || !phi || !g || !y || !stats) return MLGPU_ERR_ARG;
+  return A->adjoint_solve(phi, g, y, stats);
+}
+
+int mlgpu_hc_adjoint_bc_gradient(mlgpu_solver *S, const double *y, double grad[12]) {
+  HCAdjSolver *A = dynamic_cast<HCAdjSolver *>(S);
+  if (!A || !y || !grad) return MLGPU_ERR_ARG;
+  return A->bc_gradient(y, grad);
+}
+
+int mlgpu_hc_backward_euler_adjoint(mlgpu_solver *S, const double *phi_new,
+                                    const double *phi_new_bar, const double *aCoef, double dt,
+                                    double *mu, double *phi_old_bar, double *src_bar,
+                                    double bc_grad[12], mlgpu_solve_stats *stats) {
+  HCAdjSolver *A = dynamic_cast<HCAdjSolver *>(S);
+  if (!A || !phi_new || !phi_new_bar || !mu || !stats || !(dt > 0)) return MLGPU_ERR_ARG;
+  if (A->op.alpha != 1.0 || A->op.beta != -dt) A->set_alpha_beta(1.0, -dt);
+  int rc = A->adjoint_solve(phi_new, phi_new_bar, mu, stats);
+  if (rc != MLGPU_OK && rc != MLGPU_ERR_NOT_CONVERGED && rc != MLGPU_ERR_HANG) return rc;
+  cudaGetLastError();
+  if (A->enter()) return MLGPU_ERR_CUDA;
+  if (phi_old_bar || src_bar)
+    CK(launch_be_adj(2 * A->L[0].G.ncell, mu, aCoef, dt, phi_old_bar, src_bar, A->s));
+  if (A->leave()) return MLGPU_ERR_CUDA;
+  if (bc_grad) {
+    int rc2 = A->bc_gradient(mu, bc_grad);
+    if (rc2) return rc2;
+  }
+  return rc;
+}
+
+int mlgpu_mac_project_adjoint(mlgpu_solver *S, const mlgpu_grid *grid, const mlgpu_bc *phi_bc,
+                              const double *ubar[3], const double *pi_face[3],
+                              const double *p, double *ustar_bar[3], double *pi_bar[3],
+                              double *q, double *scratch, mlgpu_solve_stats *stats) {
+  if (!S || !valid_grid(grid) || !phi_bc || !ubar || !ustar_bar || !q || !scratch || !stats)
+    return MLGPU_ERR_ARG;
+  if (!valid_bc(*phi_bc, grid->dim, false)) return MLGPU_ERR_ARG;
+  if (pi_bar && !p) return MLGPU_ERR_ARG;
+  VCSolver *V = dynamic_cast<VCSolver *>(S);
+  if (!V) return MLGPU_ERR_ARG;
+  for (int d = 0; d < 3; d++)
+    if (grid->n[d] != V->op.grid.n[d]) return MLGPU_ERR_ARG;
+  for (int d = 0; d < grid->dim; d++)
+    if (!ubar[d] || !ustar_bar[d]) return MLGPU_ERR_ARG;
+  Geom G = make_geom(*grid);
+  BCD b = make_bcd(*phi_bc);
+  const double *y[3] = {ubar[0], ubar[1], grid->dim == 3 ? ubar[2] : nullptr};
+  const double *sc[3] = {nullptr, nullptr, nullptr};
+  if (pi_face)
+    for (int d = 0; d < grid->dim; d++) sc[d] = pi_face[d];
+  cudaGetLastError();
+  if (S->enter()) return MLGPU_ERR_CUDA;
+  CK(launch_mac_grad_t(G, b, y, sc, scratch, S->s));
+  int rc = S->solve(q, scratch, stats);
+  if (rc != MLGPU_OK && rc != MLGPU_ERR_NOT_CONVERGED && rc != MLGPU_ERR_HANG) return rc;
+  for (int d = 0; d < grid->dim; d++) {
+    CK(launch_mac_div_t(G, d, q, ubar[d], ustar_bar[d], S->s));
+    if (pi_bar && pi_bar[d]) CK(launch_mac_pi_bar(G, b, d, p, ustar_bar[d], pi_bar[d], S->s));
+  }
+  if (S->leave()) return MLGPU_ERR_CUDA;
+  return rc;
 }
 
 int mlgpu_solver_destroy(mlgpu_solver *s) {

@@ -266,8 +266,9 @@ class _Solver:
         lib = abi.load()
         self.desc = op.desc()
         nbytes = C.c_size_t()
-        fn_ws = lib.mlgpu_hc_solver_workspace if kind == "hc" else lib.mlgpu_vc_solver_workspace
-        fn_cr = lib.mlgpu_hc_solver_create if kind == "hc" else lib.mlgpu_vc_solver_create
+        fn_ws, fn_cr = {"hc": (lib.mlgpu_hc_solver_workspace, lib.mlgpu_hc_solver_create),
+                        "vc": (lib.mlgpu_vc_solver_workspace, lib.mlgpu_vc_solver_create),
+                        "adj": (lib.mlgpu_hc_adjoint_workspace, lib.mlgpu_hc_adjoint_create)}[kind]
         abi.check(fn_ws(C.byref(self.desc), C.byref(opts), C.byref(nbytes)), "workspace")
         self.ws = torch.empty(nbytes.value // 8 + 64, dtype=torch.float64, device="cuda")
         base = self.ws.data_ptr()
@@ -343,3 +344,93 @@ class AMRMultiGrid(_Solver):
         if rc not in (abi.OK, abi.ERR_NOT_CONVERGED, abi.ERR_HANG):
             abi.check(rc, "levelMacProject")
         return st, rc
+
+
+def _ok(rc, what):
+    if rc not in (abi.OK, abi.ERR_NOT_CONVERGED, abi.ERR_HANG):
+        abi.check(rc, what)
+
+
+def closureJacobian(grid, params, HC):
+    """d(T, C_l)/d(H, C) of every cell: tensor [4][cells...]."""
+    J = torch.empty((4,) + tuple(HC.shape[1:]), dtype=torch.float64, device=HC.device)
+    abi.check(abi.load().mlgpu_closure_jacobian(C.byref(grid), C.byref(params), _ptr(HC),
+                                                _ptr(J), _stream()), "closureJacobian")
+    return J
+
+
+def adjointApply(op, phi, J, y, g=None):
+    """A^T y (g None) or g - A^T y, A = dN/dphi of `op` at phi (J of phi)."""
+    out = torch.empty_like(y)
+    abi.check(abi.load().mlgpu_hc_adjoint_apply(C.byref(op.desc()), _ptr(phi), _ptr(J), _ptr(y),
+                                                _ptr(g), _ptr(out), _stream()), "adjointApply")
+    return out
+
+
+def adjointGSRBPass(op, phi, J, y, g, pass_):
+    abi.check(abi.load().mlgpu_hc_adjoint_gsrb_pass(C.byref(op.desc()), _ptr(phi), _ptr(J),
+                                                    _ptr(y), _ptr(g), int(pass_), _stream()),
+              "adjointGSRBPass")
+
+
+def adjointRestrict(op, phi, J, y, g):
+    gc = cell_tensor(coarse_grid(op.grid), 2, torch.float64)
+    abi.check(abi.load().mlgpu_hc_adjoint_restrict(C.byref(op.desc()), _ptr(phi), _ptr(J),
+                                                   _ptr(y), _ptr(g), _ptr(gc), _stream()),
+              "adjointRestrict")
+    return gc
+
+
+class AdjointMultiGrid(_Solver):
+    """Multigrid for A^T y = g, A the Jacobian of NLMultiCompOp at a state
+    (the discrete adjoint of the converged nonlinear solve)."""
+
+    def __init__(self, op, opts=None):
+        super().__init__(op, opts or default_options(True), "adj")
+
+    def adjointSolve(self, phi, g, y):
+        st = abi.SolveStats()
+        rc = abi.load().mlgpu_hc_adjoint_solve(self.h, _ptr(phi), _ptr(g), _ptr(y), C.byref(st))
+        _ok(rc, "adjointSolve")
+        return st, rc
+
+    def bcGradient(self, y):
+        """-y^T dN/dv for the 12 wall values [dir][side][comp] at the last state."""
+        out = (C.c_double * 12)()
+        torch.cuda.current_stream().synchronize()
+        abi.check(abi.load().mlgpu_hc_adjoint_bc_gradient(self.h, _ptr(y), out), "bcGradient")
+        return [out[q] for q in range(12)]
+
+    def backwardEulerAdjoint(self, phi_new, phi_new_bar, dt, mu, aCoef=None, want_src=True):
+        """Adjoint of backwardEuler: returns (phi_old_bar, src_bar, bc_grad, stats, rc)."""
+        old_bar = torch.empty_like(phi_new)
+        src_bar = torch.empty_like(phi_new) if want_src else None
+        bcg = (C.c_double * 12)()
+        st = abi.SolveStats()
+        rc = abi.load().mlgpu_hc_backward_euler_adjoint(
+            self.h, _ptr(phi_new), _ptr(phi_new_bar), _ptr(aCoef), float(dt), _ptr(mu),
+            _ptr(old_bar), _ptr(src_bar), bcg, C.byref(st))
+        _ok(rc, "backwardEulerAdjoint")
+        return old_bar, src_bar, [bcg[q] for q in range(12)], st, rc
+
+
+def macProjectAdjoint(solver, ubar, pi_face, p, q=None, phi_bc=None, want_pi=True):
+    """Adjoint of AMRMultiGrid.levelMacProject: returns (ustar_bar, pi_bar, q, stats, rc)."""
+    g = solver.op.grid
+    dim = g.dim
+    scratch = cell_tensor(g, 1, torch.float64)
+    if q is None:
+        q = cell_tensor(g, 1, torch.float64)
+        q.zero_()
+    usb = [torch.empty_like(ubar[d]) for d in range(dim)]
+    pib = [torch.empty_like(ubar[d]) for d in range(dim)] if want_pi else None
+    st = abi.SolveStats()
+    bc = phi_bc if phi_bc is not None else solver.op.bc
+    pad = lambda L: list(L) + [None] * (3 - len(L))
+    rc = abi.load().mlgpu_mac_project_adjoint(
+        solver.h, C.byref(g), C.byref(bc), _faces3(pad(ubar[:dim])),
+        _faces3(pad(pi_face[:dim])) if pi_face is not None else None, _ptr(p),
+        _faces3(pad(usb)), _faces3(pad(pib)) if want_pi else None, _ptr(q), _ptr(scratch),
+        C.byref(st))
+    _ok(rc, "macProjectAdjoint")
+    return usb, pib, q, st, rc

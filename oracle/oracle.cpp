@@ -1350,3 +1350,562 @@ int orc_vc_solve(const mlgpu_vcop *op, const mlgpu_mg_options *o, double *phi,
 }
 
 }  // extern "C"
+
+// ================================================================ adjoint
+// Discrete adjoint of the nonlinear operator (no counterpart in the
+// reference).  With f = (T, C_l) of (H, C) and J = df/d(H, C) (t_cl_jac), the
+// Jacobian of N(phi) = alpha a phi - beta dxinv sum_f b_f (f_nb - f) is
+//   A x = alpha a x - beta dxinv sum_f b_f (J_nb x_nb - J x)
+// with the wall ghost of J x from the condition N uses: the derived
+// condition's homogeneous rule on J x, or J_g S x with J_g the Jacobian at the
+// (H, C)-condition ghost state and S its homogeneous signs.  Its transpose,
+// per cell, is alpha a y - beta dxinv (J^T w + e) with
+//   w = sum_f b_f (y_g - y),  y_g = neighbour, derived-rule ghost of y, or 0
+//   e = sum over (H, C)-condition faces of S J_g^T (b_f y).
+// The functions below restate that, and A itself, on ghosted FABs.
+namespace {
+
+struct AdjCtx {
+  const mlgpu_nlop &op;
+  Faces B;
+  const double *a, *J, *u;
+  double dxinv;
+  size_t n;
+  AdjCtx(const mlgpu_nlop &o, const double *phi, const double *Jd) : op(o), J(Jd), u(phi) {
+    B = make_faces(o.grid, o.bCoef);
+    a = (const double *)o.aCoef;
+    dxinv = 1.0 / (o.grid.dx * o.grid.dx);
+    n = ncells(o.grid);
+  }
+  double jac(size_t q, int m) const { return J[m * n + q]; }
+};
+
+// ghosts of the adjoint variable: periodic copies; the derived condition's
+// homogeneous rule when N applies it; zero under the (H, C) condition
+void adj_fill(Fab &y, const mlgpu_nlop &op) {
+  exchange(y, op.grid);
+  if (op.apply_derived_bc) {
+    physbc(y, op.grid, op.derived_bc, true);
+    return;
+  }
+  for (int d = 0; d < op.grid.dim; d++) {
+    if (op.grid.periodic[d]) continue;
+    for (int side = 0; side < 2; side++) {
+      int lo[3] = {0, 0, 0}, hi[3] = {y.n[0] - 1, y.n[1] - 1, y.n[2] - 1};
+      lo[d] = hi[d] = side == 0 ? -1 : y.n[d];
+      for (int c = 0; c < 2; c++)
+        for (int k = lo[2]; k <= hi[2]; k++)
+          for (int j = lo[1]; j <= hi[1]; j++)
+            for (int i = lo[0]; i <= hi[0]; i++) y(i, j, k, c) = 0.0;
+    }
+  }
+}
+
+// Jacobian at the (H, C)-condition ghost state across (d, side) of cell q
+void ghost_jac(const AdjCtx &X, size_t q, int d, int side, double Jg[4]) {
+  const mlgpu_bc &bc = X.op.phi_bc;
+  double st[2];
+  for (int c = 0; c < 2; c++) {
+    double interior = X.u[c * X.n + q];
+    double val = bc.value[d][side][c];
+    if (bc.type[d][side][c] == MLGPU_BC_DIRICHLET)
+      st[c] = 2 * val - interior;
+    else
+      st[c] = interior + ((side == 0 ? -1 : 1) * X.op.grid.dx) * val;
+  }
+  t_cl_jac(st[0], st[1], X.op.params, Jg);
+}
+
+// (A^T y) of cell (i,j,k); M = its 2x2 diagonal block (row-major) if asked
+void adj_row(const AdjCtx &X, const Fab &y, int i, int j, int k, double out[2], double *M) {
+  const mlgpu_grid &g = X.op.grid;
+  const size_t q = cidx(g, i, j, k, 0);
+  const double y0[2] = {y(i, j, k, 0), y(i, j, k, 1)};
+  double w[2], P[2], ex[2] = {0.0, 0.0}, Xm[4] = {0.0, 0.0, 0.0, 0.0};
+  bool any_phi = false;
+  const int at[3] = {i, j, k};
+  for (int c = 0; c < 2; c++) {
+    // w_c = sum over faces of (b_nb y_nb - b y0): the neighbour's row reads
+    // its own face coefficient, which differs from this cell's only across a
+    // periodic seam (face n for cell n-1, face 0 for cell 0)
+    double s = 0.0;
+    for (int d = 0; d < g.dim; d++)
+      for (int side = 1; side >= 0; side--) {
+        int fi[3] = {i, j, k}, nbc[3] = {i, j, k};
+        if (side) fi[d] += 1;
+        nbc[d] += side ? 1 : -1;
+        double bf = X.B(d, fi[0], fi[1], fi[2], c);
+        double yn = y(nbc[0], nbc[1], nbc[2], c);
+        double t;
+        bool seam = g.periodic[d] && (nbc[d] < 0 || nbc[d] >= g.n[d]);
+        if (seam && g.n[d] == 1) {
+          t = 0.0;
+        } else if (seam) {
+          int fs[3] = {i, j, k};
+          fs[d] = side ? 0 : g.n[d];
+          double bn = X.B(d, fs[0], fs[1], fs[2], c);
+          t = side ? bn * yn - bf * y0[c] : bf * y0[c] - bn * yn;
+        } else {
+          t = side ? bf * (yn - y0[c]) : bf * (y0[c] - yn);
+        }
+        if (side)
+          s = d == 0 ? t : s + t;
+        else
+          s = s - t;
+      }
+    w[c] = s;
+    // d w_c / d y_c = -P_c
+    double p = 0.0;
+    for (int d = 0; d < g.dim; d++)
+      for (int side = 1; side >= 0; side--) {
+        int fi[3] = {i, j, k};
+        if (side) fi[d] += 1;
+        double bf = X.B(d, fi[0], fi[1], fi[2], c);
+        int nb = at[d] + (side ? 1 : -1);
+        double dp;
+        if (nb >= 0 && nb < g.n[d])
+          dp = bf;
+        else if (g.periodic[d])
+          dp = g.n[d] == 1 ? 0.0 : bf;
+        else if (X.op.apply_derived_bc)
+          dp = X.op.derived_bc.type[d][side][c] == MLGPU_BC_DIRICHLET ? 2 * bf : 0.0;
+        else {
+          dp = bf;
+          any_phi = true;
+        }
+        p = p + dp;
+      }
+    P[c] = p;
+  }
+  if (any_phi) {
+    for (int d = 0; d < g.dim; d++) {
+      if (g.periodic[d]) continue;
+      for (int side = 0; side < 2; side++) {
+        if (side ? at[d] != g.n[d] - 1 : at[d] != 0) continue;
+        int fi[3] = {i, j, k};
+        if (side) fi[d] += 1;
+        const double b0 = X.B(d, fi[0], fi[1], fi[2], 0), b1 = X.B(d, fi[0], fi[1], fi[2], 1);
+        double Jg[4];
+        ghost_jac(X, q, d, side, Jg);
+        for (int c = 0; c < 2; c++) {
+          double sc = X.op.phi_bc.type[d][side][c] == MLGPU_BC_DIRICHLET ? -1.0 : 1.0;
+          double g0 = Jg[c], g1 = Jg[2 + c];
+          ex[c] = ex[c] + sc * (g0 * (b0 * y0[0]) + g1 * (b1 * y0[1]));
+          Xm[2 * c + 0] = Xm[2 * c + 0] + sc * (g0 * b0);
+          Xm[2 * c + 1] = Xm[2 * c + 1] + sc * (g1 * b1);
+        }
+      }
+    }
+  }
+  for (int c = 0; c < 2; c++) {
+    double t = X.jac(q, c) * w[0] + X.jac(q, 2 + c) * w[1];
+    if (any_phi) t = t + ex[c];
+    double av = X.a ? X.a[q + c * X.n] : 1.0;
+    out[c] = X.op.alpha * av * y0[c] - X.op.beta * t * X.dxinv;
+    if (M)
+      for (int cp = 0; cp < 2; cp++) {
+        double v = X.op.beta * X.dxinv * (X.jac(q, 2 * cp + c) * P[cp] - Xm[2 * c + cp]);
+        if (cp == c) v = X.op.alpha * av + v;
+        M[2 * c + cp] = v;
+      }
+  }
+}
+
+void adj_load(Fab &y, const mlgpu_nlop &op, const double *yd) {
+  y.define(op.grid, 2);
+  y.load(yd);
+  adj_fill(y, op);
+}
+
+// one red/black pass of the block smoother: each cell of the colour solves
+// its two rows exactly, y += M^-1 (g - A^T y)
+void adj_gsrb_pass_fab(Fab &y, const AdjCtx &X, const double *g, int pass) {
+  const mlgpu_grid &gr = X.op.grid;
+  adj_fill(y, X.op);
+  for (int k = 0; k < gr.n[2]; k++)
+    for (int j = 0; j < gr.n[1]; j++) {
+      int imin = std::abs((j + k + pass) % 2);
+      for (int i = imin; i < gr.n[0]; i += 2) {
+        double out[2], M[4];
+        adj_row(X, y, i, j, k, out, M);
+        size_t q = cidx(gr, i, j, k, 0);
+        double r0 = g[q] - out[0], r1 = g[q + X.n] - out[1];
+        double det = M[0] * M[3] - M[1] * M[2];
+        double y0 = y(i, j, k, 0), y1 = y(i, j, k, 1);
+        y(i, j, k, 0) = y0 + (M[3] * r0 - M[1] * r1) / det;
+        y(i, j, k, 1) = y1 + (M[0] * r1 - M[2] * r0) / det;
+      }
+    }
+}
+
+// A x (the linearised operator) on ghosted FABs of J x
+void lin_apply(const AdjCtx &X, const double *xd, double *out) {
+  const mlgpu_nlop &op = X.op;
+  const mlgpu_grid &g = op.grid;
+  Fab x(g, 2), jx(g, 2);
+  x.load(xd);
+  for (int k = 0; k < g.n[2]; k++)
+    for (int j = 0; j < g.n[1]; j++)
+      for (int i = 0; i < g.n[0]; i++) {
+        size_t q = cidx(g, i, j, k, 0);
+        double x0 = x(i, j, k, 0), x1 = x(i, j, k, 1);
+        jx(i, j, k, 0) = X.jac(q, 0) * x0 + X.jac(q, 1) * x1;
+        jx(i, j, k, 1) = X.jac(q, 2) * x0 + X.jac(q, 3) * x1;
+      }
+  exchange(jx, g);
+  if (op.apply_derived_bc) {
+    physbc(jx, g, op.derived_bc, true);
+  } else {
+    for (int d = 0; d < g.dim; d++) {
+      if (g.periodic[d]) continue;
+      for (int side = 0; side < 2; side++) {
+        int lo[3] = {0, 0, 0}, hi[3] = {g.n[0] - 1, g.n[1] - 1, g.n[2] - 1};
+        lo[d] = hi[d] = side == 0 ? 0 : g.n[d] - 1;
+        for (int k = lo[2]; k <= hi[2]; k++)
+          for (int j = lo[1]; j <= hi[1]; j++)
+            for (int i = lo[0]; i <= hi[0]; i++) {
+              size_t q = cidx(g, i, j, k, 0);
+              double Jg[4];
+              ghost_jac(X, q, d, side, Jg);
+              double s0 = op.phi_bc.type[d][side][0] == MLGPU_BC_DIRICHLET ? -1.0 : 1.0;
+              double s1 = op.phi_bc.type[d][side][1] == MLGPU_BC_DIRICHLET ? -1.0 : 1.0;
+              double e0 = s0 * x(i, j, k, 0), e1 = s1 * x(i, j, k, 1);
+              int t[3] = {i, j, k};
+              t[d] += side == 0 ? -1 : 1;
+              jx(t[0], t[1], t[2], 0) = Jg[0] * e0 + Jg[1] * e1;
+              jx(t[0], t[1], t[2], 1) = Jg[2] * e0 + Jg[3] * e1;
+            }
+      }
+    }
+  }
+  for (int c = 0; c < 2; c++)
+    for (int k = 0; k < g.n[2]; k++)
+      for (int j = 0; j < g.n[1]; j++)
+        for (int i = 0; i < g.n[0]; i++) {
+          size_t q = cidx(g, i, j, k, c);
+          double av = X.a ? X.a[q] : 1.0;
+          out[q] = op.alpha * av * x(i, j, k, c) -
+                   op.beta * flux_sum(X.B, jx, i, j, k, c, g.dim) * X.dxinv;
+        }
+}
+
+// ---- multigrid for A^T y = g (the device driver restated)
+struct AdjLevelO {
+  mlgpu_grid g;
+  std::vector<double> a, b[3], u, J, y, gg, r;
+};
+
+struct AdjSolver {
+  mlgpu_nlop op0;
+  mlgpu_mg_options o;
+  std::vector<AdjLevelO> L;
+  double updates = 0;
+
+  mlgpu_nlop op_at(int l) {
+    mlgpu_nlop op = op0;
+    op.grid = L[l].g;
+    op.aCoef = L[l].a.empty() ? nullptr : L[l].a.data();
+    for (int d = 0; d < 3; d++) op.bCoef[d] = d < op.grid.dim ? L[l].b[d].data() : nullptr;
+    return op;
+  }
+  void build(const double *phi) {
+    std::vector<Level> LL;
+    build_levels(LL, op0.grid, 2, (const double *)op0.aCoef, nullptr, op0.bCoef, o.max_coarse);
+    L.assign(LL.size(), AdjLevelO());
+    for (size_t l = 0; l < LL.size(); l++) {
+      L[l].g = LL[l].g;
+      L[l].a = LL[l].a;
+      for (int d = 0; d < 3; d++) L[l].b[d] = LL[l].b[d];
+      size_t n = 2 * ncells(L[l].g);
+      L[l].u.assign(n, 0);
+      L[l].J.assign(2 * n, 0);
+      L[l].y.assign(n, 0);
+      L[l].gg.assign(n, 0);
+      L[l].r.assign(n, 0);
+    }
+    std::copy(phi, phi + L[0].u.size(), L[0].u.begin());
+    for (size_t l = 1; l < L.size(); l++)
+      orc_restrict_average(&L[l - 1].g, 2, L[l].u.data(), L[l - 1].u.data());
+    for (auto &lv : L) orc_closure_jac(&lv.g, &op0.params, lv.u.data(), lv.J.data());
+  }
+  void smooth(int l, int n) {
+    mlgpu_nlop op = op_at(l);
+    AdjCtx X(op, L[l].u.data(), L[l].J.data());
+    Fab y;
+    y.define(op.grid, 2);
+    y.load(L[l].y.data());
+    for (int s = 0; s < n; s++) {
+      adj_gsrb_pass_fab(y, X, L[l].gg.data(), 0);
+      adj_gsrb_pass_fab(y, X, L[l].gg.data(), 1);
+    }
+    y.store(L[l].y.data());
+  }
+  void cycle(int l) {
+    const int last = (int)L.size() - 1;
+    if (l > 0) std::fill(L[l].y.begin(), L[l].y.end(), 0.0);
+    if (l == last) {
+      smooth(l, o.bottom_max_iter);
+      updates += (double)o.bottom_max_iter * ncells(L[l].g);
+      return;
+    }
+    smooth(l, o.num_smooth_down);
+    mlgpu_nlop op = op_at(l);
+    orc_hc_adjoint_restrict_impl(op, L[l].u.data(), L[l].J.data(), L[l].y.data(),
+                                 L[l].gg.data(), L[l + 1].gg.data());
+    for (int m = 0; m < o.num_mg; m++) cycle(l + 1);
+    mlgpu_bc ybc = op0.apply_derived_bc ? op0.derived_bc : op0.phi_bc;
+    orc_prolong_increment(&L[l].g, &ybc, 2, o.prolong, L[l].y.data(), L[l + 1].y.data());
+    smooth(l, o.num_smooth_up);
+    updates += (double)(o.num_smooth_down + o.num_smooth_up + 1) * ncells(L[l].g);
+  }
+  static void orc_hc_adjoint_restrict_impl(const mlgpu_nlop &op, const double *phi,
+                                           const double *J, const double *yd, const double *g,
+                                           double *gc) {
+    AdjCtx X(op, phi, J);
+    Fab y;
+    adj_load(y, op, yd);
+    mlgpu_grid cg = coarsen_grid(op.grid);
+    const double denom = op.grid.dim == 3 ? 8.0 : 4.0;
+    size_t nc = ncells(cg);
+    for (int K = 0; K < cg.n[2]; K++)
+      for (int J2 = 0; J2 < cg.n[1]; J2++)
+        for (int I = 0; I < cg.n[0]; I++) {
+          double acc[2] = {0.0, 0.0};
+          for (int kk = 0; kk < (op.grid.dim == 3 ? 2 : 1); kk++)
+            for (int jj = 0; jj < 2; jj++)
+              for (int ii = 0; ii < 2; ii++) {
+                int i = 2 * I + ii, j = 2 * J2 + jj, k = op.grid.dim == 3 ? 2 * K + kk : 0;
+                double o2[2];
+                adj_row(X, y, i, j, k, o2, nullptr);
+                size_t q = cidx(op.grid, i, j, k, 0);
+                for (int c = 0; c < 2; c++) acc[c] = acc[c] + (g[q + c * X.n] - o2[c]) / denom;
+              }
+          size_t Q = cidx(cg, I, J2, K, 0);
+          gc[Q] = acc[0];
+          gc[Q + nc] = acc[1];
+        }
+  }
+};
+
+}  // namespace
+
+extern "C" {
+
+int orc_hc_adjoint_apply(const mlgpu_nlop *op, const double *phi, const double *J,
+                         const double *yd, const double *g, double *out) {
+  AdjCtx X(*op, phi, J);
+  Fab y;
+  adj_load(y, *op, yd);
+  const mlgpu_grid &gr = op->grid;
+  for (int k = 0; k < gr.n[2]; k++)
+    for (int j = 0; j < gr.n[1]; j++)
+      for (int i = 0; i < gr.n[0]; i++) {
+        double o2[2];
+        adj_row(X, y, i, j, k, o2, nullptr);
+        size_t q = cidx(gr, i, j, k, 0);
+        for (int c = 0; c < 2; c++) out[q + c * X.n] = g ? g[q + c * X.n] - o2[c] : o2[c];
+      }
+  return 0;
+}
+
+int orc_hc_adjoint_gsrb_pass(const mlgpu_nlop *op, const double *phi, const double *J,
+                             double *yd, const double *g, int pass) {
+  AdjCtx X(*op, phi, J);
+  Fab y;
+  y.define(op->grid, 2);
+  y.load(yd);
+  adj_gsrb_pass_fab(y, X, g, pass);
+  y.store(yd);
+  return 0;
+}
+
+int orc_hc_adjoint_restrict(const mlgpu_nlop *op, const double *phi, const double *J,
+                            const double *y, const double *g, double *gc) {
+  AdjSolver::orc_hc_adjoint_restrict_impl(*op, phi, J, y, g, gc);
+  return 0;
+}
+
+int orc_hc_linearized_apply(const mlgpu_nlop *op, const double *phi, const double *J,
+                            const double *x, double *out) {
+  AdjCtx X(*op, phi, J);
+  lin_apply(X, x, out);
+  return 0;
+}
+
+int orc_hc_adjoint_solve(const mlgpu_nlop *op, const mlgpu_mg_options *o, const double *phi,
+                         const double *g, double *y, mlgpu_solve_stats *st) {
+  AdjSolver S;
+  S.op0 = *op;
+  S.o = *o;
+  S.build(phi);
+  memset(st, 0, sizeof(*st));
+  st->levels = (int)S.L.size();
+  size_t n = 2 * ncells(op->grid);
+  std::copy(y, y + n, S.L[0].y.begin());
+  std::copy(g, g + n, S.L[0].gg.begin());
+  mlgpu_nlop op0 = S.op_at(0);
+  auto resnorm = [&]() {
+    orc_hc_adjoint_apply(&op0, S.L[0].u.data(), S.L[0].J.data(), S.L[0].y.data(),
+                         S.L[0].gg.data(), S.L[0].r.data());
+    S.updates += ncells(op->grid);
+    return norm_of(S.L[0].r.data(), n, o->norm_type);
+  };
+  int cycles = 0;
+  auto iterate = [&]() {
+    S.cycle(0);
+    cycles++;
+  };
+  int rc = outer_loop(*o, st, resnorm, iterate);
+  st->cycles = cycles;
+  st->cell_updates = S.updates;
+  std::copy(S.L[0].y.begin(), S.L[0].y.end(), y);
+  return rc;
+}
+
+// -y^T dN/dv for the wall values, grad[(d * 2 + side) * 2 + c]
+int orc_hc_adjoint_bc_gradient(const mlgpu_nlop *op, const double *phi, const double *J,
+                               const double *y, double *grad) {
+  AdjCtx X(*op, phi, J);
+  const mlgpu_grid &g = op->grid;
+  for (int q = 0; q < 12; q++) grad[q] = 0.0;
+  const mlgpu_bc &bc = op->apply_derived_bc ? op->derived_bc : op->phi_bc;
+  for (int d = 0; d < g.dim; d++) {
+    if (g.periodic[d]) continue;
+    for (int side = 0; side < 2; side++) {
+      int lo[3] = {0, 0, 0}, hi[3] = {g.n[0] - 1, g.n[1] - 1, g.n[2] - 1};
+      lo[d] = hi[d] = side == 0 ? 0 : g.n[d] - 1;
+      double acc[2] = {0.0, 0.0};
+      for (int k = lo[2]; k <= hi[2]; k++)
+        for (int j = lo[1]; j <= hi[1]; j++)
+          for (int i = lo[0]; i <= hi[0]; i++) {
+            size_t q = cidx(g, i, j, k, 0);
+            int fi[3] = {i, j, k};
+            if (side) fi[d] += 1;
+            double yb0 = y[q] * X.B(d, fi[0], fi[1], fi[2], 0);
+            double yb1 = y[q + X.n] * X.B(d, fi[0], fi[1], fi[2], 1);
+            if (op->apply_derived_bc) {
+              acc[0] += yb0;
+              acc[1] += yb1;
+            } else {
+              double Jg[4];
+              ghost_jac(X, q, d, side, Jg);
+              acc[0] += yb0 * Jg[0] + yb1 * Jg[2];
+              acc[1] += yb0 * Jg[1] + yb1 * Jg[3];
+            }
+          }
+      for (int c = 0; c < 2; c++) {
+        double df = bc.type[d][side][c] == MLGPU_BC_DIRICHLET ? 2.0 : (side ? 1.0 : -1.0) * g.dx;
+        grad[(d * 2 + side) * 2 + c] = op->beta * X.dxinv * df * acc[c];
+      }
+    }
+  }
+  return 0;
+}
+
+// adjoint of orc_hc_backward_euler: A^T mu = phi_new_bar (alpha 1, beta -dt),
+// phi_old_bar = a mu, src_bar = dt mu, bc gradient of -mu^T N
+int orc_hc_backward_euler_adjoint(const mlgpu_nlop *op, const mlgpu_mg_options *o,
+                                  const double *phi_new, const double *phi_new_bar,
+                                  const double *a, double dt, double *mu, double *phi_old_bar,
+                                  double *src_bar, double *bc_grad, mlgpu_solve_stats *st) {
+  mlgpu_nlop be = *op;
+  be.alpha = 1.0;
+  be.beta = -dt;
+  int rc = orc_hc_adjoint_solve(&be, o, phi_new, phi_new_bar, mu, st);
+  size_t n = 2 * ncells(op->grid);
+  for (size_t q = 0; q < n; q++) {
+    if (phi_old_bar) phi_old_bar[q] = a ? a[q] * mu[q] : mu[q];
+    if (src_bar) src_bar[q] = dt * mu[q];
+  }
+  if (bc_grad) {
+    std::vector<double> J(2 * n);
+    orc_closure_jac(&op->grid, &op->params, phi_new, J.data());
+    orc_hc_adjoint_bc_gradient(&be, phi_new, J.data(), mu, bc_grad);
+  }
+  return rc;
+}
+
+// adjoint of orc_mac_project: D Pi G q = G^T (Pi ubar), ustar_bar = ubar - D^T q,
+// pi_bar = -ustar_bar (G p)
+int orc_mac_project_adjoint(const mlgpu_vcop *op, const mlgpu_mg_options *o,
+                            const mlgpu_bc *phi_bc, const double *ubar[3], const double *pi[3],
+                            const double *p, double *ustar_bar[3], double *pi_bar[3], double *q,
+                            mlgpu_solve_stats *st) {
+  const mlgpu_grid &g = op->grid;
+  const size_t n = ncells(g);
+  std::vector<double> r(n);
+  const double one_on_dx = 1.0 / g.dx;
+  for (int k = 0; k < g.n[2]; k++)
+    for (int j = 0; j < g.n[1]; j++)
+      for (int i = 0; i < g.n[0]; i++) {
+        const int at[3] = {i, j, k};
+        double v = 0.0;
+        for (int d = 0; d < g.dim; d++) {
+          const int m = g.n[d], a = at[d];
+          int f[3] = {i, j, k};
+          size_t flo = fidx(g, d, f[0], f[1], f[2], 0);
+          f[d] += 1;
+          size_t fhi = fidx(g, d, f[0], f[1], f[2], 0);
+          auto yv = [&](size_t ff) { return pi && pi[d] ? ubar[d][ff] * pi[d][ff] : ubar[d][ff]; };
+          double clo = 1.0, chi = -1.0;
+          if (!g.periodic[d]) {
+            if (a == 0) clo = phi_bc->type[d][0][0] == MLGPU_BC_DIRICHLET ? 2.0 : 0.0;
+            if (a == m - 1) chi = phi_bc->type[d][1][0] == MLGPU_BC_DIRICHLET ? -2.0 : 0.0;
+          }
+          double t = clo * yv(flo) + chi * yv(fhi);
+          if (g.periodic[d]) {
+            if (a == 0) {
+              f[d] = m;
+              t = t + yv(fidx(g, d, f[0], f[1], f[2], 0));
+            }
+            if (a == m - 1) {
+              f[d] = 0;
+              t = t - yv(fidx(g, d, f[0], f[1], f[2], 0));
+            }
+          }
+          v = v + t / g.dx;
+        }
+        r[cidx(g, i, j, k, 0)] = v;
+      }
+  int rc = orc_vc_solve(op, o, q, r.data(), st);
+  for (int d = 0; d < g.dim; d++) {
+    int m[3];
+    for (int e = 0; e < 3; e++) m[e] = g.n[e] + (e == d);
+    for (int k = 0; k < m[2]; k++)
+      for (int j = 0; j < m[1]; j++)
+        for (int i = 0; i < m[0]; i++) {
+          int f[3] = {i, j, k};
+          const int b = f[d];
+          double dt = 0.0;
+          if (b >= 1) {
+            int c[3] = {i, j, k};
+            c[d] = b - 1;
+            dt = dt + one_on_dx * q[cidx(g, c[0], c[1], c[2], 0)];
+          }
+          if (b <= g.n[d] - 1) dt = dt - one_on_dx * q[cidx(g, i, j, k, 0)];
+          size_t ff = fidx(g, d, i, j, k, 0);
+          ustar_bar[d][ff] = ubar[d][ff] - dt;
+        }
+  }
+  if (pi_bar) {
+    Fab ph(g, 1);
+    ph.load(p);
+    fill_ghosts(ph, g, *phi_bc, false);
+    for (int d = 0; d < g.dim; d++) {
+      if (!pi_bar[d]) continue;
+      int m[3];
+      for (int e = 0; e < 3; e++) m[e] = g.n[e] + (e == d);
+      for (int k = 0; k < m[2]; k++)
+        for (int j = 0; j < m[1]; j++)
+          for (int i = 0; i < m[0]; i++) {
+            int ii = i - (d == 0), jj = j - (d == 1), kk = k - (d == 2);
+            size_t ff = fidx(g, d, i, j, k, 0);
+            double grad = (ph(i, j, k, 0) - ph(ii, jj, kk, 0)) / g.dx;
+            pi_bar[d][ff] = -(ustar_bar[d][ff] * grad);
+          }
+    }
+  }
+  return rc;
+}
+
+}  // extern "C"

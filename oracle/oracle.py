@@ -54,6 +54,17 @@ def lib():
             "orc_mg_default_options": (None, [P(abi.MGOptions), i]),
             "orc_mg_depth": (i, [P(abi.Grid), i]),
             "orc_pd_temperature": (d, [d, d, P(abi.Params)]),
+            "orc_hc_adjoint_apply": (i, [P(abi.NLOp), vp, vp, vp, vp, vp]),
+            "orc_hc_adjoint_gsrb_pass": (i, [P(abi.NLOp), vp, vp, vp, vp, i]),
+            "orc_hc_adjoint_restrict": (i, [P(abi.NLOp), vp, vp, vp, vp, vp]),
+            "orc_hc_linearized_apply": (i, [P(abi.NLOp), vp, vp, vp, vp]),
+            "orc_hc_adjoint_solve": (i, [P(abi.NLOp), P(abi.MGOptions), vp, vp, vp,
+                                         P(abi.SolveStats)]),
+            "orc_hc_adjoint_bc_gradient": (i, [P(abi.NLOp), vp, vp, vp, vp]),
+            "orc_hc_backward_euler_adjoint": (i, [P(abi.NLOp), P(abi.MGOptions), vp, vp, vp, d,
+                                                  vp, vp, vp, vp, P(abi.SolveStats)]),
+            "orc_mac_project_adjoint": (i, [P(abi.VCOp), P(abi.MGOptions), P(abi.BC), vp * 3,
+                                            vp * 3, vp, vp * 3, vp * 3, vp, P(abi.SolveStats)]),
             "orc_hc_solve": (i, [P(abi.NLOp), P(abi.MGOptions), vp, vp, P(abi.SolveStats)]),
             "orc_vc_solve": (i, [P(abi.VCOp), P(abi.MGOptions), vp, vp, P(abi.SolveStats)]),
             "orc_mac_project": (i, [P(abi.VCOp), P(abi.MGOptions), P(abi.BC), vp * 3, vp * 3,
@@ -317,3 +328,66 @@ def hc_backward_euler(o, opts, phi_new, phi_old, dt, src=None, a=None):
     rc = lib().orc_hc_backward_euler(C.byref(o.op), C.byref(opts), _p(phi_new), _p(phi_old),
                                      _p(src), _p(a), float(dt), C.byref(st))
     return phi_new, st, rc
+
+
+# ------------------------------------------------------------------ adjoint
+def adjoint_apply(o, phi, J, y, g=None):
+    """A^T y (g None) or g - A^T y, A = dN/dphi at phi (J = closure_jac(phi))."""
+    out = np.empty_like(y)
+    lib().orc_hc_adjoint_apply(C.byref(o.op), _p(phi), _p(J), _p(y), _p(g), _p(out))
+    return out
+
+
+def adjoint_gsrb_pass(o, phi, J, y, g, pass_):
+    y = y.copy()
+    lib().orc_hc_adjoint_gsrb_pass(C.byref(o.op), _p(phi), _p(J), _p(y), _p(g), int(pass_))
+    return y
+
+
+def adjoint_restrict(o, phi, J, y, g):
+    gc = np.zeros(coarse_shape(o.g, 2))
+    lib().orc_hc_adjoint_restrict(C.byref(o.op), _p(phi), _p(J), _p(y), _p(g), _p(gc))
+    return gc
+
+
+def linearized_apply(o, phi, J, x):
+    """A x, the Jacobian of the nonlinear operator at phi applied to x."""
+    out = np.empty_like(x)
+    lib().orc_hc_linearized_apply(C.byref(o.op), _p(phi), _p(J), _p(x), _p(out))
+    return out
+
+
+def adjoint_solve(o, opts, phi, g, y=None):
+    y = np.zeros_like(g) if y is None else y.copy()
+    st = abi.SolveStats()
+    rc = lib().orc_hc_adjoint_solve(C.byref(o.op), C.byref(opts), _p(phi), _p(g), _p(y),
+                                    C.byref(st))
+    return y, st, rc
+
+
+def adjoint_bc_gradient(o, phi, J, y):
+    out = np.zeros(12)
+    lib().orc_hc_adjoint_bc_gradient(C.byref(o.op), _p(phi), _p(J), _p(y), _p(out))
+    return out
+
+
+def backward_euler_adjoint(o, opts, phi_new, phi_new_bar, dt, a=None, mu=None):
+    mu = np.zeros_like(phi_new) if mu is None else mu.copy()
+    old_bar, src_bar, bcg = np.empty_like(phi_new), np.empty_like(phi_new), np.zeros(12)
+    st = abi.SolveStats()
+    rc = lib().orc_hc_backward_euler_adjoint(C.byref(o.op), C.byref(opts), _p(phi_new),
+                                             _p(phi_new_bar), _p(a), float(dt), _p(mu),
+                                             _p(old_bar), _p(src_bar), _p(bcg), C.byref(st))
+    return old_bar, src_bar, bcg, mu, st, rc
+
+
+def mac_project_adjoint(o, opts, phi_bc, ubar, pi, p, q=None):
+    g = o.g
+    q = np.zeros(abi.cell_shape(g)) if q is None else q.copy()
+    usb = [np.empty_like(ubar[d]) for d in range(g.dim)]
+    pib = [np.empty_like(ubar[d]) for d in range(g.dim)]
+    st = abi.SolveStats()
+    rc = lib().orc_mac_project_adjoint(C.byref(o.op), C.byref(opts), C.byref(phi_bc),
+                                       _faces3(ubar), _faces3(pi) if pi is not None else None,
+                                       _p(p), _faces3(usb), _faces3(pib), _p(q), C.byref(st))
+    return usb, pib, q, st, rc
