@@ -361,6 +361,10 @@ int mlgpu_solver_solve(mlgpu_solver *s, double *phi, const double *rhs,
 /* Re-read alpha/beta (setAlphaAndBeta) and rebuild coarse coefficients. */
 int mlgpu_solver_set_alpha_beta(mlgpu_solver *s, double alpha, double beta);
 int mlgpu_solver_destroy(mlgpu_solver *s);
+/* Replace the wall conditions of an (H, C) solver or adjoint solver
+ * (either pointer may be NULL to keep that one); MLGPU_ERR_ARG if the new
+ * set is not allowed for the solver. */
+int mlgpu_hc_solver_set_bcs(mlgpu_solver *s, const mlgpu_bc *phi_bc, const mlgpu_bc *derived_bc);
 
 /* MAC projection of a face velocity, the sequence of
  * Projector::levelMacProject (srcSubcycle/Projector.cpp:858-982):
@@ -397,6 +401,9 @@ int mlgpu_hc_backward_euler(mlgpu_solver *S, double *phi_new, const double *phi_
 /* J of every cell: [4][cells] = dT/dH, dT/dC, dC_l/dH, dC_l/dC. */
 int mlgpu_closure_jacobian(const mlgpu_grid *g, const mlgpu_params *p, const double *HC,
                            double *J, void *stream);
+/* d porosity / d(H, C) of every cell: [2][cells] (porosity of mlgpu_closure). */
+int mlgpu_porosity_jacobian(const mlgpu_grid *g, const mlgpu_params *p, const double *HC,
+                            double *dpor, void *stream);
 /* out = A^T y (g NULL) or g - A^T y, A at state phi whose Jacobian is J
  * (mlgpu_closure_jacobian of phi); op FP64. */
 int mlgpu_hc_adjoint_apply(const mlgpu_nlop *op, const double *phi, const double *J,

@@ -200,6 +200,19 @@ __global__ void __launch_bounds__(kBlock) adj_jac_kernel(Geom G, ClosureParams c
   }
 }
 
+// {d por/dH, d por/dC} of every cell
+__global__ void __launch_bounds__(kBlock) porosity_jac_kernel(Geom G, ClosureParams cp,
+                                                              const double *__restrict__ u,
+                                                              double *__restrict__ dp) {
+  const long long n = G.ncell;
+  for (long long q = gtid(); q < n; q += gstride()) {
+    double d2[2];
+    porosity_jac(u[q], u[q + n], cp, d2);
+    dp[q] = d2[0];
+    dp[q + n] = d2[1];
+  }
+}
+
 // out = A^T y (ADJ_APPLY) or g - A^T y with a fused norm (ADJ_RESIDUAL)
 template <class T, int DIM, int MODE, int NORM>
 __global__ void __launch_bounds__(kBlock) adj_op_kernel(AdjArgs<T> A, const T *__restrict__ y,

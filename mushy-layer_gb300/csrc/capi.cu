@@ -204,6 +204,13 @@ int mlgpu_closure_jacobian(const mlgpu_grid *g, const mlgpu_params *p, const dou
   return status_of(launch_adj_jac(make_geom(*g), make_cp(*p), HC, J, (cudaStream_t)stream));
 }
 
+int mlgpu_porosity_jacobian(const mlgpu_grid *g, const mlgpu_params *p, const double *HC,
+                            double *dpor, void *stream) {
+  if (!valid_grid(g) || !p || !HC || !dpor) return MLGPU_ERR_ARG;
+  return status_of(
+      launch_porosity_jac(make_geom(*g), make_cp(*p), HC, dpor, (cudaStream_t)stream));
+}
+
 int mlgpu_hc_adjoint_apply(const mlgpu_nlop *op, const double *phi, const double *J,
                            const double *y, const double *g, double *out, void *stream) {
   if (!valid_adjoint_op(op) || !phi || !J || !y || !out) return MLGPU_ERR_ARG;

@@ -52,6 +52,8 @@ cudaError_t launch_be_adj(long long n, const double *mu, const double *a, double
                           double *old_bar, double *src_bar, cudaStream_t s);
 cudaError_t launch_adj_jac(const Geom &G, const ClosureParams &cp, const double *u, double *J,
                            cudaStream_t s);
+cudaError_t launch_porosity_jac(const Geom &G, const ClosureParams &cp, const double *u,
+                                double *dp, cudaStream_t s);
 cudaError_t launch_adj_op(const AdjArgs<double> &A, int mode, int norm, const double *y,
                           const double *g, double *out, double *part, cudaStream_t s);
 cudaError_t launch_adj_gsrb(const AdjArgs<double> &A, double *y, const double *g, int pass,

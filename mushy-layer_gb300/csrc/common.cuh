@@ -195,6 +195,35 @@ __device__ __forceinline__ void t_cl_jac(double H, double C, const ClosureParams
   }
 }
 
+// Derivative of the porosity of the full closure (CALCULATEPOROSITY,
+// src/EnthalpyVariablesF.ChF): {d por/dH, d por/dC} -- zero in the solid and
+// the liquid, 1/(St + te (1 - cp)) in H on the eutectic, the porosity root
+// differentiated implicitly in the mush (C clamped at -CR as
+// CALCULATEPOROSITYMUSH does).  No counterpart in the reference.
+__device__ __forceinline__ void porosity_jac(double H, double C, const ClosureParams &p,
+                                             double dp[2]) {
+  double Hs, He, Hl;
+  bounding_energy(C, p, Hs, He, Hl);
+  dp[0] = dp[1] = 0.0;
+  if (H <= Hs) {
+  } else if (H > Hs && H <= He) {
+    dp[0] = 1.0 / (p.St + p.te * (1 - p.cp));
+  } else if (H > He && H < Hl) {
+    if (p.St != 0) {
+      const bool clamp = !(C >= -p.CR);
+      const double validC = clamp ? -p.CR : C;
+      const double a = p.CR * (p.cp - 1) + p.St * (p.k - 1);
+      const double b = p.CR * (1 - 2 * p.cp) + H * (1 - p.k) - validC * (p.cp - 1) - p.k * p.St;
+      const double c = (p.CR + validC) * p.cp + p.k * H;
+      const double sD = sqrt(b * b - 4 * a * c);
+      const double dbH = 1 - p.k, dbC = clamp ? 0.0 : -(p.cp - 1);
+      const double dcH = p.k, dcC = clamp ? 0.0 : p.cp;
+      dp[0] = (-dbH - (b * dbH - 2 * a * dcH) / sD) / (2 * a);
+      dp[1] = (-dbC - (b * dbC - 2 * a * dcC) / sD) / (2 * a);
+    }
+  }
+}
+
 // ------------------------------------------- nonlinear temperature conditions
 // computeTemperature of the scalar phase diagram (src/phaseDiagram.cpp:225-258
 // with computeBoundingEnergy :326-341 and computePorosityMushyLayer :298-324),

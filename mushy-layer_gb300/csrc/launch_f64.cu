@@ -212,6 +212,11 @@ cudaError_t launch_adj_jac(const Geom &G, const ClosureParams &cp, const double 
   adj_jac_kernel<double><<<blocks_for(G.ncell), kBlock, 0, s>>>(G, cp, u, J);
   return cudaGetLastError();
 }
+cudaError_t launch_porosity_jac(const Geom &G, const ClosureParams &cp, const double *u,
+                                double *dp, cudaStream_t s) {
+  porosity_jac_kernel<<<blocks_for(G.ncell), kBlock, 0, s>>>(G, cp, u, dp);
+  return cudaGetLastError();
+}
 cudaError_t launch_adj_op(const AdjArgs<double> &A, int mode, int norm, const double *y,
                           const double *g, double *out, double *part, cudaStream_t s) {
   const int nb = blocks_for(A.G.ncell);

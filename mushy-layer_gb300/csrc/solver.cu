@@ -1129,6 +1129,21 @@ class HCSolver : public mlgpu_solver {
     return outer_finish(o, S, st);
   }
 
+  // new wall conditions: kernel arguments only (1/diag does not see them)
+  int set_bcs(const mlgpu_bc *phi_bc, const mlgpu_bc *derived_bc) {
+    mlgpu_nlop t = op;
+    if (phi_bc) t.phi_bc = *phi_bc;
+    if (derived_bc) t.derived_bc = *derived_bc;
+    if (!valid_nl_bcs(t)) return MLGPU_ERR_ARG;
+    op = t;
+    for (auto *gp : {&graph, &graph_m})
+      if (*gp) {
+        cudaGraphExecDestroy(*gp);
+        *gp = nullptr;
+      }
+    return MLGPU_OK;
+  }
+
   int set_alpha_beta(double a, double b) override {
     op.alpha = a;
     op.beta = b;
@@ -1372,6 +1387,15 @@ class HCAdjSolver : public mlgpu_solver {
     }
     return MLGPU_OK;
   }
+
+  int set_bcs(const mlgpu_bc *phi_bc, const mlgpu_bc *derived_bc) {
+    mlgpu_nlop t = op;
+    if (phi_bc) t.phi_bc = *phi_bc;
+    if (derived_bc) t.derived_bc = *derived_bc;
+    if (!valid_adjoint_op(&t)) return MLGPU_ERR_ARG;
+    op = t;
+    return set_alpha_beta(op.alpha, op.beta);
+  }
 };
 
 bool valid_options(const mlgpu_mg_options *o) {
@@ -1526,6 +1550,12 @@ int mlgpu_solver_solve(mlgpu_solver *s, double *phi, const double *rhs, mlgpu_so
 int mlgpu_solver_set_alpha_beta(mlgpu_solver *s, double a, double b) {
   if (!s) return MLGPU_ERR_ARG;
   return s->set_alpha_beta(a, b);
+}
+
+int mlgpu_hc_solver_set_bcs(mlgpu_solver *S, const mlgpu_bc *phi_bc, const mlgpu_bc *derived_bc) {
+  if (HCSolver *H = dynamic_cast<HCSolver *>(S)) return H->set_bcs(phi_bc, derived_bc);
+  if (HCAdjSolver *A = dynamic_cast<HCAdjSolver *>(S)) return A->set_bcs(phi_bc, derived_bc);
+  return MLGPU_ERR_ARG;
 }
 
 int mlgpu_mac_project(mlgpu_solver *S, const mlgpu_grid *grid, const mlgpu_bc *phi_bc,

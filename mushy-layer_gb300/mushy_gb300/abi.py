@@ -204,6 +204,8 @@ def _declare(lib):
         "mlgpu_mac_project": (i, [vp, P(Grid), P(BC), vp * 3, vp * 3, vp, vp, P(SolveStats)]),
         "mlgpu_hc_backward_euler": (i, [vp, vp, vp, vp, vp, d, vp, P(SolveStats)]),
         "mlgpu_closure_jacobian": (i, [P(Grid), P(Params), vp, vp, vp]),
+        "mlgpu_hc_solver_set_bcs": (i, [vp, P(BC), P(BC)]),
+        "mlgpu_porosity_jacobian": (i, [P(Grid), P(Params), vp, vp, vp]),
         "mlgpu_hc_adjoint_apply": (i, [P(NLOp), vp, vp, vp, vp, vp, vp]),
         "mlgpu_hc_adjoint_gsrb_pass": (i, [P(NLOp), vp, vp, vp, vp, i, vp]),
         "mlgpu_hc_adjoint_restrict": (i, [P(NLOp), vp, vp, vp, vp, vp, vp]),

@@ -1,0 +1,156 @@
+"""torch.autograd bindings of the discrete adjoint in libmlgpu.
+
+Each Function runs the path's forward on the GPU and, in backward, its
+hand-written adjoint kernels:
+
+* ``Closure``            (H, C) -> (T, C_l, porosity); backward through the
+                         closure Jacobian and the porosity derivative.
+* ``BackwardEulerStep``  phi_new = BE step of phi_old with source and one
+                         wall temperature; backward = one transposed-Jacobian
+                         multigrid solve (mlgpu_hc_backward_euler_adjoint).
+* ``MacProject``         u = u* - Pi G p; backward = the projection's adjoint
+                         solve (mlgpu_mac_project_adjoint), giving u*-bar and
+                         Pi-bar.
+
+``checkpointed(steps, ...)`` runs a time loop keeping only every k-th state
+and recomputes a segment during the backward sweep (two-level checkpointing;
+the recomputation is bitwise deterministic).
+"""
+import torch
+import torch.utils.checkpoint as tcp
+
+from . import abi, ops
+
+
+class Closure(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, HC, grid, params):
+        full = ops.closureFull(grid, params, HC.contiguous())
+        ctx.save_for_backward(HC)
+        ctx.grid, ctx.params = grid, params
+        return full["T"], full["Cl"], full["porosity"]
+
+    @staticmethod
+    def backward(ctx, gT, gCl, gpor):
+        (HC,) = ctx.saved_tensors
+        J = ops.closureJacobian(ctx.grid, ctx.params, HC.contiguous())
+        dp = ops.porosityJacobian(ctx.grid, ctx.params, HC.contiguous())
+        z = torch.zeros_like(HC[0])
+        gT = z if gT is None else gT
+        gCl = z if gCl is None else gCl
+        gpor = z if gpor is None else gpor
+        gH = J[0] * gT + J[2] * gCl + dp[0] * gpor
+        gC = J[1] * gT + J[3] * gCl + dp[1] * gpor
+        return torch.stack([gH, gC]), None, None
+
+
+class BEStepper:
+    """The solvers of one backward-Euler (H, C) step whose derived-variable
+    wall value at `wall` = (dir, side, comp) is a differentiable input."""
+
+    def __init__(self, op, opts, adj_opts, wall=(1, 0, 0)):
+        self.op, self.wall = op, wall
+        self.S = ops.AMRFASMultiGrid(op, opts)
+        self.A = ops.AdjointMultiGrid(op, adj_opts)
+        self._value = None
+
+    def set_wall(self, v):
+        v = float(v)
+        if v == self._value:
+            return
+        d, s, c = self.wall
+        bc = abi.BC()
+        bc.type, bc.value = self.op.derived_bc.type, self.op.derived_bc.value
+        bc.value[d][s][c] = v
+        self.op.derived_bc = bc
+        self.S.setBCs(derived_bc=bc)
+        self.A.setBCs(derived_bc=bc)
+        self._value = v
+
+    def slot(self):
+        d, s, c = self.wall
+        return (d * 2 + s) * 2 + c
+
+
+class BackwardEulerStep(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, phi_old, src, wall_value, stepper, dt):
+        stepper.set_wall(wall_value.item())
+        phi_new = phi_old.detach().clone()
+        st, rc = stepper.S.backwardEuler(phi_new, phi_old.detach().contiguous(), dt,
+                                         src=src.detach().contiguous())
+        if rc not in (abi.OK, abi.ERR_HANG):
+            abi.check(rc, "BackwardEulerStep")
+        ctx.save_for_backward(phi_new, wall_value)
+        ctx.stepper, ctx.dt = stepper, dt
+        return phi_new
+
+    @staticmethod
+    def backward(ctx, g):
+        phi_new, wall_value = ctx.saved_tensors
+        stp = ctx.stepper
+        stp.set_wall(wall_value.item())
+        mu = torch.zeros_like(phi_new)
+        old_bar, src_bar, bcg, st, rc = stp.A.backwardEulerAdjoint(
+            phi_new, g.contiguous(), ctx.dt, mu)
+        if rc not in (abi.OK, abi.ERR_HANG):
+            abi.check(rc, "BackwardEulerStep.backward")
+        wbar = torch.tensor(bcg[stp.slot()], dtype=torch.float64, device=phi_new.device)
+        return old_bar, src_bar, wbar, None, None
+
+
+class Projector:
+    """A projection solver bound to one set of face permeabilities."""
+
+    def __init__(self, grid, pi_faces, opts, bc=None):
+        self.grid = grid
+        self.pi = [p.detach().contiguous() for p in pi_faces]
+        self.bc = bc if bc is not None else abi.make_bc()
+        self.op = ops.ProjectionOp(grid, self.bc, 0.0, 1.0, None, [-p for p in self.pi])
+        self.S = ops.AMRMultiGrid(self.op, opts)
+
+
+class MacProject(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, ux, uz, pi_x, pi_z, projector):
+        u = [ux.detach().clone().contiguous(), uz.detach().clone().contiguous()]
+        p = torch.zeros(abi.cell_shape(projector.grid), dtype=torch.float64, device=ux.device)
+        st, rc = projector.S.levelMacProject(u, projector.pi, p)
+        if rc not in (abi.OK, abi.ERR_HANG):
+            abi.check(rc, "MacProject")
+        ctx.save_for_backward(p)
+        ctx.projector = projector
+        return u[0], u[1]
+
+    @staticmethod
+    def backward(ctx, gx, gz):
+        (p,) = ctx.saved_tensors
+        P = ctx.projector
+        ub = [gx.contiguous() if gx is not None else torch.zeros_like(P.pi[0]),
+              gz.contiguous() if gz is not None else torch.zeros_like(P.pi[1])]
+        usb, pib, q, st, rc = ops.macProjectAdjoint(P.S, ub, P.pi, p, phi_bc=P.bc)
+        if rc not in (abi.OK, abi.ERR_HANG):
+            abi.check(rc, "MacProject.backward")
+        return usb[0], usb[1], pib[0], pib[1], None
+
+
+def checkpointed(step, state, nsteps, every, *params):
+    """state <- step(state, *params) nsteps times, storing the state only at
+    every `every`-th step: each segment is recomputed in the backward sweep."""
+
+    def segment(k):
+        def run(s, *pp):
+            for _ in range(k):
+                s = step(s, *pp)
+            return s
+        return run
+
+    done = 0
+    while done < nsteps:
+        k = min(every, nsteps - done)
+        if torch.is_grad_enabled():
+            state = tcp.checkpoint(segment(k), state, *params, use_reentrant=False)
+        else:
+            state = segment(k)(state, *params)
+        done += k
+    return state

@@ -290,6 +290,12 @@ class _Solver:
     def setAlphaAndBeta(self, a, b):
         abi.check(abi.load().mlgpu_solver_set_alpha_beta(self.h, a, b), "setAlphaAndBeta")
 
+    def setBCs(self, phi_bc=None, derived_bc=None):
+        """New wall conditions for an (H, C) or adjoint solver."""
+        abi.check(abi.load().mlgpu_hc_solver_set_bcs(
+            self.h, C.byref(phi_bc) if phi_bc is not None else None,
+            C.byref(derived_bc) if derived_bc is not None else None), "setBCs")
+
     def __del__(self):
         if getattr(self, "h", None):
             try:
@@ -357,6 +363,24 @@ def closureJacobian(grid, params, HC):
     abi.check(abi.load().mlgpu_closure_jacobian(C.byref(grid), C.byref(params), _ptr(HC),
                                                 _ptr(J), _stream()), "closureJacobian")
     return J
+
+
+def porosityJacobian(grid, params, HC):
+    """d porosity/d(H, C) of every cell: tensor [2][cells...]."""
+    dp = torch.empty_like(HC)
+    abi.check(abi.load().mlgpu_porosity_jacobian(C.byref(grid), C.byref(params), _ptr(HC),
+                                                 _ptr(dp), _stream()), "porosityJacobian")
+    return dp
+
+
+def closureFull(grid, params, HC):
+    """updateEnthalpyVariables: dict of T, porosity, Cl, Cs, Hs, He, Hl tensors."""
+    keys = ("T", "porosity", "Cl", "Cs", "Hs", "He", "Hl")
+    out = {k: torch.empty(tuple(HC.shape[1:]), dtype=torch.float64, device=HC.device)
+           for k in keys}
+    abi.check(abi.load().mlgpu_closure(C.byref(grid), C.byref(params), _ptr(HC),
+                                       *[_ptr(out[k]) for k in keys], _stream()), "closure")
+    return out
 
 
 def adjointApply(op, phi, J, y, g=None):

@@ -771,6 +771,39 @@ int orc_closure_tcl(const mlgpu_grid *g, const mlgpu_params *p, const double *HC
 }
 
 // J[4][cells] = d(T, C_l)/d(H, C) of every cell
+// d porosity/d(H, C) of the full closure (no counterpart in the reference):
+// eutectic 1/(St + te (1 - cp)) in H, the mush root differentiated
+// implicitly (C clamped at -CR), zero elsewhere
+int orc_porosity_jac(const mlgpu_grid *g, const mlgpu_params *p, const double *HC, double *dp) {
+  size_t n = ncells(*g);
+  const double CR = p->compositionRatio, k = p->waterDistributionCoeff,
+               cp = p->specificHeatRatio, St = p->stefan, te = p->thetaEutectic;
+  for (size_t q = 0; q < n; q++) {
+    double H = HC[q], C = HC[q + n], Hs, He, Hl;
+    bounding_energy(C, *p, Hs, He, Hl);
+    double d0 = 0.0, d1 = 0.0;
+    if (H <= Hs) {
+    } else if (H > Hs && H <= He) {
+      d0 = 1.0 / (St + te * (1 - cp));
+    } else if (H > He && H < Hl) {
+      if (St != 0) {
+        const bool clamp = !(C >= -CR);
+        const double vC = clamp ? -CR : C;
+        const double a = CR * (cp - 1) + St * (k - 1);
+        const double b = CR * (1 - 2 * cp) + H * (1 - k) - vC * (cp - 1) - k * St;
+        const double c = (CR + vC) * cp + k * H;
+        const double sD = std::sqrt(b * b - 4 * a * c);
+        const double dbH = 1 - k, dbC = clamp ? 0.0 : -(cp - 1), dcH = k, dcC = clamp ? 0.0 : cp;
+        d0 = (-dbH - (b * dbH - 2 * a * dcH) / sD) / (2 * a);
+        d1 = (-dbC - (b * dbC - 2 * a * dcC) / sD) / (2 * a);
+      }
+    }
+    dp[q] = d0;
+    dp[q + n] = d1;
+  }
+  return 0;
+}
+
 int orc_closure_jac(const mlgpu_grid *g, const mlgpu_params *p, const double *HC, double *J) {
   size_t n = ncells(*g);
 #pragma omp parallel for schedule(static)

@@ -30,6 +30,7 @@ def lib():
             "orc_closure": (i, [P(abi.Grid), P(abi.Params)] + [vp] * 8),
             "orc_closure_tcl": (i, [P(abi.Grid), P(abi.Params), vp, vp]),
             "orc_closure_jac": (i, [P(abi.Grid), P(abi.Params), vp, vp]),
+            "orc_porosity_jac": (i, [P(abi.Grid), P(abi.Params), vp, vp]),
             "orc_nl_residual": (i, [P(abi.NLOp), vp, vp, vp]),
             "orc_nl_apply": (i, [P(abi.NLOp), vp, vp]),
             "orc_nl_gsrb_pass": (i, [P(abi.NLOp), vp, vp, i]),
@@ -106,6 +107,13 @@ def closure(g, p, HC):
 def closure_tcl(g, p, HC):
     out = np.zeros_like(HC)
     lib().orc_closure_tcl(C.byref(g), C.byref(p), _p(HC), _p(out))
+    return out
+
+
+def porosity_jac(g, p, HC):
+    """d porosity/d(H, C) per cell: [2][cells]."""
+    out = np.zeros_like(HC)
+    lib().orc_porosity_jac(C.byref(g), C.byref(p), _p(HC), _p(out))
     return out
 
 
