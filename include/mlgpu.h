@@ -412,6 +412,12 @@ int mlgpu_hc_adjoint_apply(const mlgpu_nlop *op, const double *phi, const double
  * each cell of the colour solves its own two rows exactly. */
 int mlgpu_hc_adjoint_gsrb_pass(const mlgpu_nlop *op, const double *phi, const double *J,
                                double *y, const double *g, int pass, void *stream);
+/* The untransposed operator: out = A x (r NULL) or r - A x, and one
+ * red/black block Gauss-Seidel pass on A x = r (Newton's linear solve). */
+int mlgpu_hc_linearized_apply(const mlgpu_nlop *op, const double *phi, const double *J,
+                              const double *x, const double *r, double *out, void *stream);
+int mlgpu_hc_linearized_gsrb_pass(const mlgpu_nlop *op, const double *phi, const double *J,
+                                  double *x, const double *r, int pass, void *stream);
 /* gc = 2^D average of g - A^T y on the grid coarsened by 2. */
 int mlgpu_hc_adjoint_restrict(const mlgpu_nlop *op, const double *phi, const double *J,
                               const double *y, const double *g, double *gc, void *stream);
@@ -430,6 +436,19 @@ int mlgpu_hc_adjoint_create(const mlgpu_nlop *op, const mlgpu_mg_options *o, voi
  * solution out. */
 int mlgpu_hc_adjoint_solve(mlgpu_solver *S, const double *phi, const double *g, double *y,
                            mlgpu_solve_stats *stats);
+/* The same object also solves N(phi) = rhs by Newton's method: each step
+ * solves A(phi) d = rhs - N(phi) with V-cycles on A (the untransposed
+ * operator, same hierarchy and block smoother) to 1e-3 relative, then
+ * phi += d, halving d (at most 4 times) while the FP64 residual grows; the
+ * options' tolerance / max_iter / hang apply to the FP64 residual.  phi:
+ * initial guess in, solution out.  No counterpart in the reference (whose
+ * FAS smoother ignores dT/dH and converges slowly through phase change). */
+int mlgpu_hc_newton_solve(mlgpu_solver *S, double *phi, const double *rhs,
+                          mlgpu_solve_stats *stats);
+/* mlgpu_hc_backward_euler with the Newton solve of `S` (an adjoint solver). */
+int mlgpu_hc_backward_euler_newton(mlgpu_solver *S, double *phi_new, const double *phi_old,
+                                   const double *src, const double *aCoef, double dt,
+                                   double *rhs_scratch, mlgpu_solve_stats *stats);
 /* grad[(d * 2 + side) * 2 + comp] = -y^T dN/dv for every boundary value v of
  * the condition N applies at the walls (derived_bc when apply_derived_bc,
  * else phi_bc), at the state of the last mlgpu_hc_adjoint_solve; 0 on

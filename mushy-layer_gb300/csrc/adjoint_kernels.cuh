@@ -170,12 +170,107 @@ __device__ __forceinline__ void adj_cell(const AdjArgs<T> &A, const T *y, int i,
   }
 }
 
-// y_j += M^-1 (g_j - (A^T y)_j): the exact solve of cell j's two rows
-template <class T, int DIM>
+// (A x) at interior cell (i,j,k), the linearised operator itself, with its
+// 2x2 diagonal block D[2c + c'] = d(A x)_c / d x_c' if asked:
+//   (A x)_c = alpha a_c x_c - beta dxinv sum_f b_f,c (g_nb,c - g_c),  g = J x,
+// ghosts of g: periodic neighbour, derived-rule ghost of the centre's g, or
+// J_g S x under the (H, C) condition;
+//   D(c, c') = delta alpha a_c + beta dxinv (P_c J(c, c') - Y(c, c')),
+//   Y(c, c') = sum over (H, C)-condition faces of b_f,c J_g(c, c') s_c'.
+// It is D^T of adj_cell's M, and the row order of the forward operator's sum.
+template <class T, int DIM, bool WANT_M>
+__device__ __forceinline__ void lin_cell(const AdjArgs<T> &A, const T *x, int i, int j, int k,
+                                         T out[2], T x0[2], T M[4]) {
+  const Geom &G = A.G;
+  const long long q = G.cell(i, j, k), n = G.ncell;
+  x0[0] = x[q];
+  x0[1] = x[q + n];
+  T g0[2];
+#pragma unroll
+  for (int c = 0; c < 2; c++) g0[c] = A.J[(2 * c) * n + q] * x0[0] + A.J[(2 * c + 1) * n + q] * x0[1];
+  T P[2], Y[4] = {T(0), T(0), T(0), T(0)};
+#pragma unroll
+  for (int c = 0; c < 2; c++) {
+    T s = T(0), p = T(0);
+#pragma unroll
+    for (int d = 0; d < DIM; d++) {
+      const int idx[3] = {i, j, k};
+      const int m = G.n(d);
+      const long long nf = G.nface(d);
+#pragma unroll
+      for (int side = 1; side >= 0; side--) {
+        int nb[3] = {idx[0], idx[1], idx[2]};
+        nb[d] += side ? 1 : -1;
+        int fi[3] = {idx[0], idx[1], idx[2]};
+        if (side) fi[d] += 1;
+        const T bf = A.b[d][c * nf + G.face(d, fi[0], fi[1], fi[2])];
+        T gn, dp;
+        bool self = false;
+        if (nb[d] >= 0 && nb[d] < m) {
+          const long long qn = G.cell(nb[0], nb[1], nb[2]);
+          gn = A.J[(2 * c) * n + qn] * x[qn] + A.J[(2 * c + 1) * n + qn] * x[qn + n];
+          dp = bf;
+        } else if (G.per(d)) {
+          nb[d] = nb[d] < 0 ? m - 1 : 0;
+          const long long qn = G.cell(nb[0], nb[1], nb[2]);
+          gn = A.J[(2 * c) * n + qn] * x[qn] + A.J[(2 * c + 1) * n + qn] * x[qn + n];
+          self = qn == q;
+          dp = self ? T(0) : bf;
+        } else if (A.apply_dbc) {
+          gn = ghost_value<T>(A.dbc, d, side, c, g0[c], A.dx, true);
+          dp = A.dbc.type[d][side][c] == MLGPU_BC_DIRICHLET ? T(2) * bf : T(0);
+        } else {
+          double Jg[4];
+          adj_ghost_jac(A, q, d, side, Jg);
+          const T s0 = A.phi_bc.type[d][side][0] == MLGPU_BC_DIRICHLET ? T(-1) : T(1);
+          const T s1 = A.phi_bc.type[d][side][1] == MLGPU_BC_DIRICHLET ? T(-1) : T(1);
+          const T e0 = s0 * x0[0], e1 = s1 * x0[1];
+          gn = (T)Jg[2 * c] * e0 + (T)Jg[2 * c + 1] * e1;
+          dp = bf;
+          if (WANT_M) {
+            Y[2 * c + 0] = Y[2 * c + 0] + bf * ((T)Jg[2 * c] * s0);
+            Y[2 * c + 1] = Y[2 * c + 1] + bf * ((T)Jg[2 * c + 1] * s1);
+          }
+        }
+        (void)self;
+        const T t = side ? bf * (gn - g0[c]) : bf * (g0[c] - gn);
+        if (side)
+          s = (d == 0) ? t : s + t;
+        else
+          s = s - t;
+        if (WANT_M) p = p + dp;
+      }
+    }
+    P[c] = p;
+    const T av = A.a ? A.a[q + c * n] : T(1);
+    out[c] = A.alpha * av * x0[c] - A.beta * s * A.dxinv;
+    if (WANT_M) {
+#pragma unroll
+      for (int cp = 0; cp < 2; cp++) {
+        T v = A.beta * A.dxinv * (P[c] * A.J[(2 * c + cp) * n + q] - Y[2 * c + cp]);
+        if (cp == c) v = A.alpha * av + v;
+        M[2 * c + cp] = v;
+      }
+    }
+  }
+}
+
+template <class T, int DIM, bool TR, bool WANT_M>
+__device__ __forceinline__ void jac_cell(const AdjArgs<T> &A, const T *y, int i, int j, int k,
+                                         T out[2], T y0[2], T M[4]) {
+  if (TR)
+    adj_cell<T, DIM, WANT_M>(A, y, i, j, k, out, y0, M);
+  else
+    lin_cell<T, DIM, WANT_M>(A, y, i, j, k, out, y0, M);
+}
+
+// y_j += M^-1 (g_j - (B y)_j), B = A^T (TR) or A: the exact solve of cell j's
+// two rows
+template <class T, int DIM, bool TR = true>
 __device__ __forceinline__ void adj_gs_cell(const AdjArgs<T> &A, T *y, const T *g, int i, int j,
                                             int k) {
   T out[2], y0[2], M[4];
-  adj_cell<T, DIM, true>(A, y, i, j, k, out, y0, M);
+  jac_cell<T, DIM, TR, true>(A, y, i, j, k, out, y0, M);
   const long long q = A.G.cell(i, j, k), n = A.G.ncell;
   const T r0 = g[q] - out[0], r1 = g[q + n] - out[1];
   const T det = M[0] * M[3] - M[1] * M[2];
@@ -214,7 +309,7 @@ __global__ void __launch_bounds__(kBlock) porosity_jac_kernel(Geom G, ClosurePar
 }
 
 // out = A^T y (ADJ_APPLY) or g - A^T y with a fused norm (ADJ_RESIDUAL)
-template <class T, int DIM, int MODE, int NORM>
+template <class T, int DIM, int MODE, int NORM, bool TR>
 __global__ void __launch_bounds__(kBlock) adj_op_kernel(AdjArgs<T> A, const T *__restrict__ y,
                                                         const T *__restrict__ g,
                                                         T *__restrict__ out,
@@ -225,7 +320,7 @@ __global__ void __launch_bounds__(kBlock) adj_op_kernel(AdjArgs<T> A, const T *_
     int i, j, k;
     cell_ijk(G, q, i, j, k);
     T o[2], y0[2];
-    adj_cell<T, DIM, false>(A, y, i, j, k, o, y0, nullptr);
+    jac_cell<T, DIM, TR, false>(A, y, i, j, k, o, y0, nullptr);
 #pragma unroll
     for (int c = 0; c < 2; c++) {
       const long long qc = q + c * G.ncell;
@@ -240,18 +335,18 @@ __global__ void __launch_bounds__(kBlock) adj_op_kernel(AdjArgs<T> A, const T *_
   }
 }
 
-template <class T, int DIM>
+template <class T, int DIM, bool TR>
 __global__ void __launch_bounds__(kBlock) adj_gsrb_kernel(AdjArgs<T> A, T *y,
                                                           const T *__restrict__ g, int pass) {
   const long long nt = colour_threads(A.G);
   for (long long t = gtid(); t < nt; t += gstride()) {
     int i, j, k;
-    if (colour_cell(A.G, pass, t, i, j, k)) adj_gs_cell<T, DIM>(A, y, g, i, j, k);
+    if (colour_cell(A.G, pass, t, i, j, k)) adj_gs_cell<T, DIM, TR>(A, y, g, i, j, k);
   }
 }
 
 // bottom: y = 0 (if zero), then `sweeps` red/black sweeps in one block
-template <class T, int DIM>
+template <class T, int DIM, bool TR>
 __global__ void __launch_bounds__(1024) adj_relax_block_kernel(AdjArgs<T> A, T *y,
                                                                const T *__restrict__ g,
                                                                int sweeps, int zero) {
@@ -265,14 +360,14 @@ __global__ void __launch_bounds__(1024) adj_relax_block_kernel(AdjArgs<T> A, T *
     for (int pass = 0; pass < 2; pass++) {
       for (long long t = threadIdx.x; t < nt; t += blockDim.x) {
         int i, j, k;
-        if (colour_cell(A.G, pass, t, i, j, k)) adj_gs_cell<T, DIM>(A, y, g, i, j, k);
+        if (colour_cell(A.G, pass, t, i, j, k)) adj_gs_cell<T, DIM, TR>(A, y, g, i, j, k);
       }
       __syncthreads();
     }
 }
 
 // coarse right-hand side: the 2^D average of g - A^T y
-template <class T, int DIM>
+template <class T, int DIM, bool TR>
 __global__ void __launch_bounds__(kBlock) adj_restrict_kernel(AdjArgs<T> A, Geom C,
                                                               const T *__restrict__ y,
                                                               const T *__restrict__ g,
@@ -291,7 +386,7 @@ __global__ void __launch_bounds__(kBlock) adj_restrict_kernel(AdjArgs<T> A, Geom
         for (int ii = 0; ii < 2; ii++) {
           const int i = 2 * I + ii, j = 2 * J + jj, k = DIM == 3 ? 2 * K + kk : 0;
           T o[2], y0[2];
-          adj_cell<T, DIM, false>(A, y, i, j, k, o, y0, nullptr);
+          jac_cell<T, DIM, TR, false>(A, y, i, j, k, o, y0, nullptr);
           const long long q = G.cell(i, j, k);
 #pragma unroll
           for (int c = 0; c < 2; c++) acc[c] = acc[c] + (g[q + c * G.ncell] - o[c]) / denom;

@@ -225,6 +225,21 @@ int mlgpu_hc_adjoint_gsrb_pass(const mlgpu_nlop *op, const double *phi, const do
   return status_of(launch_adj_gsrb(make_adj_args(*op, phi, J), y, g, pass, (cudaStream_t)stream));
 }
 
+int mlgpu_hc_linearized_apply(const mlgpu_nlop *op, const double *phi, const double *J,
+                              const double *x, const double *r, double *out, void *stream) {
+  if (!valid_adjoint_op(op) || !phi || !J || !x || !out) return MLGPU_ERR_ARG;
+  return status_of(launch_adj_op(make_adj_args(*op, phi, J), r ? ADJ_RESIDUAL : ADJ_APPLY, -1, x,
+                                 r, out, nullptr, (cudaStream_t)stream, false));
+}
+
+int mlgpu_hc_linearized_gsrb_pass(const mlgpu_nlop *op, const double *phi, const double *J,
+                                  double *x, const double *r, int pass, void *stream) {
+  if (!valid_adjoint_op(op) || !phi || !J || !x || !r || (pass != 0 && pass != 1))
+    return MLGPU_ERR_ARG;
+  return status_of(
+      launch_adj_gsrb(make_adj_args(*op, phi, J), x, r, pass, (cudaStream_t)stream, false));
+}
+
 int mlgpu_hc_adjoint_restrict(const mlgpu_nlop *op, const double *phi, const double *J,
                               const double *y, const double *g, double *gc, void *stream) {
   if (!valid_adjoint_op(op) || !phi || !J || !y || !g || !gc || !coarsenable(op->grid))

@@ -54,14 +54,16 @@ cudaError_t launch_adj_jac(const Geom &G, const ClosureParams &cp, const double 
                            cudaStream_t s);
 cudaError_t launch_porosity_jac(const Geom &G, const ClosureParams &cp, const double *u,
                                 double *dp, cudaStream_t s);
+// tr: A^T (the adjoint) or A (the linearised operator of a Newton step)
 cudaError_t launch_adj_op(const AdjArgs<double> &A, int mode, int norm, const double *y,
-                          const double *g, double *out, double *part, cudaStream_t s);
+                          const double *g, double *out, double *part, cudaStream_t s,
+                          bool tr = true);
 cudaError_t launch_adj_gsrb(const AdjArgs<double> &A, double *y, const double *g, int pass,
-                            cudaStream_t s);
+                            cudaStream_t s, bool tr = true);
 cudaError_t launch_adj_relax_block(const AdjArgs<double> &A, double *y, const double *g,
-                                   int sweeps, int zero, cudaStream_t s);
+                                   int sweeps, int zero, cudaStream_t s, bool tr = true);
 cudaError_t launch_adj_restrict(const AdjArgs<double> &A, const Geom &C, const double *y,
-                                const double *g, double *gc, cudaStream_t s);
+                                const double *g, double *gc, cudaStream_t s, bool tr = true);
 cudaError_t launch_adj_bc_grad(const AdjArgs<double> &A, const double *y, double *out,
                                cudaStream_t s);
 cudaError_t launch_outer_coefs(const VCArgs<double> &A, double *cx, double *cy, double *diag,

@@ -1182,10 +1182,15 @@ class HCAdjSolver : public mlgpu_solver {
   double *part = nullptr, *host_norm = nullptr, *bcg = nullptr;
   double updates_per_iter = 0;
   int kern_iter = -1, kern_init = -1;
-  cudaGraphExec_t graph = nullptr;
+  // tr: cycles on A^T (adjoint) or on A (the linear solve of a Newton step);
+  // one captured iteration graph per mode
+  bool tr = true;
+  cudaGraphExec_t graph = nullptr, graph_lin = nullptr;
+  double *nf = nullptr, *nuold = nullptr;  // Newton: rhs of N(u) = f, previous u
 
   ~HCAdjSolver() override {
     if (graph) cudaGraphExecDestroy(graph);
+    if (graph_lin) cudaGraphExecDestroy(graph_lin);
     if (host_norm) cudaFreeHost(host_norm);
   }
 
@@ -1215,6 +1220,8 @@ class HCAdjSolver : public mlgpu_solver {
     }
     part = A.get<double>(kNormScratchDoubles);
     bcg = A.get<double>(16);
+    nf = A.get<double>(2 * ncells(op.grid));
+    nuold = A.get<double>(2 * ncells(op.grid));
     return A.off + 256;
   }
 
@@ -1250,6 +1257,10 @@ class HCAdjSolver : public mlgpu_solver {
   int set_state(const double *phi) {
     CK(cudaMemcpyAsync(L[0].u, phi, sizeof(double) * 2 * L[0].G.ncell, cudaMemcpyDeviceToDevice,
                        s));
+    return state_levels();
+  }
+  // the coarse states averaged from level 0's, J everywhere
+  int state_levels() {
     for (size_t l = 1; l < L.size(); l++)
       CK(launch_restrict_avg<double>(L[l - 1].G, 2, L[l - 1].u, L[l].u, s));
     const ClosureParams cp = make_cp(op.params);
@@ -1260,7 +1271,7 @@ class HCAdjSolver : public mlgpu_solver {
   int smooth(int l, int n) {
     AdjArgs<double> A = args(l);
     for (int i = 0; i < n; i++)
-      for (int pass = 0; pass < 2; pass++) CK(launch_adj_gsrb(A, L[l].y, L[l].g, pass, s));
+      for (int pass = 0; pass < 2; pass++) CK(launch_adj_gsrb(A, L[l].y, L[l].g, pass, s, tr));
     return MLGPU_OK;
   }
 
@@ -1269,13 +1280,13 @@ class HCAdjSolver : public mlgpu_solver {
     const int last = (int)L.size() - 1;
     AdjArgs<double> A = args(l);
     if (l == last) {
-      CK(launch_adj_relax_block(A, L[l].y, L[l].g, o.bottom_max_iter, l > 0 ? 1 : 0, s));
+      CK(launch_adj_relax_block(A, L[l].y, L[l].g, o.bottom_max_iter, l > 0 ? 1 : 0, s, tr));
       return MLGPU_OK;
     }
     if (l > 0) CK(cudaMemsetAsync(L[l].y, 0, sizeof(double) * 2 * L[l].G.ncell, s));
     int rc = smooth(l, o.num_smooth_down);
     if (rc) return rc;
-    CK(launch_adj_restrict(A, L[l + 1].G, L[l].y, L[l].g, L[l + 1].g, s));
+    CK(launch_adj_restrict(A, L[l + 1].G, L[l].y, L[l].g, L[l + 1].g, s, tr));
     for (int m = 0; m < o.num_mg; m++) {
       rc = cycle(l + 1);
       if (rc) return rc;
@@ -1285,7 +1296,7 @@ class HCAdjSolver : public mlgpu_solver {
   }
 
   int residual_norm() {
-    CK(launch_adj_op(args(0), ADJ_RESIDUAL, o.norm_type, L[0].y, L[0].g, L[0].r, part, s));
+    CK(launch_adj_op(args(0), ADJ_RESIDUAL, o.norm_type, L[0].y, L[0].g, L[0].r, part, s, tr));
     CK(launch_finalize_norm(o.norm_type, part, norm_parts(L[0].G.ncell), part + kMaxBlocks, s));
     CK(cudaMemcpyAsync(host_norm, part + kMaxBlocks, sizeof(double), cudaMemcpyDeviceToHost, s));
     return MLGPU_OK;
@@ -1299,19 +1310,89 @@ class HCAdjSolver : public mlgpu_solver {
 
   int run_iteration() {
     if (!o.use_graph) return iteration();
-    if (!graph) {
+    cudaGraphExec_t &gx = tr ? graph : graph_lin;
+    if (!gx) {
       cudaGraph_t g;
       CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
       int rc = iteration();
       cudaError_t e = cudaStreamEndCapture(s, &g);
       if (rc) return rc;
       CK(e);
-      e = cudaGraphInstantiate(&graph, g, 0);
+      e = cudaGraphInstantiate(&gx, g, 0);
       cudaGraphDestroy(g);
       CK(e);
     }
-    CK(cudaGraphLaunch(graph, s));
+    CK(cudaGraphLaunch(gx, s));
     return MLGPU_OK;
+  }
+
+  // ---- Newton for N(u) = f: u += d, A(u) d = f - N(u) solved by these
+  // cycles on A to `lin_tol` relative (at most `lin_max` cycles), halving d
+  // while the FP64 residual grows (at most 4 times)
+  double lin_tol = 1e-3;
+  int lin_max = 12;
+
+  // f - N(u) into L[0].g and its norm to the host
+  int nl_residual() {
+    CK(launch_nl_op<double>(make_nl_args<double>(op), NL_RESIDUAL, o.norm_type, L[0].u, nf,
+                            L[0].g, nullptr, part, s));
+    CK(launch_finalize_norm(o.norm_type, part, norm_parts(L[0].G.ncell), part + kMaxBlocks, s));
+    CK(cudaMemcpyAsync(host_norm, part + kMaxBlocks, sizeof(double), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    return MLGPU_OK;
+  }
+
+  int newton(double *user_u, const double *user_f, mlgpu_solve_stats *st) {
+    const long long n2 = 2 * L[0].G.ncell;
+    const size_t bytes = sizeof(double) * n2;
+    cudaGetLastError();
+    if (enter()) return MLGPU_ERR_CUDA;
+    CK(cudaMemcpyAsync(L[0].u, user_u, bytes, cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(nf, user_f, bytes, cudaMemcpyDeviceToDevice, s));
+    tr = false;
+    int rc = nl_residual();
+    if (rc) return rc;
+    Outer S;
+    S.norm0 = S.norm = S.prev = *host_norm;
+    stats_begin(st, (int)L.size(), S.norm0);
+    st->cell_updates = (double)L[0].G.ncell;
+    if (!std::isfinite(S.norm0)) S.status = 8;
+    while (outer_continue(o, S)) {
+      rc = state_levels();
+      if (rc) return rc;
+      // linear solve A d = r, d in L[0].y from zero
+      CK(cudaMemsetAsync(L[0].y, 0, bytes, s));
+      rc = residual_norm();
+      if (rc) return rc;
+      CK(cudaStreamSynchronize(s));
+      const double l0 = *host_norm;
+      for (int c = 0; c < lin_max && *host_norm > lin_tol * l0; c++) {
+        rc = run_iteration();
+        if (rc) return rc;
+        CK(cudaStreamSynchronize(s));
+        st->cycles += 1;
+        st->cell_updates += updates_per_iter;
+      }
+      CK(cudaMemcpyAsync(nuold, L[0].u, bytes, cudaMemcpyDeviceToDevice, s));
+      double scale = 1.0;
+      for (int h = 0; h <= 4; h++) {
+        // u = u_old + scale d
+        CK(cudaMemcpyAsync(L[0].u, nuold, bytes, cudaMemcpyDeviceToDevice, s));
+        CK(launch_axpby<double>(n2, scale, L[0].y, 1.0, L[0].u, s));
+        rc = nl_residual();
+        if (rc) return rc;
+        st->cell_updates += (double)L[0].G.ncell;
+        if (std::isfinite(*host_norm) && *host_norm <= S.norm) break;
+        scale *= 0.5;
+      }
+      S.norm = *host_norm;
+      outer_after(o, S, st);
+    }
+    CK(cudaMemcpyAsync(user_u, L[0].u, bytes, cudaMemcpyDeviceToDevice, s));
+    CK(cudaStreamSynchronize(s));
+    tr = true;
+    if (leave()) return MLGPU_ERR_CUDA;
+    return outer_finish(o, S, st);
   }
 
   // A^T y = g at the state already set; y, g device arrays of the caller
@@ -1381,10 +1462,11 @@ class HCAdjSolver : public mlgpu_solver {
   int set_alpha_beta(double a, double b) override {
     op.alpha = a;
     op.beta = b;
-    if (graph) {
-      cudaGraphExecDestroy(graph);
-      graph = nullptr;
-    }
+    for (auto *gp : {&graph, &graph_lin})
+      if (*gp) {
+        cudaGraphExecDestroy(*gp);
+        *gp = nullptr;
+      }
     return MLGPU_OK;
   }
 
@@ -1648,6 +1730,26 @@ int mlgpu_hc_adjoint_solve(mlgpu_solver *S, const double *phi, const double *g, 
   HCAdjSolver *A = dynamic_cast<HCAdjSolver *>(S);
   if (!A || !phi || !g || !y || !stats) return MLGPU_ERR_ARG;
   return A->adjoint_solve(phi, g, y, stats);
+}
+
+int mlgpu_hc_newton_solve(mlgpu_solver *S, double *phi, const double *rhs,
+                          mlgpu_solve_stats *stats) {
+  HCAdjSolver *A = dynamic_cast<HCAdjSolver *>(S);
+  if (!A || !phi || !rhs || !stats) return MLGPU_ERR_ARG;
+  return A->newton(phi, rhs, stats);
+}
+
+int mlgpu_hc_backward_euler_newton(mlgpu_solver *S, double *phi_new, const double *phi_old,
+                                   const double *src, const double *aCoef, double dt,
+                                   double *rhs_scratch, mlgpu_solve_stats *stats) {
+  HCAdjSolver *A = dynamic_cast<HCAdjSolver *>(S);
+  if (!A || !phi_new || !phi_old || !rhs_scratch || !stats || !(dt > 0)) return MLGPU_ERR_ARG;
+  if (A->op.alpha != 1.0 || A->op.beta != -dt) A->set_alpha_beta(1.0, -dt);
+  cudaGetLastError();
+  if (A->enter()) return MLGPU_ERR_CUDA;
+  CK(launch_be_rhs(2 * A->L[0].G.ncell, phi_old, aCoef, src, dt, rhs_scratch, A->s));
+  if (A->leave()) return MLGPU_ERR_CUDA;
+  return A->newton(phi_new, rhs_scratch, stats);
 }
 
 int mlgpu_hc_adjoint_bc_gradient(mlgpu_solver *S, const double *y, double grad[12]) {

@@ -209,10 +209,14 @@ def _declare(lib):
         "mlgpu_hc_adjoint_apply": (i, [P(NLOp), vp, vp, vp, vp, vp, vp]),
         "mlgpu_hc_adjoint_gsrb_pass": (i, [P(NLOp), vp, vp, vp, vp, i, vp]),
         "mlgpu_hc_adjoint_restrict": (i, [P(NLOp), vp, vp, vp, vp, vp, vp]),
+        "mlgpu_hc_linearized_apply": (i, [P(NLOp), vp, vp, vp, vp, vp, vp]),
+        "mlgpu_hc_linearized_gsrb_pass": (i, [P(NLOp), vp, vp, vp, vp, i, vp]),
         "mlgpu_hc_adjoint_workspace": (i, [P(NLOp), P(MGOptions), P(sz)]),
         "mlgpu_hc_adjoint_create": (i, [P(NLOp), P(MGOptions), vp, sz, vp, P(vp)]),
         "mlgpu_hc_adjoint_solve": (i, [vp, vp, vp, vp, P(SolveStats)]),
         "mlgpu_hc_adjoint_bc_gradient": (i, [vp, vp, P(d)]),
+        "mlgpu_hc_newton_solve": (i, [vp, vp, vp, P(SolveStats)]),
+        "mlgpu_hc_backward_euler_newton": (i, [vp, vp, vp, vp, vp, d, vp, P(SolveStats)]),
         "mlgpu_hc_backward_euler_adjoint": (i, [vp, vp, vp, vp, d, vp, vp, vp, P(d),
                                                 P(SolveStats)]),
         "mlgpu_mac_project_adjoint": (i, [vp, P(Grid), P(BC), vp * 3, vp * 3, vp, vp * 3,

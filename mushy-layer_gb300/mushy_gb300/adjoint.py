@@ -6,7 +6,8 @@ hand-written adjoint kernels:
 * ``Closure``            (H, C) -> (T, C_l, porosity); backward through the
                          closure Jacobian and the porosity derivative.
 * ``BackwardEulerStep``  phi_new = BE step of phi_old with source and one
-                         wall temperature; backward = one transposed-Jacobian
+                         wall temperature (Newton on the Jacobian hierarchy, or
+                         the FAS solver); backward = one transposed-Jacobian
                          multigrid solve (mlgpu_hc_backward_euler_adjoint).
 * ``MacProject``         u = u* - Pi G p; backward = the projection's adjoint
                          solve (mlgpu_mac_project_adjoint), giving u*-bar and
@@ -48,11 +49,12 @@ class BEStepper:
     """The solvers of one backward-Euler (H, C) step whose derived-variable
     wall value at `wall` = (dir, side, comp) is a differentiable input."""
 
-    def __init__(self, op, opts, adj_opts, wall=(1, 0, 0)):
-        self.op, self.wall = op, wall
-        self.S = ops.AMRFASMultiGrid(op, opts)
+    def __init__(self, op, opts, adj_opts, wall=(1, 0, 0), accept=1e-10, newton=True):
+        self.op, self.wall, self.accept, self.newton = op, wall, accept, newton
+        self.S = None if newton else ops.AMRFASMultiGrid(op, opts)
         self.A = ops.AdjointMultiGrid(op, adj_opts)
         self._value = None
+        self.iterations = {"forward": [], "adjoint": []}  # per solve, for reporting
 
     def set_wall(self, v):
         v = float(v)
@@ -63,7 +65,8 @@ class BEStepper:
         bc.type, bc.value = self.op.derived_bc.type, self.op.derived_bc.value
         bc.value[d][s][c] = v
         self.op.derived_bc = bc
-        self.S.setBCs(derived_bc=bc)
+        if self.S is not None:
+            self.S.setBCs(derived_bc=bc)
         self.A.setBCs(derived_bc=bc)
         self._value = v
 
@@ -72,15 +75,26 @@ class BEStepper:
         return (d * 2 + s) * 2 + c
 
 
+def _accept(st, rc, accept, what):
+    """A solve is used if it converged, or stopped (stagnation / iteration
+    cap) with its residual already `accept` times below the initial one."""
+    if rc == abi.OK:
+        return
+    if rc in (abi.ERR_HANG, abi.ERR_NOT_CONVERGED) and st.final_norm <= accept * st.initial_norm:
+        return
+    raise RuntimeError("%s: solve stopped at %.3g of its initial residual (status %d)"
+                       % (what, st.final_norm / max(st.initial_norm, 1e-300), rc))
+
+
 class BackwardEulerStep(torch.autograd.Function):
     @staticmethod
     def forward(ctx, phi_old, src, wall_value, stepper, dt):
         stepper.set_wall(wall_value.item())
         phi_new = phi_old.detach().clone()
-        st, rc = stepper.S.backwardEuler(phi_new, phi_old.detach().contiguous(), dt,
-                                         src=src.detach().contiguous())
-        if rc not in (abi.OK, abi.ERR_HANG):
-            abi.check(rc, "BackwardEulerStep")
+        solve = stepper.A.backwardEulerNewton if stepper.newton else stepper.S.backwardEuler
+        st, rc = solve(phi_new, phi_old.detach().contiguous(), dt, src=src.detach().contiguous())
+        _accept(st, rc, stepper.accept, "BackwardEulerStep")
+        stepper.iterations["forward"].append(st.iterations)
         ctx.save_for_backward(phi_new, wall_value)
         ctx.stepper, ctx.dt = stepper, dt
         return phi_new
@@ -93,8 +107,8 @@ class BackwardEulerStep(torch.autograd.Function):
         mu = torch.zeros_like(phi_new)
         old_bar, src_bar, bcg, st, rc = stp.A.backwardEulerAdjoint(
             phi_new, g.contiguous(), ctx.dt, mu)
-        if rc not in (abi.OK, abi.ERR_HANG):
-            abi.check(rc, "BackwardEulerStep.backward")
+        _accept(st, rc, stp.accept, "BackwardEulerStep.backward")
+        stp.iterations["adjoint"].append(st.iterations)
         wbar = torch.tensor(bcg[stp.slot()], dtype=torch.float64, device=phi_new.device)
         return old_bar, src_bar, wbar, None, None
 
@@ -102,8 +116,8 @@ class BackwardEulerStep(torch.autograd.Function):
 class Projector:
     """A projection solver bound to one set of face permeabilities."""
 
-    def __init__(self, grid, pi_faces, opts, bc=None):
-        self.grid = grid
+    def __init__(self, grid, pi_faces, opts, bc=None, accept=1e-10):
+        self.grid, self.accept = grid, accept
         self.pi = [p.detach().contiguous() for p in pi_faces]
         self.bc = bc if bc is not None else abi.make_bc()
         self.op = ops.ProjectionOp(grid, self.bc, 0.0, 1.0, None, [-p for p in self.pi])
@@ -116,8 +130,7 @@ class MacProject(torch.autograd.Function):
         u = [ux.detach().clone().contiguous(), uz.detach().clone().contiguous()]
         p = torch.zeros(abi.cell_shape(projector.grid), dtype=torch.float64, device=ux.device)
         st, rc = projector.S.levelMacProject(u, projector.pi, p)
-        if rc not in (abi.OK, abi.ERR_HANG):
-            abi.check(rc, "MacProject")
+        _accept(st, rc, projector.accept, "MacProject")
         ctx.save_for_backward(p)
         ctx.projector = projector
         return u[0], u[1]
@@ -129,8 +142,7 @@ class MacProject(torch.autograd.Function):
         ub = [gx.contiguous() if gx is not None else torch.zeros_like(P.pi[0]),
               gz.contiguous() if gz is not None else torch.zeros_like(P.pi[1])]
         usb, pib, q, st, rc = ops.macProjectAdjoint(P.S, ub, P.pi, p, phi_bc=P.bc)
-        if rc not in (abi.OK, abi.ERR_HANG):
-            abi.check(rc, "MacProject.backward")
+        _accept(st, rc, P.accept, "MacProject.backward")
         return usb[0], usb[1], pib[0], pib[1], None
 
 

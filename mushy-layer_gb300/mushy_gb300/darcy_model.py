@@ -15,6 +15,10 @@ index).  One step of length dt:
    diffusion D_C, T Dirichlet at the bottom (T_b, differentiable) and top,
    no solute flux at the walls                                [BackwardEulerStep]
 
+Defaults: liquid H = 6.2 (T = 1.2), C = -1 with 1e-3 noise; T = 1.2 at the
+top and T_b = 0.5 (below the liquidus T = 1 of C = -1, above the eutectic)
+at the bottom, so a mushy layer grows from the bottom.
+
 Objective: final mean solid fraction (1 - porosity) plus the mean heat flux
 through the top wall, 2 (T_top - T)/dx on its row.  Gradients with respect
 to the per-cell log-permeability, Ra and T_b come from the adjoint Functions
@@ -31,7 +35,8 @@ from .adjoint import BEStepper, BackwardEulerStep, Closure, MacProject, Projecto
 
 
 class DarcySolidification:
-    def __init__(self, n, dt=5e-4, Da=5e-6, Dc=1e-2, T_top=0.5, tol=1e-13, params=None):
+    def __init__(self, n, dt=5e-4, Da=5e-6, Dc=1e-2, T_top=1.2, tol=1e-13, params=None,
+                 precision=abi.PREC_F64, newton=True):
         self.n, self.dt, self.Da, self.T_top = n, dt, Da, T_top
         self.grid = abi.make_grid([n, n], 1.0 / n, [1, 0, 0])
         self.params = params or abi.make_params(stefan=5.0, compositionRatio=5.0,
@@ -45,14 +50,18 @@ class DarcySolidification:
             b.append(dev(torch.stack([-torch.ones(fs, dtype=torch.float64),
                                       -Dc * torch.ones(fs, dtype=torch.float64)])))
         self.bcoef = b
-        der = abi.make_bc({(1, 0, 0): (abi.BC_DIRICHLET, -1.0),
+        der = abi.make_bc({(1, 0, 0): (abi.BC_DIRICHLET, 0.5),
                            (1, 1, 0): (abi.BC_DIRICHLET, T_top)})
         self.hop = ops.NLMultiCompOp(g, self.params, abi.make_bc(), der, 1.0, -dt, None, b)
+        # the step: Newton on the Jacobian hierarchy (newton=True) or the FAS
+        # solver; iterate through a transient residual growth (stop only on a
+        # doubling); the adjoint solves to the same tolerance
         o = ops.default_options(True)
-        o.tolerance, o.hang, o.max_iter = tol, 0.0, 100
+        o.tolerance, o.hang, o.max_iter = tol, -1.0, 200
+        o.precision = precision
         oa = ops.default_options(True)
-        oa.tolerance, oa.hang, oa.max_iter = tol, 0.0, 100
-        self.stepper = BEStepper(self.hop, o, oa, wall=(1, 0, 0))
+        oa.tolerance, oa.hang, oa.max_iter = tol, -1.0, 200
+        self.stepper = BEStepper(self.hop, o, oa, wall=(1, 0, 0), newton=newton)
         self.popts = ops.default_options(False)
         self.popts.tolerance, self.popts.hang, self.popts.max_iter = tol, 0.0, 400
         self.projector = None
@@ -114,11 +123,12 @@ class DarcySolidification:
         return self.objective(phi)
 
 
-def initial_state(n, seed=0):
-    """Liquid H = 1 + St, C = -1 with 1e-3 seeded noise."""
+def initial_state(n, seed=0, H0=6.2):
+    """Liquid H = H0 (1 + St = 6 is the liquidus at C = -1), C = -1, with
+    1e-3 seeded noise."""
     g = torch.Generator().manual_seed(seed)
     phi = torch.empty((2, 1, n, n), dtype=torch.float64)
-    phi[0] = 6.0 + 1e-3 * torch.randn((1, n, n), generator=g, dtype=torch.float64)
+    phi[0] = H0 + 1e-3 * torch.randn((1, n, n), generator=g, dtype=torch.float64)
     phi[1] = -1.0 + 1e-3 * torch.randn((1, n, n), generator=g, dtype=torch.float64)
     return phi.cuda()
 

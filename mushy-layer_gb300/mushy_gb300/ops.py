@@ -397,6 +397,21 @@ def adjointGSRBPass(op, phi, J, y, g, pass_):
               "adjointGSRBPass")
 
 
+def linearizedApply(op, phi, J, x, r=None):
+    """A x (r None) or r - A x, A = dN/dphi of `op` at phi."""
+    out = torch.empty_like(x)
+    abi.check(abi.load().mlgpu_hc_linearized_apply(C.byref(op.desc()), _ptr(phi), _ptr(J),
+                                                   _ptr(x), _ptr(r), _ptr(out), _stream()),
+              "linearizedApply")
+    return out
+
+
+def linearizedGSRBPass(op, phi, J, x, r, pass_):
+    abi.check(abi.load().mlgpu_hc_linearized_gsrb_pass(C.byref(op.desc()), _ptr(phi), _ptr(J),
+                                                       _ptr(x), _ptr(r), int(pass_), _stream()),
+              "linearizedGSRBPass")
+
+
 def adjointRestrict(op, phi, J, y, g):
     gc = cell_tensor(coarse_grid(op.grid), 2, torch.float64)
     abi.check(abi.load().mlgpu_hc_adjoint_restrict(C.byref(op.desc()), _ptr(phi), _ptr(J),
@@ -416,6 +431,22 @@ class AdjointMultiGrid(_Solver):
         st = abi.SolveStats()
         rc = abi.load().mlgpu_hc_adjoint_solve(self.h, _ptr(phi), _ptr(g), _ptr(y), C.byref(st))
         _ok(rc, "adjointSolve")
+        return st, rc
+
+    def newtonSolve(self, phi, rhs):
+        """N(phi) = rhs by Newton steps on the Jacobian hierarchy (phi in/out)."""
+        st = abi.SolveStats()
+        rc = abi.load().mlgpu_hc_newton_solve(self.h, _ptr(phi), _ptr(rhs), C.byref(st))
+        _ok(rc, "newtonSolve")
+        return st, rc
+
+    def backwardEulerNewton(self, phi_new, phi_old, dt, src=None, aCoef=None):
+        scratch = torch.empty_like(phi_old)
+        st = abi.SolveStats()
+        rc = abi.load().mlgpu_hc_backward_euler_newton(self.h, _ptr(phi_new), _ptr(phi_old),
+                                                       _ptr(src), _ptr(aCoef), float(dt),
+                                                       _ptr(scratch), C.byref(st))
+        _ok(rc, "backwardEulerNewton")
         return st, rc
 
     def bcGradient(self, y):

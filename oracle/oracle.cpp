@@ -1622,6 +1622,64 @@ void lin_apply(const AdjCtx &X, const double *xd, double *out) {
         }
 }
 
+// one red/black pass of the block smoother on A x = r (the Newton step's
+// linear solve): out and the diagonal block D of each colour cell from J x
+// with its ghosts, x += D^-1 (r - A x)
+void lin_gsrb_pass(const AdjCtx &X, double *xd, const double *r, int pass) {
+  const mlgpu_nlop &op = X.op;
+  const mlgpu_grid &g = op.grid;
+  std::vector<double> out(2 * X.n);
+  lin_apply(X, xd, out.data());
+  for (int k = 0; k < g.n[2]; k++)
+    for (int j = 0; j < g.n[1]; j++) {
+      int imin = std::abs((j + k + pass) % 2);
+      for (int i = imin; i < g.n[0]; i += 2) {
+        const size_t q = cidx(g, i, j, k, 0);
+        const int at[3] = {i, j, k};
+        double P[2], Y[4] = {0.0, 0.0, 0.0, 0.0}, M[4];
+        for (int c = 0; c < 2; c++) {
+          double p = 0.0;
+          for (int d = 0; d < g.dim; d++)
+            for (int side = 1; side >= 0; side--) {
+              int fi[3] = {i, j, k};
+              if (side) fi[d] += 1;
+              double bf = X.B(d, fi[0], fi[1], fi[2], c);
+              int nb = at[d] + (side ? 1 : -1);
+              double dp;
+              if (nb >= 0 && nb < g.n[d])
+                dp = bf;
+              else if (g.periodic[d])
+                dp = g.n[d] == 1 ? 0.0 : bf;
+              else if (op.apply_derived_bc)
+                dp = op.derived_bc.type[d][side][c] == MLGPU_BC_DIRICHLET ? 2 * bf : 0.0;
+              else {
+                double Jg[4];
+                ghost_jac(X, q, d, side, Jg);
+                double s0 = op.phi_bc.type[d][side][0] == MLGPU_BC_DIRICHLET ? -1.0 : 1.0;
+                double s1 = op.phi_bc.type[d][side][1] == MLGPU_BC_DIRICHLET ? -1.0 : 1.0;
+                dp = bf;
+                Y[2 * c + 0] = Y[2 * c + 0] + bf * (Jg[2 * c] * s0);
+                Y[2 * c + 1] = Y[2 * c + 1] + bf * (Jg[2 * c + 1] * s1);
+              }
+              p = p + dp;
+            }
+          P[c] = p;
+          double av = X.a ? X.a[q + c * X.n] : 1.0;
+          for (int cp = 0; cp < 2; cp++) {
+            double v = op.beta * X.dxinv * (P[c] * X.jac(q, 2 * c + cp) - Y[2 * c + cp]);
+            if (cp == c) v = op.alpha * av + v;
+            M[2 * c + cp] = v;
+          }
+        }
+        double r0 = r[q] - out[q], r1 = r[q + X.n] - out[q + X.n];
+        double det = M[0] * M[3] - M[1] * M[2];
+        double x0 = xd[q], x1 = xd[q + X.n];
+        xd[q] = x0 + (M[3] * r0 - M[1] * r1) / det;
+        xd[q + X.n] = x1 + (M[0] * r1 - M[2] * r0) / det;
+      }
+    }
+}
+
 // ---- multigrid for A^T y = g (the device driver restated)
 struct AdjLevelO {
   mlgpu_grid g;
@@ -1762,6 +1820,13 @@ int orc_hc_linearized_apply(const mlgpu_nlop *op, const double *phi, const doubl
                             const double *x, double *out) {
   AdjCtx X(*op, phi, J);
   lin_apply(X, x, out);
+  return 0;
+}
+
+int orc_hc_lin_gsrb_pass(const mlgpu_nlop *op, const double *phi, const double *J, double *x,
+                         const double *r, int pass) {
+  AdjCtx X(*op, phi, J);
+  lin_gsrb_pass(X, x, r, pass);
   return 0;
 }
 

@@ -59,6 +59,7 @@ def lib():
             "orc_hc_adjoint_gsrb_pass": (i, [P(abi.NLOp), vp, vp, vp, vp, i]),
             "orc_hc_adjoint_restrict": (i, [P(abi.NLOp), vp, vp, vp, vp, vp]),
             "orc_hc_linearized_apply": (i, [P(abi.NLOp), vp, vp, vp, vp]),
+            "orc_hc_lin_gsrb_pass": (i, [P(abi.NLOp), vp, vp, vp, vp, i]),
             "orc_hc_adjoint_solve": (i, [P(abi.NLOp), P(abi.MGOptions), vp, vp, vp,
                                          P(abi.SolveStats)]),
             "orc_hc_adjoint_bc_gradient": (i, [P(abi.NLOp), vp, vp, vp, vp]),
@@ -363,6 +364,12 @@ def linearized_apply(o, phi, J, x):
     out = np.empty_like(x)
     lib().orc_hc_linearized_apply(C.byref(o.op), _p(phi), _p(J), _p(x), _p(out))
     return out
+
+
+def lin_gsrb_pass(o, phi, J, x, r, pass_):
+    x = x.copy()
+    lib().orc_hc_lin_gsrb_pass(C.byref(o.op), _p(phi), _p(J), _p(x), _p(r), int(pass_))
+    return x
 
 
 def adjoint_solve(o, opts, phi, g, y=None):

@@ -139,3 +139,54 @@ def test_mac_project_adjoint_matches_oracle():
     for d in range(2):
         exact(host(usb[d]), usb_r[d])
         exact(host(pib[d]), pib_r[d])
+
+
+@pytest.mark.parametrize("n,per,dbc", CASES)
+def test_linearized_kernels_bitwise(n, per, dbc):
+    """The untransposed Jacobian A (Newton's linear operator): apply and one
+    block red/black pass against the oracle."""
+    from mushy_gb300 import ops
+    g, p, ref, op, phi, rng = setup(n, per, 24, dbc, mush=True)
+    d_phi = dev(phi)
+    J = ops.closureJacobian(g, p, d_phi)
+    Jr = O.closure_jac(g, p, phi)
+    x = rng.standard_normal(phi.shape)
+    r = rng.standard_normal(phi.shape)
+    d_x, d_r = dev(x), dev(r)
+    exact(host(ops.linearizedApply(op, d_phi, J, d_x)), O.linearized_apply(ref, phi, Jr, x))
+    ops.linearizedGSRBPass(op, d_phi, J, d_x, d_r, 0)
+    x1 = O.lin_gsrb_pass(ref, phi, Jr, x, r, 0)
+    exact(host(d_x), x1)
+    ops.linearizedGSRBPass(op, d_phi, J, d_x, d_r, 1)
+    exact(host(d_x), O.lin_gsrb_pass(ref, phi, Jr, x1, r, 1))
+
+
+@pytest.mark.parametrize("n", [(64, 64), (32, 32, 32)])
+def test_newton_backward_euler_matches_fas(n):
+    """Newton on the Jacobian hierarchy reaches the FP64 residual tolerance
+    of the FAS solve in a few steps and lands on the same solution."""
+    from mushy_gb300 import ops
+    g = P.grid(n)
+    p = P.mushy_params()
+    phi_bc, der = P.hc_bcs("mixed")
+    rng = np.random.default_rng(25)
+    phi = P.hc_state(g, rng, regimes=False)
+    phi[0] = rng.uniform(4.6, 6.4, phi[0].shape)
+    b = [np.stack([-np.ones(abi.face_shape(g, d)), -0.01 * np.ones(abi.face_shape(g, d))])
+         for d in range(len(n))]
+    op = ops.NLMultiCompOp(g, p, phi_bc, der, 1.0, -1e-3, None, [dev(x) for x in b])
+    dt = 2e-3
+    o = ops.default_options(True)
+    o.tolerance, o.hang, o.max_iter = 1e-12, -1.0, 300
+    fas = dev(phi)
+    st_f, rc_f = ops.AMRFASMultiGrid(op, o).backwardEuler(fas, dev(phi), dt)
+    A = ops.AdjointMultiGrid(op, o)
+    nt = dev(phi)
+    st_n, rc_n = A.backwardEulerNewton(nt, dev(phi), dt)
+    assert rc_n == 0 and st_n.iterations <= 8, (rc_n, st_n.iterations)
+    assert st_n.final_norm <= 1e-12 * st_n.initial_norm
+    ref = O.NLOpHost(g, p, phi_bc, der, 1.0, -dt, None, b)
+    r = O.nl_residual(ref, host(nt), phi)
+    assert np.abs(r).max() <= 1.01e-12 * st_n.initial_norm
+    scale = np.abs(host(fas)).max()
+    assert np.abs(host(nt) - host(fas)).max() <= 1e-9 * scale
