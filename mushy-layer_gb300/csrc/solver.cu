@@ -1357,6 +1357,7 @@ class HCAdjSolver : public mlgpu_solver {
     stats_begin(st, (int)L.size(), S.norm0);
     st->cell_updates = (double)L[0].G.ncell;
     if (!std::isfinite(S.norm0)) S.status = 8;
+    int stall = 0;  // consecutive steps that cut the residual by under 5%
     while (outer_continue(o, S)) {
       rc = state_levels();
       if (rc) return rc;
@@ -1386,7 +1387,12 @@ class HCAdjSolver : public mlgpu_solver {
         scale *= 0.5;
       }
       S.norm = *host_norm;
+      stall = S.norm >= 0.95 * S.prev ? stall + 1 : 0;
       outer_after(o, S, st);
+      // three stalled steps far below the start: the FP64 residual has
+      // reached its round-off floor (stalls of the damped early steps, where
+      // the closure's regime switches cut the step, do not count)
+      if (stall >= 3 && S.norm < 1e-8 * S.norm0 && S.status == 0) S.status = 2;
     }
     CK(cudaMemcpyAsync(user_u, L[0].u, bytes, cudaMemcpyDeviceToDevice, s));
     CK(cudaStreamSynchronize(s));

@@ -5,7 +5,8 @@ State phi = (H, C) on a 2D box, periodic in x, walls in z (the second
 index).  One step of length dt:
 
 1. (T, C_l, porosity) = closure(H, C)                       [Closure]
-2. Darcy buoyancy on the interior z faces, u*_z = Ra Da Pi_f T_f, with the
+2. thermal Darcy buoyancy on the interior z faces (z up),
+   u*_z = Ra Da Pi_f (T - T_top)_f, with the
    face permeability Pi_f = exp of the mean log-permeability of the two
    cells (the cell value at a wall); u*_x = 0
 3. u = u* - Pi G p with D Pi G p = D u*                      [MacProject]
@@ -15,9 +16,12 @@ index).  One step of length dt:
    diffusion D_C, T Dirichlet at the bottom (T_b, differentiable) and top,
    no solute flux at the walls                                [BackwardEulerStep]
 
-Defaults: liquid H = 6.2 (T = 1.2), C = -1 with 1e-3 noise; T = 1.2 at the
-top and T_b = 0.5 (below the liquidus T = 1 of C = -1, above the eutectic)
-at the bottom, so a mushy layer grows from the bottom.
+Defaults: liquid H = 6.3 + 0.2 cos(2 pi x) (T = 1.1 .. 1.5), C = -1, with
+1e-3 noise; T = 1.3 at the top and T_b = 0.5 (below the liquidus T = 1 of
+C = -1, above the eutectic) at the bottom, so a mushy layer grows from the
+bottom while the horizontal temperature contrast drives a cellular flow
+(buoyancy that depends on z alone would be hydrostatic: the projection
+removes it).
 
 Objective: final mean solid fraction (1 - porosity) plus the mean heat flux
 through the top wall, 2 (T_top - T)/dx on its row.  Gradients with respect
@@ -35,7 +39,7 @@ from .adjoint import BEStepper, BackwardEulerStep, Closure, MacProject, Projecto
 
 
 class DarcySolidification:
-    def __init__(self, n, dt=5e-4, Da=5e-6, Dc=1e-2, T_top=1.2, tol=1e-13, params=None,
+    def __init__(self, n, dt=5e-4, Da=2e-5, Dc=1e-2, T_top=1.3, tol=1e-12, params=None,
                  precision=abi.PREC_F64, newton=True):
         self.n, self.dt, self.Da, self.T_top = n, dt, Da, T_top
         self.grid = abi.make_grid([n, n], 1.0 / n, [1, 0, 0])
@@ -97,7 +101,7 @@ class DarcySolidification:
 
     def step(self, phi, pi_x, pi_z, Ra, Tb):
         T, Cl, _ = Closure.apply(phi, self.grid, self.params)
-        uz_star = Ra * self.Da * pi_z * self._z_faces_interior(T)
+        uz_star = Ra * self.Da * pi_z * self._z_faces_interior(T - self.T_top)
         ux_star = torch.zeros_like(pi_x)
         ux, uz = MacProject.apply(ux_star, uz_star.contiguous(), pi_x, pi_z,
                                   self.projector_for(pi_x, pi_z))
@@ -123,12 +127,14 @@ class DarcySolidification:
         return self.objective(phi)
 
 
-def initial_state(n, seed=0, H0=6.2):
-    """Liquid H = H0 (1 + St = 6 is the liquidus at C = -1), C = -1, with
-    1e-3 seeded noise."""
+def initial_state(n, seed=0, H0=6.3, amp=0.2):
+    """Liquid H = H0 + amp cos(2 pi x) (1 + St = 6 is the liquidus at
+    C = -1), C = -1, with 1e-3 seeded noise."""
     g = torch.Generator().manual_seed(seed)
     phi = torch.empty((2, 1, n, n), dtype=torch.float64)
-    phi[0] = H0 + 1e-3 * torch.randn((1, n, n), generator=g, dtype=torch.float64)
+    x = (torch.arange(n, dtype=torch.float64) + 0.5) / n
+    phi[0] = (H0 + amp * torch.cos(2 * math.pi * x)).reshape(1, 1, n) + \
+        1e-3 * torch.randn((1, n, n), generator=g, dtype=torch.float64)
     phi[1] = -1.0 + 1e-3 * torch.randn((1, n, n), generator=g, dtype=torch.float64)
     return phi.cuda()
 
