@@ -41,7 +41,7 @@ SEED = 1
 # profiles/vc_solve_mixed_512x512_launch_list.md): the ~25 MB working set
 # stays in the 129 MB L2 between iterations, so DRAM sees ~1% of the
 # algorithmic bytes
-ITERATION_DRAM_BYTES = 389120
+ITERATION_DRAM_BYTES = 389781
 TOL = 1e-10
 METRIC = "FAS V-cycle cell-updates/s on 1 GB300: mixed vs FP64 at 1e-10 rel residual"
 PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
@@ -81,10 +81,12 @@ TILE_BYTES_PER_CELL = 50
 COARSE_CYCLE_CELLS = 1024
 
 
-def iteration_bytes(n0, n1, levels):
+def iteration_bytes(n0, n1, levels, cycles=1):
+    """Algorithmic bytes of one outer iteration: the FP64 outer step plus
+    `cycles` FP32 V-cycles."""
     cells = [(n0 >> l) * (n1 >> l) for l in range(levels)]
     tiled = sum(c for l, c in enumerate(cells) if c > COARSE_CYCLE_CELLS and l < levels - 1)
-    return OUTER_BYTES_PER_CELL * cells[0] + TILE_BYTES_PER_CELL * tiled
+    return OUTER_BYTES_PER_CELL * cells[0] + cycles * TILE_BYTES_PER_CELL * tiled
 
 
 class Clocks:
@@ -251,7 +253,8 @@ def run_gpu(args):
     # graph loop; their individual shares come from the ncu launch list)
     hbm, kind = peaks()
     it_us = ms_mixed * 1e3 / max(it_mixed, 1)
-    alg_bytes = iteration_bytes(g.n[0], g.n[1], st_mixed.levels)
+    cyc_per_it = st_mixed.cycles / max(st_mixed.iterations, 1)
+    alg_bytes = iteration_bytes(g.n[0], g.n[1], st_mixed.levels, round(cyc_per_it))
     achieved = alg_bytes / (it_us * 1e-6) / 1e9
     clocks = clk.summary()
     value = upd_mixed / (ms_mixed * 1e-3) * world

@@ -155,7 +155,9 @@ typedef struct mlgpu_mg_options {
   int max_coarse;        /* s_maxCoarse: coarsen while coarsenable(2^d * max_coarse) */
   int prolong;           /* MLGPU_PROLONG_* */
   int precision;         /* MLGPU_PREC_F64 or MLGPU_PREC_MIXED */
-  int inner_cycles;      /* mixed: FP32 cycles per FP64 defect-correction step */
+  int inner_cycles;      /* V-cycles per outer iteration (FP32 cycles per FP64
+                            defect-correction step in mixed precision); 0
+                            (default): 3 in mixed precision, 1 in FP64 */
   int norm_type;         /* MLGPU_NORM_MAX (reference default) or L2 */
   int use_graph;         /* 0: plain launches; 1: one outer iteration captured in a
                             CUDA graph and replayed; 2 (default): the whole outer

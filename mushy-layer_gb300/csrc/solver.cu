@@ -197,6 +197,11 @@ struct VCLevel {
 
 class VCSolver : public mlgpu_solver {
  public:
+  // V-cycles per outer iteration: the option, or by default 3 in mixed
+  // precision (amortises the FP64 outer step over more FP32 cycles; the
+  // convergence test stays on the FP64 residual) and 1 in FP64 (the
+  // reference's one cycle per AMRMultiGrid iteration)
+  int inner_cycles() const { return o.inner_cycles > 0 ? o.inner_cycles : (mixed ? 3 : 1); }
   mlgpu_vcop op;
   mlgpu_mg_options o;
   std::vector<VCLevel> L;
@@ -343,7 +348,7 @@ class VCSolver : public mlgpu_solver {
     double u = 0;
     int last = (int)L.size() - 1;
     std::vector<double> visits(L.size(), 0);
-    visits[0] = std::max(1, o.inner_cycles);
+    visits[0] = inner_cycles();
     for (int l = 1; l <= last; l++) visits[l] = visits[l - 1] * o.num_mg;
     for (int l = 0; l <= last; l++) {
       double n = (double)L[l].G.ncell;
@@ -607,7 +612,7 @@ class VCSolver : public mlgpu_solver {
   // the loop runs on the device, and then the decision kernel ends the body
   int iteration(int from, const int *par = nullptr, cudaGraphConditionalHandle h = 0) {
     int rc;
-    int cycles = std::max(1, o.inner_cycles);
+    int cycles = inner_cycles();
     for (int c = 0; c < cycles; c++) {
       rc = mixed ? cycle<float>(0, c == 0) : cycle<double>(0, c == 0);
       if (rc) return rc;
@@ -748,7 +753,7 @@ class VCSolver : public mlgpu_solver {
         S.status = host_state->status;
         for (int i = 1; i <= S.iter && i < 64; i++) st->norm_history[i] = host_state->hist[i];
         cur = host_state->parity;
-        st->cycles = S.iter * std::max(1, o.inner_cycles);
+        st->cycles = S.iter * inner_cycles();
         st->cell_updates += S.iter * updates_per_iter;
         st->kernel_launches += (double)S.iter * kern_loop;
       }
@@ -759,7 +764,7 @@ class VCSolver : public mlgpu_solver {
       CK(cudaStreamSynchronize(s));
       cur = 1 - cur;
       S.norm = *host_norm;
-      st->cycles += std::max(1, o.inner_cycles);
+      st->cycles += inner_cycles();
       st->cell_updates += updates_per_iter;
       st->kernel_launches += kern_iter;
       outer_after(o, S, st);
@@ -1520,7 +1525,7 @@ void mlgpu_mg_default_options(mlgpu_mg_options *o, int hc) {
   o->max_coarse = 2;
   o->prolong = hc ? MLGPU_PROLONG_LINEAR : MLGPU_PROLONG_CONSTANT;
   o->precision = MLGPU_PREC_F64;
-  o->inner_cycles = 1;
+  o->inner_cycles = 0;
   o->norm_type = MLGPU_NORM_MAX;
   o->use_graph = 2;
   o->fuse_levels = 1;

@@ -1274,7 +1274,7 @@ void orc_mg_default_options(mlgpu_mg_options *o, int hc) {
   o->max_coarse = 2;
   o->prolong = hc ? MLGPU_PROLONG_LINEAR : MLGPU_PROLONG_CONSTANT;
   o->precision = MLGPU_PREC_F64;
-  o->inner_cycles = 1;
+  o->inner_cycles = 0;
   o->norm_type = MLGPU_NORM_MAX;
   o->use_graph = 0;
   o->fuse_levels = 1;
