@@ -416,6 +416,10 @@ def test_vc_fused_levels_match_unfused_multiwave(mixed):
         o = ops.default_options(False)
         o.tolerance, o.hang, o.max_iter, o.fuse_levels = 1e-30, 0.0, 6, fuse
         o.precision = abi.PREC_MIXED if mixed else abi.PREC_F64
+        # one FP32 cycle per outer step: several cycles on one FP32
+        # correction reach the FP32 floor of this ill-conditioned operator,
+        # where the lean and the per-level forms stall at different levels
+        o.inner_cycles = 1
         d_phi = torch.zeros_like(dev(f))
         st, rc = ops.AMRMultiGrid(op, o).solve(d_phi, dev(f))
         out[fuse] = (host(d_phi), [st.norm_history[i] for i in range(7)])
@@ -441,6 +445,7 @@ def one_cycle_agrees(op, f, rel=2e-5, pre=None, post=None):
         o = ops.default_options(False)
         o.tolerance, o.hang, o.max_iter, o.fuse_levels = 1e-30, 0.0, 1, fuse
         o.precision = abi.PREC_MIXED
+        o.inner_cycles = 1
         if pre is not None:
             o.num_smooth_down, o.num_smooth_up = pre, post
         d_phi = torch.zeros_like(dev(f))
