@@ -622,8 +622,8 @@ def config5(args, torch, abi, ops, O, P):
             "fd_rel_err": {"max": max(rels), "per_direction": rels, "step": h},
             "dJ_dRa": gra, "dJ_dTb": gtb, "dJ_dlogk_abs_sum": float(gk.abs().sum()),
             "fd_wall_s": fd_s,
-            "solves_in_gradient": {"forward_fas": len(fwd_its),
-                                   "forward_fas_iterations_mean": float(np.mean(fwd_its)),
+            "solves_in_gradient": {"forward_steps": len(fwd_its),
+                                   "forward_newton_iterations_mean": float(np.mean(fwd_its)),
                                    "adjoint": len(adj_its),
                                    "adjoint_iterations_mean": float(np.mean(adj_its))},
             "config": {"workload": "2D 256x256 Darcy solidification, periodic x, T_b=0.5 / "

@@ -441,7 +441,8 @@ int mlgpu_hc_adjoint_solve(mlgpu_solver *S, const double *phi, const double *g, 
 /* The same object also solves N(phi) = rhs by Newton's method: each step
  * solves A(phi) d = rhs - N(phi) with V-cycles on A (the untransposed
  * operator, same hierarchy and block smoother) to 1e-3 relative, then
- * phi += d, halving d (at most 4 times) while the FP64 residual grows; the
+ * phi += d, halving d (at most 4 times) while the L2 norm of the FP64
+ * residual grows; the
  * options' tolerance / max_iter / hang apply to the FP64 residual, and three
  * consecutive steps that cut it by under 5% once it is below 1e-8 of its
  * start end the solve with the hang status (its round-off floor).  phi:

@@ -1337,12 +1337,22 @@ class HCAdjSolver : public mlgpu_solver {
   double lin_tol = 1e-3;
   int lin_max = 12;
 
-  // f - N(u) into L[0].g and its norm to the host
+  // f - N(u) into L[0].g; host_norm[0] = its norm of the options' kind (the
+  // stopping test), host_norm[1] = its L2 norm (the merit of the step
+  // halving: a max norm would halve every cell's step for the one cell that
+  // crosses a closure regime boundary)
   int nl_residual() {
-    CK(launch_nl_op<double>(make_nl_args<double>(op), NL_RESIDUAL, o.norm_type, L[0].u, nf,
+    const long long n2 = 2 * L[0].G.ncell;
+    CK(launch_nl_op<double>(make_nl_args<double>(op), NL_RESIDUAL, MLGPU_NORM_L2, L[0].u, nf,
                             L[0].g, nullptr, part, s));
-    CK(launch_finalize_norm(o.norm_type, part, norm_parts(L[0].G.ncell), part + kMaxBlocks, s));
-    CK(cudaMemcpyAsync(host_norm, part + kMaxBlocks, sizeof(double), cudaMemcpyDeviceToHost, s));
+    CK(launch_finalize_norm(MLGPU_NORM_L2, part, norm_parts(L[0].G.ncell), part + kMaxBlocks,
+                            s));
+    CK(cudaMemcpyAsync(host_norm + 1, part + kMaxBlocks, sizeof(double), cudaMemcpyDeviceToHost,
+                       s));
+    CK(launch_norm_partial<double>(n2, L[0].g, o.norm_type, part, s));
+    CK(launch_finalize_norm(o.norm_type, part, norm_parts(n2), part + kMaxBlocks + 1, s));
+    CK(cudaMemcpyAsync(host_norm, part + kMaxBlocks + 1, sizeof(double), cudaMemcpyDeviceToHost,
+                       s));
     CK(cudaStreamSynchronize(s));
     return MLGPU_OK;
   }
@@ -1363,6 +1373,7 @@ class HCAdjSolver : public mlgpu_solver {
     st->cell_updates = (double)L[0].G.ncell;
     if (!std::isfinite(S.norm0)) S.status = 8;
     int stall = 0;  // consecutive steps that cut the residual by under 5%
+    double merit = host_norm[1];
     while (outer_continue(o, S)) {
       rc = state_levels();
       if (rc) return rc;
@@ -1388,12 +1399,22 @@ class HCAdjSolver : public mlgpu_solver {
         rc = nl_residual();
         if (rc) return rc;
         st->cell_updates += (double)L[0].G.ncell;
-        if (std::isfinite(*host_norm) && *host_norm <= S.norm) break;
+        if (std::isfinite(host_norm[1]) && host_norm[1] <= merit) break;
         scale *= 0.5;
       }
-      S.norm = *host_norm;
+      const double merit_prev = merit;
+      merit = host_norm[1];
+      S.norm = host_norm[0];
       stall = S.norm >= 0.95 * S.prev ? stall + 1 : 0;
-      outer_after(o, S, st);
+      // as outer_after, with the stagnation test on the L2 merit (the max
+      // norm may rise while the step is accepted)
+      S.iter++;
+      if (S.iter < 64) st->norm_history[S.iter] = S.norm;
+      if (!std::isfinite(S.norm) || !std::isfinite(merit))
+        S.status = 8;
+      else if (merit > (1.0 - o.hang) * merit_prev && S.norm > o.tolerance * S.norm0)
+        S.status = 2;
+      S.prev = S.norm;
       // three stalled steps far below the start: the FP64 residual has
       // reached its round-off floor (stalls of the damped early steps, where
       // the closure's regime switches cut the step, do not count)
@@ -1721,7 +1742,7 @@ int mlgpu_hc_adjoint_create(const mlgpu_nlop *op, const mlgpu_mg_options *o, voi
     return MLGPU_ERR_WORKSPACE;
   }
   S->layout((char *)ws);
-  if (cudaHostAlloc((void **)&S->host_norm, sizeof(double), cudaHostAllocDefault) != cudaSuccess) {
+  if (cudaHostAlloc((void **)&S->host_norm, 2 * sizeof(double), cudaHostAllocDefault) != cudaSuccess) {
     delete S;
     return MLGPU_ERR_CUDA;
   }
