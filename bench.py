@@ -500,6 +500,18 @@ def config3(args, torch, abi, ops, O, P):
         step()
         ms, res = _events_ms(step)
         out[prec] = (ms, res)
+    # the (H, C) step solved to 1e-10 by Newton on the Jacobian hierarchy
+    # (the FAS solve above stops at the reference's 10-iteration cap)
+    on = ops.default_options(True)
+    on.tolerance, on.hang, on.max_iter = TOL, -1.0, 60
+    AN = ops.AdjointMultiGrid(hop, on)
+
+    def newton_step():
+        new = d_phi0.clone()
+        return AN.backwardEulerNewton(new, d_phi0, 1e-5), new
+
+    newton_step()
+    ms_newton, ((st_n, rc_n), h_newton) = _events_ms(newton_step)
     ms64, (h64, v64, u64, it64) = out["fp64"]
     msm, (hm, vm, um, itm) = out["mixed"]
     rel = lambda a, b: float((a - b).abs().max() / b.abs().max())
@@ -507,6 +519,9 @@ def config3(args, torch, abi, ops, O, P):
             "value": msm, "unit": "ms/step (mixed)", "higher_is_better": False,
             "fp64_ms": ms64, "ratio_fp64_over_mixed": ms64 / msm,
             "iterations": {"fp64": it64, "mixed": itm},
+            "hc_newton_to_1e-10": {"ms": ms_newton, "iterations": st_n.iterations, "rc": rc_n,
+                                   "final_rel_residual": st_n.final_norm / st_n.initial_norm,
+                                   "linear_cycles": st_n.cycles},
             "mixed_vs_fp64": {"hc_rel": rel(hm, h64),
                               "velocity_rel": max(rel(vm[c], v64[c]) for c in range(2)),
                               "mac_u_rel": max(rel(um[d], u64[d]) for d in range(2))},
@@ -670,6 +685,26 @@ def run_profile(args):
         print(json.dumps({"profile": "hc", "iterations": st.iterations,
                           "kernel_launches": st.kernel_launches}))
         return
+    if args.profile == "adjoint":
+        # one Newton backward-Euler step and its adjoint solve on the 256^2
+        # solidification state (the adjoint workload's first step), plain
+        # launches
+        from mushy_gb300 import darcy_model as M
+        model = M.DarcySolidification(256)
+        phi0 = M.initial_state(256, seed=5)
+        o = ops.default_options(True)
+        o.tolerance, o.hang, o.max_iter, o.use_graph = 1e-12, -1.0, 60, 0
+        A = ops.AdjointMultiGrid(model.hop, o)
+        new = phi0.clone()
+        st_n, rc_n = A.backwardEulerNewton(new, phi0, model.dt)
+        g_bar = torch.ones_like(new)
+        mu = torch.zeros_like(new)
+        _, _, _, st_a, rc_a = A.backwardEulerAdjoint(new, g_bar, model.dt, mu)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile": "adjoint", "newton_iterations": st_n.iterations,
+                          "newton_linear_cycles": st_n.cycles,
+                          "adjoint_cycles": st_a.iterations}))
+        return
     g, b, f = make_problem()
     dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
     op = ops.ProjectionOp(g, abi.make_bc(), 0.0, 1.0, None, [dev(x) for x in b])
@@ -694,7 +729,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--profile", choices=["mixed", "fp64", "hc"],
+    ap.add_argument("--profile", choices=["mixed", "fp64", "hc", "adjoint"],
                     help="run one short solve for a profiler and exit")
     ap.add_argument("--config", type=int, choices=[1, 3, 4, 5],
                     help="measure another configuration (one JSON line) and exit")
