@@ -279,6 +279,9 @@ __device__ __forceinline__ void adj_gs_cell(const AdjArgs<T> &A, T *y, const T *
 }
 
 enum { ADJ_APPLY = 0, ADJ_RESIDUAL = 1 };
+// bottom levels with at most this many unknowns (2 per cell) are solved
+// exactly (adj_bottom_direct_kernel)
+constexpr int kAdjDirectMax = 32;
 
 #if defined(MLGPU_FP64_UNIT) || defined(MLGPU_FP32_UNIT)
 // closure Jacobian of every cell in the kernels' precision
@@ -363,6 +366,71 @@ __global__ void __launch_bounds__(1024) adj_relax_block_kernel(AdjArgs<T> A, T *
         if (colour_cell(A.G, pass, t, i, j, k)) adj_gs_cell<T, DIM, TR>(A, y, g, i, j, k);
       }
       __syncthreads();
+    }
+}
+
+// Exact bottom solve of B y = g (B = A^T or A) when the level has at most
+// kAdjDirectMax unknowns: thread k evaluates column k of B as B e_k, cell by
+// cell, into the augmented matrix; Gaussian elimination with partial
+// pivoting (the first row of largest |pivot|), then back substitution by
+// thread 0.  A relaxation bottom of these tiny levels is a chain of ~80
+// dependent FP64 phases (0.5 ms for 40 sweeps on 2x2 cells).
+template <class T, int DIM, bool TR>
+__global__ void __launch_bounds__(kAdjDirectMax) adj_bottom_direct_kernel(
+    AdjArgs<T> A, T *__restrict__ y, const T *__restrict__ g) {
+  __shared__ T M[kAdjDirectMax][kAdjDirectMax + 1];
+  __shared__ T unit[kAdjDirectMax][kAdjDirectMax];
+  __shared__ int piv;
+  const long long nc = A.G.ncell;
+  const int n = (int)(2 * nc);
+  const int k = threadIdx.x;
+  if (k < n) {
+    for (int m = 0; m < n; m++) unit[k][m] = T(0);
+    unit[k][k] = T(1);
+    for (long long q = 0; q < nc; q++) {
+      int i, j, kk;
+      cell_ijk(A.G, q, i, j, kk);
+      T o[2], y0[2];
+      jac_cell<T, DIM, TR, false>(A, unit[k], i, j, kk, o, y0, nullptr);
+      M[q][k] = o[0];
+      M[q + nc][k] = o[1];
+    }
+    M[k][n] = g[k];
+  }
+  __syncthreads();
+  for (int p = 0; p < n; p++) {
+    if (k == 0) {
+      int best = p;
+      T bv = fabs(M[p][p]);
+      for (int r = p + 1; r < n; r++) {
+        const T v = fabs(M[r][p]);
+        if (v > bv) {
+          bv = v;
+          best = r;
+        }
+      }
+      piv = best;
+    }
+    __syncthreads();
+    const int pr = piv;
+    if (pr != p)
+      for (int col = k; col <= n; col += blockDim.x) {
+        const T t = M[p][col];
+        M[p][col] = M[pr][col];
+        M[pr][col] = t;
+      }
+    __syncthreads();
+    for (int r = p + 1 + k; r < n; r += blockDim.x) {
+      const T l = M[r][p] / M[p][p];
+      for (int col = p; col <= n; col++) M[r][col] = M[r][col] - l * M[p][col];
+    }
+    __syncthreads();
+  }
+  if (k == 0)
+    for (int r = n - 1; r >= 0; r--) {
+      T s = M[r][n];
+      for (int col = r + 1; col < n; col++) s = s - M[r][col] * y[col];
+      y[r] = s / M[r][r];
     }
 }
 

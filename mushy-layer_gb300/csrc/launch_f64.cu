@@ -251,6 +251,12 @@ cudaError_t launch_adj_relax_block(const AdjArgs<double> &A, double *y, const do
   MLGPU_TR_SWITCH(tr, MLGPU_DIM_SWITCH(A.G.dim, (adj_relax_block_kernel<double, DIM, TR><<<1, 1024, 0, s>>>(A, y, g, sweeps, zero))));
   return cudaGetLastError();
 }
+cudaError_t launch_adj_bottom_direct(const AdjArgs<double> &A, double *y, const double *g,
+                                     cudaStream_t s, bool tr) {
+  if (2 * A.G.ncell > kAdjDirectMax) return cudaErrorInvalidValue;
+  MLGPU_TR_SWITCH(tr, MLGPU_DIM_SWITCH(A.G.dim, (adj_bottom_direct_kernel<double, DIM, TR><<<1, kAdjDirectMax, 0, s>>>(A, y, g))));
+  return cudaGetLastError();
+}
 cudaError_t launch_adj_restrict(const AdjArgs<double> &A, const Geom &C, const double *y,
                                 const double *g, double *gc, cudaStream_t s, bool tr) {
   MLGPU_TR_SWITCH(tr, MLGPU_DIM_SWITCH(A.G.dim, (adj_restrict_kernel<double, DIM, TR><<<blocks_for(C.ncell), kBlock, 0, s>>>(A, C, y, g, gc))));

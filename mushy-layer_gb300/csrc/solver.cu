@@ -1170,7 +1170,8 @@ class HCSolver : public mlgpu_solver {
 // The hierarchy is the FAS solver's: coefficients coarsened the same way,
 // the state averaged down, J per level from its state; correction-scheme
 // V-cycles (block red/black smoothing, 2^D residual averaging, the solver's
-// prolongation with the adjoint variable's wall rule, single-CTA bottom
+// prolongation with the adjoint variable's wall rule; at the bottom an exact
+// dense solve when it has at most kAdjDirectMax unknowns, else single-CTA
 // relaxation) inside an FP64 residual loop.
 struct AdjLevel {
   mlgpu_grid grid;
@@ -1285,7 +1286,10 @@ class HCAdjSolver : public mlgpu_solver {
     const int last = (int)L.size() - 1;
     AdjArgs<double> A = args(l);
     if (l == last) {
-      CK(launch_adj_relax_block(A, L[l].y, L[l].g, o.bottom_max_iter, l > 0 ? 1 : 0, s, tr));
+      if (2 * L[l].G.ncell <= kAdjDirectMax)
+        CK(launch_adj_bottom_direct(A, L[l].y, L[l].g, s, tr));
+      else
+        CK(launch_adj_relax_block(A, L[l].y, L[l].g, o.bottom_max_iter, l > 0 ? 1 : 0, s, tr));
       return MLGPU_OK;
     }
     if (l > 0) CK(cudaMemsetAsync(L[l].y, 0, sizeof(double) * 2 * L[l].G.ncell, s));

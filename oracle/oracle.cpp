@@ -1731,11 +1731,65 @@ struct AdjSolver {
     }
     y.store(L[l].y.data());
   }
+  // exact bottom solve (at most 32 unknowns): columns A^T e_k, Gaussian
+  // elimination with partial pivoting (first largest |pivot|), back
+  // substitution -- the device's operation order
+  void direct(int l) {
+    mlgpu_nlop op = op_at(l);
+    AdjCtx X(op, L[l].u.data(), L[l].J.data());
+    const size_t nc = ncells(L[l].g);
+    const int n = (int)(2 * nc);
+    std::vector<double> M((size_t)n * (n + 1));
+    auto at = [&](int r, int c) -> double & { return M[(size_t)r * (n + 1) + c]; };
+    std::vector<double> e(n, 0.0);
+    for (int k = 0; k < n; k++) {
+      std::fill(e.begin(), e.end(), 0.0);
+      e[k] = 1.0;
+      Fab y;
+      adj_load(y, op, e.data());
+      for (int kk = 0; kk < L[l].g.n[2]; kk++)
+        for (int j = 0; j < L[l].g.n[1]; j++)
+          for (int i = 0; i < L[l].g.n[0]; i++) {
+            double o2[2];
+            adj_row(X, y, i, j, kk, o2, nullptr);
+            size_t q = cidx(L[l].g, i, j, kk, 0);
+            at((int)q, k) = o2[0];
+            at((int)(q + nc), k) = o2[1];
+          }
+      at(k, n) = L[l].gg[k];
+    }
+    for (int p = 0; p < n; p++) {
+      int best = p;
+      double bv = std::fabs(at(p, p));
+      for (int r = p + 1; r < n; r++) {
+        double v = std::fabs(at(r, p));
+        if (v > bv) {
+          bv = v;
+          best = r;
+        }
+      }
+      if (best != p)
+        for (int c = 0; c <= n; c++) std::swap(at(p, c), at(best, c));
+      for (int r = p + 1; r < n; r++) {
+        double lr = at(r, p) / at(p, p);
+        for (int c = p; c <= n; c++) at(r, c) = at(r, c) - lr * at(p, c);
+      }
+    }
+    for (int r = n - 1; r >= 0; r--) {
+      double s = at(r, n);
+      for (int c = r + 1; c < n; c++) s = s - at(r, c) * L[l].y[c];
+      L[l].y[r] = s / at(r, r);
+    }
+  }
+
   void cycle(int l) {
     const int last = (int)L.size() - 1;
     if (l > 0) std::fill(L[l].y.begin(), L[l].y.end(), 0.0);
     if (l == last) {
-      smooth(l, o.bottom_max_iter);
+      if (2 * ncells(L[l].g) <= 32)
+        direct(l);
+      else
+        smooth(l, o.bottom_max_iter);
       updates += (double)o.bottom_max_iter * ncells(L[l].g);
       return;
     }
