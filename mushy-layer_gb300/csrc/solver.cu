@@ -1361,14 +1361,22 @@ class HCAdjSolver : public mlgpu_solver {
     return MLGPU_OK;
   }
 
+  // the cycles run on A for the duration of a Newton solve, on A^T otherwise
+  // (also after an error return)
+  struct ForwardMode {
+    bool &tr;
+    explicit ForwardMode(bool &t) : tr(t) { tr = false; }
+    ~ForwardMode() { tr = true; }
+  };
+
   int newton(double *user_u, const double *user_f, mlgpu_solve_stats *st) {
+    ForwardMode mode(tr);
     const long long n2 = 2 * L[0].G.ncell;
     const size_t bytes = sizeof(double) * n2;
     cudaGetLastError();
     if (enter()) return MLGPU_ERR_CUDA;
     CK(cudaMemcpyAsync(L[0].u, user_u, bytes, cudaMemcpyDeviceToDevice, s));
     CK(cudaMemcpyAsync(nf, user_f, bytes, cudaMemcpyDeviceToDevice, s));
-    tr = false;
     int rc = nl_residual();
     if (rc) return rc;
     Outer S;
@@ -1426,7 +1434,6 @@ class HCAdjSolver : public mlgpu_solver {
     }
     CK(cudaMemcpyAsync(user_u, L[0].u, bytes, cudaMemcpyDeviceToDevice, s));
     CK(cudaStreamSynchronize(s));
-    tr = true;
     if (leave()) return MLGPU_ERR_CUDA;
     return outer_finish(o, S, st);
   }
