@@ -37,6 +37,10 @@ struct AdjArgs {
   const T *b[3];        // [2][faces_d]
   const T *J;           // [4][cells]: dT/dH, dT/dC, dC_l/dH, dC_l/dC
   const double *u;      // [2][cells] state (ghost Jacobians of the (H, C) condition)
+  // [4][cells] inverse of each cell's 2x2 diagonal block M of A^T (row-major;
+  // A's block is its transpose), precomputed once per state, or null:
+  // the smoother then forms and inverts M inline
+  const T *Minv = nullptr;
 };
 
 // Jacobian of the closure at the (H, C)-condition ghost of cell q across
@@ -269,6 +273,23 @@ __device__ __forceinline__ void jac_cell(const AdjArgs<T> &A, const T *y, int i,
 template <class T, int DIM, bool TR = true>
 __device__ __forceinline__ void adj_gs_cell(const AdjArgs<T> &A, T *y, const T *g, int i, int j,
                                             int k) {
+  if (A.Minv) {
+    // stored inverse (of M; the transpose serves A): no block assembly and
+    // no division in the sweep
+    T out[2], y0[2];
+    jac_cell<T, DIM, TR, false>(A, y, i, j, k, out, y0, nullptr);
+    const long long q = A.G.cell(i, j, k), n = A.G.ncell;
+    const T r0 = g[q] - out[0], r1 = g[q + n] - out[1];
+    const T m0 = A.Minv[q], m1 = A.Minv[q + n], m2 = A.Minv[q + 2 * n], m3 = A.Minv[q + 3 * n];
+    if (TR) {
+      y[q] = y0[0] + (m0 * r0 + m1 * r1);
+      y[q + n] = y0[1] + (m2 * r0 + m3 * r1);
+    } else {
+      y[q] = y0[0] + (m0 * r0 + m2 * r1);
+      y[q + n] = y0[1] + (m1 * r0 + m3 * r1);
+    }
+    return;
+  }
   T out[2], y0[2], M[4];
   jac_cell<T, DIM, TR, true>(A, y, i, j, k, out, y0, M);
   const long long q = A.G.cell(i, j, k), n = A.G.ncell;
@@ -308,6 +329,25 @@ __global__ void __launch_bounds__(kBlock) porosity_jac_kernel(Geom G, ClosurePar
     porosity_jac(u[q], u[q + n], cp, d2);
     dp[q] = d2[0];
     dp[q + n] = d2[1];
+  }
+}
+
+// the inverse of every cell's diagonal block M of A^T: {M3, -M1, -M2, M0}/det
+template <class T, int DIM>
+__global__ void __launch_bounds__(kBlock) adj_minv_kernel(AdjArgs<T> A, const T *__restrict__ zero,
+                                                          T *__restrict__ Minv) {
+  const Geom &G = A.G;
+  const long long n = G.ncell;
+  for (long long q = gtid(); q < n; q += gstride()) {
+    int i, j, k;
+    cell_ijk(G, q, i, j, k);
+    T out[2], y0[2], M[4];
+    adj_cell<T, DIM, true>(A, zero, i, j, k, out, y0, M);
+    const T det = M[0] * M[3] - M[1] * M[2];
+    Minv[q] = M[3] / det;
+    Minv[q + n] = -M[1] / det;
+    Minv[q + 2 * n] = -M[2] / det;
+    Minv[q + 3 * n] = M[0] / det;
   }
 }
 

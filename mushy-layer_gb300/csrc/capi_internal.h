@@ -66,6 +66,9 @@ cudaError_t launch_adj_restrict(const AdjArgs<double> &A, const Geom &C, const d
                                 const double *g, double *gc, cudaStream_t s, bool tr = true);
 cudaError_t launch_adj_bottom_direct(const AdjArgs<double> &A, double *y, const double *g,
                                      cudaStream_t s, bool tr = true);
+// inverse diagonal blocks of A^T per cell (`zero`: a zero field of the level)
+cudaError_t launch_adj_minv(const AdjArgs<double> &A, const double *zero, double *Minv,
+                            cudaStream_t s);
 cudaError_t launch_adj_bc_grad(const AdjArgs<double> &A, const double *y, double *out,
                                cudaStream_t s);
 cudaError_t launch_outer_coefs(const VCArgs<double> &A, double *cx, double *cy, double *diag,

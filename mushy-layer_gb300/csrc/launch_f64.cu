@@ -251,6 +251,11 @@ cudaError_t launch_adj_relax_block(const AdjArgs<double> &A, double *y, const do
   MLGPU_TR_SWITCH(tr, MLGPU_DIM_SWITCH(A.G.dim, (adj_relax_block_kernel<double, DIM, TR><<<1, 1024, 0, s>>>(A, y, g, sweeps, zero))));
   return cudaGetLastError();
 }
+cudaError_t launch_adj_minv(const AdjArgs<double> &A, const double *zero, double *Minv,
+                            cudaStream_t s) {
+  MLGPU_DIM_SWITCH(A.G.dim, (adj_minv_kernel<double, DIM><<<blocks_for(A.G.ncell), kBlock, 0, s>>>(A, zero, Minv)));
+  return cudaGetLastError();
+}
 cudaError_t launch_adj_bottom_direct(const AdjArgs<double> &A, double *y, const double *g,
                                      cudaStream_t s, bool tr) {
   if (2 * A.G.ncell > kAdjDirectMax) return cudaErrorInvalidValue;

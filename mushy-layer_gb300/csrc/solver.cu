@@ -1178,6 +1178,7 @@ struct AdjLevel {
   Geom G;
   Coefs<double> c64;
   double *u = nullptr, *J = nullptr, *y = nullptr, *g = nullptr, *r = nullptr;
+  double *Minv = nullptr;  // inverse diagonal blocks of A^T, per state
 };
 
 class HCAdjSolver : public mlgpu_solver {
@@ -1219,6 +1220,7 @@ class HCAdjSolver : public mlgpu_solver {
       }
       L[l].u = A.get<double>(n);
       L[l].J = A.get<double>(2 * n);
+      L[l].Minv = A.get<double>(2 * n);
       L[l].y = A.get<double>(n);
       L[l].g = A.get<double>(n);
       L[l].r = A.get<double>(n);
@@ -1253,7 +1255,9 @@ class HCAdjSolver : public mlgpu_solver {
     lop.grid = L[l].grid;
     lop.aCoef = L[l].c64.a;
     for (int d = 0; d < 3; d++) lop.bCoef[d] = L[l].c64.b[d];
-    return make_adj_args(lop, L[l].u, L[l].J);
+    AdjArgs<double> A = make_adj_args(lop, L[l].u, L[l].J);
+    A.Minv = L[l].Minv;
+    return A;
   }
 
   // the wall rule of the adjoint variable in the prolongation
@@ -1271,6 +1275,11 @@ class HCAdjSolver : public mlgpu_solver {
       CK(launch_restrict_avg<double>(L[l - 1].G, 2, L[l - 1].u, L[l].u, s));
     const ClosureParams cp = make_cp(op.params);
     for (auto &lv : L) CK(launch_adj_jac(lv.G, cp, lv.u, lv.J, s));
+    // the smoother's inverse diagonal blocks (r is free here: a zero field)
+    for (size_t l = 0; l < L.size(); l++) {
+      CK(cudaMemsetAsync(L[l].r, 0, sizeof(double) * 2 * L[l].G.ncell, s));
+      CK(launch_adj_minv(args((int)l), L[l].r, L[l].Minv, s));
+    }
     return MLGPU_OK;
   }
 

@@ -1550,21 +1550,53 @@ void adj_load(Fab &y, const mlgpu_nlop &op, const double *yd) {
   adj_fill(y, op);
 }
 
+// inverse of every cell's diagonal block M of A^T, {M3, -M1, -M2, M0}/det
+// (the driver's smoother stores it once per state)
+void adj_minv(const AdjCtx &X, double *Minv) {
+  const mlgpu_grid &gr = X.op.grid;
+  Fab z;
+  std::vector<double> zero(2 * X.n, 0.0);
+  adj_load(z, X.op, zero.data());
+  for (int k = 0; k < gr.n[2]; k++)
+    for (int j = 0; j < gr.n[1]; j++)
+      for (int i = 0; i < gr.n[0]; i++) {
+        double out[2], M[4];
+        adj_row(X, z, i, j, k, out, M);
+        size_t q = cidx(gr, i, j, k, 0);
+        double det = M[0] * M[3] - M[1] * M[2];
+        Minv[q] = M[3] / det;
+        Minv[q + X.n] = -M[1] / det;
+        Minv[q + 2 * X.n] = -M[2] / det;
+        Minv[q + 3 * X.n] = M[0] / det;
+      }
+}
+
 // one red/black pass of the block smoother: each cell of the colour solves
-// its two rows exactly, y += M^-1 (g - A^T y)
-void adj_gsrb_pass_fab(Fab &y, const AdjCtx &X, const double *g, int pass) {
+// its two rows exactly, y += M^-1 (g - A^T y); with Minv given the stored
+// inverse is applied, else M is formed and inverted inline
+void adj_gsrb_pass_fab(Fab &y, const AdjCtx &X, const double *g, int pass,
+                       const double *Minv = nullptr) {
   const mlgpu_grid &gr = X.op.grid;
   adj_fill(y, X.op);
   for (int k = 0; k < gr.n[2]; k++)
     for (int j = 0; j < gr.n[1]; j++) {
       int imin = std::abs((j + k + pass) % 2);
       for (int i = imin; i < gr.n[0]; i += 2) {
+        size_t q = cidx(gr, i, j, k, 0);
+        double y0 = y(i, j, k, 0), y1 = y(i, j, k, 1);
+        if (Minv) {
+          double out[2];
+          adj_row(X, y, i, j, k, out, nullptr);
+          double r0 = g[q] - out[0], r1 = g[q + X.n] - out[1];
+          double m0 = Minv[q], m1 = Minv[q + X.n], m2 = Minv[q + 2 * X.n], m3 = Minv[q + 3 * X.n];
+          y(i, j, k, 0) = y0 + (m0 * r0 + m1 * r1);
+          y(i, j, k, 1) = y1 + (m2 * r0 + m3 * r1);
+          continue;
+        }
         double out[2], M[4];
         adj_row(X, y, i, j, k, out, M);
-        size_t q = cidx(gr, i, j, k, 0);
         double r0 = g[q] - out[0], r1 = g[q + X.n] - out[1];
         double det = M[0] * M[3] - M[1] * M[2];
-        double y0 = y(i, j, k, 0), y1 = y(i, j, k, 1);
         y(i, j, k, 0) = y0 + (M[3] * r0 - M[1] * r1) / det;
         y(i, j, k, 1) = y1 + (M[0] * r1 - M[2] * r0) / det;
       }
@@ -1683,7 +1715,7 @@ void lin_gsrb_pass(const AdjCtx &X, double *xd, const double *r, int pass) {
 // ---- multigrid for A^T y = g (the device driver restated)
 struct AdjLevelO {
   mlgpu_grid g;
-  std::vector<double> a, b[3], u, J, y, gg, r;
+  std::vector<double> a, b[3], u, J, y, gg, r, Minv;
 };
 
 struct AdjSolver {
@@ -1718,6 +1750,12 @@ struct AdjSolver {
     for (size_t l = 1; l < L.size(); l++)
       orc_restrict_average(&L[l - 1].g, 2, L[l].u.data(), L[l - 1].u.data());
     for (auto &lv : L) orc_closure_jac(&lv.g, &op0.params, lv.u.data(), lv.J.data());
+    for (size_t l = 0; l < L.size(); l++) {
+      L[l].Minv.assign(2 * L[l].u.size(), 0.0);
+      mlgpu_nlop op = op_at((int)l);
+      AdjCtx X(op, L[l].u.data(), L[l].J.data());
+      adj_minv(X, L[l].Minv.data());
+    }
   }
   void smooth(int l, int n) {
     mlgpu_nlop op = op_at(l);
@@ -1726,8 +1764,8 @@ struct AdjSolver {
     y.define(op.grid, 2);
     y.load(L[l].y.data());
     for (int s = 0; s < n; s++) {
-      adj_gsrb_pass_fab(y, X, L[l].gg.data(), 0);
-      adj_gsrb_pass_fab(y, X, L[l].gg.data(), 1);
+      adj_gsrb_pass_fab(y, X, L[l].gg.data(), 0, L[l].Minv.data());
+      adj_gsrb_pass_fab(y, X, L[l].gg.data(), 1, L[l].Minv.data());
     }
     y.store(L[l].y.data());
   }
