@@ -393,3 +393,15 @@ def test_temperature_conditions_rejected_off_enthalpy():
     vc.bc = abi.make_bc({(1, 1, 0): (abi.BC_FIXED_TEMPERATURE, 0.0)})
     lib.mlgpu_mg_default_options(C.byref(opts), 0)
     assert lib.mlgpu_vc_solver_workspace(C.byref(vc), C.byref(opts), C.byref(nbytes)) == abi.ERR_ARG
+
+
+def test_temperature_condition_large_residual_is_zeroed():
+    """NonlinearTemperatureBCRobin zeroes a residual above 10 (the reference
+    warns and leaves the ghost enthalpy at its guess): a fixed temperature 20
+    above the interior gives the interior enthalpy as ghost, i.e. no flux."""
+    spec = {(0, 0, 0): (abi.BC_FIXED_TEMPERATURE, 25.0)}
+    for method in (abi.NLBC_PICARD, abi.NLBC_NEWTON):
+        Tg, T0, _ = _ghost_temperature(abi.make_nlbc(method=method), spec, LIQUID, (0, 3),
+                                       (0, 0))
+        assert Tg == T0
+
