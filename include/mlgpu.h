@@ -192,7 +192,7 @@ typedef struct mlgpu_solver mlgpu_solver;  /* opaque */
 const char *mlgpu_status_string(int status);
 int mlgpu_version(void);
 
-/* ------------------------------------------------ closure (a1-a5) -------
+/* ------------------------------------------------------------ closure -------
  * Full enthalpy closure H, C -> T, porosity, C_l, C_s and the bounding
  * energies, FP64 on every cell.  Replaces updateEnthalpyVariables
  * (src/phaseDiagram.cpp:92-177) and the Fortran CALCULATE_BOUNDING_ENERGY /
@@ -210,7 +210,7 @@ int mlgpu_closure(const mlgpu_grid *grid, const mlgpu_params *p,
 int mlgpu_closure_tcl(const mlgpu_grid *grid, const mlgpu_params *p,
                       const double *HC, double *TCl, void *stream);
 
-/* ---------------------------------------- nonlinear operator (a6-a12) --- */
+/* ------------------------------------------------- nonlinear operator --- */
 /* Bytes of device scratch the fused norms need (norm_type >= 0 below). */
 size_t mlgpu_norm_workspace_bytes(void);
 
@@ -252,7 +252,7 @@ int mlgpu_nl_lambda(const mlgpu_nlop *op, void *lambda, void *stream);
 int mlgpu_nl_restrict_residual(const mlgpu_nlop *op, void *res_coarse,
                                const void *phi, const void *rhs, void *stream);
 
-/* -------------------------------------------- transfers (a12-a15, a18) -- */
+/* ----------------------------------------------------------- transfers -- */
 /* phi_c = avg_{2^D} phi_f for ncomp components (restrictR :492-514 ->
  * RESTRICT F.ChF:555-585; also CoarseAverage for cell coefficients). */
 int mlgpu_restrict_average(const mlgpu_grid *fine, int ncomp, int dtype,
@@ -277,7 +277,7 @@ int mlgpu_coarsen_faces(const mlgpu_grid *fine, int ncomp, int dtype, int dir,
 int mlgpu_face_geomean(const mlgpu_grid *grid, const double *cell,
                        double *faces[3], void *stream);
 
-/* ----------------------------------- linear operators (a16, a17, a19) -- */
+/* ---------------------------------------------------- linear operators -- */
 /* res = rhs - L(phi) for the projection (c == NULL) or Darcy-Brinkman op:
  * VCCOMPUTERES / DBCOMPUTERES (src/DarcyBrinkmanOpF.ChF:299-396). */
 int mlgpu_vc_residual(const mlgpu_vcop *op, void *res, const void *phi,
@@ -308,7 +308,7 @@ int mlgpu_vc_lambda(const mlgpu_vcop *op, void *lambda, void *stream);
 int mlgpu_vc_restrict_residual(const mlgpu_vcop *op, void *res_coarse,
                                const void *phi, const void *rhs, void *stream);
 
-/* ------------------------------------ MAC projection pieces (8f row 1) -- */
+/* ----------------------------------------------- MAC projection pieces -- */
 /* div = sum_d (u_d[i+e_d] - u_d[i]) / dx  (DIVERGENCE, util/DivergenceF.ChF) */
 int mlgpu_mac_divergence(const mlgpu_grid *grid, double *div,
                          const double *u[3], void *stream);
@@ -389,6 +389,18 @@ int mlgpu_mac_project(mlgpu_solver *S, const mlgpu_grid *grid, const mlgpu_bc *p
 int mlgpu_hc_backward_euler(mlgpu_solver *S, double *phi_new, const double *phi_old,
                             const double *src, const double *aCoef, double dt,
                             double *rhs_scratch, mlgpu_solve_stats *stats);
+
+/* ----------------------------------------------- device memory helpers
+ * For hosts that link only libmlgpu.so (no CUDA runtime of their own, e.g.
+ * the C++ classes of mlgpu.hpp or a Fortran stepper): these are the only
+ * entry points that allocate or free device memory.  kind: 0 host to
+ * device, 1 device to host, 2 device to device; copies are asynchronous on
+ * `stream` (NULL: the legacy default stream). */
+int mlgpu_device_alloc(size_t bytes, void **ptr);
+int mlgpu_device_free(void *ptr);
+int mlgpu_memcpy(void *dst, const void *src, size_t bytes, int kind, void *stream);
+int mlgpu_memset_zero(void *ptr, size_t bytes, void *stream);
+int mlgpu_stream_synchronize(void *stream);
 
 /* ------------------------------------------------------------ adjoint
  * Discrete adjoint of the path (no counterpart in the reference, which has

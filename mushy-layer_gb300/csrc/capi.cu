@@ -198,6 +198,36 @@ int mlgpu_closure_tcl(const mlgpu_grid *g, const mlgpu_params *p, const double *
   return status_of(launch_closure_tcl(G.ncell, make_cp(*p), HC, TCl, (cudaStream_t)stream));
 }
 
+int mlgpu_device_alloc(size_t bytes, void **ptr) {
+  if (!ptr) return MLGPU_ERR_ARG;
+  *ptr = nullptr;
+  if (bytes == 0) return MLGPU_OK;
+  return status_of(cudaMalloc(ptr, bytes));
+}
+
+int mlgpu_device_free(void *ptr) { return ptr ? status_of(cudaFree(ptr)) : MLGPU_OK; }
+
+int mlgpu_memcpy(void *dst, const void *src, size_t bytes, int kind, void *stream) {
+  if ((!dst || !src) && bytes) return MLGPU_ERR_ARG;
+  cudaMemcpyKind k = kind == 0   ? cudaMemcpyHostToDevice
+                     : kind == 1 ? cudaMemcpyDeviceToHost
+                     : kind == 2 ? cudaMemcpyDeviceToDevice
+                                 : cudaMemcpyDefault;
+  if (kind < 0 || kind > 2) return MLGPU_ERR_ARG;
+  if (!bytes) return MLGPU_OK;
+  return status_of(cudaMemcpyAsync(dst, src, bytes, k, (cudaStream_t)stream));
+}
+
+int mlgpu_memset_zero(void *ptr, size_t bytes, void *stream) {
+  if (!ptr && bytes) return MLGPU_ERR_ARG;
+  if (!bytes) return MLGPU_OK;
+  return status_of(cudaMemsetAsync(ptr, 0, bytes, (cudaStream_t)stream));
+}
+
+int mlgpu_stream_synchronize(void *stream) {
+  return status_of(cudaStreamSynchronize((cudaStream_t)stream));
+}
+
 int mlgpu_closure_jacobian(const mlgpu_grid *g, const mlgpu_params *p, const double *HC,
                            double *J, void *stream) {
   if (!valid_grid(g) || !p || !HC || !J) return MLGPU_ERR_ARG;

@@ -204,6 +204,11 @@ def _declare(lib):
         "mlgpu_mac_project": (i, [vp, P(Grid), P(BC), vp * 3, vp * 3, vp, vp, P(SolveStats)]),
         "mlgpu_hc_backward_euler": (i, [vp, vp, vp, vp, vp, d, vp, P(SolveStats)]),
         "mlgpu_closure_jacobian": (i, [P(Grid), P(Params), vp, vp, vp]),
+        "mlgpu_device_alloc": (i, [sz, P(vp)]),
+        "mlgpu_device_free": (i, [vp]),
+        "mlgpu_memcpy": (i, [vp, vp, sz, i, vp]),
+        "mlgpu_memset_zero": (i, [vp, sz, vp]),
+        "mlgpu_stream_synchronize": (i, [vp]),
         "mlgpu_hc_solver_set_bcs": (i, [vp, P(BC), P(BC)]),
         "mlgpu_porosity_jacobian": (i, [P(Grid), P(Params), vp, vp, vp]),
         "mlgpu_hc_adjoint_apply": (i, [P(NLOp), vp, vp, vp, vp, vp, vp]),
