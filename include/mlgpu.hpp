@@ -434,7 +434,50 @@ class AdjointMultiGrid : public Solver {
     tolerate(rc, "AdjointMultiGrid::newtonSolve");
     return st;
   }
+  // adjoint of AMRFASMultiGrid::backwardEuler: A^T mu = phi_new_bar, then
+  // phi_old_bar = a mu, src_bar = dt mu and the wall-value gradient
+  // (bc_grad[(dir * 2 + side) * 2 + comp]); outputs may be null
+  mlgpu_solve_stats backwardEulerAdjoint(const DeviceField &phi_new,
+                                         const DeviceField &phi_new_bar, double dt,
+                                         DeviceField &mu, DeviceField *phi_old_bar,
+                                         DeviceField *src_bar, double bc_grad[12] = nullptr,
+                                         const DeviceField *aCoef = nullptr) {
+    mlgpu_solve_stats st;
+    int rc = mlgpu_hc_backward_euler_adjoint(
+        h_, (const double *)phi_new.data(), (const double *)phi_new_bar.data(),
+        aCoef ? (const double *)aCoef->data() : nullptr, dt, (double *)mu.data(),
+        phi_old_bar ? (double *)phi_old_bar->data() : nullptr,
+        src_bar ? (double *)src_bar->data() : nullptr, bc_grad, &st);
+    tolerate(rc, "AdjointMultiGrid::backwardEulerAdjoint");
+    return st;
+  }
 };
+
+// adjoint of AMRMultiGrid::levelMacProject on the solver `mg` that ran the
+// forward: ustar_bar = ubar - D^T q with D Pi G q = G^T (Pi ubar), and
+// pi_bar = -ustar_bar (G p) when pi_bar is given (p: the forward pressure)
+inline mlgpu_solve_stats macProjectAdjoint(AMRMultiGrid &mg, const mlgpu_grid &grid,
+                                           const mlgpu_bc &bc, const DeviceField *ubar[3],
+                                           const DeviceField *pi_face[3], const DeviceField &p,
+                                           DeviceField *ustar_bar[3], DeviceField *pi_bar[3],
+                                           DeviceField &q) {
+  DeviceField scratch(grid, 1);
+  const double *ub[3] = {nullptr, nullptr, nullptr}, *pf[3] = {nullptr, nullptr, nullptr};
+  double *us[3] = {nullptr, nullptr, nullptr}, *pb[3] = {nullptr, nullptr, nullptr};
+  for (int d = 0; d < grid.dim; d++) {
+    ub[d] = (const double *)ubar[d]->data();
+    us[d] = (double *)ustar_bar[d]->data();
+    if (pi_face) pf[d] = (const double *)pi_face[d]->data();
+    if (pi_bar) pb[d] = (double *)pi_bar[d]->data();
+  }
+  mlgpu_solve_stats st;
+  int rc = mlgpu_mac_project_adjoint(mg.handle(), &grid, &bc, ub, pi_face ? pf : nullptr,
+                                     (const double *)p.data(), us, pi_bar ? pb : nullptr,
+                                     (double *)q.data(), (double *)scratch.data(), &st);
+  if (rc != MLGPU_OK && rc != MLGPU_ERR_NOT_CONVERGED && rc != MLGPU_ERR_HANG)
+    check(rc, "macProjectAdjoint");
+  return st;
+}
 
 }  // namespace mlgpu
 
