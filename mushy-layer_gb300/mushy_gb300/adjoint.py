@@ -15,7 +15,8 @@ hand-written adjoint kernels:
 
 ``checkpointed(steps, ...)`` runs a time loop keeping only every k-th state
 and recomputes a segment during the backward sweep (two-level checkpointing;
-the recomputation is bitwise deterministic).
+the recomputation is bitwise deterministic); ``revolve(...)`` reverses the
+loop with a bounded number of snapshots on the optimal binomial schedule.
 """
 import torch
 import torch.utils.checkpoint as tcp
@@ -166,3 +167,102 @@ def checkpointed(step, state, nsteps, every, *params):
             state = segment(k)(state, *params)
         done += k
     return state
+
+
+# ------------------------------------------------ binomial (revolve) schedule
+def revolve_schedule(n, s):
+    """Optimal reversal of an n-step chain holding at most `s` snapshots
+    besides the chain's first state (the recursive scheme of binomial
+    checkpointing): reversing steps [a, b) costs
+        cost(1, s) = 1,   cost(n, 0) = n (n + 1) / 2,
+        cost(n, s) = min_m  m + cost(n - m, s - 1) + cost(m, s),
+    i.e. advance m steps to a new snapshot, reverse the tail with one
+    snapshot fewer, then reverse the head.  Returns (cost table, split
+    table) indexed [n][s]; split[n][s] is the best m (0 for the base
+    cases).  Costs count step evaluations during the reversal."""
+    INF = float("inf")
+    cost = [[0] * (s + 1) for _ in range(n + 1)]
+    split = [[0] * (s + 1) for _ in range(n + 1)]
+    for k in range(1, n + 1):
+        for j in range(s + 1):
+            if k == 1:
+                cost[k][j] = 1
+            elif j == 0:
+                cost[k][j] = k * (k + 1) // 2
+            else:
+                best, arg = INF, 1
+                for m in range(1, k):
+                    c = m + cost[k - m][j - 1] + cost[m][j]
+                    if c < best:
+                        best, arg = c, m
+                cost[k][j] = best
+                split[k][j] = arg
+    return cost, split
+
+
+class _Revolve(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, step, nsteps, snapshots, state, *params):
+        with torch.no_grad():
+            s = state
+            for _ in range(nsteps):
+                s = step(s, *params)
+        ctx.step, ctx.n, ctx.snaps = step, nsteps, snapshots
+        ctx.save_for_backward(state, *params)
+        return s
+
+    @staticmethod
+    def backward(ctx, g):
+        state0, *params = ctx.saved_tensors
+        step = ctx.step
+        _, split = revolve_schedule(ctx.n, ctx.snaps)
+        pgrads = [torch.zeros_like(p) if p.requires_grad else None for p in params]
+
+        def advance(s, k):
+            with torch.no_grad():
+                for _ in range(k):
+                    s = step(s, *params)
+            return s
+
+        def one_step_adjoint(s, gout):
+            # the step recomputed with its tape, then backpropagated
+            with torch.enable_grad():
+                x = s.detach().requires_grad_(True)
+                ps = [p.detach().requires_grad_(p.requires_grad) for p in params]
+                y = step(x, *ps)
+                wrt = [x] + [p for p in ps if p.requires_grad]
+                gr = torch.autograd.grad(y, wrt, gout, allow_unused=True)
+            it = iter(gr[1:])
+            for i, p in enumerate(params):
+                if p.requires_grad:
+                    gi = next(it)
+                    if gi is not None:
+                        pgrads[i] = pgrads[i] + gi
+            return gr[0] if gr[0] is not None else torch.zeros_like(s)
+
+        def reverse(s_a, n, free, gout):
+            # adjoint of n steps starting from state s_a, `free` snapshots left
+            if n == 1:
+                return one_step_adjoint(s_a, gout)
+            if free == 0:
+                for k in range(n - 1, -1, -1):
+                    gout = one_step_adjoint(advance(s_a, k), gout)
+                return gout
+            m = split[n][free]
+            s_m = advance(s_a, m)  # the new snapshot
+            gout = reverse(s_m, n - m, free - 1, gout)
+            del s_m
+            return reverse(s_a, m, free, gout)
+
+        g0 = reverse(state0, ctx.n, ctx.snaps, g)
+        return (None, None, None, g0) + tuple(pgrads)
+
+
+def revolve(step, state, nsteps, snapshots, *params):
+    """state <- step(state, *params) nsteps times, differentiable with at
+    most `snapshots` intermediate states alive in the backward sweep (plus
+    the first one): the binomial schedule of revolve_schedule, so the
+    recomputation is the least possible for that memory."""
+    if nsteps < 1:
+        return state
+    return _Revolve.apply(step, int(nsteps), int(snapshots), state, *params)

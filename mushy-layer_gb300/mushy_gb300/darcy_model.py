@@ -35,7 +35,8 @@ import math
 import torch
 
 from . import abi, ops
-from .adjoint import BEStepper, BackwardEulerStep, Closure, MacProject, Projector, checkpointed
+from .adjoint import (BEStepper, BackwardEulerStep, Closure, MacProject, Projector, checkpointed,
+                      revolve)
 
 
 class DarcySolidification:
@@ -116,14 +117,20 @@ class DarcySolidification:
         flux = (2.0 * (self.T_top - T[..., -1, :]) / self.grid.dx).mean()
         return solid + flux
 
-    def run(self, phi0, logperm, Ra, Tb, nsteps, every=10):
+    def run(self, phi0, logperm, Ra, Tb, nsteps, every=10, snapshots=None):
+        """Objective after nsteps; checkpoints every `every` steps, or, with
+        `snapshots` given, the binomial (revolve) schedule holding at most
+        that many intermediate states."""
         pi_x, pi_z = self.pi_faces(logperm)
         self.projector_for(pi_x.detach(), pi_z.detach())
 
         def step(s, px, pz, ra, tb):
             return self.step(s, px, pz, ra, tb)
 
-        phi = checkpointed(step, phi0, nsteps, every, pi_x, pi_z, Ra, Tb)
+        if snapshots is not None and torch.is_grad_enabled():
+            phi = revolve(step, phi0, nsteps, snapshots, pi_x, pi_z, Ra, Tb)
+        else:
+            phi = checkpointed(step, phi0, nsteps, every, pi_x, pi_z, Ra, Tb)
         return self.objective(phi)
 
 
