@@ -64,3 +64,20 @@ def test_gradient_matches_finite_differences():
         fd = (J(h) - J(-h)) / (2 * h)
         ad = float((gk * dk).sum()) + gra * dra + gtb * dtb
         assert abs(ad - fd) <= 1e-5 * abs(fd), (ad, fd)
+
+
+def test_revolve_schedule_gives_the_same_gradient():
+    """Binomial checkpointing with 2 snapshots over 6 steps reverses the
+    same rollout as the segment checkpoints (recomputation is bitwise
+    deterministic; parameter gradients summed in another order)."""
+    model, phi0, logk = _problem()
+    a = _grads(model, phi0, logk, 2e5, 0.5, 6, 3)
+    lk = logk.clone().requires_grad_(True)
+    ra = torch.tensor(2e5, dtype=torch.float64, device="cuda", requires_grad=True)
+    tb = torch.tensor(0.5, dtype=torch.float64, device="cuda", requires_grad=True)
+    J = model.run(phi0, lk, ra, tb, 6, snapshots=2)
+    J.backward()
+    assert float(J.detach()) == a[0]
+    assert torch.allclose(lk.grad, a[1], rtol=1e-10, atol=1e-16)
+    assert abs(float(ra.grad) - a[2]) <= 1e-10 * abs(a[2])
+    assert abs(float(tb.grad) - a[3]) <= 1e-10 * abs(a[3])
