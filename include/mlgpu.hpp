@@ -117,19 +117,22 @@ class DeviceField {
   void *ptr_ = nullptr;
 };
 
-// Scratch for fused norms.
+// Scratch for fused norms, allocated on first use (an operator that never
+// asks for a norm holds no device memory of its own).
 class NormScratch {
  public:
-  NormScratch() : f_(one_cell(), 1, MLGPU_F64, mlgpu_norm_workspace_bytes() / 8 + 1) {}
-  void *data() { return f_.data(); }
-  size_t bytes() const { return f_.bytes(); }
+  void *data() { return get().data(); }
+  size_t bytes() { return get().bytes(); }
 
  private:
-  static mlgpu_grid one_cell() {
-    mlgpu_grid g = {2, {1, 1, 1}, 1.0, {0, 0, 0}};
-    return g;
+  DeviceField &get() {
+    if (!f_) {
+      mlgpu_grid g = {2, {1, 1, 1}, 1.0, {0, 0, 0}};
+      f_.reset(new DeviceField(g, 1, MLGPU_F64, mlgpu_norm_workspace_bytes() / 8 + 1));
+    }
+    return *f_;
   }
-  DeviceField f_;
+  std::unique_ptr<DeviceField> f_;
 };
 
 // ------------------------------------------------- AMRNonLinearMultiCompOp

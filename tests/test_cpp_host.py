@@ -17,17 +17,26 @@ SRC = os.path.join(ROOT, "tests", "cpp", "host_classes.cpp")
 LIBDIR = os.path.join(ROOT, "mushy-layer_gb300", "_build")
 
 
-def _build_program(out):
+def _build_program(out, src=SRC):
     import __graft_entry__
     __graft_entry__.build()
     cmd = ["g++", "-std=c++17", "-O2", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"),
-           SRC, "-o", out, "-L", LIBDIR, "-lmlgpu", "-Wl,-rpath," + LIBDIR]
+           src, "-o", out, "-L", LIBDIR, "-lmlgpu", "-Wl,-rpath," + LIBDIR]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
 
 
 def test_cpp_host_classes_compile_and_link(tmp_path):
     _build_program(str(tmp_path / "host_classes"))
+
+
+def test_cpp_host_logic_without_gpu(tmp_path):
+    """Box arithmetic, the factories' coarsening limit and the status-code
+    exceptions of the C++ layer, run on the host."""
+    exe = str(tmp_path / "host_logic")
+    _build_program(exe, os.path.join(ROOT, "tests", "cpp", "host_logic.cpp"))
+    r = subprocess.run([exe], capture_output=True, text=True)
+    assert r.returncode == 0 and r.stdout.strip() == "ok", (r.stdout, r.stderr)
 
 
 @pytest.mark.gpu
