@@ -179,7 +179,9 @@ def revolve_schedule(n, s):
     i.e. advance m steps to a new snapshot, reverse the tail with one
     snapshot fewer, then reverse the head.  Returns (cost table, split
     table) indexed [n][s]; split[n][s] is the best m (0 for the base
-    cases).  Costs count step evaluations during the reversal."""
+    cases).  Costs count step evaluations during the reversal; cost - n is
+    Griewank and Walther's binomial optimum t n - C(c + t, t - 1) for
+    c = s + 1 checkpoints (tested)."""
     INF = float("inf")
     cost = [[0] * (s + 1) for _ in range(n + 1)]
     split = [[0] * (s + 1) for _ in range(n + 1)]

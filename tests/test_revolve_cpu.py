@@ -52,3 +52,21 @@ def test_revolve_gradient_matches_plain_autograd(n, s):
     assert fwd == n and back == cost[n][s]
     for a, b in zip((x0.grad, w.grad, c.grad), ref):
         assert torch.allclose(a, b, rtol=1e-12, atol=1e-14)
+
+
+def test_schedule_is_the_binomial_optimum():
+    """The dynamic program reproduces Griewank and Walther's minimal number
+    of forward steps for reversing n steps with c checkpoints (the first
+    state counted): t n - C(c + t, t - 1), t the least with C(c + t, t) >= n."""
+    from math import comb
+
+    def optimum(n, c):
+        t = 0
+        while comb(c + t, t) < n:
+            t += 1
+        return t * n - comb(c + t, t - 1) if t > 0 else 0
+
+    cost, _ = revolve_schedule(80, 9)
+    for n in range(1, 81):
+        for s in range(0, 9):
+            assert cost[n][s] - n == optimum(n, s + 1), (n, s)
