@@ -1,7 +1,10 @@
 """GB300-native (sm_103a) elliptic/closure hot path of mushy-layer.
 
 `abi` is the ctypes mirror of include/mlgpu.h, `ops` the reference-shaped
-operator and solver classes over it, `build` compiles libmlgpu.so.
+operator and solver classes over it, `build` compiles libmlgpu.so,
+`adjoint` the torch.autograd bindings of the discrete adjoint (with segment
+and binomial checkpointing), `darcy_model` the differentiable solidification
+model the adjoint is measured on, `chombo_hdf5` the plotfile reader.
 """
 from . import abi  # noqa: F401
 

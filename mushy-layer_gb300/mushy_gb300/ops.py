@@ -8,6 +8,12 @@ prolongIncrement, createCoarser, resetLambda/computeLambda, norm.  Fields are
 torch CUDA tensors ([comp][k][j][i], no ghosts); every call goes through
 libmlgpu.so on the current torch stream.  Errors raise RuntimeError with the
 library's status string (the reference aborts through MayDay instead).
+
+Beyond the reference's surface: the Jacobian pieces of the discrete adjoint
+(closureJacobian, porosityJacobian, adjointApply, adjointGSRBPass,
+adjointRestrict, linearizedApply, linearizedGSRBPass), AdjointMultiGrid
+(transposed-Jacobian solves, Newton steps, wall-value gradients) and
+macProjectAdjoint.
 """
 import ctypes as C
 
