@@ -77,9 +77,10 @@ def _dense_adjoint(o, phi, J):
     return A_T
 
 
-@pytest.mark.parametrize("dbc", [True, False])
-def test_adjoint_solve_matches_dense_solve(dbc):
-    g, o, phi, J, rng = _op((8, 8), (0, 0, 0), 5, dbc, alpha=1.0, beta=-1e-2)
+@pytest.mark.parametrize("n,per,dbc", [((8, 8), (0, 0, 0), True), ((8, 8), (0, 0, 0), False),
+                                       ((8, 4), (1, 0, 0), True), ((4, 4, 4), (0, 0, 1), True)])
+def test_adjoint_solve_matches_dense_solve(n, per, dbc):
+    g, o, phi, J, rng = _op(n, per, 5, dbc, alpha=1.0, beta=-1e-2)
     A_T = _dense_adjoint(o, phi, J)
     gg = rng.standard_normal(phi.shape)
     ref = np.linalg.solve(A_T, gg.ravel()).reshape(phi.shape)
