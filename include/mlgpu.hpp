@@ -291,11 +291,39 @@ class VCOp {
     return std::unique_ptr<DeviceField>(
         new DeviceField(coarsened(fine.grid()), fine.ncomp(), fine.dtype()));
   }
+  // MGnewOp (AMRProjectionOpFactory / DarcyBrinkmanOpFactory): the operator
+  // one level coarser, a and c averaged over 2^D cells, the faces over
+  // 2^(D-1); nullptr at the coarsening limit
+  std::unique_ptr<VCOp> MGnewOp() const {
+    if (!coarsenable(d_.grid)) return nullptr;
+    std::unique_ptr<VCOp> c(new VCOp(d_, s_));
+    const mlgpu_grid cg = coarsened(d_.grid);
+    c->d_.grid = cg;
+    const void *cell[2] = {d_.aCoef, d_.cCoef};
+    const void **dst[2] = {&c->d_.aCoef, &c->d_.cCoef};
+    for (int m = 0; m < 2; m++) {
+      if (!cell[m]) continue;
+      c->own_cell_[m].reset(new DeviceField(cg, 1, d_.dtype));
+      check(mlgpu_restrict_average(&d_.grid, 1, d_.dtype, c->own_cell_[m]->data(), cell[m], s_),
+            "VCOp::MGnewOp");
+      *dst[m] = c->own_cell_[m]->data();
+    }
+    for (int d = 0; d < 3; d++) {
+      c->d_.bCoef[d] = nullptr;
+      if (d >= d_.grid.dim) continue;
+      c->own_b_[d].reset(new DeviceField(cg, 1, d_.dtype, faces(cg, d)));
+      check(mlgpu_coarsen_faces(&d_.grid, 1, d_.dtype, d, c->own_b_[d]->data(), d_.bCoef[d], s_),
+            "VCOp::MGnewOp");
+      c->d_.bCoef[d] = c->own_b_[d]->data();
+    }
+    return c;
+  }
 
  protected:
   mlgpu_vcop d_;
   void *s_;
   NormScratch ws_;
+  std::unique_ptr<DeviceField> own_cell_[2], own_b_[3];  // coefficients of an MGnewOp level
 };
 
 // alpha = 0, bCoef = -Pi_face, beta = 1, cCoef = NULL (srcSubcycle/Projector.cpp:2942-2973)

@@ -109,6 +109,13 @@ int main(int argc, char **argv) {
     mlgpu::ProjectionOp pop(v);
     mlgpu::DeviceField f(g, 1), p(g, 1);
     f.upload(load(dir + "/f.bin", nc).data());
+    // the projection operator one level coarser applied to the averaged f
+    std::unique_ptr<mlgpu::VCOp> pc_op = pop.MGnewOp();
+    std::unique_ptr<mlgpu::DeviceField> fc = pop.createCoarser(f);
+    pop.restrictR(*fc, f);
+    mlgpu::DeviceField lfc(fc->grid(), 1);
+    pc_op->applyOp(lfc, *fc);
+    save(dir + "/out_projection_coarse_apply.bin", fetch(lfc));
     p.setToZero();
     mlgpu::AMRMultiGrid mg(pop);
     const mlgpu_solve_stats sp = mg.solve(p, f);

@@ -41,6 +41,11 @@ int main() {
   d.dtype = MLGPU_F64;
   mlgpu::NLMultiCompOp op(d);
   EXPECT(op.MGnewOp() == nullptr);
+  mlgpu_vcop v = {};
+  v.grid = c;
+  v.dtype = MLGPU_F64;
+  mlgpu::ProjectionOp pop(v);
+  EXPECT(pop.MGnewOp() == nullptr);
   // invalid descriptors are refused before any device work
   mlgpu_mg_options o = mlgpu::default_options(true);
   o.relax_mode = 7;

@@ -78,6 +78,10 @@ def test_cpp_host_classes_match_oracle(tmp_path):
     assert stats["fas_iterations"] == st.iterations and stats["fas_status"] == st.exit_status
     assert np.array_equal(out("fas", phi.shape), sol)
     vref = O.VCOpHost(g, abi.make_bc(), 0.0, 1.0, None, vb)
+    cvb = [O.coarsen_faces(g, 1, d, vb[d]) for d in range(2)]
+    cvref = O.VCOpHost(cg, abi.make_bc(), 0.0, 1.0, None, cvb)
+    fc = O.restrict_average(g, 1, f)
+    assert np.array_equal(out("projection_coarse_apply", fc.shape), O.vc_apply(cvref, fc))
     psol, pst, prc = O.vc_solve(vref, O.default_options(0), np.zeros(abi.cell_shape(g)), f)
     assert stats["projection_iterations"] == pst.iterations
     assert np.array_equal(out("projection", abi.cell_shape(g)), psol)
