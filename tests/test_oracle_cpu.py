@@ -405,3 +405,40 @@ def test_temperature_condition_large_residual_is_zeroed():
                                        (0, 0))
         assert Tg == T0
 
+
+
+@pytest.mark.parametrize("a,b,F,Tref", [(0.5, -1.0, -1.0, 2.0), (1.0, 0.0, -0.7, 0.0),
+                                        (0.5, -1.0, -0.5, 4.0)])
+def test_steady_robin_conduction_matches_the_analytic_profile(a, b, F, Tref):
+    """The reference's diffusive-growth check (test/diffusiveGrowth/
+    testDiffusionAndBCs.py, V = 0): steady conduction between a fixed
+    temperature T_max at the bottom and the mixed condition
+    a dT/dz = F + b (T - T_ref) at the top has the linear solution
+    T = T_max + s z, s = (F + b (T_max - T_ref)) / (a - b).  Liquid
+    throughout, both walls as nonlinear temperature conditions on H (Newton
+    ghost solves run to convergence), backward-Euler steps with a long time
+    step to the steady state; the discrete profile is exact for a linear T."""
+    n = 32
+    g = abi.make_grid([4, n], 1.0 / n, [1, 0, 0])
+    p = P.mushy_params()  # St = 5, CR = 5: liquid for C = -1 above T = 1
+    T_max = 3.0
+    s = (F + b * (T_max - Tref)) / (a - b)
+    phi_bc = abi.make_bc({(1, 0, 0): (abi.BC_FIXED_TEMPERATURE, T_max),
+                          (1, 1, 0): (abi.BC_TEMPERATURE_FLUX_RADIATION, F)})
+    nl = abi.make_nlbc(radiation={(1, 1): (a, b, Tref)}, method=abi.NLBC_NEWTON, max_iter=50,
+                       max_residual=1e-14)
+    phi = np.empty((2, 1, n, 4))
+    phi[0] = 5.0 + 2.5
+    phi[1] = -1.0
+    bcoef = [np.stack([-np.ones(abi.face_shape(g, d)), np.zeros(abi.face_shape(g, d))])
+             for d in range(2)]
+    ref = O.NLOpHost(g, p, phi_bc, abi.make_bc(), 1.0, -1.0, None, bcoef, apply_derived_bc=0,
+                     nlbc=nl)
+    opts = O.default_options(1)
+    opts.tolerance, opts.hang, opts.max_iter = 1e-13, 0.0, 200
+    for _ in range(6):
+        phi, st, rc = O.hc_backward_euler(ref, opts, phi, phi, 1e4)
+    T = phi[0, 0, :, 0] - 5.0  # liquid: T = H - St
+    z = (np.arange(n) + 0.5) / n
+    assert np.abs(T - (T_max + s * z)).max() < 1e-8 * max(1.0, abs(s))
+    assert np.abs(phi[1] + 1.0).max() == 0.0  # no solute diffusion: C unchanged
