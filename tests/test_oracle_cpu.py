@@ -442,3 +442,34 @@ def test_steady_robin_conduction_matches_the_analytic_profile(a, b, F, Tref):
     z = (np.arange(n) + 0.5) / n
     assert np.abs(T - (T_max + s * z)).max() < 1e-8 * max(1.0, abs(s))
     assert np.abs(phi[1] + 1.0).max() == 0.0  # no solute diffusion: C unchanged
+
+
+def test_darcy_brinkman_poiseuille_matches_the_analytic_profile():
+    """The reference's Poiseuille check (test/poiseuilleFlow/
+    testPoiseuilleFlow.py): v'' = (chi / Pi) v / Da - chi F between no-slip
+    walls.  With chi = Pi = 1, Da = 0.01 the solution is
+    v = F Da (1 - cosh((x - 1/2) / sqrt(Da)) / cosh(1 / (2 sqrt(Da)))).
+    DarcyBrinkmanOp with c = chi / (Pi Da), b = -1, beta = -1 (so
+    L v = c v - v'') solved by the linear multigrid: second-order
+    convergence to the profile."""
+    Da, F = 0.01, 2.0
+    errs = []
+    for n in (32, 64, 128):
+        g = abi.make_grid([n, n], 1.0 / n, [0, 1, 0])  # square: a deep hierarchy
+        bc = abi.make_bc({(0, 0, 0): (abi.BC_DIRICHLET, 0.0), (0, 1, 0): (abi.BC_DIRICHLET, 0.0)})
+        b = [-np.ones(abi.face_shape(g, d)) for d in range(2)]
+        c = np.full(abi.cell_shape(g), 1.0 / Da)
+        ref = O.VCOpHost(g, bc, 0.0, -1.0, None, b, cCoef=c)
+        rho = np.full(abi.cell_shape(g), F)
+        opts = O.default_options(0)
+        opts.tolerance, opts.hang, opts.max_iter = 1e-13, 0.0, 200
+        v, st, rc = O.vc_solve(ref, opts, np.zeros(abi.cell_shape(g)), rho)
+        x = (np.arange(n) + 0.5) / n
+        exact = F * Da * (1 - np.cosh((x - 0.5) / np.sqrt(Da)) / np.cosh(0.5 / np.sqrt(Da)))
+        errs.append(np.abs(v[0, 0, :] - exact).max() / exact.max())
+        # uniform along the periodic direction (to the red/black rounding)
+        assert np.abs(v - v[:, :1, :]).max() <= 1e-14 * np.abs(v).max()
+    # the Brinkman layer (width sqrt(Da) = 0.1) on 32, 64, 128 cells:
+    # relative errors 9.9e-3, 2.8e-3, 7.3e-4
+    assert errs[-1] < 1e-3, errs
+    assert 3.4 < errs[0] / errs[1] < 4.6 and 3.4 < errs[1] / errs[2] < 4.6, errs
