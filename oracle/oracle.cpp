@@ -1657,7 +1657,10 @@ void lin_apply(const AdjCtx &X, const double *xd, double *out) {
 // one red/black pass of the block smoother on A x = r (the Newton step's
 // linear solve): out and the diagonal block D of each colour cell from J x
 // with its ghosts, x += D^-1 (r - A x)
-void lin_gsrb_pass(const AdjCtx &X, double *xd, const double *r, int pass) {
+// With Minv (the stored inverse of A^T's diagonal blocks) its transpose is
+// applied instead of forming D.
+void lin_gsrb_pass(const AdjCtx &X, double *xd, const double *r, int pass,
+                   const double *Minv = nullptr) {
   const mlgpu_nlop &op = X.op;
   const mlgpu_grid &g = op.grid;
   std::vector<double> out(2 * X.n);
@@ -1667,6 +1670,14 @@ void lin_gsrb_pass(const AdjCtx &X, double *xd, const double *r, int pass) {
       int imin = std::abs((j + k + pass) % 2);
       for (int i = imin; i < g.n[0]; i += 2) {
         const size_t q = cidx(g, i, j, k, 0);
+        if (Minv) {
+          double r0 = r[q] - out[q], r1 = r[q + X.n] - out[q + X.n];
+          double m0 = Minv[q], m1 = Minv[q + X.n], m2 = Minv[q + 2 * X.n], m3 = Minv[q + 3 * X.n];
+          double x0 = xd[q], x1 = xd[q + X.n];
+          xd[q] = x0 + (m0 * r0 + m2 * r1);
+          xd[q + X.n] = x1 + (m1 * r0 + m3 * r1);
+          continue;
+        }
         const int at[3] = {i, j, k};
         double P[2], Y[4] = {0.0, 0.0, 0.0, 0.0}, M[4];
         for (int c = 0; c < 2; c++) {
@@ -1723,6 +1734,7 @@ struct AdjSolver {
   mlgpu_mg_options o;
   std::vector<AdjLevelO> L;
   double updates = 0;
+  bool tr = true;  // cycles on A^T (adjoint) or on A (Newton's linear solve)
 
   mlgpu_nlop op_at(int l) {
     mlgpu_nlop op = op0;
@@ -1747,6 +1759,10 @@ struct AdjSolver {
       L[l].r.assign(n, 0);
     }
     std::copy(phi, phi + L[0].u.size(), L[0].u.begin());
+    refresh();
+  }
+  // coarse states averaged from level 0's, J and the inverse blocks per level
+  void refresh() {
     for (size_t l = 1; l < L.size(); l++)
       orc_restrict_average(&L[l - 1].g, 2, L[l].u.data(), L[l - 1].u.data());
     for (auto &lv : L) orc_closure_jac(&lv.g, &op0.params, lv.u.data(), lv.J.data());
@@ -1763,6 +1779,13 @@ struct AdjSolver {
     Fab y;
     y.define(op.grid, 2);
     y.load(L[l].y.data());
+    if (!tr) {
+      for (int s = 0; s < n; s++) {
+        lin_gsrb_pass(X, L[l].y.data(), L[l].gg.data(), 0, L[l].Minv.data());
+        lin_gsrb_pass(X, L[l].y.data(), L[l].gg.data(), 1, L[l].Minv.data());
+      }
+      return;
+    }
     for (int s = 0; s < n; s++) {
       adj_gsrb_pass_fab(y, X, L[l].gg.data(), 0, L[l].Minv.data());
       adj_gsrb_pass_fab(y, X, L[l].gg.data(), 1, L[l].Minv.data());
@@ -1779,21 +1802,26 @@ struct AdjSolver {
     const int n = (int)(2 * nc);
     std::vector<double> M((size_t)n * (n + 1));
     auto at = [&](int r, int c) -> double & { return M[(size_t)r * (n + 1) + c]; };
-    std::vector<double> e(n, 0.0);
+    std::vector<double> e(n, 0.0), col(n);
     for (int k = 0; k < n; k++) {
       std::fill(e.begin(), e.end(), 0.0);
       e[k] = 1.0;
-      Fab y;
-      adj_load(y, op, e.data());
-      for (int kk = 0; kk < L[l].g.n[2]; kk++)
-        for (int j = 0; j < L[l].g.n[1]; j++)
-          for (int i = 0; i < L[l].g.n[0]; i++) {
-            double o2[2];
-            adj_row(X, y, i, j, kk, o2, nullptr);
-            size_t q = cidx(L[l].g, i, j, kk, 0);
-            at((int)q, k) = o2[0];
-            at((int)(q + nc), k) = o2[1];
-          }
+      if (tr) {
+        Fab y;
+        adj_load(y, op, e.data());
+        for (int kk = 0; kk < L[l].g.n[2]; kk++)
+          for (int j = 0; j < L[l].g.n[1]; j++)
+            for (int i = 0; i < L[l].g.n[0]; i++) {
+              double o2[2];
+              adj_row(X, y, i, j, kk, o2, nullptr);
+              size_t q = cidx(L[l].g, i, j, kk, 0);
+              col[q] = o2[0];
+              col[q + nc] = o2[1];
+            }
+      } else {
+        lin_apply(X, e.data(), col.data());
+      }
+      for (int r = 0; r < n; r++) at(r, k) = col[r];
       at(k, n) = L[l].gg[k];
     }
     for (int p = 0; p < n; p++) {
@@ -1833,14 +1861,45 @@ struct AdjSolver {
     }
     smooth(l, o.num_smooth_down);
     mlgpu_nlop op = op_at(l);
-    orc_hc_adjoint_restrict_impl(op, L[l].u.data(), L[l].J.data(), L[l].y.data(),
-                                 L[l].gg.data(), L[l + 1].gg.data());
+    if (tr)
+      orc_hc_adjoint_restrict_impl(op, L[l].u.data(), L[l].J.data(), L[l].y.data(),
+                                   L[l].gg.data(), L[l + 1].gg.data());
+    else
+      lin_restrict(op, L[l].u.data(), L[l].J.data(), L[l].y.data(), L[l].gg.data(),
+                   L[l + 1].gg.data());
     for (int m = 0; m < o.num_mg; m++) cycle(l + 1);
     mlgpu_bc ybc = op0.apply_derived_bc ? op0.derived_bc : op0.phi_bc;
     orc_prolong_increment(&L[l].g, &ybc, 2, o.prolong, L[l].y.data(), L[l + 1].y.data());
     smooth(l, o.num_smooth_up);
     updates += (double)(o.num_smooth_down + o.num_smooth_up + 1) * ncells(L[l].g);
   }
+  // 2^D average of g - A y (the children in the device's order)
+  static void lin_restrict(const mlgpu_nlop &op, const double *phi, const double *J,
+                           const double *yd, const double *g, double *gc) {
+    AdjCtx X(op, phi, J);
+    std::vector<double> ay(2 * X.n);
+    lin_apply(X, yd, ay.data());
+    mlgpu_grid cg = coarsen_grid(op.grid);
+    const double denom = op.grid.dim == 3 ? 8.0 : 4.0;
+    size_t nc = ncells(cg);
+    for (int K = 0; K < cg.n[2]; K++)
+      for (int J2 = 0; J2 < cg.n[1]; J2++)
+        for (int I = 0; I < cg.n[0]; I++) {
+          double acc[2] = {0.0, 0.0};
+          for (int kk = 0; kk < (op.grid.dim == 3 ? 2 : 1); kk++)
+            for (int jj = 0; jj < 2; jj++)
+              for (int ii = 0; ii < 2; ii++) {
+                int i = 2 * I + ii, j = 2 * J2 + jj, k = op.grid.dim == 3 ? 2 * K + kk : 0;
+                size_t q = cidx(op.grid, i, j, k, 0);
+                for (int c = 0; c < 2; c++)
+                  acc[c] = acc[c] + (g[q + c * X.n] - ay[q + c * X.n]) / denom;
+              }
+          size_t Q = cidx(cg, I, J2, K, 0);
+          gc[Q] = acc[0];
+          gc[Q + nc] = acc[1];
+        }
+  }
+
   static void orc_hc_adjoint_restrict_impl(const mlgpu_nlop &op, const double *phi,
                                            const double *J, const double *yd, const double *g,
                                            double *gc) {
@@ -2099,3 +2158,82 @@ int orc_mac_project_adjoint(const mlgpu_vcop *op, const mlgpu_mg_options *o,
 }
 
 }  // extern "C"
+
+// Newton for N(phi) = rhs on the Jacobian hierarchy (the device's
+// mlgpu_hc_newton_solve restated): A(u) d = rhs - N(u) by V-cycles on A to
+// 1e-3 relative (at most 12), u += d halving d while the L2 residual grows
+// (at most 4 times), stagnation on the L2 merit, three stalled steps below
+// 1e-8 of the start end the solve
+extern "C" int orc_hc_newton_solve(const mlgpu_nlop *op, const mlgpu_mg_options *o, double *phi,
+                                   const double *rhs, mlgpu_solve_stats *st) {
+  AdjSolver S;
+  S.op0 = *op;
+  S.o = *o;
+  S.tr = false;
+  S.build(phi);
+  memset(st, 0, sizeof(*st));
+  st->levels = (int)S.L.size();
+  const size_t n = 2 * ncells(op->grid);
+  std::vector<double> r(n), uold(n), lr(n);
+  mlgpu_nlop op0 = S.op_at(0);
+  auto nl = [&](double &merit) {
+    orc_nl_residual(&op0, r.data(), S.L[0].u.data(), rhs);
+    merit = norm_of(r.data(), n, MLGPU_NORM_L2);
+    return norm_of(r.data(), n, o->norm_type);
+  };
+  auto lin_norm = [&]() {
+    AdjCtx X(op0, S.L[0].u.data(), S.L[0].J.data());
+    lin_apply(X, S.L[0].y.data(), lr.data());
+    for (size_t q = 0; q < n; q++) lr[q] = S.L[0].gg[q] - lr[q];
+    return norm_of(lr.data(), n, o->norm_type);
+  };
+  double merit;
+  const double norm0 = nl(merit);
+  double norm = norm0, prev = norm0;
+  st->initial_norm = norm0;
+  st->norm_history[0] = norm0;
+  int iter = 0, status = std::isfinite(norm0) ? 0 : 8, stall = 0, cycles = 0;
+  while (norm > o->tolerance * norm0 && norm0 > o->norm_thresh && iter < o->max_iter &&
+         status == 0) {
+    S.refresh();
+    std::fill(S.L[0].y.begin(), S.L[0].y.end(), 0.0);
+    std::copy(r.begin(), r.end(), S.L[0].gg.begin());
+    const double l0 = lin_norm();
+    double ln = l0;
+    for (int c = 0; c < 12 && ln > 1e-3 * l0; c++) {
+      S.cycle(0);
+      cycles++;
+      ln = lin_norm();
+    }
+    uold = S.L[0].u;
+    double scale = 1.0, merit_new = merit, norm_new = norm;
+    for (int h = 0; h <= 4; h++) {
+      for (size_t q = 0; q < n; q++) S.L[0].u[q] = scale * S.L[0].y[q] + 1.0 * uold[q];
+      norm_new = nl(merit_new);
+      if (std::isfinite(merit_new) && merit_new <= merit) break;
+      scale *= 0.5;
+    }
+    const double merit_prev = merit;
+    merit = merit_new;
+    norm = norm_new;
+    stall = norm >= 0.95 * prev ? stall + 1 : 0;
+    iter++;
+    if (iter < 64) st->norm_history[iter] = norm;
+    if (!std::isfinite(norm) || !std::isfinite(merit))
+      status = 8;
+    else if (merit > (1.0 - o->hang) * merit_prev && norm > o->tolerance * norm0)
+      status = 2;
+    prev = norm;
+    if (stall >= 3 && norm < 1e-8 * norm0 && status == 0) status = 2;
+  }
+  std::copy(S.L[0].u.begin(), S.L[0].u.end(), phi);
+  st->iterations = iter;
+  st->cycles = cycles;
+  st->final_norm = norm;
+  if (status == 0 && norm > o->tolerance * norm0 && norm0 > o->norm_thresh) status = 4;
+  st->exit_status = status;
+  if (status == 8) return MLGPU_ERR_NAN;
+  if (status == 2) return MLGPU_ERR_HANG;
+  if (status == 4) return MLGPU_ERR_NOT_CONVERGED;
+  return MLGPU_OK;
+}

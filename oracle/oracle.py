@@ -60,6 +60,8 @@ def lib():
             "orc_hc_adjoint_restrict": (i, [P(abi.NLOp), vp, vp, vp, vp, vp]),
             "orc_hc_linearized_apply": (i, [P(abi.NLOp), vp, vp, vp, vp]),
             "orc_hc_lin_gsrb_pass": (i, [P(abi.NLOp), vp, vp, vp, vp, i]),
+            "orc_hc_newton_solve": (i, [P(abi.NLOp), P(abi.MGOptions), vp, vp,
+                                        P(abi.SolveStats)]),
             "orc_hc_adjoint_solve": (i, [P(abi.NLOp), P(abi.MGOptions), vp, vp, vp,
                                          P(abi.SolveStats)]),
             "orc_hc_adjoint_bc_gradient": (i, [P(abi.NLOp), vp, vp, vp, vp]),
@@ -406,3 +408,11 @@ def mac_project_adjoint(o, opts, phi_bc, ubar, pi, p, q=None):
                                        _faces3(ubar), _faces3(pi) if pi is not None else None,
                                        _p(p), _faces3(usb), _faces3(pib), _p(q), C.byref(st))
     return usb, pib, q, st, rc
+
+
+def newton_solve(o, opts, phi, rhs):
+    """N(phi) = rhs by the Newton driver on the Jacobian hierarchy."""
+    phi = phi.copy()
+    st = abi.SolveStats()
+    rc = lib().orc_hc_newton_solve(C.byref(o.op), C.byref(opts), _p(phi), _p(rhs), C.byref(st))
+    return phi, st, rc

@@ -198,3 +198,32 @@ def test_mac_project_adjoint_dot_product_and_permeability_gradient():
     fd = (jp - jm) / (2 * h)
     ad = sum(float((pib[d] * dpi[d]).sum()) for d in range(2))
     assert abs(ad - fd) <= 1e-6 * abs(fd), (ad, fd)
+
+
+@pytest.mark.parametrize("dbc", [True, False])
+def test_newton_driver_matches_fas_solution(dbc):
+    """The Newton driver on the Jacobian hierarchy (oracle restatement of
+    mlgpu_hc_newton_solve) reaches the FP64 tolerance in fewer iterations
+    than FAS cycles and lands on the FAS solution of the same step."""
+    # the GPU Newton test's problem: mush and liquid, heat and weak solute
+    # diffusion
+    rng = np.random.default_rng(8)
+    g = P.grid((32, 32))
+    p = P.mushy_params()
+    phi_bc, der = P.hc_bcs("mixed")
+    if not dbc:
+        phi_bc = abi.make_bc({(1, 0, 0): (abi.BC_DIRICHLET, 5.5), (1, 1, 1): (abi.BC_NEUMANN, 0.0)})
+    phi = P.hc_state(g, rng, regimes=False)
+    phi[0] = rng.uniform(4.6, 6.4, phi[0].shape)
+    b = [np.stack([-np.ones(abi.face_shape(g, d)), -0.01 * np.ones(abi.face_shape(g, d))])
+         for d in range(2)]
+    o = O.NLOpHost(g, p, phi_bc, der, 1.0, -2e-3, None, b, apply_derived_bc=int(dbc))
+    opts = O.default_options(1)
+    opts.tolerance, opts.hang, opts.max_iter = 1e-12, -1.0, 300
+    rhs = phi.copy()
+    u_fas, st_f, rc_f = O.hc_solve(o, opts, phi, rhs)
+    u_n, st_n, rc_n = O.newton_solve(o, opts, phi, rhs)
+    assert rc_n in (0, abi.ERR_HANG) and st_n.final_norm <= 1e-10 * st_n.initial_norm
+    assert st_n.iterations < st_f.iterations, (st_n.iterations, st_f.iterations)
+    assert np.abs(O.nl_residual(o, u_n, rhs)).max() <= 1.01 * st_n.final_norm
+    assert np.abs(u_n - u_fas).max() <= 1e-9 * np.abs(u_fas).max()
