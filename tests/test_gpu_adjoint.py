@@ -193,3 +193,31 @@ def test_newton_backward_euler_matches_fas(n):
     assert np.abs(r).max() <= 1.01e-12 * st_n.initial_norm
     scale = np.abs(host(fas)).max()
     assert np.abs(host(nt) - host(fas)).max() <= 1e-9 * scale
+
+
+def test_newton_driver_agrees_with_oracle():
+    """The device Newton driver against its oracle restatement on the same
+    step (same linear cycles, stored inverse blocks, step halving); the L2
+    merit is summed in another order on the device, so the comparison is to
+    1e-10 rather than bitwise."""
+    from mushy_gb300 import ops
+    rng = np.random.default_rng(26)
+    g = P.grid((32, 32))
+    p = P.mushy_params()
+    phi_bc, der = P.hc_bcs("mixed")
+    phi = P.hc_state(g, rng, regimes=False)
+    phi[0] = rng.uniform(4.6, 6.4, phi[0].shape)
+    b = [np.stack([-np.ones(abi.face_shape(g, d)), -0.01 * np.ones(abi.face_shape(g, d))])
+         for d in range(2)]
+    ref = O.NLOpHost(g, p, phi_bc, der, 1.0, -2e-3, None, b)
+    opts = O.default_options(1)
+    opts.tolerance, opts.hang, opts.max_iter = 1e-12, -1.0, 100
+    u_ref, st_ref, rc_ref = O.newton_solve(ref, opts, phi, phi.copy())
+    op = ops.NLMultiCompOp(g, p, phi_bc, der, 1.0, -2e-3, None, [dev(x) for x in b])
+    o = ops.default_options(True)
+    o.tolerance, o.hang, o.max_iter = 1e-12, -1.0, 100
+    A = ops.AdjointMultiGrid(op, o)
+    d_u = dev(phi)
+    st, rc = A.newtonSolve(d_u, dev(phi))
+    assert rc == rc_ref and abs(st.iterations - st_ref.iterations) <= 1
+    assert np.abs(host(d_u) - u_ref).max() <= 1e-10 * np.abs(u_ref).max()
