@@ -4,7 +4,7 @@
 operator and solver classes over it, `build` compiles libmlgpu.so,
 `adjoint` the torch.autograd bindings of the discrete adjoint (with segment
 and binomial checkpointing), `darcy_model` the differentiable solidification
-model the adjoint is measured on, `chombo_hdf5` the plotfile reader.
+model the adjoint is measured on, `chombo_hdf5` the plotfile and checkpoint reader.
 """
 from . import abi  # noqa: F401
 

@@ -9,6 +9,9 @@ AMRLevelMushyLayer) can be read without h5py or libhdf5.
 `read_plotfile(path)` returns the root attributes, the component names and,
 per level, the boxes and the cell data per component (Fortran order inside
 each box, i fastest), the layout plotting/MushyPltFile.py relies on.
+`read_checkpoint(path)` reads a checkpoint's per-variable datasets, cell
+(FArrayBox) and face (FluxBox) variables, as plotting/ChkFile.py does, and
+`level_state` turns a one-box level into the operators' (H, C) layout.
 """
 import struct
 
@@ -261,6 +264,119 @@ def read_plotfile(path):
         levels.append({"attrs": lattrs, "boxes": lb})
         lev += 1
     return {"attrs": attrs, "components": names, "levels": levels}
+
+
+def _extent(lo, hi):
+    return np.asarray(hi) - np.asarray(lo) + 1
+
+
+def _strip(arr, ghost, ext):
+    """Valid region of one component block of shape ext[::-1] + 2 ghost."""
+    if not np.any(ghost):
+        return arr
+    sl = (slice(None),) + tuple(slice(g, g + e) for g, e in zip(ghost[::-1], ext[::-1]))
+    return arr[sl]
+
+
+def _unpack_box(chunk, ncomp, ext, ghost):
+    """One box of a checkpoint variable: a cell field (FArrayBox, comp-major,
+    i fastest) or a face field (FluxBox: the faces normal to direction 0 for
+    every component, then direction 1, ...), told apart by the chunk size."""
+    dim = len(ext)
+    ncell = int(np.prod(ext + 2 * ghost))
+    if chunk.size == ncomp * ncell:
+        arr = chunk.reshape((ncomp,) + tuple((ext + 2 * ghost)[::-1]))
+        return np.ascontiguousarray(_strip(arr, ghost, ext))
+    nface = [int(np.prod(ext + 2 * ghost + (np.arange(dim) == d))) for d in range(dim)]
+    if chunk.size == ncomp * sum(nface):
+        out, p = [], 0
+        for d in range(dim):
+            fext = ext + (np.arange(dim) == d)
+            arr = chunk[p:p + ncomp * nface[d]].reshape((ncomp,) + tuple((fext + 2 * ghost)[::-1]))
+            out.append(np.ascontiguousarray(_strip(arr, ghost, fext)))
+            p += ncomp * nface[d]
+        return out
+    raise ValueError("box of %d values matches neither %d cells nor %d faces x %d components"
+                     % (chunk.size, ncell, sum(nface), ncomp))
+
+
+def read_checkpoint(path):
+    """A Chombo checkpoint (chk*.hdf5, AMRLevelMushyLayer::writeCheckpointLevel):
+    per level, one dataset per variable (`<name>:datatype=0` with its
+    `<name>:offsets=0` box offsets and `<name>_attributes` {comps, ghost,
+    outputGhost, objectType}) instead of the plotfile's single `data` block;
+    the layout plotting/ChkFile.py:118-260 reads.
+
+    Returns {"attrs", "space_dim", "components", "levels"}; each level holds
+    its attributes, its boxes as (lo, hi) pairs and `fields`: variable name ->
+    one entry per box, an array (comps, [nz,] ny, nx) for cell variables or a
+    list of D arrays (comps, face extents) for face variables such as the
+    advection velocity `advVel`."""
+    data = open(path, "rb").read()
+    R = _Reader(data)
+    attrs = R.attributes(R.root["header"])
+    entries = _group_children(R, R.root["header"])
+    glob = R.attributes(entries["Chombo_global"]["header"]) if "Chombo_global" in entries else {}
+    ncomp = int(attrs.get("num_components", 0))
+    levels = []
+    lev = 0
+    while "level_%d" % lev in entries:
+        ge = entries["level_%d" % lev]
+        lattrs = R.attributes(ge["header"])
+        kids = _group_children(R, ge["header"])
+        raw = R.dataset(kids["boxes"]["header"])
+        boxes = []
+        for box in raw:
+            f = list(box.tolist())
+            dim = len(f) // 2
+            boxes.append((np.array(f[:dim]), np.array(f[dim:])))
+        fields = {}
+        for key in sorted(kids):
+            if not key.endswith(":datatype=0"):
+                continue
+            name = key[:-len(":datatype=0")]
+            va = R.attributes(kids[name + "_attributes"]["header"]) \
+                if name + "_attributes" in kids else {}
+            nc = int(va.get("comps", 1))
+            ghost = va.get("outputGhost", None)
+            flat = R.dataset(kids[key]["header"])
+            offs = R.dataset(kids[name + ":offsets=0"]["header"])
+            per_box = []
+            for b, (lo, hi) in enumerate(boxes):
+                g = np.zeros(len(lo), dtype=int)
+                if ghost is not None:
+                    gv = list(ghost.tolist()) if hasattr(ghost, "tolist") else [ghost]
+                    g = np.array(gv[:len(lo)], dtype=int)
+                chunk = flat[int(offs[b]):int(offs[b + 1])]
+                per_box.append(_unpack_box(chunk, nc, _extent(lo, hi), g))
+            fields[name] = per_box
+        levels.append({"attrs": lattrs, "boxes": boxes, "fields": fields})
+        lev += 1
+    return {"attrs": attrs, "space_dim": int(glob.get("SpaceDim", len(levels[0]["boxes"][0][0])
+                                                      if levels else 0)),
+            "components": [attrs["component_%d" % i] for i in range(ncomp)],
+            "levels": levels}
+
+
+def level_state(chk, level, names=("Enthalpy", "Bulk concentration")):
+    """The (H, C) state of a one-box checkpoint level in the layout of the
+    operators, [comp][k][j][i] (k of extent 1 in 2D), with the level's box
+    and spacing: a restart state for NLMultiCompOp / the solvers."""
+    L = chk["levels"][level]
+    if len(L["boxes"]) != 1:
+        raise ValueError("level %d has %d boxes; one box per level is needed"
+                         % (level, len(L["boxes"])))
+    comps = []
+    for name in names:
+        a = L["fields"][name][0]
+        if isinstance(a, list):
+            raise ValueError("%s is a face variable" % name)
+        comps.extend(a)
+    st = np.stack(comps)
+    if st.ndim == 3:
+        st = st[:, None]
+    lo, hi = L["boxes"][0]
+    return np.ascontiguousarray(st), (lo, hi), float(L["attrs"]["dx"])
 
 
 def _group_children(R, header):

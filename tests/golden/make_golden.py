@@ -1,4 +1,5 @@
-"""Generates tests/golden/closure_plt000100.npz from the reference's own data.
+"""Generates tests/golden/closure_plt000100.npz and
+tests/golden/checkpoint_chk000100.npz from the reference's own data.
 
 Source: test/unit/data/plt000100.2d.hdf5 of the mushy-layer project, a
 3-level AMR plotfile written by the reference (AMRLevelMushyLayer plot
@@ -7,6 +8,10 @@ Porosity, Liquid concentration, the last three produced by
 updateEnthalpyVariables, src/phaseDiagram.cpp:92-177).  The phase-diagram
 parameters are the file's root attributes (C = compositionRatio,
 S = stefan, cp = specificHeatRatio, pc = waterDistributionCoeff).
+
+The second fixture comes from test/unit/data/chk000100.2d.hdf5, the
+checkpoint the same run wrote at the same step: the (H, C) state and the
+face-centred advection velocity (advVel) of its one-box levels 0 and 1.
 
 The reference tree is only present where the fixture is generated; the GPU
 box and the tests read the committed .npz.  Run:
@@ -44,6 +49,19 @@ def main(ref_root):
         max_enthalpy_level0=max(b["data"][0].max() for b in pf["levels"][0]["boxes"]),
         max_enthalpy_level2=max(b["data"][0].max() for b in pf["levels"][2]["boxes"]))
     print("wrote", out, H.size, "cells")
+
+    chk = chombo_hdf5.read_checkpoint(
+        os.path.join(ref_root, "test", "unit", "data", "chk000100.2d.hdf5"))
+    fx = {}
+    for lev in (0, 1):
+        state, (lo, hi), dx = chombo_hdf5.level_state(chk, lev)
+        fx["state%d" % lev] = state
+        fx["lo%d" % lev], fx["hi%d" % lev], fx["dx%d" % lev] = lo, hi, dx
+        for d, f in enumerate(chk["levels"][lev]["fields"]["advVel"][0]):
+            fx["advVel%d_%d" % (lev, d)] = f
+    out = os.path.join(HERE, "checkpoint_chk000100.npz")
+    np.savez_compressed(out, **fx)
+    print("wrote", out)
 
 
 if __name__ == "__main__":

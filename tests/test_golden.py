@@ -75,3 +75,65 @@ def test_gpu_closure_bitwise_vs_reference_output():
     torch.cuda.synchronize()
     for k in outs:
         assert np.array_equal(outs[k].cpu().numpy(), z[k]), k
+
+
+CHK_GOLD = os.path.join(HERE, "golden", "checkpoint_chk000100.npz")
+REF_CHK = "/root/reference/test/unit/data/chk000100.2d.hdf5"
+
+
+def test_checkpoint_state_closure_matches_plotfile():
+    """The reference's checkpoint of step 100 as a restart state: its one-box
+    levels' (H, C), in the operators' layout, closed by the oracle, give the
+    temperature, porosity and liquid concentration the plotfile of the same
+    step holds, bit for bit."""
+    z, p, _, _ = _load()
+    c = np.load(CHK_GOLD)
+    for lev in (0, 1):
+        st = c["state%d" % lev]
+        ny, nx = st.shape[-2:]
+        g = abi.make_grid([nx, ny], float(c["dx%d" % lev]))
+        out = O.closure(g, p, np.ascontiguousarray(st))
+        sel = z["level"] == lev
+        assert np.array_equal(st[0].ravel(), z["H"][sel])
+        assert np.array_equal(st[1].ravel(), z["C"][sel])
+        for k in ("T", "porosity", "Cl"):
+            assert np.array_equal(out[k].ravel(), z[k][sel]), (lev, k)
+
+
+@pytest.mark.skipif(not (os.path.exists(REF_CHK) and os.path.exists(REF_PLT)),
+                    reason="reference tree not mounted")
+def test_checkpoint_reader_against_plotfile():
+    """Checkpoint and plotfile of the same step: same boxes, the same (H, C)
+    bit for bit on every level, and the face-centred advection velocity
+    (FluxBox advVel) averaged to cells equals the plotfile's cell-centred
+    advection velocity bit for bit -- the face layout (x faces, then y faces,
+    i fastest) is read as written."""
+    from mushy_gb300 import chombo_hdf5
+    chk = chombo_hdf5.read_checkpoint(REF_CHK)
+    pf = chombo_hdf5.read_plotfile(REF_PLT)
+    ci = {n: i for i, n in enumerate(pf["components"])}
+    assert chk["space_dim"] == 2 and chk["attrs"]["iteration"] == 100
+    assert chk["components"][:2] == ["Enthalpy", "Bulk concentration"]
+    assert len(chk["levels"]) == len(pf["levels"]) == 3
+    for lev, (L, P) in enumerate(zip(chk["levels"], pf["levels"])):
+        assert len(L["boxes"]) == len(P["boxes"])
+        for b, ((lo, hi), pb) in enumerate(zip(L["boxes"], P["boxes"])):
+            assert np.array_equal(lo, pb["lo"]) and np.array_equal(hi, pb["hi"])
+            for name in ("Enthalpy", "Bulk concentration"):
+                assert np.array_equal(L["fields"][name][b][0], pb["data"][ci[name]]), (lev, b, name)
+            ux, uy = L["fields"]["advVel"][b]
+            assert np.array_equal(0.5 * (ux[0][:, :-1] + ux[0][:, 1:]),
+                                  pb["data"][ci["xAdvection velocity"]]), (lev, b)
+            assert np.array_equal(0.5 * (uy[0][:-1, :] + uy[0][1:, :]),
+                                  pb["data"][ci["yAdvection velocity"]]), (lev, b)
+            dv = L["fields"]["Darcy velocity"][b]
+            assert np.array_equal(dv[0], pb["data"][ci["xDarcy velocity"]])
+    c = np.load(CHK_GOLD)
+    for lev in (0, 1):
+        st, (lo, hi), dx = chombo_hdf5.level_state(chk, lev)
+        assert np.array_equal(st, c["state%d" % lev]) and dx == float(c["dx%d" % lev])
+        for d in range(2):
+            assert np.array_equal(chk["levels"][lev]["fields"]["advVel"][0][d],
+                                  c["advVel%d_%d" % (lev, d)])
+    with pytest.raises(ValueError):
+        chombo_hdf5.level_state(chk, 2)   # seven boxes
