@@ -721,7 +721,12 @@ void coarsen_faces(const mlgpu_grid &fg, int ncomp, int d, double *cf, const dou
 double norm_of(const double *x, size_t n, int type) {
   double r = 0;
   if (type == MLGPU_NORM_MAX) {
-    for (size_t i = 0; i < n; i++) r = std::max(r, std::fabs(x[i]));
+    // a NaN stays in the maximum (std::max would drop it and report a
+    // poisoned field as converged), so every solver reads it as non-finite
+    for (size_t i = 0; i < n; i++) {
+      const double a = std::fabs(x[i]);
+      if (a > r || a != a) r = a;
+    }
     return r;
   }
   if (type == MLGPU_NORM_L1) {
