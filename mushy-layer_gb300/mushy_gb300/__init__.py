@@ -4,7 +4,9 @@
 operator and solver classes over it, `build` compiles libmlgpu.so,
 `adjoint` the torch.autograd bindings of the discrete adjoint (with segment
 and binomial checkpointing), `darcy_model` the differentiable solidification
-model the adjoint is measured on, `chombo_hdf5` the plotfile and checkpoint reader.
+model the adjoint is measured on, `chombo_hdf5` the plotfile and checkpoint reader,
+`inputs` the reader of the reference's inputs files (parameters, walls, solver
+settings).
 """
 from . import abi  # noqa: F401
 

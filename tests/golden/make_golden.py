@@ -12,11 +12,15 @@ S = stefan, cp = specificHeatRatio, pc = waterDistributionCoeff).
 The second fixture comes from test/unit/data/chk000100.2d.hdf5, the
 checkpoint the same run wrote at the same step: the (H, C) state and the
 face-centred advection velocity (advVel) of its one-box levels 0 and 1.
+The third, inputs_unit_data.json, keeps the keys of the run's
+test/unit/data/inputs that mushy_gb300.inputs reads, beside the parameters
+and base spacing the run wrote into its plotfile.
 
 The reference tree is only present where the fixture is generated; the GPU
 box and the tests read the committed .npz.  Run:
     python tests/golden/make_golden.py /path/to/mushy-layer
 """
+import json
 import os
 import sys
 
@@ -61,6 +65,24 @@ def main(ref_root):
             fx["advVel%d_%d" % (lev, d)] = f
     out = os.path.join(HERE, "checkpoint_chk000100.npz")
     np.savez_compressed(out, **fx)
+    print("wrote", out)
+
+    # the run's inputs, reduced to the keys the inputs reader takes, with
+    # the parameters and spacing the run wrote into its plotfile
+    from mushy_gb300 import inputs as mi
+    inp = mi.Inputs.read(os.path.join(ref_root, "test", "unit", "data", "inputs"))
+    keep = ("parameters.", "bc.", "main.num_cells", "main.domain_", "main.periodic_bc",
+            "main.nondimensionalisation", "main.max_bc", "main.bc_", "main.nonlinear_bc",
+            "main.apply_diagnostic_bcs", "HCMultigrid.", "projection.", "VelocityMultigrid.")
+    table = {k: v for k, v in sorted(inp.table.items()) if k.startswith(keep)}
+    written = {k: float(a[k]) for k in ("C", "D", "L", "S", "cp", "k", "pc")}
+    written.update(timescale=a["timescale"], velocity_scale=a["velocity_scale"],
+                   dx0=float(pf["levels"][0]["attrs"]["dx"]),
+                   prob_domain=[int(x) for x in pf["levels"][0]["attrs"]["prob_domain"].tolist()])
+    out = os.path.join(HERE, "inputs_unit_data.json")
+    with open(out, "w") as f:
+        json.dump({"inputs": table, "plotfile": written}, f, indent=1, sort_keys=True)
+        f.write("\n")
     print("wrote", out)
 
 

@@ -1,0 +1,215 @@
+"""The inputs-file reader (mushy_gb300/inputs.py) against the reference's
+own run: tests/golden/inputs_unit_data.json holds the keys of the inputs of
+test/unit/data (the run that wrote plt000100.2d.hdf5) and the parameters and
+base spacing that run wrote into its plotfile.  The reader must derive
+exactly those values, and the wall values of the (H, C) operator from the
+same phase diagram the oracle restates."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import problems as P
+from mushy_gb300 import abi
+from mushy_gb300 import inputs as mi
+from oracle import oracle as O
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+FIX = os.path.join(HERE, "golden", "inputs_unit_data.json")
+REF_INPUTS = "/root/reference/test/unit/data/inputs"
+
+
+def _run_inputs():
+    z = json.load(open(FIX))
+    text = "\n".join("%s = %s" % (k, " ".join(v)) for k, v in z["inputs"].items())
+    return mi.Inputs.parse(text), z["plotfile"]
+
+
+def test_parameters_equal_the_values_the_run_wrote():
+    inp, w = _run_inputs()
+    p, q = inp.params()
+    assert p.compositionRatio == w["C"] and p.stefan == w["S"]
+    assert p.specificHeatRatio == w["cp"] and p.heatConductivityRatio == w["k"]
+    assert p.waterDistributionCoeff == w["pc"]
+    assert q["lewis"] == w["L"] and q["darcy"] == w["D"]
+    assert (w["timescale"], w["velocity_scale"]) == ("Diffusive", "Advective")
+    assert q["nondimensionalisation"] == 0
+    # diffusive timescale, advective velocity (src/MushyLayerParams.cpp:734-751)
+    assert p.heatDiffusionCoeff == 1.0 and p.saltDiffusionCoeff == 1 / w["L"]
+    assert p.viscosityCoeff == q["prandtl"] and p.darcyCoeff == q["prandtl"] / w["D"]
+    # reference point at the eutectic: theta_e = Theta_e = 0
+    assert p.thetaEutectic == 0.0 and p.ThetaEutectic == 0.0
+    assert q["ThetaInitial"] == -1.0 and q["heleShawPermeability"] == 1e4
+    g = inp.grid(2)
+    lo_i, lo_j, hi_i, hi_j = w["prob_domain"]
+    assert (g.n[0], g.n[1]) == (hi_i - lo_i + 1, hi_j - lo_j + 1)
+    assert g.dx == w["dx0"] and list(g.periodic) == [0, 0, 0]
+
+
+def test_wall_values_of_the_run():
+    """The run's walls: x no flux; y bottom H 6.3 with no-flux C (closed with
+    the initial bulk concentration: liquid, T = 1.3, C_l = -1); y top H 2.5,
+    C -1 (eutectic point: T = C_l = 0)."""
+    inp, _ = _run_inputs()
+    p, q = inp.params()
+    g = inp.grid(2)
+    T, V = inp.scalar_bcs(2, q)
+    assert T["temperatureLo"] == [1, 1] and T["temperatureHi"] == [1, 0]
+    assert V["temperatureLo"][1] == O.pd_temperature(p, 6.3, -1.0) == 6.3 - 5.0
+    assert V["liquidConcentrationLo"][1] == -1.0
+    assert V["temperatureHi"][1] == O.pd_temperature(p, 2.5, -1.0) == 0.0
+    assert V["liquidConcentrationHi"][1] == 0.0 and V["porosityHi"][1] == 0.5
+    phi_bc, der, adb, nl = inp.hc_bcs(g)
+    assert adb == 1
+    for d in range(2):
+        for s in range(2):
+            for c in range(2):
+                assert phi_bc.type[d][s][c] == abi.BC_NEUMANN and phi_bc.value[d][s][c] == 0.0
+                want = (abi.BC_DIRICHLET, 0.0) if (d, s) == (1, 1) else (abi.BC_NEUMANN, 0.0)
+                assert (der.type[d][s][c], der.value[d][s][c]) == want, (d, s, c)
+    assert (nl.method, nl.max_iter, nl.max_residual, nl.relax_coeff, nl.dx) == \
+        (abi.NLBC_PICARD, 2, 1e-5, 0.5, g.dx)
+    o = inp.hc_options()
+    assert (o.num_smooth_down, o.num_smooth_up, o.max_iter, o.bottom_max_iter) == (1, 4, 10, 40)
+    assert (o.tolerance, o.hang, o.norm_thresh) == (1e-10, 1e-10, 1e-10)
+    o = inp.projection_options()
+    assert (o.num_smooth_down, o.num_smooth_up, o.max_iter) == (2, 8, 20)   # numSmoothUp=8
+    assert o.tolerance == 1e-15
+
+
+@pytest.mark.skipif(not os.path.exists(REF_INPUTS), reason="reference tree not mounted")
+def test_fixture_is_the_runs_inputs():
+    inp = mi.Inputs.read(REF_INPUTS)
+    z = json.load(open(FIX))
+    for k, v in z["inputs"].items():
+        assert inp.table[k] == v, k
+
+
+def test_phase_diagram_point_against_the_oracle():
+    """The wall-value phase diagram equals the oracle's scalar restatement
+    (temperature, bitwise) and the closure (porosity, C_l) over every
+    regime."""
+    rng = np.random.default_rng(80)
+    p = P.mushy_params()
+    q = {k: getattr(p, k) for k in ("compositionRatio", "waterDistributionCoeff",
+                                    "specificHeatRatio", "stefan", "thetaEutectic",
+                                    "ThetaEutectic")}
+    H = rng.uniform(-0.5, 7.0, 400)
+    Cc = rng.uniform(-4.0, -0.5, 400)
+    g = abi.make_grid([400, 1])
+    cl = O.closure(g, p, np.ascontiguousarray(np.stack([H, Cc]).reshape(2, 1, 1, 400)))
+    regimes = set()
+    for i in range(400):
+        por, theta, c_l, _ = mi.phase_diagram_point(H[i], Cc[i], q)
+        assert theta == O.pd_temperature(p, H[i], Cc[i])
+        assert abs(por - cl["porosity"][i]) <= 1e-13 and abs(c_l - cl["Cl"][i]) <= 1e-12
+        regimes.add(0 if por == 0 else 1 if por == 1 else 2)
+    assert regimes == {0, 1, 2}
+
+
+def test_parser_rules():
+    inp = mi.Inputs.parse("""
+# comment line
+parameters.stefan = 4.0   # trailing comment
+parameters.stefan = 6.0
+bc.scalarLo = noflux fixed open
+bc.scalarHi = -1 1
+bc.temperatureHi = 1 -1
+bc.aLo = 0.1 0.2
+bc.bHi = 0.3 0.7
+bc.TRefLo = -1.1 0
+bc.enthalpyLoVal = 6.0 6.0
+bc.enthalpyHiVal = 6.0 1.0
+bc.bulkConcentrationLoVal = -1 -1
+bc.bulkConcentrationHiVal = -1 -1
+main.title = "two words"
+main.apply_diagnostic_bcs = false
+main.num_cells = 64 32
+main.domain_width = 2.0
+main.periodic_bc = 1 0
+HCMultigrid.relaxMode = 4
+HCMultigrid.useRelaxBottomSolver = false
+VelocityMultigrid.num_smooth = 3
+parameters.compositionRatio = 2
+parameters.waterDistributionCoeff = 1e-3
+parameters.specificHeatRatio = 1
+parameters.heatConductivityRatio = 1
+parameters.lewis = 100
+parameters.darcy = 0
+parameters.eutecticTemp = -23
+parameters.eutecticComposition = 230
+parameters.initialComposition = 30
+parameters.liquidusSlope = -0.1
+""")
+    assert inp.get("parameters.stefan") == 6.0                 # last definition wins
+    assert inp.table["main.title"] == ["two words"]
+    T, V = inp.scalar_bcs(2)
+    assert T["enthalpyLo"] == [1, 0]                           # names, first match
+    assert T["enthalpyHi"] == [0, 0]    # "-1" is not all digits: every token read as a name
+    assert T["temperatureHi"] == [1, 0]    # -1 keeps the default (scalarHi, read as names)
+    g = inp.grid(2)
+    assert list(g.n)[:2] == [64, 32] and g.dx == 2.0 / 64 and g.periodic[0] == 1
+    phi_bc, der, adb, nl = inp.hc_bcs(g)
+    assert adb == 0 and all(der.type[d][s][c] == abi.BC_NEUMANN for d in range(2)
+                            for s in range(2) for c in range(2))
+    f32 = lambda v: float(np.float32(v))
+    assert nl.a[0][0] == f32(0.1) != 0.1 and nl.a[1][0] == f32(0.2)
+    assert nl.b[1][1] == f32(0.7) and nl.T_ref[0][0] == f32(-1.1)
+    assert nl.a[0][1] == 0.0                                   # absent: 0
+    o = inp.hc_options()
+    assert o.relax_mode == abi.RELAX_JACOBI and o.bottom_solver == abi.BOTTOM_BICGSTAB
+    o = inp.velocity_options()
+    assert (o.num_smooth_down, o.num_smooth_up, o.max_iter, o.tolerance) == (3, 3, 10, 1e-10)
+    with pytest.raises(ValueError):
+        mi.Inputs.parse("parameters.darcy = 0\nmain.nondimensionalisation = 1\n"
+                        "parameters.lewis = 1\nparameters.prandtl = 1").params()
+
+
+def test_temperature_condition_on_enthalpy_from_inputs():
+    """A fixed-temperature enthalpy wall (type 6) becomes the temperature
+    condition on H with its wall value; a diagnostic condition the path does
+    not have is refused."""
+    base = """
+bc.scalarLo = 1 1
+bc.enthalpyHi = 1 6
+bc.enthalpyLoVal = 0 6.3
+bc.enthalpyHiVal = 0 -0.4
+bc.bulkConcentrationLoVal = -1 -1
+bc.bulkConcentrationHiVal = -1 -1
+main.num_cells = 16 16
+main.domain_width = 1
+parameters.stefan = 5
+parameters.compositionRatio = 2
+parameters.waterDistributionCoeff = 1e-5
+parameters.specificHeatRatio = 1
+parameters.heatConductivityRatio = 1
+parameters.lewis = 200
+parameters.darcy = 0
+parameters.prandtl = 0
+parameters.eutecticTemp = -23
+parameters.eutecticComposition = 230
+parameters.initialComposition = 30
+parameters.liquidusSlope = -0.1
+"""
+    for adb_key in ("false", "true"):
+        inp = mi.Inputs.parse(base + "bc.scalarHi = 1 0\nmain.apply_diagnostic_bcs = %s\n"
+                              % adb_key)
+        phi_bc, der, adb, nl = inp.hc_bcs(inp.grid(2))
+        assert phi_bc.type[1][1][0] == abi.BC_FIXED_TEMPERATURE
+        assert phi_bc.value[1][1][0] == -0.4 and phi_bc.type[1][0][0] == abi.BC_NEUMANN
+        assert adb == (adb_key == "true")
+    # the scalar type reaches the diagnostic temperature too: refused
+    inp = mi.Inputs.parse(base + "bc.scalarHi = 1 6\n")
+    with pytest.raises(ValueError, match="not on this path"):
+        inp.hc_bcs(inp.grid(2))
+
+
+def test_hc_face_coefficients_order():
+    chi = [np.array([[0.0, 0.25, 1.0]]), np.array([[0.5, 0.75]])]
+    q = {"heatConductivityRatio": 2.0, "heatDiffusionCoeff": 1.0, "saltDiffusionCoeff": 0.005}
+    b = mi.hc_face_coefficients(chi, q)
+    assert b[0].shape == (2, 1, 3)
+    assert np.array_equal(b[0][0], ((1.0 - chi[0]) * 2.0 + chi[0]) * -1.0)
+    assert np.array_equal(b[0][1], chi[0] * -0.005)
+    assert b[0][0][0, 2] == -1.0 and b[0][0][0, 0] == -2.0
