@@ -14,12 +14,35 @@ Beyond the reference's surface: the Jacobian pieces of the discrete adjoint
 adjointRestrict, linearizedApply, linearizedGSRBPass), AdjointMultiGrid
 (transposed-Jacobian solves, Newton steps, wall-value gradients) and
 macProjectAdjoint.
+
+setSolveLog(log) installs a mushy_gb300.solvelog.SolveLog: every solver call
+then appends one JSON line (status, residual history, work, wall time).
 """
 import ctypes as C
+import time
 
 import torch
 
 from . import abi
+
+_SOLVE_LOG = None
+
+
+def setSolveLog(log):
+    """Install a SolveLog (None: no logging) for every solver call."""
+    global _SOLVE_LOG
+    _SOLVE_LOG = log
+
+
+def _log(what, solver, st, rc, t0):
+    """One log line for `solver`'s call started at perf_counter() == t0 (the
+    C calls return after their stream is synchronised)."""
+    if _SOLVE_LOG is None:
+        return
+    d = solver.desc
+    _SOLVE_LOG.record(what, solver.kind, d.grid, solver.opts, st, rc,
+                      time.perf_counter() - t0, has_a=bool(d.aCoef),
+                      has_c=bool(getattr(d, "cCoef", None)))
 
 
 def _stream():
@@ -268,7 +291,7 @@ def default_options(hc):
 
 class _Solver:
     def __init__(self, op, opts, kind):
-        self.op, self.opts = op, opts
+        self.op, self.opts, self.kind = op, opts, kind
         lib = abi.load()
         self.desc = op.desc()
         nbytes = C.c_size_t()
@@ -286,7 +309,9 @@ class _Solver:
 
     def solve(self, phi, rhs, check=False):
         st = abi.SolveStats()
+        t0 = time.perf_counter()
         rc = abi.load().mlgpu_solver_solve(self.h, _ptr(phi), _ptr(rhs), C.byref(st))
+        _log("solve", self, st, rc, t0)
         if check:
             abi.check(rc, "solve")
         elif rc not in (abi.OK, abi.ERR_NOT_CONVERGED, abi.ERR_HANG):
@@ -328,9 +353,11 @@ class AMRFASMultiGrid(_Solver):
         """LevelBackwardEuler::updateSoln: solve (a - dt L) phi_new = a phi_old + dt src."""
         scratch = torch.empty_like(phi_old)
         st = abi.SolveStats()
+        t0 = time.perf_counter()
         rc = abi.load().mlgpu_hc_backward_euler(self.h, _ptr(phi_new), _ptr(phi_old), _ptr(src),
                                                 _ptr(aCoef), float(dt), _ptr(scratch),
                                                 C.byref(st))
+        _log("backwardEuler", self, st, rc, t0)
         if rc not in (abi.OK, abi.ERR_NOT_CONVERGED, abi.ERR_HANG):
             abi.check(rc, "backwardEuler")
         return st, rc
@@ -348,11 +375,13 @@ class AMRMultiGrid(_Solver):
         scratch = cell_tensor(g, 1, torch.float64)
         st = abi.SolveStats()
         bc = phi_bc if phi_bc is not None else self.op.bc
+        t0 = time.perf_counter()
         rc = abi.load().mlgpu_mac_project(self.h, C.byref(g), C.byref(bc),
                                           _faces3(list(u) + [None] * (3 - len(u))),
                                           _faces3(list(pi_face) + [None] * (3 - len(pi_face)))
                                           if pi_face is not None else None,
                                           _ptr(phi), _ptr(scratch), C.byref(st))
+        _log("levelMacProject", self, st, rc, t0)
         if rc not in (abi.OK, abi.ERR_NOT_CONVERGED, abi.ERR_HANG):
             abi.check(rc, "levelMacProject")
         return st, rc
@@ -435,23 +464,29 @@ class AdjointMultiGrid(_Solver):
 
     def adjointSolve(self, phi, g, y):
         st = abi.SolveStats()
+        t0 = time.perf_counter()
         rc = abi.load().mlgpu_hc_adjoint_solve(self.h, _ptr(phi), _ptr(g), _ptr(y), C.byref(st))
+        _log("adjointSolve", self, st, rc, t0)
         _ok(rc, "adjointSolve")
         return st, rc
 
     def newtonSolve(self, phi, rhs):
         """N(phi) = rhs by Newton steps on the Jacobian hierarchy (phi in/out)."""
         st = abi.SolveStats()
+        t0 = time.perf_counter()
         rc = abi.load().mlgpu_hc_newton_solve(self.h, _ptr(phi), _ptr(rhs), C.byref(st))
+        _log("newtonSolve", self, st, rc, t0)
         _ok(rc, "newtonSolve")
         return st, rc
 
     def backwardEulerNewton(self, phi_new, phi_old, dt, src=None, aCoef=None):
         scratch = torch.empty_like(phi_old)
         st = abi.SolveStats()
+        t0 = time.perf_counter()
         rc = abi.load().mlgpu_hc_backward_euler_newton(self.h, _ptr(phi_new), _ptr(phi_old),
                                                        _ptr(src), _ptr(aCoef), float(dt),
                                                        _ptr(scratch), C.byref(st))
+        _log("backwardEulerNewton", self, st, rc, t0)
         _ok(rc, "backwardEulerNewton")
         return st, rc
 
@@ -468,9 +503,11 @@ class AdjointMultiGrid(_Solver):
         src_bar = torch.empty_like(phi_new) if want_src else None
         bcg = (C.c_double * 12)()
         st = abi.SolveStats()
+        t0 = time.perf_counter()
         rc = abi.load().mlgpu_hc_backward_euler_adjoint(
             self.h, _ptr(phi_new), _ptr(phi_new_bar), _ptr(aCoef), float(dt), _ptr(mu),
             _ptr(old_bar), _ptr(src_bar), bcg, C.byref(st))
+        _log("backwardEulerAdjoint", self, st, rc, t0)
         _ok(rc, "backwardEulerAdjoint")
         return old_bar, src_bar, [bcg[q] for q in range(12)], st, rc
 
@@ -488,10 +525,12 @@ def macProjectAdjoint(solver, ubar, pi_face, p, q=None, phi_bc=None, want_pi=Tru
     st = abi.SolveStats()
     bc = phi_bc if phi_bc is not None else solver.op.bc
     pad = lambda L: list(L) + [None] * (3 - len(L))
+    t0 = time.perf_counter()
     rc = abi.load().mlgpu_mac_project_adjoint(
         solver.h, C.byref(g), C.byref(bc), _faces3(pad(ubar[:dim])),
         _faces3(pad(pi_face[:dim])) if pi_face is not None else None, _ptr(p),
         _faces3(pad(usb)), _faces3(pad(pib)) if want_pi else None, _ptr(q), _ptr(scratch),
         C.byref(st))
+    _log("macProjectAdjoint", solver, st, rc, t0)
     _ok(rc, "macProjectAdjoint")
     return usb, pib, q, st, rc

@@ -154,3 +154,33 @@ def test_newton_and_adjoint_status_match_oracle():
                   dev(np.zeros_like(phi)))
     _same(st, rc, st_r, rc_r)
     assert rc == abi.ERR_NAN
+
+
+def test_solve_log_records_device_solves():
+    """With a SolveLog installed, each solver call appends one line that
+    carries the call's own stats."""
+    import io
+    import json
+    from mushy_gb300 import ops, solvelog
+    g, chi, perm, u = P.projection_problem((64, 64), 5, sigma=8.0)
+    b = [-f for f in O.face_geomean(g, perm)]
+    f = O.mac_divergence(g, u)
+    f -= f.mean()
+    buf = io.StringIO()
+    ops.setSolveLog(solvelog.SolveLog(buf))
+    try:
+        op = ops.ProjectionOp(g, abi.make_bc(), 0.0, 1.0, None, [dev(x) for x in b])
+        o = ops.default_options(False)
+        o.tolerance, o.max_iter = 1e-10, 40
+        st, rc = ops.AMRMultiGrid(op, o).solve(torch.zeros_like(dev(f)), dev(f))
+        gh, p, phi_bc, der, phi, bh, _ = _hc_case()
+        hop = ops.NLMultiCompOp(gh, p, phi_bc, der, 1.0, -1e-3, None, [dev(x) for x in bh])
+        st2, rc2 = ops.AMRFASMultiGrid(hop).backwardEuler(dev(phi), dev(phi), 1e-3)
+    finally:
+        ops.setSolveLog(None)
+    recs = [json.loads(x) for x in buf.getvalue().splitlines()]
+    assert [r["what"] for r in recs] == ["solve", "backwardEuler"]
+    for r, s, c in zip(recs, (st, st2), (rc, rc2)):
+        assert r["rc"] == c and r["iterations"] == s.iterations
+        assert r["cell_updates"] == s.cell_updates and r["seconds"] > 0
+        assert r["residual_history"][0] == s.initial_norm
