@@ -150,7 +150,9 @@ typedef struct mlgpu_mg_options {
   double hang;           /* stop when |r| > (1 - hang) * |r_prev| */
   double norm_thresh;    /* stop when |r0| <= norm_thresh */
   int relax_mode;        /* MLGPU_RELAX_GSRB or MLGPU_RELAX_JACOBI */
-  int bottom_solver;     /* MLGPU_BOTTOM_RELAX or MLGPU_BOTTOM_BICGSTAB */
+  int bottom_solver;     /* MLGPU_BOTTOM_RELAX; MLGPU_BOTTOM_BICGSTAB (Chombo's
+                            BiCGStabSolver, the projection's default in the
+                            reference) is not built: MLGPU_ERR_ARG */
   int bottom_max_iter;   /* m_imax of the bottom solver */
   int max_coarse;        /* s_maxCoarse: coarsen while coarsenable(2^d * max_coarse) */
   int prolong;           /* MLGPU_PROLONG_* */

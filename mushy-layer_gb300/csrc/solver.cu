@@ -1538,6 +1538,8 @@ bool valid_options(const mlgpu_mg_options *o) {
     return false;
   if (o->relax_mode != MLGPU_RELAX_GSRB && o->relax_mode != MLGPU_RELAX_JACOBI) return false;
   if (o->bottom_max_iter < 0 || o->max_coarse < 1) return false;
+  // the BiCGStab bottom solver is not built: refused rather than replaced
+  if (o->bottom_solver != MLGPU_BOTTOM_RELAX) return false;
   if (o->prolong != MLGPU_PROLONG_CONSTANT && o->prolong != MLGPU_PROLONG_LINEAR) return false;
   if (o->precision != MLGPU_PREC_F64 && o->precision != MLGPU_PREC_MIXED) return false;
   if (o->norm_type < MLGPU_NORM_MAX || o->norm_type > MLGPU_NORM_L2) return false;

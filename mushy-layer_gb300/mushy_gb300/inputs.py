@@ -25,7 +25,9 @@ quirks kept:
   Neumann is always a zero gradient (PhysBCUtil.cpp:975-981);
 * solver settings: HCMultigrid.* and VelocityMultigrid.*
   (srcSubcycle/MushyLayerSubcycleUtils.cpp:654-692), projection.*
-  (srcSubcycle/Projector.cpp:44-64,388-443);
+  (srcSubcycle/Projector.cpp:44-64,388-443); the bottom solver is always
+  relaxation (a BiCGStab bottom, the projection's default there, is not
+  built);
 * the grid: main.num_cells, main.domain_width / domain_length /
   domain_height (srcSubcycle/MushyLayerSubcycleUtils.cpp:115-140),
   main.periodic_bc.
@@ -399,8 +401,8 @@ class Inputs:
             ("num_smooth_down", "HCMultigrid.numSmoothDown", int),
             ("relax_mode", "HCMultigrid.relaxMode", int),
             ("bottom_max_iter", "HCMultigrid.bottomSolveIterations", int)])
-        if not self.get("HCMultigrid.useRelaxBottomSolver", True, bool):
-            o.bottom_solver = abi.BOTTOM_BICGSTAB
+        # HCMultigrid.useRelaxBottomSolver = false asks for Chombo's BiCGStab
+        # bottom solver, which is not built: the relaxation bottom stays
         return o
 
     def projection_options(self):

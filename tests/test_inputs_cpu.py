@@ -158,7 +158,7 @@ parameters.liquidusSlope = -0.1
     assert nl.b[1][1] == f32(0.7) and nl.T_ref[0][0] == f32(-1.1)
     assert nl.a[0][1] == 0.0                                   # absent: 0
     o = inp.hc_options()
-    assert o.relax_mode == abi.RELAX_JACOBI and o.bottom_solver == abi.BOTTOM_BICGSTAB
+    assert o.relax_mode == abi.RELAX_JACOBI and o.bottom_solver == abi.BOTTOM_RELAX
     o = inp.velocity_options()
     assert (o.num_smooth_down, o.num_smooth_up, o.max_iter, o.tolerance) == (3, 3, 10, 1e-10)
     with pytest.raises(ValueError):

@@ -274,6 +274,10 @@ def test_argument_validation_without_gpu():
     assert nbytes.value > 64 * 64 * 8 * 3
     opts.relax_mode = 7
     assert lib.mlgpu_vc_solver_workspace(C.byref(op), C.byref(opts), C.byref(nbytes)) == abi.ERR_ARG
+    # a bottom solver that is not built is refused, not replaced
+    lib.mlgpu_mg_default_options(C.byref(opts), 0)
+    opts.bottom_solver = abi.BOTTOM_BICGSTAB
+    assert lib.mlgpu_vc_solver_workspace(C.byref(op), C.byref(opts), C.byref(nbytes)) == abi.ERR_ARG
 
 
 # ------------------------------------------- nonlinear temperature conditions
