@@ -477,3 +477,46 @@ def test_darcy_brinkman_poiseuille_matches_the_analytic_profile():
     # relative errors 9.9e-3, 2.8e-3, 7.3e-4
     assert errs[-1] < 1e-3, errs
     assert 3.4 < errs[0] / errs[1] < 4.6 and 3.4 < errs[1] / errs[2] < 4.6, errs
+
+
+# ------------------------------------------------------------- MAC projection
+def _projected(n=(64, 32), seed=23):
+    g, chi, perm, u = P.projection_problem(n, seed, sigma=6.0)
+    u[0][..., -1] = u[0][..., 0]          # one periodic seam value
+    u[1][:, 0, :] = 0.0                   # no flux through the walls
+    u[1][:, -1, :] = 0.0
+    pi = O.face_geomean(g, perm)
+    bc = abi.make_bc()
+    ref = O.VCOpHost(g, bc, 0.0, 1.0, None, [-x for x in pi])
+    opts = O.default_options(0)
+    opts.tolerance, opts.hang, opts.max_iter = 1e-13, 0.0, 400
+    return g, bc, ref, opts, pi, u
+
+
+def test_mac_projection_properties():
+    """levelMacProject's size-independent properties on the oracle:
+    divergence-free output, idempotence, exact removal of a pi-weighted
+    gradient, and the output orthogonal to the removed gradient."""
+    g, bc, ref, opts, pi, u = _projected()
+    zero = np.zeros(abi.cell_shape(g))
+    u1, p1, st, rc = O.mac_project(ref, opts, bc, u, pi, zero)
+    d0 = np.abs(O.mac_divergence(g, u)).max()
+    assert np.abs(O.mac_divergence(g, u1)).max() <= 1e-10 * d0
+    scale = max(np.abs(x).max() for x in u1)
+    # idempotent
+    u2, p2, _, _ = O.mac_project(ref, opts, bc, u1, pi, zero)
+    assert max(np.abs(a - b).max() for a, b in zip(u2, u1)) <= 1e-10 * scale
+    # u1 + Pi G q projects back onto u1
+    q = np.random.default_rng(5).standard_normal(abi.cell_shape(g))
+    ug = O.mac_correct(g, bc, -q, u1, pi)
+    u3, p3, _, _ = O.mac_project(ref, opts, bc, ug, pi, zero)
+    added = max(np.abs(a - b).max() for a, b in zip(ug, u1))     # |Pi G q|, ~1e5
+    assert max(np.abs(a - b).max() for a, b in zip(u3, u1)) <= 1e-11 * added
+    # the pressure is q up to its constant (Neumann walls, periodic x)
+    assert np.abs((p3 - p3.mean()) - (q - q.mean())).max() <= 5e-8 * np.abs(q).max()
+    # discrete orthogonality: sum over faces of u1 . G p1 = -sum D u1 p1 = 0
+    gp = [a - b for a, b in zip(u, u1)]            # Pi G p1, face by face
+    inner = sum((a[..., :-1] * b[..., :-1]).sum() if d == 0 else (a * b).sum()
+                for d, (a, b) in enumerate(zip(u1, [x / y for x, y in zip(gp, pi)])))
+    norm = np.sqrt(sum((a * a).sum() for a in u1) * sum((b * b).sum() for b in gp))
+    assert abs(inner) <= 1e-9 * norm
