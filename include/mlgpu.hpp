@@ -368,7 +368,8 @@ class Solver {
     mlgpu_grid g = {2, {1, 1, 1}, 1.0, {0, 0, 0}};
     ws_.reset(new DeviceField(g, 1, MLGPU_F64, bytes / 8 + 64));
   }
-  // the workspace must be 256-byte aligned: allocations from the library are
+  // the workspace must be 256-byte aligned, which every device allocation
+  // made through the library (cudaMalloc) is
   void *ws() { return ws_->data(); }
   size_t ws_bytes() const { return ws_->bytes(); }
 
