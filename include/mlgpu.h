@@ -362,7 +362,10 @@ int mlgpu_vc_solver_create(const mlgpu_vcop *op, const mlgpu_mg_options *o,
 /* Solve L(phi) = rhs in place (phi holds the initial guess), FP64 arrays. */
 int mlgpu_solver_solve(mlgpu_solver *s, double *phi, const double *rhs,
                        mlgpu_solve_stats *stats);
-/* Re-read alpha/beta (setAlphaAndBeta) and rebuild coarse coefficients. */
+/* Re-read alpha/beta (setAlphaAndBeta) and rebuild what depends on them:
+ * the stored 1/diag of every level and, in mixed precision, the FP32 face
+ * weights.  The coefficient arrays themselves are coarsened once, when the
+ * solver is created: new coefficients need a new solver. */
 int mlgpu_solver_set_alpha_beta(mlgpu_solver *s, double alpha, double beta);
 int mlgpu_solver_destroy(mlgpu_solver *s);
 /* Replace the wall conditions of an (H, C) solver or adjoint solver
