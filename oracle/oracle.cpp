@@ -22,6 +22,13 @@
 // The multigrid drivers restate Chombo's AMRMultiGrid / AMRFASMultiGrid /
 // RelaxSolver (Chombo fork c00e7b62, not in the reference tree); parity at
 // the driver level is unpinned.
+//
+// Pins: the closure reproduces the reference's own plotfile output bit for
+// bit (tests/test_golden.py); the operators, wall conditions and solvers
+// reproduce the analytic answers of the reference's physics tests: steady
+// Robin conduction (test/diffusiveGrowth), Poiseuille-Brinkman flow
+// (test/poiseuilleFlow) and the directional-solidification mushy layer of
+// test/testDiffusiveSolidification.py (second-order convergence).
 
 #include <cmath>
 #include <cstdio>
