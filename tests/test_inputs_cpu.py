@@ -213,3 +213,53 @@ def test_hc_face_coefficients_order():
     assert np.array_equal(b[0][0], ((1.0 - chi[0]) * 2.0 + chi[0]) * -1.0)
     assert np.array_equal(b[0][1], chi[0] * -0.005)
     assert b[0][0][0, 2] == -1.0 and b[0][0][0, 0] == -2.0
+
+
+REG = "/root/reference/test/regression"
+
+
+@pytest.mark.skipif(not os.path.exists(REG), reason="reference tree not mounted")
+def test_regression_restart_cases():
+    """The reference's two restart regression cases read end to end: inputs
+    -> grid, parameters and walls; checkpoint -> restart state.  The grid
+    the inputs describe is the checkpoint's base level; later definitions
+    win; a wall the path does not have is refused."""
+    from mushy_gb300 import chombo_hdf5
+    # Darcy-Brinkman restart: the unit-test run, with the Hele-Shaw cell
+    # given as nonDimReluctance instead of heleShawPermeability
+    inp = mi.Inputs.read(os.path.join(REG, "AMRRestartDarcyBrinkman", "inputs"))
+    chk = chombo_hdf5.read_checkpoint(os.path.join(REG, "AMRRestartDarcyBrinkman",
+                                                   "restart.2d.hdf5"))
+    g = inp.grid(2)
+    state, (lo, hi), dx = chombo_hdf5.level_state(chk, 0)
+    assert dx == g.dx and list(hi - lo + 1) == [g.n[0], g.n[1]]
+    assert int(chk["levels"][0]["attrs"]["is_periodic_0"]) == g.periodic[0] == 0
+    p, q = inp.params()
+    ref_inp, _ = _run_inputs()
+    p_ref, q_ref = ref_inp.params()
+    for k in ("compositionRatio", "stefan", "specificHeatRatio", "waterDistributionCoeff",
+              "heatConductivityRatio", "saltDiffusionCoeff", "darcyCoeff"):
+        assert getattr(p, k) == getattr(p_ref, k), k
+    assert q["heleShawPermeability"] == q_ref["heleShawPermeability"] == 1e4
+    phi_bc, der, adb, nl = inp.hc_bcs(g)
+    cl = O.closure(abi.make_grid([g.n[0], g.n[1]], g.dx), p, state)
+    z = np.load(os.path.join(HERE, "golden", "closure_plt000100.npz"))
+    sel = z["level"] == 0
+    for key in ("T", "porosity", "Cl"):
+        assert np.array_equal(cl[key].ravel(), z[key][sel]), key
+    # Darcy restart: periodic in x, later definitions of a key win, the
+    # partition coefficient is never given (the reference keeps its -999
+    # default), and the bottom's inflow/outflow wall is not on the path
+    inp = mi.Inputs.read(os.path.join(REG, "AMRRestartDarcy", "inputs"))
+    chk = chombo_hdf5.read_checkpoint(os.path.join(REG, "AMRRestartDarcy", "restart.2d.hdf5"))
+    g = inp.grid(2)
+    state, (lo, hi), dx = chombo_hdf5.level_state(chk, 0)
+    assert dx == g.dx and list(hi - lo + 1) == [g.n[0], g.n[1]]
+    assert int(chk["levels"][0]["attrs"]["is_periodic_0"]) == g.periodic[0] == 1
+    p, q = inp.params()
+    assert q["rayleighComposition"] == 400 and q["heleShawPermeability"] == 2.0
+    assert p.waterDistributionCoeff == -999.0 and p.specificHeatRatio == 0.529
+    T, _ = inp.scalar_bcs(2, q)
+    assert T["temperatureLo"][1] == mi.INFLOW_OUTFLOW
+    with pytest.raises(ValueError, match="not on this path"):
+        inp.hc_bcs(g)
