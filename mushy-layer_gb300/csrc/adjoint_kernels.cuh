@@ -304,7 +304,7 @@ enum { ADJ_APPLY = 0, ADJ_RESIDUAL = 1 };
 // exactly (adj_bottom_direct_kernel)
 constexpr int kAdjDirectMax = 32;
 
-#if defined(MLGPU_FP64_UNIT) || defined(MLGPU_FP32_UNIT)
+#ifdef MLGPU_ADJ_UNIT  // kernels compiled in launch_f64_adj.cu only
 // closure Jacobian of every cell in the kernels' precision
 template <class T>
 __global__ void __launch_bounds__(kBlock) adj_jac_kernel(Geom G, ClosureParams cp,

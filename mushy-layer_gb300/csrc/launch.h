@@ -1,7 +1,9 @@
 // launch.h -- host launchers of the sm_103a kernels.  Each precision is
-// instantiated in its own translation unit: launch_f64.cu is compiled with
-// --fmad=false so FP64 keeps the reference's unfused evaluation (bitwise
-// parity with the CPU restatement), launch_f32.cu with FMA contraction on.
+// instantiated in its own translation units: the FP64 units (launch_f64.cu,
+// launch_f64_nlc.cu for the cached-closure (H, C) kernels, launch_f64_adj.cu
+// for the Jacobian / adjoint kernels, compiled in parallel) use --fmad=false
+// so FP64 keeps the reference's unfused evaluation (bitwise parity with the
+// CPU restatement), launch_f32.cu has FMA contraction on.
 #pragma once
 #include <cuda_runtime.h>
 #include "common.cuh"

@@ -4,9 +4,7 @@
 #define MLGPU_FP64_UNIT 1
 #include "launch_impl.cuh"
 #include "outer_fast_kernels.cuh"
-#include "nl_cached_kernels.cuh"
 #include "hcm_kernels.cuh"
-#include "adjoint_kernels.cuh"
 
 namespace mlgpu {
 
@@ -39,50 +37,6 @@ cudaError_t launch_vc_outer_fast(const OuterFast &P, int norm, cudaStream_t s) {
   long long tiles = (long long)((P.G.n0 + kOTX - 1) / kOTX) * ((P.G.n1 + kOTY - 1) / kOTY);
   int grid = (int)(tiles < kMaxBlocks ? tiles : kMaxBlocks);
   MLGPU_NORM_SWITCH(norm, (vc_outer_fast_kernel<NORM><<<grid, kOTThreads, 0, s>>>(P)));
-  return cudaGetLastError();
-}
-
-cudaError_t launch_nlc_closure(const NLArgs<double> &A, const double *phi, double *tcl,
-                               cudaStream_t s) {
-  MLGPU_DIM_SWITCH(A.G.dim, (nlc_closure_kernel<DIM><<<nlc_blocks(A.G.ncell), kNLCBlock, 0, s>>>(A, phi, tcl)));
-  return cudaGetLastError();
-}
-
-cudaError_t launch_nlc_gsrb(const NLArgs<double> &A, double *phi, const double *rhs, double *tcl,
-                            const double *lam, int pass, cudaStream_t s) {
-  const int nb = nlc_blocks(colour_threads(A.G));
-  MLGPU_DIM_SWITCH(A.G.dim, (nlc_gsrb_kernel<DIM><<<nb, kNLCBlock, 0, s>>>(A, phi, rhs, tcl, lam, pass)));
-  return cudaGetLastError();
-}
-
-cudaError_t launch_nlc_relax_block(const NLArgs<double> &A, double *phi, const double *rhs,
-                                   double *tcl, const double *lam, int sweeps, int init,
-                                   cudaStream_t s) {
-  // one warp per colour cell, at most 32 warps
-  long long nt = colour_threads(A.G);
-  int threads = (int)(32 * (nt < 32 ? (nt < 1 ? 1 : nt) : 32));
-  MLGPU_DIM_SWITCH(A.G.dim, (nlc_relax_block_kernel<DIM><<<1, threads, 0, s>>>(A, phi, rhs, tcl, lam, sweeps, init)));
-  return cudaGetLastError();
-}
-
-cudaError_t launch_nlc_op(const NLArgs<double> &A, int mode, int norm, const double *phi,
-                          const double *tcl, const double *rhs, double *out, double *copy,
-                          double *part, cudaStream_t s) {
-  const int nb = nlc_blocks(A.G.ncell);
-  if (mode == NL_RESIDUAL) {
-    MLGPU_DIM_SWITCH(A.G.dim, MLGPU_NORM_SWITCH(norm, (nlc_op_kernel<DIM, NL_RESIDUAL, NORM><<<nb, kNLCBlock, 0, s>>>(A, phi, tcl, rhs, out, copy, part))));
-  } else if (mode == NL_APPLY_PLUS) {
-    MLGPU_DIM_SWITCH(A.G.dim, (nlc_op_kernel<DIM, NL_APPLY_PLUS, -1><<<nb, kNLCBlock, 0, s>>>(A, phi, tcl, rhs, out, copy, part)));
-  } else {
-    return cudaErrorInvalidValue;
-  }
-  return cudaGetLastError();
-}
-
-cudaError_t launch_nlc_restrict(const NLArgs<double> &A, const Geom &C, const double *phi,
-                                const double *tcl, const double *rhs, double *res_c,
-                                double *phi_c, cudaStream_t s) {
-  MLGPU_DIM_SWITCH(A.G.dim, (nlc_restrict_kernel<DIM><<<nlc_blocks(C.ncell), kNLCBlock, 0, s>>>(A, C, phi, tcl, rhs, res_c, phi_c)));
   return cudaGetLastError();
 }
 
@@ -205,71 +159,6 @@ cudaError_t launch_mac_pi_bar(const Geom &G, const BCD &bc, int d, const double 
 cudaError_t launch_be_adj(long long n, const double *mu, const double *a, double dt,
                           double *old_bar, double *src_bar, cudaStream_t s) {
   be_adj_kernel<<<blocks_for(n), kBlock, 0, s>>>(n, mu, a, dt, old_bar, src_bar);
-  return cudaGetLastError();
-}
-cudaError_t launch_adj_jac(const Geom &G, const ClosureParams &cp, const double *u, double *J,
-                           cudaStream_t s) {
-  adj_jac_kernel<double><<<blocks_for(G.ncell), kBlock, 0, s>>>(G, cp, u, J);
-  return cudaGetLastError();
-}
-cudaError_t launch_porosity_jac(const Geom &G, const ClosureParams &cp, const double *u,
-                                double *dp, cudaStream_t s) {
-  porosity_jac_kernel<<<blocks_for(G.ncell), kBlock, 0, s>>>(G, cp, u, dp);
-  return cudaGetLastError();
-}
-#define MLGPU_TR_SWITCH(tr, ...) \
-  do {                            \
-    if (tr) {                     \
-      constexpr bool TR = true;   \
-      __VA_ARGS__;                \
-    } else {                      \
-      constexpr bool TR = false;  \
-      __VA_ARGS__;                \
-    }                             \
-  } while (0)
-
-cudaError_t launch_adj_op(const AdjArgs<double> &A, int mode, int norm, const double *y,
-                          const double *g, double *out, double *part, cudaStream_t s, bool tr) {
-  const int nb = blocks_for(A.G.ncell);
-  if (mode == ADJ_RESIDUAL && norm >= 0) {
-    if (!part) return cudaErrorInvalidValue;
-    MLGPU_TR_SWITCH(tr, MLGPU_DIM_SWITCH(A.G.dim, MLGPU_NORM_SWITCH(norm, (adj_op_kernel<double, DIM, ADJ_RESIDUAL, NORM, TR><<<nb, kBlock, 0, s>>>(A, y, g, out, part)))));
-  } else if (mode == ADJ_RESIDUAL) {
-    MLGPU_TR_SWITCH(tr, MLGPU_DIM_SWITCH(A.G.dim, (adj_op_kernel<double, DIM, ADJ_RESIDUAL, -1, TR><<<nb, kBlock, 0, s>>>(A, y, g, out, part))));
-  } else {
-    MLGPU_TR_SWITCH(tr, MLGPU_DIM_SWITCH(A.G.dim, (adj_op_kernel<double, DIM, ADJ_APPLY, -1, TR><<<nb, kBlock, 0, s>>>(A, y, g, out, part))));
-  }
-  return cudaGetLastError();
-}
-cudaError_t launch_adj_gsrb(const AdjArgs<double> &A, double *y, const double *g, int pass,
-                            cudaStream_t s, bool tr) {
-  MLGPU_TR_SWITCH(tr, MLGPU_DIM_SWITCH(A.G.dim, (adj_gsrb_kernel<double, DIM, TR><<<blocks_for(colour_threads(A.G)), kBlock, 0, s>>>(A, y, g, pass))));
-  return cudaGetLastError();
-}
-cudaError_t launch_adj_relax_block(const AdjArgs<double> &A, double *y, const double *g,
-                                   int sweeps, int zero, cudaStream_t s, bool tr) {
-  MLGPU_TR_SWITCH(tr, MLGPU_DIM_SWITCH(A.G.dim, (adj_relax_block_kernel<double, DIM, TR><<<1, 1024, 0, s>>>(A, y, g, sweeps, zero))));
-  return cudaGetLastError();
-}
-cudaError_t launch_adj_minv(const AdjArgs<double> &A, const double *zero, double *Minv,
-                            cudaStream_t s) {
-  MLGPU_DIM_SWITCH(A.G.dim, (adj_minv_kernel<double, DIM><<<blocks_for(A.G.ncell), kBlock, 0, s>>>(A, zero, Minv)));
-  return cudaGetLastError();
-}
-cudaError_t launch_adj_bottom_direct(const AdjArgs<double> &A, double *y, const double *g,
-                                     cudaStream_t s, bool tr) {
-  if (2 * A.G.ncell > kAdjDirectMax) return cudaErrorInvalidValue;
-  MLGPU_TR_SWITCH(tr, MLGPU_DIM_SWITCH(A.G.dim, (adj_bottom_direct_kernel<double, DIM, TR><<<1, kAdjDirectMax, 0, s>>>(A, y, g))));
-  return cudaGetLastError();
-}
-cudaError_t launch_adj_restrict(const AdjArgs<double> &A, const Geom &C, const double *y,
-                                const double *g, double *gc, cudaStream_t s, bool tr) {
-  MLGPU_TR_SWITCH(tr, MLGPU_DIM_SWITCH(A.G.dim, (adj_restrict_kernel<double, DIM, TR><<<blocks_for(C.ncell), kBlock, 0, s>>>(A, C, y, g, gc))));
-  return cudaGetLastError();
-}
-cudaError_t launch_adj_bc_grad(const AdjArgs<double> &A, const double *y, double *out,
-                               cudaStream_t s) {
-  MLGPU_DIM_SWITCH(A.G.dim, (adj_bc_grad_kernel<double, DIM><<<6, kBlock, 0, s>>>(A, y, out)));
   return cudaGetLastError();
 }
 

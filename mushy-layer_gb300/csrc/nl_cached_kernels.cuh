@@ -27,7 +27,7 @@ inline int nlc_blocks(long long n) {
   return (int)b;
 }
 
-#ifdef MLGPU_FP64_UNIT  // kernels compiled in launch_f64.cu only
+#ifdef MLGPU_NLC_UNIT  // kernels compiled in launch_f64_nlc.cu only
 // (T, C_l) at neighbour (i,j,k) + s e_d of an interior cell whose own (H, C)
 // and (T, C_l) are h0, c0, t0, l0 (nl_dv_nb with the cache)
 __device__ __forceinline__ void nlc_dv_nb(const NLArgs<double> &A, const double *tcl, int i, int j,
@@ -246,6 +246,6 @@ __global__ void __launch_bounds__(kNLCBlock) nlc_restrict_kernel(NLArgs<double> 
     }
   }
 }
-#endif  // MLGPU_FP64_UNIT
+#endif  // MLGPU_NLC_UNIT
 
 }  // namespace mlgpu

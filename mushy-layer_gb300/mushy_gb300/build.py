@@ -24,6 +24,8 @@ COMMON = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contra
           "-I" + os.path.join(REPO, "include")]
 UNITS = {
     "launch_f64.cu": ["--fmad=false"],
+    "launch_f64_adj.cu": ["--fmad=false"],
+    "launch_f64_nlc.cu": ["--fmad=false"],
     "launch_f32.cu": [],
     "capi.cu": ["--fmad=false"],
     "solver.cu": ["--fmad=false"],
