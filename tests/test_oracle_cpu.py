@@ -520,3 +520,31 @@ def test_mac_projection_properties():
                 for d, (a, b) in enumerate(zip(u1, [x / y for x, y in zip(gp, pi)])))
     norm = np.sqrt(sum((a * a).sum() for a in u1) * sum((b * b).sum() for b in gp))
     assert abs(inner) <= 1e-9 * norm
+
+
+@pytest.mark.parametrize("dim", [2, 3])
+def test_linear_prolongation_exact_on_linear_fields(dim):
+    """Linear prolongation (weights 3/4, 1/4 per direction) reproduces a
+    linear field exactly at every fine cell whose stencil stays inside the
+    box; piecewise-constant prolongation copies the coarse value to its
+    2^D children everywhere."""
+    n = [16, 12, 8][:dim]
+    g = abi.make_grid(n, 1.0 / n[0])
+    cs = O.coarse_shape(g, 1)
+    H = g.dx * 2
+    k, j, i = np.meshgrid(*[np.arange(m) for m in cs[1:]], indexing="ij")
+    slope = (0.7, -1.3, 0.4)
+    lin = lambda x, y, z: 2.0 + slope[0] * x + slope[1] * y + (slope[2] * z if dim == 3 else 0)
+    coarse = lin((i + 0.5) * H, (j + 0.5) * H, (k + 0.5) * H)[None]
+    zero = np.zeros((1,) + abi.cell_shape(g))
+    fine = O.prolong_increment(g, abi.make_bc(), 1, abi.PROLONG_LINEAR, zero, coarse)
+    kf, jf, if_ = np.meshgrid(*[np.arange(m) for m in abi.cell_shape(g)], indexing="ij")
+    want = lin((if_ + 0.5) * g.dx, (jf + 0.5) * g.dx, (kf + 0.5) * g.dx)
+    inner = (slice(1, -1) if dim == 3 else slice(None), slice(1, -1), slice(1, -1))
+    assert np.abs(fine[0][inner] - want[inner]).max() <= 1e-13
+    const = O.prolong_increment(g, abi.make_bc(), 1, abi.PROLONG_CONSTANT, zero, coarse)
+    rep = coarse[0]
+    for ax in range(3):
+        if const[0].shape[ax] == 2 * rep.shape[ax]:
+            rep = np.repeat(rep, 2, axis=ax)
+    assert np.array_equal(const[0], rep)
