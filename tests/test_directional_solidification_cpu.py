@@ -19,6 +19,8 @@ cell temperatures and porosities converge to the analytic profile at second
 order.  The device solvers equal the oracle bit for bit (GPU tests), so the
 pin carries over to them.
 """
+import os
+
 import numpy as np
 import pytest
 from scipy.optimize import brentq
@@ -27,7 +29,8 @@ from mushy_gb300 import abi
 from oracle import oracle as O
 
 ST, CR, K, V = 5.0, 5.0, 1e-3, 1.0
-T_BOTTOM, H_BOTTOM, T_TOP = 1.1, 6.1, 0.0
+H_BOTTOM, T_TOP = 6.1, 0.0
+T_BOTTOM = H_BOTTOM - ST   # the liquid closure of the bottom wall, as the reference forms it
 Z_EUTECTIC = 1.0   # the top wall: the top temperature is the eutectic's
 
 
@@ -118,3 +121,27 @@ def test_steady_mushy_layer_converges_to_the_analytic_profile():
     assert ec16 < 4e-4 and ec32 < 1.2e-4, errs
     # second order in dz
     assert eT16 / eT32 > 3.2 and ec16 / ec32 > 3.0, errs
+
+
+PARAMS = "/root/reference/params/convergenceTest/noFlowConvTest.parameters"
+
+
+@pytest.mark.skipif(not os.path.exists(PARAMS), reason="reference tree not mounted")
+def test_setup_is_the_reference_parameter_file():
+    """The constants above are what the inputs reader derives from the
+    reference's own parameter file of that test."""
+    from mushy_gb300.inputs import Inputs
+    inp = Inputs.read(PARAMS)
+    p, q = inp.params()
+    assert (p.stefan, p.compositionRatio, p.waterDistributionCoeff) == (ST, CR, K)
+    assert (p.specificHeatRatio, p.heatConductivityRatio) == (1.0, 1.0)
+    assert (p.thetaEutectic, p.ThetaEutectic, q["ThetaInitial"]) == (0.0, 0.0, -1.0)
+    assert inp.get("parameters.nonDimVel") == V        # the later definition wins
+    assert p.saltDiffusionCoeff == 1e-300             # Lewis number 1e300
+    g = inp.grid(2)
+    assert g.periodic[0] == 1 and g.periodic[1] == 0
+    phi_bc, der, adb, nl = inp.hc_bcs(g)
+    assert adb == 1
+    assert (der.type[1][0][0], der.value[1][0][0]) == (abi.BC_DIRICHLET, T_BOTTOM)
+    assert (der.type[1][1][0], der.value[1][1][0]) == (abi.BC_DIRICHLET, T_TOP)
+    assert (der.value[1][0][1], der.value[1][1][1]) == (-1.0, 0.0)
