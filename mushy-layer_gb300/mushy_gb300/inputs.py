@@ -359,6 +359,13 @@ class Inputs:
                         der[(d, s, c)] = (abi.BC_DIRICHLET, V[var + lab][d])
                     elif t == NEUMANN:
                         der[(d, s, c)] = (abi.BC_NEUMANN, 0.0)
+                    elif t == MIXED_T_S:
+                        raise ValueError(
+                            "bc type 9 (MixedBCTemperatureSalinity, a linear Robin ghost "
+                            "on the diagnostic temperature) of %s on side %s of direction "
+                            "%d is not on this path: give the enthalpy the same condition "
+                            "as TemperatureFluxRadiation (type 8) with "
+                            "main.apply_diagnostic_bcs = false" % (var, lab, d))
                     else:
                         raise ValueError(
                             "bc type %d of %s on side %s of direction %d is not on this "
