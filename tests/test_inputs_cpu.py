@@ -263,3 +263,22 @@ def test_regression_restart_cases():
     assert T["temperatureLo"][1] == mi.INFLOW_OUTFLOW
     with pytest.raises(ValueError, match="not on this path"):
         inp.hc_bcs(g)
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(os.path.dirname(REG), "diffusiveGrowth")),
+                    reason="reference tree not mounted")
+def test_diffusive_growth_inputs():
+    """The reference's diffusive-growth case: its Robin coefficients read
+    (through single precision, exact here), and its top wall, a mixed
+    temperature/salinity condition on the diagnostic temperature, refused
+    with the equivalent condition on the enthalpy named."""
+    inp = mi.Inputs.read(os.path.join(os.path.dirname(REG), "diffusiveGrowth", "inputs"))
+    g = inp.grid(2)
+    T, V = inp.scalar_bcs(2)
+    assert T["temperatureHi"][1] == mi.MIXED_T_S
+    with pytest.raises(ValueError, match="MixedBCTemperatureSalinity"):
+        inp.hc_bcs(g)
+    a, b = inp._bc_info("a", 2), inp._bc_info("b", 2)
+    tref = inp._bc_info("TRef", 2)
+    assert (a[1][1], b[1][1], tref[1][1]) == (0.5, -1.0, 4.0)
+    assert (a[0][1], b[0][1], tref[0][1]) == (1.0, 1.0, 0.0)
