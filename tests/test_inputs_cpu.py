@@ -282,3 +282,20 @@ def test_diffusive_growth_inputs():
     tref = inp._bc_info("TRef", 2)
     assert (a[1][1], b[1][1], tref[1][1]) == (0.5, -1.0, 4.0)
     assert (a[0][1], b[0][1], tref[0][1]) == (1.0, 1.0, 0.0)
+
+
+POISEUILLE = os.path.join(os.path.dirname(REG), "poiseuilleFlow", "inputs")
+
+
+@pytest.mark.skipif(not os.path.exists(POISEUILLE), reason="reference tree not mounted")
+def test_poiseuille_inputs_give_the_pinned_coefficients():
+    """The reference's Poiseuille case (Da 0.01, Pr 1, diffusive timescale):
+    the Darcy-Brinkman coefficients the reader derives are the ones the
+    Poiseuille-Brinkman pin of the oracle uses, c = chi / (Pi Da) = 100 for
+    chi = Pi = 1 and viscosity 1 (b = -1)."""
+    inp = mi.Inputs.read(POISEUILLE)
+    p, q = inp.params()
+    assert q["nondimensionalisation"] == 0 and q["darcy"] == 0.01 and q["prandtl"] == 1.0
+    assert p.darcyCoeff == 1 / 0.01 == 100.0 and p.viscosityCoeff == 1.0
+    g = inp.grid(2)
+    assert list(g.n)[:2] == [64, 64] and g.dx == 1.0 / 64
