@@ -302,7 +302,9 @@ int mlgpu_vc_jacobi(const mlgpu_vcop *op, void *phi, const void *rhs,
    1,048,576 FP64 / 2,097,152 FP32 cells (else MLGPU_ERR_SCRATCH, nothing
    launched).  One scratch per device: calls that may overlap in time on one
    device race.  The first call on a device looks the scratch up and should
-   come before any stream capture. */
+   come before any stream capture; the address is kept until exit, so after a
+   reset of that device's context the library must be reloaded before this
+   entry point is called there again. */
 int mlgpu_vc_jacobi_noalloc(const mlgpu_vcop *op, void *phi, const void *rhs,
                             void *stream);
 int mlgpu_vc_lambda(const mlgpu_vcop *op, void *lambda, void *stream);

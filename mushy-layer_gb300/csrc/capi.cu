@@ -245,7 +245,7 @@ int mlgpu_hc_adjoint_apply(const mlgpu_nlop *op, const double *phi, const double
                            const double *y, const double *g, double *out, void *stream) {
   if (!valid_adjoint_op(op) || !phi || !J || !y || !out) return MLGPU_ERR_ARG;
   return status_of(launch_adj_op(make_adj_args(*op, phi, J), g ? ADJ_RESIDUAL : ADJ_APPLY, -1,
-                                 y, g, out, nullptr, (cudaStream_t)stream));
+                                 y, g, out, nullptr, nullptr, (cudaStream_t)stream));
 }
 
 int mlgpu_hc_adjoint_gsrb_pass(const mlgpu_nlop *op, const double *phi, const double *J,
@@ -259,7 +259,7 @@ int mlgpu_hc_linearized_apply(const mlgpu_nlop *op, const double *phi, const dou
                               const double *x, const double *r, double *out, void *stream) {
   if (!valid_adjoint_op(op) || !phi || !J || !x || !out) return MLGPU_ERR_ARG;
   return status_of(launch_adj_op(make_adj_args(*op, phi, J), r ? ADJ_RESIDUAL : ADJ_APPLY, -1, x,
-                                 r, out, nullptr, (cudaStream_t)stream, false));
+                                 r, out, nullptr, nullptr, (cudaStream_t)stream, false));
 }
 
 int mlgpu_hc_linearized_gsrb_pass(const mlgpu_nlop *op, const double *phi, const double *J,
@@ -289,18 +289,18 @@ int mlgpu_nl_residual(const mlgpu_nlop *op, void *res, const void *phi, const vo
   if (want && (!norm || !ws)) return MLGPU_ERR_ARG;
   if (want && ws_bytes < mlgpu_norm_workspace_bytes()) return MLGPU_ERR_WORKSPACE;
   cudaStream_t s = (cudaStream_t)stream;
-  double *part = (double *)ws;
-  int nt = want ? norm_type : -1;
+  double *part = want ? (double *)ws : nullptr;
+  int nt = want ? norm_type : -1, nparts = 0;
   cudaError_t e;
   if (op->dtype == MLGPU_F64)
     e = launch_nl_op<double>(make_nl_args<double>(*op), NL_RESIDUAL, nt, (const double *)phi,
-                             (const double *)rhs, (double *)res, nullptr, part, s);
+                             (const double *)rhs, (double *)res, nullptr, part, &nparts, s);
   else
     e = launch_nl_op<float>(make_nl_args<float>(*op), NL_RESIDUAL, nt, (const float *)phi,
-                            (const float *)rhs, (float *)res, nullptr, part, s);
+                            (const float *)rhs, (float *)res, nullptr, part, &nparts, s);
   if (e != cudaSuccess) return MLGPU_ERR_CUDA;
   if (!want) return MLGPU_OK;
-  return finish_norm(norm_type, part, norm_parts(make_geom(op->grid).ncell), norm, s);
+  return finish_norm(norm_type, part, nparts, norm, s);
 }
 
 int mlgpu_nl_apply(const mlgpu_nlop *op, void *lhs, const void *phi, void *stream) {
@@ -309,10 +309,10 @@ int mlgpu_nl_apply(const mlgpu_nlop *op, void *lhs, const void *phi, void *strea
   cudaError_t e;
   if (op->dtype == MLGPU_F64)
     e = launch_nl_op<double>(make_nl_args<double>(*op), NL_APPLY, -1, (const double *)phi,
-                             nullptr, (double *)lhs, nullptr, nullptr, s);
+                             nullptr, (double *)lhs, nullptr, nullptr, nullptr, s);
   else
     e = launch_nl_op<float>(make_nl_args<float>(*op), NL_APPLY, -1, (const float *)phi, nullptr,
-                            (float *)lhs, nullptr, nullptr, s);
+                            (float *)lhs, nullptr, nullptr, nullptr, s);
   return status_of(e);
 }
 
@@ -348,11 +348,11 @@ int mlgpu_nl_jacobi(const mlgpu_nlop *op, void *phi, const void *rhs, void *tmp,
   size_t bytes;
   if (op->dtype == MLGPU_F64) {
     e = launch_nl_op<double>(make_nl_args<double>(*op), NL_JACOBI, -1, (const double *)phi,
-                             (const double *)rhs, (double *)tmp, nullptr, nullptr, s);
+                             (const double *)rhs, (double *)tmp, nullptr, nullptr, nullptr, s);
     bytes = n * sizeof(double);
   } else {
     e = launch_nl_op<float>(make_nl_args<float>(*op), NL_JACOBI, -1, (const float *)phi,
-                            (const float *)rhs, (float *)tmp, nullptr, nullptr, s);
+                            (const float *)rhs, (float *)tmp, nullptr, nullptr, nullptr, s);
     bytes = n * sizeof(float);
   }
   if (e != cudaSuccess) return MLGPU_ERR_CUDA;
@@ -441,18 +441,18 @@ int mlgpu_vc_residual(const mlgpu_vcop *op, void *res, const void *phi, const vo
   if (want && (!norm || !ws)) return MLGPU_ERR_ARG;
   if (want && ws_bytes < mlgpu_norm_workspace_bytes()) return MLGPU_ERR_WORKSPACE;
   cudaStream_t s = (cudaStream_t)stream;
-  double *part = (double *)ws;
-  int nt = want ? norm_type : -1;
+  double *part = want ? (double *)ws : nullptr;
+  int nt = want ? norm_type : -1, nparts = 0;
   cudaError_t e;
   if (op->dtype == MLGPU_F64)
     e = launch_vc_op<double>(make_vc_args<double>(*op), VC_RESIDUAL, nt, (const double *)phi,
-                             (const double *)rhs, (double *)res, homogeneous, part, s);
+                             (const double *)rhs, (double *)res, homogeneous, part, &nparts, s);
   else
     e = launch_vc_op<float>(make_vc_args<float>(*op), VC_RESIDUAL, nt, (const float *)phi,
-                            (const float *)rhs, (float *)res, homogeneous, part, s);
+                            (const float *)rhs, (float *)res, homogeneous, part, &nparts, s);
   if (e != cudaSuccess) return MLGPU_ERR_CUDA;
   if (!want) return MLGPU_OK;
-  return finish_norm(norm_type, part, norm_parts(make_geom(op->grid).ncell), norm, s);
+  return finish_norm(norm_type, part, nparts, norm, s);
 }
 
 int mlgpu_vc_apply(const mlgpu_vcop *op, void *lhs, const void *phi, int homogeneous,
@@ -462,9 +462,9 @@ int mlgpu_vc_apply(const mlgpu_vcop *op, void *lhs, const void *phi, int homogen
   if (op->dtype == MLGPU_F64)
     return status_of(launch_vc_op<double>(make_vc_args<double>(*op), VC_APPLY, -1,
                                           (const double *)phi, nullptr, (double *)lhs,
-                                          homogeneous, nullptr, s));
+                                          homogeneous, nullptr, nullptr, s));
   return status_of(launch_vc_op<float>(make_vc_args<float>(*op), VC_APPLY, -1, (const float *)phi,
-                                       nullptr, (float *)lhs, homogeneous, nullptr, s));
+                                       nullptr, (float *)lhs, homogeneous, nullptr, nullptr, s));
 }
 
 int mlgpu_vc_gsrb_pass(const mlgpu_vcop *op, void *phi, const void *rhs, int pass,
@@ -496,11 +496,11 @@ int mlgpu_vc_jacobi(const mlgpu_vcop *op, void *phi, const void *rhs, void *tmp,
   size_t bytes;
   if (op->dtype == MLGPU_F64) {
     e = launch_vc_op<double>(make_vc_args<double>(*op), VC_JACOBI, -1, (const double *)phi,
-                             (const double *)rhs, (double *)tmp, 1, nullptr, s);
+                             (const double *)rhs, (double *)tmp, 1, nullptr, nullptr, s);
     bytes = n * sizeof(double);
   } else {
     e = launch_vc_op<float>(make_vc_args<float>(*op), VC_JACOBI, -1, (const float *)phi,
-                            (const float *)rhs, (float *)tmp, 1, nullptr, s);
+                            (const float *)rhs, (float *)tmp, 1, nullptr, nullptr, s);
     bytes = n * sizeof(float);
   }
   if (e != cudaSuccess) return MLGPU_ERR_CUDA;
@@ -566,15 +566,16 @@ int mlgpu_norm(size_t n, int dtype, const void *x, int norm_type, double *out, v
   if (ws_bytes < mlgpu_norm_workspace_bytes()) return MLGPU_ERR_WORKSPACE;
   cudaStream_t s = (cudaStream_t)stream;
   double *part = (double *)ws;
+  int nparts = 0;
   cudaError_t e;
   if (dtype == MLGPU_F64)
-    e = launch_norm_partial<double>((long long)n, (const double *)x, norm_type, part, s);
+    e = launch_norm_partial<double>((long long)n, (const double *)x, norm_type, part, &nparts, s);
   else if (dtype == MLGPU_F32)
-    e = launch_norm_partial<float>((long long)n, (const float *)x, norm_type, part, s);
+    e = launch_norm_partial<float>((long long)n, (const float *)x, norm_type, part, &nparts, s);
   else
     return MLGPU_ERR_ARG;
   if (e != cudaSuccess) return MLGPU_ERR_CUDA;
-  return finish_norm(norm_type, part, norm_parts((long long)n), out, s);
+  return finish_norm(norm_type, part, nparts, out, s);
 }
 
 int mlgpu_convert(size_t n, int dd, void *dst, int ds, const void *src, void *stream) {

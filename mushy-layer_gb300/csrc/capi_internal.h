@@ -56,8 +56,8 @@ cudaError_t launch_porosity_jac(const Geom &G, const ClosureParams &cp, const do
                                 double *dp, cudaStream_t s);
 // tr: A^T (the adjoint) or A (the linearised operator of a Newton step)
 cudaError_t launch_adj_op(const AdjArgs<double> &A, int mode, int norm, const double *y,
-                          const double *g, double *out, double *part, cudaStream_t s,
-                          bool tr = true);
+                          const double *g, double *out, double *part, int *nparts,
+                          cudaStream_t s, bool tr = true);
 cudaError_t launch_adj_gsrb(const AdjArgs<double> &A, double *y, const double *g, int pass,
                             cudaStream_t s, bool tr = true);
 cudaError_t launch_adj_relax_block(const AdjArgs<double> &A, double *y, const double *g,
@@ -87,7 +87,7 @@ cudaError_t launch_nlc_relax_block(const NLArgs<double> &A, double *phi, const d
                                    cudaStream_t s);
 cudaError_t launch_nlc_op(const NLArgs<double> &A, int mode, int norm, const double *phi,
                           const double *tcl, const double *rhs, double *out, double *copy,
-                          double *part, cudaStream_t s);
+                          double *part, int *nparts, cudaStream_t s);
 cudaError_t launch_nlc_restrict(const NLArgs<double> &A, const Geom &C, const double *phi,
                                 const double *tcl, const double *rhs, double *res_c,
                                 double *phi_c, cudaStream_t s);

@@ -23,6 +23,10 @@
 //  * the first call on each device looks up the scratch address with
 //    cudaGetSymbolAddress while that device is current; make that first call
 //    before any stream capture begins.
+//  * the address is kept for the life of the process.  A cudaDeviceReset
+//    (or any other reset of a device's primary context) destroys the context
+//    it belongs to, so a process that resets a device must not call this
+//    entry point on that device again without reloading the library.
 #include <mutex>
 
 #include "capi_internal.h"
@@ -71,10 +75,10 @@ extern "C" int mlgpu_vc_jacobi_noalloc(const mlgpu_vcop *op, void *phi, const vo
   cudaError_t e;
   if (op->dtype == MLGPU_F64)
     e = launch_vc_op<double>(make_vc_args<double>(*op), VC_JACOBI, -1, (const double *)phi,
-                             (const double *)rhs, (double *)tmp, 1, nullptr, s);
+                             (const double *)rhs, (double *)tmp, 1, nullptr, nullptr, s);
   else
     e = launch_vc_op<float>(make_vc_args<float>(*op), VC_JACOBI, -1, (const float *)phi,
-                            (const float *)rhs, (float *)tmp, 1, nullptr, s);
+                            (const float *)rhs, (float *)tmp, 1, nullptr, nullptr, s);
   if (e != cudaSuccess) return MLGPU_ERR_CUDA;
   return status_of(cudaMemcpyAsync(phi, tmp, bytes, cudaMemcpyDeviceToDevice, s));
 }

@@ -148,7 +148,10 @@ __device__ __forceinline__ void t_cl(double H, double C, const ClosureParams &p,
   } else if (H >= Hl) {
     T = H - p.St;
     Cl = C;
-  } else {  // NaN input
+  } else {
+    // NaN input (a departure from CALCULATE_T_CL, which takes no branch and
+    // leaves the output untouched): T and C_l become NaN so the solvers'
+    // NaN detection sees the poisoned state
     T = H;
     Cl = C;
   }

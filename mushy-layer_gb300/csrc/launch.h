@@ -28,7 +28,7 @@ constexpr size_t kNormScratchDoubles = kMaxBlocks + 8;
 
 template <class T>
 cudaError_t launch_nl_op(const NLArgs<T> &A, int mode, int norm, const T *phi, const T *rhs, T *out,
-                         T *copy, double *part, cudaStream_t s);
+                         T *copy, double *part, int *nparts, cudaStream_t s);
 template <class T>
 cudaError_t launch_nl_gsrb(const NLArgs<T> &A, T *phi, const T *rhs, int pass, cudaStream_t s);
 template <class T>
@@ -42,11 +42,12 @@ cudaError_t launch_nl_lambda(const NLArgs<T> &A, T *lam, cudaStream_t s);
 
 template <class T>
 cudaError_t launch_vc_op(const VCArgs<T> &A, int mode, int norm, const T *phi, const T *rhs, T *out,
-                         int homog, double *part, cudaStream_t s);
+                         int homog, double *part, int *nparts, cudaStream_t s);
 template <class T, class E>
 cudaError_t launch_vc_update_residual(const VCArgs<T> &A, int norm, const T *phi, const E *e,
                                       const T *rhs, T *out_phi, T *res, E *res_inner,
-                                      double *part, cudaStream_t s, const int *par = nullptr);
+                                      double *part, int *nparts, cudaStream_t s,
+                                      const int *par = nullptr);
 template <class T>
 cudaError_t launch_vc_gsrb(const VCArgs<T> &A, T *phi, const T *rhs, int pass, cudaStream_t s);
 template <class T>
@@ -96,12 +97,15 @@ cudaError_t launch_coarsen_faces(const Geom &F, int ncomp, int d, const T *ff, T
 template <class T>
 cudaError_t launch_axpby(long long n, T a, const T *x, T b, T *y, cudaStream_t s);
 template <class T>
-cudaError_t launch_norm_partial(long long n, const T *x, int norm, double *part, cudaStream_t s);
+cudaError_t launch_norm_partial(long long n, const T *x, int norm, double *part, int *nparts,
+                                cudaStream_t s);
 template <class D, class S>
 cudaError_t launch_convert(long long n, D *dst, const S *src, cudaStream_t s);
 
-// number of partials a fused-norm launch over n items writes
-inline int norm_parts(long long n) { return blocks_for(n); }
+// Every launcher that writes fused-norm partials (one per block) stores the
+// number it wrote in *nparts (when part is non-null); the finalize call is
+// given that count, so a launch and the combine of its partials cannot
+// disagree about the grid.
 cudaError_t launch_finalize_norm(int norm, const double *part, int nparts, double *out,
                                  cudaStream_t s);
 

@@ -10,7 +10,8 @@
 namespace mlgpu {
 
 template cudaError_t launch_nl_op<float>(const NLArgs<float> &, int, int, const float *,
-                                         const float *, float *, float *, double *, cudaStream_t);
+                                         const float *, float *, float *, double *, int *,
+                                         cudaStream_t);
 template cudaError_t launch_nl_gsrb<float>(const NLArgs<float> &, float *, const float *, int,
                                            cudaStream_t);
 template cudaError_t launch_nl_relax_block<float>(const NLArgs<float> &, float *, const float *,
@@ -19,7 +20,8 @@ template cudaError_t launch_nl_restrict<float>(const NLArgs<float> &, const Geom
                                                const float *, float *, float *, cudaStream_t);
 template cudaError_t launch_nl_lambda<float>(const NLArgs<float> &, float *, cudaStream_t);
 template cudaError_t launch_vc_op<float>(const VCArgs<float> &, int, int, const float *,
-                                         const float *, float *, int, double *, cudaStream_t);
+                                         const float *, float *, int, double *, int *,
+                                         cudaStream_t);
 template cudaError_t launch_vc_gsrb<float>(const VCArgs<float> &, float *, const float *, int,
                                            cudaStream_t);
 template cudaError_t launch_vc_gsrb_zero<float>(const VCArgs<float> &, float *, const float *,
@@ -37,7 +39,7 @@ template cudaError_t launch_coarsen_faces<float>(const Geom &, int, int, const f
                                                  cudaStream_t);
 template cudaError_t launch_axpby<float>(long long, float, const float *, float, float *,
                                          cudaStream_t);
-template cudaError_t launch_norm_partial<float>(long long, const float *, int, double *,
+template cudaError_t launch_norm_partial<float>(long long, const float *, int, double *, int *,
                                                 cudaStream_t);
 template cudaError_t launch_convert<float, double>(long long, float *, const double *,
                                                   cudaStream_t);

@@ -9,7 +9,7 @@
 namespace mlgpu {
 
 template cudaError_t launch_nl_op<double>(const NLArgs<double> &, int, int, const double *,
-                                          const double *, double *, double *, double *,
+                                          const double *, double *, double *, double *, int *,
                                           cudaStream_t);
 template cudaError_t launch_nl_gsrb<double>(const NLArgs<double> &, double *, const double *, int,
                                             cudaStream_t);
@@ -20,17 +20,18 @@ template cudaError_t launch_nl_restrict<double>(const NLArgs<double> &, const Ge
                                                 double *, cudaStream_t);
 template cudaError_t launch_nl_lambda<double>(const NLArgs<double> &, double *, cudaStream_t);
 template cudaError_t launch_vc_op<double>(const VCArgs<double> &, int, int, const double *,
-                                          const double *, double *, int, double *, cudaStream_t);
+                                          const double *, double *, int, double *, int *,
+                                          cudaStream_t);
 template cudaError_t launch_vc_update_residual<double, double>(const VCArgs<double> &, int,
                                                                const double *, const double *,
                                                                const double *, double *,
                                                                double *, double *, double *,
-                                                               cudaStream_t, const int *);
+                                                               int *, cudaStream_t, const int *);
 template cudaError_t launch_vc_update_residual<double, float>(const VCArgs<double> &, int,
                                                               const double *, const float *,
                                                               const double *, double *, double *,
-                                                              float *, double *, cudaStream_t,
-                                                              const int *);
+                                                              float *, double *, int *,
+                                                              cudaStream_t, const int *);
 
 cudaError_t launch_vc_outer_fast(const OuterFast &P, int norm, cudaStream_t s) {
   if (P.G.dim != 2 || !P.count || !P.part || !P.res_inner) return cudaErrorInvalidValue;
@@ -83,7 +84,7 @@ template cudaError_t launch_coarsen_faces<double>(const Geom &, int, int, const 
                                                   cudaStream_t);
 template cudaError_t launch_axpby<double>(long long, double, const double *, double, double *,
                                           cudaStream_t);
-template cudaError_t launch_norm_partial<double>(long long, const double *, int, double *,
+template cudaError_t launch_norm_partial<double>(long long, const double *, int, double *, int *,
                                                  cudaStream_t);
 template cudaError_t launch_convert<double, float>(long long, double *, const float *,
                                                    cudaStream_t);
@@ -92,6 +93,8 @@ template cudaError_t launch_convert<double, double>(long long, double *, const d
 
 cudaError_t launch_finalize_norm(int norm, const double *part, int nparts, double *out,
                                  cudaStream_t s) {
+  // nparts comes from the launch that wrote the partials; 0 means it wrote none
+  if (nparts < 1 || nparts > kMaxBlocks) return cudaErrorInvalidValue;
   switch (norm) {
     case MLGPU_NORM_L1:
       finalize_norm_kernel<MLGPU_NORM_L1><<<1, 1024, 0, s>>>(part, nparts, out);

@@ -29,8 +29,10 @@ cudaError_t launch_porosity_jac(const Geom &G, const ClosureParams &cp, const do
   } while (0)
 
 cudaError_t launch_adj_op(const AdjArgs<double> &A, int mode, int norm, const double *y,
-                          const double *g, double *out, double *part, cudaStream_t s, bool tr) {
+                          const double *g, double *out, double *part, int *nparts,
+                          cudaStream_t s, bool tr) {
   const int nb = blocks_for(A.G.ncell);
+  if (nparts) *nparts = (part && mode == ADJ_RESIDUAL && norm >= 0) ? nb : 0;
   if (mode == ADJ_RESIDUAL && norm >= 0) {
     if (!part) return cudaErrorInvalidValue;
     MLGPU_TR_SWITCH(tr, MLGPU_DIM_SWITCH(A.G.dim, MLGPU_NORM_SWITCH(norm, (adj_op_kernel<double, DIM, ADJ_RESIDUAL, NORM, TR><<<nb, kBlock, 0, s>>>(A, y, g, out, part)))));

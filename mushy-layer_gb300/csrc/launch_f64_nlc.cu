@@ -33,8 +33,9 @@ cudaError_t launch_nlc_relax_block(const NLArgs<double> &A, double *phi, const d
 
 cudaError_t launch_nlc_op(const NLArgs<double> &A, int mode, int norm, const double *phi,
                           const double *tcl, const double *rhs, double *out, double *copy,
-                          double *part, cudaStream_t s) {
+                          double *part, int *nparts, cudaStream_t s) {
   const int nb = nlc_blocks(A.G.ncell);
+  if (nparts) *nparts = (part && mode == NL_RESIDUAL && norm >= 0) ? nb : 0;
   if (mode == NL_RESIDUAL) {
     MLGPU_DIM_SWITCH(A.G.dim, MLGPU_NORM_SWITCH(norm, (nlc_op_kernel<DIM, NL_RESIDUAL, NORM><<<nb, kNLCBlock, 0, s>>>(A, phi, tcl, rhs, out, copy, part))));
   } else if (mode == NL_APPLY_PLUS) {

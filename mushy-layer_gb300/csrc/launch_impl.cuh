@@ -66,8 +66,9 @@ cudaError_t launch_vc_tile_smooth(const TileSmooth<T> &P, cudaStream_t s) {
 
 template <class T>
 cudaError_t launch_nl_op(const NLArgs<T> &A, int mode, int norm, const T *phi, const T *rhs, T *out,
-                         T *copy, double *part, cudaStream_t s) {
+                         T *copy, double *part, int *nparts, cudaStream_t s) {
   int nb = blocks_for(A.G.ncell);
+  if (nparts) *nparts = (part && norm >= 0) ? nb : 0;
   MLGPU_DIM_SWITCH(A.G.dim, MLGPU_NORM_SWITCH(norm, {
     switch (mode) {
       case NL_RESIDUAL:
@@ -122,8 +123,9 @@ cudaError_t launch_nl_lambda(const NLArgs<T> &A, T *lam, cudaStream_t s) {
 
 template <class T>
 cudaError_t launch_vc_op(const VCArgs<T> &A, int mode, int norm, const T *phi, const T *rhs, T *out,
-                         int homog, double *part, cudaStream_t s) {
+                         int homog, double *part, int *nparts, cudaStream_t s) {
   int nb = blocks_for(A.G.ncell);
+  if (nparts) *nparts = (part && norm >= 0) ? nb : 0;
   MLGPU_DIM_SWITCH(A.G.dim, MLGPU_NORM_SWITCH(norm, {
     switch (mode) {
       case VC_RESIDUAL:
@@ -143,8 +145,10 @@ cudaError_t launch_vc_op(const VCArgs<T> &A, int mode, int norm, const T *phi, c
 template <class T, class E>
 cudaError_t launch_vc_update_residual(const VCArgs<T> &A, int norm, const T *phi, const E *e,
                                       const T *rhs, T *out_phi, T *res, E *res_inner,
-                                      double *part, cudaStream_t s, const int *par) {
+                                      double *part, int *nparts, cudaStream_t s,
+                                      const int *par) {
   int nb = blocks_for(A.G.ncell);
+  if (nparts) *nparts = nb;
   if (norm < 0) norm = MLGPU_NORM_MAX;
   MLGPU_DIM_SWITCH(A.G.dim, MLGPU_NORM_SWITCH(norm, {
     if (NORM >= 0)
@@ -244,8 +248,10 @@ cudaError_t launch_axpby(long long n, T a, const T *x, T b, T *y, cudaStream_t s
 }
 
 template <class T>
-cudaError_t launch_norm_partial(long long n, const T *x, int norm, double *part, cudaStream_t s) {
+cudaError_t launch_norm_partial(long long n, const T *x, int norm, double *part, int *nparts,
+                                cudaStream_t s) {
   int nb = blocks_for(n);
+  if (nparts) *nparts = norm >= 0 ? nb : 0;
   MLGPU_NORM_SWITCH(norm, {
     if (NORM >= 0) norm_partial_kernel<T, (NORM < 0 ? 0 : NORM)><<<nb, kBlock, 0, s>>>(n, x, part);
   });

@@ -448,7 +448,7 @@ class VCSolver : public mlgpu_solver {
     if (o.relax_mode == MLGPU_RELAX_JACOBI) {
       if (zero_init) CK(cudaMemsetAsync(e, 0, sizeof(T) * L[l].G.ncell, s));
       for (int i = 0; i < n; i++) {
-        CK(launch_vc_op<T>(A, VC_JACOBI, -1, e, r, (T *)L[l].t, 1, nullptr, s));
+        CK(launch_vc_op<T>(A, VC_JACOBI, -1, e, r, (T *)L[l].t, 1, nullptr, nullptr, s));
         CK(cudaMemcpyAsync(e, L[l].t, sizeof(T) * L[l].G.ncell, cudaMemcpyDeviceToDevice, s));
       }
       return MLGPU_OK;
@@ -629,15 +629,18 @@ class VCSolver : public mlgpu_solver {
     A.a = (const double *)op.aCoef;
     A.c = (const double *)op.cCoef;
     for (int d = 0; d < 3; d++) A.b[d] = (const double *)op.bCoef[d];
+    int nparts = 0;
     if (mixed)
       CK((launch_vc_update_residual<double, float>(A, o.norm_type, phi[from],
                                                    (const float *)L[0].ecur, rhs, phi[1 - from],
-                                                   nullptr, (float *)L[0].r, part, s, par)));
+                                                   nullptr, (float *)L[0].r, part, &nparts, s,
+                                                   par)));
     else
       CK((launch_vc_update_residual<double, double>(A, o.norm_type, phi[from],
                                                     (const double *)L[0].ecur, rhs, phi[1 - from],
-                                                    nullptr, (double *)L[0].r, part, s, par)));
-    CK(launch_finalize_norm(o.norm_type, part, norm_parts(L[0].G.ncell), part + kMaxBlocks, s));
+                                                    nullptr, (double *)L[0].r, part, &nparts, s,
+                                                    par)));
+    CK(launch_finalize_norm(o.norm_type, part, nparts, part + kMaxBlocks, s));
     if (par) {
       OuterCfg cfg{o.tolerance, o.hang, o.norm_thresh, o.max_iter};
       CK(launch_outer_decide(dev_state, part + kMaxBlocks, cfg, h, s));
@@ -703,13 +706,15 @@ class VCSolver : public mlgpu_solver {
       int rc0 = outer_fast(phi[0], nullptr, nullptr, nullptr, nullptr, 0);
       if (rc0) return rc0;
     } else {
+      int nparts = 0;
       if (mixed)
         CK((launch_vc_update_residual<double, float>(A, o.norm_type, phi[0], nullptr, rhs, nullptr,
-                                                     nullptr, (float *)L[0].r, part, s)));
+                                                     nullptr, (float *)L[0].r, part, &nparts, s)));
       else
         CK((launch_vc_update_residual<double, double>(A, o.norm_type, phi[0], nullptr, rhs, nullptr,
-                                                      nullptr, (double *)L[0].r, part, s)));
-      CK(launch_finalize_norm(o.norm_type, part, norm_parts(L[0].G.ncell), part + kMaxBlocks, s));
+                                                      nullptr, (double *)L[0].r, part, &nparts,
+                                                      s)));
+      CK(launch_finalize_norm(o.norm_type, part, nparts, part + kMaxBlocks, s));
     }
     return MLGPU_OK;
   }
@@ -996,7 +1001,8 @@ class HCSolver : public mlgpu_solver {
     NLArgs<double> A = args(l);
     for (int i = 0; i < n; i++) {
       if (o.relax_mode == MLGPU_RELAX_JACOBI) {
-        CK(launch_nl_op<double>(A, NL_JACOBI, -1, L[l].u, L[l].f, L[l].t, nullptr, nullptr, s));
+        CK(launch_nl_op<double>(A, NL_JACOBI, -1, L[l].u, L[l].f, L[l].t, nullptr, nullptr, nullptr,
+                                s));
         CK(cudaMemcpyAsync(L[l].u, L[l].t, sizeof(double) * 2 * L[l].G.ncell,
                            cudaMemcpyDeviceToDevice, s));
         tcl_ok[l] = 0;
@@ -1029,7 +1035,8 @@ class HCSolver : public mlgpu_solver {
     tcl_ok[l + 1] = 0;
     rc = ensure_tcl(l + 1);
     if (rc) return rc;
-    CK(launch_nlc_op(args(l + 1), NL_APPLY_PLUS, -1, C.u, C.tcl, C.r, C.f, C.uold, nullptr, s));
+    CK(launch_nlc_op(args(l + 1), NL_APPLY_PLUS, -1, C.u, C.tcl, C.r, C.f, C.uold, nullptr, nullptr,
+                     s));
     for (int m = 0; m < o.num_mg; m++) {
       rc = cycle(l + 1);
       if (rc) return rc;
@@ -1042,9 +1049,10 @@ class HCSolver : public mlgpu_solver {
   int residual_norm() {
     int rc = ensure_tcl(0);
     if (rc) return rc;
+    int nparts = 0;
     CK(launch_nlc_op(args(0), NL_RESIDUAL, o.norm_type, L[0].u, L[0].tcl, L[0].f, L[0].r, nullptr,
-                     part, s));
-    CK(launch_finalize_norm(o.norm_type, part, norm_parts(L[0].G.ncell), part + kMaxBlocks, s));
+                     part, &nparts, s));
+    CK(launch_finalize_norm(o.norm_type, part, nparts, part + kMaxBlocks, s));
     CK(cudaMemcpyAsync(host_norm, part + kMaxBlocks, sizeof(double), cudaMemcpyDeviceToHost, s));
     return MLGPU_OK;
   }
@@ -1314,8 +1322,10 @@ class HCAdjSolver : public mlgpu_solver {
   }
 
   int residual_norm() {
-    CK(launch_adj_op(args(0), ADJ_RESIDUAL, o.norm_type, L[0].y, L[0].g, L[0].r, part, s, tr));
-    CK(launch_finalize_norm(o.norm_type, part, norm_parts(L[0].G.ncell), part + kMaxBlocks, s));
+    int nparts = 0;
+    CK(launch_adj_op(args(0), ADJ_RESIDUAL, o.norm_type, L[0].y, L[0].g, L[0].r, part, &nparts, s,
+                     tr));
+    CK(launch_finalize_norm(o.norm_type, part, nparts, part + kMaxBlocks, s));
     CK(cudaMemcpyAsync(host_norm, part + kMaxBlocks, sizeof(double), cudaMemcpyDeviceToHost, s));
     return MLGPU_OK;
   }
@@ -1356,14 +1366,14 @@ class HCAdjSolver : public mlgpu_solver {
   // crosses a closure regime boundary)
   int nl_residual() {
     const long long n2 = 2 * L[0].G.ncell;
+    int nparts = 0;
     CK(launch_nl_op<double>(make_nl_args<double>(op), NL_RESIDUAL, MLGPU_NORM_L2, L[0].u, nf,
-                            L[0].g, nullptr, part, s));
-    CK(launch_finalize_norm(MLGPU_NORM_L2, part, norm_parts(L[0].G.ncell), part + kMaxBlocks,
-                            s));
+                            L[0].g, nullptr, part, &nparts, s));
+    CK(launch_finalize_norm(MLGPU_NORM_L2, part, nparts, part + kMaxBlocks, s));
     CK(cudaMemcpyAsync(host_norm + 1, part + kMaxBlocks, sizeof(double), cudaMemcpyDeviceToHost,
                        s));
-    CK(launch_norm_partial<double>(n2, L[0].g, o.norm_type, part, s));
-    CK(launch_finalize_norm(o.norm_type, part, norm_parts(n2), part + kMaxBlocks + 1, s));
+    CK(launch_norm_partial<double>(n2, L[0].g, o.norm_type, part, &nparts, s));
+    CK(launch_finalize_norm(o.norm_type, part, nparts, part + kMaxBlocks + 1, s));
     CK(cudaMemcpyAsync(host_norm, part + kMaxBlocks + 1, sizeof(double), cudaMemcpyDeviceToHost,
                        s));
     CK(cudaStreamSynchronize(s));

@@ -35,6 +35,9 @@
 #include <cstring>
 #include <vector>
 #include <algorithm>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 
 #include "../include/mlgpu.h"
 
@@ -243,7 +246,12 @@ inline void t_cl(double H, double C, const mlgpu_params &p, double &T, double &C
   } else if (H >= Hl) {
     T = H - p.stefan;
     Cl = C;
-  } else {  // NaN input: no branch taken in the Fortran either
+  } else {
+    // NaN input.  This departs from the reference: CALCULATE_T_CL takes no
+    // branch for a NaN and leaves T and C_l as they were in the output
+    // array.  Here both become NaN (T = H, C_l = C), so a poisoned state
+    // stays poisoned and the solvers' NaN detection sees it; the device
+    // closure does the same.
     T = H;
     Cl = C;
   }
@@ -754,6 +762,18 @@ bool has_nan(const double *x, size_t n) {
 
 // ====================================================================== C ABI
 extern "C" {
+
+// host threads of the OpenMP loops (the timed CPU baseline runs at 1 and at
+// all cores); returns the count now in effect
+int orc_set_threads(int n) {
+#ifdef _OPENMP
+  if (n > 0) omp_set_num_threads(n);
+  return omp_get_max_threads();
+#else
+  (void)n;
+  return 1;
+#endif
+}
 
 int orc_closure(const mlgpu_grid *g, const mlgpu_params *p, const double *HC, double *T,
                 double *por, double *Cl, double *Cs, double *Hs, double *He,

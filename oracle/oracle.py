@@ -52,6 +52,7 @@ def lib():
             "orc_mac_divergence": (i, [P(abi.Grid), vp, vp * 3]),
             "orc_mac_correct": (i, [P(abi.Grid), P(abi.BC), vp, vp * 3, vp * 3]),
             "orc_norm": (d, [sz, vp, i]),
+            "orc_set_threads": (i, [i]),
             "orc_mg_default_options": (None, [P(abi.MGOptions), i]),
             "orc_mg_depth": (i, [P(abi.Grid), i]),
             "orc_pd_temperature": (d, [d, d, P(abi.Params)]),
@@ -292,6 +293,12 @@ def mac_correct(g, bc, phi, u, scale=None):
     lib().orc_mac_correct(C.byref(g), C.byref(bc), _p(phi), sc,
                           _faces3(u + [None] * (3 - len(u))))
     return u
+
+
+def set_threads(n=0):
+    """Host threads of the oracle's OpenMP loops (n <= 0: leave as is);
+    returns the count in effect."""
+    return lib().orc_set_threads(int(n))
 
 
 def norm(x, kind=abi.NORM_MAX):

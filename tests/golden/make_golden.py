@@ -87,4 +87,8 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    # default: MUSHY_LAYER_REFERENCE, else the directory `reference` beside
+    # this repository's root (tests/refpaths.py)
+    sys.path.insert(0, os.path.dirname(HERE))
+    import refpaths
+    main(sys.argv[1] if len(sys.argv) > 1 else refpaths.reference_root())

@@ -25,6 +25,7 @@ import numpy as np
 import pytest
 from scipy.optimize import brentq
 
+import refpaths
 from mushy_gb300 import abi
 from oracle import oracle as O
 
@@ -123,7 +124,7 @@ def test_steady_mushy_layer_converges_to_the_analytic_profile():
     assert eT16 / eT32 > 3.2 and ec16 / ec32 > 3.0, errs
 
 
-PARAMS = "/root/reference/params/convergenceTest/noFlowConvTest.parameters"
+PARAMS = refpaths.ref("params", "convergenceTest", "noFlowConvTest.parameters")
 
 
 @pytest.mark.skipif(not os.path.exists(PARAMS), reason="reference tree not mounted")

@@ -12,12 +12,13 @@ import os
 import numpy as np
 import pytest
 
+import refpaths
 from mushy_gb300 import abi
 from oracle import oracle as O
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 GOLD = os.path.join(HERE, "golden", "closure_plt000100.npz")
-REF_PLT = "/root/reference/test/unit/data/plt000100.2d.hdf5"
+REF_PLT = refpaths.ref("test", "unit", "data", "plt000100.2d.hdf5")
 
 
 def _load():
@@ -78,7 +79,7 @@ def test_gpu_closure_bitwise_vs_reference_output():
 
 
 CHK_GOLD = os.path.join(HERE, "golden", "checkpoint_chk000100.npz")
-REF_CHK = "/root/reference/test/unit/data/chk000100.2d.hdf5"
+REF_CHK = refpaths.ref("test", "unit", "data", "chk000100.2d.hdf5")
 
 
 def test_checkpoint_state_closure_matches_plotfile():

@@ -11,13 +11,14 @@ import numpy as np
 import pytest
 
 import problems as P
+import refpaths
 from mushy_gb300 import abi
 from mushy_gb300 import inputs as mi
 from oracle import oracle as O
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 FIX = os.path.join(HERE, "golden", "inputs_unit_data.json")
-REF_INPUTS = "/root/reference/test/unit/data/inputs"
+REF_INPUTS = refpaths.ref("test", "unit", "data", "inputs")
 
 
 def _run_inputs():
@@ -215,7 +216,7 @@ def test_hc_face_coefficients_order():
     assert b[0][0][0, 2] == -1.0 and b[0][0][0, 0] == -2.0
 
 
-REG = "/root/reference/test/regression"
+REG = refpaths.ref("test", "regression")
 
 
 @pytest.mark.skipif(not os.path.exists(REG), reason="reference tree not mounted")
