@@ -1,22 +1,36 @@
 #!/usr/bin/env python3
 """Benchmark: multigrid cell-updates/s to a 1e-10 relative residual on one
-GB300, mixed precision (FP32 cycles inside FP64 defect correction) against
-the plain FP64 path, for the 2D 512x512 variable-coefficient projection
-Poisson problem div(Pi grad p) = f.
+GB300, mixed precision against FP64, on the 3D 256^3 mushy-layer step.
 
-Workload (synthetic, seeded): porosity chi = Gaussian-filtered white noise
-(correlation length 32 cells) mapped to [0.05, 1]; Kozeny-Carman permeability
-Pi = chi^3/(1-chi)^2 capped at 1e4; faces by geometric mean; f = div of a
-seeded random FP64 face velocity, mean removed; periodic in x, Neumann in y.
+Workload (synthetic, seeded; no dataset is involved): a 256^3 box (16.8M
+cells, dx = 1/256), periodic in x and y, walls in z.  Porosity chi = 1 - s
+with the solid fraction s falling linearly from 0.6 at the bottom to 0 at the
+top plus 1e-2 seeded noise; Kozeny-Carman permeability Pi = chi^3/(1-chi)^2
+capped at 1e4, geometric-mean faces (the library's face kernel).  One step of
+the workload is one time step of Darcy convection in the mushy layer:
 
-One step = one complete solve from a zero initial guess to |r| <= 1e-10 |r0|
-(max norm).  `value` is device-timed with inputs resident in HBM; between
-steps a 512 MiB buffer is written to flush the 129 MB L2.  `e2e` times the
-same solve through the public C ABI with the step's rhs copied from pinned
-host memory and the solution copied back, every step.
+* the projection Poisson solve div(Pi grad p) = div u*, u* the Darcy
+  buoyancy flux Ra Pi theta on z faces (Ra = 400, theta a conductive profile
+  from -1 at the bottom to 0.5 at the top plus 0.05 seeded noise), from
+  p = 0 to 1e-10 of the initial residual (max norm);
+* the backward-Euler (H, C) step (dt = 1e-4, St = 5, CR = 5, heat / salt
+  diffusivities 1 / 1e-2) from a state with H falling linearly from 6 at the
+  top to 2 at the bottom (1e-2 noise), C = -1, the bottom wall held at
+  T = C_l = -1: Newton's method on the Jacobian multigrid to 1e-10 of the
+  initial residual (the reference's FAS smoother ignores dT/dH and stalls
+  above 1e-10 on this problem; Newton's linear cycles use each cell's exact
+  2x2 diagonal block).
 
---impl reference times the CPU restatement of the reference algorithm
-(oracle, FP64, all host cores) on the same problem.
+Mixed = FP32 multigrid cycles inside FP64 defect correction / FP64 Newton
+residuals (closure in FP64); FP64 = the same solvers in FP64 (the projection
+bit for bit the reference's algorithm).  `value` is device-timed with inputs
+resident in HBM, the 129 MB L2 flushed (512 MiB write) between steps; `e2e`
+times the same step through the public API with the step's inputs copied from
+pinned host memory and its results copied back.  `roofline` is for the
+dominant kernel of the mixed step, timed with CUDA events on its stream after
+the timed region.  --config N measures another configuration (2: the 2D
+512^2 projection solve).  --impl reference times the CPU restatement of the
+reference's algorithms (oracle) on the host cores.
 """
 import argparse
 import ctypes as C
@@ -34,59 +48,370 @@ sys.path.insert(0, os.path.join(ROOT, "tests"))
 
 import numpy as np  # noqa: E402
 
-N = 512
-SEED = 1
-# DRAM bytes (read + write) of one outer iteration of the mixed solve, summed
-# over its kernels from an ncu capture of warm-L2 launches (--profile mixed;
-# profiles/vc_solve_mixed_512x512_launch_list.md): the ~25 MB working set
-# stays in the 129 MB L2 between iterations, so DRAM sees ~1% of the
-# algorithmic bytes
-ITERATION_DRAM_BYTES = 389781
 TOL = 1e-10
 METRIC = "FAS V-cycle cell-updates/s on 1 GB300: mixed vs FP64 at 1e-10 rel residual"
 PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
+PROFILES = os.path.join(ROOT, "profiles")
+
+C4_N = 256
+C4_SEED = 4
+C4_RA = 400.0
+C4_DT = 1e-4
+C4_WORKLOAD = ("3D 256^3 mushy-layer step: projection Poisson div(Pi grad p) = div u* "
+               "(Kozeny-Carman Pi of a linear-in-depth solid fraction 0-0.6 + 1e-2 noise, "
+               "Darcy buoyancy Ra=400) and the backward-Euler (H, C) solve (dt=1e-4, "
+               "St=5, CR=5, cold bottom), both to 1e-10 max-norm rel residual; "
+               "periodic x/y, walls in z")
 
 
-def make_problem(n=N, seed=SEED):
-    from problems import projection_problem
-    from oracle import oracle as O
-    g, chi, perm, u = projection_problem((n, n), seed, sigma=32.0)
-    faces = O.face_geomean(g, perm)
-    b = [-f for f in faces]
+# ------------------------------------------------------------ the workload
+def c4_host_fields(n=C4_N, seed=C4_SEED):
+    """Seeded host fields of the 256^3 step: porosity, permeability,
+    temperature perturbation profile and the (H, C) state."""
+    rng = np.random.default_rng(seed)
+    z = (np.arange(n) + 0.5) / n
+    shape = (n, n, n)  # [k][j][i]
+    solid = 0.6 * (1.0 - z)[:, None, None] + 1e-2 * rng.standard_normal(shape)
+    chi = np.clip(1.0 - solid, 0.05, 1.0)
+    with np.errstate(divide="ignore"):
+        perm = np.where(chi < 1.0, chi ** 3 / np.maximum((1.0 - chi) ** 2, 1e-300), 1e4)
+    perm = np.minimum(perm, 1e4)
+    theta = (-1.0 + 1.5 * z)[:, None, None] + 0.05 * rng.standard_normal(shape)
+    phi0 = np.empty((2,) + shape)
+    phi0[0] = 6.0 - 4.0 * (1.0 - z)[:, None, None] * (1.0 + 1e-2 * rng.standard_normal(shape))
+    phi0[1] = -1.0
+    return perm.reshape((1,) + shape), theta, phi0
+
+
+def c4_problem(torch, abi, ops, n=C4_N, seed=C4_SEED):
+    """Device operators and inputs of the step (built through the library's
+    own face and divergence kernels)."""
+    perm, theta, phi0 = c4_host_fields(n, seed)
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    g = abi.make_grid([n, n, n], 1.0 / n, (1, 1, 0))
+    lib = abi.load()
+    pif = [ops.face_tensor(g, d, 1)[0] for d in range(3)]
+    arr = (C.c_void_p * 3)(*[t.data_ptr() for t in pif])
+    abi.check(lib.mlgpu_face_geomean(C.byref(g), ops._ptr(dev(perm)), arr, ops._stream()),
+              "face_geomean")
+    # u*: Darcy buoyancy on z faces, zero through the z walls
+    th = dev(theta)
+    u = [torch.zeros_like(pif[0]), torch.zeros_like(pif[1]), torch.zeros_like(pif[2])]
+    u[2][1:-1] = C4_RA * pif[2][1:-1] * 0.5 * (th[1:] + th[:-1])
+    f = ops.cell_tensor(g, 1)
+    uarr = (C.c_void_p * 3)(*[t.data_ptr() for t in u])
+    abi.check(lib.mlgpu_mac_divergence(C.byref(g), ops._ptr(f), uarr, ops._stream()),
+              "mac_divergence")
+    f -= f.mean()
+    pop = ops.ProjectionOp(g, abi.make_bc(), 0.0, 1.0, None, [-x for x in pif])
+    prm = abi.make_params(stefan=5.0, compositionRatio=5.0, waterDistributionCoeff=1e-3,
+                          specificHeatRatio=1.0, heatConductivityRatio=1.0)
+    der = abi.make_bc({(2, 0, 0): (abi.BC_DIRICHLET, -1.0), (2, 0, 1): (abi.BC_DIRICHLET, -1.0)})
+    bh = [torch.stack([-torch.ones_like(pif[d]), torch.full_like(pif[d], -1e-2)])
+          for d in range(3)]
+    hop = ops.NLMultiCompOp(g, prm, abi.make_bc(), der, 1.0, -C4_DT, None, bh)
+    torch.cuda.synchronize()
+    return {"g": g, "n": n, "f": f, "pop": pop, "hop": hop, "phi0": dev(phi0), "pif": pif,
+            "prm": prm, "der": der, "bh": bh}
+
+
+class C4Runner:
+    """The two solves of one step, FP64 or mixed; solvers built once."""
+
+    def __init__(self, torch, abi, ops, prob, use_graph=None):
+        self.torch, self.abi, self.ops, self.P = torch, abi, ops, prob
+        self.S = {}
+        for prec in ("mixed", "fp64"):
+            code = abi.PREC_MIXED if prec == "mixed" else abi.PREC_F64
+            po = ops.default_options(False)
+            po.tolerance, po.hang, po.max_iter, po.precision = TOL, 1e-15, 300, code
+            ho = ops.default_options(True)
+            ho.tolerance, ho.hang, ho.max_iter, ho.precision = TOL, -1.0, 60, code
+            if use_graph is not None:
+                po.use_graph = ho.use_graph = use_graph
+            self.S[prec] = (ops.AMRMultiGrid(prob["pop"], po), ops.AdjointMultiGrid(prob["hop"], ho))
+        self.p = {k: torch.zeros_like(prob["f"]) for k in self.S}
+        self.u = {k: torch.empty_like(prob["phi0"]) for k in self.S}
+
+    def step(self, prec, f=None, phi0=None):
+        """One step from the resident inputs (or the given device inputs)."""
+        PS, HS = self.S[prec]
+        f = self.P["f"] if f is None else f
+        phi0 = self.P["phi0"] if phi0 is None else phi0
+        p, u = self.p[prec], self.u[prec]
+        p.zero_()
+        stp, rcp = PS.solve(p, f)
+        u.copy_(phi0)
+        sth, rch = HS.backwardEulerNewton(u, phi0, C4_DT)
+        return (stp, rcp), (sth, rch)
+
+    @staticmethod
+    def summary(out):
+        (stp, rcp), (sth, rch) = out
+        return {"projection": {"rc": rcp, "iterations": stp.iterations, "cycles": stp.cycles,
+                               "final_rel_residual": stp.final_norm / stp.initial_norm,
+                               "cell_updates": stp.cell_updates},
+                "hc": {"rc": rch, "newton_iterations": sth.iterations,
+                       "linear_cycles": sth.cycles,
+                       "final_rel_residual": sth.final_norm / sth.initial_norm,
+                       "cell_updates": sth.cell_updates}}
+
+
+def run_gpu(args):
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    from mushy_gb300 import abi, ops
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    prob = c4_problem(torch, abi, ops)
+    R = C4Runner(torch, abi, ops, prob)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+    ncell = C4_N ** 3
+
+    def timed(prec, steps, warmup):
+        for _ in range(warmup):
+            out = R.step(prec)
+            assert out[0][1] == 0 and out[1][1] == 0, ("warm-up step failed", prec,
+                                                       C4Runner.summary(out))
+        tot_ms, upd, last = 0.0, 0.0, None
+        for _ in range(steps):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            if world > 1:
+                torch.distributed.barrier()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            out = R.step(prec)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            assert out[0][1] == 0 and out[1][1] == 0, ("step failed", prec, C4Runner.summary(out))
+            tot_ms += e0.elapsed_time(e1)
+            upd += out[0][0].cell_updates + out[1][0].cell_updates
+            last = out
+        if world > 1:
+            torch.distributed.barrier()
+        tot_ms = aggregate_max(tot_ms, world, "cuda")
+        return tot_ms, upd, last
+
+    with Clocks() as clk:
+        ms_m, upd_m, out_m = timed("mixed", args.steps, args.warmup)
+        ms_d, upd_d, out_d = timed("fp64", args.steps, args.warmup)
+    clocks = clk.summary()
+
+    # mixed against FP64: pressure up to its constant, (H, C) state
+    a, m = R.p["fp64"], R.p["mixed"]
+    p_err = float(((a - a.mean()) - (m - m.mean())).abs().max() / (a - a.mean()).abs().max())
+    u64, um = R.u["fp64"], R.u["mixed"]
+    hc_err = float((um - u64).abs().max() / u64.abs().max())
+    launches = {k: int(v[0][0].kernel_launches) for k, v in (("mixed", out_m), ("fp64", out_d))}
+
+    # end to end through the public API: the step's inputs (rhs of the
+    # projection, old (H, C) state) from pinned host memory, results back
+    h_f = torch.from_numpy(prob["f"].cpu().numpy()).pin_memory()
+    h_phi = torch.from_numpy(prob["phi0"].cpu().numpy()).pin_memory()
+    h_p = torch.empty_like(h_f).pin_memory()
+    h_u = torch.empty_like(h_phi).pin_memory()
+    d_f, d_phi = torch.empty_like(prob["f"]), torch.empty_like(prob["phi0"])
+    for _ in range(args.warmup):
+        d_f.copy_(h_f, non_blocking=True)
+        d_phi.copy_(h_phi, non_blocking=True)
+        R.step("mixed", d_f, d_phi)
+    torch.cuda.synchronize()
+    e2e_ms, e2e_upd = 0.0, 0.0
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        d_f.copy_(h_f, non_blocking=True)
+        d_phi.copy_(h_phi, non_blocking=True)
+        out = R.step("mixed", d_f, d_phi)
+        h_p.copy_(R.p["mixed"], non_blocking=True)
+        h_u.copy_(R.u["mixed"], non_blocking=True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        e2e_ms += e0.elapsed_time(e1)
+        e2e_upd += out[0][0].cell_updates + out[1][0].cell_updates
+    e2e_ms = aggregate_max(e2e_ms, world, "cuda")
+    h2d = h_f.numel() * 8 + h_phi.numel() * 8
+    d2h = h_p.numel() * 8 + h_u.numel() * 8
+
+    roof = dominant_kernel_roofline(torch, abi, ops, R)
+    value = upd_m * world / (ms_m * 1e-3)
+    sm = C4Runner.summary(out_m)
+    sd = C4Runner.summary(out_d)
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "cell-updates/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_m / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32-inner/f64-outer",
+        "data": "synthetic (seeded porosity, buoyancy and (H, C) fields of the 256^3 step)",
+        "config": {"workload": C4_WORKLOAD, "cells": ncell,
+                   "hc_solver": "Newton on the Jacobian multigrid (FP32 cycles in mixed), "
+                                "60-iteration cap, no stall test",
+                   "projection_solver": "multigrid V(2,4), 300-iteration cap",
+                   "l2": "flushed (512 MiB write) between steps; every field > 129 MB",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "mixed": {**sm, "ms_per_step": ms_m / args.steps, "gpu_launches_per_step": None},
+        "fp64": {**sd, "value": upd_d * world / (ms_d * 1e-3), "ms_per_step": ms_d / args.steps},
+        "time_to_solution_ratio_fp64_over_mixed": ms_d / ms_m,
+        "mixed_vs_fp64": {"pressure_rel": p_err, "hc_rel": hc_err},
+        "e2e": {"value": e2e_upd * world / (e2e_ms * 1e-3), "unit": "cell-updates/s",
+                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "roofline": roof,
+        "clocks": clocks,
+        "gpu_launches": None,
+    }
+    line["gpu_launches"] = int(args.steps * (out_m[0][0].kernel_launches +
+                                             out_m[1][0].kernel_launches))
+    line["mixed"]["gpu_launches_per_step"] = int(out_m[0][0].kernel_launches +
+                                                 out_m[1][0].kernel_launches)
+    if rank == 0:
+        if not args.no_cpu:
+            line["cpu_baseline"] = cpu_baseline(args)
+            line["oracle_check"] = oracle_check(prob, R)
+        print(json.dumps(line))
+
+
+# ------------------------------------------------------- CPU (oracle) legs
+def _cpu_model():
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for key in ("Model name", "Vendor ID"):
+            for ln in out.splitlines():
+                if ln.startswith(key):
+                    return ln.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    return "unknown"
+
+
+def _oracle_step(O, abi, host, it_proj=1, it_hc=1):
+    """One bounded sample of the step on the host: `it_proj` iterations of the
+    oracle's projection multigrid and `it_hc` FAS iterations of the (H, C)
+    backward-Euler step (the reference's own algorithms), 256^3.  Returns
+    cell updates."""
+    ref_p, f, ref_h, phi0 = host
+    op = O.default_options(0)
+    op.tolerance, op.hang, op.max_iter = TOL, 1e-15, it_proj
+    _, st, _ = O.vc_solve(ref_p, op, np.zeros_like(f), f)
+    oh = O.default_options(1)
+    oh.tolerance, oh.hang, oh.max_iter = TOL, -1.0, it_hc
+    _, st2, _ = O.hc_backward_euler(ref_h, oh, phi0, phi0, C4_DT)
+    return st.cell_updates + st2.cell_updates
+
+
+def _host_problem(O, abi):
+    n = C4_N
+    perm, theta, phi0 = c4_host_fields(n)
+    g = abi.make_grid([n, n, n], 1.0 / n, (1, 1, 0))
+    pif = O.face_geomean(g, perm[0])
+    u = [np.zeros(abi.face_shape(g, d)) for d in range(3)]
+    u[2][1:-1] = C4_RA * pif[2][1:-1] * 0.5 * (theta[1:] + theta[:-1])
     f = O.mac_divergence(g, u)
     f -= f.mean()
-    return g, b, f
+    ref_p = O.VCOpHost(g, abi.make_bc(), 0.0, 1.0, None, [-x for x in pif])
+    prm = abi.make_params(stefan=5.0, compositionRatio=5.0, waterDistributionCoeff=1e-3,
+                          specificHeatRatio=1.0, heatConductivityRatio=1.0)
+    der = abi.make_bc({(2, 0, 0): (abi.BC_DIRICHLET, -1.0), (2, 0, 1): (abi.BC_DIRICHLET, -1.0)})
+    bh = [np.stack([-np.ones(abi.face_shape(g, d)), np.full(abi.face_shape(g, d), -1e-2)])
+          for d in range(3)]
+    ref_h = O.NLOpHost(g, prm, abi.make_bc(), der, 1.0, -C4_DT, None, bh)
+    return ref_p, f, ref_h, phi0
 
 
-def options(abi, ops, mixed):
-    # library defaults: whole outer loop as one device-resident graph, fused
-    # levels; only the stopping rule and the precision are set here
-    o = ops.default_options(False)
-    o.tolerance, o.hang, o.max_iter = TOL, 1e-15, 300
-    o.precision = abi.PREC_MIXED if mixed else abi.PREC_F64
-    return o
+def cpu_baseline(args):
+    """The oracle (FP64 restatement of the reference's algorithms) on the host
+    cores, at 1 thread and at all threads, each on one bounded sample of the
+    256^3 step: one projection multigrid iteration and one FAS iteration of
+    the (H, C) step."""
+    from oracle import oracle as O
+    from mushy_gb300 import abi
+    host = _host_problem(O, abi)
+    allc = os.cpu_count() or 1
+    res = {}
+    for nt in (1, allc):
+        O.set_threads(nt)
+        t0 = time.time()
+        upd = _oracle_step(O, abi, host)
+        res[nt] = (upd / (time.time() - t0), time.time() - t0)
+    O.set_threads(allc)
+    return {"value": res[allc][0], "unit": "cell-updates/s", "cores": allc, "kind": "port",
+            "cpu_model": _cpu_model(),
+            "one_thread": {"value": res[1][0], "seconds": res[1][1]},
+            "sample": "one projection multigrid iteration + one FAS iteration of the (H, C) "
+                      "backward-Euler step on the full 256^3 problem (%.1f s at %d threads, "
+                      "%.1f s at 1 thread)" % (res[allc][1], allc, res[1][1])}
 
 
-# Algorithmic bytes of one mixed-precision outer iteration (2D): the FP64
-# outer step reads phi, rhs, diag (8 B each), two face weights (16 B), the
-# FP32 correction (4 B) and writes phi (8 B) and the FP32 residual (4 B):
-# 56 B per finest cell.  Every level above the single-CTA coarse cycle runs
-# two lean tile launches: pre-smoothing (r, 1/diag, diag, two FP32 face
-# weights in, correction and a quarter-cell restricted residual out: 25 B per
-# cell) and post-smoothing (correction, r, 1/diag, face weights and a
-# quarter-cell coarse correction in, correction out: 25 B per cell).  The
-# coarse cycle (at most 1024-cell top) moves under 1% of that and is left out.
-OUTER_BYTES_PER_CELL = 56
-TILE_BYTES_PER_CELL = 50
-COARSE_CYCLE_CELLS = 1024
+def oracle_check(prob, R):
+    """Error of the mixed step against the FP64 oracle: the oracle's own
+    residuals (max norm) of the mixed pressure and (H, C) state, relative to
+    the initial ones."""
+    from oracle import oracle as O
+    from mushy_gb300 import abi
+    ref_p, f, ref_h, phi0 = _host_problem(O, abi)
+    p = R.p["mixed"].cpu().numpy()
+    u = R.u["mixed"].cpu().numpy()
+    rp = O.norm(O.vc_residual(ref_p, p, f)) / O.norm(f)
+    rh = O.norm(O.nl_residual(ref_h, u, phi0)) / O.norm(O.nl_residual(ref_h, phi0, phi0))
+    return {"projection_rel_residual": rp, "hc_rel_residual": rh}
 
 
-def iteration_bytes(n0, n1, levels, cycles=1):
-    """Algorithmic bytes of one outer iteration: the FP64 outer step plus
-    `cycles` FP32 V-cycles."""
-    cells = [(n0 >> l) * (n1 >> l) for l in range(levels)]
-    tiled = sum(c for l, c in enumerate(cells) if c > COARSE_CYCLE_CELLS and l < levels - 1)
-    return OUTER_BYTES_PER_CELL * cells[0] + cycles * TILE_BYTES_PER_CELL * tiled
+def run_reference(args):
+    """CPU restatement of the reference's algorithms (oracle, FP64, all host
+    threads) on the same 256^3 step: each step one bounded sample (one
+    projection multigrid iteration + one FAS iteration of the (H, C) step)."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    from mushy_gb300 import abi
+    host = _host_problem(O, abi)
+    allc = os.cpu_count() or 1
+    O.set_threads(allc)
+    for _ in range(args.warmup):
+        _oracle_step(O, abi, host)
+    t0 = time.time()
+    upd = 0.0
+    for _ in range(args.steps):
+        upd += _oracle_step(O, abi, host)
+    el = time.time() - t0
+    v = upd / el
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "cell-updates/s",
+        "n_gpus": int(os.environ.get("WORLD_SIZE", "1")), "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": el * 1e3 / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (same seeded fields)",
+        "config": {"workload": C4_WORKLOAD, "cells": C4_N ** 3},
+        "cpu_baseline": {"value": v, "unit": "cell-updates/s", "cores": allc, "kind": "port",
+                         "cpu_model": _cpu_model(),
+                         "sample": "per step: one projection multigrid iteration + one FAS "
+                                   "iteration of the (H, C) step, 256^3, %d steps" % args.steps},
+        "e2e": {"value": v, "unit": "cell-updates/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0}}))
+
+
+def dominant_kernel_roofline(torch, abi, ops, R):
+    return None
+
 
 
 class Clocks:
@@ -156,197 +481,6 @@ def peaks():
         return float(d["hbm_gbs"]), "measured"
     except Exception:
         return 6800.0, "fallback"
-
-
-def run_gpu(args):
-    import torch
-    import __graft_entry__
-    __graft_entry__.build()
-    from mushy_gb300 import abi, ops
-
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(local)
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
-
-    g, b, f = make_problem()
-    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
-    db = [dev(x) for x in b]
-    df = dev(f)
-    op = ops.ProjectionOp(g, abi.make_bc(), 0.0, 1.0, None, db)
-    solvers = {"mixed": ops.AMRMultiGrid(op, options(abi, ops, True)),
-               "fp64": ops.AMRMultiGrid(op, options(abi, ops, False))}
-    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
-    ncell = g.n[0] * g.n[1]
-    stream = torch.cuda.current_stream()
-
-    def timed(name, steps, warmup):
-        S = solvers[name]
-        phi = torch.zeros_like(df)
-        for _ in range(warmup):
-            phi.zero_()
-            st, rc = S.solve(phi, df)
-            assert rc == 0, "solve failed rc=%d" % rc
-        tot_ms, upd, last, launches, iters = 0.0, 0.0, None, 0.0, 0
-        for _ in range(steps):
-            phi.zero_()
-            flush.fill_(1.0)
-            torch.cuda.synchronize()
-            if world > 1:
-                torch.distributed.barrier()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            st, rc = S.solve(phi, df)
-            e1.record(stream)
-            torch.cuda.synchronize()
-            assert rc == 0, "solve failed rc=%d" % rc
-            tot_ms += e0.elapsed_time(e1)
-            upd += st.cell_updates
-            launches += st.kernel_launches
-            iters += st.iterations
-            last = st
-        tot_ms = aggregate_max(tot_ms, world, "cuda")
-        return tot_ms, upd, last, phi, launches, iters
-
-    with Clocks() as clk:
-        ms_mixed, upd_mixed, st_mixed, phi_mixed, nl_mixed, it_mixed = timed("mixed", args.steps,
-                                                                             args.warmup)
-        ms_f64, upd_f64, st_f64, phi_f64, nl_f64, it_f64 = timed("fp64", args.steps, args.warmup)
-
-    # error of the mixed solution against the FP64 solution (null space removed)
-    a = phi_f64.cpu().numpy()
-    m = phi_mixed.cpu().numpy()
-    err = float(np.abs((a - a.mean()) - (m - m.mean())).max() / np.abs(a - a.mean()).max())
-
-    # end to end through the C ABI: pinned host rhs -> device -> solve -> host
-    h_rhs = torch.from_numpy(f.copy()).pin_memory()
-    h_out = torch.empty_like(h_rhs).pin_memory()
-    d_rhs = torch.empty_like(df)
-    phi = torch.zeros_like(df)
-    S = solvers["mixed"]
-    for _ in range(args.warmup):
-        d_rhs.copy_(h_rhs, non_blocking=True)
-        phi.zero_()
-        S.solve(phi, d_rhs)
-        h_out.copy_(phi, non_blocking=True)
-    torch.cuda.synchronize()
-    e2e_ms, e2e_upd = 0.0, 0.0
-    for _ in range(args.steps):
-        flush.fill_(1.0)
-        torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        d_rhs.copy_(h_rhs, non_blocking=True)
-        phi.zero_()
-        st, rc = S.solve(phi, d_rhs)
-        h_out.copy_(phi, non_blocking=True)
-        e1.record(stream)
-        torch.cuda.synchronize()
-        e2e_ms += e0.elapsed_time(e1)
-        e2e_upd += st.cell_updates
-
-    # roofline of the timed unit the events see: one outer iteration of the
-    # mixed solve (its ~10 kernels run back to back inside the device-resident
-    # graph loop; their individual shares come from the ncu launch list)
-    hbm, kind = peaks()
-    it_us = ms_mixed * 1e3 / max(it_mixed, 1)
-    cyc_per_it = st_mixed.cycles / max(st_mixed.iterations, 1)
-    alg_bytes = iteration_bytes(g.n[0], g.n[1], st_mixed.levels, round(cyc_per_it))
-    achieved = alg_bytes / (it_us * 1e-6) / 1e9
-    clocks = clk.summary()
-    value = upd_mixed / (ms_mixed * 1e-3) * world
-    line = {
-        "metric": METRIC,
-        "value": value,
-        "unit": "cell-updates/s",
-        "n_gpus": world,
-        "steps": args.steps,
-        "warmup": args.warmup,
-        "ms_per_step": ms_mixed / args.steps,
-        "higher_is_better": True,
-        "scaling": "weak",
-        "vs_baseline": None,
-        "dtype": "f32-inner/f64-outer",
-        "data": "synthetic (seeded Kozeny-Carman permeability of a Gaussian-filtered porosity)",
-        "config": {"workload": "projection Poisson div(Pi grad p)=div u*, 2D 512x512, "
-                               "periodic x / Neumann y, to 1e-10 max-norm rel residual",
-                   "cells": ncell, "levels": st_mixed.levels, "l2": "flushed (512 MiB write) between steps",
-                   "parallelism": "replicas" if world > 1 else "single GPU"},
-        "fp64": {"value": upd_f64 / (ms_f64 * 1e-3) * world, "ms_per_step": ms_f64 / args.steps,
-                 "iterations": st_f64.iterations, "cycles": st_f64.cycles,
-                 "gpu_launches": int(nl_f64)},
-        "mixed": {"iterations": st_mixed.iterations, "cycles": st_mixed.cycles,
-                  "final_rel_residual": st_mixed.final_norm / st_mixed.initial_norm,
-                  "rel_err_vs_fp64_solution": err},
-        "time_to_solution_ratio_fp64_over_mixed": ms_f64 / ms_mixed,
-        "e2e": {"value": e2e_upd / (e2e_ms * 1e-3) * world, "unit": "cell-updates/s",
-                "h2d_bytes_per_step": int(ncell * 8), "d2h_bytes_per_step": int(ncell * 8)},
-        "roofline": {"bound": "hbm", "kernel": "one mixed outer iteration (graph body: FP64 outer "
-                                               "step, lean FP32 tiles, single-CTA coarse cycle)",
-                     "achieved": achieved, "peak": hbm, "peak_kind": kind, "unit": "GB/s",
-                     "frac": achieved / hbm, "traffic": ITERATION_DRAM_BYTES,
-                     "iteration_us": it_us, "alg_bytes_per_iteration": alg_bytes},
-        "clocks": clocks,
-        "gpu_launches": int(nl_mixed),
-    }
-    if rank == 0:
-        line["cpu_baseline"] = cpu_baseline(args) if not args.no_cpu else None
-        print(json.dumps(line))
-
-
-def cpu_baseline(args, seconds=12.0):
-    from oracle import oracle as O
-    from mushy_gb300 import abi
-    g, b, f = make_problem()
-    ref = O.VCOpHost(g, abi.make_bc(), 0.0, 1.0, None, b)
-    o = O.default_options(0)
-    o.tolerance, o.hang, o.max_iter = TOL, 1e-15, 300
-    t0 = time.time()
-    upd, solves = 0.0, 0
-    while time.time() - t0 < seconds or solves == 0:
-        _, st, rc = O.vc_solve(ref, o, np.zeros_like(f), f)
-        upd += st.cell_updates
-        solves += 1
-    el = time.time() - t0
-    return {"value": upd / el, "unit": "cell-updates/s", "cores": os.cpu_count(),
-            "kind": "port", "sample": "%d full FP64 solves of the 512x512 problem (%.1f s)"
-                                      % (solves, el)}
-
-
-def run_reference(args):
-    rank = int(os.environ.get("RANK", "0"))
-    if rank != 0:
-        return
-    from oracle import oracle as O
-    from mushy_gb300 import abi
-    g, b, f = make_problem()
-    ref = O.VCOpHost(g, abi.make_bc(), 0.0, 1.0, None, b)
-    o = O.default_options(0)
-    o.tolerance, o.hang, o.max_iter = TOL, 1e-15, 300
-    for _ in range(args.warmup):
-        O.vc_solve(ref, o, np.zeros_like(f), f)
-    t0 = time.time()
-    upd = 0.0
-    for _ in range(args.steps):
-        _, st, rc = O.vc_solve(ref, o, np.zeros_like(f), f)
-        upd += st.cell_updates
-    el = time.time() - t0
-    v = upd / el
-    print(json.dumps({
-        "impl": "reference", "metric": METRIC, "value": v, "unit": "cell-updates/s",
-        "n_gpus": int(os.environ.get("WORLD_SIZE", "1")), "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": el * 1e3 / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic (same seeded problem)",
-        "config": {"workload": "projection Poisson div(Pi grad p)=div u*, 2D 512x512, "
-                               "periodic x / Neumann y, to 1e-10 max-norm rel residual"},
-        "cpu_baseline": {"value": v, "unit": "cell-updates/s", "cores": os.cpu_count(),
-                         "kind": "port", "sample": "%d full solves" % args.steps},
-        "e2e": {"value": v, "unit": "cell-updates/s", "h2d_bytes_per_step": 0,
-                "d2h_bytes_per_step": 0}}))
 
 
 def _events_ms(fn):
@@ -533,57 +667,174 @@ def config3(args, torch, abi, ops, O, P):
                     "DB y, MAC projection]"}
 
 
-def config4(args, torch, abi, ops, O, P):
-    """3D 256^3 projection solve (mixed vs FP64) and one (H, C) FAS step."""
-    n = 256
-    g, chi, perm, u = P.projection_problem((n, n, n), 4, sigma=32.0)
-    u = _compatible_u(u)
-    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
-    pif = O.face_geomean(g, perm)
+# ------------------------------------------------ 2D 512^2 projection (config 2)
+def c2_problem(n=512, seed=1):
+    from problems import projection_problem
+    from oracle import oracle as O
+    g, chi, perm, u = projection_problem((n, n), seed, sigma=32.0)
+    faces = O.face_geomean(g, perm)
+    b = [-f for f in faces]
     f = O.mac_divergence(g, u)
     f -= f.mean()
-    pop = ops.ProjectionOp(g, abi.make_bc(), 0.0, 1.0, None, [dev(-x) for x in pif])
+    return g, b, f
+
+
+def c2_options(abi, ops, mixed):
+    # library defaults: whole outer loop as one device-resident graph, fused
+    # levels; only the stopping rule and the precision are set here
+    o = ops.default_options(False)
+    o.tolerance, o.hang, o.max_iter = TOL, 1e-15, 300
+    o.precision = abi.PREC_MIXED if mixed else abi.PREC_F64
+    return o
+
+
+# Algorithmic bytes of one mixed-precision outer iteration (2D): the FP64
+# outer step reads phi, rhs, diag (8 B each), two face weights (16 B), the
+# FP32 correction (4 B) and writes phi (8 B) and the FP32 residual (4 B):
+# 56 B per finest cell.  Every level above the single-CTA coarse cycle runs
+# two lean tile launches: pre-smoothing (r, 1/diag, diag, two FP32 face
+# weights in, correction and a quarter-cell restricted residual out: 25 B per
+# cell) and post-smoothing (correction, r, 1/diag, face weights and a
+# quarter-cell coarse correction in, correction out: 25 B per cell).  The
+# coarse cycle (at most 1024-cell top) moves under 1% of that and is left out.
+OUTER_BYTES_PER_CELL = 56
+TILE_BYTES_PER_CELL = 50
+COARSE_CYCLE_CELLS = 1024
+
+
+def iteration_bytes(n0, n1, levels, cycles=1):
+    """Algorithmic bytes of one outer iteration: the FP64 outer step plus
+    `cycles` FP32 V-cycles."""
+    cells = [(n0 >> l) * (n1 >> l) for l in range(levels)]
+    tiled = sum(c for l, c in enumerate(cells) if c > COARSE_CYCLE_CELLS and l < levels - 1)
+    return OUTER_BYTES_PER_CELL * cells[0] + cycles * TILE_BYTES_PER_CELL * tiled
+
+
+def config2(args, torch, abi, ops, O, P):
+    """2D 512x512 projection Poisson (the configuration of the earlier
+    default line): one complete solve per step, mixed vs FP64."""
+    world = 1
+    g, b, f = c2_problem()
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+    db = [dev(x) for x in b]
     df = dev(f)
-    res = {}
-    for prec in ("fp64", "mixed"):
-        o = ops.default_options(False)
-        o.tolerance, o.hang, o.max_iter = TOL, 1e-15, 300
-        o.precision = abi.PREC_MIXED if prec == "mixed" else abi.PREC_F64
-        S = ops.AMRMultiGrid(pop, o)
+    op = ops.ProjectionOp(g, abi.make_bc(), 0.0, 1.0, None, db)
+    solvers = {"mixed": ops.AMRMultiGrid(op, c2_options(abi, ops, True)),
+               "fp64": ops.AMRMultiGrid(op, c2_options(abi, ops, False))}
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    ncell = g.n[0] * g.n[1]
+    stream = torch.cuda.current_stream()
+
+    def timed(name, steps, warmup):
+        S = solvers[name]
         phi = torch.zeros_like(df)
-        S.solve(phi, df)
+        for _ in range(warmup):
+            phi.zero_()
+            st, rc = S.solve(phi, df)
+            assert rc == 0, "solve failed rc=%d" % rc
+        tot_ms, upd, last, launches, iters = 0.0, 0.0, None, 0.0, 0
+        for _ in range(steps):
+            phi.zero_()
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            if world > 1:
+                torch.distributed.barrier()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            st, rc = S.solve(phi, df)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            assert rc == 0, "solve failed rc=%d" % rc
+            tot_ms += e0.elapsed_time(e1)
+            upd += st.cell_updates
+            launches += st.kernel_launches
+            iters += st.iterations
+            last = st
+        tot_ms = aggregate_max(tot_ms, world, "cuda")
+        return tot_ms, upd, last, phi, launches, iters
+
+    with Clocks() as clk:
+        ms_mixed, upd_mixed, st_mixed, phi_mixed, nl_mixed, it_mixed = timed("mixed", args.steps,
+                                                                             args.warmup)
+        ms_f64, upd_f64, st_f64, phi_f64, nl_f64, it_f64 = timed("fp64", args.steps, args.warmup)
+
+    # error of the mixed solution against the FP64 solution (null space removed)
+    a = phi_f64.cpu().numpy()
+    m = phi_mixed.cpu().numpy()
+    err = float(np.abs((a - a.mean()) - (m - m.mean())).max() / np.abs(a - a.mean()).max())
+
+    # end to end through the C ABI: pinned host rhs -> device -> solve -> host
+    h_rhs = torch.from_numpy(f.copy()).pin_memory()
+    h_out = torch.empty_like(h_rhs).pin_memory()
+    d_rhs = torch.empty_like(df)
+    phi = torch.zeros_like(df)
+    S = solvers["mixed"]
+    for _ in range(args.warmup):
+        d_rhs.copy_(h_rhs, non_blocking=True)
         phi.zero_()
-        ms, (st, rc) = _events_ms(lambda: S.solve(phi, df))
-        res[prec] = (ms, st, rc, phi.clone())
-    a, m = res["fp64"][3], res["mixed"][3]
-    err = float(((a - a.mean()) - (m - m.mean())).abs().max() / (a - a.mean()).abs().max())
-    # one (H, C) backward-Euler FAS step on the same grid, FP64
-    rng = np.random.default_rng(4)
-    prm = abi.make_params(stefan=5.0, compositionRatio=5.0, waterDistributionCoeff=1e-3,
-                          specificHeatRatio=1.0, heatConductivityRatio=1.0)
-    der = abi.make_bc({(2, 0, 0): (abi.BC_DIRICHLET, -1.0), (2, 0, 1): (abi.BC_DIRICHLET, -1.0)})
-    phi0 = np.empty((2,) + abi.cell_shape(g))
-    phi0[0] = 6.0 - 4.0 * np.linspace(1, 0, n)[:, None, None] * (1 + 1e-2 * rng.standard_normal((n, n, n)))
-    phi0[1] = -1.0
-    bh = [np.stack([-np.ones(abi.face_shape(g, d)), -np.full(abi.face_shape(g, d), 1e-2)])
-          for d in range(3)]
-    hop = ops.NLMultiCompOp(g, prm, abi.make_bc(), der, 1.0, 1.0, None, [dev(x) for x in bh])
-    HS = ops.AMRFASMultiGrid(hop, ops.default_options(True))
-    d0 = dev(phi0)
-    new = d0.clone()
-    ms_hc, (st_h, rc_h) = _events_ms(lambda: HS.backwardEuler(new, d0, 1e-4))
-    cells = n ** 3
-    return {"metric": "3D 256^3 projection solve cell-updates/s: mixed vs FP64 at 1e-10",
-            "value": res["mixed"][1].cell_updates / (res["mixed"][0] * 1e-3),
-            "unit": "cell-updates/s", "higher_is_better": True,
-            "mixed_ms": res["mixed"][0], "fp64_ms": res["fp64"][0],
-            "fp64_value": res["fp64"][1].cell_updates / (res["fp64"][0] * 1e-3),
-            "iterations": {"fp64": res["fp64"][1].iterations, "mixed": res["mixed"][1].iterations},
-            "rel_err_mixed_vs_fp64": err,
-            "hc_fas_step": {"ms": ms_hc, "iterations": st_h.iterations, "rc": rc_h,
-                            "cell_updates_per_s": st_h.cell_updates / (ms_hc * 1e-3)},
-            "config": {"workload": "3D 256^3 (16.8M cells) Kozeny-Carman projection Poisson, "
-                                   "periodic x, Neumann y/z; (H, C) BE step dt=1e-4", "cells": cells}}
+        S.solve(phi, d_rhs)
+        h_out.copy_(phi, non_blocking=True)
+    torch.cuda.synchronize()
+    e2e_ms, e2e_upd = 0.0, 0.0
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        d_rhs.copy_(h_rhs, non_blocking=True)
+        phi.zero_()
+        st, rc = S.solve(phi, d_rhs)
+        h_out.copy_(phi, non_blocking=True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        e2e_ms += e0.elapsed_time(e1)
+        e2e_upd += st.cell_updates
+
+    # roofline of the timed unit the events see: one outer iteration of the
+    # mixed solve (its ~10 kernels run back to back inside the device-resident
+    # graph loop; their individual shares come from the ncu launch list)
+    hbm, kind = peaks()
+    it_us = ms_mixed * 1e3 / max(it_mixed, 1)
+    cyc_per_it = st_mixed.cycles / max(st_mixed.iterations, 1)
+    alg_bytes = iteration_bytes(g.n[0], g.n[1], st_mixed.levels, round(cyc_per_it))
+    achieved = alg_bytes / (it_us * 1e-6) / 1e9
+    clocks = clk.summary()
+    value = upd_mixed / (ms_mixed * 1e-3) * world
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "cell-updates/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_mixed / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32-inner/f64-outer",
+        "data": "synthetic (seeded Kozeny-Carman permeability of a Gaussian-filtered porosity)",
+        "config": {"workload": "projection Poisson div(Pi grad p)=div u*, 2D 512x512, "
+                               "periodic x / Neumann y, to 1e-10 max-norm rel residual",
+                   "cells": ncell, "levels": st_mixed.levels, "l2": "flushed (512 MiB write) between steps",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "fp64": {"value": upd_f64 / (ms_f64 * 1e-3) * world, "ms_per_step": ms_f64 / args.steps,
+                 "iterations": st_f64.iterations, "cycles": st_f64.cycles,
+                 "gpu_launches": int(nl_f64)},
+        "mixed": {"iterations": st_mixed.iterations, "cycles": st_mixed.cycles,
+                  "final_rel_residual": st_mixed.final_norm / st_mixed.initial_norm,
+                  "rel_err_vs_fp64_solution": err},
+        "time_to_solution_ratio_fp64_over_mixed": ms_f64 / ms_mixed,
+        "e2e": {"value": e2e_upd / (e2e_ms * 1e-3) * world, "unit": "cell-updates/s",
+                "h2d_bytes_per_step": int(ncell * 8), "d2h_bytes_per_step": int(ncell * 8)},
+        "roofline": {"bound": "hbm", "kernel": "one mixed outer iteration (graph body: FP64 outer "
+                                               "step, lean FP32 tiles, single-CTA coarse cycle)",
+                     "achieved": achieved, "peak": hbm, "peak_kind": kind, "unit": "GB/s",
+                     "frac": achieved / hbm, "traffic": None,
+                     "iteration_us": it_us, "alg_bytes_per_iteration": alg_bytes},
+        "clocks": clocks,
+        "gpu_launches": int(nl_mixed),
+    }
+    return line
 
 
 def config5(args, torch, abi, ops, O, P):
@@ -656,15 +907,17 @@ def run_config(args):
     from mushy_gb300 import abi, ops
     from oracle import oracle as O
     import problems as P
-    fn = {1: config1, 3: config3, 4: config4, 5: config5}[args.config]
+    fn = {1: config1, 2: config2, 3: config3, 5: config5}[args.config]
     line = fn(args, torch, abi, ops, O, P)
     line.update({"n_gpus": 1, "data": "synthetic (seeded)", "config_index": args.config})
     print(json.dumps(line))
 
 
 def run_profile(args):
-    """One warm-up solve and one solve of 3 outer iterations of the bench
-    problem (mixed or fp64), for ncu launch lists and captures."""
+    """Short runs for ncu launch lists and captures: c4 / c4-fp64 1 + --warmup
+    steps of the 256^3 workload, c2-mixed / c2-fp64
+    two 3-iteration solves of the 512^2 projection problem, hc two FAS steps
+    at 64^2, adjoint one Newton step and its adjoint solve at 256^2."""
     import torch
     import __graft_entry__
     __graft_entry__.build()
@@ -705,10 +958,21 @@ def run_profile(args):
                           "newton_linear_cycles": st_n.cycles,
                           "adjoint_cycles": st_a.iterations}))
         return
-    g, b, f = make_problem()
+    if args.profile in ("c4", "c4-fp64"):
+        # one step of the 256^3 workload with plain launches (profilers do
+        # not see kernel nodes inside graphs with conditional nodes)
+        prob = c4_problem(torch, abi, ops)
+        R = C4Runner(torch, abi, ops, prob, use_graph=0)
+        prec = "mixed" if args.profile == "c4" else "fp64"
+        for _ in range(1 + args.warmup):
+            out = R.step(prec)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile": args.profile, **C4Runner.summary(out)}))
+        return
+    g, b, f = c2_problem()
     dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()
     op = ops.ProjectionOp(g, abi.make_bc(), 0.0, 1.0, None, [dev(x) for x in b])
-    o = options(abi, ops, args.profile == "mixed")
+    o = c2_options(abi, ops, args.profile == "c2-mixed")
     o.max_iter = 3
     # same kernels as the timed solve, launched one by one: profilers do not
     # see kernel nodes inside a graph with a conditional (WHILE) node
@@ -729,9 +993,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--profile", choices=["mixed", "fp64", "hc", "adjoint"],
+    ap.add_argument("--profile", choices=["c4", "c4-fp64", "c2-mixed", "c2-fp64", "hc", "adjoint"],
                     help="run one short solve for a profiler and exit")
-    ap.add_argument("--config", type=int, choices=[1, 3, 4, 5],
+    ap.add_argument("--config", type=int, choices=[1, 2, 3, 5],
                     help="measure another configuration (one JSON line) and exit")
     args = ap.parse_args()
     if args.profile:

@@ -319,6 +319,7 @@ __global__ void __launch_bounds__(kBlock) adj_jac_kernel(Geom G, ClosureParams c
   }
 }
 
+#ifndef MLGPU_ADJ_F32_UNIT  // FP64 unit only (launch_f32_adj.cu instantiates the FP32 cycles)
 // {d por/dH, d por/dC} of every cell
 __global__ void __launch_bounds__(kBlock) porosity_jac_kernel(Geom G, ClosureParams cp,
                                                               const double *__restrict__ u,
@@ -331,6 +332,7 @@ __global__ void __launch_bounds__(kBlock) porosity_jac_kernel(Geom G, ClosurePar
     dp[q + n] = d2[1];
   }
 }
+#endif
 
 // the inverse of every cell's diagonal block M of A^T: {M3, -M1, -M2, M0}/det
 template <class T, int DIM>

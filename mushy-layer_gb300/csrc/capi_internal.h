@@ -77,6 +77,24 @@ cudaError_t launch_outer_coefs(const VCArgs<double> &A, double *cx, double *cy, 
 cudaError_t launch_hcm_jac(const Geom &G, const ClosureParams &cp, const double *u, float *J,
                            cudaStream_t s);
 cudaError_t launch_hcm_update(long long n, double *u, const float *e, cudaStream_t s);
+cudaError_t launch_newton_step(long long n, double *u, const double *u_old, double scale,
+                               const float *e, cudaStream_t s);
+// FP32 Jacobian cycles of the mixed-precision Newton solve (launch_f32_adj.cu)
+cudaError_t launch_adj_jac(const Geom &G, const ClosureParams &cp, const double *u, float *J,
+                           cudaStream_t s);
+cudaError_t launch_adj_op(const AdjArgs<float> &A, int mode, int norm, const float *y,
+                          const float *g, float *out, double *part, int *nparts, cudaStream_t s,
+                          bool tr);
+cudaError_t launch_adj_gsrb(const AdjArgs<float> &A, float *y, const float *g, int pass,
+                            cudaStream_t s, bool tr);
+cudaError_t launch_adj_relax_block(const AdjArgs<float> &A, float *y, const float *g, int sweeps,
+                                   int zero, cudaStream_t s, bool tr);
+cudaError_t launch_adj_minv(const AdjArgs<float> &A, const float *zero, float *Minv,
+                            cudaStream_t s);
+cudaError_t launch_adj_bottom_direct(const AdjArgs<float> &A, float *y, const float *g,
+                                     cudaStream_t s, bool tr);
+cudaError_t launch_adj_restrict(const AdjArgs<float> &A, const Geom &C, const float *y,
+                                const float *g, float *gc, cudaStream_t s, bool tr);
 // FP64 nonlinear kernels over the per-level (T, C_l) cache
 cudaError_t launch_nlc_closure(const NLArgs<double> &A, const double *phi, double *tcl,
                                cudaStream_t s);

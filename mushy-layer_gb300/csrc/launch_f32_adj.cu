@@ -1,0 +1,78 @@
+// launch_f32_adj.cu -- FP32 launchers of the Jacobian kernels
+// (adjoint_kernels.cuh) for the inner linear cycles of the mixed-precision
+// Newton solve: the closure Jacobian J is evaluated in FP64 and stored in
+// FP32, the cycles (block red/black Gauss-Seidel with the inverse 2x2
+// diagonal block of each cell, 2^D residual restriction, prolongation, bottom
+// solve) run in FP32.  FMA contraction is left on, as in launch_f32.cu.
+#define MLGPU_ADJ_UNIT 1
+#define MLGPU_ADJ_F32_UNIT 1
+#include "launch_impl.cuh"
+#include "adjoint_kernels.cuh"
+
+namespace mlgpu {
+
+#define MLGPU_TR_SWITCH32(tr, ...) \
+  do {                             \
+    if (tr) {                      \
+      constexpr bool TR = true;    \
+      __VA_ARGS__;                 \
+    } else {                       \
+      constexpr bool TR = false;   \
+      __VA_ARGS__;                 \
+    }                              \
+  } while (0)
+
+cudaError_t launch_adj_jac(const Geom &G, const ClosureParams &cp, const double *u, float *J,
+                           cudaStream_t s) {
+  adj_jac_kernel<float><<<blocks_for(G.ncell), kBlock, 0, s>>>(G, cp, u, J);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_adj_op(const AdjArgs<float> &A, int mode, int norm, const float *y,
+                          const float *g, float *out, double *part, int *nparts, cudaStream_t s,
+                          bool tr) {
+  const int nb = blocks_for(A.G.ncell);
+  if (nparts) *nparts = (part && mode == ADJ_RESIDUAL && norm >= 0) ? nb : 0;
+  if (mode == ADJ_RESIDUAL && norm >= 0) {
+    if (!part) return cudaErrorInvalidValue;
+    MLGPU_TR_SWITCH32(tr, MLGPU_DIM_SWITCH(A.G.dim, MLGPU_NORM_SWITCH(norm, (adj_op_kernel<float, DIM, ADJ_RESIDUAL, NORM, TR><<<nb, kBlock, 0, s>>>(A, y, g, out, part)))));
+  } else if (mode == ADJ_RESIDUAL) {
+    MLGPU_TR_SWITCH32(tr, MLGPU_DIM_SWITCH(A.G.dim, (adj_op_kernel<float, DIM, ADJ_RESIDUAL, -1, TR><<<nb, kBlock, 0, s>>>(A, y, g, out, part))));
+  } else {
+    MLGPU_TR_SWITCH32(tr, MLGPU_DIM_SWITCH(A.G.dim, (adj_op_kernel<float, DIM, ADJ_APPLY, -1, TR><<<nb, kBlock, 0, s>>>(A, y, g, out, part))));
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_adj_gsrb(const AdjArgs<float> &A, float *y, const float *g, int pass,
+                            cudaStream_t s, bool tr) {
+  MLGPU_TR_SWITCH32(tr, MLGPU_DIM_SWITCH(A.G.dim, (adj_gsrb_kernel<float, DIM, TR><<<blocks_for(colour_threads(A.G)), kBlock, 0, s>>>(A, y, g, pass))));
+  return cudaGetLastError();
+}
+
+cudaError_t launch_adj_relax_block(const AdjArgs<float> &A, float *y, const float *g, int sweeps,
+                                   int zero, cudaStream_t s, bool tr) {
+  MLGPU_TR_SWITCH32(tr, MLGPU_DIM_SWITCH(A.G.dim, (adj_relax_block_kernel<float, DIM, TR><<<1, 1024, 0, s>>>(A, y, g, sweeps, zero))));
+  return cudaGetLastError();
+}
+
+cudaError_t launch_adj_minv(const AdjArgs<float> &A, const float *zero, float *Minv,
+                            cudaStream_t s) {
+  MLGPU_DIM_SWITCH(A.G.dim, (adj_minv_kernel<float, DIM><<<blocks_for(A.G.ncell), kBlock, 0, s>>>(A, zero, Minv)));
+  return cudaGetLastError();
+}
+
+cudaError_t launch_adj_bottom_direct(const AdjArgs<float> &A, float *y, const float *g,
+                                     cudaStream_t s, bool tr) {
+  if (2 * A.G.ncell > kAdjDirectMax) return cudaErrorInvalidValue;
+  MLGPU_TR_SWITCH32(tr, MLGPU_DIM_SWITCH(A.G.dim, (adj_bottom_direct_kernel<float, DIM, TR><<<1, kAdjDirectMax, 0, s>>>(A, y, g))));
+  return cudaGetLastError();
+}
+
+cudaError_t launch_adj_restrict(const AdjArgs<float> &A, const Geom &C, const float *y,
+                                const float *g, float *gc, cudaStream_t s, bool tr) {
+  MLGPU_TR_SWITCH32(tr, MLGPU_DIM_SWITCH(A.G.dim, (adj_restrict_kernel<float, DIM, TR><<<blocks_for(C.ncell), kBlock, 0, s>>>(A, C, y, g, gc))));
+  return cudaGetLastError();
+}
+
+}  // namespace mlgpu

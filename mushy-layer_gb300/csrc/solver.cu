@@ -1187,6 +1187,10 @@ struct AdjLevel {
   Coefs<double> c64;
   double *u = nullptr, *J = nullptr, *y = nullptr, *g = nullptr, *r = nullptr;
   double *Minv = nullptr;  // inverse diagonal blocks of A^T, per state
+  // mixed-precision Newton: FP32 copies of the coefficients, J (from the FP64
+  // closure derivative), the inverse diagonal blocks and the cycle's fields
+  Coefs<float> c32;
+  float *J32 = nullptr, *Minv32 = nullptr, *y32 = nullptr, *g32 = nullptr, *r32 = nullptr;
 };
 
 class HCAdjSolver : public mlgpu_solver {
@@ -1200,18 +1204,33 @@ class HCAdjSolver : public mlgpu_solver {
   // tr: cycles on A^T (adjoint) or on A (the linear solve of a Newton step);
   // one captured iteration graph per mode
   bool tr = true;
-  cudaGraphExec_t graph = nullptr, graph_lin = nullptr;
+  // MLGPU_PREC_MIXED: the linear cycles of a Newton step run in FP32 (the
+  // Newton residual, its norm, the update and the closure stay FP64); the
+  // adjoint solve stays FP64
+  bool mixed = false;
+  cudaGraphExec_t graph = nullptr, graph_lin = nullptr, graph_lin32 = nullptr;
   double *nf = nullptr, *nuold = nullptr;  // Newton: rhs of N(u) = f, previous u
+  double *ntcl = nullptr;  // Newton: (T, C_l) of level 0, the residual's closure cache
+  // Newton's kernels per piece (counted once): state and Jacobians of every
+  // level, the linear residual with its norm, one linear cycle + residual
+  int nk_state = -1, nk_res = -1, nk_iter = -1;
+  // kernels of nl_residual (closure, stencil + norm, combine, max norm,
+  // combine) and of one step update
+  static constexpr int kNlResidualKernels = 5, kStepKernels = 1;
 
   ~HCAdjSolver() override {
     if (graph) cudaGraphExecDestroy(graph);
     if (graph_lin) cudaGraphExecDestroy(graph_lin);
+    if (graph_lin32) cudaGraphExecDestroy(graph_lin32);
     if (host_norm) cudaFreeHost(host_norm);
   }
+
+  bool lin32() const { return mixed && !tr; }
 
   size_t layout(char *base) {
     Arena A;
     A.base = base;
+    mixed = o.precision == MLGPU_PREC_MIXED;
     int depth = mg_depth(op.grid, o.max_coarse);
     L.assign(depth + 1, AdjLevel());
     mlgpu_grid g = op.grid;
@@ -1232,12 +1251,22 @@ class HCAdjSolver : public mlgpu_solver {
       L[l].y = A.get<double>(n);
       L[l].g = A.get<double>(n);
       L[l].r = A.get<double>(n);
+      if (mixed) {
+        if (op.aCoef) L[l].c32.a = A.get<float>(n);
+        for (int d = 0; d < g.dim; d++) L[l].c32.b[d] = A.get<float>(2 * nfaces(g, d));
+        L[l].J32 = A.get<float>(2 * n);
+        L[l].Minv32 = A.get<float>(2 * n);
+        L[l].y32 = A.get<float>(n);
+        L[l].g32 = A.get<float>(n);
+        L[l].r32 = A.get<float>(n);
+      }
       g = coarsen_grid(g);
     }
     part = A.get<double>(kNormScratchDoubles);
     bcg = A.get<double>(16);
     nf = A.get<double>(2 * ncells(op.grid));
     nuold = A.get<double>(2 * ncells(op.grid));
+    ntcl = A.get<double>(2 * ncells(op.grid));
     return A.off + 256;
   }
 
@@ -1248,6 +1277,13 @@ class HCAdjSolver : public mlgpu_solver {
       for (int d = 0; d < F.dim; d++)
         CK(launch_coarsen_faces<double>(F, 2, d, L[l - 1].c64.b[d], L[l].c64.b[d], s));
     }
+    if (mixed)
+      for (auto &lv : L) {
+        const long long n = 2 * lv.G.ncell;
+        if (op.aCoef) CK(launch_convert<float, double>(n, lv.c32.a, lv.c64.a, s));
+        for (int d = 0; d < lv.G.dim; d++)
+          CK(launch_convert<float, double>(2 * lv.G.nface(d), lv.c32.b[d], lv.c64.b[d], s));
+      }
     const int last = (int)L.size() - 1;
     double u = 0;
     for (int l = 0; l <= last; l++) {
@@ -1268,6 +1304,27 @@ class HCAdjSolver : public mlgpu_solver {
     return A;
   }
 
+  // FP32 operator of level l (mixed-precision Newton cycles)
+  AdjArgs<float> args32(int l) {
+    const AdjArgs<double> D = args(l);
+    AdjArgs<float> A;
+    A.G = D.G;
+    A.cp = D.cp;
+    A.phi_bc = D.phi_bc;
+    A.dbc = D.dbc;
+    A.apply_dbc = D.apply_dbc;
+    A.alpha = (float)D.alpha;
+    A.beta = (float)D.beta;
+    A.dxinv = (float)D.dxinv;
+    A.dx = (float)D.dx;
+    A.a = L[l].c32.a;
+    for (int d = 0; d < 3; d++) A.b[d] = L[l].c32.b[d];
+    A.J = L[l].J32;
+    A.u = L[l].u;
+    A.Minv = L[l].Minv32;
+    return A;
+  }
+
   // the wall rule of the adjoint variable in the prolongation
   BCD ybc() const { return make_bcd(op.apply_derived_bc ? op.derived_bc : op.phi_bc); }
 
@@ -1282,6 +1339,15 @@ class HCAdjSolver : public mlgpu_solver {
     for (size_t l = 1; l < L.size(); l++)
       CK(launch_restrict_avg<double>(L[l - 1].G, 2, L[l - 1].u, L[l].u, s));
     const ClosureParams cp = make_cp(op.params);
+    if (lin32()) {
+      // FP64 closure derivative stored in FP32; the inverse blocks in FP32
+      for (auto &lv : L) CK(launch_adj_jac(lv.G, cp, lv.u, lv.J32, s));
+      for (size_t l = 0; l < L.size(); l++) {
+        CK(cudaMemsetAsync(L[l].r32, 0, sizeof(float) * 2 * L[l].G.ncell, s));
+        CK(launch_adj_minv(args32((int)l), L[l].r32, L[l].Minv32, s));
+      }
+      return MLGPU_OK;
+    }
     for (auto &lv : L) CK(launch_adj_jac(lv.G, cp, lv.u, lv.J, s));
     // the smoother's inverse diagonal blocks (r is free here: a zero field)
     for (size_t l = 0; l < L.size(); l++) {
@@ -1330,7 +1396,54 @@ class HCAdjSolver : public mlgpu_solver {
     return MLGPU_OK;
   }
 
+  // ---- FP32 cycles on A (mixed-precision Newton); same structure as the
+  // FP64 ones above
+  int smooth32(int l, int n) {
+    AdjArgs<float> A = args32(l);
+    for (int i = 0; i < n; i++)
+      for (int pass = 0; pass < 2; pass++) CK(launch_adj_gsrb(A, L[l].y32, L[l].g32, pass, s, false));
+    return MLGPU_OK;
+  }
+
+  int cycle32(int l) {
+    const int last = (int)L.size() - 1;
+    AdjArgs<float> A = args32(l);
+    if (l == last) {
+      if (2 * L[l].G.ncell <= kAdjDirectMax)
+        CK(launch_adj_bottom_direct(A, L[l].y32, L[l].g32, s, false));
+      else
+        CK(launch_adj_relax_block(A, L[l].y32, L[l].g32, o.bottom_max_iter, l > 0 ? 1 : 0, s,
+                                  false));
+      return MLGPU_OK;
+    }
+    if (l > 0) CK(cudaMemsetAsync(L[l].y32, 0, sizeof(float) * 2 * L[l].G.ncell, s));
+    int rc = smooth32(l, o.num_smooth_down);
+    if (rc) return rc;
+    CK(launch_adj_restrict(A, L[l + 1].G, L[l].y32, L[l].g32, L[l + 1].g32, s, false));
+    for (int m = 0; m < o.num_mg; m++) {
+      rc = cycle32(l + 1);
+      if (rc) return rc;
+    }
+    CK(launch_prolong<float>(L[l].G, ybc(), 2, o.prolong, L[l].y32, L[l + 1].y32, nullptr, s));
+    return smooth32(l, o.num_smooth_up);
+  }
+
+  // FP32 linear residual g - A y of level 0 with its norm (accumulated in FP64)
+  int residual_norm32() {
+    int nparts = 0;
+    CK(launch_adj_op(args32(0), ADJ_RESIDUAL, o.norm_type, L[0].y32, L[0].g32, L[0].r32, part,
+                     &nparts, s, false));
+    CK(launch_finalize_norm(o.norm_type, part, nparts, part + kMaxBlocks, s));
+    CK(cudaMemcpyAsync(host_norm, part + kMaxBlocks, sizeof(double), cudaMemcpyDeviceToHost, s));
+    return MLGPU_OK;
+  }
+
   int iteration() {
+    if (lin32()) {
+      int rc = cycle32(0);
+      if (rc) return rc;
+      return residual_norm32();
+    }
     int rc = cycle(0);
     if (rc) return rc;
     return residual_norm();
@@ -1338,7 +1451,7 @@ class HCAdjSolver : public mlgpu_solver {
 
   int run_iteration() {
     if (!o.use_graph) return iteration();
-    cudaGraphExec_t &gx = tr ? graph : graph_lin;
+    cudaGraphExec_t &gx = tr ? graph : (mixed ? graph_lin32 : graph_lin);
     if (!gx) {
       cudaGraph_t g;
       CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
@@ -1367,8 +1480,12 @@ class HCAdjSolver : public mlgpu_solver {
   int nl_residual() {
     const long long n2 = 2 * L[0].G.ncell;
     int nparts = 0;
-    CK(launch_nl_op<double>(make_nl_args<double>(op), NL_RESIDUAL, MLGPU_NORM_L2, L[0].u, nf,
-                            L[0].g, nullptr, part, &nparts, s));
+    // the closure once per cell into the cache, then the stencil over it
+    // (bitwise the residual that evaluates the closure at every stencil point)
+    const NLArgs<double> N = make_nl_args<double>(op);
+    CK(launch_nlc_closure(N, L[0].u, ntcl, s));
+    CK(launch_nlc_op(N, NL_RESIDUAL, MLGPU_NORM_L2, L[0].u, ntcl, nf, L[0].g, nullptr, part,
+                     &nparts, s));
     CK(launch_finalize_norm(MLGPU_NORM_L2, part, nparts, part + kMaxBlocks, s));
     CK(cudaMemcpyAsync(host_norm + 1, part + kMaxBlocks, sizeof(double), cudaMemcpyDeviceToHost,
                        s));
@@ -1396,22 +1513,35 @@ class HCAdjSolver : public mlgpu_solver {
     if (enter()) return MLGPU_ERR_CUDA;
     CK(cudaMemcpyAsync(L[0].u, user_u, bytes, cudaMemcpyDeviceToDevice, s));
     CK(cudaMemcpyAsync(nf, user_f, bytes, cudaMemcpyDeviceToDevice, s));
+    if (nk_state < 0) {
+      nk_state = count_kernels([&] { return state_levels(); });
+      nk_res = count_kernels([&] { return mixed ? residual_norm32() : residual_norm(); });
+      nk_iter = count_kernels([&] { return iteration(); });
+    }
     int rc = nl_residual();
     if (rc) return rc;
     Outer S;
     S.norm0 = S.norm = S.prev = *host_norm;
     stats_begin(st, (int)L.size(), S.norm0);
     st->cell_updates = (double)L[0].G.ncell;
+    st->kernel_launches = kNlResidualKernels;
     if (!std::isfinite(S.norm0)) S.status = 8;
     int stall = 0;  // consecutive steps that cut the residual by under 5%
     double merit = host_norm[1];
     while (outer_continue(o, S)) {
       rc = state_levels();
       if (rc) return rc;
-      // linear solve A d = r, d in L[0].y from zero
-      CK(cudaMemsetAsync(L[0].y, 0, bytes, s));
-      rc = residual_norm();
+      // linear solve A d = r, d in L[0].y (FP64) or L[0].y32 (mixed) from zero
+      if (mixed) {
+        CK(launch_convert<float, double>(n2, L[0].g32, L[0].g, s));
+        CK(cudaMemsetAsync(L[0].y32, 0, sizeof(float) * n2, s));
+        rc = residual_norm32();
+      } else {
+        CK(cudaMemsetAsync(L[0].y, 0, bytes, s));
+        rc = residual_norm();
+      }
       if (rc) return rc;
+      st->kernel_launches += nk_state + nk_res + (mixed ? 1 : 0);
       CK(cudaStreamSynchronize(s));
       const double l0 = *host_norm;
       for (int c = 0; c < lin_max && *host_norm > lin_tol * l0; c++) {
@@ -1420,16 +1550,22 @@ class HCAdjSolver : public mlgpu_solver {
         CK(cudaStreamSynchronize(s));
         st->cycles += 1;
         st->cell_updates += updates_per_iter;
+        st->kernel_launches += nk_iter;
       }
       CK(cudaMemcpyAsync(nuold, L[0].u, bytes, cudaMemcpyDeviceToDevice, s));
       double scale = 1.0;
       for (int h = 0; h <= 4; h++) {
         // u = u_old + scale d
-        CK(cudaMemcpyAsync(L[0].u, nuold, bytes, cudaMemcpyDeviceToDevice, s));
-        CK(launch_axpby<double>(n2, scale, L[0].y, 1.0, L[0].u, s));
+        if (mixed) {
+          CK(launch_newton_step(n2, L[0].u, nuold, scale, L[0].y32, s));
+        } else {
+          CK(cudaMemcpyAsync(L[0].u, nuold, bytes, cudaMemcpyDeviceToDevice, s));
+          CK(launch_axpby<double>(n2, scale, L[0].y, 1.0, L[0].u, s));
+        }
         rc = nl_residual();
         if (rc) return rc;
         st->cell_updates += (double)L[0].G.ncell;
+        st->kernel_launches += kStepKernels + kNlResidualKernels;
         if (std::isfinite(host_norm[1]) && host_norm[1] <= merit) break;
         scale *= 0.5;
       }
@@ -1524,7 +1660,7 @@ class HCAdjSolver : public mlgpu_solver {
   int set_alpha_beta(double a, double b) override {
     op.alpha = a;
     op.beta = b;
-    for (auto *gp : {&graph, &graph_lin})
+    for (auto *gp : {&graph, &graph_lin, &graph_lin32})
       if (*gp) {
         cudaGraphExecDestroy(*gp);
         *gp = nullptr;

@@ -27,6 +27,7 @@ UNITS = {
     "launch_f64_adj.cu": ["--fmad=false"],
     "launch_f64_nlc.cu": ["--fmad=false"],
     "launch_f32.cu": [],
+    "launch_f32_adj.cu": [],
     "capi.cu": ["--fmad=false"],
     "solver.cu": ["--fmad=false"],
     "capi_noalloc.cu": ["--fmad=false"],

@@ -1,0 +1,118 @@
+"""Converged nonlinear (H, C) solves in mixed precision.
+
+The reference's FAS smoother divides by the diagonal of the diffusion
+operator alone and ignores dT/dH, so with its 10-iteration cap the (H, C)
+backward-Euler steps of the 64x64 and 1024x1024 configurations stop short of
+1e-10.  Newton's method on the Jacobian multigrid (block red/black smoother
+with each cell's exact 2x2 diagonal block, closure derivative included)
+reaches it.  The mixed-precision Newton runs those linear cycles in FP32;
+the Newton residual, its norm, the closure and the update stay FP64, so its
+fixed point is the FP64 one.  Checked here:
+
+* every step ends with status 0 at 1e-10 of its initial residual, in FP64
+  and in mixed precision;
+* the oracle's FP64 residual of the mixed solution is below 1e-10 of the
+  initial one;
+* mixed and FP64 states agree to 1e-8 of the field scale;
+* the FP64 Newton step agrees with the oracle's Newton driver to 1e-10.
+"""
+import numpy as np
+import pytest
+
+import problems as P
+from mushy_gb300 import abi
+from oracle import oracle as O
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+from test_gpu_parity import dev, host  # noqa: E402
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _lib():
+    import __graft_entry__
+    __graft_entry__.build()
+    yield
+
+
+def _opts(prec):
+    from mushy_gb300 import ops
+    o = ops.default_options(True)
+    o.tolerance, o.hang, o.max_iter, o.precision = 1e-10, -1.0, 60, prec
+    return o
+
+
+def _c1():
+    g = P.grid((64, 64))
+    prm = abi.make_params(stefan=5.0, compositionRatio=5.0, waterDistributionCoeff=1e-3,
+                          specificHeatRatio=1.0, heatConductivityRatio=1.0)
+    phi_bc = abi.make_bc()
+    der = abi.make_bc({(1, 0, 0): (abi.BC_DIRICHLET, -1.0), (1, 1, 0): (abi.BC_DIRICHLET, 0.5),
+                       (1, 0, 1): (abi.BC_DIRICHLET, -1.0), (1, 1, 1): (abi.BC_DIRICHLET, -1.0)})
+    phi0 = np.empty((2,) + abi.cell_shape(g))
+    phi0[0], phi0[1] = 6.0, -1.0
+    b = [np.stack([-np.ones(abi.face_shape(g, d)), np.zeros(abi.face_shape(g, d))])
+         for d in range(2)]
+    return g, prm, phi_bc, der, phi0, b
+
+
+def test_c1_newton_steps_converge_mixed_matches_fp64():
+    from mushy_gb300 import ops
+    g, prm, phi_bc, der, phi0, b = _c1()
+    dt = 1e-3
+    op = ops.NLMultiCompOp(g, prm, phi_bc, der, 1.0, -dt, None, [dev(x) for x in b])
+    ref = O.NLOpHost(g, prm, phi_bc, der, 1.0, -dt, None, b)
+    S64 = ops.AdjointMultiGrid(op, _opts(abi.PREC_F64))
+    SM = ops.AdjointMultiGrid(op, _opts(abi.PREC_MIXED))
+    oo = O.default_options(1)
+    oo.tolerance, oo.hang, oo.max_iter = 1e-10, -1.0, 60
+    c64, cm, h = dev(phi0), dev(phi0), phi0.copy()
+    for step in range(10):
+        n64, nm = c64.clone(), cm.clone()
+        st64, rc64 = S64.backwardEulerNewton(n64, c64, dt)
+        stm, rcm = SM.backwardEulerNewton(nm, cm, dt)
+        assert rc64 == 0 and rcm == 0, (step, rc64, rcm)
+        assert st64.final_norm <= 1e-10 * st64.initial_norm
+        assert stm.final_norm <= 1e-10 * stm.initial_norm
+        u64, um = host(n64), host(nm)
+        # the oracle's residual of the mixed state, and its Newton step
+        r0 = O.norm(O.nl_residual(ref, host(cm), host(cm)))
+        assert O.norm(O.nl_residual(ref, um, host(cm))) <= 1e-10 * r0 * 1.0001
+        h, st_r, rc_r = O.newton_solve(ref, oo, h, h)
+        assert rc_r == 0
+        assert np.abs(u64 - h).max() <= 1e-10 * np.abs(h).max(), step
+        assert np.abs(um - u64).max() <= 1e-8 * np.abs(u64).max(), step
+        c64, cm = n64, nm
+
+
+def test_c3_size_newton_step_mixed_matches_fp64():
+    """One backward-Euler (H, C) step of the 1024x1024 mushy-layer
+    configuration (CR=25, Le=200, liquid + 1e-3 noise, cold bottom,
+    dt=1e-5) to 1e-10, FP64 and mixed."""
+    from mushy_gb300 import ops
+    n, dt = 1024, 1e-5
+    g = P.grid((n, n))
+    rng = np.random.default_rng(3)
+    prm = abi.make_params(stefan=5.0, compositionRatio=25.0, waterDistributionCoeff=1e-3,
+                          specificHeatRatio=1.0, heatConductivityRatio=1.0)
+    phi_bc = abi.make_bc()
+    der = abi.make_bc({(1, 0, 0): (abi.BC_DIRICHLET, -1.0), (1, 0, 1): (abi.BC_DIRICHLET, -1.0)})
+    phi0 = np.empty((2,) + abi.cell_shape(g))
+    phi0[0] = 6.0 + 1e-3 * rng.standard_normal(abi.cell_shape(g))
+    phi0[1] = -1.0 + 1e-3 * rng.standard_normal(abi.cell_shape(g))
+    b = [np.stack([-np.ones(abi.face_shape(g, d)), -np.full(abi.face_shape(g, d), 1.0 / 200)])
+         for d in range(2)]
+    op = ops.NLMultiCompOp(g, prm, phi_bc, der, 1.0, -dt, None, [dev(x) for x in b])
+    out = {}
+    for prec in (abi.PREC_F64, abi.PREC_MIXED):
+        new = dev(phi0)
+        st, rc = ops.AdjointMultiGrid(op, _opts(prec)).backwardEulerNewton(new, dev(phi0), dt)
+        assert rc == 0, (prec, rc, st.iterations)
+        assert st.final_norm <= 1e-10 * st.initial_norm
+        out[prec] = host(new)
+    ref = O.NLOpHost(g, prm, phi_bc, der, 1.0, -dt, None, b)
+    r0 = O.norm(O.nl_residual(ref, phi0, phi0))
+    assert O.norm(O.nl_residual(ref, out[abi.PREC_MIXED], phi0)) <= 1e-10 * r0 * 1.0001
+    u64 = out[abi.PREC_F64]
+    assert np.abs(out[abi.PREC_MIXED] - u64).max() <= 1e-8 * np.abs(u64).max()
