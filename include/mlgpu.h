@@ -150,9 +150,13 @@ typedef struct mlgpu_mg_options {
   double hang;           /* stop when |r| > (1 - hang) * |r_prev| */
   double norm_thresh;    /* stop when |r0| <= norm_thresh */
   int relax_mode;        /* MLGPU_RELAX_GSRB or MLGPU_RELAX_JACOBI */
-  int bottom_solver;     /* MLGPU_BOTTOM_RELAX; MLGPU_BOTTOM_BICGSTAB (Chombo's
-                            BiCGStabSolver, the projection's default in the
-                            reference) is not built: MLGPU_ERR_ARG */
+  int bottom_solver;     /* MLGPU_BOTTOM_RELAX; MLGPU_BOTTOM_BICGSTAB (the role
+                            of Chombo's BiCGStabSolver, the projection's and
+                            velocity solves' default bottom in the reference,
+                            srcSubcycle/Projector.cpp:2976-2986,3012-3020):
+                            linear solvers only, one thread block in FP64,
+                            bottom_max_iter iterations at most; the FAS and
+                            Jacobian solvers refuse it (MLGPU_ERR_ARG) */
   int bottom_max_iter;   /* m_imax of the bottom solver */
   int max_coarse;        /* s_maxCoarse: coarsen while coarsenable(2^d * max_coarse) */
   int prolong;           /* MLGPU_PROLONG_* */

@@ -13,6 +13,7 @@
 #include "nl_cached_kernels.cuh"
 #include "hcm_kernels.cuh"
 #include "adjoint_kernels.cuh"
+#include "bicgstab_kernels.cuh"
 
 namespace mlgpu {
 
@@ -77,6 +78,10 @@ cudaError_t launch_outer_coefs(const VCArgs<double> &A, double *cx, double *cy, 
 cudaError_t launch_hcm_jac(const Geom &G, const ClosureParams &cp, const double *u, float *J,
                            cudaStream_t s);
 cudaError_t launch_hcm_update(long long n, double *u, const float *e, cudaStream_t s);
+// BiCGStab bottom solve of L e = rhs on one level (FP64 arithmetic, storage S)
+template <class S>
+cudaError_t launch_vc_bicgstab(const VCArgs<double> &A, S *e, const S *rhs, double *ws,
+                               int imax, cudaStream_t s);
 cudaError_t launch_newton_step(long long n, double *u, const double *u_old, double scale,
                                const float *e, cudaStream_t s);
 // FP32 Jacobian cycles of the mixed-precision Newton solve (launch_f32_adj.cu)

@@ -220,6 +220,8 @@ class VCSolver : public mlgpu_solver {
   // level pack of the lean FP32 coarse cycle (mixed 2D): levels cyc_top..last
   float *cyc_pack = nullptr;
   int cyc_top = -1;
+  // BiCGStab bottom solve: FP64 work arrays of the coarsest level
+  double *bicg_ws = nullptr;
   std::vector<int> cyc_off;
 
   ~VCSolver() override {
@@ -290,7 +292,12 @@ class VCSolver : public mlgpu_solver {
       }
       g = coarsen_grid(g);
     }
-    use_block_cycle = o.relax_mode == MLGPU_RELAX_GSRB && o.num_mg == 1 && o.fuse_levels;
+    // the fused single-block coarse cycles end in relaxation: a BiCGStab
+    // bottom takes the per-level path
+    use_block_cycle = o.relax_mode == MLGPU_RELAX_GSRB && o.num_mg == 1 && o.fuse_levels &&
+                      o.bottom_solver == MLGPU_BOTTOM_RELAX;
+    if (o.bottom_solver == MLGPU_BOTTOM_BICGSTAB)
+      bicg_ws = A.get<double>(kBiCGArrays * ncells(L[depth].grid));
     // the lean coarse cycle starts at the first level of at most kFastCycCells
     cyc_top = -1;
     cyc_off.clear();
@@ -588,6 +595,13 @@ class VCSolver : public mlgpu_solver {
       return MLGPU_OK;
     }
     if (l == last) {
+      if (o.bottom_solver == MLGPU_BOTTOM_BICGSTAB) {
+        if (zero_init) CK(cudaMemsetAsync(L[l].e, 0, sizeof(T) * L[l].G.ncell, s));
+        VCArgs<double> A64 = args<double>(l);
+        CK(launch_vc_bicgstab<T>(A64, (T *)L[l].e, (const T *)L[l].r, bicg_ws,
+                                 o.bottom_max_iter, s));
+        return MLGPU_OK;
+      }
       if (o.relax_mode == MLGPU_RELAX_JACOBI) return relax<T>(l, o.bottom_max_iter, zero_init);
       CK(launch_vc_relax_block<T>(A, (T *)L[l].e, (const T *)L[l].r, o.bottom_max_iter,
                                   zero_init ? 1 : 0, s));
@@ -1684,8 +1698,8 @@ bool valid_options(const mlgpu_mg_options *o) {
     return false;
   if (o->relax_mode != MLGPU_RELAX_GSRB && o->relax_mode != MLGPU_RELAX_JACOBI) return false;
   if (o->bottom_max_iter < 0 || o->max_coarse < 1) return false;
-  // the BiCGStab bottom solver is not built: refused rather than replaced
-  if (o->bottom_solver != MLGPU_BOTTOM_RELAX) return false;
+  if (o->bottom_solver != MLGPU_BOTTOM_RELAX && o->bottom_solver != MLGPU_BOTTOM_BICGSTAB)
+    return false;
   if (o->prolong != MLGPU_PROLONG_CONSTANT && o->prolong != MLGPU_PROLONG_LINEAR) return false;
   if (o->precision != MLGPU_PREC_F64 && o->precision != MLGPU_PREC_MIXED) return false;
   if (o->norm_type < MLGPU_NORM_MAX || o->norm_type > MLGPU_NORM_L2) return false;
@@ -1774,7 +1788,8 @@ int mlgpu_vc_solver_create(const mlgpu_vcop *op, const mlgpu_mg_options *o, void
 
 int mlgpu_hc_solver_workspace(const mlgpu_nlop *op, const mlgpu_mg_options *o, size_t *bytes) {
   if (!op || !valid_grid(&op->grid) || !valid_options(o) || !bytes) return MLGPU_ERR_ARG;
-  if (!valid_nl_bcs(*op)) return MLGPU_ERR_ARG;
+  // the FAS bottom solve is relaxation (the reference's HC default)
+  if (!valid_nl_bcs(*op) || o->bottom_solver != MLGPU_BOTTOM_RELAX) return MLGPU_ERR_ARG;
   HCSolver S;
   S.op = *op;
   S.o = *o;
@@ -1786,6 +1801,7 @@ int mlgpu_hc_solver_workspace(const mlgpu_nlop *op, const mlgpu_mg_options *o, s
 int mlgpu_hc_solver_create(const mlgpu_nlop *op, const mlgpu_mg_options *o, void *ws,
                            size_t bytes, void *stream, mlgpu_solver **out) {
   if (!op || !valid_grid(&op->grid) || !valid_options(o) || !ws || !out) return MLGPU_ERR_ARG;
+  if (o->bottom_solver != MLGPU_BOTTOM_RELAX) return MLGPU_ERR_ARG;
   if (op->dtype != MLGPU_F64 || !valid_nl_bcs(*op)) return MLGPU_ERR_ARG;
   // mixed precision needs red/black smoothing (the linearised cycles)
   if (o->precision == MLGPU_PREC_MIXED && o->relax_mode != MLGPU_RELAX_GSRB) return MLGPU_ERR_ARG;
@@ -1885,6 +1901,7 @@ int mlgpu_hc_backward_euler(mlgpu_solver *S, double *phi_new, const double *phi_
 int mlgpu_hc_adjoint_workspace(const mlgpu_nlop *op, const mlgpu_mg_options *o,
                                size_t *bytes) {
   if (!valid_adjoint_op(op) || !valid_options(o) || !bytes) return MLGPU_ERR_ARG;
+  if (o->bottom_solver != MLGPU_BOTTOM_RELAX) return MLGPU_ERR_ARG;
   HCAdjSolver S;
   S.op = *op;
   S.o = *o;
@@ -1895,6 +1912,7 @@ int mlgpu_hc_adjoint_workspace(const mlgpu_nlop *op, const mlgpu_mg_options *o,
 int mlgpu_hc_adjoint_create(const mlgpu_nlop *op, const mlgpu_mg_options *o, void *ws,
                             size_t bytes, void *stream, mlgpu_solver **out) {
   if (!valid_adjoint_op(op) || !valid_options(o) || !ws || !out) return MLGPU_ERR_ARG;
+  if (o->bottom_solver != MLGPU_BOTTOM_RELAX) return MLGPU_ERR_ARG;
   if (((uintptr_t)ws) & 255) return MLGPU_ERR_WORKSPACE;
   HCAdjSolver *S = new HCAdjSolver;
   S->op = *op;

@@ -25,9 +25,9 @@ quirks kept:
   Neumann is always a zero gradient (PhysBCUtil.cpp:975-981);
 * solver settings: HCMultigrid.* and VelocityMultigrid.*
   (srcSubcycle/MushyLayerSubcycleUtils.cpp:654-692), projection.*
-  (srcSubcycle/Projector.cpp:44-64,388-443); the bottom solver is always
-  relaxation (a BiCGStab bottom, the projection's default there, is not
-  built);
+  (srcSubcycle/Projector.cpp:44-64,388-443); the projection and velocity
+  solves take the BiCGStab bottom as the reference does (relaxation when
+  projection.relax_bottom_solver is set), the (H, C) solve relaxation;
 * the grid: main.num_cells, main.domain_width / domain_length /
   domain_height (srcSubcycle/MushyLayerSubcycleUtils.cpp:115-140),
   main.periodic_bc.
@@ -408,8 +408,8 @@ class Inputs:
             ("num_smooth_down", "HCMultigrid.numSmoothDown", int),
             ("relax_mode", "HCMultigrid.relaxMode", int),
             ("bottom_max_iter", "HCMultigrid.bottomSolveIterations", int)])
-        # HCMultigrid.useRelaxBottomSolver = false asks for Chombo's BiCGStab
-        # bottom solver, which is not built: the relaxation bottom stays
+        # HCMultigrid.useRelaxBottomSolver = false would lend the FAS solve the
+        # velocity solves' BiCGStab; the FAS bottom here is always relaxation
         return o
 
     def projection_options(self):
@@ -423,6 +423,10 @@ class Inputs:
             ("bottom_max_iter", "projection.bottomSolveMaxIter", int),
             ("hang", "projection.solverHang", float),
             ("relax_mode", "projection.mg_relaxation", int)])
+        # BiCGStab unless projection.relax_bottom_solver (Projector.cpp:58,440,
+        # 2976-2986)
+        relax = self.get("projection.relax_bottom_solver", False, bool)
+        o.bottom_solver = abi.BOTTOM_RELAX if relax else abi.BOTTOM_BICGSTAB
         return o
 
     def velocity_options(self):
@@ -438,6 +442,10 @@ class Inputs:
             ("num_smooth_up", "VelocityMultigrid.num_smooth", int)],
             tolerance=1e-10, hang=1e-10, norm_thresh=1e-10, num_mg=1, max_iter=10,
             num_smooth_down=2, num_smooth_up=2)
+        # the velocity solves' bottom is BiCGStab (s_botSolverUStar,
+        # srcSubcycle/AMRLevelMushyLayerInit.cpp:738-739) at its default 80
+        # iterations
+        o.bottom_solver, o.bottom_max_iter = abi.BOTTOM_BICGSTAB, 80
         return o
 
 

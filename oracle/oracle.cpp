@@ -1198,6 +1198,11 @@ struct HCSolver {
   }
 };
 
+// BiCGStab bottom-solver settings (relative tolerance, restart threshold,
+// restarts); the device kernel uses the same ones
+constexpr double kBiCGEps = 1e-6, kBiCGHang = 1e-8;
+constexpr int kBiCGRestarts = 5;
+
 struct VCSolver {
   mlgpu_vcop op0;
   mlgpu_mg_options o;
@@ -1224,11 +1229,111 @@ struct VCSolver {
       updates += cells(l);
     }
   }
+  // Dot product in the device's fixed order: 32 lane sums (lane l takes the
+  // cells q = l mod 32 in increasing q), then a halving tree over the lanes.
+  static double lane_dot(const std::vector<double> &a, const std::vector<double> &b) {
+    double part[32] = {0.0};
+    for (size_t q = 0; q < a.size(); q++) part[q & 31] = part[q & 31] + a[q] * b[q];
+    for (int w = 16; w > 0; w >>= 1)
+      for (int l = 0; l < w; l++) part[l] = part[l] + part[l + w];
+    return part[0];
+  }
+  // the operator's preconditioner (DarcyBrinkmanOp::preCond,
+  // src/DarcyBrinkmanOp.cpp:89-121): x = lambda y, then two red/black sweeps
+  // of L x = y, homogeneous walls
+  void precond(const mlgpu_vcop &op, const std::vector<double> &lam, const std::vector<double> &y,
+               std::vector<double> &x) {
+    for (size_t q = 0; q < y.size(); q++) x[q] = y[q] * lam[q];
+    for (int s = 0; s < 2; s++) {
+      orc_vc_gsrb_pass(&op, x.data(), y.data(), 0);
+      orc_vc_gsrb_pass(&op, x.data(), y.data(), 1);
+    }
+  }
+  // BiCGStab bottom solve of L e = r (the reference's default bottom solver
+  // of the MAC projection and velocity solves, srcSubcycle/Projector.cpp:
+  // 3012-3020, 2976-2986; Chombo's BiCGStabSolver, absent from the tree).
+  // Restated from van der Vorst's right-preconditioned BiCGStab with the
+  // operator's preCond: relative tolerance 1e-6 of the initial residual (L2
+  // norm), at most bottom_max_iter iterations, a restart from the true
+  // residual when an iteration gains less than 1e-8 (at most 5), and an exit
+  // on breakdown (rho or <r~, v> zero).
+  void bicgstab(int l, double *e, const double *rhs) {
+    const mlgpu_vcop op = op_at(l);
+    const size_t n = cells(l);
+    std::vector<double> lam(n), r(n), rt(n), x(n, 0.0), p(n, 0.0), v(n, 0.0), ph(n), s(n),
+        sh(n), t(n), tmp(n);
+    orc_vc_lambda(&op, lam.data());
+    auto residual = [&]() {  // r = rhs - L(e), homogeneous
+      orc_vc_apply(&op, tmp.data(), e, 1);
+      for (size_t q = 0; q < n; q++) r[q] = rhs[q] - tmp[q];
+    };
+    residual();
+    rt = r;
+    const double norm0 = std::sqrt(lane_dot(r, r));
+    double norm = norm0, rho0 = 0.0, rho1 = 0.0, alpha = 0.0, omega = 0.0;
+    bool init = true;
+    int restarts = 0;
+    for (int it = 0; it < o.bottom_max_iter && norm > kBiCGEps * norm0 && restarts <= kBiCGRestarts;
+         it++) {
+      rho1 = rho0;
+      rho0 = lane_dot(rt, r);
+      if (rho0 == 0.0) break;
+      if (init) {
+        p = r;
+        init = false;
+      } else {
+        const double beta = (rho0 / rho1) * (alpha / omega);
+        for (size_t q = 0; q < n; q++) p[q] = r[q] + beta * (p[q] - omega * v[q]);
+      }
+      precond(op, lam, p, ph);
+      orc_vc_apply(&op, v.data(), ph.data(), 1);
+      const double m = lane_dot(rt, v);
+      if (m == 0.0) break;
+      alpha = rho0 / m;
+      for (size_t q = 0; q < n; q++) {
+        s[q] = r[q] - alpha * v[q];
+        x[q] = x[q] + alpha * ph[q];
+      }
+      const double snorm = std::sqrt(lane_dot(s, s));
+      if (snorm <= kBiCGEps * norm0) {
+        norm = snorm;
+        break;
+      }
+      precond(op, lam, s, sh);
+      orc_vc_apply(&op, t.data(), sh.data(), 1);
+      const double tt = lane_dot(t, t);
+      omega = tt > 0.0 ? lane_dot(t, s) / tt : 0.0;
+      for (size_t q = 0; q < n; q++) {
+        x[q] = x[q] + omega * sh[q];
+        r[q] = s[q] - omega * t[q];
+      }
+      const double prev = norm;
+      norm = std::sqrt(lane_dot(r, r));
+      if (omega == 0.0 || norm > (1.0 - kBiCGHang) * prev) {
+        // restart from the true residual of e + x
+        for (size_t q = 0; q < n; q++) {
+          e[q] = e[q] + x[q];
+          x[q] = 0.0;
+        }
+        residual();
+        rt = r;
+        norm = std::sqrt(lane_dot(r, r));
+        init = true;
+        restarts++;
+      }
+    }
+    for (size_t q = 0; q < n; q++) e[q] = e[q] + x[q];
+    // counted as the relaxation bottom is (bottom_max_iter updates per cell)
+    updates += (double)o.bottom_max_iter * n;
+  }
   // MultiGrid::cycle (homogeneous correction form)
   void cycle(int l, double *e, const double *r) {
     int last = (int)L.size() - 1;
     if (l == last) {
-      relax(l, e, r, o.bottom_max_iter);
+      if (o.bottom_solver == MLGPU_BOTTOM_BICGSTAB)
+        bicgstab(l, e, r);
+      else
+        relax(l, e, r, o.bottom_max_iter);
       return;
     }
     relax(l, e, r, o.num_smooth_down);

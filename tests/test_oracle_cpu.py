@@ -274,10 +274,18 @@ def test_argument_validation_without_gpu():
     assert nbytes.value > 64 * 64 * 8 * 3
     opts.relax_mode = 7
     assert lib.mlgpu_vc_solver_workspace(C.byref(op), C.byref(opts), C.byref(nbytes)) == abi.ERR_ARG
-    # a bottom solver that is not built is refused, not replaced
+    # BiCGStab bottom: the linear solver takes it (and its FP64 work arrays),
+    # the FAS solver refuses it (its bottom is relaxation); unknown ones refused
     lib.mlgpu_mg_default_options(C.byref(opts), 0)
     opts.bottom_solver = abi.BOTTOM_BICGSTAB
-    assert lib.mlgpu_vc_solver_workspace(C.byref(op), C.byref(opts), C.byref(nbytes)) == abi.ERR_ARG
+    nb2 = C.c_size_t()
+    assert lib.mlgpu_vc_solver_workspace(C.byref(op), C.byref(opts), C.byref(nb2)) == 0
+    assert nb2.value > nbytes.value
+    hop = abi.NLOp()
+    hop.grid = abi.make_grid([64, 64])
+    assert lib.mlgpu_hc_solver_workspace(C.byref(hop), C.byref(opts), C.byref(nb2)) == abi.ERR_ARG
+    opts.bottom_solver = 2
+    assert lib.mlgpu_vc_solver_workspace(C.byref(op), C.byref(opts), C.byref(nb2)) == abi.ERR_ARG
 
 
 # ------------------------------------------- nonlinear temperature conditions
