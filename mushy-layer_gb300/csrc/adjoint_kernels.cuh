@@ -334,10 +334,12 @@ __global__ void __launch_bounds__(kBlock) porosity_jac_kernel(Geom G, ClosurePar
 }
 #endif
 
-// the inverse of every cell's diagonal block M of A^T: {M3, -M1, -M2, M0}/det
+// the inverse of every cell's diagonal block M of A^T: {M3, -M1, -M2, M0}/det;
+// with Dout also A's own block D = M^T (the lean FP32 cycles' residual)
 template <class T, int DIM>
 __global__ void __launch_bounds__(kBlock) adj_minv_kernel(AdjArgs<T> A, const T *__restrict__ zero,
-                                                          T *__restrict__ Minv) {
+                                                          T *__restrict__ Minv,
+                                                          T *__restrict__ Dout) {
   const Geom &G = A.G;
   const long long n = G.ncell;
   for (long long q = gtid(); q < n; q += gstride()) {
@@ -350,6 +352,12 @@ __global__ void __launch_bounds__(kBlock) adj_minv_kernel(AdjArgs<T> A, const T 
     Minv[q + n] = -M[1] / det;
     Minv[q + 2 * n] = -M[2] / det;
     Minv[q + 3 * n] = M[0] / det;
+    if (Dout) {
+      Dout[q] = M[0];
+      Dout[q + n] = M[2];
+      Dout[q + 2 * n] = M[1];
+      Dout[q + 3 * n] = M[3];
+    }
   }
 }
 

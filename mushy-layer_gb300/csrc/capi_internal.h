@@ -14,6 +14,7 @@
 #include "hcm_kernels.cuh"
 #include "adjoint_kernels.cuh"
 #include "bicgstab_kernels.cuh"
+#include "lin_lean_kernels.cuh"
 
 namespace mlgpu {
 
@@ -94,8 +95,16 @@ cudaError_t launch_adj_gsrb(const AdjArgs<float> &A, float *y, const float *g, i
                             cudaStream_t s, bool tr);
 cudaError_t launch_adj_relax_block(const AdjArgs<float> &A, float *y, const float *g, int sweeps,
                                    int zero, cudaStream_t s, bool tr);
-cudaError_t launch_adj_minv(const AdjArgs<float> &A, const float *zero, float *Minv,
+cudaError_t launch_adj_minv(const AdjArgs<float> &A, const float *zero, float *Minv, float *D,
                             cudaStream_t s);
+// lean FP32 cycles of the Newton step (lin_lean_kernels.cuh)
+cudaError_t launch_lean_gsrb(const LinLean &P, int pass, cudaStream_t s);
+cudaError_t launch_lean_residual(const LinLean &P, int norm, float *out, double *part,
+                                 int *nparts, cudaStream_t s);
+cudaError_t launch_lean_restrict(const LinLean &P, const Geom &C, float *gc, float *xc, float *wc,
+                                 cudaStream_t s);
+cudaError_t launch_lean_prolong(const LinLean &P, const Geom &C, int kind, const float *xc,
+                                cudaStream_t s);
 cudaError_t launch_adj_bottom_direct(const AdjArgs<float> &A, float *y, const float *g,
                                      cudaStream_t s, bool tr);
 cudaError_t launch_adj_restrict(const AdjArgs<float> &A, const Geom &C, const float *y,

@@ -8,6 +8,7 @@
 #define MLGPU_ADJ_F32_UNIT 1
 #include "launch_impl.cuh"
 #include "adjoint_kernels.cuh"
+#include "lin_lean_kernels.cuh"
 
 namespace mlgpu {
 
@@ -56,9 +57,9 @@ cudaError_t launch_adj_relax_block(const AdjArgs<float> &A, float *y, const floa
   return cudaGetLastError();
 }
 
-cudaError_t launch_adj_minv(const AdjArgs<float> &A, const float *zero, float *Minv,
+cudaError_t launch_adj_minv(const AdjArgs<float> &A, const float *zero, float *Minv, float *D,
                             cudaStream_t s) {
-  MLGPU_DIM_SWITCH(A.G.dim, (adj_minv_kernel<float, DIM><<<blocks_for(A.G.ncell), kBlock, 0, s>>>(A, zero, Minv)));
+  MLGPU_DIM_SWITCH(A.G.dim, (adj_minv_kernel<float, DIM><<<blocks_for(A.G.ncell), kBlock, 0, s>>>(A, zero, Minv, D)));
   return cudaGetLastError();
 }
 
@@ -72,6 +73,39 @@ cudaError_t launch_adj_bottom_direct(const AdjArgs<float> &A, float *y, const fl
 cudaError_t launch_adj_restrict(const AdjArgs<float> &A, const Geom &C, const float *y,
                                 const float *g, float *gc, cudaStream_t s, bool tr) {
   MLGPU_TR_SWITCH32(tr, MLGPU_DIM_SWITCH(A.G.dim, (adj_restrict_kernel<float, DIM, TR><<<blocks_for(C.ncell), kBlock, 0, s>>>(A, C, y, g, gc))));
+  return cudaGetLastError();
+}
+
+// ---- lean cycles of the Newton step (lin_lean_kernels.cuh)
+cudaError_t launch_lean_gsrb(const LinLean &P, int pass, cudaStream_t s) {
+  MLGPU_DIM_SWITCH(P.G.dim, (lean_gsrb_kernel<DIM><<<blocks_for(colour_threads(P.G)), kBlock, 0, s>>>(P, pass)));
+  return cudaGetLastError();
+}
+
+cudaError_t launch_lean_residual(const LinLean &P, int norm, float *out, double *part,
+                                 int *nparts, cudaStream_t s) {
+  const int nb = blocks_for(P.G.ncell);
+  if (nparts) *nparts = nb;
+  if (norm < 0) norm = MLGPU_NORM_MAX;
+  MLGPU_DIM_SWITCH(P.G.dim, MLGPU_NORM_SWITCH(norm, {
+    if (NORM >= 0) lean_residual_kernel<DIM, (NORM < 0 ? 0 : NORM)><<<nb, kBlock, 0, s>>>(P, out, part);
+  }));
+  return cudaGetLastError();
+}
+
+cudaError_t launch_lean_restrict(const LinLean &P, const Geom &C, float *gc, float *xc, float *wc,
+                                 cudaStream_t s) {
+  MLGPU_DIM_SWITCH(P.G.dim, (lean_restrict_kernel<DIM><<<blocks_for(C.ncell), kBlock, 0, s>>>(P, C, gc, xc, wc)));
+  return cudaGetLastError();
+}
+
+cudaError_t launch_lean_prolong(const LinLean &P, const Geom &C, int kind, const float *xc,
+                                cudaStream_t s) {
+  if (kind == MLGPU_PROLONG_LINEAR) {
+    MLGPU_DIM_SWITCH(P.G.dim, (lean_prolong_kernel<DIM, MLGPU_PROLONG_LINEAR><<<blocks_for(P.G.ncell), kBlock, 0, s>>>(P, C, xc)));
+  } else {
+    MLGPU_DIM_SWITCH(P.G.dim, (lean_prolong_kernel<DIM, MLGPU_PROLONG_CONSTANT><<<blocks_for(P.G.ncell), kBlock, 0, s>>>(P, C, xc)));
+  }
   return cudaGetLastError();
 }
 

@@ -1,0 +1,207 @@
+// lin_lean_kernels.cuh -- lean FP32 kernels of the linear cycles inside the
+// mixed-precision Newton solve of the (H, C) system, A x = g with A the
+// Jacobian of the nonlinear operator at the current state:
+//   (A x)_c = alpha a_c x_c - beta dxinv sum_f b_f,c (w_nb,c - w_c),  w = J x,
+// J = d(T, C_l)/d(H, C) per cell.  Every wall ghost of w depends on the cell
+// itself (the derived-variable rule on the centre's w, or the (H, C)
+// condition mapped through the ghost state's Jacobian), so it lives in the
+// cell's 2x2 diagonal block D, which the state set-up stores together with
+// K = (D^T)^-1 (adj_minv_kernel, from the same device functions as the FP64
+// operator).  What couples cells is then only
+//   (A x)_j = D_j x_j - beta dxinv sum_(interior faces) b_f w_nb,
+// interior meaning inside the box or across a periodic seam.  The kernels
+// keep w = J x of every cell next to x, so a red/black update reads its own
+// g, K and J, the neighbours' w and the face coefficients:
+//   x_j = K_j^T (g_j + beta dxinv sum b_f w_nb),   w_j = J_j x_j,
+// about half the loads and a fraction of the arithmetic of the generic
+// linearised kernel (which forms J_nb x_nb for every neighbour), and the same
+// update in exact arithmetic.  Residual (with a fused norm), restriction of
+// the residual fused with the zeroing of the coarse unknowns, and
+// prolongation fused with the refresh of w complete the cycle; the bottom
+// solve is the generic one (its w is never read).  FP32 inside the FP64
+// Newton loop: its residual, norm and update stay FP64.
+#pragma once
+#include "adjoint_kernels.cuh"
+
+namespace mlgpu {
+
+struct LinLean {
+  Geom G;
+  BCD ybc;           // wall rule of the prolongation
+  float bdx;         // beta / dx^2
+  const float *b[3]; // [2][faces_d] face coefficients
+  const float *J;    // [4][cells] closure Jacobian (row-major 2x2 per cell)
+  const float *K;    // [4][cells] (D^T)^-1
+  const float *D;    // [4][cells] diagonal block of A (row-major)
+  float *x, *w;      // [2][cells]: unknown and J x
+  const float *g;    // [2][cells]: right-hand side
+};
+
+#ifdef MLGPU_ADJ_F32_UNIT
+// s_c = sum over the interior faces of b_f,c w_nb,c (periodic seams wrap;
+// a one-cell periodic direction couples the cell to itself and adds nothing)
+template <int DIM>
+__device__ __forceinline__ void lean_nbsum(const LinLean &P, int i, int j, int k, long long q,
+                                           float s[2]) {
+  const Geom &G = P.G;
+  const long long n = G.ncell;
+  const float *w = P.w;
+  float s0 = 0.f, s1 = 0.f;
+  {
+    const long long f = ((long long)k * G.n1 + j) * (G.n0 + 1) + i;
+    const long long nf = (long long)(G.n0 + 1) * G.n1 * G.n2;
+    const long long ql = i > 0 ? q - 1 : (G.per0 && G.n0 > 1 ? q + (G.n0 - 1) : -1);
+    const long long qh = i < G.n0 - 1 ? q + 1 : (G.per0 && G.n0 > 1 ? q - (G.n0 - 1) : -1);
+    if (ql >= 0) {
+      s0 = fmaf(P.b[0][f], w[ql], s0);
+      s1 = fmaf(P.b[0][nf + f], w[n + ql], s1);
+    }
+    if (qh >= 0) {
+      s0 = fmaf(P.b[0][f + 1], w[qh], s0);
+      s1 = fmaf(P.b[0][nf + f + 1], w[n + qh], s1);
+    }
+  }
+  {
+    const long long s = G.n0;
+    const long long f = ((long long)k * (G.n1 + 1) + j) * G.n0 + i;
+    const long long nf = (long long)G.n0 * (G.n1 + 1) * G.n2;
+    const long long ql = j > 0 ? q - s : (G.per1 && G.n1 > 1 ? q + (G.n1 - 1) * s : -1);
+    const long long qh = j < G.n1 - 1 ? q + s : (G.per1 && G.n1 > 1 ? q - (G.n1 - 1) * s : -1);
+    if (ql >= 0) {
+      s0 = fmaf(P.b[1][f], w[ql], s0);
+      s1 = fmaf(P.b[1][nf + f], w[n + ql], s1);
+    }
+    if (qh >= 0) {
+      s0 = fmaf(P.b[1][f + s], w[qh], s0);
+      s1 = fmaf(P.b[1][nf + f + s], w[n + qh], s1);
+    }
+  }
+  if (DIM == 3) {
+    const long long s = (long long)G.n0 * G.n1;
+    const long long f = q;
+    const long long nf = s * (G.n2 + 1);
+    const long long ql = k > 0 ? q - s : (G.per2 && G.n2 > 1 ? q + (G.n2 - 1) * s : -1);
+    const long long qh = k < G.n2 - 1 ? q + s : (G.per2 && G.n2 > 1 ? q - (G.n2 - 1) * s : -1);
+    if (ql >= 0) {
+      s0 = fmaf(P.b[2][f], w[ql], s0);
+      s1 = fmaf(P.b[2][nf + f], w[n + ql], s1);
+    }
+    if (qh >= 0) {
+      s0 = fmaf(P.b[2][f + s], w[qh], s0);
+      s1 = fmaf(P.b[2][nf + f + s], w[n + qh], s1);
+    }
+  }
+  s[0] = s0;
+  s[1] = s1;
+}
+
+// red/black half sweep: x_j = K^T (g + bdx s), w_j = J x_j on the cells of
+// colour `pass`
+template <int DIM>
+__global__ void __launch_bounds__(kBlock) lean_gsrb_kernel(LinLean P, int pass) {
+  const Geom &G = P.G;
+  const long long nt = colour_threads(G), n = G.ncell;
+  for (long long t = gtid(); t < nt; t += gstride()) {
+    int i, j, k;
+    if (!colour_cell(G, pass, t, i, j, k)) continue;
+    const long long q = G.cell(i, j, k);
+    float s[2];
+    lean_nbsum<DIM>(P, i, j, k, q, s);
+    const float r0 = fmaf(P.bdx, s[0], P.g[q]), r1 = fmaf(P.bdx, s[1], P.g[n + q]);
+    const float x0 = fmaf(P.K[q], r0, P.K[2 * n + q] * r1);
+    const float x1 = fmaf(P.K[n + q], r0, P.K[3 * n + q] * r1);
+    P.x[q] = x0;
+    P.x[n + q] = x1;
+    P.w[q] = fmaf(P.J[q], x0, P.J[n + q] * x1);
+    P.w[n + q] = fmaf(P.J[2 * n + q], x0, P.J[3 * n + q] * x1);
+  }
+}
+
+// g - A x at cell q (both components)
+template <int DIM>
+__device__ __forceinline__ void lean_res(const LinLean &P, int i, int j, int k, long long q,
+                                         float r[2]) {
+  const long long n = P.G.ncell;
+  float s[2];
+  lean_nbsum<DIM>(P, i, j, k, q, s);
+  const float x0 = P.x[q], x1 = P.x[n + q];
+  const float ax0 = fmaf(P.D[q], x0, P.D[n + q] * x1);
+  const float ax1 = fmaf(P.D[2 * n + q], x0, P.D[3 * n + q] * x1);
+  r[0] = fmaf(P.bdx, s[0], P.g[q]) - ax0;
+  r[1] = fmaf(P.bdx, s[1], P.g[n + q]) - ax1;
+}
+
+// out = g - A x with a fused norm of both components (partials per block)
+template <int DIM, int NORM>
+__global__ void __launch_bounds__(kBlock) lean_residual_kernel(LinLean P, float *out,
+                                                               double *part) {
+  const Geom &G = P.G;
+  const long long n = G.ncell;
+  double acc = 0.0;
+  for (long long q = gtid(); q < n; q += gstride()) {
+    int i, j, k;
+    cell_ijk(G, q, i, j, k);
+    float r[2];
+    lean_res<DIM>(P, i, j, k, q, r);
+    if (out) {
+      out[q] = r[0];
+      out[n + q] = r[1];
+    }
+    acc = norm_accum<NORM>(acc, (double)r[0]);
+    acc = norm_accum<NORM>(acc, (double)r[1]);
+  }
+  const double v = block_reduce<NORM>(acc);
+  if (threadIdx.x == 0) part[blockIdx.x] = v;
+}
+
+// coarse g = 2^D average of the fine residual; the coarse x and w start at 0
+template <int DIM>
+__global__ void __launch_bounds__(kBlock) lean_restrict_kernel(LinLean P, Geom C, float *gc,
+                                                               float *xc, float *wc) {
+  const long long nc = C.ncell;
+  const float wgt = DIM == 3 ? 0.125f : 0.25f;
+  for (long long Q = gtid(); Q < nc; Q += gstride()) {
+    int I, J, K;
+    cell_ijk(C, Q, I, J, K);
+    float a0 = 0.f, a1 = 0.f;
+#pragma unroll
+    for (int kk = 0; kk < (DIM == 3 ? 2 : 1); kk++)
+#pragma unroll
+      for (int jj = 0; jj < 2; jj++)
+#pragma unroll
+        for (int ii = 0; ii < 2; ii++) {
+          const int i = 2 * I + ii, j = 2 * J + jj, k = DIM == 3 ? 2 * K + kk : 0;
+          float r[2];
+          lean_res<DIM>(P, i, j, k, P.G.cell(i, j, k), r);
+          a0 += r[0];
+          a1 += r[1];
+        }
+    gc[Q] = a0 * wgt;
+    gc[nc + Q] = a1 * wgt;
+    xc[Q] = 0.f;
+    xc[nc + Q] = 0.f;
+    wc[Q] = 0.f;
+    wc[nc + Q] = 0.f;
+  }
+}
+
+// x += prolongation of the coarse correction; w = J x
+template <int DIM, int KIND>
+__global__ void __launch_bounds__(kBlock) lean_prolong_kernel(LinLean P, Geom C,
+                                                              const float *__restrict__ xc) {
+  const Geom &G = P.G;
+  const long long n = G.ncell;
+  for (long long q = gtid(); q < n; q += gstride()) {
+    int i, j, k;
+    cell_ijk(G, q, i, j, k);
+    const float x0 = prolong_add<float, DIM, KIND>(C, P.ybc, 0, i, j, k, P.x[q], xc, nullptr);
+    const float x1 = prolong_add<float, DIM, KIND>(C, P.ybc, 1, i, j, k, P.x[n + q], xc, nullptr);
+    P.x[q] = x0;
+    P.x[n + q] = x1;
+    P.w[q] = fmaf(P.J[q], x0, P.J[n + q] * x1);
+    P.w[n + q] = fmaf(P.J[2 * n + q], x0, P.J[3 * n + q] * x1);
+  }
+}
+#endif  // MLGPU_ADJ_F32_UNIT
+
+}  // namespace mlgpu

@@ -1205,6 +1205,7 @@ struct AdjLevel {
   // closure derivative), the inverse diagonal blocks and the cycle's fields
   Coefs<float> c32;
   float *J32 = nullptr, *Minv32 = nullptr, *y32 = nullptr, *g32 = nullptr, *r32 = nullptr;
+  float *D32 = nullptr, *w32 = nullptr;  // diagonal blocks of A, and w = J y (lean cycles)
 };
 
 class HCAdjSolver : public mlgpu_solver {
@@ -1270,7 +1271,9 @@ class HCAdjSolver : public mlgpu_solver {
         for (int d = 0; d < g.dim; d++) L[l].c32.b[d] = A.get<float>(2 * nfaces(g, d));
         L[l].J32 = A.get<float>(2 * n);
         L[l].Minv32 = A.get<float>(2 * n);
+        L[l].D32 = A.get<float>(2 * n);
         L[l].y32 = A.get<float>(n);
+        L[l].w32 = A.get<float>(n);
         L[l].g32 = A.get<float>(n);
         L[l].r32 = A.get<float>(n);
       }
@@ -1339,6 +1342,23 @@ class HCAdjSolver : public mlgpu_solver {
     return A;
   }
 
+  // lean FP32 operator of level l (lin_lean_kernels.cuh)
+  LinLean lean(int l) {
+    const AdjArgs<double> D = args(l);
+    LinLean P;
+    P.G = D.G;
+    P.ybc = ybc();
+    P.bdx = (float)(D.beta * D.dxinv);
+    for (int d = 0; d < 3; d++) P.b[d] = L[l].c32.b[d];
+    P.J = L[l].J32;
+    P.K = L[l].Minv32;
+    P.D = L[l].D32;
+    P.x = L[l].y32;
+    P.w = L[l].w32;
+    P.g = L[l].g32;
+    return P;
+  }
+
   // the wall rule of the adjoint variable in the prolongation
   BCD ybc() const { return make_bcd(op.apply_derived_bc ? op.derived_bc : op.phi_bc); }
 
@@ -1358,7 +1378,7 @@ class HCAdjSolver : public mlgpu_solver {
       for (auto &lv : L) CK(launch_adj_jac(lv.G, cp, lv.u, lv.J32, s));
       for (size_t l = 0; l < L.size(); l++) {
         CK(cudaMemsetAsync(L[l].r32, 0, sizeof(float) * 2 * L[l].G.ncell, s));
-        CK(launch_adj_minv(args32((int)l), L[l].r32, L[l].Minv32, s));
+        CK(launch_adj_minv(args32((int)l), L[l].r32, L[l].Minv32, L[l].D32, s));
       }
       return MLGPU_OK;
     }
@@ -1412,17 +1432,20 @@ class HCAdjSolver : public mlgpu_solver {
 
   // ---- FP32 cycles on A (mixed-precision Newton); same structure as the
   // FP64 ones above
+  // The lean cycles keep w = J y next to y on every level: zero together,
+  // refreshed by every update and by the prolongation
   int smooth32(int l, int n) {
-    AdjArgs<float> A = args32(l);
+    const LinLean P = lean(l);
     for (int i = 0; i < n; i++)
-      for (int pass = 0; pass < 2; pass++) CK(launch_adj_gsrb(A, L[l].y32, L[l].g32, pass, s, false));
+      for (int pass = 0; pass < 2; pass++) CK(launch_lean_gsrb(P, pass, s));
     return MLGPU_OK;
   }
 
   int cycle32(int l) {
     const int last = (int)L.size() - 1;
-    AdjArgs<float> A = args32(l);
     if (l == last) {
+      // the bottom solve updates y alone: its w is never read
+      AdjArgs<float> A = args32(l);
       if (2 * L[l].G.ncell <= kAdjDirectMax)
         CK(launch_adj_bottom_direct(A, L[l].y32, L[l].g32, s, false));
       else
@@ -1430,23 +1453,27 @@ class HCAdjSolver : public mlgpu_solver {
                                   false));
       return MLGPU_OK;
     }
-    if (l > 0) CK(cudaMemsetAsync(L[l].y32, 0, sizeof(float) * 2 * L[l].G.ncell, s));
+    // a coarse level's y and w were zeroed by the restriction that fed it
     int rc = smooth32(l, o.num_smooth_down);
     if (rc) return rc;
-    CK(launch_adj_restrict(A, L[l + 1].G, L[l].y32, L[l].g32, L[l + 1].g32, s, false));
+    const LinLean P = lean(l);
+    CK(launch_lean_restrict(P, L[l + 1].G, L[l + 1].g32, L[l + 1].y32, L[l + 1].w32, s));
     for (int m = 0; m < o.num_mg; m++) {
+      if (m > 0) {  // every coarse visit starts from zero
+        CK(cudaMemsetAsync(L[l + 1].y32, 0, sizeof(float) * 2 * L[l + 1].G.ncell, s));
+        CK(cudaMemsetAsync(L[l + 1].w32, 0, sizeof(float) * 2 * L[l + 1].G.ncell, s));
+      }
       rc = cycle32(l + 1);
       if (rc) return rc;
     }
-    CK(launch_prolong<float>(L[l].G, ybc(), 2, o.prolong, L[l].y32, L[l + 1].y32, nullptr, s));
+    CK(launch_lean_prolong(P, L[l + 1].G, o.prolong, L[l + 1].y32, s));
     return smooth32(l, o.num_smooth_up);
   }
 
   // FP32 linear residual g - A y of level 0 with its norm (accumulated in FP64)
   int residual_norm32() {
     int nparts = 0;
-    CK(launch_adj_op(args32(0), ADJ_RESIDUAL, o.norm_type, L[0].y32, L[0].g32, L[0].r32, part,
-                     &nparts, s, false));
+    CK(launch_lean_residual(lean(0), o.norm_type, L[0].r32, part, &nparts, s));
     CK(launch_finalize_norm(o.norm_type, part, nparts, part + kMaxBlocks, s));
     CK(cudaMemcpyAsync(host_norm, part + kMaxBlocks, sizeof(double), cudaMemcpyDeviceToHost, s));
     return MLGPU_OK;
@@ -1549,6 +1576,7 @@ class HCAdjSolver : public mlgpu_solver {
       if (mixed) {
         CK(launch_convert<float, double>(n2, L[0].g32, L[0].g, s));
         CK(cudaMemsetAsync(L[0].y32, 0, sizeof(float) * n2, s));
+        CK(cudaMemsetAsync(L[0].w32, 0, sizeof(float) * n2, s));
         rc = residual_norm32();
       } else {
         CK(cudaMemsetAsync(L[0].y, 0, bytes, s));
