@@ -118,10 +118,10 @@ def c4_problem(torch, abi, ops, n=C4_N, seed=C4_SEED):
 class C4Runner:
     """The two solves of one step, FP64 or mixed; solvers built once."""
 
-    def __init__(self, torch, abi, ops, prob, use_graph=None):
+    def __init__(self, torch, abi, ops, prob, use_graph=None, precs=("mixed", "fp64")):
         self.torch, self.abi, self.ops, self.P = torch, abi, ops, prob
         self.S = {}
-        for prec in ("mixed", "fp64"):
+        for prec in precs:
             code = abi.PREC_MIXED if prec == "mixed" else abi.PREC_F64
             po = ops.default_options(False)
             po.tolerance, po.hang, po.max_iter, po.precision = TOL, 1e-15, 300, code
@@ -144,6 +144,9 @@ class C4Runner:
         u.copy_(phi0)
         sth, rch = HS.backwardEulerNewton(u, phi0, C4_DT)
         return (stp, rcp), (sth, rch)
+
+    def cells(self):
+        return self.P["n"] ** 3
 
     @staticmethod
     def summary(out):
@@ -409,8 +412,47 @@ def run_reference(args):
                 "d2h_bytes_per_step": 0}}))
 
 
-def dominant_kernel_roofline(torch, abi, ops, R):
+# Compulsory bytes of one FP32 red/black half sweep of the Newton step's
+# linear cycles (lin_lean_kernels.cuh lean_gsrb_kernel), per cell of the box:
+# the updated half of the cells read g (2 floats), K (4) and J (4) and write
+# x (2) and w (2); every face coefficient is read once (3 directions x 2
+# components); the other half's w is read once (2 floats each).
+# (5 + 6 + 1 + 2) floats = 56 B.
+LEAN_SWEEP_BYTES_PER_CELL = 56
+LEAN_SWEEP_PROFILE = os.path.join(PROFILES, "lean_gsrb_kernel_256cubed.md")
+
+
+def profiled_traffic(path, key):
+    """DRAM bytes per launch recorded in a committed ncu summary (a line
+    `key: <bytes>`), or None."""
+    try:
+        for ln in open(path):
+            if ln.strip().startswith(key + ":"):
+                return float(ln.split(":", 1)[1].split()[0])
+    except OSError:
+        pass
     return None
+
+
+def dominant_kernel_roofline(torch, abi, ops, R):
+    """The mixed step's dominant kernel (the FP32 red/black half sweep of the
+    Newton cycles on the 256^3 level, 26% of the step in the ncu launch list)
+    timed with CUDA events on the solver's stream at the state of the last
+    timed step; achieved = its compulsory bytes / its time."""
+    HS = R.S["mixed"][1]
+    ms = C.c_double()
+    abi.check(abi.load().mlgpu_hc_newton_sweep_time(HS.h, 40, C.byref(ms)), "sweep time")
+    ncell = R.cells()
+    alg = LEAN_SWEEP_BYTES_PER_CELL * ncell
+    achieved = alg / (ms.value * 1e-3) / 1e9
+    hbm, kind = peaks()
+    return {"bound": "hbm", "kernel": "lean_gsrb_kernel<3> (FP32 red/black half sweep, "
+                                       "Newton linear cycles, 256^3 level)",
+            "achieved": achieved, "peak": hbm, "peak_kind": kind, "unit": "GB/s",
+            "frac": achieved / hbm,
+            "traffic": profiled_traffic(LEAN_SWEEP_PROFILE, "dram_bytes_per_launch_256cubed"),
+            "alg_bytes_per_launch": alg, "launch_us": ms.value * 1e3,
+            "timing": "CUDA events on the solver stream, 40 launches after the timed region"}
 
 
 
@@ -959,11 +1001,12 @@ def run_profile(args):
                           "adjoint_cycles": st_a.iterations}))
         return
     if args.profile in ("c4", "c4-fp64"):
-        # one step of the 256^3 workload with plain launches (profilers do
-        # not see kernel nodes inside graphs with conditional nodes)
-        prob = c4_problem(torch, abi, ops)
-        R = C4Runner(torch, abi, ops, prob, use_graph=0)
+        # one step of the 256^3 workload (or --n^3) with plain launches
+        # (profilers do not see kernel nodes inside graphs with conditional
+        # nodes)
+        prob = c4_problem(torch, abi, ops, n=args.n)
         prec = "mixed" if args.profile == "c4" else "fp64"
+        R = C4Runner(torch, abi, ops, prob, use_graph=0, precs=(prec,))
         for _ in range(1 + args.warmup):
             out = R.step(prec)
         torch.cuda.synchronize()
@@ -993,6 +1036,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--n", type=int, default=C4_N,
+                    help="box edge of the --profile c4 runs (ncu captures of a smaller case)")
     ap.add_argument("--profile", choices=["c4", "c4-fp64", "c2-mixed", "c2-fp64", "hc", "adjoint"],
                     help="run one short solve for a profiler and exit")
     ap.add_argument("--config", type=int, choices=[1, 2, 3, 5],

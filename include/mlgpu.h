@@ -470,9 +470,18 @@ int mlgpu_hc_adjoint_solve(mlgpu_solver *S, const double *phi, const double *g, 
  * consecutive steps that cut it by under 5% once it is below 1e-8 of its
  * start end the solve with the hang status (its round-off floor).  phi:
  * initial guess in, solution out.  No counterpart in the reference (whose
- * FAS smoother ignores dT/dH and converges slowly through phase change). */
+ * FAS smoother ignores dT/dH and converges slowly through phase change).
+ * With options.precision == MLGPU_PREC_MIXED the V-cycles of each step run
+ * in FP32 (J from the FP64 closure derivative, stored FP32; w = J d kept per
+ * cell, wall ghosts folded into the stored diagonal blocks); the residual,
+ * its norms, the step and the closure stay FP64. */
 int mlgpu_hc_newton_solve(mlgpu_solver *S, double *phi, const double *rhs,
                           mlgpu_solve_stats *stats);
+/* Measurement: device time (ms per launch, host double) of `reps` FP32
+ * red/black half sweeps on the finest level of a mixed-precision Newton
+ * solver, at the state of its last step, timed with CUDA events on the
+ * solver's stream.  No counterpart in the reference. */
+int mlgpu_hc_newton_sweep_time(mlgpu_solver *S, int reps, double *ms_per_launch);
 /* mlgpu_hc_backward_euler with the Newton solve of `S` (an adjoint solver). */
 int mlgpu_hc_backward_euler_newton(mlgpu_solver *S, double *phi_new, const double *phi_old,
                                    const double *src, const double *aCoef, double dt,

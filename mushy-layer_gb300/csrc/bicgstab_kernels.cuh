@@ -91,11 +91,16 @@ __device__ __forceinline__ void bicg_precond(const VCArgs<double> &A, double *x,
     }
 }
 
-// L e = rhs on one (coarsest) level; e in/out, ws: kBiCGArrays * ncell doubles
+// L e = rhs on one (coarsest) level; e in/out, ws: kBiCGArrays * ncell doubles.
+// remove_mean: the operator is singular (no alpha, no c, no Dirichlet wall:
+// constants are its null space) and the right-hand side came through FP32,
+// whose rounding leaves it a small mean that no correction can remove;
+// subtract that mean first (the mixed-precision cycles only).
 template <class S, int DIM>
 __global__ void __launch_bounds__(kBiCGThreads) vc_bicgstab_kernel(VCArgs<double> A, S *e_io,
                                                                    const S *rhs_in,
-                                                                   double *ws, int imax) {
+                                                                   double *ws, int imax,
+                                                                   int remove_mean) {
   __shared__ double slot;
   const long long n = A.G.ncell;
   double *e = ws, *f = ws + n, *r = ws + 2 * n, *rt = ws + 3 * n, *x = ws + 4 * n,
@@ -107,8 +112,14 @@ __global__ void __launch_bounds__(kBiCGThreads) vc_bicgstab_kernel(VCArgs<double
     x[q] = 0.0;
     p[q] = 0.0;
     v[q] = 0.0;
+    t[q] = 1.0;
   }
   __syncthreads();
+  if (remove_mean) {
+    const double mean = bicg_dot(f, t, n, &slot) / (double)n;
+    for (long long q = threadIdx.x; q < n; q += blockDim.x) f[q] = f[q] - mean;
+    __syncthreads();
+  }
   // r = rhs - L(e), r~ = r
   bicg_apply<DIM>(A, t, e);
   for (long long q = threadIdx.x; q < n; q += blockDim.x) {

@@ -82,7 +82,7 @@ cudaError_t launch_hcm_update(long long n, double *u, const float *e, cudaStream
 // BiCGStab bottom solve of L e = rhs on one level (FP64 arithmetic, storage S)
 template <class S>
 cudaError_t launch_vc_bicgstab(const VCArgs<double> &A, S *e, const S *rhs, double *ws,
-                               int imax, cudaStream_t s);
+                               int imax, int remove_mean, cudaStream_t s);
 cudaError_t launch_newton_step(long long n, double *u, const double *u_old, double scale,
                                const float *e, cudaStream_t s);
 // FP32 Jacobian cycles of the mixed-precision Newton solve (launch_f32_adj.cu)

@@ -11,14 +11,14 @@ namespace mlgpu {
 
 template <class S>
 cudaError_t launch_vc_bicgstab(const VCArgs<double> &A, S *e, const S *rhs, double *ws,
-                               int imax, cudaStream_t s) {
-  MLGPU_DIM_SWITCH(A.G.dim, (vc_bicgstab_kernel<S, DIM><<<1, kBiCGThreads, 0, s>>>(A, e, rhs, ws, imax)));
+                               int imax, int remove_mean, cudaStream_t s) {
+  MLGPU_DIM_SWITCH(A.G.dim, (vc_bicgstab_kernel<S, DIM><<<1, kBiCGThreads, 0, s>>>(A, e, rhs, ws, imax, remove_mean)));
   return cudaGetLastError();
 }
 template cudaError_t launch_vc_bicgstab<double>(const VCArgs<double> &, double *, const double *,
-                                                double *, int, cudaStream_t);
+                                                double *, int, int, cudaStream_t);
 template cudaError_t launch_vc_bicgstab<float>(const VCArgs<double> &, float *, const float *,
-                                               double *, int, cudaStream_t);
+                                               double *, int, int, cudaStream_t);
 
 template cudaError_t launch_nl_op<double>(const NLArgs<double> &, int, int, const double *,
                                           const double *, double *, double *, double *, int *,

@@ -131,13 +131,28 @@ __device__ __forceinline__ void lean_res(const LinLean &P, int i, int j, int k, 
   r[1] = fmaf(P.bdx, s[1], P.g[n + q]) - ax1;
 }
 
-// out = g - A x with a fused norm of both components (partials per block)
+// FP32 norm accumulation of one value (max keeps NaN, as norm_accum)
+template <int NORM>
+__device__ __forceinline__ float lean_accum(float acc, float v) {
+  if (NORM == MLGPU_NORM_MAX) {
+    const float a = fabsf(v);
+    return (a > acc || a != a) ? a : acc;
+  }
+  if (NORM == MLGPU_NORM_L1) return acc + fabsf(v);
+  return fmaf(v, v, acc);
+}
+
+// out = g - A x with a fused norm of both components (partials per block).
+// Each thread accumulates its few cells in FP32 (the values are FP32, a max
+// is exact, a sum of a few dozen squares loses nothing that matters for the
+// linear stopping test) and the block combines in FP64: on GB300 an FP64
+// operation per cell would cost more than the cell's memory traffic.
 template <int DIM, int NORM>
 __global__ void __launch_bounds__(kBlock) lean_residual_kernel(LinLean P, float *out,
                                                                double *part) {
   const Geom &G = P.G;
   const long long n = G.ncell;
-  double acc = 0.0;
+  float acc = 0.f;
   for (long long q = gtid(); q < n; q += gstride()) {
     int i, j, k;
     cell_ijk(G, q, i, j, k);
@@ -147,10 +162,10 @@ __global__ void __launch_bounds__(kBlock) lean_residual_kernel(LinLean P, float 
       out[q] = r[0];
       out[n + q] = r[1];
     }
-    acc = norm_accum<NORM>(acc, (double)r[0]);
-    acc = norm_accum<NORM>(acc, (double)r[1]);
+    acc = lean_accum<NORM>(acc, r[0]);
+    acc = lean_accum<NORM>(acc, r[1]);
   }
-  const double v = block_reduce<NORM>(acc);
+  const double v = block_reduce<NORM>((double)acc);
   if (threadIdx.x == 0) part[blockIdx.x] = v;
 }
 

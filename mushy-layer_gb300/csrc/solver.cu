@@ -244,6 +244,17 @@ class VCSolver : public mlgpu_solver {
     }
   }
 
+  // constants are in the operator's null space: no alpha a term, no c, and
+  // no Dirichlet wall
+  bool singular() const {
+    if (op.alpha != 0.0 || op.cCoef) return false;
+    for (int d = 0; d < op.grid.dim; d++)
+      if (!op.grid.periodic[d])
+        for (int s2 = 0; s2 < 2; s2++)
+          if (op.bc.type[d][s2][0] == MLGPU_BC_DIRICHLET) return false;
+    return true;
+  }
+
   // lay out (or size, when base is null) the workspace
   size_t layout(char *base) {
     Arena A;
@@ -599,7 +610,7 @@ class VCSolver : public mlgpu_solver {
         if (zero_init) CK(cudaMemsetAsync(L[l].e, 0, sizeof(T) * L[l].G.ncell, s));
         VCArgs<double> A64 = args<double>(l);
         CK(launch_vc_bicgstab<T>(A64, (T *)L[l].e, (const T *)L[l].r, bicg_ws,
-                                 o.bottom_max_iter, s));
+                                 o.bottom_max_iter, (sizeof(T) == 4 && singular()) ? 1 : 0, s));
         return MLGPU_OK;
       }
       if (o.relax_mode == MLGPU_RELAX_JACOBI) return relax<T>(l, o.bottom_max_iter, zero_init);
@@ -1473,7 +1484,7 @@ class HCAdjSolver : public mlgpu_solver {
   // FP32 linear residual g - A y of level 0 with its norm (accumulated in FP64)
   int residual_norm32() {
     int nparts = 0;
-    CK(launch_lean_residual(lean(0), o.norm_type, L[0].r32, part, &nparts, s));
+    CK(launch_lean_residual(lean(0), o.norm_type, nullptr, part, &nparts, s));
     CK(launch_finalize_norm(o.norm_type, part, nparts, part + kMaxBlocks, s));
     CK(cudaMemcpyAsync(host_norm, part + kMaxBlocks, sizeof(double), cudaMemcpyDeviceToHost, s));
     return MLGPU_OK;
@@ -1633,6 +1644,36 @@ class HCAdjSolver : public mlgpu_solver {
     CK(cudaStreamSynchronize(s));
     if (leave()) return MLGPU_ERR_CUDA;
     return outer_finish(o, S, st);
+  }
+
+  // Device time of the lean red/black half sweep on the finest level, at the
+  // state and right-hand side of the last mixed-precision Newton step: `reps`
+  // launches, passes alternating, between two events on the solver's stream
+  // (y and w of the finest level are scratch between Newton steps).
+  int time_lean_sweep(int reps, double *ms_per_launch) {
+    if (!mixed || reps < 1 || !ms_per_launch) return MLGPU_ERR_ARG;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaGetLastError();
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+      if (e0) cudaEventDestroy(e0);
+      return MLGPU_ERR_CUDA;
+    }
+    int rc = enter();
+    const LinLean P = lean(0);
+    if (!rc && launch_lean_gsrb(P, 0, s) != cudaSuccess) rc = MLGPU_ERR_CUDA;  // warm
+    if (!rc && cudaEventRecord(e0, s) != cudaSuccess) rc = MLGPU_ERR_CUDA;
+    for (int i = 0; i < reps && !rc; i++)
+      if (launch_lean_gsrb(P, i & 1, s) != cudaSuccess) rc = MLGPU_ERR_CUDA;
+    if (!rc && cudaEventRecord(e1, s) != cudaSuccess) rc = MLGPU_ERR_CUDA;
+    float ms = 0.f;
+    if (!rc && (cudaEventSynchronize(e1) != cudaSuccess ||
+                cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess))
+      rc = MLGPU_ERR_CUDA;
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (leave()) rc = MLGPU_ERR_CUDA;
+    if (!rc) *ms_per_launch = (double)ms / reps;
+    return rc;
   }
 
   // A^T y = g at the state already set; y, g device arrays of the caller
@@ -1996,6 +2037,12 @@ int mlgpu_hc_backward_euler_newton(mlgpu_solver *S, double *phi_new, const doubl
   CK(launch_be_rhs(2 * A->L[0].G.ncell, phi_old, aCoef, src, dt, rhs_scratch, A->s));
   if (A->leave()) return MLGPU_ERR_CUDA;
   return A->newton(phi_new, rhs_scratch, stats);
+}
+
+int mlgpu_hc_newton_sweep_time(mlgpu_solver *S, int reps, double *ms_per_launch) {
+  HCAdjSolver *A = dynamic_cast<HCAdjSolver *>(S);
+  if (!A) return MLGPU_ERR_ARG;
+  return A->time_lean_sweep(reps, ms_per_launch);
 }
 
 int mlgpu_hc_adjoint_bc_gradient(mlgpu_solver *S, const double *y, double grad[12]) {
