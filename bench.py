@@ -412,14 +412,17 @@ def run_reference(args):
                 "d2h_bytes_per_step": 0}}))
 
 
-# Compulsory bytes of one FP32 red/black half sweep of the Newton step's
-# linear cycles (lin_lean_kernels.cuh lean_gsrb_kernel), per cell of the box:
-# the updated half of the cells read g (2 floats), K (4) and J (4) and write
-# x (2) and w (2); every face coefficient is read once (3 directions x 2
-# components); the other half's w is read once (2 floats each).
-# (5 + 6 + 1 + 2) floats = 56 B.
-LEAN_SWEEP_BYTES_PER_CELL = 56
-LEAN_SWEEP_PROFILE = os.path.join(PROFILES, "lean_gsrb_kernel_256cubed.md")
+# Compulsory bytes per cell of the box of the Newton step's FP32 smoothing
+# launches (lin_lean_kernels.cuh):
+# * one red/black half sweep (lean_gsrb_kernel): the updated half of the
+#   cells read g (2 floats), K (4) and J (4) and write x (2) and w (2); every
+#   face coefficient is read once (3 directions x 2 components); the other
+#   half's w is read once (2 floats each): (5 + 6 + 1 + 2) floats = 56 B;
+# * one fused red + black sweep (lean_sweep3_kernel): every cell's g, K, J
+#   (10 floats), the faces (6), w in (2), x and w out (4): 22 floats = 88 B.
+LEAN_HALF_SWEEP_BYTES_PER_CELL = 56
+LEAN_SWEEP_BYTES_PER_CELL = 88
+LEAN_SWEEP_PROFILE = os.path.join(PROFILES, "lean_sweep3_kernel_256cubed.md")
 
 
 def profiled_traffic(path, key):
@@ -434,25 +437,37 @@ def profiled_traffic(path, key):
     return None
 
 
-def dominant_kernel_roofline(torch, abi, ops, R):
-    """The mixed step's dominant kernel (the FP32 red/black half sweep of the
-    Newton cycles on the 256^3 level, 26% of the step in the ncu launch list)
-    timed with CUDA events on the solver's stream at the state of the last
-    timed step; achieved = its compulsory bytes / its time."""
-    HS = R.S["mixed"][1]
+def _sweep_time(abi, HS, kind, reps=40):
     ms = C.c_double()
-    abi.check(abi.load().mlgpu_hc_newton_sweep_time(HS.h, 40, C.byref(ms)), "sweep time")
+    abi.check(abi.load().mlgpu_hc_newton_sweep_time(HS.h, kind, reps, C.byref(ms)), "sweep time")
+    return ms.value
+
+
+def dominant_kernel_roofline(torch, abi, ops, R):
+    """The mixed step's dominant HBM-bound kernel, the fused FP32 red + black
+    sweep of the Newton cycles on the 256^3 level, timed with CUDA events on
+    the solver's stream at the state of the last timed step; achieved = its
+    compulsory bytes / its time.  The half sweep (the pre-smoothing sweep) is
+    reported beside it."""
+    HS = R.S["mixed"][1]
     ncell = R.cells()
-    alg = LEAN_SWEEP_BYTES_PER_CELL * ncell
-    achieved = alg / (ms.value * 1e-3) / 1e9
     hbm, kind = peaks()
-    return {"bound": "hbm", "kernel": "lean_gsrb_kernel<3> (FP32 red/black half sweep, "
+    ms = _sweep_time(abi, HS, 1)
+    alg = LEAN_SWEEP_BYTES_PER_CELL * ncell
+    achieved = alg / (ms * 1e-3) / 1e9
+    ms_h = _sweep_time(abi, HS, 0)
+    alg_h = LEAN_HALF_SWEEP_BYTES_PER_CELL * ncell
+    ach_h = alg_h / (ms_h * 1e-3) / 1e9
+    return {"bound": "hbm", "kernel": "lean_sweep3_kernel (FP32 fused red + black sweep, "
                                        "Newton linear cycles, 256^3 level)",
             "achieved": achieved, "peak": hbm, "peak_kind": kind, "unit": "GB/s",
             "frac": achieved / hbm,
             "traffic": profiled_traffic(LEAN_SWEEP_PROFILE, "dram_bytes_per_launch_256cubed"),
-            "alg_bytes_per_launch": alg, "launch_us": ms.value * 1e3,
-            "timing": "CUDA events on the solver stream, 40 launches after the timed region"}
+            "alg_bytes_per_launch": alg, "launch_us": ms * 1e3,
+            "timing": "CUDA events on the solver stream, 40 launches after the timed region",
+            "half_sweep": {"kernel": "lean_gsrb_kernel<3>", "achieved": ach_h,
+                           "frac": ach_h / hbm, "alg_bytes_per_launch": alg_h,
+                           "launch_us": ms_h * 1e3}}
 
 
 

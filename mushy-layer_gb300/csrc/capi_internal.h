@@ -105,6 +105,7 @@ cudaError_t launch_lean_restrict(const LinLean &P, const Geom &C, float *gc, flo
                                  cudaStream_t s);
 cudaError_t launch_lean_prolong(const LinLean &P, const Geom &C, int kind, const float *xc,
                                 cudaStream_t s);
+cudaError_t launch_lean_sweep3(const LeanSweep3 &S, cudaStream_t s);
 cudaError_t launch_adj_bottom_direct(const AdjArgs<float> &A, float *y, const float *g,
                                      cudaStream_t s, bool tr);
 cudaError_t launch_adj_restrict(const AdjArgs<float> &A, const Geom &C, const float *y,

@@ -109,4 +109,11 @@ cudaError_t launch_lean_prolong(const LinLean &P, const Geom &C, int kind, const
   return cudaGetLastError();
 }
 
+cudaError_t launch_lean_sweep3(const LeanSweep3 &S, cudaStream_t s) {
+  if (S.P.G.dim != 3 || S.P.G.per2) return cudaErrorInvalidValue;
+  const int nb = S.ntx * S.nty * S.nchunk;
+  lean_sweep3_kernel<<<nb, kZMThreads, 0, s>>>(S);
+  return cudaGetLastError();
+}
+
 }  // namespace mlgpu

@@ -219,4 +219,179 @@ __global__ void __launch_bounds__(kBlock) lean_prolong_kernel(LinLean P, Geom C,
 }
 #endif  // MLGPU_ADJ_F32_UNIT
 
+// ---- one full red + black sweep per launch in 3D (z-march) ----------------
+// A half-sweep launch touches every cache line of every array although it
+// updates half the cells, so a sweep costs two passes over memory.  Here one
+// thread block owns an x-y tile and marches up a chunk of planes; at the step
+// that brings plane t in, it updates the red cells of plane t-1 (their black
+// neighbours in planes t-2..t are still old) and then the black cells of
+// plane t-2 (their red neighbours in planes t-3..t-1 are now new): exactly
+// the red-then-black sweep, with the old/new w of four planes staged in
+// shared memory and each array read once.  Black cells at the tile edge need
+// updated red neighbours of the next tile, so the red pass also runs on a
+// one-cell ring around the tile (and one plane below / above the chunk) from
+// the same old data: redundant work, identical values, no dependence on
+// block order.  The launch reads (x, w) and writes (x_out, w_out), so no block
+// sees another's new values; every cell of the box is written once.  The
+// arithmetic is that of lean_gsrb_kernel in the same order (a neighbour
+// outside the box contributes b * 0), so one launch gives the bits of the
+// red and black half sweeps it replaces.  Non-periodic z only (the planes
+// beyond the walls are zero).
+constexpr int kZMTX = 30, kZMTY = 14;                    // output tile
+constexpr int kZMRX = kZMTX + 2, kZMRY = kZMTY + 2;      // red region: one thread per column
+constexpr int kZMWX = kZMTX + 4, kZMWY = kZMTY + 4;      // w region (red region + its neighbours)
+constexpr int kZMThreads = kZMRX * kZMRY;                // 512
+constexpr int kZMChunk = 32;                             // planes per block
+
+struct LeanSweep3 {
+  LinLean P;             // x, w: input of the sweep
+  float *x_out, *w_out;  // output of the sweep
+  int ntx, nty, nchunk;
+};
+
+#ifdef MLGPU_ADJ_F32_UNIT
+__global__ void __launch_bounds__(kZMThreads, 2) lean_sweep3_kernel(LeanSweep3 S) {
+  __shared__ float sw[4][2][kZMWY * kZMWX];
+  const LinLean &P = S.P;
+  const Geom &G = P.G;
+  const int n0 = G.n0, n1 = G.n1, n2 = G.n2;
+  const long long n = G.ncell, plane = (long long)n0 * n1;
+  const long long nfx = G.nface(0), nfy = G.nface(1), nfz = G.nface(2);
+  int item = blockIdx.x;
+  const int tx = item % S.ntx;
+  item /= S.ntx;
+  const int ty = item % S.nty, cz = item / S.nty;
+  const int x0 = tx * kZMTX, y0 = ty * kZMTY, z0 = cz * kZMChunk;
+  const int z1 = min(z0 + kZMChunk, n2);
+  const int lx = threadIdx.x % kZMRX, ly = threadIdx.x / kZMRX;
+  int gx = x0 - 1 + lx, gy = y0 - 1 + ly;
+  const bool interior = lx >= 1 && lx <= kZMTX && ly >= 1 && ly <= kZMTY && gx < n0 && gy < n1;
+  bool valid = true;
+  if (gx < 0 || gx >= n0) {
+    if (G.per0)
+      gx = ((gx % n0) + n0) % n0;
+    else
+      valid = false;
+  }
+  if (gy < 0 || gy >= n1) {
+    if (G.per1)
+      gy = ((gy % n1) + n1) % n1;
+    else
+      valid = false;
+  }
+  const long long col = valid ? (long long)gy * n0 + gx : 0;
+  const int wc = (ly + 1) * kZMWX + (lx + 1);
+  const int tb = z0 - 2, te = z1 + 1;
+  float T[10], R[10], B[10];
+#pragma unroll
+  for (int m = 0; m < 10; m++) T[m] = R[m] = B[m] = 0.f;
+
+  // the update of this column's cell at plane p: own data D (g, K, J), w of
+  // planes p-1, p, p+1 in shared memory
+  auto update = [&](int p, const float *D, float &xo0, float &xo1, float &wo0, float &wo1) {
+    const int sm = (p - 1 - tb) & 3, s0 = (p - tb) & 3, sp = (p + 1 - tb) & 3;
+    const long long cp = col + (long long)p * plane;
+    const long long fx = ((long long)p * n1 + gy) * (n0 + 1) + gx;
+    const long long fy = ((long long)p * (n1 + 1) + gy) * n0 + gx;
+    float s[2];
+#pragma unroll
+    for (int c = 0; c < 2; c++) {
+      const float *w0 = sw[s0][c];
+      float a = P.b[0][c * nfx + fx] * w0[wc - 1];
+      a = fmaf(P.b[0][c * nfx + fx + 1], w0[wc + 1], a);
+      a = fmaf(P.b[1][c * nfy + fy], w0[wc - kZMWX], a);
+      a = fmaf(P.b[1][c * nfy + fy + n0], w0[wc + kZMWX], a);
+      a = fmaf(P.b[2][c * nfz + cp], sw[sm][c][wc], a);
+      a = fmaf(P.b[2][c * nfz + cp + plane], sw[sp][c][wc], a);
+      s[c] = a;
+    }
+    const float r0 = fmaf(P.bdx, s[0], D[0]), r1 = fmaf(P.bdx, s[1], D[1]);
+    xo0 = fmaf(D[2], r0, D[4] * r1);
+    xo1 = fmaf(D[3], r0, D[5] * r1);
+    wo0 = fmaf(D[6], xo0, D[7] * xo1);
+    wo1 = fmaf(D[8], xo0, D[9] * xo1);
+  };
+
+  for (int t = tb; t <= te; t++) {
+    const int slot = (t - tb) & 3;
+    const bool pin = t >= 0 && t < n2;
+    // w of plane t over the w region (zero outside the box)
+    for (int idx = threadIdx.x; idx < kZMWX * kZMWY; idx += kZMThreads) {
+      int ax = x0 - 2 + idx % kZMWX, ay = y0 - 2 + idx / kZMWX;
+      bool ok = pin;
+      if (ax < 0 || ax >= n0) {
+        if (G.per0)
+          ax = ((ax % n0) + n0) % n0;
+        else
+          ok = false;
+      }
+      if (ay < 0 || ay >= n1) {
+        if (G.per1)
+          ay = ((ay % n1) + n1) % n1;
+        else
+          ok = false;
+      }
+      const long long q = (long long)t * plane + (long long)ay * n0 + ax;
+      sw[slot][0][idx] = ok ? P.w[q] : 0.f;
+      sw[slot][1][idx] = ok ? P.w[n + q] : 0.f;
+    }
+    // this column's own data of plane t: g (2), K (4), J (4)
+    const bool own = valid && pin && t >= z0 - 1 && t <= z1;
+    if (own) {
+      const long long q = col + (long long)t * plane;
+      T[0] = P.g[q];
+      T[1] = P.g[n + q];
+      T[2] = P.K[q];
+      T[3] = P.K[n + q];
+      T[4] = P.K[2 * n + q];
+      T[5] = P.K[3 * n + q];
+      T[6] = P.J[q];
+      T[7] = P.J[n + q];
+      T[8] = P.J[2 * n + q];
+      T[9] = P.J[3 * n + q];
+    }
+    __syncthreads();
+    // red cells of plane t-1 (on the tile and its ring; the chunk +- a plane)
+    const int p = t - 1;
+    if (valid && p >= 0 && p < n2 && p >= z0 - 1 && p <= z1 && ((gx + gy + p) & 1) == 0) {
+      float xa, xb, wa, wb;
+      update(p, R, xa, xb, wa, wb);
+      const int s0 = (p - tb) & 3;
+      sw[s0][0][wc] = wa;
+      sw[s0][1][wc] = wb;
+      if (interior && p >= z0 && p < z1) {
+        const long long q = col + (long long)p * plane;
+        S.x_out[q] = xa;
+        S.x_out[n + q] = xb;
+        S.w_out[q] = wa;
+        S.w_out[n + q] = wb;
+      }
+    }
+    __syncthreads();
+    // black cells of plane t-2 (on the tile)
+    const int p2 = t - 2;
+    if (interior && p2 >= z0 && p2 < z1 && ((gx + gy + p2) & 1) == 1) {
+      float xa, xb, wa, wb;
+      update(p2, B, xa, xb, wa, wb);
+      const long long q = col + (long long)p2 * plane;
+      S.x_out[q] = xa;
+      S.x_out[n + q] = xb;
+      S.w_out[q] = wa;
+      S.w_out[n + q] = wb;
+    }
+    // plane t's data waits for its red step (t+1) or its black step (t+2)
+    if (own) {
+      if (((gx + gy + t) & 1) == 0) {
+#pragma unroll
+        for (int m = 0; m < 10; m++) R[m] = T[m];
+      } else {
+#pragma unroll
+        for (int m = 0; m < 10; m++) B[m] = T[m];
+      }
+    }
+    __syncthreads();
+  }
+}
+#endif  // MLGPU_ADJ_F32_UNIT
+
 }  // namespace mlgpu

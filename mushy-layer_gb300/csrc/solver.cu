@@ -1217,6 +1217,9 @@ struct AdjLevel {
   Coefs<float> c32;
   float *J32 = nullptr, *Minv32 = nullptr, *y32 = nullptr, *g32 = nullptr, *r32 = nullptr;
   float *D32 = nullptr, *w32 = nullptr;  // diagonal blocks of A, and w = J y (lean cycles)
+  // second (y, w) of the fused 3D sweeps, which read one pair and write the
+  // other; between smoothing calls the values are always in (y32, w32)
+  float *y32b = nullptr, *w32b = nullptr;
 };
 
 class HCAdjSolver : public mlgpu_solver {
@@ -1253,6 +1256,17 @@ class HCAdjSolver : public mlgpu_solver {
 
   bool lin32() const { return mixed && !tr; }
 
+  // levels the fused red + black sweep (lean_sweep3_kernel) takes when the
+  // options' fuse_levels is set: 3D, at least 32 cells each way, walls in z,
+  // periodic x / y only with an even count (a red/black colouring consistent
+  // across the seam)
+  static bool fused_ok(const Geom &G) {
+    if (G.dim != 3 || G.per2) return false;
+    if (G.n0 < 32 || G.n1 < 32 || G.n2 < 32) return false;
+    if ((G.per0 && (G.n0 & 1)) || (G.per1 && (G.n1 & 1))) return false;
+    return true;
+  }
+
   size_t layout(char *base) {
     Arena A;
     A.base = base;
@@ -1285,6 +1299,10 @@ class HCAdjSolver : public mlgpu_solver {
         L[l].D32 = A.get<float>(2 * n);
         L[l].y32 = A.get<float>(n);
         L[l].w32 = A.get<float>(n);
+        if (o.fuse_levels && fused_ok(make_geom(g))) {
+          L[l].y32b = A.get<float>(n);
+          L[l].w32b = A.get<float>(n);
+        }
         L[l].g32 = A.get<float>(n);
         L[l].r32 = A.get<float>(n);
       }
@@ -1445,11 +1463,31 @@ class HCAdjSolver : public mlgpu_solver {
   // FP64 ones above
   // The lean cycles keep w = J y next to y on every level: zero together,
   // refreshed by every update and by the prolongation
+  // an even number of fused sweeps (ping-pong, ending back in (y32, w32), so
+  // every captured cycle starts from the same buffers), the rest as
+  // in-place half sweeps
   int smooth32(int l, int n) {
     const LinLean P = lean(l);
-    for (int i = 0; i < n; i++)
+    const int nf = L[l].y32b ? n - (n & 1) : 0;
+    for (int i = 0; i < nf; i++) CK(launch_lean_sweep3(fused(l, i & 1), s));
+    for (int i = nf; i < n; i++)
       for (int pass = 0; pass < 2; pass++) CK(launch_lean_gsrb(P, pass, s));
     return MLGPU_OK;
+  }
+
+  // fused sweep of level l reading pair `from` (0: y32, w32; 1: y32b, w32b)
+  LeanSweep3 fused(int l, int from) {
+    LeanSweep3 S;
+    S.P = lean(l);
+    S.P.x = from ? L[l].y32b : L[l].y32;
+    S.P.w = from ? L[l].w32b : L[l].w32;
+    S.x_out = from ? L[l].y32 : L[l].y32b;
+    S.w_out = from ? L[l].w32 : L[l].w32b;
+    const Geom &G = L[l].G;
+    S.ntx = (G.n0 + kZMTX - 1) / kZMTX;
+    S.nty = (G.n1 + kZMTY - 1) / kZMTY;
+    S.nchunk = (G.n2 + kZMChunk - 1) / kZMChunk;
+    return S;
   }
 
   int cycle32(int l) {
@@ -1650,8 +1688,9 @@ class HCAdjSolver : public mlgpu_solver {
   // state and right-hand side of the last mixed-precision Newton step: `reps`
   // launches, passes alternating, between two events on the solver's stream
   // (y and w of the finest level are scratch between Newton steps).
-  int time_lean_sweep(int reps, double *ms_per_launch) {
+  int time_lean_sweep(int kind, int reps, double *ms_per_launch) {
     if (!mixed || reps < 1 || !ms_per_launch) return MLGPU_ERR_ARG;
+    if (kind != 0 && (kind != 1 || !L[0].y32b)) return MLGPU_ERR_ARG;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     cudaGetLastError();
     if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
@@ -1660,10 +1699,13 @@ class HCAdjSolver : public mlgpu_solver {
     }
     int rc = enter();
     const LinLean P = lean(0);
-    if (!rc && launch_lean_gsrb(P, 0, s) != cudaSuccess) rc = MLGPU_ERR_CUDA;  // warm
+    auto one = [&](int i) {
+      return kind ? launch_lean_sweep3(fused(0, i & 1), s) : launch_lean_gsrb(P, i & 1, s);
+    };
+    if (!rc && one(0) != cudaSuccess) rc = MLGPU_ERR_CUDA;  // warm
     if (!rc && cudaEventRecord(e0, s) != cudaSuccess) rc = MLGPU_ERR_CUDA;
     for (int i = 0; i < reps && !rc; i++)
-      if (launch_lean_gsrb(P, i & 1, s) != cudaSuccess) rc = MLGPU_ERR_CUDA;
+      if (one(i + 1) != cudaSuccess) rc = MLGPU_ERR_CUDA;
     if (!rc && cudaEventRecord(e1, s) != cudaSuccess) rc = MLGPU_ERR_CUDA;
     float ms = 0.f;
     if (!rc && (cudaEventSynchronize(e1) != cudaSuccess ||
@@ -2039,10 +2081,10 @@ int mlgpu_hc_backward_euler_newton(mlgpu_solver *S, double *phi_new, const doubl
   return A->newton(phi_new, rhs_scratch, stats);
 }
 
-int mlgpu_hc_newton_sweep_time(mlgpu_solver *S, int reps, double *ms_per_launch) {
+int mlgpu_hc_newton_sweep_time(mlgpu_solver *S, int kind, int reps, double *ms_per_launch) {
   HCAdjSolver *A = dynamic_cast<HCAdjSolver *>(S);
   if (!A) return MLGPU_ERR_ARG;
-  return A->time_lean_sweep(reps, ms_per_launch);
+  return A->time_lean_sweep(kind, reps, ms_per_launch);
 }
 
 int mlgpu_hc_adjoint_bc_gradient(mlgpu_solver *S, const double *y, double grad[12]) {

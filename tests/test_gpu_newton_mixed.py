@@ -116,3 +116,49 @@ def test_c3_size_newton_step_mixed_matches_fp64():
     assert O.norm(O.nl_residual(ref, out[abi.PREC_MIXED], phi0)) <= 1e-10 * r0 * 1.0001
     u64 = out[abi.PREC_F64]
     assert np.abs(out[abi.PREC_MIXED] - u64).max() <= 1e-8 * np.abs(u64).max()
+
+
+def _c4_like(n):
+    """A 3D box like the 256^3 benchmark step (periodic x / y, cold bottom
+    wall, H falling from 6 at the top to 2 at the bottom with 1e-2 noise)."""
+    from mushy_gb300 import ops
+    rng = np.random.default_rng(4)
+    g = abi.make_grid([n, n, n], 1.0 / n, (1, 1, 0))
+    z = (np.arange(n) + 0.5) / n
+    phi0 = np.empty((2, n, n, n))
+    phi0[0] = 6.0 - 4.0 * (1.0 - z)[:, None, None] * (1.0 + 1e-2 * rng.standard_normal((n, n, n)))
+    phi0[1] = -1.0
+    prm = abi.make_params(stefan=5.0, compositionRatio=5.0, waterDistributionCoeff=1e-3,
+                          specificHeatRatio=1.0, heatConductivityRatio=1.0)
+    der = abi.make_bc({(2, 0, 0): (abi.BC_DIRICHLET, -1.0), (2, 0, 1): (abi.BC_DIRICHLET, -1.0)})
+    b = [np.stack([-np.ones(abi.face_shape(g, d)), np.full(abi.face_shape(g, d), -1e-2)])
+         for d in range(3)]
+    dt = 1e-4
+    op = ops.NLMultiCompOp(g, prm, abi.make_bc(), der, 1.0, -dt, None, [dev(x) for x in b])
+    ref = O.NLOpHost(g, prm, abi.make_bc(), der, 1.0, -dt, None, b)
+    return g, phi0, op, ref, dt
+
+
+def test_3d_newton_step_fused_sweep_bitwise_and_converged():
+    """64^3: the fused red + black sweep (one launch per sweep) gives the
+    same bits as the two half-sweep launches it replaces, and the mixed step
+    reaches 1e-10 under the oracle's residual, within 1e-8 of FP64 Newton."""
+    from mushy_gb300 import ops
+    g, phi0, op, ref, dt = _c4_like(64)
+    out = {}
+    for key, prec, fuse in (("fused", abi.PREC_MIXED, 1), ("half", abi.PREC_MIXED, 0),
+                            ("fp64", abi.PREC_F64, 1)):
+        o = _opts(prec)
+        o.fuse_levels = fuse
+        new = dev(phi0)
+        st, rc = ops.AdjointMultiGrid(op, o).backwardEulerNewton(new, dev(phi0), dt)
+        assert rc == 0, (key, rc, st.iterations)
+        assert st.final_norm <= 1e-10 * st.initial_norm
+        out[key] = (host(new), st)
+    (uf, sf), (uh, sh) = out["fused"], out["half"]
+    assert sf.iterations == sh.iterations and sf.cycles == sh.cycles
+    assert np.array_equal(uf, uh)
+    r0 = O.norm(O.nl_residual(ref, phi0, phi0))
+    assert O.norm(O.nl_residual(ref, uf, phi0)) <= 1e-10 * r0 * 1.0001
+    u64 = out["fp64"][0]
+    assert np.abs(uf - u64).max() <= 1e-8 * np.abs(u64).max()
