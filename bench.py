@@ -118,7 +118,8 @@ def c4_problem(torch, abi, ops, n=C4_N, seed=C4_SEED):
 class C4Runner:
     """The two solves of one step, FP64 or mixed; solvers built once."""
 
-    def __init__(self, torch, abi, ops, prob, use_graph=None, precs=("mixed", "fp64")):
+    def __init__(self, torch, abi, ops, prob, use_graph=None,
+                 precs=("mixed", "fp64", "fp64_fast")):
         self.torch, self.abi, self.ops, self.P = torch, abi, ops, prob
         self.S = {}
         for prec in precs:
@@ -127,6 +128,10 @@ class C4Runner:
             po.tolerance, po.hang, po.max_iter, po.precision = TOL, 1e-15, 300, code
             ho = ops.default_options(True)
             ho.tolerance, ho.hang, ho.max_iter, ho.precision = TOL, -1.0, 60, code
+            if prec == "fp64_fast":
+                # Newton's cycles with the mixed path's kernels (lean update,
+                # fused 3D sweep) in FP64: the same design, FP64 data
+                ho.fuse_levels = 2
             if use_graph is not None:
                 po.use_graph = ho.use_graph = use_graph
             self.S[prec] = (ops.AMRMultiGrid(prob["pop"], po), ops.AdjointMultiGrid(prob["hop"], ho))
@@ -208,6 +213,7 @@ def run_gpu(args):
     with Clocks() as clk:
         ms_m, upd_m, out_m = timed("mixed", args.steps, args.warmup)
         ms_d, upd_d, out_d = timed("fp64", args.steps, args.warmup)
+        ms_f, upd_f, out_f = timed("fp64_fast", args.steps, args.warmup)
     clocks = clk.summary()
 
     # mixed against FP64: pressure up to its constant, (H, C) state
@@ -215,6 +221,7 @@ def run_gpu(args):
     p_err = float(((a - a.mean()) - (m - m.mean())).abs().max() / (a - a.mean()).abs().max())
     u64, um = R.u["fp64"], R.u["mixed"]
     hc_err = float((um - u64).abs().max() / u64.abs().max())
+    hc_err_fast = float((R.u["fp64_fast"] - u64).abs().max() / u64.abs().max())
     launches = {k: int(v[0][0].kernel_launches) for k, v in (("mixed", out_m), ("fp64", out_d))}
 
     # end to end through the public API: the step's inputs (rhs of the
@@ -272,8 +279,16 @@ def run_gpu(args):
                    "l2": "flushed (512 MiB write) between steps; every field > 129 MB",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "mixed": {**sm, "ms_per_step": ms_m / args.steps, "gpu_launches_per_step": None},
-        "fp64": {**sd, "value": upd_d * world / (ms_d * 1e-3), "ms_per_step": ms_d / args.steps},
+        "fp64": {**sd, "value": upd_d * world / (ms_d * 1e-3), "ms_per_step": ms_d / args.steps,
+                 "note": "reference expression order (bitwise the oracle's kernels)"},
+        "fp64_fast": {**C4Runner.summary(out_f), "value": upd_f * world / (ms_f * 1e-3),
+                      "ms_per_step": ms_f / args.steps,
+                      "note": "FP64 with the mixed path's kernel design (lean Jacobian "
+                              "update, fused 3D sweep) for Newton's cycles; projection "
+                              "as fp64",
+                      "hc_rel_vs_fp64": hc_err_fast},
         "time_to_solution_ratio_fp64_over_mixed": ms_d / ms_m,
+        "time_to_solution_ratio_fp64_fast_over_mixed": ms_f / ms_m,
         "mixed_vs_fp64": {"pressure_rel": p_err, "hc_rel": hc_err},
         "e2e": {"value": e2e_upd * world / (e2e_ms * 1e-3), "unit": "cell-updates/s",
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
@@ -422,7 +437,7 @@ def run_reference(args):
 #   (10 floats), the faces (6), w in (2), x and w out (4): 22 floats = 88 B.
 LEAN_HALF_SWEEP_BYTES_PER_CELL = 56
 LEAN_SWEEP_BYTES_PER_CELL = 88
-LEAN_SWEEP_PROFILE = os.path.join(PROFILES, "lean_sweep3_kernel_256cubed.md")
+LEAN_SWEEP_PROFILE = os.path.join(PROFILES, "lean_gsrb_kernel_256cubed.md")
 
 
 def profiled_traffic(path, key):
@@ -444,30 +459,23 @@ def _sweep_time(abi, HS, kind, reps=40):
 
 
 def dominant_kernel_roofline(torch, abi, ops, R):
-    """The mixed step's dominant HBM-bound kernel, the fused FP32 red + black
-    sweep of the Newton cycles on the 256^3 level, timed with CUDA events on
-    the solver's stream at the state of the last timed step; achieved = its
-    compulsory bytes / its time.  The half sweep (the pre-smoothing sweep) is
-    reported beside it."""
+    """The mixed step's dominant HBM-bound kernel, the FP32 red/black half
+    sweep of the Newton cycles on the 256^3 level (lean_gsrb_kernel<3>),
+    timed with CUDA events on the solver's stream at the state of the last
+    timed step; achieved = its compulsory bytes / its time."""
     HS = R.S["mixed"][1]
     ncell = R.cells()
     hbm, kind = peaks()
-    ms = _sweep_time(abi, HS, 1)
-    alg = LEAN_SWEEP_BYTES_PER_CELL * ncell
+    ms = _sweep_time(abi, HS, 0)
+    alg = LEAN_HALF_SWEEP_BYTES_PER_CELL * ncell
     achieved = alg / (ms * 1e-3) / 1e9
-    ms_h = _sweep_time(abi, HS, 0)
-    alg_h = LEAN_HALF_SWEEP_BYTES_PER_CELL * ncell
-    ach_h = alg_h / (ms_h * 1e-3) / 1e9
-    return {"bound": "hbm", "kernel": "lean_sweep3_kernel (FP32 fused red + black sweep, "
+    return {"bound": "hbm", "kernel": "lean_gsrb_kernel<3> (FP32 red/black half sweep, "
                                        "Newton linear cycles, 256^3 level)",
             "achieved": achieved, "peak": hbm, "peak_kind": kind, "unit": "GB/s",
             "frac": achieved / hbm,
             "traffic": profiled_traffic(LEAN_SWEEP_PROFILE, "dram_bytes_per_launch_256cubed"),
             "alg_bytes_per_launch": alg, "launch_us": ms * 1e3,
-            "timing": "CUDA events on the solver stream, 40 launches after the timed region",
-            "half_sweep": {"kernel": "lean_gsrb_kernel<3>", "achieved": ach_h,
-                           "frac": ach_h / hbm, "alg_bytes_per_launch": alg_h,
-                           "launch_us": ms_h * 1e3}}
+            "timing": "CUDA events on the solver stream, 40 launches after the timed region"}
 
 
 
@@ -1015,12 +1023,12 @@ def run_profile(args):
                           "newton_linear_cycles": st_n.cycles,
                           "adjoint_cycles": st_a.iterations}))
         return
-    if args.profile in ("c4", "c4-fp64"):
+    if args.profile in ("c4", "c4-fp64", "c4-fp64-fast"):
         # one step of the 256^3 workload (or --n^3) with plain launches
         # (profilers do not see kernel nodes inside graphs with conditional
         # nodes)
         prob = c4_problem(torch, abi, ops, n=args.n)
-        prec = "mixed" if args.profile == "c4" else "fp64"
+        prec = {"c4": "mixed", "c4-fp64": "fp64", "c4-fp64-fast": "fp64_fast"}[args.profile]
         R = C4Runner(torch, abi, ops, prob, use_graph=0, precs=(prec,))
         for _ in range(1 + args.warmup):
             out = R.step(prec)
@@ -1053,7 +1061,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--n", type=int, default=C4_N,
                     help="box edge of the --profile c4 runs (ncu captures of a smaller case)")
-    ap.add_argument("--profile", choices=["c4", "c4-fp64", "c2-mixed", "c2-fp64", "hc", "adjoint"],
+    ap.add_argument("--profile", choices=["c4", "c4-fp64", "c4-fp64-fast", "c2-mixed", "c2-fp64",
+                                          "hc", "adjoint"],
                     help="run one short solve for a profiler and exit")
     ap.add_argument("--config", type=int, choices=[1, 2, 3, 5],
                     help="measure another configuration (one JSON line) and exit")

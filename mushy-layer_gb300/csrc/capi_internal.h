@@ -70,7 +70,7 @@ cudaError_t launch_adj_bottom_direct(const AdjArgs<double> &A, double *y, const 
                                      cudaStream_t s, bool tr = true);
 // inverse diagonal blocks of A^T per cell (`zero`: a zero field of the level)
 cudaError_t launch_adj_minv(const AdjArgs<double> &A, const double *zero, double *Minv,
-                            cudaStream_t s);
+                            double *D, cudaStream_t s);
 cudaError_t launch_adj_bc_grad(const AdjArgs<double> &A, const double *y, double *out,
                                cudaStream_t s);
 cudaError_t launch_outer_coefs(const VCArgs<double> &A, double *cx, double *cy, double *diag,
@@ -97,15 +97,20 @@ cudaError_t launch_adj_relax_block(const AdjArgs<float> &A, float *y, const floa
                                    int zero, cudaStream_t s, bool tr);
 cudaError_t launch_adj_minv(const AdjArgs<float> &A, const float *zero, float *Minv, float *D,
                             cudaStream_t s);
-// lean FP32 cycles of the Newton step (lin_lean_kernels.cuh)
-cudaError_t launch_lean_gsrb(const LinLean &P, int pass, cudaStream_t s);
-cudaError_t launch_lean_residual(const LinLean &P, int norm, float *out, double *part,
+// lean cycles of the Newton step (lin_lean_kernels.cuh); T = float or double
+template <class T>
+cudaError_t launch_lean_gsrb(const LinLeanT<T> &P, int pass, cudaStream_t s);
+template <class T>
+cudaError_t launch_lean_residual(const LinLeanT<T> &P, int norm, T *out, double *part,
                                  int *nparts, cudaStream_t s);
-cudaError_t launch_lean_restrict(const LinLean &P, const Geom &C, float *gc, float *xc, float *wc,
+template <class T>
+cudaError_t launch_lean_restrict(const LinLeanT<T> &P, const Geom &C, T *gc, T *xc, T *wc,
                                  cudaStream_t s);
-cudaError_t launch_lean_prolong(const LinLean &P, const Geom &C, int kind, const float *xc,
+template <class T>
+cudaError_t launch_lean_prolong(const LinLeanT<T> &P, const Geom &C, int kind, const T *xc,
                                 cudaStream_t s);
-cudaError_t launch_lean_sweep3(const LeanSweep3 &S, cudaStream_t s);
+template <class T>
+cudaError_t launch_lean_sweep3(const LeanSweep3T<T> &S, cudaStream_t s);
 cudaError_t launch_adj_bottom_direct(const AdjArgs<float> &A, float *y, const float *g,
                                      cudaStream_t s, bool tr);
 cudaError_t launch_adj_restrict(const AdjArgs<float> &A, const Geom &C, const float *y,

@@ -76,44 +76,62 @@ cudaError_t launch_adj_restrict(const AdjArgs<float> &A, const Geom &C, const fl
   return cudaGetLastError();
 }
 
-// ---- lean cycles of the Newton step (lin_lean_kernels.cuh)
-cudaError_t launch_lean_gsrb(const LinLean &P, int pass, cudaStream_t s) {
-  MLGPU_DIM_SWITCH(P.G.dim, (lean_gsrb_kernel<DIM><<<blocks_for(colour_threads(P.G)), kBlock, 0, s>>>(P, pass)));
+// ---- lean cycles of the Newton step (lin_lean_kernels.cuh), FP32 for the
+// mixed-precision solve and FP64 for the comparison path built the same way
+template <class T>
+cudaError_t launch_lean_gsrb(const LinLeanT<T> &P, int pass, cudaStream_t s) {
+  MLGPU_DIM_SWITCH(P.G.dim, (lean_gsrb_kernel<T, DIM><<<blocks_for(colour_threads(P.G)), kBlock, 0, s>>>(P, pass)));
   return cudaGetLastError();
 }
 
-cudaError_t launch_lean_residual(const LinLean &P, int norm, float *out, double *part,
+template <class T>
+cudaError_t launch_lean_residual(const LinLeanT<T> &P, int norm, T *out, double *part,
                                  int *nparts, cudaStream_t s) {
   const int nb = blocks_for(P.G.ncell);
   if (nparts) *nparts = nb;
   if (norm < 0) norm = MLGPU_NORM_MAX;
   MLGPU_DIM_SWITCH(P.G.dim, MLGPU_NORM_SWITCH(norm, {
-    if (NORM >= 0) lean_residual_kernel<DIM, (NORM < 0 ? 0 : NORM)><<<nb, kBlock, 0, s>>>(P, out, part);
+    if (NORM >= 0) lean_residual_kernel<T, DIM, (NORM < 0 ? 0 : NORM)><<<nb, kBlock, 0, s>>>(P, out, part);
   }));
   return cudaGetLastError();
 }
 
-cudaError_t launch_lean_restrict(const LinLean &P, const Geom &C, float *gc, float *xc, float *wc,
+template <class T>
+cudaError_t launch_lean_restrict(const LinLeanT<T> &P, const Geom &C, T *gc, T *xc, T *wc,
                                  cudaStream_t s) {
-  MLGPU_DIM_SWITCH(P.G.dim, (lean_restrict_kernel<DIM><<<blocks_for(C.ncell), kBlock, 0, s>>>(P, C, gc, xc, wc)));
+  MLGPU_DIM_SWITCH(P.G.dim, (lean_restrict_kernel<T, DIM><<<blocks_for(C.ncell), kBlock, 0, s>>>(P, C, gc, xc, wc)));
   return cudaGetLastError();
 }
 
-cudaError_t launch_lean_prolong(const LinLean &P, const Geom &C, int kind, const float *xc,
+template <class T>
+cudaError_t launch_lean_prolong(const LinLeanT<T> &P, const Geom &C, int kind, const T *xc,
                                 cudaStream_t s) {
   if (kind == MLGPU_PROLONG_LINEAR) {
-    MLGPU_DIM_SWITCH(P.G.dim, (lean_prolong_kernel<DIM, MLGPU_PROLONG_LINEAR><<<blocks_for(P.G.ncell), kBlock, 0, s>>>(P, C, xc)));
+    MLGPU_DIM_SWITCH(P.G.dim, (lean_prolong_kernel<T, DIM, MLGPU_PROLONG_LINEAR><<<blocks_for(P.G.ncell), kBlock, 0, s>>>(P, C, xc)));
   } else {
-    MLGPU_DIM_SWITCH(P.G.dim, (lean_prolong_kernel<DIM, MLGPU_PROLONG_CONSTANT><<<blocks_for(P.G.ncell), kBlock, 0, s>>>(P, C, xc)));
+    MLGPU_DIM_SWITCH(P.G.dim, (lean_prolong_kernel<T, DIM, MLGPU_PROLONG_CONSTANT><<<blocks_for(P.G.ncell), kBlock, 0, s>>>(P, C, xc)));
   }
   return cudaGetLastError();
 }
 
-cudaError_t launch_lean_sweep3(const LeanSweep3 &S, cudaStream_t s) {
+template <class T>
+cudaError_t launch_lean_sweep3(const LeanSweep3T<T> &S, cudaStream_t s) {
   if (S.P.G.dim != 3 || S.P.G.per2) return cudaErrorInvalidValue;
   const int nb = S.ntx * S.nty * S.nchunk;
-  lean_sweep3_kernel<<<nb, kZMThreads, 0, s>>>(S);
+  lean_sweep3_kernel<T><<<nb, kZMThreads, 0, s>>>(S);
   return cudaGetLastError();
 }
+
+#define MLGPU_LEAN_INST(T)                                                                     \
+  template cudaError_t launch_lean_gsrb<T>(const LinLeanT<T> &, int, cudaStream_t);           \
+  template cudaError_t launch_lean_residual<T>(const LinLeanT<T> &, int, T *, double *, int *, \
+                                              cudaStream_t);                                  \
+  template cudaError_t launch_lean_restrict<T>(const LinLeanT<T> &, const Geom &, T *, T *,    \
+                                              T *, cudaStream_t);                             \
+  template cudaError_t launch_lean_prolong<T>(const LinLeanT<T> &, const Geom &, int,          \
+                                             const T *, cudaStream_t);                        \
+  template cudaError_t launch_lean_sweep3<T>(const LeanSweep3T<T> &, cudaStream_t);
+MLGPU_LEAN_INST(float)
+MLGPU_LEAN_INST(double)
 
 }  // namespace mlgpu

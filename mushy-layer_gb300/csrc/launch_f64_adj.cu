@@ -54,8 +54,8 @@ cudaError_t launch_adj_relax_block(const AdjArgs<double> &A, double *y, const do
   return cudaGetLastError();
 }
 cudaError_t launch_adj_minv(const AdjArgs<double> &A, const double *zero, double *Minv,
-                            cudaStream_t s) {
-  MLGPU_DIM_SWITCH(A.G.dim, (adj_minv_kernel<double, DIM><<<blocks_for(A.G.ncell), kBlock, 0, s>>>(A, zero, Minv, nullptr)));
+                            double *D, cudaStream_t s) {
+  MLGPU_DIM_SWITCH(A.G.dim, (adj_minv_kernel<double, DIM><<<blocks_for(A.G.ncell), kBlock, 0, s>>>(A, zero, Minv, D)));
   return cudaGetLastError();
 }
 cudaError_t launch_adj_bottom_direct(const AdjArgs<double> &A, double *y, const double *g,

@@ -1220,6 +1220,9 @@ struct AdjLevel {
   // second (y, w) of the fused 3D sweeps, which read one pair and write the
   // other; between smoothing calls the values are always in (y32, w32)
   float *y32b = nullptr, *w32b = nullptr;
+  // FP64 lean cycles (the comparison path): w = J y, A's diagonal blocks, the
+  // fused sweeps' second pair
+  double *w64 = nullptr, *D64 = nullptr, *y64b = nullptr, *w64b = nullptr;
 };
 
 class HCAdjSolver : public mlgpu_solver {
@@ -1237,6 +1240,11 @@ class HCAdjSolver : public mlgpu_solver {
   // Newton residual, its norm, the update and the closure stay FP64); the
   // adjoint solve stays FP64
   bool mixed = false;
+  // FP64 with options.fuse_levels >= 2: Newton's linear cycles run the lean
+  // kernels (and the fused 3D sweep) in FP64 -- the same design as the mixed
+  // cycles, the reference's expression order given up -- the comparison
+  // path for the mixed-precision speed-up
+  bool fast64 = false;
   cudaGraphExec_t graph = nullptr, graph_lin = nullptr, graph_lin32 = nullptr;
   double *nf = nullptr, *nuold = nullptr;  // Newton: rhs of N(u) = f, previous u
   double *ntcl = nullptr;  // Newton: (T, C_l) of level 0, the residual's closure cache
@@ -1257,9 +1265,10 @@ class HCAdjSolver : public mlgpu_solver {
   bool lin32() const { return mixed && !tr; }
 
   // levels the fused red + black sweep (lean_sweep3_kernel) takes when the
-  // options' fuse_levels is set: 3D, at least 32 cells each way, walls in z,
-  // periodic x / y only with an even count (a red/black colouring consistent
-  // across the seam)
+  // options' fuse_levels is 3 or more: 3D, at least 32 cells each way, walls
+  // in z, periodic x / y only with an even count (a red/black colouring
+  // consistent across the seam).  Off by default: it reads the compulsory
+  // bytes once but, latency-bound, runs slower than the two half sweeps.
   static bool fused_ok(const Geom &G) {
     if (G.dim != 3 || G.per2) return false;
     if (G.n0 < 32 || G.n1 < 32 || G.n2 < 32) return false;
@@ -1271,6 +1280,7 @@ class HCAdjSolver : public mlgpu_solver {
     Arena A;
     A.base = base;
     mixed = o.precision == MLGPU_PREC_MIXED;
+    fast64 = !mixed && o.fuse_levels >= 2;
     int depth = mg_depth(op.grid, o.max_coarse);
     L.assign(depth + 1, AdjLevel());
     mlgpu_grid g = op.grid;
@@ -1299,12 +1309,20 @@ class HCAdjSolver : public mlgpu_solver {
         L[l].D32 = A.get<float>(2 * n);
         L[l].y32 = A.get<float>(n);
         L[l].w32 = A.get<float>(n);
-        if (o.fuse_levels && fused_ok(make_geom(g))) {
+        if (o.fuse_levels >= 3 && fused_ok(make_geom(g))) {
           L[l].y32b = A.get<float>(n);
           L[l].w32b = A.get<float>(n);
         }
         L[l].g32 = A.get<float>(n);
         L[l].r32 = A.get<float>(n);
+      }
+      if (fast64) {
+        L[l].w64 = A.get<double>(n);
+        L[l].D64 = A.get<double>(2 * n);
+        if (o.fuse_levels >= 3 && fused_ok(make_geom(g))) {
+          L[l].y64b = A.get<double>(n);
+          L[l].w64b = A.get<double>(n);
+        }
       }
       g = coarsen_grid(g);
     }
@@ -1371,21 +1389,43 @@ class HCAdjSolver : public mlgpu_solver {
     return A;
   }
 
-  // lean FP32 operator of level l (lin_lean_kernels.cuh)
-  LinLean lean(int l) {
+  // lean operator of level l (lin_lean_kernels.cuh): FP32 arrays for the
+  // mixed-precision cycles, FP64 ones for the FP64 comparison path
+  template <class T>
+  LinLeanT<T> leanT(int l) {
     const AdjArgs<double> D = args(l);
-    LinLean P;
+    LinLeanT<T> P;
     P.G = D.G;
     P.ybc = ybc();
-    P.bdx = (float)(D.beta * D.dxinv);
-    for (int d = 0; d < 3; d++) P.b[d] = L[l].c32.b[d];
-    P.J = L[l].J32;
-    P.K = L[l].Minv32;
-    P.D = L[l].D32;
-    P.x = L[l].y32;
-    P.w = L[l].w32;
-    P.g = L[l].g32;
+    P.bdx = (T)(D.beta * D.dxinv);
+    if constexpr (sizeof(T) == 4) {
+      for (int d = 0; d < 3; d++) P.b[d] = L[l].c32.b[d];
+      P.J = L[l].J32;
+      P.K = L[l].Minv32;
+      P.D = L[l].D32;
+      P.x = L[l].y32;
+      P.w = L[l].w32;
+      P.g = L[l].g32;
+    } else {
+      for (int d = 0; d < 3; d++) P.b[d] = L[l].c64.b[d];
+      P.J = L[l].J;
+      P.K = L[l].Minv;
+      P.D = L[l].D64;
+      P.x = L[l].y;
+      P.w = L[l].w64;
+      P.g = L[l].g;
+    }
     return P;
+  }
+  LinLean lean(int l) { return leanT<float>(l); }
+  // second (y, w) pair of the fused sweeps, or null
+  template <class T>
+  T *yb(int l) {
+    if constexpr (sizeof(T) == 4) return L[l].y32b; else return L[l].y64b;
+  }
+  template <class T>
+  T *wb(int l) {
+    if constexpr (sizeof(T) == 4) return L[l].w32b; else return L[l].w64b;
   }
 
   // the wall rule of the adjoint variable in the prolongation
@@ -1415,7 +1455,8 @@ class HCAdjSolver : public mlgpu_solver {
     // the smoother's inverse diagonal blocks (r is free here: a zero field)
     for (size_t l = 0; l < L.size(); l++) {
       CK(cudaMemsetAsync(L[l].r, 0, sizeof(double) * 2 * L[l].G.ncell, s));
-      CK(launch_adj_minv(args((int)l), L[l].r, L[l].Minv, s));
+      CK(launch_adj_minv(args((int)l), L[l].r, L[l].Minv, (fast64 && !tr) ? L[l].D64 : nullptr,
+                         s));
     }
     return MLGPU_OK;
   }
@@ -1461,78 +1502,101 @@ class HCAdjSolver : public mlgpu_solver {
 
   // ---- FP32 cycles on A (mixed-precision Newton); same structure as the
   // FP64 ones above
-  // The lean cycles keep w = J y next to y on every level: zero together,
-  // refreshed by every update and by the prolongation
-  // an even number of fused sweeps (ping-pong, ending back in (y32, w32), so
-  // every captured cycle starts from the same buffers), the rest as
-  // in-place half sweeps
-  int smooth32(int l, int n) {
-    const LinLean P = lean(l);
-    const int nf = L[l].y32b ? n - (n & 1) : 0;
-    for (int i = 0; i < nf; i++) CK(launch_lean_sweep3(fused(l, i & 1), s));
+  // ---- lean cycles on A (Newton's linear solve): FP32 in mixed precision,
+  // FP64 on the comparison path built the same way; same structure as the
+  // generic cycles above.  They keep w = J y next to y on every level: zero
+  // together, refreshed by every update and by the prolongation.
+  // Smoothing: an even number of fused sweeps (ping-pong, ending back in the
+  // level's (y, w), so every captured cycle starts from the same buffers),
+  // the rest as in-place half sweeps.
+  template <class T>
+  int lin_smooth(int l, int n) {
+    const LinLeanT<T> P = leanT<T>(l);
+    const int nf = yb<T>(l) ? n - (n & 1) : 0;
+    for (int i = 0; i < nf; i++) CK(launch_lean_sweep3<T>(fusedT<T>(l, i & 1), s));
     for (int i = nf; i < n; i++)
-      for (int pass = 0; pass < 2; pass++) CK(launch_lean_gsrb(P, pass, s));
+      for (int pass = 0; pass < 2; pass++) CK(launch_lean_gsrb<T>(P, pass, s));
     return MLGPU_OK;
   }
 
-  // fused sweep of level l reading pair `from` (0: y32, w32; 1: y32b, w32b)
-  LeanSweep3 fused(int l, int from) {
-    LeanSweep3 S;
-    S.P = lean(l);
-    S.P.x = from ? L[l].y32b : L[l].y32;
-    S.P.w = from ? L[l].w32b : L[l].w32;
-    S.x_out = from ? L[l].y32 : L[l].y32b;
-    S.w_out = from ? L[l].w32 : L[l].w32b;
+  // fused sweep of level l reading pair `from` (0: the level's y, w; 1: the
+  // second pair)
+  template <class T>
+  LeanSweep3T<T> fusedT(int l, int from) {
+    LeanSweep3T<T> S;
+    S.P = leanT<T>(l);
+    T *y0 = S.P.x, *w0 = S.P.w;
+    S.P.x = from ? yb<T>(l) : y0;
+    S.P.w = from ? wb<T>(l) : w0;
+    S.x_out = from ? y0 : yb<T>(l);
+    S.w_out = from ? w0 : wb<T>(l);
     const Geom &G = L[l].G;
     S.ntx = (G.n0 + kZMTX - 1) / kZMTX;
     S.nty = (G.n1 + kZMTY - 1) / kZMTY;
     S.nchunk = (G.n2 + kZMChunk - 1) / kZMChunk;
     return S;
   }
+  LeanSweep3 fused(int l, int from) { return fusedT<float>(l, from); }
 
-  int cycle32(int l) {
+  template <class T>
+  int lin_cycle(int l) {
     const int last = (int)L.size() - 1;
+    const LinLeanT<T> P = leanT<T>(l);
     if (l == last) {
       // the bottom solve updates y alone: its w is never read
-      AdjArgs<float> A = args32(l);
-      if (2 * L[l].G.ncell <= kAdjDirectMax)
-        CK(launch_adj_bottom_direct(A, L[l].y32, L[l].g32, s, false));
-      else
-        CK(launch_adj_relax_block(A, L[l].y32, L[l].g32, o.bottom_max_iter, l > 0 ? 1 : 0, s,
-                                  false));
+      if constexpr (sizeof(T) == 4) {
+        AdjArgs<float> A = args32(l);
+        if (2 * L[l].G.ncell <= kAdjDirectMax)
+          CK(launch_adj_bottom_direct(A, P.x, P.g, s, false));
+        else
+          CK(launch_adj_relax_block(A, P.x, P.g, o.bottom_max_iter, l > 0 ? 1 : 0, s, false));
+      } else {
+        AdjArgs<double> A = args(l);
+        if (2 * L[l].G.ncell <= kAdjDirectMax)
+          CK(launch_adj_bottom_direct(A, P.x, P.g, s, false));
+        else
+          CK(launch_adj_relax_block(A, P.x, P.g, o.bottom_max_iter, l > 0 ? 1 : 0, s, false));
+      }
       return MLGPU_OK;
     }
     // a coarse level's y and w were zeroed by the restriction that fed it
-    int rc = smooth32(l, o.num_smooth_down);
+    int rc = lin_smooth<T>(l, o.num_smooth_down);
     if (rc) return rc;
-    const LinLean P = lean(l);
-    CK(launch_lean_restrict(P, L[l + 1].G, L[l + 1].g32, L[l + 1].y32, L[l + 1].w32, s));
+    const LinLeanT<T> C = leanT<T>(l + 1);
+    CK(launch_lean_restrict<T>(P, C.G, (T *)C.g, C.x, C.w, s));
     for (int m = 0; m < o.num_mg; m++) {
       if (m > 0) {  // every coarse visit starts from zero
-        CK(cudaMemsetAsync(L[l + 1].y32, 0, sizeof(float) * 2 * L[l + 1].G.ncell, s));
-        CK(cudaMemsetAsync(L[l + 1].w32, 0, sizeof(float) * 2 * L[l + 1].G.ncell, s));
+        CK(cudaMemsetAsync(C.x, 0, sizeof(T) * 2 * C.G.ncell, s));
+        CK(cudaMemsetAsync(C.w, 0, sizeof(T) * 2 * C.G.ncell, s));
       }
-      rc = cycle32(l + 1);
+      rc = lin_cycle<T>(l + 1);
       if (rc) return rc;
     }
-    CK(launch_lean_prolong(P, L[l + 1].G, o.prolong, L[l + 1].y32, s));
-    return smooth32(l, o.num_smooth_up);
+    CK(launch_lean_prolong<T>(P, C.G, o.prolong, C.x, s));
+    return lin_smooth<T>(l, o.num_smooth_up);
   }
 
-  // FP32 linear residual g - A y of level 0 with its norm (accumulated in FP64)
-  int residual_norm32() {
+  // linear residual g - A y of level 0 with its norm (combined in FP64)
+  template <class T>
+  int lin_residual_norm() {
     int nparts = 0;
-    CK(launch_lean_residual(lean(0), o.norm_type, nullptr, part, &nparts, s));
+    CK(launch_lean_residual<T>(leanT<T>(0), o.norm_type, nullptr, part, &nparts, s));
     CK(launch_finalize_norm(o.norm_type, part, nparts, part + kMaxBlocks, s));
     CK(cudaMemcpyAsync(host_norm, part + kMaxBlocks, sizeof(double), cudaMemcpyDeviceToHost, s));
     return MLGPU_OK;
   }
+  int residual_norm32() { return lin_residual_norm<float>(); }
 
   int iteration() {
     if (lin32()) {
-      int rc = cycle32(0);
+      int rc = lin_cycle<float>(0);
       if (rc) return rc;
-      return residual_norm32();
+      return lin_residual_norm<float>();
+    }
+    if (fast64 && !tr) {
+      int rc = lin_cycle<double>(0);
+      if (rc) return rc;
+      return lin_residual_norm<double>();
     }
     int rc = cycle(0);
     if (rc) return rc;
@@ -1605,7 +1669,10 @@ class HCAdjSolver : public mlgpu_solver {
     CK(cudaMemcpyAsync(nf, user_f, bytes, cudaMemcpyDeviceToDevice, s));
     if (nk_state < 0) {
       nk_state = count_kernels([&] { return state_levels(); });
-      nk_res = count_kernels([&] { return mixed ? residual_norm32() : residual_norm(); });
+      nk_res = count_kernels([&] {
+        return mixed ? lin_residual_norm<float>()
+                     : (fast64 ? lin_residual_norm<double>() : residual_norm());
+      });
       nk_iter = count_kernels([&] { return iteration(); });
     }
     int rc = nl_residual();
@@ -1627,6 +1694,10 @@ class HCAdjSolver : public mlgpu_solver {
         CK(cudaMemsetAsync(L[0].y32, 0, sizeof(float) * n2, s));
         CK(cudaMemsetAsync(L[0].w32, 0, sizeof(float) * n2, s));
         rc = residual_norm32();
+      } else if (fast64) {
+        CK(cudaMemsetAsync(L[0].y, 0, bytes, s));
+        CK(cudaMemsetAsync(L[0].w64, 0, bytes, s));
+        rc = lin_residual_norm<double>();
       } else {
         CK(cudaMemsetAsync(L[0].y, 0, bytes, s));
         rc = residual_norm();

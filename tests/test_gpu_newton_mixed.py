@@ -86,6 +86,25 @@ def test_c1_newton_steps_converge_mixed_matches_fp64():
         c64, cm = n64, nm
 
 
+def test_fp64_lean_cycles_2d_match_reference_order():
+    """The FP64 Newton on the lean kernels (options.fuse_levels = 2) against
+    the FP64 Newton in the reference's expression order, 2D 64^2 config:
+    both converge, same FP64 fixed point to 1e-11."""
+    from mushy_gb300 import ops
+    g, prm, phi_bc, der, phi0, b = _c1()
+    dt = 1e-3
+    op = ops.NLMultiCompOp(g, prm, phi_bc, der, 1.0, -dt, None, [dev(x) for x in b])
+    out = []
+    for fuse in (1, 2):
+        o = _opts(abi.PREC_F64)
+        o.fuse_levels = fuse
+        new = dev(phi0)
+        st, rc = ops.AdjointMultiGrid(op, o).backwardEulerNewton(new, dev(phi0), dt)
+        assert rc == 0 and st.final_norm <= 1e-10 * st.initial_norm
+        out.append(host(new))
+    assert np.abs(out[1] - out[0]).max() <= 1e-11 * np.abs(out[0]).max()
+
+
 def test_c3_size_newton_step_mixed_matches_fp64():
     """One backward-Euler (H, C) step of the 1024x1024 mushy-layer
     configuration (CR=25, Le=200, liquid + 1e-3 noise, cold bottom,
@@ -146,8 +165,8 @@ def test_3d_newton_step_fused_sweep_bitwise_and_converged():
     from mushy_gb300 import ops
     g, phi0, op, ref, dt = _c4_like(64)
     out = {}
-    for key, prec, fuse in (("fused", abi.PREC_MIXED, 1), ("half", abi.PREC_MIXED, 0),
-                            ("fp64", abi.PREC_F64, 1)):
+    for key, prec, fuse in (("fused", abi.PREC_MIXED, 3), ("half", abi.PREC_MIXED, 1),
+                            ("fp64", abi.PREC_F64, 1), ("fp64_fast", abi.PREC_F64, 2)):
         o = _opts(prec)
         o.fuse_levels = fuse
         new = dev(phi0)
@@ -162,3 +181,5 @@ def test_3d_newton_step_fused_sweep_bitwise_and_converged():
     assert O.norm(O.nl_residual(ref, uf, phi0)) <= 1e-10 * r0 * 1.0001
     u64 = out["fp64"][0]
     assert np.abs(uf - u64).max() <= 1e-8 * np.abs(u64).max()
+    # the FP64 path on the lean kernels reaches the same FP64 solution
+    assert np.abs(out["fp64_fast"][0] - u64).max() <= 1e-11 * np.abs(u64).max()

@@ -179,9 +179,12 @@ def test_adjoint_norms_bitwise():
     o.tolerance, o.max_iter = 1e-12, 60
     A = ops.AdjointMultiGrid(op, o)
     st = abi.SolveStats()
-    d_y = dev(np.zeros_like(phi))
-    rc = abi.load().mlgpu_hc_adjoint_solve(A.h, ops._ptr(dev(phi)), ops._ptr(dev(gg)),
-                                           ops._ptr(d_y), C.byref(st))
+    # the device arrays are held for the whole call (a temporary passed
+    # straight to ops._ptr would be freed, and its block handed to the next
+    # tensor, before the library reads it)
+    d_phi, d_g, d_y = dev(phi), dev(gg), dev(np.zeros_like(phi))
+    rc = abi.load().mlgpu_hc_adjoint_solve(A.h, ops._ptr(d_phi), ops._ptr(d_g), ops._ptr(d_y),
+                                           C.byref(st))
     assert rc == rc_r
     _same_norms(st, st_r)
     exact(host(d_y), y_r)
