@@ -935,22 +935,38 @@ def config5(args, torch, abi, ops, O, P):
     fwd_its, adj_its = list(its["forward"]), list(its["adjoint"])
     rng = np.random.default_rng(5)
     h = 1e-6
-    rels = []
+    rels, dirs = [], []
     t0 = time.time()
+
+    def central(dk, dra, dtb, hh):
+        return (forward_only(logk + hh * dk, Ra + hh * dra, Tb + hh * dtb) -
+                forward_only(logk - hh * dk, Ra - hh * dra, Tb - hh * dtb)) / (2 * hh)
+
     for _ in range(8):
         dk = torch.from_numpy(rng.standard_normal(tuple(logk.shape))).cuda()
         dra = float(rng.standard_normal()) * Ra
         dtb = float(rng.standard_normal())
-        fd = (forward_only(logk + h * dk, Ra + h * dra, Tb + h * dtb) -
-              forward_only(logk - h * dk, Ra - h * dra, Tb - h * dtb)) / (2 * h)
+        fd = central(dk, dra, dtb, h)
         ad = float((gk * dk).sum()) + gra * dra + gtb * dtb
         rels.append(abs(ad - fd) / abs(fd))
+        dirs.append((dk, dra, dtb, ad))
+    # the direction furthest from the adjoint, central differences over a
+    # range of steps: truncation error falls as h^2, round-off grows as 1/h,
+    # and a switch of a cell's closure regime inside [-h, h] gives an O(1)
+    # jump in the third derivative that no step removes
+    worst = int(np.argmax(rels))
+    dk, dra, dtb, ad = dirs[worst]
+    sweep = []
+    for hh in (1e-4, 3e-5, 1e-5, 3e-6, 1e-6, 3e-7, 1e-7, 1e-8):
+        fd = central(dk, dra, dtb, hh)
+        sweep.append({"step": hh, "fd": fd, "rel_err": abs(ad - fd) / abs(fd)})
     fd_s = time.time() - t0
     return {"metric": "adjoint gradient of a 50-step 256^2 rollout: time and FD agreement",
             "value": ms_grad, "unit": "ms per gradient (forward + checkpointed backward)",
             "higher_is_better": False, "forward_ms": ms_fwd, "gradient_over_forward": ms_grad / ms_fwd,
             "objective": J0, "objective_in_gradient_run": J1,
             "fd_rel_err": {"max": max(rels), "per_direction": rels, "step": h},
+            "fd_step_sweep": {"direction": worst, "adjoint": dirs[worst][3], "steps": sweep},
             "dJ_dRa": gra, "dJ_dTb": gtb, "dJ_dlogk_abs_sum": float(gk.abs().sum()),
             "fd_wall_s": fd_s,
             "solves_in_gradient": {"forward_steps": len(fwd_its),

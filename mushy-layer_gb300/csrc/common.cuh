@@ -389,6 +389,26 @@ __device__ __forceinline__ bool colour_cell(const Geom &G, int pass, long long t
   return i < G.n0 && k < G.n2;
 }
 
+// Colour-split index of cell (i, j, k) on a level with an even n0: the cells
+// of colour (i + j + k) & 1 fill their own half of the array, row by row
+// (each row holds n0 / 2 cells of each colour), so a red/black half sweep
+// streams the data of its own colour only.
+__device__ __forceinline__ long long cs_index(const Geom &G, int i, int j, int k) {
+  return ((i + j + k) & 1) * (G.ncell >> 1) + ((long long)k * G.n1 + j) * (G.n0 >> 1) + (i >> 1);
+}
+
+// cell-array index functors (natural [k][j][i] order, or colour-split)
+struct NaturalIdx {
+  __device__ __forceinline__ long long operator()(const Geom &G, int i, int j, int k) const {
+    return G.cell(i, j, k);
+  }
+};
+struct SplitIdx {
+  __device__ __forceinline__ long long operator()(const Geom &G, int i, int j, int k) const {
+    return cs_index(G, i, j, k);
+  }
+};
+
 __host__ __device__ inline long long colour_threads(const Geom &G) {
   return (long long)((G.n0 + 1) / 2) * G.n1 * G.n2;
 }

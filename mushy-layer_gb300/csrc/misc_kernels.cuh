@@ -36,7 +36,7 @@ __global__ void __launch_bounds__(kBlock) restrict_avg_kernel(Geom F, Geom C, in
 // ---------------------------------------------------------------- prolong
 // Coarse value with the homogeneous ghost rule applied per direction:
 // periodic wrap, else clamp to the boundary cell and negate for Dirichlet.
-template <class T>
+template <class T, class IDX = NaturalIdx>
 __device__ __forceinline__ T coarse_at(const Geom &C, const BCD &bc, int comp,
                                        const T *__restrict__ a, const T *__restrict__ b,
                                        int I, int J, int K) {
@@ -56,7 +56,7 @@ __device__ __forceinline__ T coarse_at(const Geom &C, const BCD &bc, int comp,
       }
     }
   }
-  long long q = comp * C.ncell + C.cell(idx[0], idx[1], idx[2]);
+  long long q = comp * C.ncell + IDX()(C, idx[0], idx[1], idx[2]);
   T v = b ? (a[q] - b[q]) : a[q];
   return sign * v;
 }
@@ -67,28 +67,28 @@ __device__ __forceinline__ T coarse_at(const Geom &C, const BCD &bc, int comp,
 // formed on the fly from its two operands.
 // p + (P (a - b))(i, j, k) for component c: the prolongation increment of one
 // fine cell, arithmetic identical to prolong_one below.
-template <class T, int DIM, int KIND>
+template <class T, int DIM, int KIND, class IDX = NaturalIdx>
 __device__ __forceinline__ T prolong_add(const Geom &C, const BCD &bc, int c, int i, int j, int k,
                                          T p, const T *__restrict__ a, const T *__restrict__ b) {
   const T den = T(1) / (DIM == 3 ? T(64) : T(16));
   const T fx1 = T(3) * den, fx2 = T(9) * den, fx3 = T(27) * den, f0 = T(1) * den;
   int ic = i >> 1, jc = j >> 1, kc = DIM == 3 ? k >> 1 : 0;
-  if (KIND == MLGPU_PROLONG_CONSTANT) return p + coarse_at(C, bc, c, a, b, ic, jc, kc);
+  if (KIND == MLGPU_PROLONG_CONSTANT) return p + coarse_at<T, IDX>(C, bc, c, a, b, ic, jc, kc);
   int o1 = 2 * (i & 1) - 1, o2 = 2 * (j & 1) - 1, o3 = DIM == 3 ? 2 * (k & 1) - 1 : 0;
   if (DIM == 2) {
-    p = p + fx2 * coarse_at(C, bc, c, a, b, ic, jc, kc) +
-        f0 * coarse_at(C, bc, c, a, b, ic + o1, jc + o2, kc);
-    p = p + fx1 * (coarse_at(C, bc, c, a, b, ic + o1, jc, kc) +
-                   coarse_at(C, bc, c, a, b, ic, jc + o2, kc));
+    p = p + fx2 * coarse_at<T, IDX>(C, bc, c, a, b, ic, jc, kc) +
+        f0 * coarse_at<T, IDX>(C, bc, c, a, b, ic + o1, jc + o2, kc);
+    p = p + fx1 * (coarse_at<T, IDX>(C, bc, c, a, b, ic + o1, jc, kc) +
+                   coarse_at<T, IDX>(C, bc, c, a, b, ic, jc + o2, kc));
   } else {
-    p = p + fx3 * coarse_at(C, bc, c, a, b, ic, jc, kc) +
-        f0 * coarse_at(C, bc, c, a, b, ic + o1, jc + o2, kc + o3);
-    p = p + fx2 * (coarse_at(C, bc, c, a, b, ic + o1, jc, kc) +
-                   coarse_at(C, bc, c, a, b, ic, jc + o2, kc) +
-                   coarse_at(C, bc, c, a, b, ic, jc, kc + o3));
-    p = p + fx1 * (coarse_at(C, bc, c, a, b, ic + o1, jc + o2, kc) +
-                   coarse_at(C, bc, c, a, b, ic, jc + o2, kc + o3) +
-                   coarse_at(C, bc, c, a, b, ic + o1, jc, kc + o3));
+    p = p + fx3 * coarse_at<T, IDX>(C, bc, c, a, b, ic, jc, kc) +
+        f0 * coarse_at<T, IDX>(C, bc, c, a, b, ic + o1, jc + o2, kc + o3);
+    p = p + fx2 * (coarse_at<T, IDX>(C, bc, c, a, b, ic + o1, jc, kc) +
+                   coarse_at<T, IDX>(C, bc, c, a, b, ic, jc + o2, kc) +
+                   coarse_at<T, IDX>(C, bc, c, a, b, ic, jc, kc + o3));
+    p = p + fx1 * (coarse_at<T, IDX>(C, bc, c, a, b, ic + o1, jc + o2, kc) +
+                   coarse_at<T, IDX>(C, bc, c, a, b, ic, jc + o2, kc + o3) +
+                   coarse_at<T, IDX>(C, bc, c, a, b, ic + o1, jc, kc + o3));
   }
   return p;
 }

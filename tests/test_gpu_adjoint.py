@@ -221,3 +221,37 @@ def test_newton_driver_agrees_with_oracle():
     st, rc = A.newtonSolve(d_u, dev(phi))
     assert rc == rc_ref and abs(st.iterations - st_ref.iterations) <= 1
     assert np.abs(host(d_u) - u_ref).max() <= 1e-10 * np.abs(u_ref).max()
+
+
+def test_adjoint_workload_step_gradient_matches_oracle_256():
+    """The adjoint workload at its own size (256^2, the solidification model's
+    operator and first step): Newton's backward-Euler step forward on the
+    GPU, then the step's adjoint on the GPU and in the oracle from the same
+    converged state -- the multiplier, the old-state and source gradients
+    bit for bit, the wall-value gradient to 1e-12 (a sum in another order)."""
+    from mushy_gb300 import darcy_model as M, ops
+    model = M.DarcySolidification(256)
+    phi0 = M.initial_state(256, seed=5)
+    g, p, dt = model.grid, model.params, model.dt
+    o = ops.default_options(True)
+    o.tolerance, o.hang, o.max_iter = 1e-12, -1.0, 200
+    A = ops.AdjointMultiGrid(model.hop, o)
+    new = phi0.clone()
+    st_n, rc_n = A.backwardEulerNewton(new, phi0, dt)
+    assert rc_n in (0, abi.ERR_HANG) and st_n.final_norm <= 1e-10 * st_n.initial_norm
+    phi = host(new)
+    b = [host(x) for x in model.bcoef]
+    der = abi.make_bc({(1, 0, 0): (abi.BC_DIRICHLET, 0.5),
+                       (1, 1, 0): (abi.BC_DIRICHLET, model.T_top)})
+    ref = O.NLOpHost(g, p, abi.make_bc(), der, 1.0, -dt, None, b)
+    w = np.random.default_rng(55).standard_normal(phi.shape)
+    opts = O.default_options(1)
+    opts.tolerance, opts.hang, opts.max_iter = 1e-12, -1.0, 200
+    old_r, src_r, bcg_r, mu_r, st_r, rc_r = O.backward_euler_adjoint(ref, opts, phi, w, dt)
+    d_phi, d_w, mu = dev(phi), dev(w), dev(np.zeros_like(phi))
+    old, src, bcg, st, rc = A.backwardEulerAdjoint(d_phi, d_w, dt, mu)
+    assert rc == rc_r and st.iterations == st_r.iterations
+    exact(host(mu), mu_r)
+    exact(host(old), old_r)
+    exact(host(src), src_r)
+    assert np.abs(np.array(bcg) - bcg_r).max() <= 1e-12 * np.abs(bcg_r).max()
