@@ -130,7 +130,7 @@ class C4Runner:
             ho.tolerance, ho.hang, ho.max_iter, ho.precision = TOL, -1.0, 60, code
             if prec == "fp64_fast":
                 # Newton's cycles with the mixed path's kernels (lean update,
-                # fused 3D sweep) in FP64: the same design, FP64 data
+                # colour-split layout) in FP64: the same design, FP64 data
                 ho.fuse_levels = 2
             if use_graph is not None:
                 po.use_graph = ho.use_graph = use_graph
@@ -284,8 +284,8 @@ def run_gpu(args):
         "fp64_fast": {**C4Runner.summary(out_f), "value": upd_f * world / (ms_f * 1e-3),
                       "ms_per_step": ms_f / args.steps,
                       "note": "FP64 with the mixed path's kernel design (lean Jacobian "
-                              "update, fused 3D sweep) for Newton's cycles; projection "
-                              "as fp64",
+                              "update, colour-split layout) for Newton's cycles; "
+                              "projection as fp64",
                       "hc_rel_vs_fp64": hc_err_fast},
         "time_to_solution_ratio_fp64_over_mixed": ms_d / ms_m,
         "time_to_solution_ratio_fp64_fast_over_mixed": ms_f / ms_m,
@@ -427,16 +427,13 @@ def run_reference(args):
                 "d2h_bytes_per_step": 0}}))
 
 
-# Compulsory bytes per cell of the box of the Newton step's FP32 smoothing
-# launches (lin_lean_kernels.cuh):
-# * one red/black half sweep (lean_gsrb_kernel): the updated half of the
-#   cells read g (2 floats), K (4) and J (4) and write x (2) and w (2); every
-#   face coefficient is read once (3 directions x 2 components); the other
-#   half's w is read once (2 floats each): (5 + 6 + 1 + 2) floats = 56 B;
-# * one fused red + black sweep (lean_sweep3_kernel): every cell's g, K, J
-#   (10 floats), the faces (6), w in (2), x and w out (4): 22 floats = 88 B.
+# Compulsory bytes per cell of the box of one FP32 red/black half sweep of
+# the Newton step's cycles (lean_gsrb_kernel, colour-split arrays): the
+# updated half of the cells read g (2 floats), K (4) and J (4) and write x (2)
+# and w (2); every face coefficient is read once (3 directions x 2
+# components); the other half's w is read once (2 floats each):
+# (7 + 6 + 1) floats = 56 B per cell of the box.
 LEAN_HALF_SWEEP_BYTES_PER_CELL = 56
-LEAN_SWEEP_BYTES_PER_CELL = 88
 LEAN_SWEEP_PROFILE = os.path.join(PROFILES, "lean_gsrb_kernel_256cubed.md")
 
 

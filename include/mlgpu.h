@@ -480,9 +480,9 @@ int mlgpu_hc_newton_solve(mlgpu_solver *S, double *phi, const double *rhs,
 /* Measurement: device time (ms per launch, host double) of `reps` FP32
  * smoothing launches on the finest level of a mixed-precision Newton solver,
  * at the state of its last step, timed with CUDA events on the solver's
- * stream: kind 0 = red/black half sweep, 1 = fused red + black sweep (3D
- * levels of at least 32^3 with walls in z, options.fuse_levels >= 3; else
- * MLGPU_ERR_ARG).  No counterpart in the reference. */
+ * stream: kind 0 = red/black half sweep (colours alternating), the only kind;
+ * MLGPU_ERR_ARG for another kind or a finest level that is also the bottom.
+ * No counterpart in the reference. */
 int mlgpu_hc_newton_sweep_time(mlgpu_solver *S, int kind, int reps, double *ms_per_launch);
 /* mlgpu_hc_backward_euler with the Newton solve of `S` (an adjoint solver). */
 int mlgpu_hc_backward_euler_newton(mlgpu_solver *S, double *phi_new, const double *phi_old,

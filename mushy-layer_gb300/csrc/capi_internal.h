@@ -83,8 +83,6 @@ cudaError_t launch_hcm_update(long long n, double *u, const float *e, cudaStream
 template <class S>
 cudaError_t launch_vc_bicgstab(const VCArgs<double> &A, S *e, const S *rhs, double *ws,
                                int imax, int remove_mean, cudaStream_t s);
-cudaError_t launch_newton_step(long long n, double *u, const double *u_old, double scale,
-                               const float *e, cudaStream_t s);
 // FP32 Jacobian cycles of the mixed-precision Newton solve (launch_f32_adj.cu)
 cudaError_t launch_adj_jac(const Geom &G, const ClosureParams &cp, const double *u, float *J,
                            cudaStream_t s);
@@ -97,20 +95,25 @@ cudaError_t launch_adj_relax_block(const AdjArgs<float> &A, float *y, const floa
                                    int zero, cudaStream_t s, bool tr);
 cudaError_t launch_adj_minv(const AdjArgs<float> &A, const float *zero, float *Minv, float *D,
                             cudaStream_t s);
-// lean cycles of the Newton step (lin_lean_kernels.cuh); T = float or double
+// lean cycles of the Newton step (lin_lean_kernels.cuh); T = float or double;
+// fine-level arrays colour-split, the coarse level's split when csplit
 template <class T>
 cudaError_t launch_lean_gsrb(const LinLeanT<T> &P, int pass, cudaStream_t s);
 template <class T>
-cudaError_t launch_lean_residual(const LinLeanT<T> &P, int norm, T *out, double *part,
+cudaError_t launch_lean_residual(const LinLeanT<T> &P, int split, int norm, double *part,
                                  int *nparts, cudaStream_t s);
 template <class T>
-cudaError_t launch_lean_restrict(const LinLeanT<T> &P, const Geom &C, T *gc, T *xc, T *wc,
-                                 cudaStream_t s);
+cudaError_t launch_lean_restrict(const LinLeanT<T> &P, const Geom &C, int csplit, T *gc, T *xc,
+                                 T *wc, cudaStream_t s);
 template <class T>
-cudaError_t launch_lean_prolong(const LinLeanT<T> &P, const Geom &C, int kind, const T *xc,
-                                cudaStream_t s);
+cudaError_t launch_lean_prolong(const LinLeanT<T> &P, const Geom &C, int csplit, int kind,
+                                const T *xc, cudaStream_t s);
+template <class T, class S>
+cudaError_t launch_lean_pack(const Geom &G, int split, int ncomp, const S *src, T *dst,
+                             cudaStream_t s);
 template <class T>
-cudaError_t launch_lean_sweep3(const LeanSweep3T<T> &S, cudaStream_t s);
+cudaError_t launch_lean_step(const Geom &G, int split, double *u, const double *u_old,
+                             double scale, const T *e, cudaStream_t s);
 cudaError_t launch_adj_bottom_direct(const AdjArgs<float> &A, float *y, const float *g,
                                      cudaStream_t s, bool tr);
 cudaError_t launch_adj_restrict(const AdjArgs<float> &A, const Geom &C, const float *y,

@@ -397,15 +397,36 @@ __device__ __forceinline__ long long cs_index(const Geom &G, int i, int j, int k
   return ((i + j + k) & 1) * (G.ncell >> 1) + ((long long)k * G.n1 + j) * (G.n0 >> 1) + (i >> 1);
 }
 
-// cell-array index functors (natural [k][j][i] order, or colour-split)
+// (i, j, k) of colour-split index t (colour c = t >= n/2) on a level with an
+// even n0: the inverse of cs_index
+__device__ __forceinline__ void cs_cell(const Geom &G, long long t, int &i, int &j, int &k) {
+  const unsigned half = (unsigned)(G.ncell >> 1), h0 = (unsigned)(G.n0 >> 1);
+  unsigned u = (unsigned)t;
+  const unsigned c = u >= half ? 1u : 0u;
+  u -= c * half;
+  const unsigned row = u / h0;
+  const unsigned kk = row / (unsigned)G.n1;
+  j = (int)(row - kk * (unsigned)G.n1);
+  k = (int)kk;
+  i = 2 * (int)(u - row * h0) + (int)(((unsigned)(j + k) + c) & 1u);
+}
+
+// cell-array index functors (natural [k][j][i] order, or colour-split):
+// index of a cell, and the cell of an index
 struct NaturalIdx {
   __device__ __forceinline__ long long operator()(const Geom &G, int i, int j, int k) const {
     return G.cell(i, j, k);
+  }
+  static __device__ __forceinline__ void ijk(const Geom &G, long long q, int &i, int &j, int &k) {
+    cell_ijk(G, q, i, j, k);
   }
 };
 struct SplitIdx {
   __device__ __forceinline__ long long operator()(const Geom &G, int i, int j, int k) const {
     return cs_index(G, i, j, k);
+  }
+  static __device__ __forceinline__ void ijk(const Geom &G, long long q, int &i, int &j, int &k) {
+    cs_cell(G, q, i, j, k);
   }
 };
 

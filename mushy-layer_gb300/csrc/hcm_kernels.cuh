@@ -192,14 +192,6 @@ __global__ void __launch_bounds__(kBlock) hcm_update_kernel(long long n, double 
                                                             const float *__restrict__ e) {
   for (long long q = gtid(); q < n; q += gstride()) u[q] = u[q] + (double)e[q];
 }
-
-// u = u_old + scale e (a Newton step with an FP32 correction, step halving)
-__global__ void __launch_bounds__(kBlock) newton_step_kernel(long long n, double *__restrict__ u,
-                                                             const double *__restrict__ u_old,
-                                                             double scale,
-                                                             const float *__restrict__ e) {
-  for (long long q = gtid(); q < n; q += gstride()) u[q] = u_old[q] + scale * (double)e[q];
-}
 #endif  // MLGPU_FP64_UNIT
 
 }  // namespace mlgpu

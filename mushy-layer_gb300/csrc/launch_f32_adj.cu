@@ -80,58 +80,98 @@ cudaError_t launch_adj_restrict(const AdjArgs<float> &A, const Geom &C, const fl
 // mixed-precision solve and FP64 for the comparison path built the same way
 template <class T>
 cudaError_t launch_lean_gsrb(const LinLeanT<T> &P, int pass, cudaStream_t s) {
-  MLGPU_DIM_SWITCH(P.G.dim, (lean_gsrb_kernel<T, DIM><<<blocks_for(colour_threads(P.G)), kBlock, 0, s>>>(P, pass)));
+  MLGPU_DIM_SWITCH(P.G.dim, (lean_gsrb_kernel<T, DIM><<<blocks_for(P.G.ncell >> 1), kBlock, 0, s>>>(P, pass)));
   return cudaGetLastError();
 }
 
 template <class T>
-cudaError_t launch_lean_residual(const LinLeanT<T> &P, int norm, T *out, double *part,
+cudaError_t launch_lean_residual(const LinLeanT<T> &P, int split, int norm, double *part,
                                  int *nparts, cudaStream_t s) {
   const int nb = blocks_for(P.G.ncell);
   if (nparts) *nparts = nb;
   if (norm < 0) norm = MLGPU_NORM_MAX;
-  MLGPU_DIM_SWITCH(P.G.dim, MLGPU_NORM_SWITCH(norm, {
-    if (NORM >= 0) lean_residual_kernel<T, DIM, (NORM < 0 ? 0 : NORM)><<<nb, kBlock, 0, s>>>(P, out, part);
-  }));
+#define MLGPU_LEAN_RES(IDX)                                                                  \
+  MLGPU_DIM_SWITCH(P.G.dim, MLGPU_NORM_SWITCH(norm, {                                        \
+    if (NORM >= 0)                                                                           \
+      lean_residual_kernel<T, DIM, (NORM < 0 ? 0 : NORM), IDX><<<nb, kBlock, 0, s>>>(P, part); \
+  }))
+  if (split)
+    MLGPU_LEAN_RES(SplitIdx);
+  else
+    MLGPU_LEAN_RES(NaturalIdx);
+#undef MLGPU_LEAN_RES
   return cudaGetLastError();
 }
 
 template <class T>
-cudaError_t launch_lean_restrict(const LinLeanT<T> &P, const Geom &C, T *gc, T *xc, T *wc,
-                                 cudaStream_t s) {
-  MLGPU_DIM_SWITCH(P.G.dim, (lean_restrict_kernel<T, DIM><<<blocks_for(C.ncell), kBlock, 0, s>>>(P, C, gc, xc, wc)));
-  return cudaGetLastError();
-}
-
-template <class T>
-cudaError_t launch_lean_prolong(const LinLeanT<T> &P, const Geom &C, int kind, const T *xc,
-                                cudaStream_t s) {
-  if (kind == MLGPU_PROLONG_LINEAR) {
-    MLGPU_DIM_SWITCH(P.G.dim, (lean_prolong_kernel<T, DIM, MLGPU_PROLONG_LINEAR><<<blocks_for(P.G.ncell), kBlock, 0, s>>>(P, C, xc)));
+cudaError_t launch_lean_restrict(const LinLeanT<T> &P, const Geom &C, int csplit, T *gc, T *xc,
+                                 T *wc, cudaStream_t s) {
+  const int nb = blocks_for(C.ncell);
+  if (csplit) {
+    MLGPU_DIM_SWITCH(P.G.dim, (lean_restrict_kernel<T, DIM, SplitIdx><<<nb, kBlock, 0, s>>>(P, C, gc, xc, wc)));
   } else {
-    MLGPU_DIM_SWITCH(P.G.dim, (lean_prolong_kernel<T, DIM, MLGPU_PROLONG_CONSTANT><<<blocks_for(P.G.ncell), kBlock, 0, s>>>(P, C, xc)));
+    MLGPU_DIM_SWITCH(P.G.dim, (lean_restrict_kernel<T, DIM, NaturalIdx><<<nb, kBlock, 0, s>>>(P, C, gc, xc, wc)));
   }
   return cudaGetLastError();
 }
 
 template <class T>
-cudaError_t launch_lean_sweep3(const LeanSweep3T<T> &S, cudaStream_t s) {
-  if (S.P.G.dim != 3 || S.P.G.per2) return cudaErrorInvalidValue;
-  const int nb = S.ntx * S.nty * S.nchunk;
-  lean_sweep3_kernel<T><<<nb, kZMThreads, 0, s>>>(S);
+cudaError_t launch_lean_prolong(const LinLeanT<T> &P, const Geom &C, int csplit, int kind,
+                                const T *xc, cudaStream_t s) {
+  const int nb = blocks_for(P.G.ncell);
+#define MLGPU_LEAN_PRO(KIND, IDX) \
+  MLGPU_DIM_SWITCH(P.G.dim, (lean_prolong_kernel<T, DIM, KIND, IDX><<<nb, kBlock, 0, s>>>(P, C, xc)))
+  if (kind == MLGPU_PROLONG_LINEAR) {
+    if (csplit)
+      MLGPU_LEAN_PRO(MLGPU_PROLONG_LINEAR, SplitIdx);
+    else
+      MLGPU_LEAN_PRO(MLGPU_PROLONG_LINEAR, NaturalIdx);
+  } else {
+    if (csplit)
+      MLGPU_LEAN_PRO(MLGPU_PROLONG_CONSTANT, SplitIdx);
+    else
+      MLGPU_LEAN_PRO(MLGPU_PROLONG_CONSTANT, NaturalIdx);
+  }
+#undef MLGPU_LEAN_PRO
+  return cudaGetLastError();
+}
+
+template <class T, class S>
+cudaError_t launch_lean_pack(const Geom &G, int split, int ncomp, const S *src, T *dst,
+                             cudaStream_t s) {
+  if (split)
+    lean_pack_kernel<T, S, SplitIdx><<<blocks_for(G.ncell), kBlock, 0, s>>>(G, ncomp, src, dst);
+  else
+    lean_pack_kernel<T, S, NaturalIdx><<<blocks_for(G.ncell), kBlock, 0, s>>>(G, ncomp, src, dst);
+  return cudaGetLastError();
+}
+
+template <class T>
+cudaError_t launch_lean_step(const Geom &G, int split, double *u, const double *u_old,
+                             double scale, const T *e, cudaStream_t s) {
+  if (split)
+    lean_step_kernel<T, SplitIdx><<<blocks_for(G.ncell), kBlock, 0, s>>>(G, u, u_old, scale, e);
+  else
+    lean_step_kernel<T, NaturalIdx><<<blocks_for(G.ncell), kBlock, 0, s>>>(G, u, u_old, scale, e);
   return cudaGetLastError();
 }
 
 #define MLGPU_LEAN_INST(T)                                                                     \
   template cudaError_t launch_lean_gsrb<T>(const LinLeanT<T> &, int, cudaStream_t);           \
-  template cudaError_t launch_lean_residual<T>(const LinLeanT<T> &, int, T *, double *, int *, \
+  template cudaError_t launch_lean_residual<T>(const LinLeanT<T> &, int, int, double *, int *, \
                                               cudaStream_t);                                  \
-  template cudaError_t launch_lean_restrict<T>(const LinLeanT<T> &, const Geom &, T *, T *,    \
-                                              T *, cudaStream_t);                             \
-  template cudaError_t launch_lean_prolong<T>(const LinLeanT<T> &, const Geom &, int,          \
+  template cudaError_t launch_lean_restrict<T>(const LinLeanT<T> &, const Geom &, int, T *,    \
+                                              T *, T *, cudaStream_t);                        \
+  template cudaError_t launch_lean_prolong<T>(const LinLeanT<T> &, const Geom &, int, int,     \
                                              const T *, cudaStream_t);                        \
-  template cudaError_t launch_lean_sweep3<T>(const LeanSweep3T<T> &, cudaStream_t);
+  template cudaError_t launch_lean_pack<T, double>(const Geom &, int, int, const double *, T *, \
+                                                  cudaStream_t);                              \
+  template cudaError_t launch_lean_step<T>(const Geom &, int, double *, const double *, double, \
+                                          const T *, cudaStream_t);
 MLGPU_LEAN_INST(float)
 MLGPU_LEAN_INST(double)
+template cudaError_t launch_lean_pack<float, float>(const Geom &, int, int, const float *,
+                                                    float *, cudaStream_t);
+#undef MLGPU_LEAN_INST
 
 }  // namespace mlgpu

@@ -63,11 +63,6 @@ cudaError_t launch_hcm_update(long long n, double *u, const float *e, cudaStream
   hcm_update_kernel<<<blocks_for(n), kBlock, 0, s>>>(n, u, e);
   return cudaGetLastError();
 }
-cudaError_t launch_newton_step(long long n, double *u, const double *u_old, double scale,
-                               const float *e, cudaStream_t s) {
-  newton_step_kernel<<<blocks_for(n), kBlock, 0, s>>>(n, u, u_old, scale, e);
-  return cudaGetLastError();
-}
 
 cudaError_t launch_outer_coefs(const VCArgs<double> &A, double *cx, double *cy, double *diag,
                                cudaStream_t s) {

@@ -1217,12 +1217,14 @@ struct AdjLevel {
   Coefs<float> c32;
   float *J32 = nullptr, *Minv32 = nullptr, *y32 = nullptr, *g32 = nullptr, *r32 = nullptr;
   float *D32 = nullptr, *w32 = nullptr;  // diagonal blocks of A, and w = J y (lean cycles)
-  // second (y, w) of the fused 3D sweeps, which read one pair and write the
-  // other; between smoothing calls the values are always in (y32, w32)
-  float *y32b = nullptr, *w32b = nullptr;
-  // FP64 lean cycles (the comparison path): w = J y, A's diagonal blocks, the
-  // fused sweeps' second pair
-  double *w64 = nullptr, *D64 = nullptr, *y64b = nullptr, *w64b = nullptr;
+  // FP64 lean cycles (the comparison path): w = J y, A's diagonal blocks, and
+  // on level 0 the right-hand side in the lean layout
+  double *w64 = nullptr, *D64 = nullptr, *g64s = nullptr;
+  // lean cycles on a smoothed level (every level above the bottom): J,
+  // K = (D^T)^-1 and D permuted to the colour-split layout, in the cycles'
+  // precision (the natural ones above feed the bottom solve and the packing)
+  float *J32s = nullptr, *K32s = nullptr, *D32s = nullptr;
+  double *J64s = nullptr, *K64s = nullptr, *D64s = nullptr;
 };
 
 class HCAdjSolver : public mlgpu_solver {
@@ -1241,9 +1243,9 @@ class HCAdjSolver : public mlgpu_solver {
   // adjoint solve stays FP64
   bool mixed = false;
   // FP64 with options.fuse_levels >= 2: Newton's linear cycles run the lean
-  // kernels (and the fused 3D sweep) in FP64 -- the same design as the mixed
-  // cycles, the reference's expression order given up -- the comparison
-  // path for the mixed-precision speed-up
+  // kernels in FP64 -- the same design and layout as the mixed cycles, the
+  // reference's expression order given up -- the comparison path for the
+  // mixed-precision speed-up
   bool fast64 = false;
   cudaGraphExec_t graph = nullptr, graph_lin = nullptr, graph_lin32 = nullptr;
   double *nf = nullptr, *nuold = nullptr;  // Newton: rhs of N(u) = f, previous u
@@ -1263,18 +1265,9 @@ class HCAdjSolver : public mlgpu_solver {
   }
 
   bool lin32() const { return mixed && !tr; }
-
-  // levels the fused red + black sweep (lean_sweep3_kernel) takes when the
-  // options' fuse_levels is 3 or more: 3D, at least 32 cells each way, walls
-  // in z, periodic x / y only with an even count (a red/black colouring
-  // consistent across the seam).  Off by default: it reads the compulsory
-  // bytes once but, latency-bound, runs slower than the two half sweeps.
-  static bool fused_ok(const Geom &G) {
-    if (G.dim != 3 || G.per2) return false;
-    if (G.n0 < 32 || G.n1 < 32 || G.n2 < 32) return false;
-    if ((G.per0 && (G.n0 & 1)) || (G.per1 && (G.n1 & 1))) return false;
-    return true;
-  }
+  // the lean cycles' arrays of level l are colour-split on every smoothed
+  // level (all but the bottom, whose dimensions are then all even)
+  bool split(int l) const { return l < (int)L.size() - 1; }
 
   size_t layout(char *base) {
     Arena A;
@@ -1309,19 +1302,22 @@ class HCAdjSolver : public mlgpu_solver {
         L[l].D32 = A.get<float>(2 * n);
         L[l].y32 = A.get<float>(n);
         L[l].w32 = A.get<float>(n);
-        if (o.fuse_levels >= 3 && fused_ok(make_geom(g))) {
-          L[l].y32b = A.get<float>(n);
-          L[l].w32b = A.get<float>(n);
-        }
         L[l].g32 = A.get<float>(n);
         L[l].r32 = A.get<float>(n);
+        if (l < depth) {
+          L[l].J32s = A.get<float>(2 * n);
+          L[l].K32s = A.get<float>(2 * n);
+          L[l].D32s = A.get<float>(2 * n);
+        }
       }
       if (fast64) {
         L[l].w64 = A.get<double>(n);
         L[l].D64 = A.get<double>(2 * n);
-        if (o.fuse_levels >= 3 && fused_ok(make_geom(g))) {
-          L[l].y64b = A.get<double>(n);
-          L[l].w64b = A.get<double>(n);
+        if (l == 0) L[l].g64s = A.get<double>(n);
+        if (l < depth) {
+          L[l].J64s = A.get<double>(2 * n);
+          L[l].K64s = A.get<double>(2 * n);
+          L[l].D64s = A.get<double>(2 * n);
         }
       }
       g = coarsen_grid(g);
@@ -1390,7 +1386,9 @@ class HCAdjSolver : public mlgpu_solver {
   }
 
   // lean operator of level l (lin_lean_kernels.cuh): FP32 arrays for the
-  // mixed-precision cycles, FP64 ones for the FP64 comparison path
+  // mixed-precision cycles, FP64 ones for the FP64 comparison path; the
+  // split copies of J, K, D on a smoothed level, the natural ones on the
+  // bottom (x and g hold whichever layout the level's kernels use)
   template <class T>
   LinLeanT<T> leanT(int l) {
     const AdjArgs<double> D = args(l);
@@ -1398,35 +1396,27 @@ class HCAdjSolver : public mlgpu_solver {
     P.G = D.G;
     P.ybc = ybc();
     P.bdx = (T)(D.beta * D.dxinv);
+    const bool sp = split(l);
     if constexpr (sizeof(T) == 4) {
       for (int d = 0; d < 3; d++) P.b[d] = L[l].c32.b[d];
-      P.J = L[l].J32;
-      P.K = L[l].Minv32;
-      P.D = L[l].D32;
+      P.J = sp ? L[l].J32s : L[l].J32;
+      P.K = sp ? L[l].K32s : L[l].Minv32;
+      P.D = sp ? L[l].D32s : L[l].D32;
       P.x = L[l].y32;
       P.w = L[l].w32;
       P.g = L[l].g32;
     } else {
       for (int d = 0; d < 3; d++) P.b[d] = L[l].c64.b[d];
-      P.J = L[l].J;
-      P.K = L[l].Minv;
-      P.D = L[l].D64;
+      P.J = sp ? L[l].J64s : L[l].J;
+      P.K = sp ? L[l].K64s : L[l].Minv;
+      P.D = sp ? L[l].D64s : L[l].D64;
       P.x = L[l].y;
       P.w = L[l].w64;
-      P.g = L[l].g;
+      P.g = l == 0 ? L[l].g64s : L[l].g;
     }
     return P;
   }
   LinLean lean(int l) { return leanT<float>(l); }
-  // second (y, w) pair of the fused sweeps, or null
-  template <class T>
-  T *yb(int l) {
-    if constexpr (sizeof(T) == 4) return L[l].y32b; else return L[l].y64b;
-  }
-  template <class T>
-  T *wb(int l) {
-    if constexpr (sizeof(T) == 4) return L[l].w32b; else return L[l].w64b;
-  }
 
   // the wall rule of the adjoint variable in the prolongation
   BCD ybc() const { return make_bcd(op.apply_derived_bc ? op.derived_bc : op.phi_bc); }
@@ -1443,20 +1433,31 @@ class HCAdjSolver : public mlgpu_solver {
       CK(launch_restrict_avg<double>(L[l - 1].G, 2, L[l - 1].u, L[l].u, s));
     const ClosureParams cp = make_cp(op.params);
     if (lin32()) {
-      // FP64 closure derivative stored in FP32; the inverse blocks in FP32
+      // FP64 closure derivative stored in FP32; the inverse blocks in FP32;
+      // the smoothed levels' copies packed to the split layout
       for (auto &lv : L) CK(launch_adj_jac(lv.G, cp, lv.u, lv.J32, s));
       for (size_t l = 0; l < L.size(); l++) {
-        CK(cudaMemsetAsync(L[l].r32, 0, sizeof(float) * 2 * L[l].G.ncell, s));
-        CK(launch_adj_minv(args32((int)l), L[l].r32, L[l].Minv32, L[l].D32, s));
+        AdjLevel &lv = L[l];
+        CK(cudaMemsetAsync(lv.r32, 0, sizeof(float) * 2 * lv.G.ncell, s));
+        CK(launch_adj_minv(args32((int)l), lv.r32, lv.Minv32, lv.D32, s));
+        if (!split((int)l)) continue;
+        CK(launch_lean_pack<float, float>(lv.G, 1, 4, lv.J32, lv.J32s, s));
+        CK(launch_lean_pack<float, float>(lv.G, 1, 4, lv.Minv32, lv.K32s, s));
+        CK(launch_lean_pack<float, float>(lv.G, 1, 4, lv.D32, lv.D32s, s));
       }
       return MLGPU_OK;
     }
+    const bool lean64 = fast64 && !tr;
     for (auto &lv : L) CK(launch_adj_jac(lv.G, cp, lv.u, lv.J, s));
     // the smoother's inverse diagonal blocks (r is free here: a zero field)
     for (size_t l = 0; l < L.size(); l++) {
-      CK(cudaMemsetAsync(L[l].r, 0, sizeof(double) * 2 * L[l].G.ncell, s));
-      CK(launch_adj_minv(args((int)l), L[l].r, L[l].Minv, (fast64 && !tr) ? L[l].D64 : nullptr,
-                         s));
+      AdjLevel &lv = L[l];
+      CK(cudaMemsetAsync(lv.r, 0, sizeof(double) * 2 * lv.G.ncell, s));
+      CK(launch_adj_minv(args((int)l), lv.r, lv.Minv, lean64 ? lv.D64 : nullptr, s));
+      if (!lean64 || !split((int)l)) continue;
+      CK(launch_lean_pack<double, double>(lv.G, 1, 4, lv.J, lv.J64s, s));
+      CK(launch_lean_pack<double, double>(lv.G, 1, 4, lv.Minv, lv.K64s, s));
+      CK(launch_lean_pack<double, double>(lv.G, 1, 4, lv.D64, lv.D64s, s));
     }
     return MLGPU_OK;
   }
@@ -1500,43 +1501,19 @@ class HCAdjSolver : public mlgpu_solver {
     return MLGPU_OK;
   }
 
-  // ---- FP32 cycles on A (mixed-precision Newton); same structure as the
-  // FP64 ones above
   // ---- lean cycles on A (Newton's linear solve): FP32 in mixed precision,
   // FP64 on the comparison path built the same way; same structure as the
   // generic cycles above.  They keep w = J y next to y on every level: zero
-  // together, refreshed by every update and by the prolongation.
-  // Smoothing: an even number of fused sweeps (ping-pong, ending back in the
-  // level's (y, w), so every captured cycle starts from the same buffers),
-  // the rest as in-place half sweeps.
+  // together, refreshed by every update and by the prolongation.  Smoothed
+  // levels hold their arrays colour-split; each red/black half sweep is one
+  // launch over its colour's contiguous half.
   template <class T>
   int lin_smooth(int l, int n) {
     const LinLeanT<T> P = leanT<T>(l);
-    const int nf = yb<T>(l) ? n - (n & 1) : 0;
-    for (int i = 0; i < nf; i++) CK(launch_lean_sweep3<T>(fusedT<T>(l, i & 1), s));
-    for (int i = nf; i < n; i++)
+    for (int i = 0; i < n; i++)
       for (int pass = 0; pass < 2; pass++) CK(launch_lean_gsrb<T>(P, pass, s));
     return MLGPU_OK;
   }
-
-  // fused sweep of level l reading pair `from` (0: the level's y, w; 1: the
-  // second pair)
-  template <class T>
-  LeanSweep3T<T> fusedT(int l, int from) {
-    LeanSweep3T<T> S;
-    S.P = leanT<T>(l);
-    T *y0 = S.P.x, *w0 = S.P.w;
-    S.P.x = from ? yb<T>(l) : y0;
-    S.P.w = from ? wb<T>(l) : w0;
-    S.x_out = from ? y0 : yb<T>(l);
-    S.w_out = from ? w0 : wb<T>(l);
-    const Geom &G = L[l].G;
-    S.ntx = (G.n0 + kZMTX - 1) / kZMTX;
-    S.nty = (G.n1 + kZMTY - 1) / kZMTY;
-    S.nchunk = (G.n2 + kZMChunk - 1) / kZMChunk;
-    return S;
-  }
-  LeanSweep3 fused(int l, int from) { return fusedT<float>(l, from); }
 
   template <class T>
   int lin_cycle(int l) {
@@ -1563,7 +1540,7 @@ class HCAdjSolver : public mlgpu_solver {
     int rc = lin_smooth<T>(l, o.num_smooth_down);
     if (rc) return rc;
     const LinLeanT<T> C = leanT<T>(l + 1);
-    CK(launch_lean_restrict<T>(P, C.G, (T *)C.g, C.x, C.w, s));
+    CK(launch_lean_restrict<T>(P, C.G, split(l + 1), (T *)C.g, C.x, C.w, s));
     for (int m = 0; m < o.num_mg; m++) {
       if (m > 0) {  // every coarse visit starts from zero
         CK(cudaMemsetAsync(C.x, 0, sizeof(T) * 2 * C.G.ncell, s));
@@ -1572,7 +1549,7 @@ class HCAdjSolver : public mlgpu_solver {
       rc = lin_cycle<T>(l + 1);
       if (rc) return rc;
     }
-    CK(launch_lean_prolong<T>(P, C.G, o.prolong, C.x, s));
+    CK(launch_lean_prolong<T>(P, C.G, split(l + 1), o.prolong, C.x, s));
     return lin_smooth<T>(l, o.num_smooth_up);
   }
 
@@ -1580,7 +1557,7 @@ class HCAdjSolver : public mlgpu_solver {
   template <class T>
   int lin_residual_norm() {
     int nparts = 0;
-    CK(launch_lean_residual<T>(leanT<T>(0), o.norm_type, nullptr, part, &nparts, s));
+    CK(launch_lean_residual<T>(leanT<T>(0), split(0), o.norm_type, part, &nparts, s));
     CK(launch_finalize_norm(o.norm_type, part, nparts, part + kMaxBlocks, s));
     CK(cudaMemcpyAsync(host_norm, part + kMaxBlocks, sizeof(double), cudaMemcpyDeviceToHost, s));
     return MLGPU_OK;
@@ -1690,11 +1667,12 @@ class HCAdjSolver : public mlgpu_solver {
       if (rc) return rc;
       // linear solve A d = r, d in L[0].y (FP64) or L[0].y32 (mixed) from zero
       if (mixed) {
-        CK(launch_convert<float, double>(n2, L[0].g32, L[0].g, s));
+        CK(launch_lean_pack<float, double>(L[0].G, split(0), 2, L[0].g, L[0].g32, s));
         CK(cudaMemsetAsync(L[0].y32, 0, sizeof(float) * n2, s));
         CK(cudaMemsetAsync(L[0].w32, 0, sizeof(float) * n2, s));
         rc = residual_norm32();
       } else if (fast64) {
+        CK(launch_lean_pack<double, double>(L[0].G, split(0), 2, L[0].g, L[0].g64s, s));
         CK(cudaMemsetAsync(L[0].y, 0, bytes, s));
         CK(cudaMemsetAsync(L[0].w64, 0, bytes, s));
         rc = lin_residual_norm<double>();
@@ -1703,7 +1681,7 @@ class HCAdjSolver : public mlgpu_solver {
         rc = residual_norm();
       }
       if (rc) return rc;
-      st->kernel_launches += nk_state + nk_res + (mixed ? 1 : 0);
+      st->kernel_launches += nk_state + nk_res + (mixed || fast64 ? 1 : 0);
       CK(cudaStreamSynchronize(s));
       const double l0 = *host_norm;
       for (int c = 0; c < lin_max && *host_norm > lin_tol * l0; c++) {
@@ -1719,7 +1697,9 @@ class HCAdjSolver : public mlgpu_solver {
       for (int h = 0; h <= 4; h++) {
         // u = u_old + scale d
         if (mixed) {
-          CK(launch_newton_step(n2, L[0].u, nuold, scale, L[0].y32, s));
+          CK(launch_lean_step<float>(L[0].G, split(0), L[0].u, nuold, scale, L[0].y32, s));
+        } else if (fast64) {
+          CK(launch_lean_step<double>(L[0].G, split(0), L[0].u, nuold, scale, L[0].y, s));
         } else {
           CK(cudaMemcpyAsync(L[0].u, nuold, bytes, cudaMemcpyDeviceToDevice, s));
           CK(launch_axpby<double>(n2, scale, L[0].y, 1.0, L[0].u, s));
@@ -1758,10 +1738,10 @@ class HCAdjSolver : public mlgpu_solver {
   // Device time of the lean red/black half sweep on the finest level, at the
   // state and right-hand side of the last mixed-precision Newton step: `reps`
   // launches, passes alternating, between two events on the solver's stream
-  // (y and w of the finest level are scratch between Newton steps).
+  // (y and w of the finest level are scratch between Newton steps).  `kind`
+  // 0 is the only kind; the finest level must be a smoothed one.
   int time_lean_sweep(int kind, int reps, double *ms_per_launch) {
-    if (!mixed || reps < 1 || !ms_per_launch) return MLGPU_ERR_ARG;
-    if (kind != 0 && (kind != 1 || !L[0].y32b)) return MLGPU_ERR_ARG;
+    if (!mixed || reps < 1 || !ms_per_launch || kind != 0 || !split(0)) return MLGPU_ERR_ARG;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     cudaGetLastError();
     if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
@@ -1770,9 +1750,7 @@ class HCAdjSolver : public mlgpu_solver {
     }
     int rc = enter();
     const LinLean P = lean(0);
-    auto one = [&](int i) {
-      return kind ? launch_lean_sweep3(fused(0, i & 1), s) : launch_lean_gsrb(P, i & 1, s);
-    };
+    auto one = [&](int i) { return launch_lean_gsrb(P, i & 1, s); };
     if (!rc && one(0) != cudaSuccess) rc = MLGPU_ERR_CUDA;  // warm
     if (!rc && cudaEventRecord(e0, s) != cudaSuccess) rc = MLGPU_ERR_CUDA;
     for (int i = 0; i < reps && !rc; i++)
