@@ -162,6 +162,9 @@ class C4Runner:
                 "hc": {"rc": rch, "newton_iterations": sth.iterations,
                        "linear_cycles": sth.cycles,
                        "final_rel_residual": sth.final_norm / sth.initial_norm,
+                       "rel_residual_history": [
+                           sth.norm_history[q] / sth.initial_norm
+                           for q in range(min(sth.iterations + 1, 64))],
                        "cell_updates": sth.cell_updates}}
 
 

@@ -157,45 +157,62 @@ __device__ __forceinline__ void t_cl(double H, double C, const ClosureParams &p,
   }
 }
 
+__device__ __forceinline__ float sqrtT(float x) { return sqrtf(x); }
+__device__ __forceinline__ double sqrtT(double x) { return sqrt(x); }
+
 // Derivative of t_cl: J = {dT/dH, dT/dC, dC_l/dH, dC_l/dC}, regime by regime
 // (solid T = H/cp; eutectic constant; mush through the porosity root
 // a por^2 + b por + c = 0, differentiated implicitly, with C clamped at -CR
 // as CALCULATEPOROSITYMUSH does; liquid T = H - St, C_l = C).  Used by the
-// linearised inner cycles of the mixed-precision nonlinear solve; it has no
+// linearised cycles of the Newton solve and by the adjoint; it has no
 // counterpart in the reference, which only evaluates the closure.
-__device__ __forceinline__ void t_cl_jac(double H, double C, const ClosureParams &p, double J[4]) {
-  double Hs, He, Hl;
-  bounding_energy(C, p, Hs, He, Hl);
-  J[0] = J[1] = J[2] = J[3] = 0.0;
+// T = double: the expressions of bounding_energy / porosity_mush in FP64;
+// T = float: the same expressions in FP32 at the FP32-rounded state (the
+// derivative only steers FP32 linear cycles, whose Newton residual and
+// update stay FP64; in FP32 the divisions and the square root cost a few
+// instructions instead of the FP64 pipe's tens of cycles per warp).
+template <class T>
+__device__ __forceinline__ void t_cl_jacT(T H, T C, const ClosureParams &p, T J[4]) {
+  const T CR = (T)p.CR, k = (T)p.k, cpv = (T)p.cp, St = (T)p.St, te = (T)p.te, Te = (T)p.Te;
+  T Hs = (C < -CR) ? T(0) : cpv * ((-C - CR) / k);
+  if (Hs < T(0)) Hs = T(0);
+  Hs = Hs + te * cpv;
+  const T pe = (CR + C) / (CR + Te);
+  const T He = pe * (St + te * (T(1) - cpv)) + cpv * te;
+  const T Hl = St - C + te + Te;
+  J[0] = J[1] = J[2] = J[3] = T(0);
   if (H <= Hs) {
-    J[0] = 1.0 / p.cp;
+    J[0] = T(1) / cpv;
   } else if (H > Hs && H <= He) {
     // eutectic: T and C_l fixed
   } else if (H > He && H < Hl) {
-    double por = 1.0, dpH = 0.0, dpC = 0.0;
-    if (p.St != 0) {
-      const bool clamp = !(C >= -p.CR);
-      const double validC = clamp ? -p.CR : C;
-      const double a = p.CR * (p.cp - 1) + p.St * (p.k - 1);
-      const double b = p.CR * (1 - 2 * p.cp) + H * (1 - p.k) - validC * (p.cp - 1) - p.k * p.St;
-      const double c = (p.CR + validC) * p.cp + p.k * H;
-      const double sD = sqrt(b * b - 4 * a * c);
-      por = (-b - sD) / (2 * a);
-      const double dbH = 1 - p.k, dbC = clamp ? 0.0 : -(p.cp - 1);
-      const double dcH = p.k, dcC = clamp ? 0.0 : p.cp;
-      dpH = (-dbH - (b * dbH - 2 * a * dcH) / sD) / (2 * a);
-      dpC = (-dbC - (b * dbC - 2 * a * dcC) / sD) / (2 * a);
+    T por = T(1), dpH = T(0), dpC = T(0);
+    if (St != T(0)) {
+      const bool clamp = !(C >= -CR);
+      const T validC = clamp ? -CR : C;
+      const T a = CR * (cpv - T(1)) + St * (k - T(1));
+      const T b = CR * (T(1) - T(2) * cpv) + H * (T(1) - k) - validC * (cpv - T(1)) - k * St;
+      const T c = (CR + validC) * cpv + k * H;
+      const T sD = sqrtT(b * b - T(4) * a * c);
+      por = (-b - sD) / (T(2) * a);
+      const T dbH = T(1) - k, dbC = clamp ? T(0) : -(cpv - T(1));
+      const T dcH = k, dcC = clamp ? T(0) : cpv;
+      dpH = (-dbH - (b * dbH - T(2) * a * dcH) / sD) / (T(2) * a);
+      dpC = (-dbC - (b * dbC - T(2) * a * dcC) / sD) / (T(2) * a);
     }
-    const double num = C + p.CR * (1 - por), den = por + p.k * (1 - por);
-    const double dCl_dpor = (-p.CR * den - num * (1 - p.k)) / (den * den);
+    const T num = C + CR * (T(1) - por), den = por + k * (T(1) - por);
+    const T dCl_dpor = (-CR * den - num * (T(1) - k)) / (den * den);
     J[2] = dCl_dpor * dpH;
-    J[3] = 1.0 / den + dCl_dpor * dpC;
+    J[3] = T(1) / den + dCl_dpor * dpC;
     J[0] = -J[2];
     J[1] = -J[3];
   } else if (H >= Hl) {
-    J[0] = 1.0;
-    J[3] = 1.0;
+    J[0] = T(1);
+    J[3] = T(1);
   }
+}
+__device__ __forceinline__ void t_cl_jac(double H, double C, const ClosureParams &p, double J[4]) {
+  t_cl_jacT<double>(H, C, p, J);
 }
 
 // Derivative of the porosity of the full closure (CALCULATEPOROSITY,
