@@ -306,7 +306,7 @@ constexpr int kAdjDirectMax = 32;
 
 #ifdef MLGPU_ADJ_UNIT  // kernels compiled in launch_f64_adj.cu only
 // closure Jacobian of every cell, evaluated in the kernels' precision (FP32:
-// at the FP32-rounded state)
+// t_cl's regime, the derivative at the FP32-rounded state)
 template <class T>
 __global__ void __launch_bounds__(kBlock) adj_jac_kernel(Geom G, ClosureParams cp,
                                                          const double *__restrict__ u,
@@ -314,7 +314,10 @@ __global__ void __launch_bounds__(kBlock) adj_jac_kernel(Geom G, ClosureParams c
   const long long n = G.ncell;
   for (long long q = gtid(); q < n; q += gstride()) {
     T j4[4];
-    t_cl_jacT<T>((T)u[q], (T)u[q + n], cp, j4);
+    if constexpr (sizeof(T) == 4)
+      t_cl_jac32(u[q], u[q + n], cp, j4);
+    else
+      t_cl_jac(u[q], u[q + n], cp, j4);
 #pragma unroll
     for (int m = 0; m < 4; m++) J[q + m * n] = j4[m];
   }

@@ -111,9 +111,10 @@ cudaError_t launch_lean_prolong(const LinLeanT<T> &P, const Geom &C, int csplit,
 template <class T, class S>
 cudaError_t launch_lean_pack(const Geom &G, int split, int ncomp, const S *src, T *dst,
                              cudaStream_t s);
+// clip: the regime clipping of the update, or null for u = u_old + scale e
 template <class T>
-cudaError_t launch_lean_step(const Geom &G, int split, double *u, const double *u_old,
-                             double scale, const T *e, cudaStream_t s);
+cudaError_t launch_lean_step(const Geom &G, int split, const StepClip *clip, double *u,
+                             const double *u_old, double scale, const T *e, cudaStream_t s);
 cudaError_t launch_adj_bottom_direct(const AdjArgs<float> &A, float *y, const float *g,
                                      cudaStream_t s, bool tr);
 cudaError_t launch_adj_restrict(const AdjArgs<float> &A, const Geom &C, const float *y,

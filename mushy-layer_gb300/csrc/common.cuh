@@ -160,32 +160,60 @@ __device__ __forceinline__ void t_cl(double H, double C, const ClosureParams &p,
 __device__ __forceinline__ float sqrtT(float x) { return sqrtf(x); }
 __device__ __forceinline__ double sqrtT(double x) { return sqrt(x); }
 
-// Derivative of t_cl: J = {dT/dH, dT/dC, dC_l/dH, dC_l/dC}, regime by regime
-// (solid T = H/cp; eutectic constant; mush through the porosity root
-// a por^2 + b por + c = 0, differentiated implicitly, with C clamped at -CR
-// as CALCULATEPOROSITYMUSH does; liquid T = H - St, C_l = C).  Used by the
-// linearised cycles of the Newton solve and by the adjoint; it has no
-// counterpart in the reference, which only evaluates the closure.
+// Regime of (H, C) as t_cl takes it: 0 solid, 1 eutectic, 2 mush, 3 liquid,
+// 4 NaN input (no branch)
+__device__ __forceinline__ int closure_regime(double H, double C, const ClosureParams &p) {
+  double Hs, He, Hl;
+  bounding_energy(C, p, Hs, He, Hl);
+  if (H <= Hs) return 0;
+  if (H > Hs && H <= He) return 1;
+  if (H > He && H < Hl) return 2;
+  if (H >= Hl) return 3;
+  return 4;
+}
+
+// The same regime from FP32 bounding energies, with the FP64 test for the
+// cells near a bound (within 1e-4 of its scale, far above the FP32 rounding
+// of the bounds): every cell gets t_cl's own regime, at FP32 cost for all but
+// the few near a phase boundary.
+__device__ __forceinline__ int closure_regime_fast(double H, double C, const ClosureParams &p) {
+  const float h = (float)H, c = (float)C;
+  const float CR = (float)p.CR, k = (float)p.k, cpv = (float)p.cp, St = (float)p.St,
+              te = (float)p.te, Te = (float)p.Te;
+  float Hs = (c < -CR) ? 0.f : cpv * ((-c - CR) / k);
+  if (Hs < 0.f) Hs = 0.f;
+  Hs = Hs + te * cpv;
+  const float He = (CR + c) / (CR + Te) * (St + te * (1.f - cpv)) + cpv * te;
+  const float Hl = St - c + te + Te;
+  const float band = 1e-4f;
+  if (fabsf(h - Hs) < band * (1.f + fabsf(Hs)) || fabsf(h - He) < band * (1.f + fabsf(He)) ||
+      fabsf(h - Hl) < band * (1.f + fabsf(Hl)))
+    return closure_regime(H, C, p);
+  if (h <= Hs) return 0;
+  if (h <= He) return 1;
+  if (h < Hl) return 2;
+  if (h >= Hl) return 3;
+  return 4;
+}
+
+// Derivative of t_cl: J = {dT/dH, dT/dC, dC_l/dH, dC_l/dC} in regime `reg`
+// (closure_regime): solid T = H/cp; eutectic constant; mush through the
+// porosity root a por^2 + b por + c = 0, differentiated implicitly, with C
+// clamped at -CR as CALCULATEPOROSITYMUSH does; liquid T = H - St, C_l = C.
+// Used by the linearised cycles of the Newton solve and by the adjoint; it
+// has no counterpart in the reference, which only evaluates the closure.
 // T = double: the expressions of bounding_energy / porosity_mush in FP64;
 // T = float: the same expressions in FP32 at the FP32-rounded state (the
 // derivative only steers FP32 linear cycles, whose Newton residual and
 // update stay FP64; in FP32 the divisions and the square root cost a few
 // instructions instead of the FP64 pipe's tens of cycles per warp).
 template <class T>
-__device__ __forceinline__ void t_cl_jacT(T H, T C, const ClosureParams &p, T J[4]) {
-  const T CR = (T)p.CR, k = (T)p.k, cpv = (T)p.cp, St = (T)p.St, te = (T)p.te, Te = (T)p.Te;
-  T Hs = (C < -CR) ? T(0) : cpv * ((-C - CR) / k);
-  if (Hs < T(0)) Hs = T(0);
-  Hs = Hs + te * cpv;
-  const T pe = (CR + C) / (CR + Te);
-  const T He = pe * (St + te * (T(1) - cpv)) + cpv * te;
-  const T Hl = St - C + te + Te;
+__device__ __forceinline__ void t_cl_jac_in(int reg, T H, T C, const ClosureParams &p, T J[4]) {
+  const T CR = (T)p.CR, k = (T)p.k, cpv = (T)p.cp, St = (T)p.St;
   J[0] = J[1] = J[2] = J[3] = T(0);
-  if (H <= Hs) {
+  if (reg == 0) {
     J[0] = T(1) / cpv;
-  } else if (H > Hs && H <= He) {
-    // eutectic: T and C_l fixed
-  } else if (H > He && H < Hl) {
+  } else if (reg == 2) {
     T por = T(1), dpH = T(0), dpC = T(0);
     if (St != T(0)) {
       const bool clamp = !(C >= -CR);
@@ -206,13 +234,19 @@ __device__ __forceinline__ void t_cl_jacT(T H, T C, const ClosureParams &p, T J[
     J[3] = T(1) / den + dCl_dpor * dpC;
     J[0] = -J[2];
     J[1] = -J[3];
-  } else if (H >= Hl) {
+  } else if (reg == 3) {
     J[0] = T(1);
     J[3] = T(1);
   }
+  // eutectic (1): T and C_l fixed; NaN input (4): zero
 }
 __device__ __forceinline__ void t_cl_jac(double H, double C, const ClosureParams &p, double J[4]) {
-  t_cl_jacT<double>(H, C, p, J);
+  t_cl_jac_in<double>(closure_regime(H, C, p), H, C, p, J);
+}
+// FP32 derivative in t_cl's own regime (closure_regime_fast)
+__device__ __forceinline__ void t_cl_jac32(double H, double C, const ClosureParams &p,
+                                           float J[4]) {
+  t_cl_jac_in<float>(closure_regime_fast(H, C, p), (float)H, (float)C, p, J);
 }
 
 // Derivative of the porosity of the full closure (CALCULATEPOROSITY,

@@ -147,12 +147,22 @@ cudaError_t launch_lean_pack(const Geom &G, int split, int ncomp, const S *src, 
 }
 
 template <class T>
-cudaError_t launch_lean_step(const Geom &G, int split, double *u, const double *u_old,
-                             double scale, const T *e, cudaStream_t s) {
-  if (split)
-    lean_step_kernel<T, SplitIdx><<<blocks_for(G.ncell), kBlock, 0, s>>>(G, u, u_old, scale, e);
-  else
-    lean_step_kernel<T, NaturalIdx><<<blocks_for(G.ncell), kBlock, 0, s>>>(G, u, u_old, scale, e);
+cudaError_t launch_lean_step(const Geom &G, int split, const StepClip *clip, double *u,
+                             const double *u_old, double scale, const T *e, cudaStream_t s) {
+  const int nb = blocks_for(G.ncell);
+  StepClip K{};
+  if (clip) K = *clip;
+#define MLGPU_LEAN_STEP(IDX)                                                           \
+  if (clip)                                                                            \
+    lean_step_kernel<T, IDX, true><<<nb, kBlock, 0, s>>>(G, K, u, u_old, scale, e);    \
+  else                                                                                 \
+    lean_step_kernel<T, IDX, false><<<nb, kBlock, 0, s>>>(G, K, u, u_old, scale, e);
+  if (split) {
+    MLGPU_LEAN_STEP(SplitIdx)
+  } else {
+    MLGPU_LEAN_STEP(NaturalIdx)
+  }
+#undef MLGPU_LEAN_STEP
   return cudaGetLastError();
 }
 
@@ -166,8 +176,8 @@ cudaError_t launch_lean_step(const Geom &G, int split, double *u, const double *
                                              const T *, cudaStream_t);                        \
   template cudaError_t launch_lean_pack<T, double>(const Geom &, int, int, const double *, T *, \
                                                   cudaStream_t);                              \
-  template cudaError_t launch_lean_step<T>(const Geom &, int, double *, const double *, double, \
-                                          const T *, cudaStream_t);
+  template cudaError_t launch_lean_step<T>(const Geom &, int, const StepClip *, double *,        \
+                                          const double *, double, const T *, cudaStream_t);
 MLGPU_LEAN_INST(float)
 MLGPU_LEAN_INST(double)
 template cudaError_t launch_lean_pack<float, float>(const Geom &, int, int, const float *,

@@ -43,6 +43,22 @@
 
 namespace mlgpu {
 
+// Regime test of the Newton update's clipping: the closure's bounding
+// energies with the divisions by constants as products with their reciprocals
+// (a boundary in the last bits may classify either way; only the clipping
+// reads it, never the closure)
+struct StepClip {
+  double CR, cp, St, te, Te, inv_k, inv_CRTe, frac;
+  __host__ __device__ int regime(double H, double C, double b[3]) const {
+    double Hs = (C < -CR) ? 0.0 : cp * ((-C - CR) * inv_k);
+    if (Hs < 0.0) Hs = 0.0;
+    b[0] = Hs + te * cp;
+    b[1] = (CR + C) * inv_CRTe * (St + te * (1 - cp)) + cp * te;
+    b[2] = St - C + te + Te;
+    return H <= b[0] ? 0 : (H <= b[1] ? 1 : (H < b[2] ? 2 : 3));
+  }
+};
+
 template <class T>
 struct LinLeanT {
   Geom G;
@@ -263,9 +279,13 @@ __global__ void __launch_bounds__(kBlock) lean_pack_kernel(Geom G, int ncomp,
 }
 
 // Newton update u = u_old + scale e, e the correction in layout IDX (both
-// components)
-template <class T, class IDX>
-__global__ void __launch_bounds__(kBlock) lean_step_kernel(Geom G, double *__restrict__ u,
+// components).  CLIP: a cell whose H would leave its closure regime (solid /
+// eutectic / mush / liquid, bounded by H_s, H_e, H_l at the new C) stops at
+// the first regime boundary it crosses plus `frac` of its overshoot, so its
+// next linearisation is the new regime's.
+template <class T, class IDX, bool CLIP>
+__global__ void __launch_bounds__(kBlock) lean_step_kernel(Geom G, StepClip K,
+                                                           double *__restrict__ u,
                                                            const double *__restrict__ u_old,
                                                            double scale,
                                                            const T *__restrict__ e) {
@@ -275,8 +295,19 @@ __global__ void __launch_bounds__(kBlock) lean_step_kernel(Geom G, double *__res
     int i, j, k;
     cell_ijk(G, q, i, j, k);
     const long long o = at(G, i, j, k);
-    u[q] = u_old[q] + scale * (double)e[o];
-    u[n + q] = u_old[n + q] + scale * (double)e[n + o];
+    const double h0 = u_old[q], c0 = u_old[n + q];
+    double h1 = h0 + scale * (double)e[o];
+    const double c1 = c0 + scale * (double)e[n + o];
+    if (CLIP) {
+      double b0[3], b1[3];
+      const int r0 = K.regime(h0, c0, b0), r1 = K.regime(h1, c1, b1);
+      if (r1 != r0) {
+        const double bnd = b1[r1 > r0 ? r0 : r0 - 1];
+        h1 = bnd + K.frac * (h1 - bnd);
+      }
+    }
+    u[q] = h1;
+    u[n + q] = c1;
   }
 }
 #endif  // MLGPU_ADJ_F32_UNIT

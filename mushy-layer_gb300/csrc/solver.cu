@@ -1600,9 +1600,29 @@ class HCAdjSolver : public mlgpu_solver {
 
   // ---- Newton for N(u) = f: u += d, A(u) d = f - N(u) solved by these
   // cycles on A to `lin_tol` relative (at most `lin_max` cycles), halving d
-  // while the FP64 residual grows (at most 4 times)
+  // while the FP64 residual grows (at most 4 times); with clip >= 0 a cell
+  // whose H would leave its closure regime stops at the first regime
+  // boundary it crosses plus `clip` of its overshoot (lean_step_kernel), so
+  // that the next step linearises the new regime instead of extrapolating
+  // the old one across the kink (halves the Newton steps of the 256^3
+  // backward-Euler step)
   double lin_tol = 1e-3;
   int lin_max = 12;
+  double clip = 0.1;
+
+  StepClip step_clip() const {
+    const ClosureParams cp = make_cp(op.params);
+    StepClip K;
+    K.CR = cp.CR;
+    K.cp = cp.cp;
+    K.St = cp.St;
+    K.te = cp.te;
+    K.Te = cp.Te;
+    K.inv_k = 1.0 / cp.k;
+    K.inv_CRTe = 1.0 / (cp.CR + cp.Te);
+    K.frac = clip;
+    return K;
+  }
 
   // f - N(u) into L[0].g; host_norm[0] = its norm of the options' kind (the
   // stopping test), host_norm[1] = its L2 norm (the merit of the step
@@ -1694,16 +1714,15 @@ class HCAdjSolver : public mlgpu_solver {
       }
       CK(cudaMemcpyAsync(nuold, L[0].u, bytes, cudaMemcpyDeviceToDevice, s));
       double scale = 1.0;
+      const StepClip K = step_clip();
+      const StepClip *kp = clip >= 0 ? &K : nullptr;
       for (int h = 0; h <= 4; h++) {
-        // u = u_old + scale d
-        if (mixed) {
-          CK(launch_lean_step<float>(L[0].G, split(0), L[0].u, nuold, scale, L[0].y32, s));
-        } else if (fast64) {
-          CK(launch_lean_step<double>(L[0].G, split(0), L[0].u, nuold, scale, L[0].y, s));
-        } else {
-          CK(cudaMemcpyAsync(L[0].u, nuold, bytes, cudaMemcpyDeviceToDevice, s));
-          CK(launch_axpby<double>(n2, scale, L[0].y, 1.0, L[0].u, s));
-        }
+        // u = u_old + scale d (d split on the lean paths' smoothed level 0)
+        if (mixed)
+          CK(launch_lean_step<float>(L[0].G, split(0), kp, L[0].u, nuold, scale, L[0].y32, s));
+        else
+          CK(launch_lean_step<double>(L[0].G, fast64 ? split(0) : 0, kp, L[0].u, nuold, scale,
+                                      L[0].y, s));
         rc = nl_residual();
         if (rc) return rc;
         st->cell_updates += (double)L[0].G.ncell;
@@ -2128,6 +2147,16 @@ int mlgpu_hc_backward_euler_newton(mlgpu_solver *S, double *phi_new, const doubl
   CK(launch_be_rhs(2 * A->L[0].G.ncell, phi_old, aCoef, src, dt, rhs_scratch, A->s));
   if (A->leave()) return MLGPU_ERR_CUDA;
   return A->newton(phi_new, rhs_scratch, stats);
+}
+
+int mlgpu_hc_newton_params(mlgpu_solver *S, double lin_tol, int lin_max, double clip) {
+  HCAdjSolver *A = dynamic_cast<HCAdjSolver *>(S);
+  if (!A || !(lin_tol > 0.0 && lin_tol < 1.0) || lin_max < 1 || !(clip < 0.0 || clip <= 1.0))
+    return MLGPU_ERR_ARG;
+  A->lin_tol = lin_tol;
+  A->lin_max = lin_max;
+  A->clip = clip < 0.0 ? -1.0 : clip;
+  return MLGPU_OK;
 }
 
 int mlgpu_hc_newton_sweep_time(mlgpu_solver *S, int kind, int reps, double *ms_per_launch) {

@@ -2296,11 +2296,31 @@ int orc_mac_project_adjoint(const mlgpu_vcop *op, const mlgpu_mg_options *o,
 
 }  // extern "C"
 
+// Regime of (H, C) for the Newton update's clipping (lean_step_kernel's
+// StepClip restated): the bounding energies with the divisions by constants
+// as products with their reciprocals; 0 solid, 1 eutectic, 2 mush, 3 liquid
+static int clip_regime(double H, double C, const mlgpu_params &p, double b[3]) {
+  const double CR = p.compositionRatio, cp = p.specificHeatRatio, St = p.stefan,
+               te = p.thetaEutectic, Te = p.ThetaEutectic;
+  const double inv_k = 1.0 / p.waterDistributionCoeff, inv_CRTe = 1.0 / (CR + Te);
+  double Hs = (C < -CR) ? 0.0 : cp * ((-C - CR) * inv_k);
+  if (Hs < 0.0) Hs = 0.0;
+  b[0] = Hs + te * cp;
+  b[1] = (CR + C) * inv_CRTe * (St + te * (1 - cp)) + cp * te;
+  b[2] = St - C + te + Te;
+  return H <= b[0] ? 0 : (H <= b[1] ? 1 : (H < b[2] ? 2 : 3));
+}
+
+// the device Newton's default clip of the update
+constexpr double kNewtonClip = 0.1;
+
 // Newton for N(phi) = rhs on the Jacobian hierarchy (the device's
 // mlgpu_hc_newton_solve restated): A(u) d = rhs - N(u) by V-cycles on A to
-// 1e-3 relative (at most 12), u += d halving d while the L2 residual grows
-// (at most 4 times), stagnation on the L2 merit, three stalled steps below
-// 1e-8 of the start end the solve
+// 1e-3 relative (at most 12), u = u_old + s d with a cell whose H would leave
+// its closure regime stopped at the first regime boundary it crosses plus
+// kNewtonClip of its overshoot, s halved while the L2 residual grows (at most
+// 4 times), stagnation on the L2 merit, three stalled steps below 1e-8 of the
+// start end the solve
 extern "C" int orc_hc_newton_solve(const mlgpu_nlop *op, const mlgpu_mg_options *o, double *phi,
                                    const double *rhs, mlgpu_solve_stats *st) {
   AdjSolver S;
@@ -2346,6 +2366,17 @@ extern "C" int orc_hc_newton_solve(const mlgpu_nlop *op, const mlgpu_mg_options 
     double scale = 1.0, merit_new = merit, norm_new = norm;
     for (int h = 0; h <= 4; h++) {
       for (size_t q = 0; q < n; q++) S.L[0].u[q] = scale * S.L[0].y[q] + 1.0 * uold[q];
+      const size_t nc = n / 2;
+      for (size_t q = 0; q < nc; q++) {
+        double b0[3], b1[3];
+        double &h1 = S.L[0].u[q];
+        const int r0 = clip_regime(uold[q], uold[nc + q], op->params, b0);
+        const int r1 = clip_regime(h1, S.L[0].u[nc + q], op->params, b1);
+        if (r1 != r0) {
+          const double bnd = b1[r1 > r0 ? r0 : r0 - 1];
+          h1 = bnd + kNewtonClip * (h1 - bnd);
+        }
+      }
       norm_new = nl(merit_new);
       if (std::isfinite(merit_new) && merit_new <= merit) break;
       scale *= 0.5;
