@@ -99,15 +99,17 @@ cudaError_t launch_adj_minv(const AdjArgs<float> &A, const float *zero, float *M
 // fine-level arrays colour-split, the coarse level's split when csplit
 template <class T>
 cudaError_t launch_lean_gsrb(const LinLeanT<T> &P, int pass, cudaStream_t s);
+// red: the red half's residual only (after a black half sweep); black: the
+// black half's prolongation only (before a red half sweep)
 template <class T>
-cudaError_t launch_lean_residual(const LinLeanT<T> &P, int split, int norm, double *part,
-                                 int *nparts, cudaStream_t s);
+cudaError_t launch_lean_residual(const LinLeanT<T> &P, int split, int red, int norm,
+                                 double *part, int *nparts, cudaStream_t s);
 template <class T>
-cudaError_t launch_lean_restrict(const LinLeanT<T> &P, const Geom &C, int csplit, T *gc, T *xc,
-                                 T *wc, cudaStream_t s);
+cudaError_t launch_lean_restrict(const LinLeanT<T> &P, const Geom &C, int csplit, int red, T *gc,
+                                 T *xc, T *wc, cudaStream_t s);
 template <class T>
-cudaError_t launch_lean_prolong(const LinLeanT<T> &P, const Geom &C, int csplit, int kind,
-                                const T *xc, cudaStream_t s);
+cudaError_t launch_lean_prolong(const LinLeanT<T> &P, const Geom &C, int csplit, int black,
+                                int kind, const T *xc, cudaStream_t s);
 template <class T, class S>
 cudaError_t launch_lean_pack(const Geom &G, int split, int ncomp, const S *src, T *dst,
                              cudaStream_t s);

@@ -85,53 +85,74 @@ cudaError_t launch_lean_gsrb(const LinLeanT<T> &P, int pass, cudaStream_t s) {
 }
 
 template <class T>
-cudaError_t launch_lean_residual(const LinLeanT<T> &P, int split, int norm, double *part,
-                                 int *nparts, cudaStream_t s) {
-  const int nb = blocks_for(P.G.ncell);
+cudaError_t launch_lean_residual(const LinLeanT<T> &P, int split, int red, int norm,
+                                 double *part, int *nparts, cudaStream_t s) {
+  red = split && red;
+  const int nb = blocks_for(red ? P.G.ncell >> 1 : P.G.ncell);
   if (nparts) *nparts = nb;
   if (norm < 0) norm = MLGPU_NORM_MAX;
-#define MLGPU_LEAN_RES(IDX)                                                                  \
-  MLGPU_DIM_SWITCH(P.G.dim, MLGPU_NORM_SWITCH(norm, {                                        \
-    if (NORM >= 0)                                                                           \
-      lean_residual_kernel<T, DIM, (NORM < 0 ? 0 : NORM), IDX><<<nb, kBlock, 0, s>>>(P, part); \
+#define MLGPU_LEAN_RES(IDX, RED)                                                          \
+  MLGPU_DIM_SWITCH(P.G.dim, MLGPU_NORM_SWITCH(norm, {                                     \
+    if (NORM >= 0)                                                                        \
+      lean_residual_kernel<T, DIM, (NORM < 0 ? 0 : NORM), IDX, RED>                       \
+          <<<nb, kBlock, 0, s>>>(P, part);                                                \
   }))
-  if (split)
-    MLGPU_LEAN_RES(SplitIdx);
+  if (red)
+    MLGPU_LEAN_RES(SplitIdx, true);
+  else if (split)
+    MLGPU_LEAN_RES(SplitIdx, false);
   else
-    MLGPU_LEAN_RES(NaturalIdx);
+    MLGPU_LEAN_RES(NaturalIdx, false);
 #undef MLGPU_LEAN_RES
   return cudaGetLastError();
 }
 
 template <class T>
-cudaError_t launch_lean_restrict(const LinLeanT<T> &P, const Geom &C, int csplit, T *gc, T *xc,
-                                 T *wc, cudaStream_t s) {
+cudaError_t launch_lean_restrict(const LinLeanT<T> &P, const Geom &C, int csplit, int red, T *gc,
+                                 T *xc, T *wc, cudaStream_t s) {
   const int nb = blocks_for(C.ncell);
+#define MLGPU_LEAN_RST(IDX, RED) \
+  MLGPU_DIM_SWITCH(P.G.dim, (lean_restrict_kernel<T, DIM, IDX, RED><<<nb, kBlock, 0, s>>>(P, C, gc, xc, wc)))
   if (csplit) {
-    MLGPU_DIM_SWITCH(P.G.dim, (lean_restrict_kernel<T, DIM, SplitIdx><<<nb, kBlock, 0, s>>>(P, C, gc, xc, wc)));
+    if (red)
+      MLGPU_LEAN_RST(SplitIdx, true);
+    else
+      MLGPU_LEAN_RST(SplitIdx, false);
   } else {
-    MLGPU_DIM_SWITCH(P.G.dim, (lean_restrict_kernel<T, DIM, NaturalIdx><<<nb, kBlock, 0, s>>>(P, C, gc, xc, wc)));
+    if (red)
+      MLGPU_LEAN_RST(NaturalIdx, true);
+    else
+      MLGPU_LEAN_RST(NaturalIdx, false);
   }
+#undef MLGPU_LEAN_RST
   return cudaGetLastError();
 }
 
 template <class T>
-cudaError_t launch_lean_prolong(const LinLeanT<T> &P, const Geom &C, int csplit, int kind,
-                                const T *xc, cudaStream_t s) {
-  const int nb = blocks_for(P.G.ncell);
-#define MLGPU_LEAN_PRO(KIND, IDX) \
-  MLGPU_DIM_SWITCH(P.G.dim, (lean_prolong_kernel<T, DIM, KIND, IDX><<<nb, kBlock, 0, s>>>(P, C, xc)))
+cudaError_t launch_lean_prolong(const LinLeanT<T> &P, const Geom &C, int csplit, int black,
+                                int kind, const T *xc, cudaStream_t s) {
+  const int nb = blocks_for(black ? P.G.ncell >> 1 : P.G.ncell);
+#define MLGPU_LEAN_PRO(KIND, IDX, BL) \
+  MLGPU_DIM_SWITCH(P.G.dim, (lean_prolong_kernel<T, DIM, KIND, IDX, BL><<<nb, kBlock, 0, s>>>(P, C, xc)))
+#define MLGPU_LEAN_PRO2(KIND, IDX)      \
+  if (black)                            \
+    MLGPU_LEAN_PRO(KIND, IDX, true);    \
+  else                                  \
+    MLGPU_LEAN_PRO(KIND, IDX, false);
   if (kind == MLGPU_PROLONG_LINEAR) {
-    if (csplit)
-      MLGPU_LEAN_PRO(MLGPU_PROLONG_LINEAR, SplitIdx);
-    else
-      MLGPU_LEAN_PRO(MLGPU_PROLONG_LINEAR, NaturalIdx);
+    if (csplit) {
+      MLGPU_LEAN_PRO2(MLGPU_PROLONG_LINEAR, SplitIdx)
+    } else {
+      MLGPU_LEAN_PRO2(MLGPU_PROLONG_LINEAR, NaturalIdx)
+    }
   } else {
-    if (csplit)
-      MLGPU_LEAN_PRO(MLGPU_PROLONG_CONSTANT, SplitIdx);
-    else
-      MLGPU_LEAN_PRO(MLGPU_PROLONG_CONSTANT, NaturalIdx);
+    if (csplit) {
+      MLGPU_LEAN_PRO2(MLGPU_PROLONG_CONSTANT, SplitIdx)
+    } else {
+      MLGPU_LEAN_PRO2(MLGPU_PROLONG_CONSTANT, NaturalIdx)
+    }
   }
+#undef MLGPU_LEAN_PRO2
 #undef MLGPU_LEAN_PRO
   return cudaGetLastError();
 }
@@ -168,12 +189,12 @@ cudaError_t launch_lean_step(const Geom &G, int split, const StepClip *clip, dou
 
 #define MLGPU_LEAN_INST(T)                                                                     \
   template cudaError_t launch_lean_gsrb<T>(const LinLeanT<T> &, int, cudaStream_t);           \
-  template cudaError_t launch_lean_residual<T>(const LinLeanT<T> &, int, int, double *, int *, \
-                                              cudaStream_t);                                  \
-  template cudaError_t launch_lean_restrict<T>(const LinLeanT<T> &, const Geom &, int, T *,    \
-                                              T *, T *, cudaStream_t);                        \
+  template cudaError_t launch_lean_residual<T>(const LinLeanT<T> &, int, int, int, double *,   \
+                                              int *, cudaStream_t);                           \
+  template cudaError_t launch_lean_restrict<T>(const LinLeanT<T> &, const Geom &, int, int,    \
+                                              T *, T *, T *, cudaStream_t);                   \
   template cudaError_t launch_lean_prolong<T>(const LinLeanT<T> &, const Geom &, int, int,     \
-                                             const T *, cudaStream_t);                        \
+                                             int, const T *, cudaStream_t);                   \
   template cudaError_t launch_lean_pack<T, double>(const Geom &, int, int, const double *, T *, \
                                                   cudaStream_t);                              \
   template cudaError_t launch_lean_step<T>(const Geom &, int, const StepClip *, double *,        \

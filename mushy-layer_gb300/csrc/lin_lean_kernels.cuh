@@ -43,17 +43,18 @@
 
 namespace mlgpu {
 
-// Regime test of the Newton update's clipping: the closure's bounding
-// energies with the divisions by constants as products with their reciprocals
-// (a boundary in the last bits may classify either way; only the clipping
-// reads it, never the closure)
+// Regime test of the Newton update's clipping, in FP32 (the bounding
+// energies with the divisions by constants as products with their
+// reciprocals): a cell within FP32 rounding of a bound may classify either
+// way and be clipped by a fraction of its tiny overshoot; only the clipping
+// reads it, never the closure.  0 solid, 1 eutectic, 2 mush, 3 liquid.
 struct StepClip {
-  double CR, cp, St, te, Te, inv_k, inv_CRTe, frac;
-  __host__ __device__ int regime(double H, double C, double b[3]) const {
-    double Hs = (C < -CR) ? 0.0 : cp * ((-C - CR) * inv_k);
-    if (Hs < 0.0) Hs = 0.0;
+  float CR, cp, St, te, Te, inv_k, inv_CRTe, frac;
+  __host__ __device__ int regime(float H, float C, float b[3]) const {
+    float Hs = (C < -CR) ? 0.f : cp * ((-C - CR) * inv_k);
+    if (Hs < 0.f) Hs = 0.f;
     b[0] = Hs + te * cp;
-    b[1] = (CR + C) * inv_CRTe * (St + te * (1 - cp)) + cp * te;
+    b[1] = (CR + C) * inv_CRTe * (St + te * (1.f - cp)) + cp * te;
     b[2] = St - C + te + Te;
     return H <= b[0] ? 0 : (H <= b[1] ? 1 : (H < b[2] ? 2 : 3));
   }
@@ -193,13 +194,16 @@ __device__ __forceinline__ T lean_accum(T acc, T v) {
 // the linear stopping test, and on GB300 an FP64 operation per cell would
 // cost more than the cell's memory traffic); the block combines in FP64.
 // IDX: split, or natural on a one-level hierarchy (whose only level is the
-// bottom's).
-template <class T, int DIM, int NORM, class IDX>
+// bottom's).  RED (split only): the red half alone -- after a black half
+// sweep the black cells' residual is zero up to rounding (each black x solves
+// its own equations against the current red w), so the norm of a V-cycle that
+// ends in post-smoothing is the red cells' norm.
+template <class T, int DIM, int NORM, class IDX, bool RED>
 __global__ void __launch_bounds__(kBlock) lean_residual_kernel(LinLeanT<T> P, double *part) {
   const Geom &G = P.G;
-  const long long n = G.ncell;
+  const long long n = G.ncell, m = RED ? (n >> 1) : n;
   T acc = T(0);
-  for (long long q = gtid(); q < n; q += gstride()) {
+  for (long long q = gtid(); q < m; q += gstride()) {
     int i, j, k;
     IDX::ijk(G, q, i, j, k);
     T r[2];
@@ -212,8 +216,10 @@ __global__ void __launch_bounds__(kBlock) lean_residual_kernel(LinLeanT<T> P, do
 }
 
 // coarse g = 2^D average of the fine residual; the coarse x and w start at 0
-// (coarse arrays split, or natural on the bottom level)
-template <class T, int DIM, class CIDX>
+// (coarse arrays split, or natural on the bottom level).  RED: after
+// pre-smoothing that ends in a black half sweep the black children's
+// residual is zero up to rounding and only the red children are summed.
+template <class T, int DIM, class CIDX, bool RED>
 __global__ void __launch_bounds__(kBlock) lean_restrict_kernel(LinLeanT<T> P, Geom C, T *gc,
                                                                T *xc, T *wc) {
   const long long nc = C.ncell;
@@ -228,6 +234,7 @@ __global__ void __launch_bounds__(kBlock) lean_restrict_kernel(LinLeanT<T> P, Ge
       for (int jj = 0; jj < 2; jj++)
 #pragma unroll
         for (int ii = 0; ii < 2; ii++) {
+          if (RED && ((ii + jj + kk) & 1)) continue;  // the child's colour
           const int i = 2 * I + ii, j = 2 * J + jj, k = DIM == 3 ? 2 * K + kk : 0;
           T r[2];
           lean_res<T, DIM, SplitIdx>(P, i, j, k, cs_index(P.G, i, j, k), r);
@@ -245,13 +252,15 @@ __global__ void __launch_bounds__(kBlock) lean_restrict_kernel(LinLeanT<T> P, Ge
 }
 
 // x += prolongation of the coarse correction (coarse split, or natural on the
-// bottom level); w = J x
-template <class T, int DIM, int KIND, class CIDX>
+// bottom level); w = J x.  BLACK: the black half alone -- when post-smoothing
+// follows, its red half sweep overwrites the red x and w without reading
+// them (x_red = K^T (g + bdx sum b w_black)), so the result is the same bits.
+template <class T, int DIM, int KIND, class CIDX, bool BLACK>
 __global__ void __launch_bounds__(kBlock) lean_prolong_kernel(LinLeanT<T> P, Geom C,
                                                               const T *__restrict__ xc) {
   const Geom &G = P.G;
-  const long long n = G.ncell;
-  for (long long q = gtid(); q < n; q += gstride()) {
+  const long long n = G.ncell, q0 = BLACK ? (n >> 1) : 0;
+  for (long long q = q0 + gtid(); q < n; q += gstride()) {
     int i, j, k;
     cs_cell(G, q, i, j, k);
     const T x0 = prolong_add<T, DIM, KIND, CIDX>(C, P.ybc, 0, i, j, k, P.x[q], xc, nullptr);
@@ -299,11 +308,12 @@ __global__ void __launch_bounds__(kBlock) lean_step_kernel(Geom G, StepClip K,
     double h1 = h0 + scale * (double)e[o];
     const double c1 = c0 + scale * (double)e[n + o];
     if (CLIP) {
-      double b0[3], b1[3];
-      const int r0 = K.regime(h0, c0, b0), r1 = K.regime(h1, c1, b1);
+      float b0[3], b1[3];
+      const int r0 = K.regime((float)h0, (float)c0, b0);
+      const int r1 = K.regime((float)h1, (float)c1, b1);
       if (r1 != r0) {
-        const double bnd = b1[r1 > r0 ? r0 : r0 - 1];
-        h1 = bnd + K.frac * (h1 - bnd);
+        const double bnd = (double)b1[r1 > r0 ? r0 : r0 - 1];
+        h1 = bnd + (double)K.frac * (h1 - bnd);
       }
     }
     u[q] = h1;

@@ -1540,7 +1540,8 @@ class HCAdjSolver : public mlgpu_solver {
     int rc = lin_smooth<T>(l, o.num_smooth_down);
     if (rc) return rc;
     const LinLeanT<T> C = leanT<T>(l + 1);
-    CK(launch_lean_restrict<T>(P, C.G, split(l + 1), (T *)C.g, C.x, C.w, s));
+    CK(launch_lean_restrict<T>(P, C.G, split(l + 1), o.num_smooth_down >= 1, (T *)C.g, C.x, C.w,
+                               s));
     for (int m = 0; m < o.num_mg; m++) {
       if (m > 0) {  // every coarse visit starts from zero
         CK(cudaMemsetAsync(C.x, 0, sizeof(T) * 2 * C.G.ncell, s));
@@ -1549,15 +1550,18 @@ class HCAdjSolver : public mlgpu_solver {
       rc = lin_cycle<T>(l + 1);
       if (rc) return rc;
     }
-    CK(launch_lean_prolong<T>(P, C.G, split(l + 1), o.prolong, C.x, s));
+    CK(launch_lean_prolong<T>(P, C.G, split(l + 1), o.num_smooth_up >= 1, o.prolong, C.x, s));
     return lin_smooth<T>(l, o.num_smooth_up);
   }
 
-  // linear residual g - A y of level 0 with its norm (combined in FP64)
+  // linear residual g - A y of level 0 with its norm (combined in FP64);
+  // after_cycle: at the end of a V-cycle whose post-smoothing ended in a
+  // black half sweep (the red cells' residual alone)
   template <class T>
-  int lin_residual_norm() {
+  int lin_residual_norm(bool after_cycle = false) {
     int nparts = 0;
-    CK(launch_lean_residual<T>(leanT<T>(0), split(0), o.norm_type, part, &nparts, s));
+    const bool red = after_cycle && o.num_smooth_up >= 1 && (int)L.size() > 1;
+    CK(launch_lean_residual<T>(leanT<T>(0), split(0), red, o.norm_type, part, &nparts, s));
     CK(launch_finalize_norm(o.norm_type, part, nparts, part + kMaxBlocks, s));
     CK(cudaMemcpyAsync(host_norm, part + kMaxBlocks, sizeof(double), cudaMemcpyDeviceToHost, s));
     return MLGPU_OK;
@@ -1568,12 +1572,12 @@ class HCAdjSolver : public mlgpu_solver {
     if (lin32()) {
       int rc = lin_cycle<float>(0);
       if (rc) return rc;
-      return lin_residual_norm<float>();
+      return lin_residual_norm<float>(true);
     }
     if (fast64 && !tr) {
       int rc = lin_cycle<double>(0);
       if (rc) return rc;
-      return lin_residual_norm<double>();
+      return lin_residual_norm<double>(true);
     }
     int rc = cycle(0);
     if (rc) return rc;
@@ -1613,14 +1617,14 @@ class HCAdjSolver : public mlgpu_solver {
   StepClip step_clip() const {
     const ClosureParams cp = make_cp(op.params);
     StepClip K;
-    K.CR = cp.CR;
-    K.cp = cp.cp;
-    K.St = cp.St;
-    K.te = cp.te;
-    K.Te = cp.Te;
-    K.inv_k = 1.0 / cp.k;
-    K.inv_CRTe = 1.0 / (cp.CR + cp.Te);
-    K.frac = clip;
+    K.CR = (float)cp.CR;
+    K.cp = (float)cp.cp;
+    K.St = (float)cp.St;
+    K.te = (float)cp.te;
+    K.Te = (float)cp.Te;
+    K.inv_k = (float)(1.0 / cp.k);
+    K.inv_CRTe = (float)(1.0 / (cp.CR + cp.Te));
+    K.frac = (float)clip;
     return K;
   }
 

@@ -2297,16 +2297,17 @@ int orc_mac_project_adjoint(const mlgpu_vcop *op, const mlgpu_mg_options *o,
 }  // extern "C"
 
 // Regime of (H, C) for the Newton update's clipping (lean_step_kernel's
-// StepClip restated): the bounding energies with the divisions by constants
+// StepClip restated): FP32 bounding energies with the divisions by constants
 // as products with their reciprocals; 0 solid, 1 eutectic, 2 mush, 3 liquid
-static int clip_regime(double H, double C, const mlgpu_params &p, double b[3]) {
-  const double CR = p.compositionRatio, cp = p.specificHeatRatio, St = p.stefan,
-               te = p.thetaEutectic, Te = p.ThetaEutectic;
-  const double inv_k = 1.0 / p.waterDistributionCoeff, inv_CRTe = 1.0 / (CR + Te);
-  double Hs = (C < -CR) ? 0.0 : cp * ((-C - CR) * inv_k);
-  if (Hs < 0.0) Hs = 0.0;
+static int clip_regime(float H, float C, const mlgpu_params &p, float b[3]) {
+  const float CR = (float)p.compositionRatio, cp = (float)p.specificHeatRatio,
+              St = (float)p.stefan, te = (float)p.thetaEutectic, Te = (float)p.ThetaEutectic;
+  const float inv_k = (float)(1.0 / p.waterDistributionCoeff),
+              inv_CRTe = (float)(1.0 / (p.compositionRatio + p.ThetaEutectic));
+  float Hs = (C < -CR) ? 0.f : cp * ((-C - CR) * inv_k);
+  if (Hs < 0.f) Hs = 0.f;
   b[0] = Hs + te * cp;
-  b[1] = (CR + C) * inv_CRTe * (St + te * (1 - cp)) + cp * te;
+  b[1] = (CR + C) * inv_CRTe * (St + te * (1.f - cp)) + cp * te;
   b[2] = St - C + te + Te;
   return H <= b[0] ? 0 : (H <= b[1] ? 1 : (H < b[2] ? 2 : 3));
 }
@@ -2368,13 +2369,13 @@ extern "C" int orc_hc_newton_solve(const mlgpu_nlop *op, const mlgpu_mg_options 
       for (size_t q = 0; q < n; q++) S.L[0].u[q] = scale * S.L[0].y[q] + 1.0 * uold[q];
       const size_t nc = n / 2;
       for (size_t q = 0; q < nc; q++) {
-        double b0[3], b1[3];
+        float b0[3], b1[3];
         double &h1 = S.L[0].u[q];
-        const int r0 = clip_regime(uold[q], uold[nc + q], op->params, b0);
-        const int r1 = clip_regime(h1, S.L[0].u[nc + q], op->params, b1);
+        const int r0 = clip_regime((float)uold[q], (float)uold[nc + q], op->params, b0);
+        const int r1 = clip_regime((float)h1, (float)S.L[0].u[nc + q], op->params, b1);
         if (r1 != r0) {
-          const double bnd = b1[r1 > r0 ? r0 : r0 - 1];
-          h1 = bnd + kNewtonClip * (h1 - bnd);
+          const double bnd = (double)b1[r1 > r0 ? r0 : r0 - 1];
+          h1 = bnd + (double)(float)kNewtonClip * (h1 - bnd);
         }
       }
       norm_new = nl(merit_new);
