@@ -43,20 +43,28 @@
 
 namespace mlgpu {
 
-// Regime test of the Newton update's clipping, in FP32 (the bounding
-// energies with the divisions by constants as products with their
-// reciprocals): a cell within FP32 rounding of a bound may classify either
-// way and be clipped by a fraction of its tiny overshoot; only the clipping
-// reads it, never the closure.  0 solid, 1 eutectic, 2 mush, 3 liquid.
+// Regime test of the Newton update's clipping.  The common case in FP32
+// (bounding energies with the divisions by constants as products with their
+// reciprocals); a cell within 1e-4 of a bound, or whose FP32 regime changes,
+// is decided again in FP64 by t_cl's own test (closure_regime), and clipped
+// at the FP64 bound: a clip at an FP32-rounded bound would pin a cell that
+// converges onto a phase boundary 1e-7 away from its solution.
 struct StepClip {
   float CR, cp, St, te, Te, inv_k, inv_CRTe, frac;
-  __host__ __device__ int regime(float H, float C, float b[3]) const {
+  ClosureParams p;  // the closure's own parameters (FP64 decisions)
+  __host__ __device__ int regime32(float H, float C, float b[3]) const {
     float Hs = (C < -CR) ? 0.f : cp * ((-C - CR) * inv_k);
     if (Hs < 0.f) Hs = 0.f;
     b[0] = Hs + te * cp;
     b[1] = (CR + C) * inv_CRTe * (St + te * (1.f - cp)) + cp * te;
     b[2] = St - C + te + Te;
     return H <= b[0] ? 0 : (H <= b[1] ? 1 : (H < b[2] ? 2 : 3));
+  }
+  __host__ __device__ static bool near(float H, const float b[3]) {
+    const float band = 1e-4f;
+    return fabsf(H - b[0]) < band * (1.f + fabsf(b[0])) ||
+           fabsf(H - b[1]) < band * (1.f + fabsf(b[1])) ||
+           fabsf(H - b[2]) < band * (1.f + fabsf(b[2]));
   }
 };
 
@@ -309,11 +317,16 @@ __global__ void __launch_bounds__(kBlock) lean_step_kernel(Geom G, StepClip K,
     const double c1 = c0 + scale * (double)e[n + o];
     if (CLIP) {
       float b0[3], b1[3];
-      const int r0 = K.regime((float)h0, (float)c0, b0);
-      const int r1 = K.regime((float)h1, (float)c1, b1);
-      if (r1 != r0) {
-        const double bnd = (double)b1[r1 > r0 ? r0 : r0 - 1];
-        h1 = bnd + (double)K.frac * (h1 - bnd);
+      const int f0 = K.regime32((float)h0, (float)c0, b0);
+      const int f1 = K.regime32((float)h1, (float)c1, b1);
+      if (f0 != f1 || StepClip::near((float)h0, b0) || StepClip::near((float)h1, b1)) {
+        const int r0 = closure_regime(h0, c0, K.p), r1 = closure_regime(h1, c1, K.p);
+        if (r0 != r1 && r0 < 4 && r1 < 4) {
+          double B[3];
+          bounding_energy(c1, K.p, B[0], B[1], B[2]);
+          const double bnd = B[r1 > r0 ? r0 : r0 - 1];
+          h1 = bnd + (double)K.frac * (h1 - bnd);
+        }
       }
     }
     u[q] = h1;

@@ -1625,6 +1625,7 @@ class HCAdjSolver : public mlgpu_solver {
     K.inv_k = (float)(1.0 / cp.k);
     K.inv_CRTe = (float)(1.0 / (cp.CR + cp.Te));
     K.frac = (float)clip;
+    K.p = cp;
     return K;
   }
 

@@ -2297,19 +2297,16 @@ int orc_mac_project_adjoint(const mlgpu_vcop *op, const mlgpu_mg_options *o,
 }  // extern "C"
 
 // Regime of (H, C) for the Newton update's clipping (lean_step_kernel's
-// StepClip restated): FP32 bounding energies with the divisions by constants
-// as products with their reciprocals; 0 solid, 1 eutectic, 2 mush, 3 liquid
-static int clip_regime(float H, float C, const mlgpu_params &p, float b[3]) {
-  const float CR = (float)p.compositionRatio, cp = (float)p.specificHeatRatio,
-              St = (float)p.stefan, te = (float)p.thetaEutectic, Te = (float)p.ThetaEutectic;
-  const float inv_k = (float)(1.0 / p.waterDistributionCoeff),
-              inv_CRTe = (float)(1.0 / (p.compositionRatio + p.ThetaEutectic));
-  float Hs = (C < -CR) ? 0.f : cp * ((-C - CR) * inv_k);
-  if (Hs < 0.f) Hs = 0.f;
-  b[0] = Hs + te * cp;
-  b[1] = (CR + C) * inv_CRTe * (St + te * (1.f - cp)) + cp * te;
-  b[2] = St - C + te + Te;
-  return H <= b[0] ? 0 : (H <= b[1] ? 1 : (H < b[2] ? 2 : 3));
+// decision restated: t_cl's own test, FP64); 0 solid, 1 eutectic, 2 mush,
+// 3 liquid, 4 NaN
+static int clip_regime(double H, double C, const mlgpu_params &p) {
+  double Hs, He, Hl;
+  bounding_energy(C, p, Hs, He, Hl);
+  if (H <= Hs) return 0;
+  if (H > Hs && H <= He) return 1;
+  if (H > He && H < Hl) return 2;
+  if (H >= Hl) return 3;
+  return 4;
 }
 
 // the device Newton's default clip of the update
@@ -2369,12 +2366,14 @@ extern "C" int orc_hc_newton_solve(const mlgpu_nlop *op, const mlgpu_mg_options 
       for (size_t q = 0; q < n; q++) S.L[0].u[q] = scale * S.L[0].y[q] + 1.0 * uold[q];
       const size_t nc = n / 2;
       for (size_t q = 0; q < nc; q++) {
-        float b0[3], b1[3];
         double &h1 = S.L[0].u[q];
-        const int r0 = clip_regime((float)uold[q], (float)uold[nc + q], op->params, b0);
-        const int r1 = clip_regime((float)h1, (float)S.L[0].u[nc + q], op->params, b1);
-        if (r1 != r0) {
-          const double bnd = (double)b1[r1 > r0 ? r0 : r0 - 1];
+        const double c1 = S.L[0].u[nc + q];
+        const int r0 = clip_regime(uold[q], uold[nc + q], op->params);
+        const int r1 = clip_regime(h1, c1, op->params);
+        if (r0 != r1 && r0 < 4 && r1 < 4) {
+          double B[3];
+          bounding_energy(c1, op->params, B[0], B[1], B[2]);
+          const double bnd = B[r1 > r0 ? r0 : r0 - 1];
           h1 = bnd + (double)(float)kNewtonClip * (h1 - bnd);
         }
       }
