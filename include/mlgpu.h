@@ -477,15 +477,18 @@ int mlgpu_hc_adjoint_solve(mlgpu_solver *S, const double *phi, const double *g, 
  * its norms, the step and the closure stay FP64. */
 int mlgpu_hc_newton_solve(mlgpu_solver *S, double *phi, const double *rhs,
                           mlgpu_solve_stats *stats);
-/* Newton settings of an adjoint solver's mlgpu_hc_newton_solve: each step's
- * linear solve runs V-cycles on A until its residual is below lin_tol (0 < .. < 1)
- * of its start, at most lin_max (>= 1) cycles (defaults 1e-3, 12).  The step is
- * u_old + s d, s halved while the L2 residual grows; with clip in [0, 1]
- * (default 0.1) a cell whose H would leave its closure regime (solid, eutectic,
- * mush, liquid) stops at the first regime boundary it crosses plus clip times
- * its overshoot; clip < 0: no clipping.  MLGPU_ERR_ARG for other values.  No
- * counterpart in the reference. */
-int mlgpu_hc_newton_params(mlgpu_solver *S, double lin_tol, int lin_max, double clip);
+/* Newton settings of an adjoint solver's mlgpu_hc_newton_solve.  Each step's
+ * linear solve runs V-cycles on A until its residual is below eta of its start,
+ * at most lin_max (>= 1) cycles: eta = lin_tol (0 < .. < 1) with forcing 0; with
+ * forcing 1 the Eisenstat-Walker forcing term (choice 2: 0.9 (|r_k| / |r_k-1|)^2,
+ * their safeguard, at most lin_tol, at least 0.5 tolerance |r_0| / |r_k|).  The
+ * step is u_old + s d, s halved while the L2 residual grows; with clip in [0, 1]
+ * a cell whose H would leave its closure regime (solid, eutectic, mush, liquid)
+ * stops at the first regime boundary it crosses plus clip times its overshoot;
+ * clip < 0: no clipping.  Defaults: lin_tol 0.3, lin_max 12, clip 0.1, forcing 1.
+ * MLGPU_ERR_ARG for other values.  No counterpart in the reference. */
+int mlgpu_hc_newton_params(mlgpu_solver *S, double lin_tol, int lin_max, double clip,
+                           int forcing);
 /* Measurement: device time (ms per launch, host double) of `reps` FP32
  * smoothing launches on the finest level of a mixed-precision Newton solver,
  * at the state of its last step, timed with CUDA events on the solver's

@@ -1603,16 +1603,23 @@ class HCAdjSolver : public mlgpu_solver {
   }
 
   // ---- Newton for N(u) = f: u += d, A(u) d = f - N(u) solved by these
-  // cycles on A to `lin_tol` relative (at most `lin_max` cycles), halving d
-  // while the FP64 residual grows (at most 4 times); with clip >= 0 a cell
+  // cycles on A to eta relative (at most `lin_max` cycles), halving d while
+  // the FP64 residual grows (at most 4 times).  eta: `lin_tol`, or with
+  // `forcing` the Eisenstat-Walker forcing term (their choice 2, gamma 0.9,
+  // alpha 2, with their safeguard; capped at lin_tol, and never below what
+  // the nonlinear tolerance needs), loose while the linearisation is poor,
+  // tight in the quadratic phase (defaults: forcing on, cap 0.3; the 256^3
+  // step then takes 9 Newton steps and 13 cycles, against 8 and 19 with a
+  // fixed 1e-3).  With clip >= 0 a cell
   // whose H would leave its closure regime stops at the first regime
   // boundary it crosses plus `clip` of its overshoot (lean_step_kernel), so
   // that the next step linearises the new regime instead of extrapolating
   // the old one across the kink (halves the Newton steps of the 256^3
   // backward-Euler step)
-  double lin_tol = 1e-3;
+  double lin_tol = 0.3;
   int lin_max = 12;
   double clip = 0.1;
+  int forcing = 1;
 
   StepClip step_clip() const {
     const ClosureParams cp = make_cp(op.params);
@@ -1687,6 +1694,7 @@ class HCAdjSolver : public mlgpu_solver {
     if (!std::isfinite(S.norm0)) S.status = 8;
     int stall = 0;  // consecutive steps that cut the residual by under 5%
     double merit = host_norm[1];
+    double eta = lin_tol;
     while (outer_continue(o, S)) {
       rc = state_levels();
       if (rc) return rc;
@@ -1709,7 +1717,7 @@ class HCAdjSolver : public mlgpu_solver {
       st->kernel_launches += nk_state + nk_res + (mixed || fast64 ? 1 : 0);
       CK(cudaStreamSynchronize(s));
       const double l0 = *host_norm;
-      for (int c = 0; c < lin_max && *host_norm > lin_tol * l0; c++) {
+      for (int c = 0; c < lin_max && *host_norm > eta * l0; c++) {
         rc = run_iteration();
         if (rc) return rc;
         CK(cudaStreamSynchronize(s));
@@ -1747,6 +1755,14 @@ class HCAdjSolver : public mlgpu_solver {
         S.status = 8;
       else if (merit > (1.0 - o.hang) * merit_prev && S.norm > o.tolerance * S.norm0)
         S.status = 2;
+      if (forcing && S.prev > 0 && std::isfinite(S.norm)) {
+        const double ratio = S.norm / S.prev;
+        double e = 0.9 * ratio * ratio;
+        const double guard = 0.9 * eta * eta;
+        if (guard > 0.1) e = std::max(e, guard);
+        e = std::min(e, lin_tol);
+        eta = std::min(lin_tol, std::max(e, 0.5 * o.tolerance * S.norm0 / S.norm));
+      }
       S.prev = S.norm;
       // three stalled steps far below the start: the FP64 residual has
       // reached its round-off floor (stalls of the damped early steps, where
@@ -2154,12 +2170,15 @@ int mlgpu_hc_backward_euler_newton(mlgpu_solver *S, double *phi_new, const doubl
   return A->newton(phi_new, rhs_scratch, stats);
 }
 
-int mlgpu_hc_newton_params(mlgpu_solver *S, double lin_tol, int lin_max, double clip) {
+int mlgpu_hc_newton_params(mlgpu_solver *S, double lin_tol, int lin_max, double clip,
+                           int forcing) {
   HCAdjSolver *A = dynamic_cast<HCAdjSolver *>(S);
-  if (!A || !(lin_tol > 0.0 && lin_tol < 1.0) || lin_max < 1 || !(clip < 0.0 || clip <= 1.0))
+  if (!A || !(lin_tol > 0.0 && lin_tol < 1.0) || lin_max < 1 || !(clip < 0.0 || clip <= 1.0) ||
+      (forcing != 0 && forcing != 1))
     return MLGPU_ERR_ARG;
   A->lin_tol = lin_tol;
   A->lin_max = lin_max;
+  A->forcing = forcing;
   A->clip = clip < 0.0 ? -1.0 : clip;
   return MLGPU_OK;
 }

@@ -2309,12 +2309,15 @@ static int clip_regime(double H, double C, const mlgpu_params &p) {
   return 4;
 }
 
-// the device Newton's default clip of the update
-constexpr double kNewtonClip = 0.1;
+// the device Newton's default clip of the update and cap of the forcing term
+constexpr double kNewtonClip = 0.1, kNewtonEtaMax = 0.3;
 
 // Newton for N(phi) = rhs on the Jacobian hierarchy (the device's
-// mlgpu_hc_newton_solve restated): A(u) d = rhs - N(u) by V-cycles on A to
-// 1e-3 relative (at most 12), u = u_old + s d with a cell whose H would leave
+// mlgpu_hc_newton_solve restated with its default settings): A(u) d =
+// rhs - N(u) by V-cycles on A to eta relative (at most 12; eta the
+// Eisenstat-Walker forcing term, choice 2, gamma 0.9, alpha 2, safeguarded,
+// capped at 0.3, at least 0.5 tolerance |r_0| / |r_k|), u = u_old + s d with a
+// cell whose H would leave
 // its closure regime stopped at the first regime boundary it crosses plus
 // kNewtonClip of its overshoot, s halved while the L2 residual grows (at most
 // 4 times), stagnation on the L2 merit, three stalled steps below 1e-8 of the
@@ -2348,6 +2351,7 @@ extern "C" int orc_hc_newton_solve(const mlgpu_nlop *op, const mlgpu_mg_options 
   st->initial_norm = norm0;
   st->norm_history[0] = norm0;
   int iter = 0, status = std::isfinite(norm0) ? 0 : 8, stall = 0, cycles = 0;
+  double eta = kNewtonEtaMax;
   while (norm > o->tolerance * norm0 && norm0 > o->norm_thresh && iter < o->max_iter &&
          status == 0) {
     S.refresh();
@@ -2355,7 +2359,7 @@ extern "C" int orc_hc_newton_solve(const mlgpu_nlop *op, const mlgpu_mg_options 
     std::copy(r.begin(), r.end(), S.L[0].gg.begin());
     const double l0 = lin_norm();
     double ln = l0;
-    for (int c = 0; c < 12 && ln > 1e-3 * l0; c++) {
+    for (int c = 0; c < 12 && ln > eta * l0; c++) {
       S.cycle(0);
       cycles++;
       ln = lin_norm();
@@ -2391,6 +2395,14 @@ extern "C" int orc_hc_newton_solve(const mlgpu_nlop *op, const mlgpu_mg_options 
       status = 8;
     else if (merit > (1.0 - o->hang) * merit_prev && norm > o->tolerance * norm0)
       status = 2;
+    if (prev > 0 && std::isfinite(norm)) {
+      const double ratio = norm / prev;
+      double e = 0.9 * ratio * ratio;
+      const double guard = 0.9 * eta * eta;
+      if (guard > 0.1) e = std::max(e, guard);
+      e = std::min(e, kNewtonEtaMax);
+      eta = std::min(kNewtonEtaMax, std::max(e, 0.5 * o->tolerance * norm0 / norm));
+    }
     prev = norm;
     if (stall >= 3 && norm < 1e-8 * norm0 && status == 0) status = 2;
   }

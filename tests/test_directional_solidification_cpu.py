@@ -96,7 +96,9 @@ def steady_state(nz, nx=4, t_end=6.0):
     cl = O.closure(g, p, np.ascontiguousarray(phi))
     T = cl["T"].reshape(nz, nx)
     chi = cl["porosity"].reshape(nz, nx)
-    assert np.array_equal(T, np.repeat(T[:, :1], nx, axis=1))   # uniform in x
+    # uniform in x (to round-off: the red/black smoother of an inexact
+    # linear solve is not invariant under a one-cell shift in x)
+    assert np.abs(T - T[:, :1]).max() <= 1e-12 * np.abs(T).max()
     return z, T[:, 0], chi[:, 0], change
 
 
