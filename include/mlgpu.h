@@ -215,6 +215,14 @@ int mlgpu_closure(const mlgpu_grid *grid, const mlgpu_params *p,
  * (src/AMRNonLinearMultiCompOp.cpp:57-98). */
 int mlgpu_closure_tcl(const mlgpu_grid *grid, const mlgpu_params *p,
                       const double *HC, double *TCl, void *stream);
+/* mlgpu_closure_tcl as the lean Newton paths evaluate it (mixed precision and
+ * the FP64 comparison path): the divisions by constants as products with
+ * their reciprocals, the porosity root's square root and the C_l quotient from
+ * FP32 seeds refined in FP64 (Markstein / Karp-Markstein iterations).  Within a
+ * few ulps of mlgpu_closure_tcl, not its bit pattern.  No counterpart in the
+ * reference. */
+int mlgpu_closure_tcl_lean(const mlgpu_grid *grid, const mlgpu_params *p,
+                           const double *HC, double *TCl, void *stream);
 
 /* ------------------------------------------------- nonlinear operator --- */
 /* Bytes of device scratch the fused norms need (norm_type >= 0 below). */

@@ -198,6 +198,14 @@ int mlgpu_closure_tcl(const mlgpu_grid *g, const mlgpu_params *p, const double *
   return status_of(launch_closure_tcl(G.ncell, make_cp(*p), HC, TCl, (cudaStream_t)stream));
 }
 
+int mlgpu_closure_tcl_lean(const mlgpu_grid *g, const mlgpu_params *p, const double *HC,
+                           double *TCl, void *stream) {
+  if (!valid_grid(g) || !p || !HC || !TCl) return MLGPU_ERR_ARG;
+  Geom G = make_geom(*g);
+  return status_of(
+      launch_closure_tcl_lean(G.ncell, make_cp(*p), HC, TCl, (cudaStream_t)stream));
+}
+
 int mlgpu_device_alloc(size_t bytes, void **ptr) {
   if (!ptr) return MLGPU_ERR_ARG;
   *ptr = nullptr;

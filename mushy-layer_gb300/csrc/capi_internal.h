@@ -34,6 +34,8 @@ cudaError_t launch_closure_full(long long n, const ClosureParams &p, const doubl
                                 double *Hl, cudaStream_t s);
 cudaError_t launch_closure_tcl(long long n, const ClosureParams &p, const double *HC, double *TCl,
                                cudaStream_t s);
+cudaError_t launch_closure_tcl_lean(long long n, const ClosureParams &p, const double *HC,
+                                   double *TCl, cudaStream_t s);
 cudaError_t launch_face_geomean(const Geom &G, int d, const double *cell, double *face,
                                 cudaStream_t s);
 cudaError_t launch_mac_div(const Geom &G, const double *u0, const double *u1, const double *u2,
@@ -122,16 +124,19 @@ cudaError_t launch_adj_bottom_direct(const AdjArgs<float> &A, float *y, const fl
 cudaError_t launch_adj_restrict(const AdjArgs<float> &A, const Geom &C, const float *y,
                                 const float *g, float *gc, cudaStream_t s, bool tr);
 // FP64 nonlinear kernels over the per-level (T, C_l) cache
+// lean: t_cl_lean (the lean Newton paths' closure) instead of t_cl
 cudaError_t launch_nlc_closure(const NLArgs<double> &A, const double *phi, double *tcl,
-                               cudaStream_t s);
+                               cudaStream_t s, int lean = 0);
 cudaError_t launch_nlc_gsrb(const NLArgs<double> &A, double *phi, const double *rhs, double *tcl,
                             const double *lam, int pass, cudaStream_t s);
 cudaError_t launch_nlc_relax_block(const NLArgs<double> &A, double *phi, const double *rhs,
                                    double *tcl, const double *lam, int sweeps, int init,
                                    cudaStream_t s);
+// part_max: with a norm, the max-norm partials too (same count)
 cudaError_t launch_nlc_op(const NLArgs<double> &A, int mode, int norm, const double *phi,
                           const double *tcl, const double *rhs, double *out, double *copy,
-                          double *part, int *nparts, cudaStream_t s);
+                          double *part, int *nparts, cudaStream_t s,
+                          double *part_max = nullptr);
 cudaError_t launch_nlc_restrict(const NLArgs<double> &A, const Geom &C, const double *phi,
                                 const double *tcl, const double *rhs, double *res_c,
                                 double *phi_c, cudaStream_t s);

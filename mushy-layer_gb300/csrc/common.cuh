@@ -157,6 +157,98 @@ __device__ __forceinline__ void t_cl(double H, double C, const ClosureParams &p,
   }
 }
 
+// ---- lean FP64 closure (the outer loops of the lean Newton paths)
+// t_cl with the closure's divisions by constants as products with their
+// reciprocals and the two per-cell operations (the porosity root's square
+// root, the liquid concentration's quotient) from an FP32 seed refined in
+// FP64: the coupled square-root / half-reciprocal-root iteration and the
+// reciprocal-then-quotient correction of Markstein ("Computation of
+// elementary functions on the IBM RISC System/6000", IBM J. Res. Dev. 34,
+// 1990) and Karp & Markstein ("High-precision division and square root",
+// ACM TOMS 23, 1997), with FMA residuals.  About half the FP64 pipe
+// operations of t_cl per mush cell; within a few ulps of it (the Newton
+// residual it feeds targets 1e-10 of the initial), not its bit pattern --
+// the reference-order paths keep t_cl.
+struct ClosureLean {
+  double CR, k, cp, St, te, Te;
+  double inv_k, inv_CRTe, He_slope, a, inv_2a, four_a, b0, omk, cpm1;
+};
+
+inline ClosureLean make_closure_lean(const ClosureParams &p) {
+  ClosureLean L;
+  L.CR = p.CR;
+  L.k = p.k;
+  L.cp = p.cp;
+  L.St = p.St;
+  L.te = p.te;
+  L.Te = p.Te;
+  L.inv_k = 1.0 / p.k;
+  L.inv_CRTe = 1.0 / (p.CR + p.Te);
+  L.He_slope = p.St + p.te * (1 - p.cp);
+  L.a = p.CR * (p.cp - 1) + p.St * (p.k - 1);
+  L.inv_2a = 1.0 / (2 * L.a);
+  L.four_a = 4 * L.a;
+  L.b0 = p.CR * (1 - 2 * p.cp) - p.k * p.St;
+  L.omk = 1 - p.k;
+  L.cpm1 = p.cp - 1;
+  return L;
+}
+
+// sqrt(D) for D well inside FP32's normal range (else the library square root)
+__device__ __forceinline__ double lean_sqrt(double D) {
+  if (!(D > 1e-30 && D < 1e30)) return sqrt(D);
+  const double y = (double)rsqrtf((float)D);  // 1/sqrt(D) to ~2^-22
+  double g = D * y, h = 0.5 * y;              // sqrt(D), 1/(2 sqrt(D))
+  const double r = fma(-g, h, 0.5);
+  g = fma(g, r, g);
+  h = fma(h, r, h);
+  const double d = fma(-g, g, D);
+  return fma(d, h, g);
+}
+
+// num / den for |den| well inside FP32's normal range and a finite quotient
+// (else the library division)
+__device__ __forceinline__ double lean_div(double num, double den) {
+  const double ad = fabs(den);
+  if (!(ad > 1e-30 && ad < 1e30 && fabs(num) < 1e250)) return num / den;
+  double y = (double)__frcp_rn((float)den);  // 1/den to 2^-24
+  y = fma(fma(-den, y, 1.0), y, y);           // to ~2^-48
+  const double q = num * y;
+  return fma(fma(-den, q, num), y, q);
+}
+
+__device__ __forceinline__ void t_cl_lean(double H, double C, const ClosureLean &p, double &T,
+                                          double &Cl) {
+  double Hs = (C < -p.CR) ? 0.0 : p.cp * ((-C - p.CR) * p.inv_k);
+  if (Hs < 0.0) Hs = 0.0;
+  Hs = Hs + p.te * p.cp;
+  const double He = (p.CR + C) * p.inv_CRTe * p.He_slope + p.cp * p.te;
+  const double Hl = p.St - C + p.te + p.Te;
+  if (H <= Hs) {
+    T = H / p.cp;
+    Cl = p.Te;
+  } else if (H <= He) {
+    T = p.te;
+    Cl = p.Te;
+  } else if (H < Hl) {
+    double por = 1.0;
+    if (p.St != 0) {
+      const double vC = (C >= -p.CR) ? C : -p.CR;
+      const double b = p.b0 + H * p.omk - vC * p.cpm1;
+      const double c = (p.CR + vC) * p.cp + p.k * H;
+      por = (-b - lean_sqrt(fma(b, b, -p.four_a * c))) * p.inv_2a;
+    }
+    Cl = lean_div(C + p.CR * (1 - por), por + p.k * (1 - por));
+    T = -Cl;
+  } else if (H >= Hl) {
+    T = H - p.St;
+    Cl = C;
+  } else {  // NaN input, as t_cl
+    T = H;
+    Cl = C;
+  }
+}
+
 __device__ __forceinline__ float sqrtT(float x) { return sqrtf(x); }
 __device__ __forceinline__ double sqrtT(double x) { return sqrt(x); }
 

@@ -133,6 +133,12 @@ cudaError_t launch_closure_tcl(long long n, const ClosureParams &p, const double
   closure_tcl_kernel<<<blocks_for(n), kBlock, 0, s>>>(n, p, HC, TCl);
   return cudaGetLastError();
 }
+
+cudaError_t launch_closure_tcl_lean(long long n, const ClosureParams &p, const double *HC,
+                                   double *TCl, cudaStream_t s) {
+  closure_tcl_lean_kernel<<<blocks_for(n), kBlock, 0, s>>>(n, make_closure_lean(p), HC, TCl);
+  return cudaGetLastError();
+}
 cudaError_t launch_face_geomean(const Geom &G, int d, const double *cell, double *face,
                                 cudaStream_t s) {
   face_geomean_kernel<<<blocks_for(G.nface(d)), kBlock, 0, s>>>(G, d, cell, face);

@@ -9,8 +9,14 @@
 namespace mlgpu {
 
 cudaError_t launch_nlc_closure(const NLArgs<double> &A, const double *phi, double *tcl,
-                               cudaStream_t s) {
-  MLGPU_DIM_SWITCH(A.G.dim, (nlc_closure_kernel<DIM><<<nlc_blocks(A.G.ncell), kNLCBlock, 0, s>>>(A, phi, tcl)));
+                               cudaStream_t s, int lean) {
+  const int nb = nlc_blocks(A.G.ncell);
+  const ClosureLean P = make_closure_lean(A.cp);
+  if (lean) {
+    MLGPU_DIM_SWITCH(A.G.dim, (nlc_closure_kernel<DIM, true><<<nb, kNLCBlock, 0, s>>>(A, P, phi, tcl)));
+  } else {
+    MLGPU_DIM_SWITCH(A.G.dim, (nlc_closure_kernel<DIM, false><<<nb, kNLCBlock, 0, s>>>(A, P, phi, tcl)));
+  }
   return cudaGetLastError();
 }
 
@@ -33,13 +39,17 @@ cudaError_t launch_nlc_relax_block(const NLArgs<double> &A, double *phi, const d
 
 cudaError_t launch_nlc_op(const NLArgs<double> &A, int mode, int norm, const double *phi,
                           const double *tcl, const double *rhs, double *out, double *copy,
-                          double *part, int *nparts, cudaStream_t s) {
+                          double *part, int *nparts, cudaStream_t s, double *part_max) {
   const int nb = nlc_blocks(A.G.ncell);
   if (nparts) *nparts = (part && mode == NL_RESIDUAL && norm >= 0) ? nb : 0;
   if (mode == NL_RESIDUAL) {
-    MLGPU_DIM_SWITCH(A.G.dim, MLGPU_NORM_SWITCH(norm, (nlc_op_kernel<DIM, NL_RESIDUAL, NORM><<<nb, kNLCBlock, 0, s>>>(A, phi, tcl, rhs, out, copy, part))));
+    if (part_max && norm >= 0) {
+      MLGPU_DIM_SWITCH(A.G.dim, MLGPU_NORM_SWITCH(norm, (nlc_op_kernel<DIM, NL_RESIDUAL, NORM, true><<<nb, kNLCBlock, 0, s>>>(A, phi, tcl, rhs, out, copy, part, part_max))));
+    } else {
+      MLGPU_DIM_SWITCH(A.G.dim, MLGPU_NORM_SWITCH(norm, (nlc_op_kernel<DIM, NL_RESIDUAL, NORM, false><<<nb, kNLCBlock, 0, s>>>(A, phi, tcl, rhs, out, copy, part, nullptr))));
+    }
   } else if (mode == NL_APPLY_PLUS) {
-    MLGPU_DIM_SWITCH(A.G.dim, (nlc_op_kernel<DIM, NL_APPLY_PLUS, -1><<<nb, kNLCBlock, 0, s>>>(A, phi, tcl, rhs, out, copy, part)));
+    MLGPU_DIM_SWITCH(A.G.dim, (nlc_op_kernel<DIM, NL_APPLY_PLUS, -1, false><<<nb, kNLCBlock, 0, s>>>(A, phi, tcl, rhs, out, copy, part, nullptr)));
   } else {
     return cudaErrorInvalidValue;
   }

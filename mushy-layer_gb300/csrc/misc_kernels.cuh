@@ -200,6 +200,14 @@ __global__ void __launch_bounds__(kBlock) closure_tcl_kernel(long long n, Closur
   for (long long q = gtid(); q < n; q += gstride()) t_cl(HC[q], HC[q + n], p, TCl[q], TCl[q + n]);
 }
 
+// the lean Newton paths' closure (t_cl_lean)
+__global__ void __launch_bounds__(kBlock) closure_tcl_lean_kernel(long long n, ClosureLean p,
+                                                                  const double *__restrict__ HC,
+                                                                  double *__restrict__ TCl) {
+  for (long long q = gtid(); q < n; q += gstride())
+    t_cl_lean(HC[q], HC[q + n], p, TCl[q], TCl[q + n]);
+}
+
 // ---------------------------------------------------- face geometric mean
 // CELLTOEDGEGEOMETRIC: sqrt(|c_lo c_hi|); non-periodic boundary faces see a
 // zero-gradient ghost (face = |c|).

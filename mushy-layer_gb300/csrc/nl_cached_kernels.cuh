@@ -90,15 +90,18 @@ __device__ __forceinline__ void nlc_lofphi(const NLArgs<double> &A, const double
   }
 }
 
-// the cache of every cell
-template <int DIM>
-__global__ void __launch_bounds__(kNLCBlock) nlc_closure_kernel(NLArgs<double> A,
+// the cache of every cell (LEAN: t_cl_lean, for the lean Newton paths)
+template <int DIM, bool LEAN>
+__global__ void __launch_bounds__(kNLCBlock) nlc_closure_kernel(NLArgs<double> A, ClosureLean P,
                                                                 const double *__restrict__ phi,
                                                                 double *__restrict__ tcl) {
   const long long n = A.G.ncell;
   for (long long q = gtid(); q < n; q += gstride()) {
     double t, cl;
-    t_cl(phi[q], phi[q + n], A.cp, t, cl);
+    if (LEAN)
+      t_cl_lean(phi[q], phi[q + n], P, t, cl);
+    else
+      t_cl(phi[q], phi[q + n], A.cp, t, cl);
     tcl[q] = t;
     tcl[q + n] = cl;
   }
@@ -173,17 +176,19 @@ __global__ void __launch_bounds__(1024) nlc_relax_block_kernel(NLArgs<double> A,
   }
 }
 
-// NL_RESIDUAL (with a fused norm) and NL_APPLY_PLUS over the cache
-template <int DIM, int MODE, int NORM>
+// NL_RESIDUAL (with a fused norm; MAX2: the max norm too, into part_max)
+// and NL_APPLY_PLUS over the cache
+template <int DIM, int MODE, int NORM, bool MAX2>
 __global__ void __launch_bounds__(kNLCBlock) nlc_op_kernel(NLArgs<double> A,
                                                            const double *__restrict__ phi,
                                                            const double *__restrict__ tcl,
                                                            const double *__restrict__ rhs,
                                                            double *__restrict__ out,
                                                            double *__restrict__ copy,
-                                                           double *__restrict__ part) {
+                                                           double *__restrict__ part,
+                                                           double *__restrict__ part_max) {
   const Geom &G = A.G;
-  double acc = 0.0;
+  double acc = 0.0, amax = 0.0;
   for (long long q = gtid(); q < G.ncell; q += gstride()) {
     int i, j, k;
     cell_ijk(G, q, i, j, k);
@@ -201,11 +206,16 @@ __global__ void __launch_bounds__(kNLCBlock) nlc_op_kernel(NLArgs<double> A,
       }
       out[qc] = v;
       if (NORM >= 0) acc = norm_accum<NORM < 0 ? 0 : NORM>(acc, v);
+      if (MAX2) amax = norm_accum<MLGPU_NORM_MAX>(amax, v);
     }
   }
   if (NORM >= 0) {
     double r = block_reduce<NORM < 0 ? 0 : NORM>(acc);
     if (threadIdx.x == 0) part[blockIdx.x] = r;
+  }
+  if (MAX2) {
+    double r = block_reduce<MLGPU_NORM_MAX>(amax);
+    if (threadIdx.x == 0) part_max[blockIdx.x] = r;
   }
 }
 

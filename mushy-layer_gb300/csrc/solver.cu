@@ -1233,6 +1233,7 @@ class HCAdjSolver : public mlgpu_solver {
   mlgpu_mg_options o;
   std::vector<AdjLevel> L;
   double *part = nullptr, *host_norm = nullptr, *bcg = nullptr;
+  double *part2 = nullptr;  // max-norm partials of the Newton residual
   double updates_per_iter = 0;
   int kern_iter = -1, kern_init = -1;
   // tr: cycles on A^T (adjoint) or on A (the linear solve of a Newton step);
@@ -1253,9 +1254,10 @@ class HCAdjSolver : public mlgpu_solver {
   // Newton's kernels per piece (counted once): state and Jacobians of every
   // level, the linear residual with its norm, one linear cycle + residual
   int nk_state = -1, nk_res = -1, nk_iter = -1;
-  // kernels of nl_residual (closure, stencil + norm, combine, max norm,
-  // combine) and of one step update
-  static constexpr int kNlResidualKernels = 5, kStepKernels = 1;
+  // kernels of nl_residual (closure, stencil + norms, combine, combine; a
+  // stopping norm other than max adds its own pass) and of one step update
+  static constexpr int kStepKernels = 1;
+  int nl_residual_kernels() const { return o.norm_type == MLGPU_NORM_MAX ? 4 : 5; }
 
   ~HCAdjSolver() override {
     if (graph) cudaGraphExecDestroy(graph);
@@ -1323,6 +1325,7 @@ class HCAdjSolver : public mlgpu_solver {
       g = coarsen_grid(g);
     }
     part = A.get<double>(kNormScratchDoubles);
+    part2 = A.get<double>(kMaxBlocks);
     bcg = A.get<double>(16);
     nf = A.get<double>(2 * ncells(op.grid));
     nuold = A.get<double>(2 * ncells(op.grid));
@@ -1643,20 +1646,26 @@ class HCAdjSolver : public mlgpu_solver {
   int nl_residual() {
     const long long n2 = 2 * L[0].G.ncell;
     int nparts = 0;
-    // the closure once per cell into the cache, then the stencil over it
-    // (bitwise the residual that evaluates the closure at every stencil point)
+    // the closure once per cell into the cache (t_cl, or t_cl_lean on the
+    // lean paths), then the stencil over it (with t_cl bitwise the residual
+    // that evaluates the closure at every stencil point) with its L2 norm and,
+    // for a max-norm stopping test, its max norm in the same pass
     const NLArgs<double> N = make_nl_args<double>(op);
-    CK(launch_nlc_closure(N, L[0].u, ntcl, s));
+    const bool both = o.norm_type == MLGPU_NORM_MAX;
+    CK(launch_nlc_closure(N, L[0].u, ntcl, s, mixed || fast64));
     CK(launch_nlc_op(N, NL_RESIDUAL, MLGPU_NORM_L2, L[0].u, ntcl, nf, L[0].g, nullptr, part,
-                     &nparts, s));
+                     &nparts, s, both ? part2 : nullptr));
     CK(launch_finalize_norm(MLGPU_NORM_L2, part, nparts, part + kMaxBlocks, s));
-    CK(cudaMemcpyAsync(host_norm + 1, part + kMaxBlocks, sizeof(double), cudaMemcpyDeviceToHost,
-                       s));
-    CK(launch_norm_partial<double>(n2, L[0].g, o.norm_type, part, &nparts, s));
-    CK(launch_finalize_norm(o.norm_type, part, nparts, part + kMaxBlocks + 1, s));
-    CK(cudaMemcpyAsync(host_norm, part + kMaxBlocks + 1, sizeof(double), cudaMemcpyDeviceToHost,
+    if (both) {
+      CK(launch_finalize_norm(MLGPU_NORM_MAX, part2, nparts, part + kMaxBlocks + 1, s));
+    } else {
+      CK(launch_norm_partial<double>(n2, L[0].g, o.norm_type, part, &nparts, s));
+      CK(launch_finalize_norm(o.norm_type, part, nparts, part + kMaxBlocks + 1, s));
+    }
+    CK(cudaMemcpyAsync(host_norm, part + kMaxBlocks, 2 * sizeof(double), cudaMemcpyDeviceToHost,
                        s));
     CK(cudaStreamSynchronize(s));
+    std::swap(host_norm[0], host_norm[1]);
     return MLGPU_OK;
   }
 
@@ -1690,7 +1699,7 @@ class HCAdjSolver : public mlgpu_solver {
     S.norm0 = S.norm = S.prev = *host_norm;
     stats_begin(st, (int)L.size(), S.norm0);
     st->cell_updates = (double)L[0].G.ncell;
-    st->kernel_launches = kNlResidualKernels;
+    st->kernel_launches = nl_residual_kernels();
     if (!std::isfinite(S.norm0)) S.status = 8;
     int stall = 0;  // consecutive steps that cut the residual by under 5%
     double merit = host_norm[1];
@@ -1739,7 +1748,7 @@ class HCAdjSolver : public mlgpu_solver {
         rc = nl_residual();
         if (rc) return rc;
         st->cell_updates += (double)L[0].G.ncell;
-        st->kernel_launches += kStepKernels + kNlResidualKernels;
+        st->kernel_launches += kStepKernels + nl_residual_kernels();
         if (std::isfinite(host_norm[1]) && host_norm[1] <= merit) break;
         scale *= 0.5;
       }

@@ -168,6 +168,7 @@ def _declare(lib):
         "mlgpu_version": (i, []),
         "mlgpu_closure": (i, [P(Grid), P(Params)] + [vp] * 8 + [vp]),
         "mlgpu_closure_tcl": (i, [P(Grid), P(Params), vp, vp, vp]),
+        "mlgpu_closure_tcl_lean": (i, [P(Grid), P(Params), vp, vp, vp]),
         "mlgpu_norm_workspace_bytes": (sz, []),
         "mlgpu_nl_residual": (i, [P(NLOp), vp, vp, vp, i, P(d), vp, sz, vp]),
         "mlgpu_nl_apply": (i, [P(NLOp), vp, vp, vp]),
