@@ -1,12 +1,19 @@
 """The lean closure of the Newton paths (t_cl_lean: reciprocal constants,
 square root and quotient from FP32 seeds refined in FP64) against the
-oracle's t_cl (the reference's CALCULATE_T_CL in FP64).
+closure evaluated in 40-digit decimal arithmetic and against the oracle's
+t_cl (the reference's CALCULATE_T_CL in FP64).
 
-Error bound tested: |lean - exact| <= 8 ulp of the closure's scale in every
-regime (solid, eutectic, mush, liquid, C clamped at -CR), on random states and
-on states within a few ulps of every regime bound; 4 ulp on the mushy states
-of the 256^3 workload's range.
+The porosity root cancels (-b - sqrt(b^2 - 4ac)), so rounding in its inputs
+is amplified: t_cl itself lies up to ~13 ulp (of max(|value|, 1)) from the
+decimal closure on random mush states.  Bound tested: the lean closure within
+32 ulp of the decimal closure and of t_cl in every regime (solid, eutectic,
+mush, liquid, C clamped at -CR), on random states, on states within a few
+ulps of every regime bound (where the regime may flip and the closure's
+continuity bounds the difference) and on the 256^3 workload's mushy range,
+with a median at most 1 ulp.
 """
+from decimal import Decimal, getcontext
+
 import ctypes as C
 
 import numpy as np
@@ -38,14 +45,47 @@ def _lean(g, p, HC):
     return host(out)
 
 
-def _check(g, p, HC, ulps=8):
+def _truth(H, C_, p):
+    """t_cl in 40-digit decimal arithmetic (regime by the decimal bounds)."""
+    getcontext().prec = 40
+    D = lambda x: Decimal(float(x))
+    CR, k, cp, St = D(p.compositionRatio), D(p.waterDistributionCoeff), D(p.specificHeatRatio), D(p.stefan)
+    te, Te = D(p.thetaEutectic), D(p.ThetaEutectic)
+    H, C_ = D(H), D(C_)
+    Hs = Decimal(0) if C_ < -CR else cp * ((-C_ - CR) / k)
+    Hs = max(Hs, Decimal(0)) + te * cp
+    He = (CR + C_) / (CR + Te) * (St + te * (1 - cp)) + cp * te
+    Hl = St - C_ + te + Te
+    if H <= Hs:
+        return float(H / cp), float(Te)
+    if H <= He:
+        return float(te), float(Te)
+    if H < Hl:
+        vC = C_ if C_ >= -CR else -CR
+        a = CR * (cp - 1) + St * (k - 1)
+        b = CR * (1 - 2 * cp) + H * (1 - k) - vC * (cp - 1) - k * St
+        c = (CR + vC) * cp + k * H
+        por = (-b - (b * b - 4 * a * c).sqrt()) / (2 * a) if St != 0 else Decimal(1)
+        cl = (C_ + CR * (1 - por)) / (por + k * (1 - por))
+        return float(-cl), float(cl)
+    return float(H - St), float(C_)
+
+
+def _check(g, p, HC, ulps=32):
     ref = O.closure_tcl(g, p, HC)
     got = _lean(g, p, HC)
-    scale = np.maximum(np.abs(ref), 1.0)
-    err = np.abs(got - ref) / (scale * np.finfo(np.float64).eps)
     assert np.all(np.isfinite(got))
-    assert err.max() <= ulps, (err.max(), np.unravel_index(err.argmax(), err.shape))
-    return err
+    eps = np.finfo(np.float64).eps
+    H, C_ = HC[0].ravel(), HC[1].ravel()
+    tru = np.array([_truth(h, c, p) for h, c in zip(H, C_)]).T.reshape(HC.shape)
+    scale = np.maximum(np.abs(tru), 1.0) * eps
+    e_lean = np.abs(got - tru) / scale
+    e_ref = np.abs(ref - tru) / scale
+    e_pair = np.abs(got - ref) / scale
+    assert e_lean.max() <= ulps, (e_lean.max(), e_ref.max())
+    assert e_pair.max() <= ulps, e_pair.max()
+    assert np.median(e_lean) <= 1.0
+    return e_lean, e_ref
 
 
 @pytest.mark.parametrize("params", [dict(), dict(compositionRatio=25.0),
@@ -88,5 +128,6 @@ def test_lean_closure_workload_range():
     p = P.mushy_params()
     H = rng.uniform(2.0, 6.0, abi.cell_shape(g))
     C_ = -1.0 + 1e-3 * rng.standard_normal(abi.cell_shape(g))
-    err = _check(g, p, np.stack([H, C_]), ulps=4)
-    assert np.median(err) <= 1.0
+    e_lean, e_ref = _check(g, p, np.stack([H, C_]))
+    # as accurate as t_cl in the large
+    assert e_lean.max() <= 2 * e_ref.max() + 4
