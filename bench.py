@@ -467,14 +467,21 @@ def dominant_kernel_roofline(torch, abi, ops, R):
     ncell = R.cells()
     hbm, kind = peaks()
     ms = _sweep_time(abi, HS, 0)
+    # the one-cell-per-thread variant of the same sweep (the same bits), for
+    # comparison; then the library default again
+    HS.setNewtonParams(vector_sweeps=0)
+    ms_scalar = _sweep_time(abi, HS, 0)
+    HS.setNewtonParams()
     alg = LEAN_HALF_SWEEP_BYTES_PER_CELL * ncell
     achieved = alg / (ms * 1e-3) / 1e9
-    return {"bound": "hbm", "kernel": "lean_gsrb_kernel<3> (FP32 red/black half sweep, "
-                                       "Newton linear cycles, 256^3 level)",
+    return {"bound": "hbm", "kernel": "lean_gsrb_vec_kernel<float, 3> (FP32 red/black half "
+                                       "sweep, 4-cell vector loads, Newton linear cycles, "
+                                       "256^3 level)",
             "achieved": achieved, "peak": hbm, "peak_kind": kind, "unit": "GB/s",
             "frac": achieved / hbm,
             "traffic": profiled_traffic(LEAN_SWEEP_PROFILE, "dram_bytes_per_launch_256cubed"),
             "alg_bytes_per_launch": alg, "launch_us": ms * 1e3,
+            "scalar_variant_launch_us": ms_scalar * 1e3,
             "timing": "CUDA events on the solver stream, 40 launches after the timed region"}
 
 

@@ -493,10 +493,13 @@ int mlgpu_hc_newton_solve(mlgpu_solver *S, double *phi, const double *rhs,
  * step is u_old + s d, s halved while the L2 residual grows; with clip in [0, 1]
  * a cell whose H would leave its closure regime (solid, eutectic, mush, liquid)
  * stops at the first regime boundary it crosses plus clip times its overshoot;
- * clip < 0: no clipping.  Defaults: lin_tol 0.3, lin_max 12, clip 0.1, forcing 1.
+ * clip < 0: no clipping.  vector_sweeps 1: the lean cycles' red/black half
+ * sweeps take 16-byte vector loads (4 FP32 / 2 FP64 cells of a row per thread)
+ * on the levels whose rows allow it, 0: one cell per thread; the same bits.
+ * Defaults: lin_tol 0.3, lin_max 12, clip 0.1, forcing 1, vector_sweeps 1.
  * MLGPU_ERR_ARG for other values.  No counterpart in the reference. */
 int mlgpu_hc_newton_params(mlgpu_solver *S, double lin_tol, int lin_max, double clip,
-                           int forcing);
+                           int forcing, int vector_sweeps);
 /* Measurement: device time (ms per launch, host double) of `reps` FP32
  * smoothing launches on the finest level of a mixed-precision Newton solver,
  * at the state of its last step, timed with CUDA events on the solver's

@@ -99,8 +99,9 @@ cudaError_t launch_adj_minv(const AdjArgs<float> &A, const float *zero, float *M
                             cudaStream_t s);
 // lean cycles of the Newton step (lin_lean_kernels.cuh); T = float or double;
 // fine-level arrays colour-split, the coarse level's split when csplit
+// vec: the vector-load kernel where the level's rows allow it (the same bits)
 template <class T>
-cudaError_t launch_lean_gsrb(const LinLeanT<T> &P, int pass, cudaStream_t s);
+cudaError_t launch_lean_gsrb(const LinLeanT<T> &P, int pass, cudaStream_t s, int vec = 0);
 // red: the red half's residual only (after a black half sweep); black: the
 // black half's prolongation only (before a red half sweep)
 template <class T>
@@ -112,6 +113,10 @@ cudaError_t launch_lean_restrict(const LinLeanT<T> &P, const Geom &C, int csplit
 template <class T>
 cudaError_t launch_lean_prolong(const LinLeanT<T> &P, const Geom &C, int csplit, int black,
                                 int kind, const T *xc, cudaStream_t s);
+// J, K, D of a smoothed level from the state u, in the split layout
+template <class T>
+cudaError_t launch_lean_state(const AdjArgs<T> &A, const double *u, T *Js, T *Ks, T *Ds,
+                              cudaStream_t s);
 template <class T, class S>
 cudaError_t launch_lean_pack(const Geom &G, int split, int ncomp, const S *src, T *dst,
                              cudaStream_t s);

@@ -79,8 +79,14 @@ cudaError_t launch_adj_restrict(const AdjArgs<float> &A, const Geom &C, const fl
 // ---- lean cycles of the Newton step (lin_lean_kernels.cuh), FP32 for the
 // mixed-precision solve and FP64 for the comparison path built the same way
 template <class T>
-cudaError_t launch_lean_gsrb(const LinLeanT<T> &P, int pass, cudaStream_t s) {
-  MLGPU_DIM_SWITCH(P.G.dim, (lean_gsrb_kernel<T, DIM><<<blocks_for(P.G.ncell >> 1), kBlock, 0, s>>>(P, pass)));
+cudaError_t launch_lean_gsrb(const LinLeanT<T> &P, int pass, cudaStream_t s, int vec) {
+  constexpr int V = Vec16<T>::V;
+  if (vec && ((P.G.n0 >> 1) % V) == 0) {
+    const long long groups = (P.G.ncell >> 1) / V;
+    MLGPU_DIM_SWITCH(P.G.dim, (lean_gsrb_vec_kernel<T, DIM><<<blocks_for(groups), kBlock, 0, s>>>(P, pass)));
+  } else {
+    MLGPU_DIM_SWITCH(P.G.dim, (lean_gsrb_kernel<T, DIM><<<blocks_for(P.G.ncell >> 1), kBlock, 0, s>>>(P, pass)));
+  }
   return cudaGetLastError();
 }
 
@@ -157,6 +163,13 @@ cudaError_t launch_lean_prolong(const LinLeanT<T> &P, const Geom &C, int csplit,
   return cudaGetLastError();
 }
 
+template <class T>
+cudaError_t launch_lean_state(const AdjArgs<T> &A, const double *u, T *Js, T *Ks, T *Ds,
+                              cudaStream_t s) {
+  MLGPU_DIM_SWITCH(A.G.dim, (lean_state_kernel<T, DIM><<<blocks_for(A.G.ncell), kBlock, 0, s>>>(A, u, Js, Ks, Ds)));
+  return cudaGetLastError();
+}
+
 template <class T, class S>
 cudaError_t launch_lean_pack(const Geom &G, int split, int ncomp, const S *src, T *dst,
                              cudaStream_t s) {
@@ -188,7 +201,7 @@ cudaError_t launch_lean_step(const Geom &G, int split, const StepClip *clip, dou
 }
 
 #define MLGPU_LEAN_INST(T)                                                                     \
-  template cudaError_t launch_lean_gsrb<T>(const LinLeanT<T> &, int, cudaStream_t);           \
+  template cudaError_t launch_lean_gsrb<T>(const LinLeanT<T> &, int, cudaStream_t, int);      \
   template cudaError_t launch_lean_residual<T>(const LinLeanT<T> &, int, int, int, double *,   \
                                               int *, cudaStream_t);                           \
   template cudaError_t launch_lean_restrict<T>(const LinLeanT<T> &, const Geom &, int, int,    \
@@ -198,7 +211,9 @@ cudaError_t launch_lean_step(const Geom &G, int split, const StepClip *clip, dou
   template cudaError_t launch_lean_pack<T, double>(const Geom &, int, int, const double *, T *, \
                                                   cudaStream_t);                              \
   template cudaError_t launch_lean_step<T>(const Geom &, int, const StepClip *, double *,        \
-                                          const double *, double, const T *, cudaStream_t);
+                                          const double *, double, const T *, cudaStream_t);     \
+  template cudaError_t launch_lean_state<T>(const AdjArgs<T> &, const double *, T *, T *, T *,   \
+                                           cudaStream_t);
 MLGPU_LEAN_INST(float)
 MLGPU_LEAN_INST(double)
 template cudaError_t launch_lean_pack<float, float>(const Geom &, int, int, const float *,

@@ -171,6 +171,176 @@ __global__ void __launch_bounds__(kBlock) lean_gsrb_kernel(LinLeanT<T> P, int pa
   }
 }
 
+// The same half sweep with V = 16 / sizeof(T) consecutive cells of one row of
+// the colour's half per thread (4 in FP32, 2 in FP64): the cells' own g, K,
+// J, the y and z neighbours' w (the same positions in the neighbouring rows of
+// the other half) as 16-byte vector loads, the x neighbours' w as one vector
+// and one scalar, x and w stored as vectors.  Each cell's arithmetic is
+// lean_gsrb_kernel's in the same order (the same bits).  Needs n0 / 2 a
+// multiple of V (then so are the row starts, the half and the array offsets).
+template <class T>
+struct Vec16;
+template <>
+struct Vec16<float> {
+  using type = float4;
+  static constexpr int V = 4;
+};
+template <>
+struct Vec16<double> {
+  using type = double2;
+  static constexpr int V = 2;
+};
+
+template <class T>
+__device__ __forceinline__ void ldv(const T *__restrict__ p, T *out) {
+  using VT = typename Vec16<T>::type;
+  const VT v = *reinterpret_cast<const VT *>(p);
+  if constexpr (Vec16<T>::V == 4) {
+    out[0] = v.x;
+    out[1] = v.y;
+    out[2] = v.z;
+    out[3] = v.w;
+  } else {
+    out[0] = v.x;
+    out[1] = v.y;
+  }
+}
+
+template <class T>
+__device__ __forceinline__ void stv(T *__restrict__ p, const T *in) {
+  using VT = typename Vec16<T>::type;
+  VT v;
+  if constexpr (Vec16<T>::V == 4) {
+    v.x = in[0];
+    v.y = in[1];
+    v.z = in[2];
+    v.w = in[3];
+  } else {
+    v.x = in[0];
+    v.y = in[1];
+  }
+  *reinterpret_cast<VT *>(p) = v;
+}
+
+template <class T, int DIM>
+__global__ void __launch_bounds__(kBlock) lean_gsrb_vec_kernel(LinLeanT<T> P, int pass) {
+  constexpr int V = Vec16<T>::V;
+  const Geom &G = P.G;
+  const long long n = G.ncell, half = n >> 1;
+  const int h0 = G.n0 >> 1;
+  const long long base = pass * half, obase = half - base;  // own / other half
+  const long long ngroups = half / V;
+  const long long nf0 = (long long)(G.n0 + 1) * G.n1 * G.n2;
+  const long long nf1 = (long long)G.n0 * (G.n1 + 1) * G.n2;
+  const long long pl = (long long)G.n0 * G.n1, nf2 = pl * (G.n2 + 1);
+  const T *w = P.w;
+  for (long long t = gtid(); t < ngroups; t += gstride()) {
+    const long long u = t * V;
+    const unsigned row = (unsigned)u / (unsigned)h0;
+    const int hh = (int)((unsigned)u - row * (unsigned)h0);
+    const int k = (int)(row / (unsigned)G.n1), j = (int)(row - (unsigned)k * G.n1);
+    const int par = (j + k + pass) & 1;  // i of the group's first cell = 2 hh + par
+    const long long q = base + u;
+    T s0[V], s1[V];
+#pragma unroll
+    for (int v = 0; v < V; v++) s0[v] = s1[v] = T(0);
+    // x: the other colour's w at hh - 1 + par .. hh + V - 1 + par of this row
+    {
+      const long long ob = obase + (long long)row * h0;
+      T wv0[V], wv1[V];
+      ldv(w + ob + hh, wv0);
+      ldv(w + n + ob + hh, wv1);
+      // the extra value: hh - 1 (par 0) or hh + V (par 1), wrapped when periodic
+      int xe = par ? hh + V : hh - 1;
+      bool has_e = true;
+      if (xe < 0) {
+        xe = h0 - 1;
+        has_e = G.per0 != 0;
+      } else if (xe >= h0) {
+        xe = 0;
+        has_e = G.per0 != 0;
+      }
+      const T e0 = has_e ? w[ob + xe] : T(0), e1 = has_e ? w[n + ob + xe] : T(0);
+      const long long f0 = (long long)row * (G.n0 + 1) + 2 * hh + par;  // low face of cell 0
+#pragma unroll
+      for (int v = 0; v < V; v++) {
+        const long long f = f0 + 2 * v;
+        // low neighbour: hh + v - 1 + par (register selects: v is a constant
+        // of the unrolled loop, only par is not)
+        const int vl = v > 0 ? v - 1 : 0, vh = v < V - 1 ? v + 1 : V - 1;
+        const bool lo_e = par == 0 && v == 0;
+        if (!lo_e || has_e) {
+          const T a0 = lo_e ? e0 : (par ? wv0[v] : wv0[vl]);
+          const T a1 = lo_e ? e1 : (par ? wv1[v] : wv1[vl]);
+          s0[v] = fmaT(P.b[0][f], a0, s0[v]);
+          s1[v] = fmaT(P.b[0][nf0 + f], a1, s1[v]);
+        }
+        // high neighbour: hh + v + par
+        const bool hi_e = par == 1 && v == V - 1;
+        if (!hi_e || has_e) {
+          const T a0 = hi_e ? e0 : (par ? wv0[vh] : wv0[v]);
+          const T a1 = hi_e ? e1 : (par ? wv1[vh] : wv1[v]);
+          s0[v] = fmaT(P.b[0][f + 1], a0, s0[v]);
+          s1[v] = fmaT(P.b[0][nf0 + f + 1], a1, s1[v]);
+        }
+      }
+    }
+    // y and z: the same positions hh .. hh + V - 1 in the neighbouring rows
+#pragma unroll
+    for (int d = 1; d < DIM; d++) {
+      const int m = d == 1 ? G.n1 : G.n2, c = d == 1 ? j : k;
+      const bool per = d == 1 ? G.per1 != 0 : G.per2 != 0;
+      const long long nf = d == 1 ? nf1 : nf2;
+      const long long step = d == 1 ? G.n0 : pl;  // face stride of the direction
+      // low face of cell v: natural face index of (i_v, j, k) in direction d
+      const long long fb = d == 1 ? ((long long)k * (G.n1 + 1) + j) * G.n0 + 2 * hh + par
+                                  : (long long)row * G.n0 + 2 * hh + par;
+#pragma unroll
+      for (int side = 0; side < 2; side++) {
+        int cn = c + (side ? 1 : -1);
+        if (cn < 0 || cn >= m) {
+          if (!per || m == 1) continue;
+          cn = cn < 0 ? m - 1 : 0;
+        }
+        const unsigned nrow = d == 1 ? (unsigned)k * G.n1 + cn : (unsigned)cn * G.n1 + j;
+        T nb0[V], nb1[V];
+        ldv(w + obase + (long long)nrow * h0 + hh, nb0);
+        ldv(w + n + obase + (long long)nrow * h0 + hh, nb1);
+#pragma unroll
+        for (int v = 0; v < V; v++) {
+          const long long f = fb + 2 * v + (side ? step : 0);
+          s0[v] = fmaT(P.b[d][f], nb0[v], s0[v]);
+          s1[v] = fmaT(P.b[d][nf + f], nb1[v], s1[v]);
+        }
+      }
+    }
+    T g0[V], g1[V], K0[V], K1[V], K2[V], K3[V], J0[V], J1[V], J2[V], J3[V];
+    ldv(P.g + q, g0);
+    ldv(P.g + n + q, g1);
+    ldv(P.K + q, K0);
+    ldv(P.K + n + q, K1);
+    ldv(P.K + 2 * n + q, K2);
+    ldv(P.K + 3 * n + q, K3);
+    ldv(P.J + q, J0);
+    ldv(P.J + n + q, J1);
+    ldv(P.J + 2 * n + q, J2);
+    ldv(P.J + 3 * n + q, J3);
+    T x0[V], x1[V], w0[V], w1[V];
+#pragma unroll
+    for (int v = 0; v < V; v++) {
+      const T r0 = fmaT(P.bdx, s0[v], g0[v]), r1 = fmaT(P.bdx, s1[v], g1[v]);
+      x0[v] = fmaT(K0[v], r0, K2[v] * r1);
+      x1[v] = fmaT(K1[v], r0, K3[v] * r1);
+      w0[v] = fmaT(J0[v], x0[v], J1[v] * x1[v]);
+      w1[v] = fmaT(J2[v], x0[v], J3[v] * x1[v]);
+    }
+    stv(P.x + q, x0);
+    stv(P.x + n + q, x1);
+    stv(P.w + q, w0);
+    stv(P.w + n + q, w1);
+  }
+}
+
 // g - A x at the cell of index q (both components)
 template <class T, int DIM, class IDX>
 __device__ __forceinline__ void lean_res(const LinLeanT<T> &P, int i, int j, int k, long long q,
@@ -277,6 +447,121 @@ __global__ void __launch_bounds__(kBlock) lean_prolong_kernel(LinLeanT<T> P, Geo
     P.x[n + q] = x1;
     P.w[q] = fmaT(P.J[q], x0, P.J[n + q] * x1);
     P.w[n + q] = fmaT(P.J[2 * n + q], x0, P.J[3 * n + q] * x1);
+  }
+}
+
+// 2x2 diagonal block M of A^T at cell (i, j, k) (row-major, M[2c + c'] =
+// d(A^T y)_c / d y_c'; A's own block is M^T), given the cell's closure
+// Jacobian Jc (row-major {dT/dH, dT/dC, dC_l/dH, dC_l/dC}): adj_cell's
+// WANT_M terms alone, which read no neighbour --
+//   M(c, c') = delta alpha a_c + beta dxinv (J(c', c) P_c' - X(c, c')),
+// P_c the sum of the cell's face coefficients by face kind (interior or
+// periodic: b; derived-rule wall: 2b Dirichlet, 0 Neumann; (H, C)-condition
+// wall: b) and X the (H, C)-condition walls' ghost-Jacobian terms.
+template <class T, int DIM>
+__device__ __forceinline__ void lean_diag_block(const AdjArgs<T> &A, long long q, int i, int j,
+                                                int k, const T Jc[4], T M[4]) {
+  const Geom &G = A.G;
+  const int idx[3] = {i, j, k};
+  T P[2], X[4] = {T(0), T(0), T(0), T(0)};
+#pragma unroll
+  for (int c = 0; c < 2; c++) {
+    T p = T(0);
+#pragma unroll
+    for (int d = 0; d < DIM; d++) {
+      const int m = G.n(d);
+      const long long nf = G.nface(d);
+#pragma unroll
+      for (int side = 1; side >= 0; side--) {
+        int fi[3] = {idx[0], idx[1], idx[2]};
+        if (side) fi[d] += 1;
+        const T bf = A.b[d][c * nf + G.face(d, fi[0], fi[1], fi[2])];
+        const int nb = idx[d] + (side ? 1 : -1);
+        T dp;
+        if (nb >= 0 && nb < m)
+          dp = bf;
+        else if (G.per(d))
+          dp = m == 1 ? T(0) : bf;
+        else if (A.apply_dbc)
+          dp = A.dbc.type[d][side][c] == MLGPU_BC_DIRICHLET ? T(2) * bf : T(0);
+        else
+          dp = bf;
+        p = p + dp;
+      }
+    }
+    P[c] = p;
+  }
+  if (!A.apply_dbc) {
+#pragma unroll
+    for (int d = 0; d < DIM; d++) {
+      if (G.per(d)) continue;
+      const int m = G.n(d);
+      const long long nf = G.nface(d);
+#pragma unroll
+      for (int side = 0; side < 2; side++) {
+        if (side ? idx[d] != m - 1 : idx[d] != 0) continue;
+        int fi[3] = {idx[0], idx[1], idx[2]};
+        if (side) fi[d] += 1;
+        const long long f = G.face(d, fi[0], fi[1], fi[2]);
+        const T b0 = A.b[d][f], b1 = A.b[d][nf + f];
+        double Jg[4];
+        adj_ghost_jac(A, q, d, side, Jg);
+#pragma unroll
+        for (int c = 0; c < 2; c++) {
+          const T sc = A.phi_bc.type[d][side][c] == MLGPU_BC_DIRICHLET ? T(-1) : T(1);
+          X[2 * c + 0] = X[2 * c + 0] + sc * ((T)Jg[c] * b0);
+          X[2 * c + 1] = X[2 * c + 1] + sc * ((T)Jg[2 + c] * b1);
+        }
+      }
+    }
+  }
+  const long long n = G.ncell;
+#pragma unroll
+  for (int c = 0; c < 2; c++) {
+    const T av = A.a ? A.a[q + c * n] : T(1);
+#pragma unroll
+    for (int cp = 0; cp < 2; cp++) {
+      T v = A.beta * A.dxinv * (Jc[2 * cp + c] * P[cp] - X[2 * c + cp]);
+      if (cp == c) v = A.alpha * av + v;
+      M[2 * c + cp] = v;
+    }
+  }
+}
+
+// Per Newton state, on a smoothed level: the closure Jacobian J (FP32 in t_cl's
+// regime for T = float, t_cl_jac for double), A's diagonal block D = M^T and
+// K = (D^T)^-1 = M^-1 of every cell, written straight to the split layout (the
+// generic route -- adj_jac, adj_minv through the full adjoint cell operator,
+// three permutations -- moves four times the bytes)
+template <class T, int DIM>
+__global__ void __launch_bounds__(kBlock) lean_state_kernel(AdjArgs<T> A,
+                                                            const double *__restrict__ u,
+                                                            T *__restrict__ Js,
+                                                            T *__restrict__ Ks,
+                                                            T *__restrict__ Ds) {
+  const Geom &G = A.G;
+  const long long n = G.ncell;
+  for (long long q = gtid(); q < n; q += gstride()) {
+    int i, j, k;
+    cell_ijk(G, q, i, j, k);
+    T Jc[4], M[4];
+    if constexpr (sizeof(T) == 4)
+      t_cl_jac32(u[q], u[q + n], A.cp, Jc);
+    else
+      t_cl_jac(u[q], u[q + n], A.cp, Jc);
+    lean_diag_block<T, DIM>(A, q, i, j, k, Jc, M);
+    const T det = M[0] * M[3] - M[1] * M[2];
+    const long long o = cs_index(G, i, j, k);
+#pragma unroll
+    for (int m = 0; m < 4; m++) Js[o + m * n] = Jc[m];
+    Ks[o] = M[3] / det;
+    Ks[o + n] = -M[1] / det;
+    Ks[o + 2 * n] = -M[2] / det;
+    Ks[o + 3 * n] = M[0] / det;
+    Ds[o] = M[0];
+    Ds[o + n] = M[2];
+    Ds[o + 2 * n] = M[1];
+    Ds[o + 3 * n] = M[3];
   }
 }
 

@@ -1436,31 +1436,32 @@ class HCAdjSolver : public mlgpu_solver {
       CK(launch_restrict_avg<double>(L[l - 1].G, 2, L[l - 1].u, L[l].u, s));
     const ClosureParams cp = make_cp(op.params);
     if (lin32()) {
-      // FP64 closure derivative stored in FP32; the inverse blocks in FP32;
-      // the smoothed levels' copies packed to the split layout
-      for (auto &lv : L) CK(launch_adj_jac(lv.G, cp, lv.u, lv.J32, s));
+      // smoothed levels: J (FP32, t_cl's regime), D and K straight to the
+      // split layout; the bottom: J, the inverse blocks and D natural, for the
+      // generic bottom solve
       for (size_t l = 0; l < L.size(); l++) {
         AdjLevel &lv = L[l];
+        if (split((int)l)) {
+          CK(launch_lean_state<float>(args32((int)l), lv.u, lv.J32s, lv.K32s, lv.D32s, s));
+          continue;
+        }
+        CK(launch_adj_jac(lv.G, cp, lv.u, lv.J32, s));
         CK(cudaMemsetAsync(lv.r32, 0, sizeof(float) * 2 * lv.G.ncell, s));
         CK(launch_adj_minv(args32((int)l), lv.r32, lv.Minv32, lv.D32, s));
-        if (!split((int)l)) continue;
-        CK(launch_lean_pack<float, float>(lv.G, 1, 4, lv.J32, lv.J32s, s));
-        CK(launch_lean_pack<float, float>(lv.G, 1, 4, lv.Minv32, lv.K32s, s));
-        CK(launch_lean_pack<float, float>(lv.G, 1, 4, lv.D32, lv.D32s, s));
       }
       return MLGPU_OK;
     }
     const bool lean64 = fast64 && !tr;
-    for (auto &lv : L) CK(launch_adj_jac(lv.G, cp, lv.u, lv.J, s));
-    // the smoother's inverse diagonal blocks (r is free here: a zero field)
     for (size_t l = 0; l < L.size(); l++) {
       AdjLevel &lv = L[l];
+      if (lean64 && split((int)l)) {
+        CK(launch_lean_state<double>(args((int)l), lv.u, lv.J64s, lv.K64s, lv.D64s, s));
+        continue;
+      }
+      CK(launch_adj_jac(lv.G, cp, lv.u, lv.J, s));
+      // the smoother's inverse diagonal blocks (r is free here: a zero field)
       CK(cudaMemsetAsync(lv.r, 0, sizeof(double) * 2 * lv.G.ncell, s));
       CK(launch_adj_minv(args((int)l), lv.r, lv.Minv, lean64 ? lv.D64 : nullptr, s));
-      if (!lean64 || !split((int)l)) continue;
-      CK(launch_lean_pack<double, double>(lv.G, 1, 4, lv.J, lv.J64s, s));
-      CK(launch_lean_pack<double, double>(lv.G, 1, 4, lv.Minv, lv.K64s, s));
-      CK(launch_lean_pack<double, double>(lv.G, 1, 4, lv.D64, lv.D64s, s));
     }
     return MLGPU_OK;
   }
@@ -1514,7 +1515,7 @@ class HCAdjSolver : public mlgpu_solver {
   int lin_smooth(int l, int n) {
     const LinLeanT<T> P = leanT<T>(l);
     for (int i = 0; i < n; i++)
-      for (int pass = 0; pass < 2; pass++) CK(launch_lean_gsrb<T>(P, pass, s));
+      for (int pass = 0; pass < 2; pass++) CK(launch_lean_gsrb<T>(P, pass, s, lean_vec));
     return MLGPU_OK;
   }
 
@@ -1623,6 +1624,7 @@ class HCAdjSolver : public mlgpu_solver {
   int lin_max = 12;
   double clip = 0.1;
   int forcing = 1;
+  int lean_vec = 1;  // vector-load half sweeps where a level's rows allow them
 
   StepClip step_clip() const {
     const ClosureParams cp = make_cp(op.params);
@@ -1799,7 +1801,7 @@ class HCAdjSolver : public mlgpu_solver {
     }
     int rc = enter();
     const LinLean P = lean(0);
-    auto one = [&](int i) { return launch_lean_gsrb(P, i & 1, s); };
+    auto one = [&](int i) { return launch_lean_gsrb(P, i & 1, s, lean_vec); };
     if (!rc && one(0) != cudaSuccess) rc = MLGPU_ERR_CUDA;  // warm
     if (!rc && cudaEventRecord(e0, s) != cudaSuccess) rc = MLGPU_ERR_CUDA;
     for (int i = 0; i < reps && !rc; i++)
@@ -2180,14 +2182,25 @@ int mlgpu_hc_backward_euler_newton(mlgpu_solver *S, double *phi_new, const doubl
 }
 
 int mlgpu_hc_newton_params(mlgpu_solver *S, double lin_tol, int lin_max, double clip,
-                           int forcing) {
+                           int forcing, int vector_sweeps) {
   HCAdjSolver *A = dynamic_cast<HCAdjSolver *>(S);
   if (!A || !(lin_tol > 0.0 && lin_tol < 1.0) || lin_max < 1 || !(clip < 0.0 || clip <= 1.0) ||
-      (forcing != 0 && forcing != 1))
+      (forcing != 0 && forcing != 1) || (vector_sweeps != 0 && vector_sweeps != 1))
     return MLGPU_ERR_ARG;
+  if (A->lean_vec != vector_sweeps) {  // the captured cycles name the kernel
+    for (auto *gp : {&A->graph, &A->graph_lin, &A->graph_lin32})
+      if (*gp) {
+        cudaGraphExecDestroy(*gp);
+        *gp = nullptr;
+      }
+    A->nk_iter = -1;
+    A->nk_state = -1;
+    A->nk_res = -1;
+  }
   A->lin_tol = lin_tol;
   A->lin_max = lin_max;
   A->forcing = forcing;
+  A->lean_vec = vector_sweeps;
   A->clip = clip < 0.0 ? -1.0 : clip;
   return MLGPU_OK;
 }

@@ -223,7 +223,7 @@ def _declare(lib):
         "mlgpu_hc_adjoint_bc_gradient": (i, [vp, vp, P(d)]),
         "mlgpu_hc_newton_solve": (i, [vp, vp, vp, P(SolveStats)]),
         "mlgpu_hc_newton_sweep_time": (i, [vp, i, i, P(d)]),
-        "mlgpu_hc_newton_params": (i, [vp, d, i, d, i]),
+        "mlgpu_hc_newton_params": (i, [vp, d, i, d, i, i]),
         "mlgpu_hc_backward_euler_newton": (i, [vp, vp, vp, vp, vp, d, vp, P(SolveStats)]),
         "mlgpu_hc_backward_euler_adjoint": (i, [vp, vp, vp, vp, d, vp, vp, vp, P(d),
                                                 P(SolveStats)]),

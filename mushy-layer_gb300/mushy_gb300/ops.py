@@ -470,12 +470,13 @@ class AdjointMultiGrid(_Solver):
         _ok(rc, "adjointSolve")
         return st, rc
 
-    def setNewtonParams(self, lin_tol=0.3, lin_max=12, clip=0.1, forcing=1):
+    def setNewtonParams(self, lin_tol=0.3, lin_max=12, clip=0.1, forcing=1, vector_sweeps=1):
         """Linear tolerance (the cap of the Eisenstat-Walker forcing term when
-        forcing=1) and cycle cap of each Newton step, and the regime clipping
-        of its update (clip < 0: off)."""
+        forcing=1) and cycle cap of each Newton step, the regime clipping of
+        its update (clip < 0: off), vector-load half sweeps (same bits)."""
         abi.check(abi.load().mlgpu_hc_newton_params(self.h, float(lin_tol), int(lin_max),
-                                                    float(clip), int(forcing)),
+                                                    float(clip), int(forcing),
+                                                    int(vector_sweeps)),
                   "setNewtonParams")
 
     def newtonSolve(self, phi, rhs):

@@ -218,3 +218,30 @@ def test_one_level_hierarchy_natural_layout(shape):
     u64 = out["fp64"]
     assert np.abs(out["mixed"] - u64).max() <= 1e-8 * np.abs(u64).max()
     assert np.abs(out["fp64_fast"] - u64).max() <= 1e-11 * np.abs(u64).max()
+
+
+@pytest.mark.parametrize("prec,fuse", [(abi.PREC_MIXED, 1), (abi.PREC_F64, 2)])
+@pytest.mark.parametrize("case", ["3d_periodic_xy", "2d_walls"])
+def test_vector_half_sweeps_same_bits(prec, fuse, case):
+    """The lean cycles' vector-load half sweeps (4 FP32 / 2 FP64 cells per
+    thread) against one cell per thread: the same Newton steps, cycles and
+    solution bits (3D periodic x / y with walls in z; 2D walls all round)."""
+    from mushy_gb300 import ops
+    if case == "3d_periodic_xy":
+        g, phi0, op, ref, dt = _c4_like(32)
+    else:
+        g, prm, phi_bc, der, phi0, b = _c1()
+        dt = 1e-3
+        op = ops.NLMultiCompOp(g, prm, phi_bc, der, 1.0, -dt, None, [dev(x) for x in b])
+    out = []
+    for vec in (0, 1):
+        o = _opts(prec)
+        o.fuse_levels = fuse
+        S = ops.AdjointMultiGrid(op, o)
+        S.setNewtonParams(vector_sweeps=vec)
+        new = dev(phi0)
+        st, rc = S.backwardEulerNewton(new, dev(phi0), dt)
+        assert rc == 0 and st.final_norm <= 1e-10 * st.initial_norm
+        out.append((host(new), st.iterations, st.cycles))
+    assert out[0][1:] == out[1][1:]
+    assert np.array_equal(out[0][0], out[1][0])
