@@ -312,10 +312,11 @@ __global__ void __launch_bounds__(kBlock) adj_jac_kernel(Geom G, ClosureParams c
                                                          const double *__restrict__ u,
                                                          T *__restrict__ J) {
   const long long n = G.ncell;
+  const ClosureF32 f = make_closure_f32(cp);
   for (long long q = gtid(); q < n; q += gstride()) {
     T j4[4];
     if constexpr (sizeof(T) == 4)
-      t_cl_jac32(u[q], u[q + n], cp, j4);
+      t_cl_jac32(u[q], u[q + n], cp, f, j4);
     else
       t_cl_jac(u[q], u[q + n], cp, j4);
 #pragma unroll

@@ -137,6 +137,11 @@ cudaError_t launch_nlc_gsrb(const NLArgs<double> &A, double *phi, const double *
 cudaError_t launch_nlc_relax_block(const NLArgs<double> &A, double *phi, const double *rhs,
                                    double *tcl, const double *lam, int sweeps, int init,
                                    cudaStream_t s);
+// the lean Newton paths' residual rhs - N(phi) over the cache, with its L2
+// (part) and max (part_max) norm partials
+cudaError_t launch_nlc_res_lean(const NLArgs<double> &A, const double *phi, const double *tcl,
+                                const double *rhs, double *out, double *part, double *part_max,
+                                int *nparts, cudaStream_t s);
 // part_max: with a norm, the max-norm partials too (same count)
 cudaError_t launch_nlc_op(const NLArgs<double> &A, int mode, int norm, const double *phi,
                           const double *tcl, const double *rhs, double *out, double *copy,

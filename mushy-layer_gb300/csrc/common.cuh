@@ -264,19 +264,49 @@ __device__ __forceinline__ int closure_regime(double H, double C, const ClosureP
   return 4;
 }
 
+// FP32 constants of the closure for the FP32 derivative and regime test
+// (reciprocals of the constant divisors, so the per-cell work has no FP32
+// division by a constant)
+struct ClosureF32 {
+  float CR, k, cp, St, te, Te, inv_k, inv_CRTe, He_slope, inv_cp, a, two_a, inv_2a, four_a, b0,
+      omk, cpm1;
+};
+
+__host__ __device__ inline ClosureF32 make_closure_f32(const ClosureParams &p) {
+  ClosureF32 f;
+  f.CR = (float)p.CR;
+  f.k = (float)p.k;
+  f.cp = (float)p.cp;
+  f.St = (float)p.St;
+  f.te = (float)p.te;
+  f.Te = (float)p.Te;
+  f.inv_k = (float)(1.0 / p.k);
+  f.inv_CRTe = (float)(1.0 / (p.CR + p.Te));
+  f.He_slope = (float)(p.St + p.te * (1 - p.cp));
+  f.inv_cp = (float)(1.0 / p.cp);
+  const double a = p.CR * (p.cp - 1) + p.St * (p.k - 1);
+  f.a = (float)a;
+  f.two_a = (float)(2 * a);
+  f.inv_2a = (float)(1.0 / (2 * a));
+  f.four_a = (float)(4 * a);
+  f.b0 = (float)(p.CR * (1 - 2 * p.cp) - p.k * p.St);
+  f.omk = (float)(1 - p.k);
+  f.cpm1 = (float)(p.cp - 1);
+  return f;
+}
+
 // The same regime from FP32 bounding energies, with the FP64 test for the
 // cells near a bound (within 1e-4 of its scale, far above the FP32 rounding
 // of the bounds): every cell gets t_cl's own regime, at FP32 cost for all but
 // the few near a phase boundary.
-__device__ __forceinline__ int closure_regime_fast(double H, double C, const ClosureParams &p) {
+__device__ __forceinline__ int closure_regime_fast(double H, double C, const ClosureParams &p,
+                                                   const ClosureF32 &f) {
   const float h = (float)H, c = (float)C;
-  const float CR = (float)p.CR, k = (float)p.k, cpv = (float)p.cp, St = (float)p.St,
-              te = (float)p.te, Te = (float)p.Te;
-  float Hs = (c < -CR) ? 0.f : cpv * ((-c - CR) / k);
+  float Hs = (c < -f.CR) ? 0.f : f.cp * ((-c - f.CR) * f.inv_k);
   if (Hs < 0.f) Hs = 0.f;
-  Hs = Hs + te * cpv;
-  const float He = (CR + c) / (CR + Te) * (St + te * (1.f - cpv)) + cpv * te;
-  const float Hl = St - c + te + Te;
+  Hs = Hs + f.te * f.cp;
+  const float He = (f.CR + c) * f.inv_CRTe * f.He_slope + f.cp * f.te;
+  const float Hl = f.St - c + f.te + f.Te;
   const float band = 1e-4f;
   if (fabsf(h - Hs) < band * (1.f + fabsf(Hs)) || fabsf(h - He) < band * (1.f + fabsf(He)) ||
       fabsf(h - Hl) < band * (1.f + fabsf(Hl)))
@@ -335,10 +365,42 @@ __device__ __forceinline__ void t_cl_jac_in(int reg, T H, T C, const ClosurePara
 __device__ __forceinline__ void t_cl_jac(double H, double C, const ClosureParams &p, double J[4]) {
   t_cl_jac_in<double>(closure_regime(H, C, p), H, C, p, J);
 }
-// FP32 derivative in t_cl's own regime (closure_regime_fast)
+// FP32 derivative in t_cl's own regime (closure_regime_fast): t_cl_jac_in's
+// expressions with the constant divisors as reciprocals and the per-cell
+// divisors (sqrt(disc), den) as one correctly rounded reciprocal each
 __device__ __forceinline__ void t_cl_jac32(double H, double C, const ClosureParams &p,
-                                           float J[4]) {
-  t_cl_jac_in<float>(closure_regime_fast(H, C, p), (float)H, (float)C, p, J);
+                                           const ClosureF32 &f, float J[4]) {
+  const int reg = closure_regime_fast(H, C, p, f);
+  const float h = (float)H, c = (float)C;
+  J[0] = J[1] = J[2] = J[3] = 0.f;
+  if (reg == 0) {
+    J[0] = f.inv_cp;
+  } else if (reg == 2) {
+    float por = 1.f, dpH = 0.f, dpC = 0.f;
+    if (f.St != 0.f) {
+      const bool clamp = !(c >= -f.CR);
+      const float vC = clamp ? -f.CR : c;
+      const float b = f.b0 + h * f.omk - vC * f.cpm1;
+      const float cc = (f.CR + vC) * f.cp + f.k * h;
+      const float sD = sqrtf(b * b - f.four_a * cc);
+      const float isD = __frcp_rn(sD);
+      por = (-b - sD) * f.inv_2a;
+      const float dbH = f.omk, dbC = clamp ? 0.f : -f.cpm1;
+      const float dcH = f.k, dcC = clamp ? 0.f : f.cp;
+      dpH = (-dbH - (b * dbH - f.two_a * dcH) * isD) * f.inv_2a;
+      dpC = (-dbC - (b * dbC - f.two_a * dcC) * isD) * f.inv_2a;
+    }
+    const float num = c + f.CR * (1.f - por), den = por + f.k * (1.f - por);
+    const float iden = __frcp_rn(den);
+    const float dCl_dpor = (-f.CR * den - num * f.omk) * iden * iden;
+    J[2] = dCl_dpor * dpH;
+    J[3] = iden + dCl_dpor * dpC;
+    J[0] = -J[2];
+    J[1] = -J[3];
+  } else if (reg == 3) {
+    J[0] = 1.f;
+    J[3] = 1.f;
+  }
 }
 
 // Derivative of the porosity of the full closure (CALCULATEPOROSITY,

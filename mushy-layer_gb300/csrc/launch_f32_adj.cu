@@ -166,7 +166,8 @@ cudaError_t launch_lean_prolong(const LinLeanT<T> &P, const Geom &C, int csplit,
 template <class T>
 cudaError_t launch_lean_state(const AdjArgs<T> &A, const double *u, T *Js, T *Ks, T *Ds,
                               cudaStream_t s) {
-  MLGPU_DIM_SWITCH(A.G.dim, (lean_state_kernel<T, DIM><<<blocks_for(A.G.ncell), kBlock, 0, s>>>(A, u, Js, Ks, Ds)));
+  const ClosureF32 f = make_closure_f32(A.cp);
+  MLGPU_DIM_SWITCH(A.G.dim, (lean_state_kernel<T, DIM><<<blocks_for(A.G.ncell), kBlock, 0, s>>>(A, f, u, Js, Ks, Ds)));
   return cudaGetLastError();
 }
 

@@ -534,7 +534,7 @@ __device__ __forceinline__ void lean_diag_block(const AdjArgs<T> &A, long long q
 // generic route -- adj_jac, adj_minv through the full adjoint cell operator,
 // three permutations -- moves four times the bytes)
 template <class T, int DIM>
-__global__ void __launch_bounds__(kBlock) lean_state_kernel(AdjArgs<T> A,
+__global__ void __launch_bounds__(kBlock) lean_state_kernel(AdjArgs<T> A, ClosureF32 f,
                                                             const double *__restrict__ u,
                                                             T *__restrict__ Js,
                                                             T *__restrict__ Ks,
@@ -546,7 +546,7 @@ __global__ void __launch_bounds__(kBlock) lean_state_kernel(AdjArgs<T> A,
     cell_ijk(G, q, i, j, k);
     T Jc[4], M[4];
     if constexpr (sizeof(T) == 4)
-      t_cl_jac32(u[q], u[q + n], A.cp, Jc);
+      t_cl_jac32(u[q], u[q + n], A.cp, f, Jc);
     else
       t_cl_jac(u[q], u[q + n], A.cp, Jc);
     lean_diag_block<T, DIM>(A, q, i, j, k, Jc, M);
@@ -554,10 +554,18 @@ __global__ void __launch_bounds__(kBlock) lean_state_kernel(AdjArgs<T> A,
     const long long o = cs_index(G, i, j, k);
 #pragma unroll
     for (int m = 0; m < 4; m++) Js[o + m * n] = Jc[m];
-    Ks[o] = M[3] / det;
-    Ks[o + n] = -M[1] / det;
-    Ks[o + 2 * n] = -M[2] / det;
-    Ks[o + 3 * n] = M[0] / det;
+    if constexpr (sizeof(T) == 4) {  // one correctly rounded reciprocal
+      const float id = __frcp_rn(det);
+      Ks[o] = M[3] * id;
+      Ks[o + n] = -M[1] * id;
+      Ks[o + 2 * n] = -M[2] * id;
+      Ks[o + 3 * n] = M[0] * id;
+    } else {  // adj_minv_kernel's divisions
+      Ks[o] = M[3] / det;
+      Ks[o + n] = -M[1] / det;
+      Ks[o + 2 * n] = -M[2] / det;
+      Ks[o + 3 * n] = M[0] / det;
+    }
     Ds[o] = M[0];
     Ds[o + n] = M[2];
     Ds[o + 2 * n] = M[1];

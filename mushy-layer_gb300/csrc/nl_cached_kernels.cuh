@@ -219,6 +219,69 @@ __global__ void __launch_bounds__(kNLCBlock) nlc_op_kernel(NLArgs<double> A,
   }
 }
 
+// NL_RESIDUAL for the lean Newton paths: the same stencil over the cache
+// with FMA (s = sum b (f_nb - f_c), lof = (alpha a) phi - (beta dxinv) s),
+// its L2 norm by FMA and its max norm on the bit patterns of |v| (for
+// non-negative doubles the integer order is the numeric order, and a NaN's
+// pattern is above every number's, so it stays sticky) -- about two thirds
+// of the reference-order kernel's FP64 pipe operations; the same values to
+// rounding, not the same bits
+template <int DIM>
+__global__ void __launch_bounds__(kNLCBlock) nlc_res_lean_kernel(NLArgs<double> A,
+                                                                 const double *__restrict__ phi,
+                                                                 const double *__restrict__ tcl,
+                                                                 const double *__restrict__ rhs,
+                                                                 double *__restrict__ out,
+                                                                 double *__restrict__ part,
+                                                                 double *__restrict__ part_max) {
+  const Geom &G = A.G;
+  const long long n = G.ncell;
+  const double bd = A.beta * A.dxinv;
+  double acc = 0.0;
+  unsigned long long amax = 0ull;
+  for (long long q = gtid(); q < n; q += gstride()) {
+    int i, j, k;
+    cell_ijk(G, q, i, j, k);
+    const double h0 = phi[q], c0 = phi[q + n];
+    const double pl0[2] = {tcl[q], tcl[q + n]};
+    double lo[3][2], hi[3][2];
+#pragma unroll
+    for (int d = 0; d < DIM; d++) {
+      nlc_dv_nb(A, tcl, i, j, k, d, 0, h0, c0, pl0[0], pl0[1], lo[d][0], lo[d][1]);
+      nlc_dv_nb(A, tcl, i, j, k, d, 1, h0, c0, pl0[0], pl0[1], hi[d][0], hi[d][1]);
+    }
+    const double ph[2] = {h0, c0};
+#pragma unroll
+    for (int c = 0; c < 2; c++) {
+      const double p0 = pl0[c];
+      double s = 0.0;
+      s = fma(bface(A, 0, c, i + 1, j, k), hi[0][c] - p0, s);
+      s = fma(bface(A, 0, c, i, j, k), lo[0][c] - p0, s);
+      s = fma(bface(A, 1, c, i, j + 1, k), hi[1][c] - p0, s);
+      s = fma(bface(A, 1, c, i, j, k), lo[1][c] - p0, s);
+      if (DIM == 3) {
+        s = fma(bface(A, 2, c, i, j, k + 1), hi[2][c] - p0, s);
+        s = fma(bface(A, 2, c, i, j, k), lo[2][c] - p0, s);
+      }
+      const double aa = A.a ? A.alpha * A.a[q + c * n] : A.alpha;
+      const double lof = fma(aa, ph[c], -(bd * s));
+      const double v = rhs[q + c * n] - lof;
+      out[q + c * n] = v;
+      acc = fma(v, v, acc);
+      const unsigned long long bits =
+          (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+      amax = bits > amax ? bits : amax;
+    }
+  }
+  // two instantiations of block_reduce: two shared arrays, no reuse race
+  const double r = block_reduce<MLGPU_NORM_L2>(acc);
+  const double m = block_reduce<MLGPU_NORM_MAX>(__longlong_as_double((long long)amax));
+  if (threadIdx.x == 0) {
+    part[blockIdx.x] = r;
+    part_max[blockIdx.x] = m;
+  }
+}
+
 // FAS restriction fused with restrictR (nl_restrict_kernel over the cache)
 template <int DIM>
 __global__ void __launch_bounds__(kNLCBlock) nlc_restrict_kernel(NLArgs<double> A, Geom C,

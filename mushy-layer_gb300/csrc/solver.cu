@@ -1654,9 +1654,13 @@ class HCAdjSolver : public mlgpu_solver {
     // for a max-norm stopping test, its max norm in the same pass
     const NLArgs<double> N = make_nl_args<double>(op);
     const bool both = o.norm_type == MLGPU_NORM_MAX;
-    CK(launch_nlc_closure(N, L[0].u, ntcl, s, mixed || fast64));
-    CK(launch_nlc_op(N, NL_RESIDUAL, MLGPU_NORM_L2, L[0].u, ntcl, nf, L[0].g, nullptr, part,
-                     &nparts, s, both ? part2 : nullptr));
+    const bool lean = mixed || fast64;
+    CK(launch_nlc_closure(N, L[0].u, ntcl, s, lean));
+    if (lean && both)
+      CK(launch_nlc_res_lean(N, L[0].u, ntcl, nf, L[0].g, part, part2, &nparts, s));
+    else
+      CK(launch_nlc_op(N, NL_RESIDUAL, MLGPU_NORM_L2, L[0].u, ntcl, nf, L[0].g, nullptr, part,
+                       &nparts, s, both ? part2 : nullptr));
     CK(launch_finalize_norm(MLGPU_NORM_L2, part, nparts, part + kMaxBlocks, s));
     if (both) {
       CK(launch_finalize_norm(MLGPU_NORM_MAX, part2, nparts, part + kMaxBlocks + 1, s));
