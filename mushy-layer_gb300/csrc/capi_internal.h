@@ -113,10 +113,13 @@ cudaError_t launch_lean_restrict(const LinLeanT<T> &P, const Geom &C, int csplit
 template <class T>
 cudaError_t launch_lean_prolong(const LinLeanT<T> &P, const Geom &C, int csplit, int black,
                                 int kind, const T *xc, cudaStream_t s);
-// J, K, D of a smoothed level from the state u, in the split layout
+// per-cell face sums P of a smoothed level (natural layout), once per solver
 template <class T>
-cudaError_t launch_lean_state(const AdjArgs<T> &A, const double *u, T *Js, T *Ks, T *Ds,
-                              cudaStream_t s);
+cudaError_t launch_lean_psum(const AdjArgs<T> &A, T *P, cudaStream_t s);
+// J, K, D of a smoothed level from the state u and P, in the split layout
+template <class T>
+cudaError_t launch_lean_state(const AdjArgs<T> &A, const double *u, const T *P, T *Js, T *Ks,
+                              T *Ds, cudaStream_t s);
 template <class T, class S>
 cudaError_t launch_lean_pack(const Geom &G, int split, int ncomp, const S *src, T *dst,
                              cudaStream_t s);

@@ -270,6 +270,7 @@ __device__ __forceinline__ int closure_regime(double H, double C, const ClosureP
 struct ClosureF32 {
   float CR, k, cp, St, te, Te, inv_k, inv_CRTe, He_slope, inv_cp, a, two_a, inv_2a, four_a, b0,
       omk, cpm1;
+  double inv_k64, inv_CRTe64;  // 1/k, 1/(CR + Te) in FP64
 };
 
 __host__ __device__ inline ClosureF32 make_closure_f32(const ClosureParams &p) {
@@ -292,7 +293,29 @@ __host__ __device__ inline ClosureF32 make_closure_f32(const ClosureParams &p) {
   f.b0 = (float)(p.CR * (1 - 2 * p.cp) - p.k * p.St);
   f.omk = (float)(1 - p.k);
   f.cpm1 = (float)(p.cp - 1);
+  f.inv_k64 = 1.0 / p.k;
+  f.inv_CRTe64 = 1.0 / (p.CR + p.Te);
   return f;
+}
+
+// The regime of a cell near a bound, in FP64 with the constant divisors as
+// reciprocals (bounding_energy to an ulp; a cell within an ulp of a bound may
+// go either way, which no FP64 iterate resolves anyway): the regime-clipped
+// Newton update leaves many cells just past a bound, and FP64 divisions there
+// would dominate the kernels that call it.  Out of line: rarely taken, and
+// its FP64 registers would lower the callers' occupancy.
+__device__ __noinline__ int closure_regime_near(double H, double C, const ClosureParams &p,
+                                                double inv_k, double inv_CRTe) {
+  double Hs = (C < -p.CR) ? 0.0 : p.cp * ((-C - p.CR) * inv_k);
+  if (Hs < 0.0) Hs = 0.0;
+  Hs = Hs + p.te * p.cp;
+  const double He = (p.CR + C) * inv_CRTe * (p.St + p.te * (1 - p.cp)) + p.cp * p.te;
+  const double Hl = p.St - C + p.te + p.Te;
+  if (H <= Hs) return 0;
+  if (H > Hs && H <= He) return 1;
+  if (H > He && H < Hl) return 2;
+  if (H >= Hl) return 3;
+  return 4;
 }
 
 // The same regime from FP32 bounding energies, with the FP64 test for the
@@ -310,7 +333,7 @@ __device__ __forceinline__ int closure_regime_fast(double H, double C, const Clo
   const float band = 1e-4f;
   if (fabsf(h - Hs) < band * (1.f + fabsf(Hs)) || fabsf(h - He) < band * (1.f + fabsf(He)) ||
       fabsf(h - Hl) < band * (1.f + fabsf(Hl)))
-    return closure_regime(H, C, p);
+    return closure_regime_near(H, C, p, f.inv_k64, f.inv_CRTe64);
   if (h <= Hs) return 0;
   if (h <= He) return 1;
   if (h < Hl) return 2;

@@ -164,10 +164,16 @@ cudaError_t launch_lean_prolong(const LinLeanT<T> &P, const Geom &C, int csplit,
 }
 
 template <class T>
-cudaError_t launch_lean_state(const AdjArgs<T> &A, const double *u, T *Js, T *Ks, T *Ds,
-                              cudaStream_t s) {
+cudaError_t launch_lean_psum(const AdjArgs<T> &A, T *P, cudaStream_t s) {
+  MLGPU_DIM_SWITCH(A.G.dim, (lean_psum_kernel<T, DIM><<<blocks_for(A.G.ncell), kBlock, 0, s>>>(A, P)));
+  return cudaGetLastError();
+}
+
+template <class T>
+cudaError_t launch_lean_state(const AdjArgs<T> &A, const double *u, const T *P, T *Js, T *Ks,
+                              T *Ds, cudaStream_t s) {
   const ClosureF32 f = make_closure_f32(A.cp);
-  MLGPU_DIM_SWITCH(A.G.dim, (lean_state_kernel<T, DIM><<<blocks_for(A.G.ncell), kBlock, 0, s>>>(A, f, u, Js, Ks, Ds)));
+  MLGPU_DIM_SWITCH(A.G.dim, (lean_state_kernel<T, DIM><<<blocks_for(A.G.ncell), kBlock, 0, s>>>(A, f, u, P, Js, Ks, Ds)));
   return cudaGetLastError();
 }
 
@@ -213,8 +219,9 @@ cudaError_t launch_lean_step(const Geom &G, int split, const StepClip *clip, dou
                                                   cudaStream_t);                              \
   template cudaError_t launch_lean_step<T>(const Geom &, int, const StepClip *, double *,        \
                                           const double *, double, const T *, cudaStream_t);     \
-  template cudaError_t launch_lean_state<T>(const AdjArgs<T> &, const double *, T *, T *, T *,   \
-                                           cudaStream_t);
+  template cudaError_t launch_lean_state<T>(const AdjArgs<T> &, const double *, const T *, T *,  \
+                                           T *, T *, cudaStream_t);                              \
+  template cudaError_t launch_lean_psum<T>(const AdjArgs<T> &, T *, cudaStream_t);
 MLGPU_LEAN_INST(float)
 MLGPU_LEAN_INST(double)
 template cudaError_t launch_lean_pack<float, float>(const Geom &, int, int, const float *,

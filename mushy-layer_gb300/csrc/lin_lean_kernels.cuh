@@ -450,20 +450,15 @@ __global__ void __launch_bounds__(kBlock) lean_prolong_kernel(LinLeanT<T> P, Geo
   }
 }
 
-// 2x2 diagonal block M of A^T at cell (i, j, k) (row-major, M[2c + c'] =
-// d(A^T y)_c / d y_c'; A's own block is M^T), given the cell's closure
-// Jacobian Jc (row-major {dT/dH, dT/dC, dC_l/dH, dC_l/dC}): adj_cell's
-// WANT_M terms alone, which read no neighbour --
-//   M(c, c') = delta alpha a_c + beta dxinv (J(c', c) P_c' - X(c, c')),
-// P_c the sum of the cell's face coefficients by face kind (interior or
-// periodic: b; derived-rule wall: 2b Dirichlet, 0 Neumann; (H, C)-condition
-// wall: b) and X the (H, C)-condition walls' ghost-Jacobian terms.
+// P_c of cell (i, j, k): the sum of its face coefficients by face kind
+// (interior or periodic: b; derived-rule wall: 2b Dirichlet, 0 Neumann;
+// (H, C)-condition wall: b), adj_cell's WANT_M face sum; it reads no state,
+// so it is formed once per solver (lean_psum_kernel)
 template <class T, int DIM>
-__device__ __forceinline__ void lean_diag_block(const AdjArgs<T> &A, long long q, int i, int j,
-                                                int k, const T Jc[4], T M[4]) {
+__device__ __forceinline__ void lean_face_sums(const AdjArgs<T> &A, int i, int j, int k,
+                                               T P[2]) {
   const Geom &G = A.G;
   const int idx[3] = {i, j, k};
-  T P[2], X[4] = {T(0), T(0), T(0), T(0)};
 #pragma unroll
   for (int c = 0; c < 2; c++) {
     T p = T(0);
@@ -491,30 +486,68 @@ __device__ __forceinline__ void lean_diag_block(const AdjArgs<T> &A, long long q
     }
     P[c] = p;
   }
-  if (!A.apply_dbc) {
+}
+
+template <class T, int DIM>
+__global__ void __launch_bounds__(kBlock) lean_psum_kernel(AdjArgs<T> A, T *__restrict__ Pout) {
+  const Geom &G = A.G;
+  const long long n = G.ncell;
+  for (long long q = gtid(); q < n; q += gstride()) {
+    int i, j, k;
+    cell_ijk(G, q, i, j, k);
+    T P[2];
+    lean_face_sums<T, DIM>(A, i, j, k, P);
+    Pout[q] = P[0];
+    Pout[n + q] = P[1];
+  }
+}
+
+// 2x2 diagonal block M of A^T at cell (i, j, k) (row-major, M[2c + c'] =
+// d(A^T y)_c / d y_c'; A's own block is M^T), given the cell's closure
+// Jacobian Jc (row-major {dT/dH, dT/dC, dC_l/dH, dC_l/dC}) and face sums P:
+// adj_cell's WANT_M terms alone, which read no neighbour --
+//   M(c, c') = delta alpha a_c + beta dxinv (J(c', c) P_c' - X(c, c')),
+// X the (H, C)-condition walls' ghost-Jacobian terms (wall cells only).
+// X of a cell on an (H, C)-condition wall (out of line: the ghost closure
+// Jacobian is FP64 and long, and only wall cells take it)
+template <class T, int DIM>
+__device__ __noinline__ void lean_wall_terms(const AdjArgs<T> &A, long long q, int i, int j,
+                                             int k, T X[4]) {
+  const Geom &G = A.G;
+  const int idx[3] = {i, j, k};
 #pragma unroll
-    for (int d = 0; d < DIM; d++) {
-      if (G.per(d)) continue;
-      const int m = G.n(d);
-      const long long nf = G.nface(d);
+  for (int d = 0; d < DIM; d++) {
+    if (G.per(d)) continue;
+    const int m = G.n(d);
+    const long long nf = G.nface(d);
 #pragma unroll
-      for (int side = 0; side < 2; side++) {
-        if (side ? idx[d] != m - 1 : idx[d] != 0) continue;
-        int fi[3] = {idx[0], idx[1], idx[2]};
-        if (side) fi[d] += 1;
-        const long long f = G.face(d, fi[0], fi[1], fi[2]);
-        const T b0 = A.b[d][f], b1 = A.b[d][nf + f];
-        double Jg[4];
-        adj_ghost_jac(A, q, d, side, Jg);
+    for (int side = 0; side < 2; side++) {
+      if (side ? idx[d] != m - 1 : idx[d] != 0) continue;
+      int fi[3] = {idx[0], idx[1], idx[2]};
+      if (side) fi[d] += 1;
+      const long long f = G.face(d, fi[0], fi[1], fi[2]);
+      const T b0 = A.b[d][f], b1 = A.b[d][nf + f];
+      double Jg[4];
+      adj_ghost_jac(A, q, d, side, Jg);
 #pragma unroll
-        for (int c = 0; c < 2; c++) {
-          const T sc = A.phi_bc.type[d][side][c] == MLGPU_BC_DIRICHLET ? T(-1) : T(1);
-          X[2 * c + 0] = X[2 * c + 0] + sc * ((T)Jg[c] * b0);
-          X[2 * c + 1] = X[2 * c + 1] + sc * ((T)Jg[2 + c] * b1);
-        }
+      for (int c = 0; c < 2; c++) {
+        const T sc = A.phi_bc.type[d][side][c] == MLGPU_BC_DIRICHLET ? T(-1) : T(1);
+        X[2 * c + 0] = X[2 * c + 0] + sc * ((T)Jg[c] * b0);
+        X[2 * c + 1] = X[2 * c + 1] + sc * ((T)Jg[2 + c] * b1);
       }
     }
   }
+}
+
+template <class T, int DIM>
+__device__ __forceinline__ void lean_diag_block(const AdjArgs<T> &A, long long q, int i, int j,
+                                                int k, const T Jc[4], const T P[2], T M[4]) {
+  const Geom &G = A.G;
+  T X[4] = {T(0), T(0), T(0), T(0)};
+  const bool wall = (!G.per0 && (i == 0 || i == G.n0 - 1)) ||
+                    (!G.per1 && (j == 0 || j == G.n1 - 1)) ||
+                    (DIM == 3 && !G.per2 && (k == 0 || k == G.n2 - 1));
+  if (!A.apply_dbc && wall) lean_wall_terms<T, DIM>(A, q, i, j, k, X);
   const long long n = G.ncell;
 #pragma unroll
   for (int c = 0; c < 2; c++) {
@@ -536,6 +569,7 @@ __device__ __forceinline__ void lean_diag_block(const AdjArgs<T> &A, long long q
 template <class T, int DIM>
 __global__ void __launch_bounds__(kBlock) lean_state_kernel(AdjArgs<T> A, ClosureF32 f,
                                                             const double *__restrict__ u,
+                                                            const T *__restrict__ Psum,
                                                             T *__restrict__ Js,
                                                             T *__restrict__ Ks,
                                                             T *__restrict__ Ds) {
@@ -549,7 +583,8 @@ __global__ void __launch_bounds__(kBlock) lean_state_kernel(AdjArgs<T> A, Closur
       t_cl_jac32(u[q], u[q + n], A.cp, f, Jc);
     else
       t_cl_jac(u[q], u[q + n], A.cp, Jc);
-    lean_diag_block<T, DIM>(A, q, i, j, k, Jc, M);
+    const T P[2] = {Psum[q], Psum[n + q]};
+    lean_diag_block<T, DIM>(A, q, i, j, k, Jc, P, M);
     const T det = M[0] * M[3] - M[1] * M[2];
     const long long o = cs_index(G, i, j, k);
 #pragma unroll

@@ -1225,6 +1225,9 @@ struct AdjLevel {
   // precision (the natural ones above feed the bottom solve and the packing)
   float *J32s = nullptr, *K32s = nullptr, *D32s = nullptr;
   double *J64s = nullptr, *K64s = nullptr, *D64s = nullptr;
+  // their face sums P (lean_face_sums, natural layout), formed once
+  float *P32 = nullptr;
+  double *P64 = nullptr;
 };
 
 class HCAdjSolver : public mlgpu_solver {
@@ -1310,6 +1313,7 @@ class HCAdjSolver : public mlgpu_solver {
           L[l].J32s = A.get<float>(2 * n);
           L[l].K32s = A.get<float>(2 * n);
           L[l].D32s = A.get<float>(2 * n);
+          L[l].P32 = A.get<float>(n);
         }
       }
       if (fast64) {
@@ -1320,6 +1324,7 @@ class HCAdjSolver : public mlgpu_solver {
           L[l].J64s = A.get<double>(2 * n);
           L[l].K64s = A.get<double>(2 * n);
           L[l].D64s = A.get<double>(2 * n);
+          L[l].P64 = A.get<double>(n);
         }
       }
       g = coarsen_grid(g);
@@ -1347,6 +1352,11 @@ class HCAdjSolver : public mlgpu_solver {
         for (int d = 0; d < lv.G.dim; d++)
           CK(launch_convert<float, double>(2 * lv.G.nface(d), lv.c32.b[d], lv.c64.b[d], s));
       }
+    // the lean cycles' face sums of every smoothed level
+    for (size_t l = 0; l < L.size(); l++) {
+      if (L[l].P32) CK(launch_lean_psum<float>(args32((int)l), L[l].P32, s));
+      if (L[l].P64) CK(launch_lean_psum<double>(args((int)l), L[l].P64, s));
+    }
     const int last = (int)L.size() - 1;
     double u = 0;
     for (int l = 0; l <= last; l++) {
@@ -1442,7 +1452,8 @@ class HCAdjSolver : public mlgpu_solver {
       for (size_t l = 0; l < L.size(); l++) {
         AdjLevel &lv = L[l];
         if (split((int)l)) {
-          CK(launch_lean_state<float>(args32((int)l), lv.u, lv.J32s, lv.K32s, lv.D32s, s));
+          CK(launch_lean_state<float>(args32((int)l), lv.u, lv.P32, lv.J32s, lv.K32s, lv.D32s,
+                                      s));
           continue;
         }
         CK(launch_adj_jac(lv.G, cp, lv.u, lv.J32, s));
@@ -1455,7 +1466,7 @@ class HCAdjSolver : public mlgpu_solver {
     for (size_t l = 0; l < L.size(); l++) {
       AdjLevel &lv = L[l];
       if (lean64 && split((int)l)) {
-        CK(launch_lean_state<double>(args((int)l), lv.u, lv.J64s, lv.K64s, lv.D64s, s));
+        CK(launch_lean_state<double>(args((int)l), lv.u, lv.P64, lv.J64s, lv.K64s, lv.D64s, s));
         continue;
       }
       CK(launch_adj_jac(lv.G, cp, lv.u, lv.J, s));
