@@ -304,8 +304,9 @@ __host__ __device__ inline ClosureF32 make_closure_f32(const ClosureParams &p) {
 // Newton update leaves many cells just past a bound, and FP64 divisions there
 // would dominate the kernels that call it.  Out of line: rarely taken, and
 // its FP64 registers would lower the callers' occupancy.
-__device__ __noinline__ int closure_regime_near(double H, double C, const ClosureParams &p,
-                                                double inv_k, double inv_CRTe) {
+static __device__ __noinline__ int closure_regime_near(double H, double C,
+                                                       const ClosureParams &p, double inv_k,
+                                                       double inv_CRTe) {
   double Hs = (C < -p.CR) ? 0.0 : p.cp * ((-C - p.CR) * inv_k);
   if (Hs < 0.0) Hs = 0.0;
   Hs = Hs + p.te * p.cp;
