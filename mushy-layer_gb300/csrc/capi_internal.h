@@ -15,6 +15,7 @@
 #include "adjoint_kernels.cuh"
 #include "bicgstab_kernels.cuh"
 #include "lin_lean_kernels.cuh"
+#include "vc_lean_kernels.cuh"
 
 namespace mlgpu {
 
@@ -113,6 +114,16 @@ cudaError_t launch_lean_restrict(const LinLeanT<T> &P, const Geom &C, int csplit
 template <class T>
 cudaError_t launch_lean_prolong(const LinLeanT<T> &P, const Geom &C, int csplit, int black,
                                 int kind, const T *xc, cudaStream_t s);
+// lean FP32 cycles of the linear operator on 3D levels (vc_lean_kernels.cuh):
+// diag and 1/diag to the split layout (once per solver), red/black half
+// sweep (zero: the other colour's e is zero), residual restriction (red: the
+// red children only) with the coarse e zeroed, black-only prolongation
+cudaError_t launch_vcl_diag(const VCArgs<float> &A, float *idg, float *dg, cudaStream_t s);
+cudaError_t launch_vcl_gsrb(const VCLean &P, int pass, int zero, cudaStream_t s);
+cudaError_t launch_vcl_restrict(const VCLean &P, const Geom &C, int csplit, int red, float *rc,
+                                float *ec, cudaStream_t s);
+cudaError_t launch_vcl_prolong(const VCLean &P, const Geom &C, const BCD &bc, int csplit,
+                               int black, int kind, const float *ec, cudaStream_t s);
 // per-cell face sums P of a smoothed level (natural layout), once per solver
 template <class T>
 cudaError_t launch_lean_psum(const AdjArgs<T> &A, T *P, cudaStream_t s);

@@ -1,14 +1,14 @@
-// launch_f32_adj.cu -- FP32 launchers of the Jacobian kernels
-// (adjoint_kernels.cuh) for the inner linear cycles of the mixed-precision
-// Newton solve: the closure Jacobian J is evaluated in FP64 and stored in
-// FP32, the cycles (block red/black Gauss-Seidel with the inverse 2x2
-// diagonal block of each cell, 2^D residual restriction, prolongation, bottom
-// solve) run in FP32.  FMA contraction is left on, as in launch_f32.cu.
+// launch_f32_adj.cu -- launchers of the lean cycles: the FP32 Jacobian
+// kernels (adjoint_kernels.cuh) and the lean colour-split kernels
+// (lin_lean_kernels.cuh, FP32 and FP64) of the Newton step's linear cycles,
+// and the lean FP32 3D cycles of the linear operator (vc_lean_kernels.cuh).
+// FMA contraction is left on, as in launch_f32.cu.
 #define MLGPU_ADJ_UNIT 1
 #define MLGPU_ADJ_F32_UNIT 1
 #include "launch_impl.cuh"
 #include "adjoint_kernels.cuh"
 #include "lin_lean_kernels.cuh"
+#include "vc_lean_kernels.cuh"
 
 namespace mlgpu {
 
@@ -204,6 +204,65 @@ cudaError_t launch_lean_step(const Geom &G, int split, const StepClip *clip, dou
     MLGPU_LEAN_STEP(NaturalIdx)
   }
 #undef MLGPU_LEAN_STEP
+  return cudaGetLastError();
+}
+
+// ---- lean FP32 cycles of the linear operator on 3D levels (vc_lean_kernels.cuh)
+cudaError_t launch_vcl_diag(const VCArgs<float> &A, float *idg, float *dg, cudaStream_t s) {
+  MLGPU_DIM_SWITCH(A.G.dim, (vcl_diag_kernel<DIM><<<blocks_for(A.G.ncell), kBlock, 0, s>>>(A, idg, dg)));
+  return cudaGetLastError();
+}
+
+cudaError_t launch_vcl_gsrb(const VCLean &P, int pass, int zero, cudaStream_t s) {
+  MLGPU_DIM_SWITCH(P.G.dim, (vcl_gsrb_kernel<DIM><<<blocks_for(P.G.ncell >> 1), kBlock, 0, s>>>(P, pass, zero)));
+  return cudaGetLastError();
+}
+
+cudaError_t launch_vcl_restrict(const VCLean &P, const Geom &C, int csplit, int red, float *rc,
+                                float *ec, cudaStream_t s) {
+  const int nb = blocks_for(C.ncell);
+#define MLGPU_VCL_RST(IDX, RED) \
+  MLGPU_DIM_SWITCH(P.G.dim, (vcl_restrict_kernel<DIM, IDX, RED><<<nb, kBlock, 0, s>>>(P, C, rc, ec)))
+  if (csplit) {
+    if (red)
+      MLGPU_VCL_RST(SplitIdx, true);
+    else
+      MLGPU_VCL_RST(SplitIdx, false);
+  } else {
+    if (red)
+      MLGPU_VCL_RST(NaturalIdx, true);
+    else
+      MLGPU_VCL_RST(NaturalIdx, false);
+  }
+#undef MLGPU_VCL_RST
+  return cudaGetLastError();
+}
+
+cudaError_t launch_vcl_prolong(const VCLean &P, const Geom &C, const BCD &bc, int csplit,
+                               int black, int kind, const float *ec, cudaStream_t s) {
+  const int nb = blocks_for(black ? P.G.ncell >> 1 : P.G.ncell);
+#define MLGPU_VCL_PRO(KIND, IDX, BL) \
+  MLGPU_DIM_SWITCH(P.G.dim, (vcl_prolong_kernel<DIM, KIND, IDX, BL><<<nb, kBlock, 0, s>>>(P, C, bc, ec)))
+#define MLGPU_VCL_PRO2(KIND, IDX)    \
+  if (black)                         \
+    MLGPU_VCL_PRO(KIND, IDX, true);  \
+  else                               \
+    MLGPU_VCL_PRO(KIND, IDX, false);
+  if (kind == MLGPU_PROLONG_LINEAR) {
+    if (csplit) {
+      MLGPU_VCL_PRO2(MLGPU_PROLONG_LINEAR, SplitIdx)
+    } else {
+      MLGPU_VCL_PRO2(MLGPU_PROLONG_LINEAR, NaturalIdx)
+    }
+  } else {
+    if (csplit) {
+      MLGPU_VCL_PRO2(MLGPU_PROLONG_CONSTANT, SplitIdx)
+    } else {
+      MLGPU_VCL_PRO2(MLGPU_PROLONG_CONSTANT, NaturalIdx)
+    }
+  }
+#undef MLGPU_VCL_PRO2
+#undef MLGPU_VCL_PRO
   return cudaGetLastError();
 }
 

@@ -193,6 +193,10 @@ struct VCLevel {
   double *lam64 = nullptr;  // stored 1/diag for FP64 inner cycles
   float *fcx = nullptr, *fcy = nullptr, *flam = nullptr, *fdiag = nullptr;  // lean FP32 tiles
   double *ocx = nullptr, *ocy = nullptr, *odiag = nullptr;  // FP64 outer step (level 0, mixed)
+  // mixed 3D levels above the single-CTA block cycle: the lean FP32 cycles
+  // (vc_lean_kernels.cuh) with e, r colour-split and the diagonal folded
+  bool lean = false;
+  float *idg = nullptr, *dg = nullptr;
 };
 
 class VCSolver : public mlgpu_solver {
@@ -331,6 +335,16 @@ class VCSolver : public mlgpu_solver {
     // FP32 tiles pay for their halo recomputation; FP64 tiles (4 extra half
     // sweeps of redundant FP64 work per tile) only when asked for explicitly
     use_tiles = use_block_cycle && (mixed || o.fuse_levels >= 2);
+    // mixed 3D: every level above the block cycle (and above the bottom)
+    // runs the lean split cycles; such a level has even extents
+    if (mixed && op.grid.dim == 3 && o.relax_mode == MLGPU_RELAX_GSRB)
+      for (int l = 0; l < depth; l++) {
+        if (use_block_cycle && L[l].G.ncell <= kBlockCycleCells && depth - l + 1 <= kMaxBlockLevels)
+          break;
+        L[l].lean = true;
+        L[l].idg = A.get<float>(ncells(L[l].grid));
+        L[l].dg = A.get<float>(ncells(L[l].grid));
+      }
     size_t n0 = ncells(op.grid);
     phi[0] = A.get<double>(n0);
     phi[1] = A.get<double>(n0);
@@ -383,6 +397,8 @@ class VCSolver : public mlgpu_solver {
   // step (2D mixed precision)
   int build_fast() {
     if (L[0].ocx) CK(launch_outer_coefs(outer_args(), L[0].ocx, L[0].ocy, L[0].odiag, s));
+    for (size_t l = 0; l < L.size(); l++)
+      if (L[l].lean) CK(launch_vcl_diag(args<float>((int)l), L[l].idg, L[l].dg, s));
     for (size_t l = 0; l < L.size(); l++) {
       if (!L[l].fcx) continue;
       VCArgs<double> A = args<double>((int)l);
@@ -547,6 +563,55 @@ class VCSolver : public mlgpu_solver {
     return MLGPU_OK;
   }
 
+  // lean FP32 operator of a lean 3D level
+  VCLean vclean(int l) {
+    const VCArgs<float> A = args<float>(l);
+    VCLean P;
+    P.G = A.G;
+    P.bd = A.beta * A.dxinv;
+    for (int d = 0; d < 3; d++) P.b[d] = A.b[d];
+    P.idg = L[l].idg;
+    P.dg = L[l].dg;
+    P.e = (float *)L[l].e;
+    P.r = (const float *)L[l].r;
+    return P;
+  }
+
+  // n red/black sweeps of a lean level; a zero start skips the first half
+  // sweep's neighbour reads
+  int relax_lean(int l, int n, bool zero_init) {
+    const VCLean P = vclean(l);
+    if (n == 0) {
+      if (zero_init) CK(cudaMemsetAsync(P.e, 0, sizeof(float) * L[l].G.ncell, s));
+      return MLGPU_OK;
+    }
+    for (int i = 0; i < n; i++) {
+      CK(launch_vcl_gsrb(P, 0, (zero_init && i == 0) ? 1 : 0, s));
+      CK(launch_vcl_gsrb(P, 1, 0, s));
+    }
+    return MLGPU_OK;
+  }
+
+  // V-cycle from a lean level: pre-smoothing, red-children restriction (the
+  // black residual vanishes after the black half sweep), the coarser levels,
+  // black-only prolongation (the red half sweep that follows overwrites the
+  // red e unread), post-smoothing
+  int cycle_lean(int l, bool zero_init) {
+    const VCLean P = vclean(l);
+    const int csplit = L[l + 1].lean ? 1 : 0;
+    int rc = relax_lean(l, o.num_smooth_down, zero_init);
+    if (rc) return rc;
+    CK(launch_vcl_restrict(P, L[l + 1].G, csplit, o.num_smooth_down >= 1 ? 1 : 0,
+                           (float *)L[l + 1].r, (float *)L[l + 1].e, s));
+    for (int m = 0; m < o.num_mg; m++) {
+      rc = cycle<float>(l + 1, m == 0);
+      if (rc) return rc;
+    }
+    CK(launch_vcl_prolong(P, L[l + 1].G, make_bcd(op.bc), csplit, o.num_smooth_up >= 1 ? 1 : 0,
+                          o.prolong, (const float *)L[l + 1].ecur, s));
+    return relax_lean(l, o.num_smooth_up, false);
+  }
+
   template <class T>
   int cycle(int l, bool zero_init) {
     int last = (int)L.size() - 1;
@@ -554,6 +619,8 @@ class VCSolver : public mlgpu_solver {
     // a fresh correction starts in e; a continued one stays where the last
     // pass left it (the tile path alternates e / t, the other paths work in e)
     if (zero_init || !L[l].ecur) L[l].ecur = L[l].e;
+    if constexpr (sizeof(T) == 4)
+      if (L[l].lean) return cycle_lean(l, zero_init);
     // the lean FP32 single-CTA cycle takes levels up to 1024 cells
     const long long block_cells = (sizeof(T) == 4 && L[l].fcx) ? kFastCycCells : kBlockCycleCells;
     if (use_tiles && l < last && L[l].G.dim == 2 && L[l].G.ncell > block_cells) {
@@ -659,7 +726,7 @@ class VCSolver : public mlgpu_solver {
       CK((launch_vc_update_residual<double, float>(A, o.norm_type, phi[from],
                                                    (const float *)L[0].ecur, rhs, phi[1 - from],
                                                    nullptr, (float *)L[0].r, part, &nparts, s,
-                                                   par)));
+                                                   par, L[0].lean ? 1 : 0)));
     else
       CK((launch_vc_update_residual<double, double>(A, o.norm_type, phi[from],
                                                     (const double *)L[0].ecur, rhs, phi[1 - from],
@@ -734,7 +801,8 @@ class VCSolver : public mlgpu_solver {
       int nparts = 0;
       if (mixed)
         CK((launch_vc_update_residual<double, float>(A, o.norm_type, phi[0], nullptr, rhs, nullptr,
-                                                     nullptr, (float *)L[0].r, part, &nparts, s)));
+                                                     nullptr, (float *)L[0].r, part, &nparts, s,
+                                                     nullptr, L[0].lean ? 1 : 0)));
       else
         CK((launch_vc_update_residual<double, double>(A, o.norm_type, phi[0], nullptr, rhs, nullptr,
                                                       nullptr, (double *)L[0].r, part, &nparts,

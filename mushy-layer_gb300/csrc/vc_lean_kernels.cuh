@@ -1,0 +1,168 @@
+// vc_lean_kernels.cuh -- lean FP32 kernels of the linear variable-coefficient
+// cycles (projection / Darcy-Brinkman operator, vc_kernels.cuh) on 3D levels,
+// inside the FP64 defect correction of the mixed-precision solve.  The
+// correction equation L e = r with homogeneous boundary conditions is
+//   (L e)_j = diag_j e_j - bd sum_(interior faces) b_f e_nb,   bd = beta / dx^2,
+//   diag_j = alpha a_j - beta c_j + bd sum_f b_f fac_f,
+// fac_f = 1 for an interior or periodic face, 2 for a Dirichlet wall (ghost
+// -e_j), 0 for a Neumann wall (ghost e_j): the wall ghosts fold into the
+// diagonal, so a red/black update is an exact Gauss-Seidel step,
+//   e_j = (r_j + bd sum b_f e_nb) / diag_j,
+// reading its own r and 1/diag, the other colour's e and the face
+// coefficients.  The per-level arrays e, r, 1/diag, diag are colour-split
+// (cs_index), as in lin_lean_kernels.cuh, so a half sweep streams its own
+// colour's data only; the face arrays keep their natural layout.  The
+// reference-order kernels (vc_gsrb_kernel with resetLambda's 1/diag, which
+// ignores the wall rule) are kept for the FP64 path; this form is the mixed
+// path's smoother, its FP64 outer residual unchanged.
+#pragma once
+#include "vc_kernels.cuh"
+#include "misc_kernels.cuh"
+
+namespace mlgpu {
+
+struct VCLean {
+  Geom G;
+  float bd;              // beta / dx^2
+  const float *b[3];     // face coefficients (natural face layout)
+  const float *idg;      // 1 / diag, split
+  const float *dg;       // diag, split
+  float *e;              // correction, split
+  const float *r;        // right-hand side, split
+};
+
+#ifdef MLGPU_ADJ_F32_UNIT
+// diag and 1/diag of every cell into the split layout (once per solver)
+template <int DIM>
+__global__ void __launch_bounds__(kBlock) vcl_diag_kernel(VCArgs<float> A, float *__restrict__ idg,
+                                                          float *__restrict__ dg) {
+  const Geom &G = A.G;
+  const float bd = A.beta * A.dxinv;
+  for (long long q = gtid(); q < G.ncell; q += gstride()) {
+    int i, j, k;
+    cell_ijk(G, q, i, j, k);
+    const int idx[3] = {i, j, k};
+    float s = 0.f;
+#pragma unroll
+    for (int d = 0; d < DIM; d++) {
+      const int m = G.n(d);
+#pragma unroll
+      for (int side = 0; side < 2; side++) {
+        int fi[3] = {i, j, k};
+        if (side) fi[d] += 1;
+        const float bf = A.b[d][G.face(d, fi[0], fi[1], fi[2])];
+        const int nb = idx[d] + (side ? 1 : -1);
+        float fac;
+        if (nb >= 0 && nb < m)
+          fac = 1.f;
+        else if (G.per(d))
+          fac = m == 1 ? 0.f : 1.f;
+        else
+          fac = A.bc.type[d][side][0] == MLGPU_BC_DIRICHLET ? 2.f : 0.f;
+        s = fmaf(bf, fac, s);
+      }
+    }
+    float dv = A.alpha * (A.a ? A.a[q] : 1.f);
+    if (A.c) dv = dv - A.beta * A.c[q];
+    dv = fmaf(bd, s, dv);
+    const long long o = cs_index(G, i, j, k);
+    dg[o] = dv;
+    idg[o] = 1.f / dv;
+  }
+}
+
+// sum over the interior faces (periodic seams wrapped) of b_f e_nb at cell
+// (i, j, k) of a split level
+template <int DIM>
+__device__ __forceinline__ float vcl_nbsum(const VCLean &P, int i, int j, int k) {
+  const Geom &G = P.G;
+  float s = 0.f;
+  {
+    const long long f = ((long long)k * G.n1 + j) * (G.n0 + 1) + i;
+    const int il = i > 0 ? i - 1 : (G.per0 && G.n0 > 1 ? G.n0 - 1 : -1);
+    const int ih = i < G.n0 - 1 ? i + 1 : (G.per0 && G.n0 > 1 ? 0 : -1);
+    if (il >= 0) s = fmaf(P.b[0][f], P.e[cs_index(G, il, j, k)], s);
+    if (ih >= 0) s = fmaf(P.b[0][f + 1], P.e[cs_index(G, ih, j, k)], s);
+  }
+  {
+    const long long f = ((long long)k * (G.n1 + 1) + j) * G.n0 + i;
+    const int jl = j > 0 ? j - 1 : (G.per1 && G.n1 > 1 ? G.n1 - 1 : -1);
+    const int jh = j < G.n1 - 1 ? j + 1 : (G.per1 && G.n1 > 1 ? 0 : -1);
+    if (jl >= 0) s = fmaf(P.b[1][f], P.e[cs_index(G, i, jl, k)], s);
+    if (jh >= 0) s = fmaf(P.b[1][f + G.n0], P.e[cs_index(G, i, jh, k)], s);
+  }
+  if (DIM == 3) {
+    const long long pl = (long long)G.n0 * G.n1;
+    const long long f = ((long long)k * G.n1 + j) * G.n0 + i;
+    const int kl = k > 0 ? k - 1 : (G.per2 && G.n2 > 1 ? G.n2 - 1 : -1);
+    const int kh = k < G.n2 - 1 ? k + 1 : (G.per2 && G.n2 > 1 ? 0 : -1);
+    if (kl >= 0) s = fmaf(P.b[2][f], P.e[cs_index(G, i, j, kl)], s);
+    if (kh >= 0) s = fmaf(P.b[2][f + pl], P.e[cs_index(G, i, j, kh)], s);
+  }
+  return s;
+}
+
+// red/black half sweep over the colour `pass` half; zero: the other colour's
+// e is zero (the first half sweep of a correction that starts from zero)
+template <int DIM>
+__global__ void __launch_bounds__(kBlock) vcl_gsrb_kernel(VCLean P, int pass, int zero) {
+  const Geom &G = P.G;
+  const long long half = G.ncell >> 1;
+  for (long long t = gtid(); t < half; t += gstride()) {
+    const long long q = pass * half + t;
+    int i, j, k;
+    cs_cell(G, q, i, j, k);
+    const float s = zero ? 0.f : vcl_nbsum<DIM>(P, i, j, k);
+    P.e[q] = P.idg[q] * fmaf(P.bd, s, P.r[q]);
+  }
+}
+
+// r - L e at a cell of a split level
+template <int DIM>
+__device__ __forceinline__ float vcl_res(const VCLean &P, int i, int j, int k, long long q) {
+  return fmaf(P.bd, vcl_nbsum<DIM>(P, i, j, k), P.r[q]) - P.dg[q] * P.e[q];
+}
+
+// coarse r = 2^D average of the fine residual (RED: of the red children, the
+// black ones' being zero to rounding after a black half sweep); coarse e = 0
+template <int DIM, class CIDX, bool RED>
+__global__ void __launch_bounds__(kBlock) vcl_restrict_kernel(VCLean P, Geom C,
+                                                              float *__restrict__ rc,
+                                                              float *__restrict__ ec) {
+  const float wgt = DIM == 3 ? 0.125f : 0.25f;
+  for (long long Q = gtid(); Q < C.ncell; Q += gstride()) {
+    int I, J, K;
+    cell_ijk(C, Q, I, J, K);
+    float a = 0.f;
+#pragma unroll
+    for (int kk = 0; kk < (DIM == 3 ? 2 : 1); kk++)
+#pragma unroll
+      for (int jj = 0; jj < 2; jj++)
+#pragma unroll
+        for (int ii = 0; ii < 2; ii++) {
+          if (RED && ((ii + jj + kk) & 1)) continue;
+          const int i = 2 * I + ii, j = 2 * J + jj, k = DIM == 3 ? 2 * K + kk : 0;
+          a += vcl_res<DIM>(P, i, j, k, cs_index(P.G, i, j, k));
+        }
+    const long long o = CIDX()(C, I, J, K);
+    rc[o] = a * wgt;
+    ec[o] = 0.f;
+  }
+}
+
+// e += prolongation of the coarse correction (BLACK: the black half alone,
+// when a red half sweep follows and overwrites the red e unread)
+template <int DIM, int KIND, class CIDX, bool BLACK>
+__global__ void __launch_bounds__(kBlock) vcl_prolong_kernel(VCLean P, Geom C, BCD bc,
+                                                             const float *__restrict__ ec) {
+  const Geom &G = P.G;
+  const long long n = G.ncell, q0 = BLACK ? (n >> 1) : 0;
+  for (long long q = q0 + gtid(); q < n; q += gstride()) {
+    int i, j, k;
+    cs_cell(G, q, i, j, k);
+    P.e[q] = prolong_add<float, DIM, KIND, CIDX>(C, bc, 0, i, j, k, P.e[q], ec, nullptr);
+  }
+}
+#endif  // MLGPU_ADJ_F32_UNIT
+
+}  // namespace mlgpu
