@@ -119,7 +119,7 @@ cudaError_t launch_lean_prolong(const LinLeanT<T> &P, const Geom &C, int csplit,
 // sweep (zero: the other colour's e is zero), residual restriction (red: the
 // red children only) with the coarse e zeroed, black-only prolongation
 cudaError_t launch_vcl_diag(const VCArgs<float> &A, float *idg, float *dg, cudaStream_t s);
-cudaError_t launch_vcl_gsrb(const VCLean &P, int pass, int zero, cudaStream_t s);
+cudaError_t launch_vcl_gsrb(const VCLean &P, int pass, int zero, cudaStream_t s, int vec = 1);
 cudaError_t launch_vcl_restrict(const VCLean &P, const Geom &C, int csplit, int red, float *rc,
                                 float *ec, cudaStream_t s);
 cudaError_t launch_vcl_prolong(const VCLean &P, const Geom &C, const BCD &bc, int csplit,

@@ -213,8 +213,12 @@ cudaError_t launch_vcl_diag(const VCArgs<float> &A, float *idg, float *dg, cudaS
   return cudaGetLastError();
 }
 
-cudaError_t launch_vcl_gsrb(const VCLean &P, int pass, int zero, cudaStream_t s) {
-  MLGPU_DIM_SWITCH(P.G.dim, (vcl_gsrb_kernel<DIM><<<blocks_for(P.G.ncell >> 1), kBlock, 0, s>>>(P, pass, zero)));
+cudaError_t launch_vcl_gsrb(const VCLean &P, int pass, int zero, cudaStream_t s, int vec) {
+  if (vec && ((P.G.n0 >> 1) % 4) == 0) {
+    MLGPU_DIM_SWITCH(P.G.dim, (vcl_gsrb_vec_kernel<DIM><<<blocks_for((P.G.ncell >> 1) / 4), kBlock, 0, s>>>(P, pass, zero)));
+  } else {
+    MLGPU_DIM_SWITCH(P.G.dim, (vcl_gsrb_kernel<DIM><<<blocks_for(P.G.ncell >> 1), kBlock, 0, s>>>(P, pass, zero)));
+  }
   return cudaGetLastError();
 }
 

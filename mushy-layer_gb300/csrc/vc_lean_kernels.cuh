@@ -117,6 +117,87 @@ __global__ void __launch_bounds__(kBlock) vcl_gsrb_kernel(VCLean P, int pass, in
   }
 }
 
+// the same half sweep with 4 consecutive cells of one row of the colour's
+// half per thread (lean_gsrb_vec_kernel's scheme: own r and 1/diag, the y / z
+// neighbours' e as float4 loads, the x neighbours' e as a float4 and one
+// scalar, e stored as a float4); each cell's arithmetic in vcl_gsrb_kernel's
+// order (the same bits).  Needs n0 / 2 a multiple of 4.
+template <int DIM>
+__global__ void __launch_bounds__(kBlock) vcl_gsrb_vec_kernel(VCLean P, int pass, int zero) {
+  constexpr int V = 4;
+  const Geom &G = P.G;
+  const long long n = G.ncell, half = n >> 1;
+  const int h0 = G.n0 >> 1;
+  const long long base = pass * half, obase = half - base;
+  const long long ngroups = half / V;
+  const long long pl = (long long)G.n0 * G.n1;
+  const float *e = P.e;
+  for (long long t = gtid(); t < ngroups; t += gstride()) {
+    const long long u = t * V;
+    const unsigned row = (unsigned)u / (unsigned)h0;
+    const int hh = (int)((unsigned)u - row * (unsigned)h0);
+    const int k = (int)(row / (unsigned)G.n1), j = (int)(row - (unsigned)k * G.n1);
+    const int par = (j + k + pass) & 1;
+    const long long q = base + u;
+    float s[V] = {0.f, 0.f, 0.f, 0.f};
+    if (!zero) {
+      {  // x: the other colour's e at hh - 1 + par .. hh + V - 1 + par of this row
+        const long long ob = obase + (long long)row * h0;
+        float wv[V];
+        ldv(e + ob + hh, wv);
+        int xe = par ? hh + V : hh - 1;
+        bool has_e = true;
+        if (xe < 0) {
+          xe = h0 - 1;
+          has_e = G.per0 != 0;
+        } else if (xe >= h0) {
+          xe = 0;
+          has_e = G.per0 != 0;
+        }
+        const float ev = has_e ? e[ob + xe] : 0.f;
+        const long long f0 = (long long)row * (G.n0 + 1) + 2 * hh + par;
+#pragma unroll
+        for (int v = 0; v < V; v++) {
+          const long long f = f0 + 2 * v;
+          const int vl = v > 0 ? v - 1 : 0, vh = v < V - 1 ? v + 1 : V - 1;
+          const bool lo_e = par == 0 && v == 0;
+          if (!lo_e || has_e) s[v] = fmaf(P.b[0][f], lo_e ? ev : (par ? wv[v] : wv[vl]), s[v]);
+          const bool hi_e = par == 1 && v == V - 1;
+          if (!hi_e || has_e) s[v] = fmaf(P.b[0][f + 1], hi_e ? ev : (par ? wv[vh] : wv[v]), s[v]);
+        }
+      }
+#pragma unroll
+      for (int d = 1; d < DIM; d++) {
+        const int m = d == 1 ? G.n1 : G.n2, c = d == 1 ? j : k;
+        const bool per = d == 1 ? G.per1 != 0 : G.per2 != 0;
+        const long long step = d == 1 ? G.n0 : pl;
+        const long long fb = d == 1 ? ((long long)k * (G.n1 + 1) + j) * G.n0 + 2 * hh + par
+                                    : (long long)row * G.n0 + 2 * hh + par;
+#pragma unroll
+        for (int side = 0; side < 2; side++) {
+          int cn = c + (side ? 1 : -1);
+          if (cn < 0 || cn >= m) {
+            if (!per || m == 1) continue;
+            cn = cn < 0 ? m - 1 : 0;
+          }
+          const unsigned nrow = d == 1 ? (unsigned)k * G.n1 + cn : (unsigned)cn * G.n1 + j;
+          float nb[V];
+          ldv(e + obase + (long long)nrow * h0 + hh, nb);
+#pragma unroll
+          for (int v = 0; v < V; v++)
+            s[v] = fmaf(P.b[d][fb + 2 * v + (side ? step : 0)], nb[v], s[v]);
+        }
+      }
+    }
+    float r[V], id[V], out[V];
+    ldv(P.r + q, r);
+    ldv(P.idg + q, id);
+#pragma unroll
+    for (int v = 0; v < V; v++) out[v] = id[v] * fmaf(P.bd, s[v], r[v]);
+    stv(P.e + q, out);
+  }
+}
+
 // r - L e at a cell of a split level
 template <int DIM>
 __device__ __forceinline__ float vcl_res(const VCLean &P, int i, int j, int k, long long q) {
