@@ -264,6 +264,31 @@ __device__ __forceinline__ int closure_regime(double H, double C, const ClosureP
   return 4;
 }
 
+// ---- FP32 <-> FP64 conversions on the integer pipe.  GB300 issues the
+// hardware conversions on its FP64 pipe (1/64 of the FP32 rate), where a
+// kernel that converts a few values per cell spends most of its time.
+// f32_trunc: x rounded toward zero to FP32 for |x| in FP32's normal range
+// (the hardware conversion otherwise: zero, subnormals, overflow, inf, NaN);
+// only decisions with a margin far above an FP32 ulp may use it.
+__device__ __forceinline__ float f32_trunc(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned hi = (unsigned)(b >> 32);
+  const int e = (int)((hi >> 20) & 0x7ffu) - 1023 + 127;
+  if (e <= 0 || e >= 255) return (float)x;
+  return __uint_as_float((hi & 0x80000000u) | ((unsigned)e << 23) | ((hi & 0xfffffu) << 3) |
+                         (unsigned)((b >> 29) & 7u));
+}
+// f64_exact: the FP64 value of f (exact, as the hardware conversion), the
+// hardware conversion for zero, subnormals, inf and NaN
+__device__ __forceinline__ double f64_exact(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned e = (u >> 23) & 0xffu;
+  if (e == 0u || e == 255u) return (double)f;
+  return __longlong_as_double((long long)(((unsigned long long)(u & 0x80000000u) << 32) |
+                                          ((unsigned long long)(e + 896u) << 52) |
+                                          ((unsigned long long)(u & 0x7fffffu) << 29)));
+}
+
 // FP32 constants of the closure for the FP32 derivative and regime test
 // (reciprocals of the constant divisors, so the per-cell work has no FP32
 // division by a constant)
@@ -325,7 +350,7 @@ static __device__ __noinline__ int closure_regime_near(double H, double C,
 // the few near a phase boundary.
 __device__ __forceinline__ int closure_regime_fast(double H, double C, const ClosureParams &p,
                                                    const ClosureF32 &f) {
-  const float h = (float)H, c = (float)C;
+  const float h = f32_trunc(H), c = f32_trunc(C);
   float Hs = (c < -f.CR) ? 0.f : f.cp * ((-c - f.CR) * f.inv_k);
   if (Hs < 0.f) Hs = 0.f;
   Hs = Hs + f.te * f.cp;
@@ -395,7 +420,7 @@ __device__ __forceinline__ void t_cl_jac(double H, double C, const ClosureParams
 __device__ __forceinline__ void t_cl_jac32(double H, double C, const ClosureParams &p,
                                            const ClosureF32 &f, float J[4]) {
   const int reg = closure_regime_fast(H, C, p, f);
-  const float h = (float)H, c = (float)C;
+  const float h = f32_trunc(H), c = f32_trunc(C);
   J[0] = J[1] = J[2] = J[3] = 0.f;
   if (reg == 0) {
     J[0] = f.inv_cp;

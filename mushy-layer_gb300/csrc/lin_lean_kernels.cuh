@@ -641,13 +641,21 @@ __global__ void __launch_bounds__(kBlock) lean_step_kernel(Geom G, StepClip K,
     cell_ijk(G, q, i, j, k);
     const long long o = at(G, i, j, k);
     const double h0 = u_old[q], c0 = u_old[n + q];
-    double h1 = h0 + scale * (double)e[o];
-    const double c1 = c0 + scale * (double)e[n + o];
+    double h1, c1;
+    if constexpr (sizeof(T) == 4) {
+      h1 = h0 + scale * f64_exact(e[o]);
+      c1 = c0 + scale * f64_exact(e[n + o]);
+    } else {
+      h1 = h0 + scale * (double)e[o];
+      c1 = c0 + scale * (double)e[n + o];
+    }
     if (CLIP) {
+      // FP32 regime test (truncated conversions: the near-bound band is 1e-4)
       float b0[3], b1[3];
-      const int f0 = K.regime32((float)h0, (float)c0, b0);
-      const int f1 = K.regime32((float)h1, (float)c1, b1);
-      if (f0 != f1 || StepClip::near((float)h0, b0) || StepClip::near((float)h1, b1)) {
+      const float h0f = f32_trunc(h0), h1f = f32_trunc(h1);
+      const int f0 = K.regime32(h0f, f32_trunc(c0), b0);
+      const int f1 = K.regime32(h1f, f32_trunc(c1), b1);
+      if (f0 != f1 || StepClip::near(h0f, b0) || StepClip::near(h1f, b1)) {
         const int r0 = closure_regime(h0, c0, K.p), r1 = closure_regime(h1, c1, K.p);
         if (r0 != r1 && r0 < 4 && r1 < 4) {
           double B[3];

@@ -1323,8 +1323,8 @@ class HCAdjSolver : public mlgpu_solver {
   double *nf = nullptr, *nuold = nullptr;  // Newton: rhs of N(u) = f, previous u
   double *ntcl = nullptr;  // Newton: (T, C_l) of level 0, the residual's closure cache
   // Newton's kernels per piece (counted once): state and Jacobians of every
-  // level, the linear residual with its norm, one linear cycle + residual
-  int nk_state = -1, nk_res = -1, nk_iter = -1;
+  // level, one linear cycle + residual
+  int nk_state = -1, nk_iter = -1;
   // kernels of nl_residual (closure, stencil + norms, combine, combine; a
   // stopping norm other than max adds its own pass) and of one step update
   static constexpr int kStepKernels = 1;
@@ -1649,7 +1649,6 @@ class HCAdjSolver : public mlgpu_solver {
     CK(cudaMemcpyAsync(host_norm, part + kMaxBlocks, sizeof(double), cudaMemcpyDeviceToHost, s));
     return MLGPU_OK;
   }
-  int residual_norm32() { return lin_residual_norm<float>(); }
 
   int iteration() {
     if (lin32()) {
@@ -1772,10 +1771,6 @@ class HCAdjSolver : public mlgpu_solver {
     CK(cudaMemcpyAsync(nf, user_f, bytes, cudaMemcpyDeviceToDevice, s));
     if (nk_state < 0) {
       nk_state = count_kernels([&] { return state_levels(); });
-      nk_res = count_kernels([&] {
-        return mixed ? lin_residual_norm<float>()
-                     : (fast64 ? lin_residual_norm<double>() : residual_norm());
-      });
       nk_iter = count_kernels([&] { return iteration(); });
     }
     int rc = nl_residual();
@@ -1792,25 +1787,23 @@ class HCAdjSolver : public mlgpu_solver {
     while (outer_continue(o, S)) {
       rc = state_levels();
       if (rc) return rc;
-      // linear solve A d = r, d in L[0].y (FP64) or L[0].y32 (mixed) from zero
+      // linear solve A d = r, d in L[0].y (FP64) or L[0].y32 (mixed) from
+      // zero: its starting residual is r itself, whose norm the nonlinear
+      // residual just gave (the options' norm kind: the linear test's)
       if (mixed) {
         CK(launch_lean_pack<float, double>(L[0].G, split(0), 2, L[0].g, L[0].g32, s));
         CK(cudaMemsetAsync(L[0].y32, 0, sizeof(float) * n2, s));
         CK(cudaMemsetAsync(L[0].w32, 0, sizeof(float) * n2, s));
-        rc = residual_norm32();
       } else if (fast64) {
         CK(launch_lean_pack<double, double>(L[0].G, split(0), 2, L[0].g, L[0].g64s, s));
         CK(cudaMemsetAsync(L[0].y, 0, bytes, s));
         CK(cudaMemsetAsync(L[0].w64, 0, bytes, s));
-        rc = lin_residual_norm<double>();
       } else {
         CK(cudaMemsetAsync(L[0].y, 0, bytes, s));
-        rc = residual_norm();
       }
-      if (rc) return rc;
-      st->kernel_launches += nk_state + nk_res + (mixed || fast64 ? 1 : 0);
-      CK(cudaStreamSynchronize(s));
-      const double l0 = *host_norm;
+      st->kernel_launches += nk_state + (mixed || fast64 ? 1 : 0);
+      const double l0 = S.norm;
+      *host_norm = l0;
       for (int c = 0; c < lin_max && *host_norm > eta * l0; c++) {
         rc = run_iteration();
         if (rc) return rc;
@@ -2278,7 +2271,6 @@ int mlgpu_hc_newton_params(mlgpu_solver *S, double lin_tol, int lin_max, double 
       }
     A->nk_iter = -1;
     A->nk_state = -1;
-    A->nk_res = -1;
   }
   A->lin_tol = lin_tol;
   A->lin_max = lin_max;
