@@ -124,6 +124,11 @@ cudaError_t launch_vcl_restrict(const VCLean &P, const Geom &C, int csplit, int 
                                 float *ec, cudaStream_t s);
 cudaError_t launch_vcl_prolong(const VCLean &P, const Geom &C, const BCD &bc, int csplit,
                                int black, int kind, const float *ec, cudaStream_t s);
+// the FP64 outer step of a mixed solve with a lean level 0 (e, res_inner split)
+cudaError_t launch_vcl_outer(const VCArgs<double> &A, int norm, const double *phi,
+                             const float *e, const double *rhs, double *out_phi,
+                             float *res_inner, double *part, int *nparts, cudaStream_t s,
+                             const int *par = nullptr);
 // per-cell face sums P of a smoothed level (natural layout), once per solver
 template <class T>
 cudaError_t launch_lean_psum(const AdjArgs<T> &A, T *P, cudaStream_t s);
@@ -152,10 +157,12 @@ cudaError_t launch_nlc_relax_block(const NLArgs<double> &A, double *phi, const d
                                    double *tcl, const double *lam, int sweeps, int init,
                                    cudaStream_t s);
 // the lean Newton paths' residual rhs - N(phi) over the cache, with its L2
-// (part) and max (part_max) norm partials
+// (part) and max (part_max) norm partials; sb: every cell's face sum per
+// component (launch_nlc_bsum, once per solver)
+cudaError_t launch_nlc_bsum(const NLArgs<double> &A, double *sb, cudaStream_t s);
 cudaError_t launch_nlc_res_lean(const NLArgs<double> &A, const double *phi, const double *tcl,
-                                const double *rhs, double *out, double *part, double *part_max,
-                                int *nparts, cudaStream_t s);
+                                const double *sb, const double *rhs, double *out, double *part,
+                                double *part_max, int *nparts, cudaStream_t s);
 // part_max: with a norm, the max-norm partials too (same count)
 cudaError_t launch_nlc_op(const NLArgs<double> &A, int mode, int norm, const double *phi,
                           const double *tcl, const double *rhs, double *out, double *copy,

@@ -157,6 +157,31 @@ __device__ __forceinline__ void t_cl(double H, double C, const ClosureParams &p,
   }
 }
 
+// ---- FP32 <-> FP64 conversions on the integer pipe.  GB300 issues the
+// hardware conversions on its FP64 pipe (1/64 of the FP32 rate), where a
+// kernel that converts a few values per cell spends most of its time.
+// f32_trunc: x rounded toward zero to FP32 for |x| in FP32's normal range
+// (the hardware conversion otherwise: zero, subnormals, overflow, inf, NaN);
+// only decisions with a margin far above an FP32 ulp may use it.
+__device__ __forceinline__ float f32_trunc(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned hi = (unsigned)(b >> 32);
+  const int e = (int)((hi >> 20) & 0x7ffu) - 1023 + 127;
+  if (e <= 0 || e >= 255) return (float)x;
+  return __uint_as_float((hi & 0x80000000u) | ((unsigned)e << 23) | ((hi & 0xfffffu) << 3) |
+                         (unsigned)((b >> 29) & 7u));
+}
+// f64_exact: the FP64 value of f (exact, as the hardware conversion), the
+// hardware conversion for zero, subnormals, inf and NaN
+__device__ __forceinline__ double f64_exact(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned e = (u >> 23) & 0xffu;
+  if (e == 0u || e == 255u) return (double)f;
+  return __longlong_as_double((long long)(((unsigned long long)(u & 0x80000000u) << 32) |
+                                          ((unsigned long long)(e + 896u) << 52) |
+                                          ((unsigned long long)(u & 0x7fffffu) << 29)));
+}
+
 // ---- lean FP64 closure (the outer loops of the lean Newton paths)
 // t_cl with the closure's divisions by constants as products with their
 // reciprocals and the two per-cell operations (the porosity root's square
@@ -171,7 +196,7 @@ __device__ __forceinline__ void t_cl(double H, double C, const ClosureParams &p,
 // the reference-order paths keep t_cl.
 struct ClosureLean {
   double CR, k, cp, St, te, Te;
-  double inv_k, inv_CRTe, He_slope, a, inv_2a, four_a, b0, omk, cpm1;
+  double inv_k, inv_CRTe, He_slope, a, inv_2a, four_a, b0, omk, cpm1, inv_cp;
 };
 
 inline ClosureLean make_closure_lean(const ClosureParams &p) {
@@ -191,6 +216,7 @@ inline ClosureLean make_closure_lean(const ClosureParams &p) {
   L.b0 = p.CR * (1 - 2 * p.cp) - p.k * p.St;
   L.omk = 1 - p.k;
   L.cpm1 = p.cp - 1;
+  L.inv_cp = 1.0 / p.cp;
   return L;
 }
 
@@ -219,18 +245,38 @@ __device__ __forceinline__ double lean_div(double num, double den) {
 
 __device__ __forceinline__ void t_cl_lean(double H, double C, const ClosureLean &p, double &T,
                                           double &Cl) {
-  double Hs = (C < -p.CR) ? 0.0 : p.cp * ((-C - p.CR) * p.inv_k);
-  if (Hs < 0.0) Hs = 0.0;
-  Hs = Hs + p.te * p.cp;
-  const double He = (p.CR + C) * p.inv_CRTe * p.He_slope + p.cp * p.te;
-  const double Hl = p.St - C + p.te + p.Te;
-  if (H <= Hs) {
-    T = H / p.cp;
+  // the regime from FP32 bounds (integer-pipe conversions), re-decided in
+  // FP64 within 1e-4 of a bound; the closure is continuous across its
+  // bounds, so a cell an ulp from one may take either side
+  int reg;
+  {
+    const float h = f32_trunc(H), c = f32_trunc(C);
+    const float CR = (float)p.CR, cpv = (float)p.cp;
+    float Hs = (c < -CR) ? 0.f : cpv * ((-c - CR) * (float)p.inv_k);
+    if (Hs < 0.f) Hs = 0.f;
+    Hs = Hs + (float)p.te * cpv;
+    const float He = (CR + c) * (float)p.inv_CRTe * (float)p.He_slope + cpv * (float)p.te;
+    const float Hl = (float)p.St - c + (float)p.te + (float)p.Te;
+    const float band = 1e-4f;
+    if (fabsf(h - Hs) < band * (1.f + fabsf(Hs)) || fabsf(h - He) < band * (1.f + fabsf(He)) ||
+        fabsf(h - Hl) < band * (1.f + fabsf(Hl))) {
+      double Hs2 = (C < -p.CR) ? 0.0 : p.cp * ((-C - p.CR) * p.inv_k);
+      if (Hs2 < 0.0) Hs2 = 0.0;
+      Hs2 = Hs2 + p.te * p.cp;
+      const double He2 = (p.CR + C) * p.inv_CRTe * p.He_slope + p.cp * p.te;
+      const double Hl2 = p.St - C + p.te + p.Te;
+      reg = H <= Hs2 ? 0 : (H <= He2 ? 1 : (H < Hl2 ? 2 : (H >= Hl2 ? 3 : 4)));
+    } else {
+      reg = h <= Hs ? 0 : (h <= He ? 1 : (h < Hl ? 2 : (h >= Hl ? 3 : 4)));
+    }
+  }
+  if (reg == 0) {
+    T = H * p.inv_cp;
     Cl = p.Te;
-  } else if (H <= He) {
+  } else if (reg == 1) {
     T = p.te;
     Cl = p.Te;
-  } else if (H < Hl) {
+  } else if (reg == 2) {
     double por = 1.0;
     if (p.St != 0) {
       const double vC = (C >= -p.CR) ? C : -p.CR;
@@ -240,7 +286,7 @@ __device__ __forceinline__ void t_cl_lean(double H, double C, const ClosureLean 
     }
     Cl = lean_div(C + p.CR * (1 - por), por + p.k * (1 - por));
     T = -Cl;
-  } else if (H >= Hl) {
+  } else if (reg == 3) {
     T = H - p.St;
     Cl = C;
   } else {  // NaN input, as t_cl
@@ -262,31 +308,6 @@ __device__ __forceinline__ int closure_regime(double H, double C, const ClosureP
   if (H > He && H < Hl) return 2;
   if (H >= Hl) return 3;
   return 4;
-}
-
-// ---- FP32 <-> FP64 conversions on the integer pipe.  GB300 issues the
-// hardware conversions on its FP64 pipe (1/64 of the FP32 rate), where a
-// kernel that converts a few values per cell spends most of its time.
-// f32_trunc: x rounded toward zero to FP32 for |x| in FP32's normal range
-// (the hardware conversion otherwise: zero, subnormals, overflow, inf, NaN);
-// only decisions with a margin far above an FP32 ulp may use it.
-__device__ __forceinline__ float f32_trunc(double x) {
-  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
-  const unsigned hi = (unsigned)(b >> 32);
-  const int e = (int)((hi >> 20) & 0x7ffu) - 1023 + 127;
-  if (e <= 0 || e >= 255) return (float)x;
-  return __uint_as_float((hi & 0x80000000u) | ((unsigned)e << 23) | ((hi & 0xfffffu) << 3) |
-                         (unsigned)((b >> 29) & 7u));
-}
-// f64_exact: the FP64 value of f (exact, as the hardware conversion), the
-// hardware conversion for zero, subnormals, inf and NaN
-__device__ __forceinline__ double f64_exact(float f) {
-  const unsigned u = __float_as_uint(f);
-  const unsigned e = (u >> 23) & 0xffu;
-  if (e == 0u || e == 255u) return (double)f;
-  return __longlong_as_double((long long)(((unsigned long long)(u & 0x80000000u) << 32) |
-                                          ((unsigned long long)(e + 896u) << 52) |
-                                          ((unsigned long long)(u & 0x7fffffu) << 29)));
 }
 
 // FP32 constants of the closure for the FP32 derivative and regime test

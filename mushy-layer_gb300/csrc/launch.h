@@ -43,12 +43,11 @@ cudaError_t launch_nl_lambda(const NLArgs<T> &A, T *lam, cudaStream_t s);
 template <class T>
 cudaError_t launch_vc_op(const VCArgs<T> &A, int mode, int norm, const T *phi, const T *rhs, T *out,
                          int homog, double *part, int *nparts, cudaStream_t s);
-// split: e and res_inner colour-split (the lean 3D FP32 cycles' level 0)
 template <class T, class E>
 cudaError_t launch_vc_update_residual(const VCArgs<T> &A, int norm, const T *phi, const E *e,
                                       const T *rhs, T *out_phi, T *res, E *res_inner,
                                       double *part, int *nparts, cudaStream_t s,
-                                      const int *par = nullptr, int split = 0);
+                                      const int *par = nullptr);
 template <class T>
 cudaError_t launch_vc_gsrb(const VCArgs<T> &A, T *phi, const T *rhs, int pass, cudaStream_t s);
 template <class T>

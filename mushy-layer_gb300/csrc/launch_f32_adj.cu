@@ -270,6 +270,21 @@ cudaError_t launch_vcl_prolong(const VCLean &P, const Geom &C, const BCD &bc, in
   return cudaGetLastError();
 }
 
+cudaError_t launch_vcl_outer(const VCArgs<double> &A, int norm, const double *phi,
+                             const float *e, const double *rhs, double *out_phi,
+                             float *res_inner, double *part, int *nparts, cudaStream_t s,
+                             const int *par) {
+  const int nb = blocks_for(A.G.ncell);
+  if (nparts) *nparts = nb;
+  if (norm < 0) norm = MLGPU_NORM_MAX;
+  MLGPU_DIM_SWITCH(A.G.dim, MLGPU_NORM_SWITCH(norm, {
+    if (NORM >= 0)
+      vcl_outer_kernel<DIM, (NORM < 0 ? 0 : NORM)>
+          <<<nb, kBlock, 0, s>>>(A, phi, e, rhs, out_phi, res_inner, part, par);
+  }));
+  return cudaGetLastError();
+}
+
 #define MLGPU_LEAN_INST(T)                                                                     \
   template cudaError_t launch_lean_gsrb<T>(const LinLeanT<T> &, int, cudaStream_t, int);      \
   template cudaError_t launch_lean_residual<T>(const LinLeanT<T> &, int, int, int, double *,   \

@@ -38,13 +38,12 @@ template cudaError_t launch_vc_update_residual<double, double>(const VCArgs<doub
                                                                const double *, const double *,
                                                                const double *, double *,
                                                                double *, double *, double *,
-                                                               int *, cudaStream_t, const int *,
-                                                               int);
+                                                               int *, cudaStream_t, const int *);
 template cudaError_t launch_vc_update_residual<double, float>(const VCArgs<double> &, int,
                                                               const double *, const float *,
                                                               const double *, double *, double *,
                                                               float *, double *, int *,
-                                                              cudaStream_t, const int *, int);
+                                                              cudaStream_t, const int *);
 
 cudaError_t launch_vc_outer_fast(const OuterFast &P, int norm, cudaStream_t s) {
   if (P.G.dim != 2 || !P.count || !P.part || !P.res_inner) return cudaErrorInvalidValue;

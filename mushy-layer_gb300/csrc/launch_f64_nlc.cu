@@ -56,12 +56,17 @@ cudaError_t launch_nlc_op(const NLArgs<double> &A, int mode, int norm, const dou
   return cudaGetLastError();
 }
 
+cudaError_t launch_nlc_bsum(const NLArgs<double> &A, double *sb, cudaStream_t s) {
+  MLGPU_DIM_SWITCH(A.G.dim, (nlc_bsum_kernel<DIM><<<nlc_blocks(A.G.ncell), kNLCBlock, 0, s>>>(A, sb)));
+  return cudaGetLastError();
+}
+
 cudaError_t launch_nlc_res_lean(const NLArgs<double> &A, const double *phi, const double *tcl,
-                                const double *rhs, double *out, double *part, double *part_max,
-                                int *nparts, cudaStream_t s) {
+                                const double *sb, const double *rhs, double *out, double *part,
+                                double *part_max, int *nparts, cudaStream_t s) {
   const int nb = nlc_blocks(A.G.ncell);
   if (nparts) *nparts = nb;
-  MLGPU_DIM_SWITCH(A.G.dim, (nlc_res_lean_kernel<DIM><<<nb, kNLCBlock, 0, s>>>(A, phi, tcl, rhs, out, part, part_max)));
+  MLGPU_DIM_SWITCH(A.G.dim, (nlc_res_lean_kernel<DIM><<<nb, kNLCBlock, 0, s>>>(A, phi, tcl, sb, rhs, out, part, part_max)));
   return cudaGetLastError();
 }
 

@@ -146,23 +146,15 @@ template <class T, class E>
 cudaError_t launch_vc_update_residual(const VCArgs<T> &A, int norm, const T *phi, const E *e,
                                       const T *rhs, T *out_phi, T *res, E *res_inner,
                                       double *part, int *nparts, cudaStream_t s,
-                                      const int *par, int split) {
+                                      const int *par) {
   int nb = blocks_for(A.G.ncell);
   if (nparts) *nparts = nb;
   if (norm < 0) norm = MLGPU_NORM_MAX;
-  if (split) {
-    MLGPU_DIM_SWITCH(A.G.dim, MLGPU_NORM_SWITCH(norm, {
-      if (NORM >= 0)
-        vc_update_residual_kernel<T, E, DIM, (NORM < 0 ? 0 : NORM), true>
-            <<<nb, kBlock, 0, s>>>(A, phi, e, rhs, out_phi, res, res_inner, part, par);
-    }));
-  } else {
-    MLGPU_DIM_SWITCH(A.G.dim, MLGPU_NORM_SWITCH(norm, {
-      if (NORM >= 0)
-        vc_update_residual_kernel<T, E, DIM, (NORM < 0 ? 0 : NORM), false>
-            <<<nb, kBlock, 0, s>>>(A, phi, e, rhs, out_phi, res, res_inner, part, par);
-    }));
-  }
+  MLGPU_DIM_SWITCH(A.G.dim, MLGPU_NORM_SWITCH(norm, {
+    if (NORM >= 0)
+      vc_update_residual_kernel<T, E, DIM, (NORM < 0 ? 0 : NORM)>
+          <<<nb, kBlock, 0, s>>>(A, phi, e, rhs, out_phi, res, res_inner, part, par);
+  }));
   return cudaGetLastError();
 }
 

@@ -219,17 +219,42 @@ __global__ void __launch_bounds__(kNLCBlock) nlc_op_kernel(NLArgs<double> A,
   }
 }
 
-// NL_RESIDUAL for the lean Newton paths: the same stencil over the cache
-// with FMA (s = sum b (f_nb - f_c), lof = (alpha a) phi - (beta dxinv) s),
-// its L2 norm by FMA and its max norm on the bit patterns of |v| (for
-// non-negative doubles the integer order is the numeric order, and a NaN's
-// pattern is above every number's, so it stays sticky) -- about two thirds
-// of the reference-order kernel's FP64 pipe operations; the same values to
-// rounding, not the same bits
+// the sum of every face coefficient of each cell, per component (the lean
+// residual's diagonal term; formed once per solver)
+template <int DIM>
+__global__ void __launch_bounds__(kNLCBlock) nlc_bsum_kernel(NLArgs<double> A,
+                                                             double *__restrict__ sb) {
+  const Geom &G = A.G;
+  const long long n = G.ncell;
+  for (long long q = gtid(); q < n; q += gstride()) {
+    int i, j, k;
+    cell_ijk(G, q, i, j, k);
+#pragma unroll
+    for (int c = 0; c < 2; c++) {
+      double s = bface(A, 0, c, i + 1, j, k) + bface(A, 0, c, i, j, k);
+      s = s + bface(A, 1, c, i, j + 1, k) + bface(A, 1, c, i, j, k);
+      if (DIM == 3) s = s + bface(A, 2, c, i, j, k + 1) + bface(A, 2, c, i, j, k);
+      sb[q + c * n] = s;
+    }
+  }
+}
+
+// NL_RESIDUAL for the lean Newton paths over the cache:
+//   sum_f b_f (f_nb - f_c) = sum_f b_f f_nb - f_c sum_f b_f
+// with sum_f b_f per cell precomputed (sb; a wall face's ghost value enters
+// as its neighbour value, so the identity holds on every face), by FMA;
+// lof = (alpha a) phi - (beta dxinv) s; its L2 norm by FMA and its max norm on
+// the bit patterns of |v| (for non-negative doubles the integer order is the
+// numeric order, and a NaN's pattern is above every number's, so it stays
+// sticky).  Half the reference-order kernel's FP64 pipe operations; the
+// cancellation in the product form costs (max |f| / max |f_nb - f_c|) ulps
+// of the flux, far below the Newton tolerance's scale for the closure's
+// bounded T and C_l.
 template <int DIM>
 __global__ void __launch_bounds__(kNLCBlock) nlc_res_lean_kernel(NLArgs<double> A,
                                                                  const double *__restrict__ phi,
                                                                  const double *__restrict__ tcl,
+                                                                 const double *__restrict__ sb,
                                                                  const double *__restrict__ rhs,
                                                                  double *__restrict__ out,
                                                                  double *__restrict__ part,
@@ -253,16 +278,15 @@ __global__ void __launch_bounds__(kNLCBlock) nlc_res_lean_kernel(NLArgs<double> 
     const double ph[2] = {h0, c0};
 #pragma unroll
     for (int c = 0; c < 2; c++) {
-      const double p0 = pl0[c];
-      double s = 0.0;
-      s = fma(bface(A, 0, c, i + 1, j, k), hi[0][c] - p0, s);
-      s = fma(bface(A, 0, c, i, j, k), lo[0][c] - p0, s);
-      s = fma(bface(A, 1, c, i, j + 1, k), hi[1][c] - p0, s);
-      s = fma(bface(A, 1, c, i, j, k), lo[1][c] - p0, s);
+      double s = bface(A, 0, c, i + 1, j, k) * hi[0][c];
+      s = fma(bface(A, 0, c, i, j, k), lo[0][c], s);
+      s = fma(bface(A, 1, c, i, j + 1, k), hi[1][c], s);
+      s = fma(bface(A, 1, c, i, j, k), lo[1][c], s);
       if (DIM == 3) {
-        s = fma(bface(A, 2, c, i, j, k + 1), hi[2][c] - p0, s);
-        s = fma(bface(A, 2, c, i, j, k), lo[2][c] - p0, s);
+        s = fma(bface(A, 2, c, i, j, k + 1), hi[2][c], s);
+        s = fma(bface(A, 2, c, i, j, k), lo[2][c], s);
       }
+      s = fma(-pl0[c], sb[q + c * n], s);
       const double aa = A.a ? A.alpha * A.a[q + c * n] : A.alpha;
       const double lof = fma(aa, ph[c], -(bd * s));
       const double v = rhs[q + c * n] - lof;

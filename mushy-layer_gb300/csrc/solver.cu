@@ -722,11 +722,14 @@ class VCSolver : public mlgpu_solver {
     A.c = (const double *)op.cCoef;
     for (int d = 0; d < 3; d++) A.b[d] = (const double *)op.bCoef[d];
     int nparts = 0;
-    if (mixed)
+    if (mixed && L[0].lean)
+      CK(launch_vcl_outer(A, o.norm_type, phi[from], (const float *)L[0].ecur, rhs,
+                          phi[1 - from], (float *)L[0].r, part, &nparts, s, par));
+    else if (mixed)
       CK((launch_vc_update_residual<double, float>(A, o.norm_type, phi[from],
                                                    (const float *)L[0].ecur, rhs, phi[1 - from],
                                                    nullptr, (float *)L[0].r, part, &nparts, s,
-                                                   par, L[0].lean ? 1 : 0)));
+                                                   par)));
     else
       CK((launch_vc_update_residual<double, double>(A, o.norm_type, phi[from],
                                                     (const double *)L[0].ecur, rhs, phi[1 - from],
@@ -799,10 +802,12 @@ class VCSolver : public mlgpu_solver {
       if (rc0) return rc0;
     } else {
       int nparts = 0;
-      if (mixed)
+      if (mixed && L[0].lean)
+        CK(launch_vcl_outer(A, o.norm_type, phi[0], nullptr, rhs, nullptr, (float *)L[0].r, part,
+                            &nparts, s));
+      else if (mixed)
         CK((launch_vc_update_residual<double, float>(A, o.norm_type, phi[0], nullptr, rhs, nullptr,
-                                                     nullptr, (float *)L[0].r, part, &nparts, s,
-                                                     nullptr, L[0].lean ? 1 : 0)));
+                                                     nullptr, (float *)L[0].r, part, &nparts, s)));
       else
         CK((launch_vc_update_residual<double, double>(A, o.norm_type, phi[0], nullptr, rhs, nullptr,
                                                       nullptr, (double *)L[0].r, part, &nparts,
@@ -1322,6 +1327,7 @@ class HCAdjSolver : public mlgpu_solver {
   cudaGraphExec_t graph = nullptr, graph_lin = nullptr, graph_lin32 = nullptr;
   double *nf = nullptr, *nuold = nullptr;  // Newton: rhs of N(u) = f, previous u
   double *ntcl = nullptr;  // Newton: (T, C_l) of level 0, the residual's closure cache
+  double *nsb = nullptr;   // lean Newton: level 0's face sums per cell and component
   // Newton's kernels per piece (counted once): state and Jacobians of every
   // level, one linear cycle + residual
   int nk_state = -1, nk_iter = -1;
@@ -1403,6 +1409,7 @@ class HCAdjSolver : public mlgpu_solver {
     nf = A.get<double>(2 * ncells(op.grid));
     nuold = A.get<double>(2 * ncells(op.grid));
     ntcl = A.get<double>(2 * ncells(op.grid));
+    if (mixed || fast64) nsb = A.get<double>(2 * ncells(op.grid));
     return A.off + 256;
   }
 
@@ -1420,6 +1427,7 @@ class HCAdjSolver : public mlgpu_solver {
         for (int d = 0; d < lv.G.dim; d++)
           CK(launch_convert<float, double>(2 * lv.G.nface(d), lv.c32.b[d], lv.c64.b[d], s));
       }
+    if (nsb) CK(launch_nlc_bsum(make_nl_args<double>(op), nsb, s));
     // the lean cycles' face sums of every smoothed level
     for (size_t l = 0; l < L.size(); l++) {
       if (L[l].P32) CK(launch_lean_psum<float>(args32((int)l), L[l].P32, s));
@@ -1735,7 +1743,7 @@ class HCAdjSolver : public mlgpu_solver {
     const bool lean = mixed || fast64;
     CK(launch_nlc_closure(N, L[0].u, ntcl, s, lean));
     if (lean && both)
-      CK(launch_nlc_res_lean(N, L[0].u, ntcl, nf, L[0].g, part, part2, &nparts, s));
+      CK(launch_nlc_res_lean(N, L[0].u, ntcl, nsb, nf, L[0].g, part, part2, &nparts, s));
     else
       CK(launch_nlc_op(N, NL_RESIDUAL, MLGPU_NORM_L2, L[0].u, ntcl, nf, L[0].g, nullptr, part,
                        &nparts, s, both ? part2 : nullptr));

@@ -51,20 +51,6 @@ struct UpdateRead {
   __device__ __forceinline__ T operator()(long long q) const { return phi[q] + (T)e[q]; }
 };
 
-// phi + e with e colour-split (the lean 3D FP32 cycles' level-0 layout):
-// the natural index of the read mapped to its split position
-template <class T, class E>
-struct SplitUpdateRead {
-  const T *phi;
-  const E *e;
-  Geom G;
-  __device__ __forceinline__ T operator()(long long q) const {
-    int i, j, k;
-    cell_ijk(G, q, i, j, k);
-    return phi[q] + (T)e[cs_index(G, i, j, k)];
-  }
-};
-
 template <class T, class R>
 __device__ __forceinline__ T vc_nb(const VCArgs<T> &A, const R &rd, int i, int j, int k, int d,
                                    int side, T p0, bool homog) {
@@ -154,9 +140,7 @@ __global__ void __launch_bounds__(kBlock) vc_op_kernel(VCArgs<T> A, const T *__r
 // phi (other threads still read the old value); it is unused when e is null.
 // With `par` non-null the two solution buffers swap roles when *par == 1
 // (ping-pong selected on the device by the outer-loop decision kernel).
-// SPLIT: e and res_inner in the colour-split layout (cs_index), the FP64
-// arrays natural; the same FP64 arithmetic.
-template <class T, class E, int DIM, int NORM, bool SPLIT>
+template <class T, class E, int DIM, int NORM>
 __global__ void __launch_bounds__(kBlock) vc_update_residual_kernel(
     VCArgs<T> A, const T *phi, const E *__restrict__ e, const T *__restrict__ rhs,
     T *out_phi, T *__restrict__ res, E *__restrict__ res_inner, double *__restrict__ part,
@@ -173,20 +157,15 @@ __global__ void __launch_bounds__(kBlock) vc_update_residual_kernel(
     cell_ijk(G, q, i, j, k);
     T p0, lam, lof;
     if (e) {
-      if (SPLIT) {
-        SplitUpdateRead<T, E> rd{phi, e, G};
-        lof = vc_lofphi<T, DIM, false>(A, rd, i, j, k, false, p0, lam);
-      } else {
-        UpdateRead<T, E> rd{phi, e};
-        lof = vc_lofphi<T, DIM, false>(A, rd, i, j, k, false, p0, lam);
-      }
+      UpdateRead<T, E> rd{phi, e};
+      lof = vc_lofphi<T, DIM, false>(A, rd, i, j, k, false, p0, lam);
     } else {
       PlainRead<T> rd{phi};
       lof = vc_lofphi<T, DIM, false>(A, rd, i, j, k, false, p0, lam);
     }
     T v = rhs[q] - lof;
     if (res) res[q] = v;
-    if (res_inner) res_inner[SPLIT ? cs_index(G, i, j, k) : q] = (E)v;
+    if (res_inner) res_inner[q] = (E)v;
     acc = norm_accum<NORM>(acc, (double)v);
     if (e) out_phi[q] = p0;
   }

@@ -244,6 +244,75 @@ __global__ void __launch_bounds__(kBlock) vcl_prolong_kernel(VCLean P, Geom C, B
     P.e[q] = prolong_add<float, DIM, KIND, CIDX>(C, bc, 0, i, j, k, P.e[q], ec, nullptr);
   }
 }
+// The FP64 outer step of a mixed solve whose level 0 is lean: phi_out = phi +
+// e (e split, FP32), r = rhs - L(phi_out) with the operator's inhomogeneous
+// boundary conditions, its FP32 copy into res_inner (split) and its norm
+// partials.  vc_update_residual_kernel's quantities in a lean FP64 form (FMA
+// differences, the FP32 values widened on the integer pipe, the max norm on
+// bit patterns): about half its FP64 pipe operations; the same residual to
+// rounding.  e null: the residual of phi itself (no update).  `par` as in
+// vc_update_residual_kernel (device ping-pong of phi and out_phi).
+template <int DIM, int NORM>
+__global__ void __launch_bounds__(kBlock) vcl_outer_kernel(
+    VCArgs<double> A, const double *phi, const float *__restrict__ e,
+    const double *__restrict__ rhs, double *out_phi, float *__restrict__ res_inner,
+    double *__restrict__ part, const int *__restrict__ par) {
+  const Geom &G = A.G;
+  if (par && *par) {
+    double *t = out_phi;
+    out_phi = (double *)phi;
+    phi = t;
+  }
+  const double bd = A.beta * A.dxinv;
+  double acc = 0.0;
+  unsigned long long amax = 0ull;
+  for (long long q = gtid(); q < G.ncell; q += gstride()) {
+    int i, j, k;
+    cell_ijk(G, q, i, j, k);
+    const double p0 = e ? phi[q] + f64_exact(e[cs_index(G, i, j, k)]) : phi[q];
+    double s = 0.0;
+#pragma unroll
+    for (int d = 0; d < DIM; d++) {
+      const int m = G.n(d);
+#pragma unroll
+      for (int side = 1; side >= 0; side--) {
+        int nb[3] = {i, j, k}, fi[3] = {i, j, k};
+        nb[d] += side ? 1 : -1;
+        if (side) fi[d] += 1;
+        double pn;
+        if (nb[d] >= 0 && nb[d] < m) {
+          const long long qn = G.cell(nb[0], nb[1], nb[2]);
+          pn = e ? phi[qn] + f64_exact(e[cs_index(G, nb[0], nb[1], nb[2])]) : phi[qn];
+        } else if (G.per(d)) {
+          nb[d] = nb[d] < 0 ? m - 1 : 0;
+          const long long qn = G.cell(nb[0], nb[1], nb[2]);
+          pn = e ? phi[qn] + f64_exact(e[cs_index(G, nb[0], nb[1], nb[2])]) : phi[qn];
+        } else {
+          pn = ghost_value<double>(A.bc, d, side, 0, p0, A.dx, false);
+        }
+        s = fma(A.b[d][G.face(d, fi[0], fi[1], fi[2])], pn - p0, s);
+      }
+    }
+    double lof = -(bd * s);
+    lof = fma(A.alpha * (A.a ? A.a[q] : 1.0), p0, lof);
+    if (A.c) lof = fma(-A.beta * A.c[q], p0, lof);
+    const double v = rhs[q] - lof;
+    if (e) out_phi[q] = p0;
+    res_inner[cs_index(G, i, j, k)] = (float)v;
+    if (NORM == MLGPU_NORM_MAX) {
+      const unsigned long long bits =
+          (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
+      amax = bits > amax ? bits : amax;
+    } else if (NORM == MLGPU_NORM_L1) {
+      acc += fabs(v);
+    } else {
+      acc = fma(v, v, acc);
+    }
+  }
+  if (NORM == MLGPU_NORM_MAX) acc = __longlong_as_double((long long)amax);
+  const double r = block_reduce<NORM>(acc);
+  if (threadIdx.x == 0) part[blockIdx.x] = r;
+}
 #endif  // MLGPU_ADJ_F32_UNIT
 
 }  // namespace mlgpu
