@@ -51,7 +51,8 @@ namespace mlgpu {
 // converges onto a phase boundary 1e-7 away from its solution.
 struct StepClip {
   float CR, cp, St, te, Te, inv_k, inv_CRTe, frac;
-  ClosureParams p;  // the closure's own parameters (FP64 decisions)
+  ClosureParams p;              // the closure's own parameters (FP64 decisions)
+  double inv_k64, inv_CRTe64;   // 1/k, 1/(CR + Te) in FP64
   __host__ __device__ int regime32(float H, float C, float b[3]) const {
     float Hs = (C < -CR) ? 0.f : cp * ((-C - CR) * inv_k);
     if (Hs < 0.f) Hs = 0.f;
@@ -67,6 +68,42 @@ struct StepClip {
            fabsf(H - b[2]) < band * (1.f + fabsf(b[2]));
   }
 };
+
+#ifdef MLGPU_ADJ_F32_UNIT
+// The FP64 decision of the clipping for a cell near a regime bound: the
+// bounds with the constant divisors as reciprocals (to an ulp of the
+// closure's own; a cell an ulp from a bound may take either side), h1 clipped
+// past the first bound crossed.  Out of line: the regime-clipped update
+// leaves many cells near a bound, and inline FP64 code here would lower the
+// kernel's occupancy.
+static __device__ __noinline__ double step_clip_near(double h0, double c0, double h1, double c1,
+                                                     const StepClip &K) {
+  const ClosureParams &p = K.p;
+  auto bounds = [&](double C, double B[3]) {
+    double Hs = (C < -p.CR) ? 0.0 : p.cp * ((-C - p.CR) * K.inv_k64);
+    if (Hs < 0.0) Hs = 0.0;
+    B[0] = Hs + p.te * p.cp;
+    B[1] = (p.CR + C) * K.inv_CRTe64 * (p.St + p.te * (1 - p.cp)) + p.cp * p.te;
+    B[2] = p.St - C + p.te + p.Te;
+  };
+  auto regime = [](double H, const double B[3]) {
+    if (H <= B[0]) return 0;
+    if (H > B[0] && H <= B[1]) return 1;
+    if (H > B[1] && H < B[2]) return 2;
+    if (H >= B[2]) return 3;
+    return 4;
+  };
+  double B0[3], B1[3];
+  bounds(c0, B0);
+  bounds(c1, B1);
+  const int r0 = regime(h0, B0), r1 = regime(h1, B1);
+  if (r0 != r1 && r0 < 4 && r1 < 4) {
+    const double bnd = B1[r1 > r0 ? r0 : r0 - 1];
+    return bnd + (double)K.frac * (h1 - bnd);
+  }
+  return h1;
+}
+#endif
 
 template <class T>
 struct LinLeanT {
@@ -655,15 +692,8 @@ __global__ void __launch_bounds__(kBlock) lean_step_kernel(Geom G, StepClip K,
       const float h0f = f32_trunc(h0), h1f = f32_trunc(h1);
       const int f0 = K.regime32(h0f, f32_trunc(c0), b0);
       const int f1 = K.regime32(h1f, f32_trunc(c1), b1);
-      if (f0 != f1 || StepClip::near(h0f, b0) || StepClip::near(h1f, b1)) {
-        const int r0 = closure_regime(h0, c0, K.p), r1 = closure_regime(h1, c1, K.p);
-        if (r0 != r1 && r0 < 4 && r1 < 4) {
-          double B[3];
-          bounding_energy(c1, K.p, B[0], B[1], B[2]);
-          const double bnd = B[r1 > r0 ? r0 : r0 - 1];
-          h1 = bnd + (double)K.frac * (h1 - bnd);
-        }
-      }
+      if (f0 != f1 || StepClip::near(h0f, b0) || StepClip::near(h1f, b1))
+        h1 = step_clip_near(h0, c0, h1, c1, K);
     }
     u[q] = h1;
     u[n + q] = c1;

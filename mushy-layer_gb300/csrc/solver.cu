@@ -1724,6 +1724,8 @@ class HCAdjSolver : public mlgpu_solver {
     K.inv_CRTe = (float)(1.0 / (cp.CR + cp.Te));
     K.frac = (float)clip;
     K.p = cp;
+    K.inv_k64 = 1.0 / cp.k;
+    K.inv_CRTe64 = 1.0 / (cp.CR + cp.Te);
     return K;
   }
 

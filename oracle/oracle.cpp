@@ -2296,16 +2296,24 @@ int orc_mac_project_adjoint(const mlgpu_vcop *op, const mlgpu_mg_options *o,
 
 }  // extern "C"
 
-// Regime of (H, C) for the Newton update's clipping (lean_step_kernel's
-// decision restated: t_cl's own test, FP64); 0 solid, 1 eutectic, 2 mush,
-// 3 liquid, 4 NaN
-static int clip_regime(double H, double C, const mlgpu_params &p) {
-  double Hs, He, Hl;
-  bounding_energy(C, p, Hs, He, Hl);
-  if (H <= Hs) return 0;
-  if (H > Hs && H <= He) return 1;
-  if (H > He && H < Hl) return 2;
-  if (H >= Hl) return 3;
+// Bounds and regime of (H, C) for the Newton update's clipping
+// (step_clip_near restated: FP64 bounds with the constant divisors as
+// reciprocals); 0 solid, 1 eutectic, 2 mush, 3 liquid, 4 NaN
+static void clip_bounds(double C, const mlgpu_params &p, double B[3]) {
+  const double CR = p.compositionRatio, cp = p.specificHeatRatio, St = p.stefan,
+               te = p.thetaEutectic, Te = p.ThetaEutectic;
+  const double inv_k = 1.0 / p.waterDistributionCoeff, inv_CRTe = 1.0 / (CR + Te);
+  double Hs = (C < -CR) ? 0.0 : cp * ((-C - CR) * inv_k);
+  if (Hs < 0.0) Hs = 0.0;
+  B[0] = Hs + te * cp;
+  B[1] = (CR + C) * inv_CRTe * (St + te * (1 - cp)) + cp * te;
+  B[2] = St - C + te + Te;
+}
+static int clip_regime(double H, const double B[3]) {
+  if (H <= B[0]) return 0;
+  if (H > B[0] && H <= B[1]) return 1;
+  if (H > B[1] && H < B[2]) return 2;
+  if (H >= B[2]) return 3;
   return 4;
 }
 
@@ -2372,12 +2380,12 @@ extern "C" int orc_hc_newton_solve(const mlgpu_nlop *op, const mlgpu_mg_options 
       for (size_t q = 0; q < nc; q++) {
         double &h1 = S.L[0].u[q];
         const double c1 = S.L[0].u[nc + q];
-        const int r0 = clip_regime(uold[q], uold[nc + q], op->params);
-        const int r1 = clip_regime(h1, c1, op->params);
+        double B0[3], B1[3];
+        clip_bounds(uold[nc + q], op->params, B0);
+        clip_bounds(c1, op->params, B1);
+        const int r0 = clip_regime(uold[q], B0), r1 = clip_regime(h1, B1);
         if (r0 != r1 && r0 < 4 && r1 < 4) {
-          double B[3];
-          bounding_energy(c1, op->params, B[0], B[1], B[2]);
-          const double bnd = B[r1 > r0 ? r0 : r0 - 1];
+          const double bnd = B1[r1 > r0 ? r0 : r0 - 1];
           h1 = bnd + (double)(float)kNewtonClip * (h1 - bnd);
         }
       }
