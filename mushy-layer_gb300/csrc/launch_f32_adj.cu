@@ -137,6 +137,15 @@ cudaError_t launch_lean_restrict(const LinLeanT<T> &P, const Geom &C, int csplit
 template <class T>
 cudaError_t launch_lean_prolong(const LinLeanT<T> &P, const Geom &C, int csplit, int black,
                                 int kind, const T *xc, cudaStream_t s) {
+  if (black && kind == MLGPU_PROLONG_LINEAR) {  // one thread per coarse cell
+    const int nbc = blocks_for(C.ncell);
+    if (csplit) {
+      MLGPU_DIM_SWITCH(P.G.dim, (lean_prolong_lin_black_kernel<T, DIM, SplitIdx><<<nbc, kBlock, 0, s>>>(P, C, xc)));
+    } else {
+      MLGPU_DIM_SWITCH(P.G.dim, (lean_prolong_lin_black_kernel<T, DIM, NaturalIdx><<<nbc, kBlock, 0, s>>>(P, C, xc)));
+    }
+    return cudaGetLastError();
+  }
   const int nb = blocks_for(black ? P.G.ncell >> 1 : P.G.ncell);
 #define MLGPU_LEAN_PRO(KIND, IDX, BL) \
   MLGPU_DIM_SWITCH(P.G.dim, (lean_prolong_kernel<T, DIM, KIND, IDX, BL><<<nb, kBlock, 0, s>>>(P, C, xc)))

@@ -645,6 +645,88 @@ __global__ void __launch_bounds__(kBlock) lean_state_kernel(AdjArgs<T> A, Closur
   }
 }
 
+// The linear prolongation onto the black half (BLACK of lean_prolong_kernel
+// with KIND linear) with one thread per coarse cell: its black children
+// (the fine cells of odd (ii + jj + kk)) share the coarse values they read
+// (23 of the 27 around the coarse cell in 3D, instead of 8 per child), and
+// each child's value is prolong_add's expression on them.
+template <class T, int DIM, class CIDX>
+__global__ void __launch_bounds__(kBlock) lean_prolong_lin_black_kernel(LinLeanT<T> P, Geom C,
+                                                                        const T *__restrict__ xc) {
+  const Geom &G = P.G;
+  const long long n = G.ncell;
+  const T den = T(1) / (DIM == 3 ? T(64) : T(16));
+  const T fx1 = T(3) * den, fx2 = T(9) * den, fx3 = T(27) * den, f0 = T(1) * den;
+  const CIDX at;
+  for (long long Q = gtid(); Q < C.ncell; Q += gstride()) {
+    int I, J, K;
+    cell_ijk(C, Q, I, J, K);
+    const int base[3] = {I, J, K};
+    // coordinate and (per component) sign of the coarse value at offset
+    // o in {-1, 0, 1} along each direction, as coarse_at forms them
+    int co[3][3];
+    T sg[2][3][3];
+#pragma unroll
+    for (int d = 0; d < 3; d++)
+#pragma unroll
+      for (int o = 0; o < 3; o++) {
+        int x = base[d] + o - 1;
+        T s0 = T(1), s1 = T(1);
+        if (d < DIM) {
+          const int m = C.n(d);
+          if (x < 0 || x >= m) {
+            const int side = x < 0 ? 0 : 1;
+            if (C.per(d)) {
+              x = x < 0 ? m - 1 : 0;
+            } else {
+              x = x < 0 ? 0 : m - 1;
+              if (P.ybc.type[d][side][0] == MLGPU_BC_DIRICHLET) s0 = -s0;
+              if (P.ybc.type[d][side][1] == MLGPU_BC_DIRICHLET) s1 = -s1;
+            }
+          }
+        } else {
+          x = base[d];
+        }
+        co[d][o] = x;
+        sg[0][d][o] = s0;
+        sg[1][d][o] = s1;
+      }
+    auto cv = [&](int c, int ox, int oy, int oz) -> T {
+      const long long q = (long long)c * C.ncell + at(C, co[0][ox + 1], co[1][oy + 1], co[2][oz + 1]);
+      return (sg[c][0][ox + 1] * sg[c][1][oy + 1] * sg[c][2][oz + 1]) * xc[q];
+    };
+#pragma unroll
+    for (int kk = 0; kk < (DIM == 3 ? 2 : 1); kk++)
+#pragma unroll
+      for (int jj = 0; jj < 2; jj++)
+#pragma unroll
+        for (int ii = 0; ii < 2; ii++) {
+          if (((ii + jj + kk) & 1) == 0) continue;  // red child: not prolonged
+          const int i = 2 * I + ii, j = 2 * J + jj, k = DIM == 3 ? 2 * K + kk : 0;
+          const long long qf = cs_index(G, i, j, k);
+          const int o1 = 2 * ii - 1, o2 = 2 * jj - 1, o3 = DIM == 3 ? 2 * kk - 1 : 0;
+          T xv[2];
+#pragma unroll
+          for (int c = 0; c < 2; c++) {
+            T p = P.x[c * n + qf];
+            if (DIM == 2) {
+              p = p + fx2 * cv(c, 0, 0, 0) + f0 * cv(c, o1, o2, 0);
+              p = p + fx1 * (cv(c, o1, 0, 0) + cv(c, 0, o2, 0));
+            } else {
+              p = p + fx3 * cv(c, 0, 0, 0) + f0 * cv(c, o1, o2, o3);
+              p = p + fx2 * (cv(c, o1, 0, 0) + cv(c, 0, o2, 0) + cv(c, 0, 0, o3));
+              p = p + fx1 * (cv(c, o1, o2, 0) + cv(c, 0, o2, o3) + cv(c, o1, 0, o3));
+            }
+            xv[c] = p;
+          }
+          P.x[qf] = xv[0];
+          P.x[n + qf] = xv[1];
+          P.w[qf] = fmaT(P.J[qf], xv[0], P.J[n + qf] * xv[1]);
+          P.w[n + qf] = fmaT(P.J[2 * n + qf], xv[0], P.J[3 * n + qf] * xv[1]);
+        }
+  }
+}
+
 // dst (T, layout IDX) = src (natural) for `ncomp` components of n cells each
 template <class T, class S, class IDX>
 __global__ void __launch_bounds__(kBlock) lean_pack_kernel(Geom G, int ncomp,
