@@ -245,3 +245,45 @@ def test_vector_half_sweeps_same_bits(prec, fuse, case):
         out.append((host(new), st.iterations, st.cycles))
     assert out[0][1:] == out[1][1:]
     assert np.array_equal(out[0][0], out[1][0])
+
+
+@pytest.mark.parametrize("shape,per", [((32, 24, 40), (0, 0, 1)), ((36, 32, 32), (1, 0, 0)),
+                                       ((48, 40, 1), (1, 0, 0))])
+def test_lean_layouts_walls_and_rows(shape, per):
+    """The lean cycles on other box shapes: walls in x with a periodic z
+    (the vector sweep's wall ends), a level-0 row of 18 cells per colour (the
+    one-cell-per-thread sweep), a 2D box periodic in x; mixed and lean FP64
+    Newton steps converge to the FP64 solution."""
+    from mushy_gb300 import ops
+    dim = 3 if shape[2] > 1 else 2
+    n = list(shape[:dim])
+    g = abi.make_grid(n, 1.0 / n[0], per)
+    rng = np.random.default_rng(31)
+    cs = abi.cell_shape(g)
+    prm = abi.make_params(stefan=5.0, compositionRatio=5.0, waterDistributionCoeff=1e-3,
+                          specificHeatRatio=1.0)
+    wall = dim - 1 if not per[dim - 1] else 0
+    der = abi.make_bc({(wall, 0, 0): (abi.BC_DIRICHLET, -1.0), (wall, 0, 1): (abi.BC_DIRICHLET, -1.0)})
+    phi0 = np.empty((2,) + cs)
+    phi0[0] = 5.0 + 0.8 * rng.standard_normal(cs)
+    phi0[1] = -1.0
+    b = [np.stack([-np.ones(abi.face_shape(g, d)), np.full(abi.face_shape(g, d), -1e-2)])
+         for d in range(dim)]
+    dt = 2e-3
+    op = ops.NLMultiCompOp(g, prm, abi.make_bc(), der, 1.0, -dt, None, [dev(x) for x in b])
+    ref = O.NLOpHost(g, prm, abi.make_bc(), der, 1.0, -dt, None, b)
+    out = {}
+    for key, prec, fuse in (("mixed", abi.PREC_MIXED, 1), ("fp64", abi.PREC_F64, 1),
+                            ("fp64_fast", abi.PREC_F64, 2)):
+        o = _opts(prec)
+        o.fuse_levels = fuse
+        new = dev(phi0)
+        st, rc = ops.AdjointMultiGrid(op, o).backwardEulerNewton(new, dev(phi0), dt)
+        assert rc == 0, (key, rc, st.iterations)
+        assert st.levels >= 2
+        out[key] = host(new)
+    u64 = out["fp64"]
+    r0 = O.norm(O.nl_residual(ref, phi0, phi0))
+    assert O.norm(O.nl_residual(ref, out["mixed"], phi0)) <= 1e-10 * r0 * 1.0001
+    assert np.abs(out["mixed"] - u64).max() <= 1e-8 * np.abs(u64).max()
+    assert np.abs(out["fp64_fast"] - u64).max() <= 1e-11 * np.abs(u64).max()

@@ -109,3 +109,24 @@ def test_lean3d_no_post_smoothing():
     path in the reference's form stops on its hang test after one iteration
     on this operator, so only the oracle's residual is checked)."""
     _check(_darcy((32, 32, 32), 23), False, fp64_converges=False, num_smooth_up=0)
+
+
+@pytest.mark.parametrize("shape,per", [((40, 24, 32), (0, 0, 1)), ((36, 32, 16), (1, 1, 1))])
+def test_lean3d_other_boxes(shape, per):
+    """Walls in x with a periodic z (the vector sweep's wall ends), and a
+    fully periodic projection with 18 cells per colour row on level 0 (the
+    one-cell-per-thread sweep)."""
+    rng = np.random.default_rng(24)
+    g = abi.make_grid(list(shape), 1.0 / shape[0], per)
+    if all(per):
+        b = [-rng.uniform(0.2, 3.0, abi.face_shape(g, d)) for d in range(3)]
+        f = rng.standard_normal(abi.cell_shape(g))
+        f -= f.mean()
+        _check((g, abi.make_bc(), 0.0, 1.0, None, b, None, f), True)
+    else:
+        bc = P.vc_bc("mixed")
+        b = [-rng.uniform(0.2, 3.0, abi.face_shape(g, d)) for d in range(3)]
+        aC = rng.uniform(0.5, 1.5, abi.cell_shape(g))
+        cC = rng.uniform(0.1, 2.0, abi.cell_shape(g))
+        f = rng.standard_normal(abi.cell_shape(g))
+        _check((g, bc, 1.0, -0.5, aC, b, cC, f), False)
