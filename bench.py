@@ -633,6 +633,30 @@ def config1(args, torch, abi, ops, O, P):
         h, st_ref, rc_ref = O.hc_backward_euler(ref, oo, h, h, dt)
     cpu_s = time.time() - t0
     diff = float(np.abs(cur.cpu().numpy() - h).max())
+    # the same ten steps solved to 1e-10 by Newton on the Jacobian hierarchy
+    # (the reference's FAS with its 10-iteration cap stops above it), FP64 and
+    # mixed, and the mixed states against the FP64 ones
+    newton = {}
+    states = {}
+    for key, code in (("fp64", abi.PREC_F64), ("mixed", abi.PREC_MIXED)):
+        no = ops.default_options(True)
+        no.tolerance, no.hang, no.max_iter, no.precision = TOL, -1.0, 60, code
+        NS = ops.AdjointMultiGrid(op, no)
+
+        def nmarch():
+            cur, out = dev(phi0), []
+            for _ in range(steps):
+                new = cur.clone()
+                st, rc = NS.backwardEulerNewton(new, cur, dt)
+                out.append((rc, st.iterations, float("%.2e" % (st.final_norm / st.initial_norm))))
+                cur = new
+            return cur, out
+        nmarch()
+        ms_n, (cur_n, out_n) = _events_ms(nmarch)
+        states[key] = cur_n.cpu().numpy()
+        newton[key] = {"ms_per_step": ms_n / steps, "steps": out_n,
+                       "converged": all(r == 0 and f <= TOL for r, _, f in out_n)}
+    newton["mixed_vs_fp64_max_abs"] = float(np.abs(states["mixed"] - states["fp64"]).max())
     return {"metric": "backward-Euler steps/s (FAS to 1e-10, FP64)", "value": steps / (ms * 1e-3),
             "unit": "steps/s", "higher_is_better": True, "ms_per_step": ms / steps,
             "cell_updates_per_s": upd / (ms * 1e-3), "fas_iterations": its, "status": rcs,
@@ -642,7 +666,9 @@ def config1(args, torch, abi, ops, O, P):
             "mixed": {"ms_per_step": ms_m / steps, "fas_iterations": its_m, "status": rcs_m,
                       "max_abs_diff_vs_fp64": float(np.abs(cur_m.cpu().numpy() -
                                                            cur.cpu().numpy()).max())},
-            "note": "latency bound (4096 cells): report only"}
+            "newton_to_1e-10": newton,
+            "note": "latency bound (4096 cells): report only; status (rc, final/initial) per "
+                    "step; Newton steps (rc, iterations, final/initial)"}
 
 
 def config3(args, torch, abi, ops, O, P):
