@@ -129,9 +129,11 @@ class C4Runner:
             ho = ops.default_options(True)
             ho.tolerance, ho.hang, ho.max_iter, ho.precision = TOL, -1.0, 60, code
             if prec == "fp64_fast":
-                # Newton's cycles with the mixed path's kernels (lean update,
-                # colour-split layout) in FP64: the same design, FP64 data
+                # the mixed path's kernels in FP64: Newton's lean cycles and
+                # outer loops, the projection's lean split cycles and outer
+                # step -- the same design, FP64 data
                 ho.fuse_levels = 2
+                po.fuse_levels = 2
             if use_graph is not None:
                 po.use_graph = ho.use_graph = use_graph
             self.S[prec] = (ops.AMRMultiGrid(prob["pop"], po), ops.AdjointMultiGrid(prob["hop"], ho))
@@ -286,9 +288,9 @@ def run_gpu(args):
                  "note": "reference expression order (bitwise the oracle's kernels)"},
         "fp64_fast": {**C4Runner.summary(out_f), "value": upd_f * world / (ms_f * 1e-3),
                       "ms_per_step": ms_f / args.steps,
-                      "note": "FP64 with the mixed path's kernel design (lean Jacobian "
-                              "update, colour-split layout) for Newton's cycles; "
-                              "projection as fp64",
+                      "note": "FP64 with the mixed path's kernel design (lean colour-split "
+                              "cycles and lean FP64 outer loops, for Newton's step "
+                              "and the projection)",
                       "hc_rel_vs_fp64": hc_err_fast},
         "time_to_solution_ratio_fp64_over_mixed": ms_d / ms_m,
         "time_to_solution_ratio_fp64_fast_over_mixed": ms_f / ms_m,

@@ -173,9 +173,13 @@ typedef struct mlgpu_mg_options {
                             (levels of at most 256 cells; in 2D mixed precision
                             1024) and, in mixed precision, 2D levels above that run
                             FP32 shared-memory tiles (smoothing fused with
-                            restriction / prolongation); 2: FP64 cycles use the
-                            tiles too; 0: one launch per smoothing pass / transfer.
-                            FP64 results are the same bits for 0, 1, 2 */
+                            restriction / prolongation), 3D levels the lean
+                            colour-split cycles; 2: FP64 cycles use the tiles (2D)
+                            and the lean cycles (3D; the Jacobian solver's Newton
+                            cycles too) as well; 0: one launch per smoothing pass /
+                            transfer.  FP64 results are the same bits for 0, 1 and
+                            for 2 in 2D (the 3D lean FP64 cycles keep the FP64
+                            residual and tolerance, not the reference's bits) */
 } mlgpu_mg_options;
 
 typedef struct mlgpu_solve_stats {

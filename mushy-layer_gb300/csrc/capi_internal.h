@@ -114,21 +114,27 @@ cudaError_t launch_lean_restrict(const LinLeanT<T> &P, const Geom &C, int csplit
 template <class T>
 cudaError_t launch_lean_prolong(const LinLeanT<T> &P, const Geom &C, int csplit, int black,
                                 int kind, const T *xc, cudaStream_t s);
-// lean FP32 cycles of the linear operator on 3D levels (vc_lean_kernels.cuh):
-// diag and 1/diag to the split layout (once per solver), red/black half
-// sweep (zero: the other colour's e is zero), residual restriction (red: the
-// red children only) with the coarse e zeroed, black-only prolongation
-cudaError_t launch_vcl_diag(const VCArgs<float> &A, float *idg, float *dg, cudaStream_t s);
-cudaError_t launch_vcl_gsrb(const VCLean &P, int pass, int zero, cudaStream_t s, int vec = 1);
-cudaError_t launch_vcl_restrict(const VCLean &P, const Geom &C, int csplit, int red, float *rc,
-                                float *ec, cudaStream_t s);
-cudaError_t launch_vcl_prolong(const VCLean &P, const Geom &C, const BCD &bc, int csplit,
-                               int black, int kind, const float *ec, cudaStream_t s);
-// the FP64 outer step of a mixed solve with a lean level 0 (e, res_inner split)
-cudaError_t launch_vcl_outer(const VCArgs<double> &A, int norm, const double *phi,
-                             const float *e, const double *rhs, double *out_phi,
-                             float *res_inner, double *part, int *nparts, cudaStream_t s,
-                             const int *par = nullptr);
+// lean cycles of the linear operator on 3D levels (vc_lean_kernels.cuh; T =
+// float for the mixed solve, double for the comparison path): diag and 1/diag
+// to the split layout (once per solver), red/black half sweep (zero: the
+// other colour's e is zero), residual restriction (red: the red children
+// only) with the coarse e zeroed, black-only prolongation, and the FP64 outer
+// step with a lean level 0 (e, res_inner split, in the cycles' precision E)
+template <class T>
+cudaError_t launch_vcl_diag(const VCArgs<T> &A, T *idg, T *dg, cudaStream_t s);
+template <class T>
+cudaError_t launch_vcl_gsrb(const VCLeanT<T> &P, int pass, int zero, cudaStream_t s,
+                            int vec = 1);
+template <class T>
+cudaError_t launch_vcl_restrict(const VCLeanT<T> &P, const Geom &C, int csplit, int red, T *rc,
+                                T *ec, cudaStream_t s);
+template <class T>
+cudaError_t launch_vcl_prolong(const VCLeanT<T> &P, const Geom &C, const BCD &bc, int csplit,
+                               int black, int kind, const T *ec, cudaStream_t s);
+template <class E>
+cudaError_t launch_vcl_outer(const VCArgs<double> &A, int norm, const double *phi, const E *e,
+                             const double *rhs, double *out_phi, E *res_inner, double *part,
+                             int *nparts, cudaStream_t s, const int *par = nullptr);
 // per-cell face sums P of a smoothed level (natural layout), once per solver
 template <class T>
 cudaError_t launch_lean_psum(const AdjArgs<T> &A, T *P, cudaStream_t s);

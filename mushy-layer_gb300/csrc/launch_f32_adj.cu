@@ -216,26 +216,31 @@ cudaError_t launch_lean_step(const Geom &G, int split, const StepClip *clip, dou
   return cudaGetLastError();
 }
 
-// ---- lean FP32 cycles of the linear operator on 3D levels (vc_lean_kernels.cuh)
-cudaError_t launch_vcl_diag(const VCArgs<float> &A, float *idg, float *dg, cudaStream_t s) {
-  MLGPU_DIM_SWITCH(A.G.dim, (vcl_diag_kernel<DIM><<<blocks_for(A.G.ncell), kBlock, 0, s>>>(A, idg, dg)));
+// ---- lean cycles of the linear operator on 3D levels (vc_lean_kernels.cuh),
+// FP32 for the mixed solve and FP64 for the comparison path
+template <class T>
+cudaError_t launch_vcl_diag(const VCArgs<T> &A, T *idg, T *dg, cudaStream_t s) {
+  MLGPU_DIM_SWITCH(A.G.dim, (vcl_diag_kernel<T, DIM><<<blocks_for(A.G.ncell), kBlock, 0, s>>>(A, idg, dg)));
   return cudaGetLastError();
 }
 
-cudaError_t launch_vcl_gsrb(const VCLean &P, int pass, int zero, cudaStream_t s, int vec) {
-  if (vec && ((P.G.n0 >> 1) % 4) == 0) {
-    MLGPU_DIM_SWITCH(P.G.dim, (vcl_gsrb_vec_kernel<DIM><<<blocks_for((P.G.ncell >> 1) / 4), kBlock, 0, s>>>(P, pass, zero)));
+template <class T>
+cudaError_t launch_vcl_gsrb(const VCLeanT<T> &P, int pass, int zero, cudaStream_t s, int vec) {
+  constexpr int V = Vec16<T>::V;
+  if (vec && ((P.G.n0 >> 1) % V) == 0) {
+    MLGPU_DIM_SWITCH(P.G.dim, (vcl_gsrb_vec_kernel<T, DIM><<<blocks_for((P.G.ncell >> 1) / V), kBlock, 0, s>>>(P, pass, zero)));
   } else {
-    MLGPU_DIM_SWITCH(P.G.dim, (vcl_gsrb_kernel<DIM><<<blocks_for(P.G.ncell >> 1), kBlock, 0, s>>>(P, pass, zero)));
+    MLGPU_DIM_SWITCH(P.G.dim, (vcl_gsrb_kernel<T, DIM><<<blocks_for(P.G.ncell >> 1), kBlock, 0, s>>>(P, pass, zero)));
   }
   return cudaGetLastError();
 }
 
-cudaError_t launch_vcl_restrict(const VCLean &P, const Geom &C, int csplit, int red, float *rc,
-                                float *ec, cudaStream_t s) {
+template <class T>
+cudaError_t launch_vcl_restrict(const VCLeanT<T> &P, const Geom &C, int csplit, int red, T *rc,
+                                T *ec, cudaStream_t s) {
   const int nb = blocks_for(C.ncell);
 #define MLGPU_VCL_RST(IDX, RED) \
-  MLGPU_DIM_SWITCH(P.G.dim, (vcl_restrict_kernel<DIM, IDX, RED><<<nb, kBlock, 0, s>>>(P, C, rc, ec)))
+  MLGPU_DIM_SWITCH(P.G.dim, (vcl_restrict_kernel<T, DIM, IDX, RED><<<nb, kBlock, 0, s>>>(P, C, rc, ec)))
   if (csplit) {
     if (red)
       MLGPU_VCL_RST(SplitIdx, true);
@@ -251,11 +256,12 @@ cudaError_t launch_vcl_restrict(const VCLean &P, const Geom &C, int csplit, int 
   return cudaGetLastError();
 }
 
-cudaError_t launch_vcl_prolong(const VCLean &P, const Geom &C, const BCD &bc, int csplit,
-                               int black, int kind, const float *ec, cudaStream_t s) {
+template <class T>
+cudaError_t launch_vcl_prolong(const VCLeanT<T> &P, const Geom &C, const BCD &bc, int csplit,
+                               int black, int kind, const T *ec, cudaStream_t s) {
   const int nb = blocks_for(black ? P.G.ncell >> 1 : P.G.ncell);
 #define MLGPU_VCL_PRO(KIND, IDX, BL) \
-  MLGPU_DIM_SWITCH(P.G.dim, (vcl_prolong_kernel<DIM, KIND, IDX, BL><<<nb, kBlock, 0, s>>>(P, C, bc, ec)))
+  MLGPU_DIM_SWITCH(P.G.dim, (vcl_prolong_kernel<T, DIM, KIND, IDX, BL><<<nb, kBlock, 0, s>>>(P, C, bc, ec)))
 #define MLGPU_VCL_PRO2(KIND, IDX)    \
   if (black)                         \
     MLGPU_VCL_PRO(KIND, IDX, true);  \
@@ -279,20 +285,34 @@ cudaError_t launch_vcl_prolong(const VCLean &P, const Geom &C, const BCD &bc, in
   return cudaGetLastError();
 }
 
-cudaError_t launch_vcl_outer(const VCArgs<double> &A, int norm, const double *phi,
-                             const float *e, const double *rhs, double *out_phi,
-                             float *res_inner, double *part, int *nparts, cudaStream_t s,
-                             const int *par) {
+template <class E>
+cudaError_t launch_vcl_outer(const VCArgs<double> &A, int norm, const double *phi, const E *e,
+                             const double *rhs, double *out_phi, E *res_inner, double *part,
+                             int *nparts, cudaStream_t s, const int *par) {
   const int nb = blocks_for(A.G.ncell);
   if (nparts) *nparts = nb;
   if (norm < 0) norm = MLGPU_NORM_MAX;
   MLGPU_DIM_SWITCH(A.G.dim, MLGPU_NORM_SWITCH(norm, {
     if (NORM >= 0)
-      vcl_outer_kernel<DIM, (NORM < 0 ? 0 : NORM)>
+      vcl_outer_kernel<E, DIM, (NORM < 0 ? 0 : NORM)>
           <<<nb, kBlock, 0, s>>>(A, phi, e, rhs, out_phi, res_inner, part, par);
   }));
   return cudaGetLastError();
 }
+
+#define MLGPU_VCL_INST(T)                                                                       \
+  template cudaError_t launch_vcl_diag<T>(const VCArgs<T> &, T *, T *, cudaStream_t);           \
+  template cudaError_t launch_vcl_gsrb<T>(const VCLeanT<T> &, int, int, cudaStream_t, int);     \
+  template cudaError_t launch_vcl_restrict<T>(const VCLeanT<T> &, const Geom &, int, int, T *,  \
+                                             T *, cudaStream_t);                               \
+  template cudaError_t launch_vcl_prolong<T>(const VCLeanT<T> &, const Geom &, const BCD &, int, \
+                                            int, int, const T *, cudaStream_t);                \
+  template cudaError_t launch_vcl_outer<T>(const VCArgs<double> &, int, const double *,         \
+                                          const T *, const double *, double *, T *, double *,  \
+                                          int *, cudaStream_t, const int *);
+MLGPU_VCL_INST(float)
+MLGPU_VCL_INST(double)
+#undef MLGPU_VCL_INST
 
 #define MLGPU_LEAN_INST(T)                                                                     \
   template cudaError_t launch_lean_gsrb<T>(const LinLeanT<T> &, int, cudaStream_t, int);      \

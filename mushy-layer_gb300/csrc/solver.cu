@@ -193,10 +193,11 @@ struct VCLevel {
   double *lam64 = nullptr;  // stored 1/diag for FP64 inner cycles
   float *fcx = nullptr, *fcy = nullptr, *flam = nullptr, *fdiag = nullptr;  // lean FP32 tiles
   double *ocx = nullptr, *ocy = nullptr, *odiag = nullptr;  // FP64 outer step (level 0, mixed)
-  // mixed 3D levels above the single-CTA block cycle: the lean FP32 cycles
-  // (vc_lean_kernels.cuh) with e, r colour-split and the diagonal folded
+  // 3D levels above the single-CTA block cycle, in mixed precision or with
+  // options.fuse_levels >= 2 in FP64: the lean cycles (vc_lean_kernels.cuh,
+  // inner precision) with e, r colour-split and the diagonal folded
   bool lean = false;
-  float *idg = nullptr, *dg = nullptr;
+  void *idg = nullptr, *dg = nullptr;
 };
 
 class VCSolver : public mlgpu_solver {
@@ -335,15 +336,17 @@ class VCSolver : public mlgpu_solver {
     // FP32 tiles pay for their halo recomputation; FP64 tiles (4 extra half
     // sweeps of redundant FP64 work per tile) only when asked for explicitly
     use_tiles = use_block_cycle && (mixed || o.fuse_levels >= 2);
-    // mixed 3D: every level above the block cycle (and above the bottom)
-    // runs the lean split cycles; such a level has even extents
-    if (mixed && op.grid.dim == 3 && o.relax_mode == MLGPU_RELAX_GSRB)
+    // 3D, mixed or FP64 with fuse_levels >= 2: every level above the block
+    // cycle (and above the bottom) runs the lean split cycles; such a level
+    // has even extents
+    if ((mixed || o.fuse_levels >= 2) && op.grid.dim == 3 && o.relax_mode == MLGPU_RELAX_GSRB)
       for (int l = 0; l < depth; l++) {
         if (use_block_cycle && L[l].G.ncell <= kBlockCycleCells && depth - l + 1 <= kMaxBlockLevels)
           break;
         L[l].lean = true;
-        L[l].idg = A.get<float>(ncells(L[l].grid));
-        L[l].dg = A.get<float>(ncells(L[l].grid));
+        const size_t nb = (mixed ? sizeof(float) : sizeof(double)) * ncells(L[l].grid);
+        L[l].idg = A.get<char>(nb);
+        L[l].dg = A.get<char>(nb);
       }
     size_t n0 = ncells(op.grid);
     phi[0] = A.get<double>(n0);
@@ -398,7 +401,8 @@ class VCSolver : public mlgpu_solver {
   int build_fast() {
     if (L[0].ocx) CK(launch_outer_coefs(outer_args(), L[0].ocx, L[0].ocy, L[0].odiag, s));
     for (size_t l = 0; l < L.size(); l++)
-      if (L[l].lean) CK(launch_vcl_diag(args<float>((int)l), L[l].idg, L[l].dg, s));
+      if (L[l].lean)
+        CK(launch_vcl_diag<float>(args<float>((int)l), (float *)L[l].idg, (float *)L[l].dg, s));
     for (size_t l = 0; l < L.size(); l++) {
       if (!L[l].fcx) continue;
       VCArgs<double> A = args<double>((int)l);
@@ -418,6 +422,7 @@ class VCSolver : public mlgpu_solver {
       VCArgs<double> A = args<double>((int)l);
       A.lam = nullptr;
       CK(launch_vc_lambda<double>(A, L[l].lam64, s));
+      if (L[l].lean) CK(launch_vcl_diag<double>(A, (double *)L[l].idg, (double *)L[l].dg, s));
     }
     return MLGPU_OK;
   }
@@ -563,31 +568,33 @@ class VCSolver : public mlgpu_solver {
     return MLGPU_OK;
   }
 
-  // lean FP32 operator of a lean 3D level
-  VCLean vclean(int l) {
-    const VCArgs<float> A = args<float>(l);
-    VCLean P;
+  // lean operator of a lean 3D level, in the inner precision T
+  template <class T>
+  VCLeanT<T> vclean(int l) {
+    const VCArgs<T> A = args<T>(l);
+    VCLeanT<T> P;
     P.G = A.G;
     P.bd = A.beta * A.dxinv;
     for (int d = 0; d < 3; d++) P.b[d] = A.b[d];
-    P.idg = L[l].idg;
-    P.dg = L[l].dg;
-    P.e = (float *)L[l].e;
-    P.r = (const float *)L[l].r;
+    P.idg = (const T *)L[l].idg;
+    P.dg = (const T *)L[l].dg;
+    P.e = (T *)L[l].e;
+    P.r = (const T *)L[l].r;
     return P;
   }
 
   // n red/black sweeps of a lean level; a zero start skips the first half
   // sweep's neighbour reads
+  template <class T>
   int relax_lean(int l, int n, bool zero_init) {
-    const VCLean P = vclean(l);
+    const VCLeanT<T> P = vclean<T>(l);
     if (n == 0) {
-      if (zero_init) CK(cudaMemsetAsync(P.e, 0, sizeof(float) * L[l].G.ncell, s));
+      if (zero_init) CK(cudaMemsetAsync(P.e, 0, sizeof(T) * L[l].G.ncell, s));
       return MLGPU_OK;
     }
     for (int i = 0; i < n; i++) {
-      CK(launch_vcl_gsrb(P, 0, (zero_init && i == 0) ? 1 : 0, s));
-      CK(launch_vcl_gsrb(P, 1, 0, s));
+      CK(launch_vcl_gsrb<T>(P, 0, (zero_init && i == 0) ? 1 : 0, s));
+      CK(launch_vcl_gsrb<T>(P, 1, 0, s));
     }
     return MLGPU_OK;
   }
@@ -596,20 +603,22 @@ class VCSolver : public mlgpu_solver {
   // black residual vanishes after the black half sweep), the coarser levels,
   // black-only prolongation (the red half sweep that follows overwrites the
   // red e unread), post-smoothing
+  template <class T>
   int cycle_lean(int l, bool zero_init) {
-    const VCLean P = vclean(l);
+    const VCLeanT<T> P = vclean<T>(l);
     const int csplit = L[l + 1].lean ? 1 : 0;
-    int rc = relax_lean(l, o.num_smooth_down, zero_init);
+    int rc = relax_lean<T>(l, o.num_smooth_down, zero_init);
     if (rc) return rc;
-    CK(launch_vcl_restrict(P, L[l + 1].G, csplit, o.num_smooth_down >= 1 ? 1 : 0,
-                           (float *)L[l + 1].r, (float *)L[l + 1].e, s));
+    CK(launch_vcl_restrict<T>(P, L[l + 1].G, csplit, o.num_smooth_down >= 1 ? 1 : 0,
+                              (T *)L[l + 1].r, (T *)L[l + 1].e, s));
     for (int m = 0; m < o.num_mg; m++) {
-      rc = cycle<float>(l + 1, m == 0);
+      rc = cycle<T>(l + 1, m == 0);
       if (rc) return rc;
     }
-    CK(launch_vcl_prolong(P, L[l + 1].G, make_bcd(op.bc), csplit, o.num_smooth_up >= 1 ? 1 : 0,
-                          o.prolong, (const float *)L[l + 1].ecur, s));
-    return relax_lean(l, o.num_smooth_up, false);
+    CK(launch_vcl_prolong<T>(P, L[l + 1].G, make_bcd(op.bc), csplit,
+                             o.num_smooth_up >= 1 ? 1 : 0, o.prolong, (const T *)L[l + 1].ecur,
+                             s));
+    return relax_lean<T>(l, o.num_smooth_up, false);
   }
 
   template <class T>
@@ -619,8 +628,7 @@ class VCSolver : public mlgpu_solver {
     // a fresh correction starts in e; a continued one stays where the last
     // pass left it (the tile path alternates e / t, the other paths work in e)
     if (zero_init || !L[l].ecur) L[l].ecur = L[l].e;
-    if constexpr (sizeof(T) == 4)
-      if (L[l].lean) return cycle_lean(l, zero_init);
+    if (L[l].lean) return cycle_lean<T>(l, zero_init);
     // the lean FP32 single-CTA cycle takes levels up to 1024 cells
     const long long block_cells = (sizeof(T) == 4 && L[l].fcx) ? kFastCycCells : kBlockCycleCells;
     if (use_tiles && l < last && L[l].G.dim == 2 && L[l].G.ncell > block_cells) {
@@ -723,8 +731,11 @@ class VCSolver : public mlgpu_solver {
     for (int d = 0; d < 3; d++) A.b[d] = (const double *)op.bCoef[d];
     int nparts = 0;
     if (mixed && L[0].lean)
-      CK(launch_vcl_outer(A, o.norm_type, phi[from], (const float *)L[0].ecur, rhs,
-                          phi[1 - from], (float *)L[0].r, part, &nparts, s, par));
+      CK(launch_vcl_outer<float>(A, o.norm_type, phi[from], (const float *)L[0].ecur, rhs,
+                                 phi[1 - from], (float *)L[0].r, part, &nparts, s, par));
+    else if (L[0].lean)
+      CK(launch_vcl_outer<double>(A, o.norm_type, phi[from], (const double *)L[0].ecur, rhs,
+                                  phi[1 - from], (double *)L[0].r, part, &nparts, s, par));
     else if (mixed)
       CK((launch_vc_update_residual<double, float>(A, o.norm_type, phi[from],
                                                    (const float *)L[0].ecur, rhs, phi[1 - from],
@@ -803,8 +814,11 @@ class VCSolver : public mlgpu_solver {
     } else {
       int nparts = 0;
       if (mixed && L[0].lean)
-        CK(launch_vcl_outer(A, o.norm_type, phi[0], nullptr, rhs, nullptr, (float *)L[0].r, part,
-                            &nparts, s));
+        CK(launch_vcl_outer<float>(A, o.norm_type, phi[0], nullptr, rhs, nullptr,
+                                   (float *)L[0].r, part, &nparts, s));
+      else if (L[0].lean)
+        CK(launch_vcl_outer<double>(A, o.norm_type, phi[0], nullptr, rhs, nullptr,
+                                    (double *)L[0].r, part, &nparts, s));
       else if (mixed)
         CK((launch_vc_update_residual<double, float>(A, o.norm_type, phi[0], nullptr, rhs, nullptr,
                                                      nullptr, (float *)L[0].r, part, &nparts, s)));

@@ -138,3 +138,21 @@ def test_lean3d_other_boxes(shape, per):
         cC = rng.uniform(0.1, 2.0, abi.cell_shape(g))
         f = rng.standard_normal(abi.cell_shape(g))
         _check((g, bc, 1.0, -0.5, aC, b, cC, f), False)
+
+
+@pytest.mark.parametrize("case", ["projection", "darcy"])
+def test_fp64_lean3d_matches_reference_order(case):
+    """The FP64 comparison path (options.fuse_levels = 2: the mixed path's
+    lean split cycles and outer step in FP64) reaches the same FP64 solution
+    as the reference-order FP64 cycles, to 1e-10 of its scale."""
+    c = _projection(32, 25) if case == "projection" else _darcy((32, 24, 16), 26)
+    g, bc, alpha, beta, aC, b, cC, f = c
+    ul, stl, rcl = _solve(c, abi.PREC_F64, fuse_levels=2)
+    ur, str_, rcr = _solve(c, abi.PREC_F64)
+    assert rcl == 0 and rcr == 0
+    ref = O.VCOpHost(g, bc, alpha, beta, aC, b, cC)
+    r0 = O.norm(O.vc_residual(ref, np.zeros_like(f), f))
+    assert O.norm(O.vc_residual(ref, ul, f)) <= 1.01e-10 * r0
+    if case == "projection":
+        ul, ur = ul - ul.mean(), ur - ur.mean()
+    assert np.abs(ul - ur).max() <= 1e-9 * np.abs(ur).max()
