@@ -475,18 +475,22 @@ int mlgpu_hc_adjoint_solve(mlgpu_solver *S, const double *phi, const double *g, 
                            mlgpu_solve_stats *stats);
 /* The same object also solves N(phi) = rhs by Newton's method: each step
  * solves A(phi) d = rhs - N(phi) with V-cycles on A (the untransposed
- * operator, same hierarchy and block smoother) to 1e-3 relative, then
- * phi += d, halving d (at most 4 times) while the L2 norm of the FP64
- * residual grows; the
- * options' tolerance / max_iter / hang apply to the FP64 residual, and three
+ * operator, same hierarchy and block smoother) to the forcing term's
+ * relative tolerance (mlgpu_hc_newton_params: by default Eisenstat-Walker,
+ * at most 0.3), then phi = phi_old + s d with the cells that would leave
+ * their closure regime clipped past the first regime bound, s halved (at
+ * most 4 times) while the L2 norm of the FP64 residual grows; the options'
+ * tolerance / max_iter / hang apply to the FP64 residual, and three
  * consecutive steps that cut it by under 5% once it is below 1e-8 of its
  * start end the solve with the hang status (its round-off floor).  phi:
  * initial guess in, solution out.  No counterpart in the reference (whose
  * FAS smoother ignores dT/dH and converges slowly through phase change).
  * With options.precision == MLGPU_PREC_MIXED the V-cycles of each step run
- * in FP32 (J from the FP64 closure derivative, stored FP32; w = J d kept per
- * cell, wall ghosts folded into the stored diagonal blocks); the residual,
- * its norms, the step and the closure stay FP64. */
+ * in FP32 (J in FP32 in the closure's own regime; w = J d kept per cell, wall
+ * ghosts folded into the stored diagonal blocks, colour-split arrays); the
+ * residual, its norms, the step and the closure stay FP64 (the lean closure,
+ * within a few ulps of mlgpu_closure_tcl).  options.fuse_levels >= 2 in FP64
+ * runs the same lean design in FP64. */
 int mlgpu_hc_newton_solve(mlgpu_solver *S, double *phi, const double *rhs,
                           mlgpu_solve_stats *stats);
 /* Newton settings of an adjoint solver's mlgpu_hc_newton_solve.  Each step's
