@@ -412,6 +412,26 @@ int mlgpu_mac_project(mlgpu_solver *S, const mlgpu_grid *grid, const mlgpu_bc *p
 int mlgpu_hc_backward_euler(mlgpu_solver *S, double *phi_new, const double *phi_old,
                             const double *src, const double *aCoef, double dt,
                             double *rhs_scratch, mlgpu_solve_stats *stats);
+/* One TGA step of the same equations (time_integration_order = 2, the
+ * reference's LevelTGA::updateSoln at srcSubcycle/AMRLevelMushyLayer.cpp:1766-
+ * 1772; Chombo's LevelTGA is not in the reference tree, so the scheme is
+ * restated from Twizell, Gumel & Arigu 1996: a = 2 - sqrt(2) - 1e-12,
+ * mu1,2 = (a -+ sqrt(a^2 - 4a + 2)) / 2, mu3 = 1 - a):
+ *   R = a phi_old + mu3 dt L(phi_old) + dt src,
+ *   (a - mu1 dt L) psi = R,   (a - mu2 dt L) phi_new = a psi,
+ * L(phi) = -div(b grad f(phi)) the nonlinear operator as the backward-Euler
+ * step takes it (the operator with alpha = 1, beta = mu3 dt gives R's first
+ * two terms); each solve by `S` (an HC solver, alpha = 1, beta = -mu dt; psi
+ * starts from phi_old, phi_new from psi).  The source enters as dt src: the
+ * scheme's second-order source weight dt (a + mu4 dt L) src is not formed for
+ * the nonlinear operator, so the step is second order in time without a
+ * source and first order in the source's contribution.  `scratch`: two fields
+ * of phi's size.  stats: the second solve's,
+ * iterations, cycles, cell updates and launches summed over both; the status
+ * is the second solve's, or the first's when the second converged. */
+int mlgpu_hc_tga_step(mlgpu_solver *S, double *phi_new, const double *phi_old,
+                      const double *src, const double *aCoef, double dt, double *scratch,
+                      mlgpu_solve_stats *stats);
 
 /* ----------------------------------------------- device memory helpers
  * For hosts that link only libmlgpu.so (no CUDA runtime of their own, e.g.

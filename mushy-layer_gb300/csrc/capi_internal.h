@@ -35,6 +35,11 @@ cudaError_t launch_closure_full(long long n, const ClosureParams &p, const doubl
                                 double *Hl, cudaStream_t s);
 cudaError_t launch_closure_tcl(long long n, const ClosureParams &p, const double *HC, double *TCl,
                                cudaStream_t s);
+// TGA pieces: out += dt src; out = a x (a null: a == 1)
+cudaError_t launch_add_dt_src(long long n, double *out, const double *src, double dt,
+                              cudaStream_t s);
+cudaError_t launch_scale_by_a(long long n, const double *x, const double *a, double *out,
+                              cudaStream_t s);
 cudaError_t launch_closure_tcl_lean(long long n, const ClosureParams &p, const double *HC,
                                    double *TCl, cudaStream_t s);
 cudaError_t launch_face_geomean(const Geom &G, int d, const double *cell, double *face,

@@ -134,6 +134,17 @@ cudaError_t launch_closure_tcl(long long n, const ClosureParams &p, const double
   return cudaGetLastError();
 }
 
+cudaError_t launch_add_dt_src(long long n, double *out, const double *src, double dt,
+                              cudaStream_t s) {
+  add_dt_src_kernel<<<blocks_for(n), kBlock, 0, s>>>(n, out, src, dt);
+  return cudaGetLastError();
+}
+cudaError_t launch_scale_by_a(long long n, const double *x, const double *a, double *out,
+                              cudaStream_t s) {
+  scale_by_a_kernel<<<blocks_for(n), kBlock, 0, s>>>(n, x, a, out);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_closure_tcl_lean(long long n, const ClosureParams &p, const double *HC,
                                    double *TCl, cudaStream_t s) {
   closure_tcl_lean_kernel<<<blocks_for(n), kBlock, 0, s>>>(n, make_closure_lean(p), HC, TCl);

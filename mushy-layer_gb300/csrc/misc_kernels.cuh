@@ -431,6 +431,19 @@ __global__ void __launch_bounds__(kBlock) be_rhs_kernel(long long n, const doubl
     rhs[q] = v;
   }
 }
+// TGA right-hand side pieces: out = base + dt src (src may be null), and
+// out = a x (a null: a == 1)
+__global__ void __launch_bounds__(kBlock) add_dt_src_kernel(long long n, double *__restrict__ out,
+                                                            const double *__restrict__ src,
+                                                            double dt) {
+  for (long long q = gtid(); q < n; q += gstride()) out[q] = out[q] + dt * src[q];
+}
+__global__ void __launch_bounds__(kBlock) scale_by_a_kernel(long long n,
+                                                            const double *__restrict__ x,
+                                                            const double *__restrict__ a,
+                                                            double *__restrict__ out) {
+  for (long long q = gtid(); q < n; q += gstride()) out[q] = a ? x[q] * a[q] : x[q];
+}
 #endif  // MLGPU_FP64_UNIT
 
 // ------------------------------------------------------------ elementwise

@@ -2209,6 +2209,63 @@ int mlgpu_hc_backward_euler(mlgpu_solver *S, double *phi_new, const double *phi_
   return S->solve(phi_new, rhs_scratch, stats);
 }
 
+// The TGA scheme's constants (Twizell, Gumel & Arigu, "Second-order,
+// L0-stable methods for the heat equation with time-dependent boundary
+// conditions", 1996, in the form Chombo's LevelTGA drives): a = 2 - sqrt(2)
+// - eps, mu1,2 = (a -+ sqrt(a^2 - 4a + 2)) / 2, mu3 = 1 - a (the source
+// weight mu4 = 1/2 - a is not used: the source enters as dt src)
+void tga_constants(double mu[3]) {
+  const double a = 2.0 - std::sqrt(2.0) - 1e-12;
+  const double d = std::sqrt(a * a - 4.0 * a + 2.0);
+  mu[0] = 0.5 * (a - d);
+  mu[1] = 0.5 * (a + d);
+  mu[2] = 1.0 - a;
+}
+
+int mlgpu_hc_tga_step(mlgpu_solver *S, double *phi_new, const double *phi_old,
+                      const double *src, const double *aCoef, double dt, double *scratch,
+                      mlgpu_solve_stats *stats) {
+  if (!S || !phi_new || !phi_old || !scratch || !stats || !(dt > 0)) return MLGPU_ERR_ARG;
+  HCSolver *H = dynamic_cast<HCSolver *>(S);
+  if (!H) return MLGPU_ERR_ARG;
+  const long long n = 2 * H->L[0].G.ncell;
+  double mu[3];
+  tga_constants(mu);
+  double *R = scratch, *psi = scratch + n;
+  cudaGetLastError();
+  if (S->enter()) return MLGPU_ERR_CUDA;
+  // R = (a + mu3 dt L) phi_old + dt src: the operator with alpha 1, beta
+  // mu3 dt applied to phi_old (alpha a phi + beta L, L = -div(b grad f(phi));
+  // the solves below take beta -mu dt, as the backward-Euler step takes -dt)
+  mlgpu_nlop opR = H->op;
+  opR.alpha = 1.0;
+  opR.beta = mu[2] * dt;
+  CK(launch_nl_op<double>(make_nl_args<double>(opR), NL_APPLY, -1, phi_old, nullptr, R, nullptr,
+                          nullptr, nullptr, S->s));
+  if (src) CK(launch_add_dt_src(n, R, src, dt, S->s));
+  CK(cudaMemcpyAsync(psi, phi_old, sizeof(double) * n, cudaMemcpyDeviceToDevice, S->s));
+  if (S->leave()) return MLGPU_ERR_CUDA;
+  // (a - mu1 dt L) psi = R, then (a - mu2 dt L) phi_new = a psi
+  mlgpu_solve_stats st1;
+  int rc = S->set_alpha_beta(1.0, -mu[0] * dt);
+  if (rc) return rc;
+  rc = S->solve(psi, R, &st1);
+  if (rc != MLGPU_OK && rc != MLGPU_ERR_NOT_CONVERGED && rc != MLGPU_ERR_HANG) return rc;
+  if (S->enter()) return MLGPU_ERR_CUDA;
+  CK(launch_scale_by_a(n, psi, aCoef, R, S->s));
+  CK(cudaMemcpyAsync(phi_new, psi, sizeof(double) * n, cudaMemcpyDeviceToDevice, S->s));
+  if (S->leave()) return MLGPU_ERR_CUDA;
+  rc = S->set_alpha_beta(1.0, -mu[1] * dt);
+  if (rc) return rc;
+  const int rc2 = S->solve(phi_new, R, stats);
+  stats->iterations += st1.iterations;
+  stats->cycles += st1.cycles;
+  stats->cell_updates += st1.cell_updates;
+  stats->kernel_launches += st1.kernel_launches;
+  if (rc2 == MLGPU_OK) return rc;  // the first solve's status when the second converged
+  return rc2;
+}
+
 int mlgpu_hc_adjoint_workspace(const mlgpu_nlop *op, const mlgpu_mg_options *o,
                                size_t *bytes) {
   if (!valid_adjoint_op(op) || !valid_options(o) || !bytes) return MLGPU_ERR_ARG;

@@ -204,6 +204,7 @@ def _declare(lib):
         "mlgpu_solver_destroy": (i, [vp]),
         "mlgpu_mac_project": (i, [vp, P(Grid), P(BC), vp * 3, vp * 3, vp, vp, P(SolveStats)]),
         "mlgpu_hc_backward_euler": (i, [vp, vp, vp, vp, vp, d, vp, P(SolveStats)]),
+        "mlgpu_hc_tga_step": (i, [vp, vp, vp, vp, vp, d, vp, P(SolveStats)]),
         "mlgpu_closure_jacobian": (i, [P(Grid), P(Params), vp, vp, vp]),
         "mlgpu_device_alloc": (i, [sz, P(vp)]),
         "mlgpu_device_free": (i, [vp]),

@@ -362,6 +362,21 @@ class AMRFASMultiGrid(_Solver):
             abi.check(rc, "backwardEuler")
         return st, rc
 
+    def tgaStep(self, phi_new, phi_old, dt, src=None, aCoef=None):
+        """LevelTGA::updateSoln (time_integration_order = 2): two solves,
+        (a - mu1 dt L) psi = (a + mu3 dt L) phi_old + dt src and
+        (a - mu2 dt L) phi_new = a psi."""
+        scratch = torch.empty((2,) + tuple(phi_old.shape), dtype=phi_old.dtype,
+                              device=phi_old.device)
+        st = abi.SolveStats()
+        t0 = time.perf_counter()
+        rc = abi.load().mlgpu_hc_tga_step(self.h, _ptr(phi_new), _ptr(phi_old), _ptr(src),
+                                          _ptr(aCoef), float(dt), _ptr(scratch), C.byref(st))
+        _log("tgaStep", self, st, rc, t0)
+        if rc not in (abi.OK, abi.ERR_NOT_CONVERGED, abi.ERR_HANG):
+            abi.check(rc, "tgaStep")
+        return st, rc
+
 
 class AMRMultiGrid(_Solver):
     """Linear multigrid driving ProjectionOp / DarcyBrinkmanOp."""

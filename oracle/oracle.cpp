@@ -1488,6 +1488,46 @@ int orc_hc_backward_euler(const mlgpu_nlop *op, const mlgpu_mg_options *o, doubl
   return orc_hc_solve(&be, o, phi_new, rhs.data(), st);
 }
 
+// mlgpu_hc_tga_step restated (the TGA scheme of Twizell, Gumel & Arigu
+// 1996 as Chombo's LevelTGA drives it; Chombo is not in the reference tree):
+// R = (a + mu3 dt L) phi_old + dt src by the operator with alpha 1, beta
+// mu3 dt; (a - mu1 dt L) psi = R from psi = phi_old; (a - mu2 dt L) phi_new
+// = a psi from phi_new = psi.  st: the second solve's, with the iterations,
+// cycles and cell updates of both
+int orc_hc_tga_step(const mlgpu_nlop *op, const mlgpu_mg_options *o, double *phi_new,
+                    const double *phi_old, const double *src, const double *a, double dt,
+                    mlgpu_solve_stats *st) {
+  const double at = 2.0 - std::sqrt(2.0) - 1e-12;
+  const double d = std::sqrt(at * at - 4.0 * at + 2.0);
+  const double mu1 = 0.5 * (at - d), mu2 = 0.5 * (at + d), mu3 = 1.0 - at;
+  const size_t n = 2 * ncells(op->grid);
+  std::vector<double> R(n), psi(phi_old, phi_old + n);
+  mlgpu_nlop opR = *op;
+  opR.alpha = 1.0;
+  opR.beta = mu3 * dt;
+  orc_nl_apply(&opR, R.data(), phi_old);
+  if (src)
+    for (size_t q = 0; q < n; q++) R[q] = R[q] + dt * src[q];
+  mlgpu_nlop s1 = *op;
+  s1.alpha = 1.0;
+  s1.beta = -mu1 * dt;
+  mlgpu_solve_stats st1;
+  const int rc1 = orc_hc_solve(&s1, o, psi.data(), R.data(), &st1);
+  if (rc1 != MLGPU_OK && rc1 != MLGPU_ERR_NOT_CONVERGED && rc1 != MLGPU_ERR_HANG) return rc1;
+  for (size_t q = 0; q < n; q++) {
+    R[q] = a ? psi[q] * a[q] : psi[q];
+    phi_new[q] = psi[q];
+  }
+  mlgpu_nlop s2 = *op;
+  s2.alpha = 1.0;
+  s2.beta = -mu2 * dt;
+  const int rc2 = orc_hc_solve(&s2, o, phi_new, R.data(), st);
+  st->iterations += st1.iterations;
+  st->cycles += st1.cycles;
+  st->cell_updates += st1.cell_updates;
+  return rc2 == MLGPU_OK ? rc1 : rc2;
+}
+
 int orc_vc_solve(const mlgpu_vcop *op, const mlgpu_mg_options *o, double *phi,
                  const double *rhs, mlgpu_solve_stats *st) {
   VCSolver S;

@@ -76,6 +76,8 @@ def lib():
                                     vp, P(abi.SolveStats)]),
             "orc_hc_backward_euler": (i, [P(abi.NLOp), P(abi.MGOptions), vp, vp, vp, vp, d,
                                           P(abi.SolveStats)]),
+            "orc_hc_tga_step": (i, [P(abi.NLOp), P(abi.MGOptions), vp, vp, vp, vp, d,
+                                          P(abi.SolveStats)]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -338,6 +340,15 @@ def mac_project(o, opts, phi_bc, u, pi, phi):
                                _faces3(u + [None] * (3 - len(u))),
                                _faces3(list(pi) + [None] * (3 - len(pi))), _p(phi), C.byref(st))
     return u, phi, st, rc
+
+
+def hc_tga_step(o, opts, phi_new, phi_old, dt, src=None, a=None):
+    """mlgpu_hc_tga_step restated: the TGA step by two FAS solves."""
+    phi_new = phi_new.copy()
+    st = abi.SolveStats()
+    rc = lib().orc_hc_tga_step(C.byref(o.op), C.byref(opts), _p(phi_new), _p(phi_old),
+                               _p(src), _p(a), float(dt), C.byref(st))
+    return phi_new, st, rc
 
 
 def hc_backward_euler(o, opts, phi_new, phi_old, dt, src=None, a=None):

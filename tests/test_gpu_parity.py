@@ -663,6 +663,38 @@ def test_backward_euler_steps_bitwise():
         h_phi, d_phi = new_ref, d_new
 
 
+@pytest.mark.parametrize("n", [(32, 32), (16, 16, 8)])
+def test_tga_steps_bitwise(n):
+    """mlgpu_hc_tga_step against the oracle's TGA step: the right-hand side
+    (a + mu3 dt L) phi_old + dt src and both FAS solves, with a source, an a
+    coefficient and mixed walls, three steps through phase change."""
+    from mushy_gb300 import ops
+    dt = 1e-3
+    g = P.grid(n)
+    p = P.mushy_params()
+    phi_bc, der = P.hc_bcs("mixed")
+    rng = np.random.default_rng(42)
+    phi = P.hc_state(g, rng, regimes=False)
+    phi[0] = rng.uniform(4.4, 5.6, phi[0].shape)
+    b = [np.stack([-np.ones(abi.face_shape(g, d)), -0.02 * np.ones(abi.face_shape(g, d))])
+         for d in range(g.dim)]
+    aC = rng.uniform(0.8, 1.2, phi.shape)
+    src = 0.1 * rng.standard_normal(phi.shape)
+    ref = O.NLOpHost(g, p, phi_bc, der, 1.0, 1.0, aC, b)
+    opts = O.default_options(1)
+    op = ops.NLMultiCompOp(g, p, phi_bc, der, 1.0, 1.0, dev(aC), [dev(x) for x in b])
+    S = ops.AMRFASMultiGrid(op, ops.default_options(True))
+    h_phi, d_phi = phi.copy(), dev(phi)
+    d_src, d_a = dev(src), dev(aC)
+    for step in range(3):
+        new_ref, st_ref, rc_ref = O.hc_tga_step(ref, opts, h_phi, h_phi, dt, src, aC)
+        d_new = d_phi.clone()
+        st, rc = S.tgaStep(d_new, d_phi, dt, src=d_src, aCoef=d_a)
+        assert rc == rc_ref and st.iterations == st_ref.iterations
+        exact(host(d_new), new_ref)
+        h_phi, d_phi = new_ref, d_new
+
+
 # ----------------------------------- nonlinear temperature conditions on H
 def nl_setup_temperature(n, per, seed, method, limit):
     from mushy_gb300 import ops
