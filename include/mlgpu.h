@@ -56,6 +56,18 @@ enum {
   MLGPU_BC_TEMPERATURE_FLUX = 3,          /* value = F (a = 1, b = 0) */
   MLGPU_BC_TEMPERATURE_FLUX_RADIATION = 4 /* value = F, a, b, T_ref from mlgpu_nlbc */
 };
+/* PhysBCUtil::MixedBCTemperatureSalinity (BCutil/PhysBCUtil.cpp:764-800) on
+ * the derived (T, C_l) state: a linear Robin ghost temperature
+ *   T_g = (T_i (a/dx + b/2) + F - b T_ref) / (a/dx - b/2),
+ * value = F, a, b, T_ref from mlgpu_nlbc's [dir][side] entries and dx its
+ * spacing (0: the grid's), the same constants as the radiation condition.
+ * Only derived_bc comp 0 (T) may use it; C_l's ghost follows comp 1's own
+ * type (the reference writes a zero-gradient C_l ghost, which comp 1's
+ * condition then overwrites).  a/dx - b/2 must be nonzero.  In linearised
+ * (Newton, adjoint) use the ghost's derivative (a/dx + b/2) / (a/dx - b/2)
+ * multiplies the interior value, and the boundary-value gradient is taken
+ * with respect to F. */
+enum { MLGPU_BC_MIXED_TEMPERATURE_SALINITY = 5 };
 enum { MLGPU_NLBC_PICARD = 0, MLGPU_NLBC_NEWTON = 1 };
 enum { MLGPU_RELAX_GSRB = 1, MLGPU_RELAX_JACOBI = 4 };     /* reference s_relaxMode */
 enum { MLGPU_PROLONG_CONSTANT = 0, MLGPU_PROLONG_LINEAR = 1 };

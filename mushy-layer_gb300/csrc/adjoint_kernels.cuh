@@ -30,7 +30,8 @@ template <class T>
 struct AdjArgs {
   Geom G;
   ClosureParams cp;
-  BCD phi_bc, dbc;
+  BCD phi_bc;
+  DBCD dbc;  // the derived (T, C_l) conditions
   int apply_dbc;
   T alpha, beta, dxinv, dx;
   const T *a;           // [2][cells] or null (a == 1)
@@ -106,7 +107,7 @@ __device__ __forceinline__ void adj_cell(const AdjArgs<T> &A, const T *y, int i,
         } else if (A.apply_dbc) {
           const T yn = ghost_value<T>(A.dbc, d, side, c, y0[c], A.dx, true);
           t = side ? bf * (yn - y0[c]) : bf * (y0[c] - yn);
-          dp = A.dbc.type[d][side][c] == MLGPU_BC_DIRICHLET ? T(2) * bf : T(0);
+          dp = dbc_wall_diag<T>(A.dbc, d, side, c, bf);
         } else {
           t = side ? bf * (T(0) - y0[c]) : bf * (y0[c] - T(0));
           dp = bf;
@@ -222,7 +223,7 @@ __device__ __forceinline__ void lin_cell(const AdjArgs<T> &A, const T *x, int i,
           dp = self ? T(0) : bf;
         } else if (A.apply_dbc) {
           gn = ghost_value<T>(A.dbc, d, side, c, g0[c], A.dx, true);
-          dp = A.dbc.type[d][side][c] == MLGPU_BC_DIRICHLET ? T(2) * bf : T(0);
+          dp = dbc_wall_diag<T>(A.dbc, d, side, c, bf);
         } else {
           double Jg[4];
           adj_ghost_jac(A, q, d, side, Jg);
@@ -569,7 +570,11 @@ __global__ void __launch_bounds__(kBlock) adj_bc_grad_kernel(AdjArgs<T> A,
     for (int c = 0; c < 2; c++) {
       double v = 0.0;
       if (d < DIM && !G.per(d)) {
-        const double df = bc.type[d][side][c] == MLGPU_BC_DIRICHLET ? 2.0 : isign * (double)A.dx;
+        // d(ghost)/d(value): 2 Dirichlet, +-dx Neumann, 1 / p2 mixed
+        const double df = bc.type[d][side][c] == MLGPU_BC_DIRICHLET ? 2.0
+                          : (A.apply_dbc && bc.type[d][side][c] == MLGPU_BC_MIXED_TEMPERATURE_SALINITY)
+                              ? A.dbc.rob[d][side][4]
+                              : isign * (double)A.dx;
         v = (double)A.beta * (double)A.dxinv * df * (c == 0 ? s0 : s1);
       }
       out[blockIdx.x * 2 + c] = v;

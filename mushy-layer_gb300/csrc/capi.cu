@@ -29,7 +29,7 @@ NLArgs<T> make_nl_args(const mlgpu_nlop &op) {
   A.G = make_geom(op.grid);
   A.cp = make_cp(op.params);
   A.phi_bc = make_bcd(op.phi_bc);
-  A.dbc = make_bcd(op.derived_bc);
+  A.dbc = make_dbcd(op.derived_bc, op.nlbc, op.grid.dx);
   A.nlbc = make_nlbcd(op.phi_bc, op.nlbc, op.grid.dx);
   A.apply_dbc = op.apply_derived_bc;
   double dxinv = 1.0 / (op.grid.dx * op.grid.dx);
@@ -79,19 +79,35 @@ bool valid_bc(const mlgpu_bc &b, int dim, bool temperature_h) {
   return true;
 }
 
+// derived conditions: Neumann/Dirichlet, and the mixed temperature condition
+// on comp 0 (T) only
+static bool valid_derived_bc(const mlgpu_bc &b, int dim) {
+  for (int d = 0; d < dim; d++)
+    for (int s = 0; s < 2; s++)
+      for (int c = 0; c < 2; c++) {
+        const int t = b.type[d][s][c];
+        if (t == MLGPU_BC_NEUMANN || t == MLGPU_BC_DIRICHLET) continue;
+        if (c == 0 && t == MLGPU_BC_MIXED_TEMPERATURE_SALINITY) continue;
+        return false;
+      }
+  return true;
+}
+
 bool valid_nl_bcs(const mlgpu_nlop &op) {
-  if (!valid_bc(op.phi_bc, op.grid.dim, true) || !valid_bc(op.derived_bc, op.grid.dim, false))
+  if (!valid_bc(op.phi_bc, op.grid.dim, true) || !valid_derived_bc(op.derived_bc, op.grid.dim))
     return false;
   const mlgpu_nlbc &n = op.nlbc;
   if (n.method != MLGPU_NLBC_PICARD && n.method != MLGPU_NLBC_NEWTON) return false;
   if (n.max_iter < 0 || !(n.dx >= 0)) return false;
   // a Robin denominator a/dx - b/2 of zero has no ghost value
+  const double dxb = n.dx > 0 ? n.dx : op.grid.dx;
   for (int d = 0; d < op.grid.dim; d++)
-    for (int s = 0; s < 2; s++)
-      if (op.phi_bc.type[d][s][0] == MLGPU_BC_TEMPERATURE_FLUX_RADIATION) {
-        const double dxb = n.dx > 0 ? n.dx : op.grid.dx;
-        if (!(n.a[d][s] / dxb - n.b[d][s] / 2 != 0)) return false;
-      }
+    for (int s = 0; s < 2; s++) {
+      const bool robin_h = op.phi_bc.type[d][s][0] == MLGPU_BC_TEMPERATURE_FLUX_RADIATION;
+      const bool robin_t = op.apply_derived_bc &&
+                           op.derived_bc.type[d][s][0] == MLGPU_BC_MIXED_TEMPERATURE_SALINITY;
+      if ((robin_h || robin_t) && !(n.a[d][s] / dxb - n.b[d][s] / 2 != 0)) return false;
+    }
   return true;
 }
 

@@ -88,6 +88,59 @@ __device__ __forceinline__ T ghost_value(const BCD &bc, int d, int s, int c, T i
   return interior + (isign * dx) * v;
 }
 
+// The derived-variable (T, C_l) conditions: BCD plus, per [dir][side], the
+// constants of the MixedBCTemperatureSalinity ghost on T
+// (BCutil/PhysBCUtil.cpp:764-800): p1 = a/dx + b/2, bt = b T_ref,
+// p2 = a/dx - b/2, the derivative g = p1 / p2 of the ghost with respect to the
+// interior value, and f = 1 / p2 with respect to F (the value)
+struct DBCD : BCD {
+  double rob[3][2][5];  // p1, bt, p2, g, f
+};
+
+inline DBCD make_dbcd(const mlgpu_bc &b, const mlgpu_nlbc &nb, double grid_dx) {
+  DBCD r;
+  static_cast<BCD &>(r) = make_bcd(b);
+  const double dx = nb.dx > 0 ? nb.dx : grid_dx;
+  for (int d = 0; d < 3; d++)
+    for (int s = 0; s < 2; s++) {
+      double *o = r.rob[d][s];
+      o[0] = o[1] = o[2] = o[3] = o[4] = 0.0;
+      if (b.type[d][s][0] != MLGPU_BC_MIXED_TEMPERATURE_SALINITY) continue;
+      const double a = nb.a[d][s], bb = nb.b[d][s];
+      o[0] = a / dx + bb / 2;
+      o[1] = bb * nb.T_ref[d][s];
+      o[2] = a / dx - bb / 2;
+      o[3] = o[0] / o[2];
+      o[4] = 1.0 / o[2];
+    }
+  return r;
+}
+
+// Derived-variable ghost: the mixed temperature condition on comp 0, else
+// ghost_value.  Inhomogeneous: (T_i p1 + F - bt) / p2 in the reference's
+// order; homogeneous (the linearised operators): g T_i.
+template <class T>
+__device__ __forceinline__ T ghost_value(const DBCD &bc, int d, int s, int c, T interior,
+                                         T dx, bool homogeneous) {
+  if (bc.type[d][s][c] == MLGPU_BC_MIXED_TEMPERATURE_SALINITY) {
+    const double *r = bc.rob[d][s];
+    if (homogeneous) return T(r[3]) * interior;
+    return (interior * T(r[0]) + T(bc.val[d][s][c]) - T(r[1])) / T(r[2]);
+  }
+  return ghost_value<T>(static_cast<const BCD &>(bc), d, s, c, interior, dx, homogeneous);
+}
+
+// A derived-condition wall's share of the diagonal face sum: the ghost's
+// homogeneous rule g T_i makes the face term b (g - 1) T_i, so the wall adds
+// (1 - g) b: 2b Dirichlet, 0 Neumann, (1 - g) b mixed
+template <class T>
+__device__ __forceinline__ T dbc_wall_diag(const DBCD &bc, int d, int s, int c, T bf) {
+  const int t = bc.type[d][s][c];
+  if (t == MLGPU_BC_DIRICHLET) return T(2) * bf;
+  if (t == MLGPU_BC_MIXED_TEMPERATURE_SALINITY) return T(1.0 - bc.rob[d][s][3]) * bf;
+  return T(0);
+}
+
 // ------------------------------------------------------------ closure (FP64)
 struct ClosureParams {
   double CR, k, cp, St, te, Te;
@@ -220,11 +273,30 @@ inline ClosureLean make_closure_lean(const ClosureParams &p) {
   return L;
 }
 
-// sqrt(D) for D well inside FP32's normal range (else the library square root)
+// 0 < x < inf with 2^-99 <= x < 2^99, decided on the sign and exponent bits
+// (integer pipe): the range where FP32 seeds are normal and the FP64
+// refinements below neither overflow nor underflow
+__device__ __forceinline__ bool lean_pos_range(double x) {
+  const unsigned se = (unsigned)((unsigned long long)__double_as_longlong(x) >> 52);
+  return se - 924u < 198u;  // sign 0, biased exponent in [1023 - 99, 1023 + 99)
+}
+// the same for |x|
+__device__ __forceinline__ bool lean_abs_range(double x) {
+  const unsigned e = (unsigned)((unsigned long long)__double_as_longlong(x) >> 52) & 0x7ffu;
+  return e - 924u < 198u;
+}
+// |x| < 2^830 (about 7e249) and x not NaN, on the exponent bits
+__device__ __forceinline__ bool lean_below_2p830(double x) {
+  const unsigned e = (unsigned)((unsigned long long)__double_as_longlong(x) >> 52) & 0x7ffu;
+  return e < 1853u;
+}
+
+// sqrt(D) for D well inside FP32's normal range (else the library square
+// root); the FP32 seed's conversions on the integer pipe
 __device__ __forceinline__ double lean_sqrt(double D) {
-  if (!(D > 1e-30 && D < 1e30)) return sqrt(D);
-  const double y = (double)rsqrtf((float)D);  // 1/sqrt(D) to ~2^-22
-  double g = D * y, h = 0.5 * y;              // sqrt(D), 1/(2 sqrt(D))
+  if (!lean_pos_range(D)) return sqrt(D);
+  const double y = f64_exact(rsqrtf(f32_trunc(D)));  // 1/sqrt(D) to ~2^-22
+  double g = D * y, h = 0.5 * y;                      // sqrt(D), 1/(2 sqrt(D))
   const double r = fma(-g, h, 0.5);
   g = fma(g, r, g);
   h = fma(h, r, h);
@@ -235,10 +307,9 @@ __device__ __forceinline__ double lean_sqrt(double D) {
 // num / den for |den| well inside FP32's normal range and a finite quotient
 // (else the library division)
 __device__ __forceinline__ double lean_div(double num, double den) {
-  const double ad = fabs(den);
-  if (!(ad > 1e-30 && ad < 1e30 && fabs(num) < 1e250)) return num / den;
-  double y = (double)__frcp_rn((float)den);  // 1/den to 2^-24
-  y = fma(fma(-den, y, 1.0), y, y);           // to ~2^-48
+  if (!(lean_abs_range(den) && lean_below_2p830(num))) return num / den;
+  double y = f64_exact(__frcp_rn(f32_trunc(den)));  // 1/den to ~2^-23
+  y = fma(fma(-den, y, 1.0), y, y);                  // to ~2^-46
   const double q = num * y;
   return fma(fma(-den, q, num), y, q);
 }

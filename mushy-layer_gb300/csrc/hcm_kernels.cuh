@@ -21,7 +21,8 @@ namespace mlgpu {
 
 struct HCMArgs {
   Geom G;
-  BCD phi_bc, dbc;
+  BCD phi_bc;
+  DBCD dbc;  // the derived (T, C_l) conditions
   int apply_dbc;
   float alpha, beta, dxinv;
   const float *a;     // [2][cells] or null (a == 1)
@@ -33,6 +34,12 @@ struct HCMArgs {
 #ifdef MLGPU_FP32_UNIT  // kernels compiled in launch_f32.cu only
 __device__ __forceinline__ float hcm_bsign(const BCD &bc, int d, int s, int c) {
   return bc.type[d][s][c] == MLGPU_BC_DIRICHLET ? -1.0f : 1.0f;
+}
+// the derived conditions' homogeneous rule: also the mixed temperature
+// condition's factor g
+__device__ __forceinline__ float hcm_bsign(const DBCD &bc, int d, int s, int c) {
+  if (bc.type[d][s][c] == MLGPU_BC_MIXED_TEMPERATURE_SALINITY) return (float)bc.rob[d][s][3];
+  return hcm_bsign(static_cast<const BCD &>(bc), d, s, c);
 }
 
 // J e at cell q

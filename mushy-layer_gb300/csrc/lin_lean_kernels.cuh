@@ -515,7 +515,7 @@ __device__ __forceinline__ void lean_face_sums(const AdjArgs<T> &A, int i, int j
         else if (G.per(d))
           dp = m == 1 ? T(0) : bf;
         else if (A.apply_dbc)
-          dp = A.dbc.type[d][side][c] == MLGPU_BC_DIRICHLET ? T(2) * bf : T(0);
+          dp = dbc_wall_diag<T>(A.dbc, d, side, c, bf);
         else
           dp = bf;
         p = p + dp;

@@ -20,7 +20,8 @@ template <class T>
 struct NLArgs {
   Geom G;
   ClosureParams cp;
-  BCD phi_bc, dbc;
+  BCD phi_bc;
+  DBCD dbc;  // the derived (T, C_l) conditions
   NLBCD nlbc;       // temperature conditions on H (phi_bc comp 0 types 2-4)
   int apply_dbc;
   T alpha, beta, dxinv, dx;

@@ -2284,6 +2284,8 @@ int mlgpu_hc_adjoint_create(const mlgpu_nlop *op, const mlgpu_mg_options *o, voi
   if (((uintptr_t)ws) & 255) return MLGPU_ERR_WORKSPACE;
   HCAdjSolver *S = new HCAdjSolver;
   S->op = *op;
+  // the mixed temperature condition keeps the finest spacing on every level
+  if (!(S->op.nlbc.dx > 0)) S->op.nlbc.dx = op->grid.dx;
   S->o = *o;
   cudaGetLastError();
   if (S->init_streams((cudaStream_t)stream)) {

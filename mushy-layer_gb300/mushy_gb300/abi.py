@@ -23,6 +23,7 @@ ERR_SCRATCH = 7
 F64, F32 = 0, 1
 BC_NEUMANN, BC_DIRICHLET = 0, 1
 BC_FIXED_TEMPERATURE, BC_TEMPERATURE_FLUX, BC_TEMPERATURE_FLUX_RADIATION = 2, 3, 4
+BC_MIXED_TEMPERATURE_SALINITY = 5  # derived_bc comp 0 only
 NLBC_PICARD, NLBC_NEWTON = 0, 1
 RELAX_GSRB, RELAX_JACOBI = 1, 4
 PROLONG_CONSTANT, PROLONG_LINEAR = 0, 1

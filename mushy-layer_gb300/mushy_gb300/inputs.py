@@ -359,17 +359,23 @@ class Inputs:
                         der[(d, s, c)] = (abi.BC_DIRICHLET, V[var + lab][d])
                     elif t == NEUMANN:
                         der[(d, s, c)] = (abi.BC_NEUMANN, 0.0)
+                    elif t == MIXED_T_S and c == 0:
+                        # the Robin ghost on T with the radiation constants
+                        # bc.a / bc.b / bc.TRef and the value as its flux
+                        der[(d, s, c)] = (abi.BC_MIXED_TEMPERATURE_SALINITY,
+                                          V[var + lab][d])
                     elif t == MIXED_T_S:
                         raise ValueError(
-                            "bc type 9 (MixedBCTemperatureSalinity, a linear Robin ghost "
-                            "on the diagnostic temperature) of %s on side %s of direction "
-                            "%d is not on this path: give the enthalpy the same condition "
-                            "as TemperatureFluxRadiation (type 8) with "
-                            "main.apply_diagnostic_bcs = false" % (var, lab, d))
+                            "bc type 9 (MixedBCTemperatureSalinity) of liquidConcentration "
+                            "on side %s of direction %d is not on this path: the reference "
+                            "then recomputes the temperature ghost with the liquid "
+                            "concentration's value as the flux; give it to the temperature"
+                            % (lab, d))
                     else:
                         raise ValueError(
                             "bc type %d of %s on side %s of direction %d is not on this "
-                            "path (Dirichlet or Neumann diagnostic conditions only)"
+                            "path (Dirichlet or Neumann diagnostic conditions, and the mixed "
+                            "temperature condition on the temperature)"
                             % (t, var, lab, d))
         a, b = self._bc_info("a", dim), self._bc_info("b", dim)
         tref, lim = self._bc_info("TRef", dim), self._bc_info("NoFluxLimit", dim)

@@ -134,9 +134,31 @@ void exchange(Fab &f, const mlgpu_grid &gr) {
   }
 }
 
+// MixedBCTemperatureSalinity on the derived T (BCutil/PhysBCUtil.cpp:764-800):
+// T_g = (T_i (a/m_dx + b/2) + F - b T_ref) / (a/m_dx - b/2), the radiation
+// constants a, b, T_ref of [dir][side] and the condition's spacing m_dx.
+// p1 = a/dx + b/2, bt = b T_ref, p2 = a/dx - b/2; g = p1 / p2 is the ghost's
+// derivative in the interior value, f = 1 / p2 in F.
+struct MixedT {
+  double p1, bt, p2, g, f;
+};
+MixedT mixed_t(const mlgpu_nlbc &nb, double grid_dx, int d, int side) {
+  const double dx = nb.dx > 0 ? nb.dx : grid_dx;
+  MixedT m;
+  m.p1 = nb.a[d][side] / dx + nb.b[d][side] / 2;
+  m.bt = nb.b[d][side] * nb.T_ref[d][side];
+  m.p2 = nb.a[d][side] / dx - nb.b[d][side] / 2;
+  m.g = m.p1 / m.p2;
+  m.f = 1.0 / m.p2;
+  return m;
+}
+
 // DIRIBC order 1 (BCutil/BCFuncF.ChF:14-57) and NEUMBC (:63-95) on the ghost
-// row adjacent to the valid box (adjCellBox, BCFunctions.cpp:101-161).
-void physbc(Fab &f, const mlgpu_grid &gr, const mlgpu_bc &bc, bool homogeneous) {
+// row adjacent to the valid box (adjCellBox, BCFunctions.cpp:101-161); with
+// `nb`, the derived state's mixed temperature condition on comp 0 (its
+// homogeneous form g T_i is the linearised rule).
+void physbc(Fab &f, const mlgpu_grid &gr, const mlgpu_bc &bc, bool homogeneous,
+            const mlgpu_nlbc *nb = nullptr) {
   for (int d = 0; d < gr.dim; d++) {
     if (gr.periodic[d]) continue;
     for (int side = 0; side < 2; side++) {
@@ -144,6 +166,8 @@ void physbc(Fab &f, const mlgpu_grid &gr, const mlgpu_bc &bc, bool homogeneous) 
       for (int c = 0; c < f.nc; c++) {
         int type = bc.type[d][side][c];
         double val = homogeneous ? 0.0 : bc.value[d][side][c];
+        const bool mixed = nb && c == 0 && type == MLGPU_BC_MIXED_TEMPERATURE_SALINITY;
+        const MixedT mt = mixed ? mixed_t(*nb, gr.dx, d, side) : MixedT{0, 0, 0, 0, 0};
         int lo[3] = {0, 0, 0}, hi[3] = {f.n[0] - 1, f.n[1] - 1, f.n[2] - 1};
         lo[d] = hi[d] = (side == 0) ? -1 : f.n[d];
         for (int k = lo[2]; k <= hi[2]; k++)
@@ -152,7 +176,9 @@ void physbc(Fab &f, const mlgpu_grid &gr, const mlgpu_bc &bc, bool homogeneous) 
               int t[3] = {i, j, k};
               t[d] -= isign;
               double phi1 = f(t[0], t[1], t[2], c);
-              if (type == MLGPU_BC_DIRICHLET)
+              if (mixed)
+                f(i, j, k, c) = homogeneous ? mt.g * phi1 : (phi1 * mt.p1 + val - mt.bt) / mt.p2;
+              else if (type == MLGPU_BC_DIRICHLET)
                 f(i, j, k, c) = 2 * val - phi1;
               else
                 f(i, j, k, c) = phi1 + (isign * gr.dx) * val;
@@ -160,6 +186,17 @@ void physbc(Fab &f, const mlgpu_grid &gr, const mlgpu_bc &bc, bool homogeneous) 
       }
     }
   }
+}
+
+// a derived-condition wall's share of the diagonal face sum (the ghost's
+// homogeneous rule g T_i gives the face term b (g - 1) T_i): 2b Dirichlet,
+// 0 Neumann, (1 - g) b for the mixed temperature condition
+double dbc_wall_diag(const mlgpu_nlop &op, int d, int side, int c, double bf) {
+  const int t = op.derived_bc.type[d][side][c];
+  if (t == MLGPU_BC_DIRICHLET) return 2 * bf;
+  if (t == MLGPU_BC_MIXED_TEMPERATURE_SALINITY && c == 0)
+    return (1.0 - mixed_t(op.nlbc, op.grid.dx, d, side).g) * bf;
+  return 0.0;
 }
 
 void fill_ghosts(Fab &f, const mlgpu_grid &gr, const mlgpu_bc &bc, bool homogeneous) {
@@ -480,7 +517,7 @@ void diffused_var(Fab &out, const Fab &phi, const mlgpu_nlop &op) {
         out(i, j, k, 0) = T;
         out(i, j, k, 1) = Cl;
       }
-  if (op.apply_derived_bc) physbc(out, op.grid, op.derived_bc, false);
+  if (op.apply_derived_bc) physbc(out, op.grid, op.derived_bc, false, &op.nlbc);
 }
 
 // --------------------------------------------------- face coefficients
@@ -1595,7 +1632,7 @@ struct AdjCtx {
 void adj_fill(Fab &y, const mlgpu_nlop &op) {
   exchange(y, op.grid);
   if (op.apply_derived_bc) {
-    physbc(y, op.grid, op.derived_bc, true);
+    physbc(y, op.grid, op.derived_bc, true, &op.nlbc);
     return;
   }
   for (int d = 0; d < op.grid.dim; d++) {
@@ -1678,7 +1715,7 @@ void adj_row(const AdjCtx &X, const Fab &y, int i, int j, int k, double out[2], 
         else if (g.periodic[d])
           dp = g.n[d] == 1 ? 0.0 : bf;
         else if (X.op.apply_derived_bc)
-          dp = X.op.derived_bc.type[d][side][c] == MLGPU_BC_DIRICHLET ? 2 * bf : 0.0;
+          dp = dbc_wall_diag(X.op, d, side, c, bf);
         else {
           dp = bf;
           any_phi = true;
@@ -1796,7 +1833,7 @@ void lin_apply(const AdjCtx &X, const double *xd, double *out) {
       }
   exchange(jx, g);
   if (op.apply_derived_bc) {
-    physbc(jx, g, op.derived_bc, true);
+    physbc(jx, g, op.derived_bc, true, &op.nlbc);
   } else {
     for (int d = 0; d < g.dim; d++) {
       if (g.periodic[d]) continue;
@@ -1871,7 +1908,7 @@ void lin_gsrb_pass(const AdjCtx &X, double *xd, const double *r, int pass,
               else if (g.periodic[d])
                 dp = g.n[d] == 1 ? 0.0 : bf;
               else if (op.apply_derived_bc)
-                dp = op.derived_bc.type[d][side][c] == MLGPU_BC_DIRICHLET ? 2 * bf : 0.0;
+                dp = dbc_wall_diag(op, d, side, c, bf);
               else {
                 double Jg[4];
                 ghost_jac(X, q, d, side, Jg);
@@ -2162,6 +2199,7 @@ int orc_hc_adjoint_solve(const mlgpu_nlop *op, const mlgpu_mg_options *o, const 
                          const double *g, double *y, mlgpu_solve_stats *st) {
   AdjSolver S;
   S.op0 = *op;
+  if (!(S.op0.nlbc.dx > 0)) S.op0.nlbc.dx = op->grid.dx;
   S.o = *o;
   S.build(phi);
   memset(st, 0, sizeof(*st));
@@ -2221,6 +2259,8 @@ int orc_hc_adjoint_bc_gradient(const mlgpu_nlop *op, const double *phi, const do
           }
       for (int c = 0; c < 2; c++) {
         double df = bc.type[d][side][c] == MLGPU_BC_DIRICHLET ? 2.0 : (side ? 1.0 : -1.0) * g.dx;
+        if (op->apply_derived_bc && bc.type[d][side][c] == MLGPU_BC_MIXED_TEMPERATURE_SALINITY)
+          df = mixed_t(op->nlbc, g.dx, d, side).f;
         grad[(d * 2 + side) * 2 + c] = op->beta * X.dxinv * df * acc[c];
       }
     }
@@ -2374,6 +2414,7 @@ extern "C" int orc_hc_newton_solve(const mlgpu_nlop *op, const mlgpu_mg_options 
                                    const double *rhs, mlgpu_solve_stats *st) {
   AdjSolver S;
   S.op0 = *op;
+  if (!(S.op0.nlbc.dx > 0)) S.op0.nlbc.dx = op->grid.dx;
   S.o = *o;
   S.tr = false;
   S.build(phi);

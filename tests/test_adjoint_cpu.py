@@ -17,11 +17,20 @@ from mushy_gb300 import abi
 from oracle import oracle as O
 
 
-def _op(n, per, seed, dbc=True, mush=False, alpha=1.0, beta=-2e-3):
+# the mixed temperature condition on the derived T (a, b, T_ref per side)
+ROBIN = {(1, 1): (0.5, -1.0, 4.0), (0, 0): (1.0, 2.0, -0.5)}
+
+
+def _op(n, per, seed, dbc=True, mush=False, alpha=1.0, beta=-2e-3, robin=False):
     rng = np.random.default_rng(seed)
     g = P.grid(n, per)
     p = P.mushy_params()
     phi_bc, der = P.hc_bcs("mixed")
+    nl = None
+    if robin:
+        nl = abi.make_nlbc(radiation=ROBIN)
+        for (d, s) in ROBIN:
+            der.type[d][s][0] = abi.BC_MIXED_TEMPERATURE_SALINITY
     if not dbc:
         phi_bc = abi.make_bc({(0, 0, 0): (abi.BC_DIRICHLET, 6.2), (0, 1, 1): (abi.BC_NEUMANN, 0.3),
                               (1, 0, 0): (abi.BC_NEUMANN, -0.4), (1, 1, 1): (abi.BC_DIRICHLET, -1.1),
@@ -31,13 +40,32 @@ def _op(n, per, seed, dbc=True, mush=False, alpha=1.0, beta=-2e-3):
         phi[0] = rng.uniform(4.4, 5.6, phi[0].shape)
     b = P.faces(g, rng, 2)
     aC = rng.uniform(0.5, 1.5, phi.shape)
-    o = O.NLOpHost(g, p, phi_bc, der, alpha, beta, aC, b, apply_derived_bc=int(dbc))
+    o = O.NLOpHost(g, p, phi_bc, der, alpha, beta, aC, b, apply_derived_bc=int(dbc), nlbc=nl)
     J = O.closure_jac(g, p, phi)
     return g, o, phi, J, rng
 
 
 CASES = [((10, 8), (0, 0, 0), True), ((10, 8), (0, 0, 0), False), ((12, 6), (1, 0, 0), True),
          ((6, 4, 4), (0, 0, 0), True), ((6, 4, 4), (0, 1, 0), False)]
+
+
+ROBIN_CASES = [((10, 8), (0, 0, 0)), ((12, 6), (0, 0, 0)), ((6, 4, 4), (0, 0, 1))]
+
+
+@pytest.mark.parametrize("n,per", ROBIN_CASES)
+def test_mixed_temperature_condition_linearization_and_transpose(n, per):
+    """The derived mixed temperature condition (linear Robin ghost on T):
+    A x against central differences of N, and A^T the transpose of A."""
+    g, o, phi, J, rng = _op(n, per, 13, True, True, robin=True)
+    x = rng.standard_normal(phi.shape)
+    Ax = O.linearized_apply(o, phi, J, x)
+    h = 1e-6
+    fd = (O.nl_apply(o, phi + h * x) - O.nl_apply(o, phi - h * x)) / (2 * h)
+    assert np.abs(Ax - fd).max() <= 1e-6 * np.abs(fd).max()
+    y = rng.standard_normal(phi.shape)
+    lhs = float((Ax * y).sum())
+    rhs = float((x * O.adjoint_apply(o, phi, J, y)).sum())
+    assert abs(lhs - rhs) <= 1e-12 * max(abs(lhs), 1.0)
 
 
 @pytest.mark.parametrize("n,per,dbc", CASES)
@@ -77,10 +105,13 @@ def _dense_adjoint(o, phi, J):
     return A_T
 
 
-@pytest.mark.parametrize("n,per,dbc", [((8, 8), (0, 0, 0), True), ((8, 8), (0, 0, 0), False),
-                                       ((8, 4), (1, 0, 0), True), ((4, 4, 4), (0, 0, 1), True)])
-def test_adjoint_solve_matches_dense_solve(n, per, dbc):
-    g, o, phi, J, rng = _op(n, per, 5, dbc, alpha=1.0, beta=-1e-2)
+@pytest.mark.parametrize("n,per,dbc,robin", [((8, 8), (0, 0, 0), True, False),
+                                             ((8, 8), (0, 0, 0), False, False),
+                                             ((8, 4), (1, 0, 0), True, False),
+                                             ((4, 4, 4), (0, 0, 1), True, False),
+                                             ((8, 8), (0, 0, 0), True, True)])
+def test_adjoint_solve_matches_dense_solve(n, per, dbc, robin):
+    g, o, phi, J, rng = _op(n, per, 5, dbc, alpha=1.0, beta=-1e-2, robin=robin)
     A_T = _dense_adjoint(o, phi, J)
     gg = rng.standard_normal(phi.shape)
     ref = np.linalg.solve(A_T, gg.ravel()).reshape(phi.shape)
@@ -94,9 +125,9 @@ def test_adjoint_solve_matches_dense_solve(n, per, dbc):
     assert np.abs(y2 - y).max() <= 1e-9 * np.abs(y).max()
 
 
-@pytest.mark.parametrize("dbc", [True, False])
-def test_bc_gradient_matches_finite_differences(dbc):
-    g, o, phi, J, rng = _op((10, 8), (0, 0, 0), 6, dbc)
+@pytest.mark.parametrize("dbc,robin", [(True, False), (False, False), (True, True)])
+def test_bc_gradient_matches_finite_differences(dbc, robin):
+    g, o, phi, J, rng = _op((10, 8), (0, 0, 0), 6, dbc, robin=robin)
     y = rng.standard_normal(phi.shape)
     grad = O.adjoint_bc_gradient(o, phi, J, y)
     bc_name = "derived_bc" if dbc else "phi_bc"

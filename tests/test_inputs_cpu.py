@@ -271,14 +271,19 @@ def test_regression_restart_cases():
 def test_diffusive_growth_inputs():
     """The reference's diffusive-growth case: its Robin coefficients read
     (through single precision, exact here), and its top wall, a mixed
-    temperature/salinity condition on the diagnostic temperature, refused
-    with the equivalent condition on the enthalpy named."""
+    temperature/salinity condition on the diagnostic temperature, given as
+    the derived condition MLGPU_BC_MIXED_TEMPERATURE_SALINITY on T with the
+    wall's flux value and the radiation constants of that side."""
     inp = mi.Inputs.read(os.path.join(os.path.dirname(REG), "diffusiveGrowth", "inputs"))
     g = inp.grid(2)
     T, V = inp.scalar_bcs(2)
     assert T["temperatureHi"][1] == mi.MIXED_T_S
-    with pytest.raises(ValueError, match="MixedBCTemperatureSalinity"):
-        inp.hc_bcs(g)
+    phi_bc, der, apply_dbc, nl = inp.hc_bcs(g)
+    assert apply_dbc == 1
+    assert der.type[1][1][0] == abi.BC_MIXED_TEMPERATURE_SALINITY
+    assert der.value[1][1][0] == -0.5
+    assert der.type[1][1][1] in (abi.BC_NEUMANN, abi.BC_DIRICHLET)
+    assert (nl.a[1][1], nl.b[1][1], nl.T_ref[1][1]) == (0.5, -1.0, 4.0)
     a, b = inp._bc_info("a", 2), inp._bc_info("b", 2)
     tref = inp._bc_info("TRef", 2)
     assert (a[1][1], b[1][1], tref[1][1]) == (0.5, -1.0, 4.0)

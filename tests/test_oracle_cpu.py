@@ -456,6 +456,43 @@ def test_steady_robin_conduction_matches_the_analytic_profile(a, b, F, Tref):
     assert np.abs(phi[1] + 1.0).max() == 0.0  # no solute diffusion: C unchanged
 
 
+@pytest.mark.parametrize("a,b,F,Tref", [(0.5, -1.0, -0.5, 4.0), (1.0, 0.0, -0.7, 0.0),
+                                        (2.0, -0.5, 0.3, -1.0)])
+def test_steady_mixed_condition_on_the_derived_temperature(a, b, F, Tref):
+    """The same steady profile with the walls as the reference's inputs
+    give them (test/diffusiveGrowth/inputs: bc.temperatureHi = 1 9): the
+    derived-variable conditions, T Dirichlet at the bottom and the
+    MixedBCTemperatureSalinity Robin ghost on T at the top
+    (BCutil/PhysBCUtil.cpp:764-800), which is linear in T, so the
+    discrete profile T = T_max + s z is exact."""
+    n = 32
+    g = abi.make_grid([4, n], 1.0 / n, [1, 0, 0])
+    p = P.mushy_params()
+    T_max = 3.0
+    s = (F + b * (T_max - Tref)) / (a - b)
+    der = abi.make_bc({(1, 0, 0): (abi.BC_DIRICHLET, T_max),
+                       (1, 1, 0): (abi.BC_MIXED_TEMPERATURE_SALINITY, F)})
+    nl = abi.make_nlbc(radiation={(1, 1): (a, b, Tref)})
+    phi = np.empty((2, 1, n, 4))
+    phi[0] = 5.0 + 2.5
+    phi[1] = -1.0
+    bcoef = [np.stack([-np.ones(abi.face_shape(g, d)), np.zeros(abi.face_shape(g, d))])
+             for d in range(2)]
+    ref = O.NLOpHost(g, p, abi.make_bc(), der, 1.0, -1.0, None, bcoef, apply_derived_bc=1,
+                     nlbc=nl)
+    opts = O.default_options(1)
+    opts.tolerance, opts.hang, opts.max_iter = 1e-13, 0.0, 200
+    for _ in range(4):
+        phi, st, rc = O.hc_backward_euler(ref, opts, phi, phi, 1e4)
+    T = phi[0, 0, :, 0] - 5.0
+    z = (np.arange(n) + 0.5) / n
+    assert np.abs(T - (T_max + s * z)).max() < 1e-8 * max(1.0, abs(s))
+    # the ghost the operator uses: a (T_g - T_i)/dx = F + b ((T_g + T_i)/2 - T_ref)
+    Ti = T[-1]
+    Tg = (Ti * (a * n + b / 2) + F - b * Tref) / (a * n - b / 2)
+    assert abs(a * (Tg - Ti) * n - (F + b * ((Tg + Ti) / 2 - Tref))) < 1e-10
+
+
 def test_darcy_brinkman_poiseuille_matches_the_analytic_profile():
     """The reference's Poiseuille check (test/poiseuilleFlow/
     testPoiseuilleFlow.py): v'' = (chi / Pi) v / Da - chi F between no-slip
