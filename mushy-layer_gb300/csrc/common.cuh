@@ -213,26 +213,58 @@ __device__ __forceinline__ void t_cl(double H, double C, const ClosureParams &p,
 // ---- FP32 <-> FP64 conversions on the integer pipe.  GB300 issues the
 // hardware conversions on its FP64 pipe (1/64 of the FP32 rate), where a
 // kernel that converts a few values per cell spends most of its time.
-// f32_trunc: x rounded toward zero to FP32 for |x| in FP32's normal range
-// (the hardware conversion otherwise: zero, subnormals, overflow, inf, NaN);
-// only decisions with a margin far above an FP32 ulp may use it.
+// FP64 <-> FP32 conversions on the integer pipe.  GB300 runs FP64 work,
+// conversions included, at 1/64 of the FP32 rate, and a fallback to the
+// hardware conversion for rare inputs is predicated by the compiler, so it
+// would still issue on the FP64 pipe for every cell: every case is formed
+// from the bit pattern instead.  Results below FP32's normal range flush to a
+// signed zero, inf stays inf and NaN a (quiet) NaN.
+// f32_trunc: x rounded toward zero (overflow: the largest finite magnitude);
+// for decisions with a margin far above an FP32 ulp and for seeds refined in
+// FP64.
 __device__ __forceinline__ float f32_trunc(double x) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(x);
   const unsigned hi = (unsigned)(b >> 32);
-  const int e = (int)((hi >> 20) & 0x7ffu) - 1023 + 127;
-  if (e <= 0 || e >= 255) return (float)x;
-  return __uint_as_float((hi & 0x80000000u) | ((unsigned)e << 23) | ((hi & 0xfffffu) << 3) |
-                         (unsigned)((b >> 29) & 7u));
+  const unsigned s = hi & 0x80000000u, ex = (hi >> 20) & 0x7ffu;
+  const int e = (int)ex - 896;  // FP32 biased exponent
+  unsigned r = s | ((unsigned)e << 23) | ((hi & 0xfffffu) << 3) | (unsigned)((b >> 29) & 7u);
+  r = e <= 0 ? s : r;
+  r = e >= 255 ? (s | 0x7f7fffffu) : r;
+  r = ex == 0x7ffu ? (s | 0x7f800000u | ((b << 12) != 0ull ? 0x400000u : 0u)) : r;
+  return __uint_as_float(r);
 }
-// f64_exact: the FP64 value of f (exact, as the hardware conversion), the
-// hardware conversion for zero, subnormals, inf and NaN
+// f32_round: x rounded to nearest, ties to even (overflow: inf)
+__device__ __forceinline__ float f32_round(double x) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const unsigned hi = (unsigned)(b >> 32);
+  const unsigned s = hi & 0x80000000u, ex = (hi >> 20) & 0x7ffu;
+  const int e = (int)ex - 896;
+  unsigned r = ((unsigned)e << 23) | ((hi & 0xfffffu) << 3) | (unsigned)((b >> 29) & 7u);
+  const unsigned rem = (unsigned)(b & 0x1fffffffull);  // the 29 dropped bits
+  r += (rem > 0x10000000u || (rem == 0x10000000u && (r & 1u))) ? 1u : 0u;  // may carry to inf
+  r = e <= 0 ? 0u : r;
+  r = e >= 255 ? 0x7f800000u : r;
+  r = ex == 0x7ffu ? (0x7f800000u | ((b << 12) != 0ull ? 0x400000u : 0u)) : r;
+  return __uint_as_float(s | r);
+}
+// f64_exact: the FP64 value of f (exact; FP32 subnormals flush to zero)
 __device__ __forceinline__ double f64_exact(float f) {
   const unsigned u = __float_as_uint(f);
   const unsigned e = (u >> 23) & 0xffu;
-  if (e == 0u || e == 255u) return (double)f;
-  return __longlong_as_double((long long)(((unsigned long long)(u & 0x80000000u) << 32) |
-                                          ((unsigned long long)(e + 896u) << 52) |
-                                          ((unsigned long long)(u & 0x7fffffu) << 29)));
+  const unsigned long long s = (unsigned long long)(u & 0x80000000u) << 32;
+  const unsigned long long m = (unsigned long long)(u & 0x7fffffu) << 29;
+  unsigned long long r = s | ((unsigned long long)(e + 896u) << 52) | m;
+  r = e == 0u ? s : r;
+  r = e == 255u ? (s | 0x7ff0000000000000ull | m) : r;
+  return __longlong_as_double((long long)r);
+}
+// the cycles' precision T from FP64: f32_round for float
+template <class T>
+__device__ __forceinline__ T narrow_to(double x) {
+  if constexpr (sizeof(T) == 4)
+    return f32_round(x);
+  else
+    return x;
 }
 
 // ---- lean FP64 closure (the outer loops of the lean Newton paths)

@@ -738,7 +738,12 @@ __global__ void __launch_bounds__(kBlock) lean_pack_kernel(Geom G, int ncomp,
     int i, j, k;
     cell_ijk(G, q, i, j, k);
     const long long o = at(G, i, j, k);
-    for (int c = 0; c < ncomp; c++) dst[c * n + o] = (T)src[c * n + q];
+    for (int c = 0; c < ncomp; c++) {
+      if constexpr (sizeof(T) == 4 && sizeof(S) == 8)
+        dst[c * n + o] = f32_round(src[c * n + q]);  // integer pipe
+      else
+        dst[c * n + o] = (T)src[c * n + q];
+    }
   }
 }
 

@@ -311,7 +311,7 @@ __global__ void __launch_bounds__(kBlock) vcl_outer_kernel(
     if (A.c) lof = fma(-A.beta * A.c[q], p0, lof);
     const double v = rhs[q] - lof;
     if (e) out_phi[q] = p0;
-    res_inner[cs_index(G, i, j, k)] = (E)v;
+    res_inner[cs_index(G, i, j, k)] = narrow_to<E>(v);
     if (NORM == MLGPU_NORM_MAX) {
       const unsigned long long bits =
           (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
