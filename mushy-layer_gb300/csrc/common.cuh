@@ -346,11 +346,21 @@ __device__ __forceinline__ double lean_div(double num, double den) {
   return fma(fma(-den, q, num), y, q);
 }
 
-__device__ __forceinline__ void t_cl_lean(double H, double C, const ClosureLean &p, double &T,
-                                          double &Cl) {
-  // the regime from FP32 bounds (integer-pipe conversions), re-decided in
-  // FP64 within 1e-4 of a bound; the closure is continuous across its
-  // bounds, so a cell an ulp from one may take either side
+// 1 / x for |x| well inside FP32's normal range (else the library division):
+// the FP32 reciprocal refined by two FMA iterations (~2^-23, 2^-46, then to
+// within an ulp)
+__device__ __forceinline__ double lean_rcp(double x) {
+  if (!lean_abs_range(x)) return 1.0 / x;
+  double y = f64_exact(__frcp_rn(f32_trunc(x)));
+  y = fma(fma(-x, y, 1.0), y, y);
+  return fma(fma(-x, y, 1.0), y, y);
+}
+
+// The regime of (H, C) (0 solid, 1 eutectic, 2 mush, 3 liquid, 4 NaN input)
+// from FP32 bounds (integer-pipe conversions), re-decided in FP64 within 1e-4
+// of a bound; the closure is continuous across its bounds, so a cell an ulp
+// from one may take either side
+__device__ __forceinline__ int lean_regime(double H, double C, const ClosureLean &p) {
   int reg;
   {
     const float h = f32_trunc(H), c = f32_trunc(C);
@@ -373,6 +383,12 @@ __device__ __forceinline__ void t_cl_lean(double H, double C, const ClosureLean 
       reg = h <= Hs ? 0 : (h <= He ? 1 : (h < Hl ? 2 : (h >= Hl ? 3 : 4)));
     }
   }
+  return reg;
+}
+
+__device__ __forceinline__ void t_cl_lean(double H, double C, const ClosureLean &p, double &T,
+                                          double &Cl) {
+  const int reg = lean_regime(H, C, p);
   if (reg == 0) {
     T = H * p.inv_cp;
     Cl = p.Te;
@@ -395,6 +411,46 @@ __device__ __forceinline__ void t_cl_lean(double H, double C, const ClosureLean 
   } else {  // NaN input, as t_cl
     T = H;
     Cl = C;
+  }
+}
+
+// d(T, C_l)/d(H, C) in FP64 for the lean FP64 Newton cycles: t_cl_jac_in's
+// expressions in the lean closure's regime, with the constant divisors as
+// reciprocals and the per-cell divisors (sqrt(disc), den) as one refined
+// reciprocal each (lean_sqrt, lean_rcp) -- a Jacobian to within a few ulps of
+// t_cl_jac's (the Newton iteration's fixed point is the residual's alone)
+__device__ __forceinline__ void t_cl_jac_lean(double H, double C, const ClosureLean &p,
+                                              double J[4]) {
+  const int reg = lean_regime(H, C, p);
+  J[0] = J[1] = J[2] = J[3] = 0.0;
+  if (reg == 0) {
+    J[0] = p.inv_cp;
+  } else if (reg == 2) {
+    double por = 1.0, dpH = 0.0, dpC = 0.0;
+    if (p.St != 0) {
+      const bool clamp = !(C >= -p.CR);
+      const double vC = clamp ? -p.CR : C;
+      const double b = p.b0 + H * p.omk - vC * p.cpm1;
+      const double c = (p.CR + vC) * p.cp + p.k * H;
+      const double sD = lean_sqrt(fma(b, b, -p.four_a * c));
+      const double isD = lean_rcp(sD);
+      por = (-b - sD) * p.inv_2a;
+      const double two_a = 2 * p.a;
+      const double dbH = p.omk, dbC = clamp ? 0.0 : -p.cpm1;
+      const double dcH = p.k, dcC = clamp ? 0.0 : p.cp;
+      dpH = (-dbH - (b * dbH - two_a * dcH) * isD) * p.inv_2a;
+      dpC = (-dbC - (b * dbC - two_a * dcC) * isD) * p.inv_2a;
+    }
+    const double num = C + p.CR * (1 - por), den = por + p.k * (1 - por);
+    const double iden = lean_rcp(den);
+    const double dCl_dpor = (-p.CR * den - num * p.omk) * iden * iden;
+    J[2] = dCl_dpor * dpH;
+    J[3] = iden + dCl_dpor * dpC;
+    J[0] = -J[2];
+    J[1] = -J[3];
+  } else if (reg == 3) {
+    J[0] = 1.0;
+    J[3] = 1.0;
   }
 }
 

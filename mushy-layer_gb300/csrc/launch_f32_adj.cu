@@ -182,7 +182,8 @@ template <class T>
 cudaError_t launch_lean_state(const AdjArgs<T> &A, const double *u, const T *P, T *Js, T *Ks,
                               T *Ds, cudaStream_t s) {
   const ClosureF32 f = make_closure_f32(A.cp);
-  MLGPU_DIM_SWITCH(A.G.dim, (lean_state_kernel<T, DIM><<<blocks_for(A.G.ncell), kBlock, 0, s>>>(A, f, u, P, Js, Ks, Ds)));
+  const ClosureLean L = make_closure_lean(A.cp);
+  MLGPU_DIM_SWITCH(A.G.dim, (lean_state_kernel<T, DIM><<<blocks_for(A.G.ncell), kBlock, 0, s>>>(A, f, L, u, P, Js, Ks, Ds)));
   return cudaGetLastError();
 }
 

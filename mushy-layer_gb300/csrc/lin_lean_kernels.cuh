@@ -599,12 +599,15 @@ __device__ __forceinline__ void lean_diag_block(const AdjArgs<T> &A, long long q
 }
 
 // Per Newton state, on a smoothed level: the closure Jacobian J (FP32 in t_cl's
-// regime for T = float, t_cl_jac for double), A's diagonal block D = M^T and
-// K = (D^T)^-1 = M^-1 of every cell, written straight to the split layout (the
-// generic route -- adj_jac, adj_minv through the full adjoint cell operator,
-// three permutations -- moves four times the bytes)
+// regime for T = float, the lean FP64 Jacobian t_cl_jac_lean for double), A's
+// diagonal block D = M^T and K = (D^T)^-1 = M^-1 of every cell (one
+// reciprocal of det M: correctly rounded in FP32, refined in FP64), written
+// straight to the split layout (the generic route -- adj_jac, adj_minv through
+// the full adjoint cell operator, three permutations -- moves four times the
+// bytes)
 template <class T, int DIM>
 __global__ void __launch_bounds__(kBlock) lean_state_kernel(AdjArgs<T> A, ClosureF32 f,
+                                                            ClosureLean L,
                                                             const double *__restrict__ u,
                                                             const T *__restrict__ Psum,
                                                             T *__restrict__ Js,
@@ -619,7 +622,7 @@ __global__ void __launch_bounds__(kBlock) lean_state_kernel(AdjArgs<T> A, Closur
     if constexpr (sizeof(T) == 4)
       t_cl_jac32(u[q], u[q + n], A.cp, f, Jc);
     else
-      t_cl_jac(u[q], u[q + n], A.cp, Jc);
+      t_cl_jac_lean(u[q], u[q + n], L, Jc);
     const T P[2] = {Psum[q], Psum[n + q]};
     lean_diag_block<T, DIM>(A, q, i, j, k, Jc, P, M);
     const T det = M[0] * M[3] - M[1] * M[2];
@@ -632,11 +635,12 @@ __global__ void __launch_bounds__(kBlock) lean_state_kernel(AdjArgs<T> A, Closur
       Ks[o + n] = -M[1] * id;
       Ks[o + 2 * n] = -M[2] * id;
       Ks[o + 3 * n] = M[0] * id;
-    } else {  // adj_minv_kernel's divisions
-      Ks[o] = M[3] / det;
-      Ks[o + n] = -M[1] / det;
-      Ks[o + 2 * n] = -M[2] / det;
-      Ks[o + 3 * n] = M[0] / det;
+    } else {
+      const double id = lean_rcp(det);
+      Ks[o] = M[3] * id;
+      Ks[o + n] = -M[1] * id;
+      Ks[o + 2 * n] = -M[2] * id;
+      Ks[o + 3 * n] = M[0] * id;
     }
     Ds[o] = M[0];
     Ds[o + n] = M[2];
@@ -662,16 +666,18 @@ __global__ void __launch_bounds__(kBlock) lean_prolong_lin_black_kernel(LinLeanT
     int I, J, K;
     cell_ijk(C, Q, I, J, K);
     const int base[3] = {I, J, K};
-    // coordinate and (per component) sign of the coarse value at offset
-    // o in {-1, 0, 1} along each direction, as coarse_at forms them
+    // coordinate and (per component) sign flip of the coarse value at offset
+    // o in {-1, 0, 1} along each direction, as coarse_at forms them (its
+    // product of +-1 signs is exact, so a negation by the flips' parity gives
+    // the same bits without FP multiplies)
     int co[3][3];
-    T sg[2][3][3];
+    unsigned fl[2][3][3];
 #pragma unroll
     for (int d = 0; d < 3; d++)
 #pragma unroll
       for (int o = 0; o < 3; o++) {
         int x = base[d] + o - 1;
-        T s0 = T(1), s1 = T(1);
+        unsigned s0 = 0u, s1 = 0u;
         if (d < DIM) {
           const int m = C.n(d);
           if (x < 0 || x >= m) {
@@ -680,20 +686,21 @@ __global__ void __launch_bounds__(kBlock) lean_prolong_lin_black_kernel(LinLeanT
               x = x < 0 ? m - 1 : 0;
             } else {
               x = x < 0 ? 0 : m - 1;
-              if (P.ybc.type[d][side][0] == MLGPU_BC_DIRICHLET) s0 = -s0;
-              if (P.ybc.type[d][side][1] == MLGPU_BC_DIRICHLET) s1 = -s1;
+              s0 = P.ybc.type[d][side][0] == MLGPU_BC_DIRICHLET ? 1u : 0u;
+              s1 = P.ybc.type[d][side][1] == MLGPU_BC_DIRICHLET ? 1u : 0u;
             }
           }
         } else {
           x = base[d];
         }
         co[d][o] = x;
-        sg[0][d][o] = s0;
-        sg[1][d][o] = s1;
+        fl[0][d][o] = s0;
+        fl[1][d][o] = s1;
       }
     auto cv = [&](int c, int ox, int oy, int oz) -> T {
       const long long q = (long long)c * C.ncell + at(C, co[0][ox + 1], co[1][oy + 1], co[2][oz + 1]);
-      return (sg[c][0][ox + 1] * sg[c][1][oy + 1] * sg[c][2][oz + 1]) * xc[q];
+      const T v = xc[q];
+      return (fl[c][0][ox + 1] ^ fl[c][1][oy + 1] ^ fl[c][2][oz + 1]) ? -v : v;
     };
 #pragma unroll
     for (int kk = 0; kk < (DIM == 3 ? 2 : 1); kk++)
