@@ -135,7 +135,8 @@ typedef struct mlgpu_nlop {
   const void *aCoef;     /* [2][cells] or NULL */
   const void *bCoef[3];  /* [2][faces_d] per direction */
   int dtype;
-  mlgpu_nlbc nlbc;       /* used where phi_bc comp 0 has a temperature type */
+  mlgpu_nlbc nlbc;       /* used where phi_bc comp 0 has a temperature type or
+                            derived_bc comp 0 the mixed temperature condition */
 } mlgpu_nlop;
 
 /* Linear variable-coefficient operator for one component
@@ -433,8 +434,10 @@ int mlgpu_hc_backward_euler(mlgpu_solver *S, double *phi_new, const double *phi_
  *   (a - mu1 dt L) psi = R,   (a - mu2 dt L) phi_new = a psi,
  * L(phi) = -div(b grad f(phi)) the nonlinear operator as the backward-Euler
  * step takes it (the operator with alpha = 1, beta = mu3 dt gives R's first
- * two terms); each solve by `S` (an HC solver, alpha = 1, beta = -mu dt; psi
- * starts from phi_old, phi_new from psi).  The source enters as dt src: the
+ * two terms); each solve by `S` with alpha = 1, beta = -mu dt (psi starts
+ * from phi_old, phi_new from psi): FAS solves on an HC solver
+ * (mlgpu_hc_solver_create), Newton solves (mlgpu_hc_newton_solve) on a
+ * Jacobian solver (mlgpu_hc_adjoint_create).  The source enters as dt src: the
  * scheme's second-order source weight dt (a + mu4 dt L) src is not formed for
  * the nonlinear operator, so the step is second order in time without a
  * source and first order in the source's contribution.  `scratch`: two fields

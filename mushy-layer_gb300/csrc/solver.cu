@@ -2222,18 +2222,18 @@ void tga_constants(double mu[3]) {
   mu[2] = 1.0 - a;
 }
 
-int mlgpu_hc_tga_step(mlgpu_solver *S, double *phi_new, const double *phi_old,
-                      const double *src, const double *aCoef, double dt, double *scratch,
-                      mlgpu_solve_stats *stats) {
-  if (!S || !phi_new || !phi_old || !scratch || !stats || !(dt > 0)) return MLGPU_ERR_ARG;
-  HCSolver *H = dynamic_cast<HCSolver *>(S);
-  if (!H) return MLGPU_ERR_ARG;
+}  // extern "C"
+
+// The TGA step on solver X (HCSolver: FAS solves; HCAdjSolver: Newton solves)
+template <class X, class Solve>
+static int tga_step(X *H, Solve solve, double *phi_new, const double *phi_old, const double *src,
+                    const double *aCoef, double dt, double *scratch, mlgpu_solve_stats *stats) {
   const long long n = 2 * H->L[0].G.ncell;
   double mu[3];
   tga_constants(mu);
   double *R = scratch, *psi = scratch + n;
   cudaGetLastError();
-  if (S->enter()) return MLGPU_ERR_CUDA;
+  if (H->enter()) return MLGPU_ERR_CUDA;
   // R = (a + mu3 dt L) phi_old + dt src: the operator with alpha 1, beta
   // mu3 dt applied to phi_old (alpha a phi + beta L, L = -div(b grad f(phi));
   // the solves below take beta -mu dt, as the backward-Euler step takes -dt)
@@ -2241,29 +2241,46 @@ int mlgpu_hc_tga_step(mlgpu_solver *S, double *phi_new, const double *phi_old,
   opR.alpha = 1.0;
   opR.beta = mu[2] * dt;
   CK(launch_nl_op<double>(make_nl_args<double>(opR), NL_APPLY, -1, phi_old, nullptr, R, nullptr,
-                          nullptr, nullptr, S->s));
-  if (src) CK(launch_add_dt_src(n, R, src, dt, S->s));
-  CK(cudaMemcpyAsync(psi, phi_old, sizeof(double) * n, cudaMemcpyDeviceToDevice, S->s));
-  if (S->leave()) return MLGPU_ERR_CUDA;
+                          nullptr, nullptr, H->s));
+  if (src) CK(launch_add_dt_src(n, R, src, dt, H->s));
+  CK(cudaMemcpyAsync(psi, phi_old, sizeof(double) * n, cudaMemcpyDeviceToDevice, H->s));
+  if (H->leave()) return MLGPU_ERR_CUDA;
   // (a - mu1 dt L) psi = R, then (a - mu2 dt L) phi_new = a psi
   mlgpu_solve_stats st1;
-  int rc = S->set_alpha_beta(1.0, -mu[0] * dt);
+  int rc = H->set_alpha_beta(1.0, -mu[0] * dt);
   if (rc) return rc;
-  rc = S->solve(psi, R, &st1);
+  rc = solve(psi, R, &st1);
   if (rc != MLGPU_OK && rc != MLGPU_ERR_NOT_CONVERGED && rc != MLGPU_ERR_HANG) return rc;
-  if (S->enter()) return MLGPU_ERR_CUDA;
-  CK(launch_scale_by_a(n, psi, aCoef, R, S->s));
-  CK(cudaMemcpyAsync(phi_new, psi, sizeof(double) * n, cudaMemcpyDeviceToDevice, S->s));
-  if (S->leave()) return MLGPU_ERR_CUDA;
-  rc = S->set_alpha_beta(1.0, -mu[1] * dt);
+  if (H->enter()) return MLGPU_ERR_CUDA;
+  CK(launch_scale_by_a(n, psi, aCoef, R, H->s));
+  CK(cudaMemcpyAsync(phi_new, psi, sizeof(double) * n, cudaMemcpyDeviceToDevice, H->s));
+  if (H->leave()) return MLGPU_ERR_CUDA;
+  rc = H->set_alpha_beta(1.0, -mu[1] * dt);
   if (rc) return rc;
-  const int rc2 = S->solve(phi_new, R, stats);
+  const int rc2 = solve(phi_new, R, stats);
   stats->iterations += st1.iterations;
   stats->cycles += st1.cycles;
   stats->cell_updates += st1.cell_updates;
   stats->kernel_launches += st1.kernel_launches;
   if (rc2 == MLGPU_OK) return rc;  // the first solve's status when the second converged
   return rc2;
+}
+
+extern "C" {
+
+int mlgpu_hc_tga_step(mlgpu_solver *S, double *phi_new, const double *phi_old,
+                      const double *src, const double *aCoef, double dt, double *scratch,
+                      mlgpu_solve_stats *stats) {
+  if (!S || !phi_new || !phi_old || !scratch || !stats || !(dt > 0)) return MLGPU_ERR_ARG;
+  if (HCSolver *H = dynamic_cast<HCSolver *>(S))
+    return tga_step(
+        H, [H](double *x, const double *r, mlgpu_solve_stats *st) { return H->solve(x, r, st); },
+        phi_new, phi_old, src, aCoef, dt, scratch, stats);
+  if (HCAdjSolver *A = dynamic_cast<HCAdjSolver *>(S))
+    return tga_step(
+        A, [A](double *x, const double *r, mlgpu_solve_stats *st) { return A->newton(x, r, st); },
+        phi_new, phi_old, src, aCoef, dt, scratch, stats);
+  return MLGPU_ERR_ARG;
 }
 
 int mlgpu_hc_adjoint_workspace(const mlgpu_nlop *op, const mlgpu_mg_options *o,

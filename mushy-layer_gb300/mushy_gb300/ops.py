@@ -514,6 +514,20 @@ class AdjointMultiGrid(_Solver):
         _ok(rc, "backwardEulerNewton")
         return st, rc
 
+    def tgaStep(self, phi_new, phi_old, dt, src=None, aCoef=None):
+        """The TGA step (time_integration_order = 2) with Newton's solves:
+        (a - mu1 dt L) psi = (a + mu3 dt L) phi_old + dt src and
+        (a - mu2 dt L) phi_new = a psi."""
+        scratch = torch.empty((2,) + tuple(phi_old.shape), dtype=phi_old.dtype,
+                              device=phi_old.device)
+        st = abi.SolveStats()
+        t0 = time.perf_counter()
+        rc = abi.load().mlgpu_hc_tga_step(self.h, _ptr(phi_new), _ptr(phi_old), _ptr(src),
+                                          _ptr(aCoef), float(dt), _ptr(scratch), C.byref(st))
+        _log("tgaStepNewton", self, st, rc, t0)
+        _ok(rc, "tgaStep")
+        return st, rc
+
     def bcGradient(self, y):
         """-y^T dN/dv for the 12 wall values [dir][side][comp] at the last state."""
         out = (C.c_double * 12)()

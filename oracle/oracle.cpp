@@ -1531,9 +1531,13 @@ int orc_hc_backward_euler(const mlgpu_nlop *op, const mlgpu_mg_options *o, doubl
 // mu3 dt; (a - mu1 dt L) psi = R from psi = phi_old; (a - mu2 dt L) phi_new
 // = a psi from phi_new = psi.  st: the second solve's, with the iterations,
 // cycles and cell updates of both
-int orc_hc_tga_step(const mlgpu_nlop *op, const mlgpu_mg_options *o, double *phi_new,
-                    const double *phi_old, const double *src, const double *a, double dt,
-                    mlgpu_solve_stats *st) {
+int orc_hc_newton_solve(const mlgpu_nlop *op, const mlgpu_mg_options *o, double *phi,
+                        const double *rhs, mlgpu_solve_stats *st);
+}  // extern "C"
+
+template <class Solve>
+static int tga_step(const mlgpu_nlop *op, Solve solve, double *phi_new, const double *phi_old,
+                    const double *src, const double *a, double dt, mlgpu_solve_stats *st) {
   const double at = 2.0 - std::sqrt(2.0) - 1e-12;
   const double d = std::sqrt(at * at - 4.0 * at + 2.0);
   const double mu1 = 0.5 * (at - d), mu2 = 0.5 * (at + d), mu3 = 1.0 - at;
@@ -1549,7 +1553,7 @@ int orc_hc_tga_step(const mlgpu_nlop *op, const mlgpu_mg_options *o, double *phi
   s1.alpha = 1.0;
   s1.beta = -mu1 * dt;
   mlgpu_solve_stats st1;
-  const int rc1 = orc_hc_solve(&s1, o, psi.data(), R.data(), &st1);
+  const int rc1 = solve(&s1, psi.data(), R.data(), &st1);
   if (rc1 != MLGPU_OK && rc1 != MLGPU_ERR_NOT_CONVERGED && rc1 != MLGPU_ERR_HANG) return rc1;
   for (size_t q = 0; q < n; q++) {
     R[q] = a ? psi[q] * a[q] : psi[q];
@@ -1558,11 +1562,36 @@ int orc_hc_tga_step(const mlgpu_nlop *op, const mlgpu_mg_options *o, double *phi
   mlgpu_nlop s2 = *op;
   s2.alpha = 1.0;
   s2.beta = -mu2 * dt;
-  const int rc2 = orc_hc_solve(&s2, o, phi_new, R.data(), st);
+  const int rc2 = solve(&s2, phi_new, R.data(), st);
   st->iterations += st1.iterations;
   st->cycles += st1.cycles;
   st->cell_updates += st1.cell_updates;
   return rc2 == MLGPU_OK ? rc1 : rc2;
+}
+
+extern "C" {
+
+int orc_hc_tga_step(const mlgpu_nlop *op, const mlgpu_mg_options *o, double *phi_new,
+                    const double *phi_old, const double *src, const double *a, double dt,
+                    mlgpu_solve_stats *st) {
+  return tga_step(
+      op,
+      [o](const mlgpu_nlop *x, double *u, const double *r, mlgpu_solve_stats *s) {
+        return orc_hc_solve(x, o, u, r, s);
+      },
+      phi_new, phi_old, src, a, dt, st);
+}
+
+// the same step with Newton solves (orc_hc_newton_solve)
+int orc_hc_tga_step_newton(const mlgpu_nlop *op, const mlgpu_mg_options *o, double *phi_new,
+                           const double *phi_old, const double *src, const double *a,
+                           double dt, mlgpu_solve_stats *st) {
+  return tga_step(
+      op,
+      [o](const mlgpu_nlop *x, double *u, const double *r, mlgpu_solve_stats *s) {
+        return orc_hc_newton_solve(x, o, u, r, s);
+      },
+      phi_new, phi_old, src, a, dt, st);
 }
 
 int orc_vc_solve(const mlgpu_vcop *op, const mlgpu_mg_options *o, double *phi,

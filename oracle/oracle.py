@@ -78,6 +78,8 @@ def lib():
                                           P(abi.SolveStats)]),
             "orc_hc_tga_step": (i, [P(abi.NLOp), P(abi.MGOptions), vp, vp, vp, vp, d,
                                           P(abi.SolveStats)]),
+            "orc_hc_tga_step_newton": (i, [P(abi.NLOp), P(abi.MGOptions), vp, vp, vp, vp, d,
+                                           P(abi.SolveStats)]),
         }
         for name, (res, args) in sig.items():
             f = getattr(L, name)
@@ -342,12 +344,14 @@ def mac_project(o, opts, phi_bc, u, pi, phi):
     return u, phi, st, rc
 
 
-def hc_tga_step(o, opts, phi_new, phi_old, dt, src=None, a=None):
-    """mlgpu_hc_tga_step restated: the TGA step by two FAS solves."""
+def hc_tga_step(o, opts, phi_new, phi_old, dt, src=None, a=None, newton=False):
+    """mlgpu_hc_tga_step restated: the TGA step by two FAS solves (newton:
+    two Newton solves, as on a Jacobian solver)."""
     phi_new = phi_new.copy()
     st = abi.SolveStats()
-    rc = lib().orc_hc_tga_step(C.byref(o.op), C.byref(opts), _p(phi_new), _p(phi_old),
-                               _p(src), _p(a), float(dt), C.byref(st))
+    f = lib().orc_hc_tga_step_newton if newton else lib().orc_hc_tga_step
+    rc = f(C.byref(o.op), C.byref(opts), _p(phi_new), _p(phi_old), _p(src), _p(a), float(dt),
+           C.byref(st))
     return phi_new, st, rc
 
 

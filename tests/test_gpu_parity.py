@@ -695,6 +695,50 @@ def test_tga_steps_bitwise(n):
         h_phi, d_phi = new_ref, d_new
 
 
+@pytest.mark.parametrize("n", [(64, 64), (32, 32, 32)])
+def test_tga_steps_newton(n):
+    """The TGA step on a Jacobian solver (Newton's solves, to 1e-10): FP64
+    against the oracle's Newton TGA step to 1e-10 (the L2 merit is summed in
+    another order), mixed precision within 1e-8 of FP64, three steps with a
+    source through the mush, slow solute diffusion."""
+    from mushy_gb300 import ops
+    dt = 2e-3
+    g = P.grid(n)
+    p = P.mushy_params()
+    phi_bc, der = P.hc_bcs("mixed")
+    rng = np.random.default_rng(43)
+    phi = P.hc_state(g, rng, regimes=False)
+    phi[0] = rng.uniform(4.6, 6.4, phi[0].shape)
+    b = [np.stack([-np.ones(abi.face_shape(g, d)), -0.01 * np.ones(abi.face_shape(g, d))])
+         for d in range(g.dim)]
+    src = 0.1 * rng.standard_normal(phi.shape)
+    ref = O.NLOpHost(g, p, phi_bc, der, 1.0, -dt, None, b)
+    oo = O.default_options(1)
+    oo.tolerance, oo.hang, oo.max_iter = 1e-10, -1.0, 60
+    op = ops.NLMultiCompOp(g, p, phi_bc, der, 1.0, -dt, None, [dev(x) for x in b])
+    solvers = {}
+    for prec in (abi.PREC_F64, abi.PREC_MIXED):
+        o = ops.default_options(True)
+        o.tolerance, o.hang, o.max_iter, o.precision = 1e-10, -1.0, 60, prec
+        solvers[prec] = ops.AdjointMultiGrid(op, o)
+    h = phi.copy()
+    cur = {k: dev(phi) for k in solvers}
+    d_src = dev(src)
+    for step in range(3):
+        h, st_r, rc_r = O.hc_tga_step(ref, oo, h, h, dt, src, newton=True)
+        assert rc_r == 0
+        out = {}
+        for k, S in solvers.items():
+            new = cur[k].clone()
+            st, rc = S.tgaStep(new, cur[k], dt, src=d_src)
+            assert rc == 0 and st.final_norm <= 1e-10 * st.initial_norm, (k, step, rc)
+            out[k] = host(new)
+            cur[k] = new
+        scale = np.abs(h).max()
+        assert np.abs(out[abi.PREC_F64] - h).max() <= 1e-10 * scale, step
+        assert np.abs(out[abi.PREC_MIXED] - out[abi.PREC_F64]).max() <= 1e-8 * scale, step
+
+
 # ----------------------------------- nonlinear temperature conditions on H
 def nl_setup_temperature(n, per, seed, method, limit):
     from mushy_gb300 import ops

@@ -45,10 +45,15 @@ def _run(step, o, phi, dt, nsteps):
     return cur
 
 
-@pytest.mark.parametrize("scheme,order", [("tga", 2), ("be", 1)])
+def _tga_newton(o, opts, phi_new, phi_old, dt):
+    return O.hc_tga_step(o, opts, phi_new, phi_old, dt, newton=True)
+
+
+@pytest.mark.parametrize("scheme,order", [("tga", 2), ("tga_newton", 2), ("be", 1)])
 def test_tga_second_order_in_time(scheme, order):
     g, o, phi, lam = _liquid()
-    step = O.hc_tga_step if scheme == "tga" else O.hc_backward_euler
+    step = {"tga": O.hc_tga_step, "tga_newton": _tga_newton,
+            "be": O.hc_backward_euler}[scheme]
     t_end = 0.04
     exact = phi.copy()
     exact[0] = 9.0 + (phi[0] - 9.0) * np.exp(lam * t_end)
@@ -59,7 +64,7 @@ def test_tga_second_order_in_time(scheme, order):
         errs.append(np.abs(out - exact).max())
     rates = [np.log2(errs[i] / errs[i + 1]) for i in range(2)]
     assert all(abs(r - order) < 0.25 for r in rates), (errs, rates)
-    if scheme == "tga":
+    if scheme != "be":
         # the TGA error at 16 steps is well below backward Euler's at 16
         be = _run(O.hc_backward_euler, o, phi, t_end / 16, 16)
         assert errs[-1] < 0.05 * np.abs(be - exact).max()
