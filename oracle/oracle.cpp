@@ -2433,7 +2433,9 @@ constexpr double kNewtonClip = 0.1, kNewtonEtaMax = 0.3;
 // mlgpu_hc_newton_solve restated with its default settings): A(u) d =
 // rhs - N(u) by V-cycles on A to eta relative (at most 12; eta the
 // Eisenstat-Walker forcing term, choice 2, gamma 0.9, alpha 2, safeguarded,
-// capped at 0.3, at least 0.5 tolerance |r_0| / |r_k|), u = u_old + s d with a
+// capped at 0.3, at least 0.5 tolerance |r_0| / |r_k|, and lowered to that
+// bound on a converging step (|r_k| / |r_k-1| < 0.1) when it is within a
+// factor 10 of the forcing), u = u_old + s d with a
 // cell whose H would leave
 // its closure regime stopped at the first regime boundary it crosses plus
 // kNewtonClip of its overshoot, s halved while the L2 residual grows (at most
@@ -2519,7 +2521,11 @@ extern "C" int orc_hc_newton_solve(const mlgpu_nlop *op, const mlgpu_mg_options 
       const double guard = 0.9 * eta * eta;
       if (guard > 0.1) e = std::max(e, guard);
       e = std::min(e, kNewtonEtaMax);
-      eta = std::min(kNewtonEtaMax, std::max(e, 0.5 * o->tolerance * norm0 / norm));
+      const double fin = 0.5 * o->tolerance * norm0 / norm;
+      eta = std::min(kNewtonEtaMax, std::max(e, fin));
+      // finishing step: down to the forcing that ends the solve when that
+      // costs at most a tenth more reduction
+      if (ratio < 0.1 && fin < eta && fin >= 0.1 * eta) eta = fin;
     }
     prev = norm;
     if (stall >= 3 && norm < 1e-8 * norm0 && status == 0) status = 2;
