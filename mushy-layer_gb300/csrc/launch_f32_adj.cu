@@ -137,8 +137,16 @@ cudaError_t launch_lean_restrict(const LinLeanT<T> &P, const Geom &C, int csplit
 template <class T>
 cudaError_t launch_lean_prolong(const LinLeanT<T> &P, const Geom &C, int csplit, int black,
                                 int kind, const T *xc, cudaStream_t s) {
-  if (black && kind == MLGPU_PROLONG_LINEAR) {  // one thread per coarse cell
-    const int nbc = blocks_for(C.ncell);
+  if (black && kind == MLGPU_PROLONG_LINEAR) {  // coarse tiles, one thread per coarse cell
+    long long ntiles;
+    if (P.G.dim == 3)
+      ntiles = (long long)((C.n0 + ProlongTile<3>::TX - 1) / ProlongTile<3>::TX) *
+               ((C.n1 + ProlongTile<3>::TY - 1) / ProlongTile<3>::TY) *
+               ((C.n2 + ProlongTile<3>::TZ - 1) / ProlongTile<3>::TZ);
+    else
+      ntiles = (long long)((C.n0 + ProlongTile<2>::TX - 1) / ProlongTile<2>::TX) *
+               ((C.n1 + ProlongTile<2>::TY - 1) / ProlongTile<2>::TY);
+    const int nbc = (int)std::min<long long>(ntiles, 1LL << 20);
     if (csplit) {
       MLGPU_DIM_SWITCH(P.G.dim, (lean_prolong_lin_black_kernel<T, DIM, SplitIdx><<<nbc, kBlock, 0, s>>>(P, C, xc)));
     } else {

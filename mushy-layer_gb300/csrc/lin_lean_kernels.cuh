@@ -650,57 +650,76 @@ __global__ void __launch_bounds__(kBlock) lean_state_kernel(AdjArgs<T> A, Closur
 }
 
 // The linear prolongation onto the black half (BLACK of lean_prolong_kernel
-// with KIND linear) with one thread per coarse cell: its black children
-// (the fine cells of odd (ii + jj + kk)) share the coarse values they read
-// (23 of the 27 around the coarse cell in 3D, instead of 8 per child), and
-// each child's value is prolong_add's expression on them.
+// with KIND linear) by coarse tiles: a block stages the coarse values of its
+// tile of kBlock coarse cells and their one-cell halo in shared memory -- each
+// value as coarse_at forms it (periodic wrap; a wall clamps to the edge cell
+// and negates it for a Dirichlet rule of that component, the product of +-1
+// signs being exact) -- and each thread forms its coarse cell's black children
+// (the fine cells of odd (ii + jj + kk)) from the tile with prolong_add's
+// expression: the same bits as one thread per fine cell, with each coarse
+// value loaded about 1.6 times per tile instead of 8 times per child.
+template <int DIM>
+struct ProlongTile {
+  static constexpr int TX = 32, TY = DIM == 3 ? 4 : 8, TZ = DIM == 3 ? 2 : 1;
+  static constexpr int HX = TX + 2, HY = TY + 2, HZ = DIM == 3 ? TZ + 2 : 1;
+  static_assert(TX * TY * TZ == kBlock, "one thread per coarse cell of the tile");
+};
+
 template <class T, int DIM, class CIDX>
 __global__ void __launch_bounds__(kBlock) lean_prolong_lin_black_kernel(LinLeanT<T> P, Geom C,
                                                                         const T *__restrict__ xc) {
+  using PT = ProlongTile<DIM>;
+  constexpr int TX = PT::TX, TY = PT::TY, TZ = PT::TZ, HX = PT::HX, HY = PT::HY, HZ = PT::HZ;
+  constexpr int HN = HX * HY * HZ;
+  __shared__ T tile[2 * HN];
   const Geom &G = P.G;
   const long long n = G.ncell;
   const T den = T(1) / (DIM == 3 ? T(64) : T(16));
   const T fx1 = T(3) * den, fx2 = T(9) * den, fx3 = T(27) * den, f0 = T(1) * den;
   const CIDX at;
-  for (long long Q = gtid(); Q < C.ncell; Q += gstride()) {
-    int I, J, K;
-    cell_ijk(C, Q, I, J, K);
-    const int base[3] = {I, J, K};
-    // coordinate and (per component) sign flip of the coarse value at offset
-    // o in {-1, 0, 1} along each direction, as coarse_at forms them (its
-    // product of +-1 signs is exact, so a negation by the flips' parity gives
-    // the same bits without FP multiplies)
-    int co[3][3];
-    unsigned fl[2][3][3];
+  const int ntx = (C.n0 + TX - 1) / TX, nty = (C.n1 + TY - 1) / TY;
+  const int ntz = DIM == 3 ? (C.n2 + TZ - 1) / TZ : 1;
+  const long long ntiles = (long long)ntx * nty * ntz;
+  const int lx = threadIdx.x % TX, ly = (threadIdx.x / TX) % TY, lz = threadIdx.x / (TX * TY);
+  for (long long tb = blockIdx.x; tb < ntiles; tb += gridDim.x) {
+    const int tx = (int)(tb % ntx), ty = (int)((tb / ntx) % nty), tz = (int)(tb / ((long long)ntx * nty));
+    const int org[3] = {tx * TX - 1, ty * TY - 1, DIM == 3 ? tz * TZ - 1 : 0};
+    __syncthreads();  // the previous tile's readers are done
+    for (int e = threadIdx.x; e < 2 * HN; e += kBlock) {
+      const int c = e / HN;
+      int r = e - c * HN;
+      const int z = r / (HX * HY);
+      r -= z * (HX * HY);
+      const int y = r / HX, xx = r - y * HX;
+      int cc[3] = {org[0] + xx, org[1] + y, org[2] + z};
+      unsigned fl = 0u;
 #pragma unroll
-    for (int d = 0; d < 3; d++)
-#pragma unroll
-      for (int o = 0; o < 3; o++) {
-        int x = base[d] + o - 1;
-        unsigned s0 = 0u, s1 = 0u;
-        if (d < DIM) {
-          const int m = C.n(d);
-          if (x < 0 || x >= m) {
-            const int side = x < 0 ? 0 : 1;
+      for (int d = 0; d < DIM; d++) {
+        const int m = C.n(d);
+        int v = cc[d];
+        if (v < 0 || v >= m) {
+          const int side = v < 0 ? 0 : 1;
+          if (v == -1 || v == m) {  // the halo of an edge tile: coarse_at's rule
             if (C.per(d)) {
-              x = x < 0 ? m - 1 : 0;
+              v = v < 0 ? m - 1 : 0;
             } else {
-              x = x < 0 ? 0 : m - 1;
-              s0 = P.ybc.type[d][side][0] == MLGPU_BC_DIRICHLET ? 1u : 0u;
-              s1 = P.ybc.type[d][side][1] == MLGPU_BC_DIRICHLET ? 1u : 0u;
+              v = v < 0 ? 0 : m - 1;
+              fl ^= P.ybc.type[d][side][c] == MLGPU_BC_DIRICHLET ? 1u : 0u;
             }
+          } else {  // past a partial tile: read by no coarse cell of the box
+            v = m - 1;
           }
-        } else {
-          x = base[d];
         }
-        co[d][o] = x;
-        fl[0][d][o] = s0;
-        fl[1][d][o] = s1;
+        cc[d] = v;
       }
+      const T v = xc[(long long)c * C.ncell + at(C, cc[0], cc[1], cc[2])];
+      tile[e] = fl ? -v : v;
+    }
+    __syncthreads();
+    const int I = org[0] + 1 + lx, J = org[1] + 1 + ly, K = DIM == 3 ? org[2] + 1 + lz : 0;
+    if (I >= C.n0 || J >= C.n1 || (DIM == 3 && K >= C.n2)) continue;
     auto cv = [&](int c, int ox, int oy, int oz) -> T {
-      const long long q = (long long)c * C.ncell + at(C, co[0][ox + 1], co[1][oy + 1], co[2][oz + 1]);
-      const T v = xc[q];
-      return (fl[c][0][ox + 1] ^ fl[c][1][oy + 1] ^ fl[c][2][oz + 1]) ? -v : v;
+      return tile[c * HN + ((DIM == 3 ? lz + 1 + oz : 0) * HY + ly + 1 + oy) * HX + lx + 1 + ox];
     };
 #pragma unroll
     for (int kk = 0; kk < (DIM == 3 ? 2 : 1); kk++)
