@@ -109,13 +109,15 @@ cudaError_t launch_adj_minv(const AdjArgs<float> &A, const float *zero, float *M
 template <class T>
 cudaError_t launch_lean_gsrb(const LinLeanT<T> &P, int pass, cudaStream_t s, int vec = 0);
 // red: the red half's residual only (after a black half sweep); black: the
-// black half's prolongation only (before a red half sweep)
+// black half's prolongation only (before a red half sweep); vec: the red
+// residual and restriction by vector groups where the rows allow it (the
+// same per-cell bits)
 template <class T>
 cudaError_t launch_lean_residual(const LinLeanT<T> &P, int split, int red, int norm,
-                                 double *part, int *nparts, cudaStream_t s);
+                                 double *part, int *nparts, cudaStream_t s, int vec = 0);
 template <class T>
 cudaError_t launch_lean_restrict(const LinLeanT<T> &P, const Geom &C, int csplit, int red, T *gc,
-                                 T *xc, T *wc, cudaStream_t s);
+                                 T *xc, T *wc, cudaStream_t s, int vec = 0);
 template <class T>
 cudaError_t launch_lean_prolong(const LinLeanT<T> &P, const Geom &C, int csplit, int black,
                                 int kind, const T *xc, cudaStream_t s);

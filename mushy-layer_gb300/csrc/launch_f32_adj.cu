@@ -92,11 +92,21 @@ cudaError_t launch_lean_gsrb(const LinLeanT<T> &P, int pass, cudaStream_t s, int
 
 template <class T>
 cudaError_t launch_lean_residual(const LinLeanT<T> &P, int split, int red, int norm,
-                                 double *part, int *nparts, cudaStream_t s) {
+                                 double *part, int *nparts, cudaStream_t s, int vec) {
   red = split && red;
+  if (norm < 0) norm = MLGPU_NORM_MAX;
+  constexpr int V = Vec16<T>::V;
+  if (vec && red && ((P.G.n0 >> 1) % V) == 0) {
+    const int nb = blocks_for((P.G.ncell >> 1) / V);
+    if (nparts) *nparts = nb;
+    MLGPU_DIM_SWITCH(P.G.dim, MLGPU_NORM_SWITCH(norm, {
+      if (NORM >= 0)
+        lean_residual_vec_kernel<T, DIM, (NORM < 0 ? 0 : NORM)><<<nb, kBlock, 0, s>>>(P, part);
+    }));
+    return cudaGetLastError();
+  }
   const int nb = blocks_for(red ? P.G.ncell >> 1 : P.G.ncell);
   if (nparts) *nparts = nb;
-  if (norm < 0) norm = MLGPU_NORM_MAX;
 #define MLGPU_LEAN_RES(IDX, RED)                                                          \
   MLGPU_DIM_SWITCH(P.G.dim, MLGPU_NORM_SWITCH(norm, {                                     \
     if (NORM >= 0)                                                                        \
@@ -115,7 +125,16 @@ cudaError_t launch_lean_residual(const LinLeanT<T> &P, int split, int red, int n
 
 template <class T>
 cudaError_t launch_lean_restrict(const LinLeanT<T> &P, const Geom &C, int csplit, int red, T *gc,
-                                 T *xc, T *wc, cudaStream_t s) {
+                                 T *xc, T *wc, cudaStream_t s, int vec) {
+  constexpr int V = Vec16<T>::V;
+  if (vec && red && ((P.G.n0 >> 1) % V) == 0 && C.n0 == (P.G.n0 >> 1)) {
+    const int nbv = blocks_for(C.ncell / V);
+    if (csplit)
+      MLGPU_DIM_SWITCH(P.G.dim, (lean_restrict_vec_kernel<T, DIM, SplitIdx><<<nbv, kBlock, 0, s>>>(P, C, gc, xc, wc)));
+    else
+      MLGPU_DIM_SWITCH(P.G.dim, (lean_restrict_vec_kernel<T, DIM, NaturalIdx><<<nbv, kBlock, 0, s>>>(P, C, gc, xc, wc)));
+    return cudaGetLastError();
+  }
   const int nb = blocks_for(C.ncell);
 #define MLGPU_LEAN_RST(IDX, RED) \
   MLGPU_DIM_SWITCH(P.G.dim, (lean_restrict_kernel<T, DIM, IDX, RED><<<nb, kBlock, 0, s>>>(P, C, gc, xc, wc)))
@@ -326,9 +345,9 @@ MLGPU_VCL_INST(double)
 #define MLGPU_LEAN_INST(T)                                                                     \
   template cudaError_t launch_lean_gsrb<T>(const LinLeanT<T> &, int, cudaStream_t, int);      \
   template cudaError_t launch_lean_residual<T>(const LinLeanT<T> &, int, int, int, double *,   \
-                                              int *, cudaStream_t);                           \
+                                              int *, cudaStream_t, int);                      \
   template cudaError_t launch_lean_restrict<T>(const LinLeanT<T> &, const Geom &, int, int,    \
-                                              T *, T *, T *, cudaStream_t);                   \
+                                              T *, T *, T *, cudaStream_t, int);              \
   template cudaError_t launch_lean_prolong<T>(const LinLeanT<T> &, const Geom &, int, int,     \
                                              int, const T *, cudaStream_t);                   \
   template cudaError_t launch_lean_pack<T, double>(const Geom &, int, int, const double *, T *, \

@@ -259,98 +259,114 @@ __device__ __forceinline__ void stv(T *__restrict__ p, const T *in) {
   *reinterpret_cast<VT *>(p) = v;
 }
 
+// The neighbour sums s_c = sum over interior faces of b_f,c w_nb,c of the V
+// cells hh .. hh + V - 1 of colour `pass` in row `row` = (j, k) of a split
+// level (the other colour's w around them: one vector load per row and
+// component, the row's extra value for x), lean_nbsum's order term by term,
+// so the same bits.
+template <class T, int DIM>
+__device__ __forceinline__ void lean_vsum(const LinLeanT<T> &P, int pass, unsigned row, int hh,
+                                          int j, int k, T *s0, T *s1) {
+  constexpr int V = Vec16<T>::V;
+  const Geom &G = P.G;
+  const long long n = G.ncell, half = n >> 1;
+  const int h0 = G.n0 >> 1;
+  const long long obase = half - pass * half;  // the other colour's half
+  const long long nf0 = (long long)(G.n0 + 1) * G.n1 * G.n2;
+  const long long nf1 = (long long)G.n0 * (G.n1 + 1) * G.n2;
+  const long long pl = (long long)G.n0 * G.n1, nf2 = pl * (G.n2 + 1);
+  const T *w = P.w;
+  const int par = (j + k + pass) & 1;  // i of the group's first cell = 2 hh + par
+#pragma unroll
+  for (int v = 0; v < V; v++) s0[v] = s1[v] = T(0);
+  // x: the other colour's w at hh - 1 + par .. hh + V - 1 + par of this row
+  {
+    const long long ob = obase + (long long)row * h0;
+    T wv0[V], wv1[V];
+    ldv(w + ob + hh, wv0);
+    ldv(w + n + ob + hh, wv1);
+    // the extra value: hh - 1 (par 0) or hh + V (par 1), wrapped when periodic
+    int xe = par ? hh + V : hh - 1;
+    bool has_e = true;
+    if (xe < 0) {
+      xe = h0 - 1;
+      has_e = G.per0 != 0;
+    } else if (xe >= h0) {
+      xe = 0;
+      has_e = G.per0 != 0;
+    }
+    const T e0 = has_e ? w[ob + xe] : T(0), e1 = has_e ? w[n + ob + xe] : T(0);
+    const long long f0 = (long long)row * (G.n0 + 1) + 2 * hh + par;  // low face of cell 0
+#pragma unroll
+    for (int v = 0; v < V; v++) {
+      const long long f = f0 + 2 * v;
+      // low neighbour: hh + v - 1 + par (register selects: v is a constant
+      // of the unrolled loop, only par is not)
+      const int vl = v > 0 ? v - 1 : 0, vh = v < V - 1 ? v + 1 : V - 1;
+      const bool lo_e = par == 0 && v == 0;
+      if (!lo_e || has_e) {
+        const T a0 = lo_e ? e0 : (par ? wv0[v] : wv0[vl]);
+        const T a1 = lo_e ? e1 : (par ? wv1[v] : wv1[vl]);
+        s0[v] = fmaT(P.b[0][f], a0, s0[v]);
+        s1[v] = fmaT(P.b[0][nf0 + f], a1, s1[v]);
+      }
+      // high neighbour: hh + v + par
+      const bool hi_e = par == 1 && v == V - 1;
+      if (!hi_e || has_e) {
+        const T a0 = hi_e ? e0 : (par ? wv0[vh] : wv0[v]);
+        const T a1 = hi_e ? e1 : (par ? wv1[vh] : wv1[v]);
+        s0[v] = fmaT(P.b[0][f + 1], a0, s0[v]);
+        s1[v] = fmaT(P.b[0][nf0 + f + 1], a1, s1[v]);
+      }
+    }
+  }
+  // y and z: the same positions hh .. hh + V - 1 in the neighbouring rows
+#pragma unroll
+  for (int d = 1; d < DIM; d++) {
+    const int m = d == 1 ? G.n1 : G.n2, c = d == 1 ? j : k;
+    const bool per = d == 1 ? G.per1 != 0 : G.per2 != 0;
+    const long long nf = d == 1 ? nf1 : nf2;
+    const long long step = d == 1 ? G.n0 : pl;  // face stride of the direction
+    // low face of cell v: natural face index of (i_v, j, k) in direction d
+    const long long fb = d == 1 ? ((long long)k * (G.n1 + 1) + j) * G.n0 + 2 * hh + par
+                                : (long long)row * G.n0 + 2 * hh + par;
+#pragma unroll
+    for (int side = 0; side < 2; side++) {
+      int cn = c + (side ? 1 : -1);
+      if (cn < 0 || cn >= m) {
+        if (!per || m == 1) continue;
+        cn = cn < 0 ? m - 1 : 0;
+      }
+      const unsigned nrow = d == 1 ? (unsigned)k * G.n1 + cn : (unsigned)cn * G.n1 + j;
+      T nb0[V], nb1[V];
+      ldv(w + obase + (long long)nrow * h0 + hh, nb0);
+      ldv(w + n + obase + (long long)nrow * h0 + hh, nb1);
+#pragma unroll
+      for (int v = 0; v < V; v++) {
+        const long long f = fb + 2 * v + (side ? step : 0);
+        s0[v] = fmaT(P.b[d][f], nb0[v], s0[v]);
+        s1[v] = fmaT(P.b[d][nf + f], nb1[v], s1[v]);
+      }
+    }
+  }
+}
+
 template <class T, int DIM>
 __global__ void __launch_bounds__(kBlock) lean_gsrb_vec_kernel(LinLeanT<T> P, int pass) {
   constexpr int V = Vec16<T>::V;
   const Geom &G = P.G;
   const long long n = G.ncell, half = n >> 1;
   const int h0 = G.n0 >> 1;
-  const long long base = pass * half, obase = half - base;  // own / other half
+  const long long base = pass * half;  // own half
   const long long ngroups = half / V;
-  const long long nf0 = (long long)(G.n0 + 1) * G.n1 * G.n2;
-  const long long nf1 = (long long)G.n0 * (G.n1 + 1) * G.n2;
-  const long long pl = (long long)G.n0 * G.n1, nf2 = pl * (G.n2 + 1);
-  const T *w = P.w;
   for (long long t = gtid(); t < ngroups; t += gstride()) {
     const long long u = t * V;
     const unsigned row = (unsigned)u / (unsigned)h0;
     const int hh = (int)((unsigned)u - row * (unsigned)h0);
     const int k = (int)(row / (unsigned)G.n1), j = (int)(row - (unsigned)k * G.n1);
-    const int par = (j + k + pass) & 1;  // i of the group's first cell = 2 hh + par
     const long long q = base + u;
     T s0[V], s1[V];
-#pragma unroll
-    for (int v = 0; v < V; v++) s0[v] = s1[v] = T(0);
-    // x: the other colour's w at hh - 1 + par .. hh + V - 1 + par of this row
-    {
-      const long long ob = obase + (long long)row * h0;
-      T wv0[V], wv1[V];
-      ldv(w + ob + hh, wv0);
-      ldv(w + n + ob + hh, wv1);
-      // the extra value: hh - 1 (par 0) or hh + V (par 1), wrapped when periodic
-      int xe = par ? hh + V : hh - 1;
-      bool has_e = true;
-      if (xe < 0) {
-        xe = h0 - 1;
-        has_e = G.per0 != 0;
-      } else if (xe >= h0) {
-        xe = 0;
-        has_e = G.per0 != 0;
-      }
-      const T e0 = has_e ? w[ob + xe] : T(0), e1 = has_e ? w[n + ob + xe] : T(0);
-      const long long f0 = (long long)row * (G.n0 + 1) + 2 * hh + par;  // low face of cell 0
-#pragma unroll
-      for (int v = 0; v < V; v++) {
-        const long long f = f0 + 2 * v;
-        // low neighbour: hh + v - 1 + par (register selects: v is a constant
-        // of the unrolled loop, only par is not)
-        const int vl = v > 0 ? v - 1 : 0, vh = v < V - 1 ? v + 1 : V - 1;
-        const bool lo_e = par == 0 && v == 0;
-        if (!lo_e || has_e) {
-          const T a0 = lo_e ? e0 : (par ? wv0[v] : wv0[vl]);
-          const T a1 = lo_e ? e1 : (par ? wv1[v] : wv1[vl]);
-          s0[v] = fmaT(P.b[0][f], a0, s0[v]);
-          s1[v] = fmaT(P.b[0][nf0 + f], a1, s1[v]);
-        }
-        // high neighbour: hh + v + par
-        const bool hi_e = par == 1 && v == V - 1;
-        if (!hi_e || has_e) {
-          const T a0 = hi_e ? e0 : (par ? wv0[vh] : wv0[v]);
-          const T a1 = hi_e ? e1 : (par ? wv1[vh] : wv1[v]);
-          s0[v] = fmaT(P.b[0][f + 1], a0, s0[v]);
-          s1[v] = fmaT(P.b[0][nf0 + f + 1], a1, s1[v]);
-        }
-      }
-    }
-    // y and z: the same positions hh .. hh + V - 1 in the neighbouring rows
-#pragma unroll
-    for (int d = 1; d < DIM; d++) {
-      const int m = d == 1 ? G.n1 : G.n2, c = d == 1 ? j : k;
-      const bool per = d == 1 ? G.per1 != 0 : G.per2 != 0;
-      const long long nf = d == 1 ? nf1 : nf2;
-      const long long step = d == 1 ? G.n0 : pl;  // face stride of the direction
-      // low face of cell v: natural face index of (i_v, j, k) in direction d
-      const long long fb = d == 1 ? ((long long)k * (G.n1 + 1) + j) * G.n0 + 2 * hh + par
-                                  : (long long)row * G.n0 + 2 * hh + par;
-#pragma unroll
-      for (int side = 0; side < 2; side++) {
-        int cn = c + (side ? 1 : -1);
-        if (cn < 0 || cn >= m) {
-          if (!per || m == 1) continue;
-          cn = cn < 0 ? m - 1 : 0;
-        }
-        const unsigned nrow = d == 1 ? (unsigned)k * G.n1 + cn : (unsigned)cn * G.n1 + j;
-        T nb0[V], nb1[V];
-        ldv(w + obase + (long long)nrow * h0 + hh, nb0);
-        ldv(w + n + obase + (long long)nrow * h0 + hh, nb1);
-#pragma unroll
-        for (int v = 0; v < V; v++) {
-          const long long f = fb + 2 * v + (side ? step : 0);
-          s0[v] = fmaT(P.b[d][f], nb0[v], s0[v]);
-          s1[v] = fmaT(P.b[d][nf + f], nb1[v], s1[v]);
-        }
-      }
-    }
+    lean_vsum<T, DIM>(P, pass, row, hh, j, k, s0, s1);
     T g0[V], g1[V], K0[V], K1[V], K2[V], K3[V], J0[V], J1[V], J2[V], J3[V];
     ldv(P.g + q, g0);
     ldv(P.g + n + q, g1);
@@ -463,6 +479,112 @@ __global__ void __launch_bounds__(kBlock) lean_restrict_kernel(LinLeanT<T> P, Ge
     xc[nc + oq] = T(0);
     wc[oq] = T(0);
     wc[nc + oq] = T(0);
+  }
+}
+
+// g - A x of the V cells at q .. q + V - 1 of a split level whose neighbour
+// sums are s (lean_res's expression per cell)
+template <class T>
+__device__ __forceinline__ void lean_vres(const LinLeanT<T> &P, long long q, const T *s0,
+                                          const T *s1, T *r0, T *r1) {
+  constexpr int V = Vec16<T>::V;
+  const long long n = P.G.ncell;
+  T g0[V], g1[V], D0[V], D1[V], D2[V], D3[V], x0[V], x1[V];
+  ldv(P.g + q, g0);
+  ldv(P.g + n + q, g1);
+  ldv(P.D + q, D0);
+  ldv(P.D + n + q, D1);
+  ldv(P.D + 2 * n + q, D2);
+  ldv(P.D + 3 * n + q, D3);
+  ldv(P.x + q, x0);
+  ldv(P.x + n + q, x1);
+#pragma unroll
+  for (int v = 0; v < V; v++) {
+    const T ax0 = fmaT(D0[v], x0[v], D1[v] * x1[v]);
+    const T ax1 = fmaT(D2[v], x0[v], D3[v] * x1[v]);
+    r0[v] = fmaT(P.bdx, s0[v], g0[v]) - ax0;
+    r1[v] = fmaT(P.bdx, s1[v], g1[v]) - ax1;
+  }
+}
+
+// lean_residual_kernel (split, RED) with V red cells of a row per thread
+// (vector loads; the per-cell values bit for bit, the norm's partial sums in
+// another order)
+template <class T, int DIM, int NORM>
+__global__ void __launch_bounds__(kBlock) lean_residual_vec_kernel(LinLeanT<T> P, double *part) {
+  constexpr int V = Vec16<T>::V;
+  const Geom &G = P.G;
+  const int h0 = G.n0 >> 1;
+  const long long ngroups = (G.ncell >> 1) / V;
+  T acc = T(0);
+  for (long long t = gtid(); t < ngroups; t += gstride()) {
+    const long long u = t * V;
+    const unsigned row = (unsigned)u / (unsigned)h0;
+    const int hh = (int)((unsigned)u - row * (unsigned)h0);
+    const int k = (int)(row / (unsigned)G.n1), j = (int)(row - (unsigned)k * G.n1);
+    T s0[V], s1[V], r0[V], r1[V];
+    lean_vsum<T, DIM>(P, 0, row, hh, j, k, s0, s1);
+    lean_vres<T>(P, u, s0, s1, r0, r1);
+#pragma unroll
+    for (int v = 0; v < V; v++) {
+      acc = lean_accum<T, NORM>(acc, r0[v]);
+      acc = lean_accum<T, NORM>(acc, r1[v]);
+    }
+  }
+  const double v = block_reduce<NORM>((double)acc);
+  if (threadIdx.x == 0) part[blockIdx.x] = v;
+}
+
+// lean_restrict_kernel (RED) with V coarse cells of a coarse row per thread:
+// the red children of coarse cells I0 .. I0 + V - 1 in fine row (2J + jj,
+// 2K + kk) are that row's red cells I0 .. I0 + V - 1 (split positions), so each
+// child class is one vector group; the children summed in the scalar
+// kernel's order (the same bits)
+template <class T, int DIM, class CIDX>
+__global__ void __launch_bounds__(kBlock) lean_restrict_vec_kernel(LinLeanT<T> P, Geom C, T *gc,
+                                                                   T *xc, T *wc) {
+  constexpr int V = Vec16<T>::V;
+  const Geom &G = P.G;
+  const long long nc = C.ncell, ngroups = nc / V;
+  const int h0 = G.n0 >> 1;
+  const T wgt = DIM == 3 ? T(0.125) : T(0.25);
+  const CIDX at;
+  for (long long t = gtid(); t < ngroups; t += gstride()) {
+    const long long U = t * V;
+    const unsigned crow = (unsigned)U / (unsigned)C.n0;
+    const int I0 = (int)((unsigned)U - crow * (unsigned)C.n0);
+    const int K = (int)(crow / (unsigned)C.n1), J = (int)(crow - (unsigned)K * C.n1);
+    T a0[V], a1[V];
+#pragma unroll
+    for (int v = 0; v < V; v++) a0[v] = a1[v] = T(0);
+#pragma unroll
+    for (int kk = 0; kk < (DIM == 3 ? 2 : 1); kk++)
+#pragma unroll
+      for (int jj = 0; jj < 2; jj++)
+#pragma unroll
+        for (int ii = 0; ii < 2; ii++) {
+          if ((ii + jj + kk) & 1) continue;  // black child
+          const int j = 2 * J + jj, k = DIM == 3 ? 2 * K + kk : 0;
+          const unsigned row = (unsigned)k * G.n1 + j;
+          T s0[V], s1[V], r0[V], r1[V];
+          lean_vsum<T, DIM>(P, 0, row, I0, j, k, s0, s1);
+          lean_vres<T>(P, (long long)row * h0 + I0, s0, s1, r0, r1);
+#pragma unroll
+          for (int v = 0; v < V; v++) {
+            a0[v] += r0[v];
+            a1[v] += r1[v];
+          }
+        }
+#pragma unroll
+    for (int v = 0; v < V; v++) {
+      const long long oq = at(C, I0 + v, J, K);
+      gc[oq] = a0[v] * wgt;
+      gc[nc + oq] = a1[v] * wgt;
+      xc[oq] = T(0);
+      xc[nc + oq] = T(0);
+      wc[oq] = T(0);
+      wc[nc + oq] = T(0);
+    }
   }
 }
 

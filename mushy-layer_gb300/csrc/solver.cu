@@ -1646,7 +1646,7 @@ class HCAdjSolver : public mlgpu_solver {
     if (rc) return rc;
     const LinLeanT<T> C = leanT<T>(l + 1);
     CK(launch_lean_restrict<T>(P, C.G, split(l + 1), o.num_smooth_down >= 1, (T *)C.g, C.x, C.w,
-                               s));
+                               s, lean_vec));
     for (int m = 0; m < o.num_mg; m++) {
       if (m > 0) {  // every coarse visit starts from zero
         CK(cudaMemsetAsync(C.x, 0, sizeof(T) * 2 * C.G.ncell, s));
@@ -1666,7 +1666,8 @@ class HCAdjSolver : public mlgpu_solver {
   int lin_residual_norm(bool after_cycle = false) {
     int nparts = 0;
     const bool red = after_cycle && o.num_smooth_up >= 1 && (int)L.size() > 1;
-    CK(launch_lean_residual<T>(leanT<T>(0), split(0), red, o.norm_type, part, &nparts, s));
+    CK(launch_lean_residual<T>(leanT<T>(0), split(0), red, o.norm_type, part, &nparts, s,
+                               lean_vec));
     CK(launch_finalize_norm(o.norm_type, part, nparts, part + kMaxBlocks, s));
     CK(cudaMemcpyAsync(host_norm, part + kMaxBlocks, sizeof(double), cudaMemcpyDeviceToHost, s));
     return MLGPU_OK;
