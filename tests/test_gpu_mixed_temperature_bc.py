@@ -190,3 +190,36 @@ def test_mixed_condition_newton_steps(n):
     h, st_r, rc_r = O.newton_solve(ref, oo, phi, phi.copy())
     assert rc_r == 0
     assert np.abs(u64 - h).max() <= 1e-10 * scale
+
+
+def test_mixed_condition_fas_mixed_precision():
+    """The FAS solve in mixed precision (FP32 linearised cycles, whose
+    homogeneous wall rule for the mixed condition is its derivative g, inside
+    the FP64 defect correction): 1e-10 under the oracle's FP64 residual and
+    within 1e-8 of the FP64 FAS solution when that one converges."""
+    from mushy_gb300 import ops
+    dt = 1e-3
+    g = P.grid((48, 32))
+    p = P.mushy_params()
+    phi_bc, der, nl = _bcs(g)
+    rng = np.random.default_rng(37)
+    phi = P.hc_state(g, rng, regimes=False)
+    b = [np.stack([-np.ones(abi.face_shape(g, d)), -0.01 * np.ones(abi.face_shape(g, d))])
+         for d in range(2)]
+    rhs = phi.copy()
+    ref = O.NLOpHost(g, p, phi_bc, der, 1.0, -dt, None, b, nlbc=nl)
+    op = ops.NLMultiCompOp(g, p, phi_bc, der, 1.0, -dt, None, [dev(x) for x in b], nlbc=nl)
+    sols = {}
+    for prec in (abi.PREC_F64, abi.PREC_MIXED):
+        o = ops.default_options(True)
+        o.max_iter, o.tolerance, o.hang, o.precision = 60, 1e-10, 1e-15, prec
+        d_phi = dev(phi)
+        st, rc = ops.AMRFASMultiGrid(op, o).solve(d_phi, dev(rhs))
+        sols[prec] = (host(d_phi), st, rc)
+    um, stm, rcm = sols[abi.PREC_MIXED]
+    assert rcm == 0 and stm.final_norm <= 1e-10 * stm.initial_norm
+    r0 = np.abs(O.nl_residual(ref, phi, rhs)).max()
+    assert np.abs(O.nl_residual(ref, um, rhs)).max() <= 1.05e-10 * r0
+    u64, st64, rc64 = sols[abi.PREC_F64]
+    if rc64 == 0:
+        assert np.abs(um - u64).max() <= 1e-8 * np.abs(u64).max()
