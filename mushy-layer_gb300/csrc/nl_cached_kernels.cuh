@@ -243,7 +243,7 @@ __global__ void __launch_bounds__(kNLCBlock) nlc_bsum_kernel(NLArgs<double> A,
 //   sum_f b_f (f_nb - f_c) = sum_f b_f f_nb - f_c sum_f b_f
 // with sum_f b_f per cell precomputed (sb; a wall face's ghost value enters
 // as its neighbour value, so the identity holds on every face), by FMA;
-// lof = (alpha a) phi - (beta dxinv) s; its L2 norm by FMA and its max norm on
+// r = rhs - (alpha a) phi + (beta dxinv) s by two FMAs; its L2 norm by FMA and its max norm on
 // the bit patterns of |v| (for non-negative doubles the integer order is the
 // numeric order, and a NaN's pattern is above every number's, so it stays
 // sticky).  Half the reference-order kernel's FP64 pipe operations; the
@@ -288,8 +288,8 @@ __global__ void __launch_bounds__(kNLCBlock) nlc_res_lean_kernel(NLArgs<double> 
       }
       s = fma(-pl0[c], sb[q + c * n], s);
       const double aa = A.a ? A.alpha * A.a[q + c * n] : A.alpha;
-      const double lof = fma(aa, ph[c], -(bd * s));
-      const double v = rhs[q + c * n] - lof;
+      // rhs - (aa phi - bd s) as two FMAs
+      const double v = fma(bd, s, fma(-aa, ph[c], rhs[q + c * n]));
       out[q + c * n] = v;
       acc = fma(v, v, acc);
       const unsigned long long bits =

@@ -306,10 +306,11 @@ __global__ void __launch_bounds__(kBlock) vcl_outer_kernel(
         s = fma(A.b[d][G.face(d, fi[0], fi[1], fi[2])], pn - p0, s);
       }
     }
-    double lof = -(bd * s);
-    lof = fma(A.alpha * (A.a ? A.a[q] : 1.0), p0, lof);
-    if (A.c) lof = fma(-A.beta * A.c[q], p0, lof);
-    const double v = rhs[q] - lof;
+    // rhs - (alpha a p0 - beta c p0 - bd s) as FMAs from rhs
+    const double aa = A.a ? A.alpha * A.a[q] : A.alpha;
+    double t = fma(-aa, p0, rhs[q]);
+    if (A.c) t = fma(A.beta * A.c[q], p0, t);
+    const double v = fma(bd, s, t);
     if (e) out_phi[q] = p0;
     res_inner[cs_index(G, i, j, k)] = narrow_to<E>(v);
     if (NORM == MLGPU_NORM_MAX) {
