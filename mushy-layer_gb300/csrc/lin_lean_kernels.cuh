@@ -737,15 +737,33 @@ __global__ void __launch_bounds__(kBlock) lean_state_kernel(AdjArgs<T> A, Closur
                                                             T *__restrict__ Ds) {
   const Geom &G = A.G;
   const long long n = G.ncell;
-  for (long long q = gtid(); q < n; q += gstride()) {
+  // the next cell's state and face sums are loaded while this one is formed
+  long long q = gtid();
+  double hn = 0.0, cn = 0.0;
+  T pn0 = T(0), pn1 = T(0);
+  if (q < n) {
+    hn = u[q];
+    cn = u[q + n];
+    pn0 = Psum[q];
+    pn1 = Psum[n + q];
+  }
+  for (; q < n; q += gstride()) {
+    const double h0 = hn, c0 = cn;
+    const T P[2] = {pn0, pn1};
+    const long long qn = q + gstride();
+    if (qn < n) {
+      hn = u[qn];
+      cn = u[qn + n];
+      pn0 = Psum[qn];
+      pn1 = Psum[n + qn];
+    }
     int i, j, k;
     cell_ijk(G, q, i, j, k);
     T Jc[4], M[4];
     if constexpr (sizeof(T) == 4)
-      t_cl_jac32(u[q], u[q + n], A.cp, f, Jc);
+      t_cl_jac32(h0, c0, A.cp, f, Jc);
     else
-      t_cl_jac_lean(u[q], u[q + n], L, Jc);
-    const T P[2] = {Psum[q], Psum[n + q]};
+      t_cl_jac_lean(h0, c0, L, Jc);
     lean_diag_block<T, DIM>(A, q, i, j, k, Jc, P, M);
     const T det = M[0] * M[3] - M[1] * M[2];
     const long long o = cs_index(G, i, j, k);
