@@ -926,18 +926,32 @@ __global__ void __launch_bounds__(kBlock) lean_step_kernel(Geom G, StepClip K,
                                                            const T *__restrict__ e) {
   const long long n = G.ncell;
   const IDX at;
-  for (long long q = gtid(); q < n; q += gstride()) {
+  // the next cell's old state and correction are loaded while this one is
+  // updated
+  auto load = [&](long long q, double &h, double &c, T &eh, T &ec) {
     int i, j, k;
     cell_ijk(G, q, i, j, k);
     const long long o = at(G, i, j, k);
-    const double h0 = u_old[q], c0 = u_old[n + q];
+    h = u_old[q];
+    c = u_old[n + q];
+    eh = e[o];
+    ec = e[n + o];
+  };
+  long long q = gtid();
+  double hn = 0.0, cn = 0.0;
+  T ehn = T(0), ecn = T(0);
+  if (q < n) load(q, hn, cn, ehn, ecn);
+  for (; q < n; q += gstride()) {
+    const double h0 = hn, c0 = cn;
+    const T eh = ehn, ec = ecn;
+    if (q + gstride() < n) load(q + gstride(), hn, cn, ehn, ecn);
     double h1, c1;
     if constexpr (sizeof(T) == 4) {
-      h1 = h0 + scale * f64_exact(e[o]);
-      c1 = c0 + scale * f64_exact(e[n + o]);
+      h1 = h0 + scale * f64_exact(eh);
+      c1 = c0 + scale * f64_exact(ec);
     } else {
-      h1 = h0 + scale * (double)e[o];
-      c1 = c0 + scale * (double)e[n + o];
+      h1 = h0 + scale * (double)eh;
+      c1 = c0 + scale * (double)ec;
     }
     if (CLIP) {
       // FP32 regime test (truncated conversions: the near-bound band is 1e-4)
