@@ -16,26 +16,40 @@ __global__ void __launch_bounds__(kBlock) restrict_avg_kernel(Geom F, Geom C, in
   // exact (for results above the subnormal range), so the sum is the same
   // bits with half the FP64 pipe operations
   const T inv = DIM == 3 ? T(0.125) : T(0.25);
+  constexpr int NCH = DIM == 3 ? 8 : 4;
   long long total = C.ncell * ncomp;
-  for (long long t = gtid(); t < total; t += gstride()) {
-    int c = (int)(t / C.ncell);
-    long long Q = t % C.ncell;
+  // the children of the next coarse cell are loaded while this one is summed
+  auto load = [&](long long t, T v[NCH]) {
+    const int c = (int)(t / C.ncell);
+    const long long Q = t % C.ncell;
     int I, J, K;
     cell_ijk(C, Q, I, J, K);
-    T acc = T(0);
 #pragma unroll
     for (int kk = 0; kk < (DIM == 3 ? 2 : 1); kk++)
 #pragma unroll
       for (int jj = 0; jj < 2; jj++)
 #pragma unroll
         for (int ii = 0; ii < 2; ii++) {
-          int k = DIM == 3 ? 2 * K + kk : 0;
-          const T f = fine[c * F.ncell + F.cell(2 * I + ii, 2 * J + jj, k)];
-          if constexpr (sizeof(T) == 4)
-            acc = fmaf(f, inv, acc);
-          else
-            acc = fma(f, inv, acc);
+          const int k = DIM == 3 ? 2 * K + kk : 0;
+          v[(kk * 2 + jj) * 2 + ii] = fine[c * F.ncell + F.cell(2 * I + ii, 2 * J + jj, k)];
         }
+  };
+  long long t = gtid();
+  T nxt[NCH];
+  if (t < total) load(t, nxt);
+  for (; t < total; t += gstride()) {
+    T cur[NCH];
+#pragma unroll
+    for (int m = 0; m < NCH; m++) cur[m] = nxt[m];
+    if (t + gstride() < total) load(t + gstride(), nxt);
+    T acc = T(0);
+#pragma unroll
+    for (int m = 0; m < NCH; m++) {  // Fortran loop order: k, j outer, i fastest
+      if constexpr (sizeof(T) == 4)
+        acc = fmaf(cur[m], inv, acc);
+      else
+        acc = fma(cur[m], inv, acc);
+    }
     coarse[t] = acc;
   }
 }
