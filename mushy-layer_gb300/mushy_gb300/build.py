@@ -27,6 +27,8 @@ UNITS = {
     "launch_f64_adj.cu": ["--fmad=false"],
     "launch_f64_nlc.cu": ["--fmad=false"],
     "launch_f32.cu": [],
+    "launch_f32_fast.cu": [],
+    "launch_f32_nlr.cu": [],
     "launch_f32_adj.cu": [],
     "capi.cu": ["--fmad=false"],
     "solver.cu": ["--fmad=false"],
