@@ -407,6 +407,50 @@ def test_temperature_conditions_rejected_off_enthalpy():
     assert lib.mlgpu_vc_solver_workspace(C.byref(vc), C.byref(opts), C.byref(nbytes)) == abi.ERR_ARG
 
 
+def test_mixed_temperature_condition_validation():
+    """The mixed temperature condition (MLGPU_BC_MIXED_TEMPERATURE_SALINITY)
+    is accepted on the derived T only, with a nonzero Robin denominator, and
+    refused on C_l, on the (H, C) condition and on a linear operator; the
+    TGA step refuses a missing solver, null fields and dt <= 0 -- all before
+    any device work."""
+    lib = abi.load()
+    g = P.grid((8, 8))
+    nl = abi.NLOp()
+    nl.grid, nl.params, nl.dtype = g, P.mushy_params(), abi.F64
+    nl.apply_derived_bc = 1
+    opts = abi.MGOptions()
+    lib.mlgpu_mg_default_options(C.byref(opts), 1)
+    nbytes = C.c_size_t()
+
+    def ws():
+        return lib.mlgpu_hc_solver_workspace(C.byref(nl), C.byref(opts), C.byref(nbytes))
+
+    mixed = abi.BC_MIXED_TEMPERATURE_SALINITY
+    nl.nlbc = abi.make_nlbc(radiation={(1, 1): (0.5, -1.0, 4.0)})
+    nl.derived_bc = abi.make_bc({(1, 1, 0): (mixed, -0.5)})
+    assert ws() == 0
+    nl.derived_bc = abi.make_bc({(1, 1, 1): (mixed, -0.5)})  # on C_l
+    assert ws() == abi.ERR_ARG
+    nl.derived_bc = abi.make_bc({(1, 1, 0): (mixed, -0.5)})
+    nl.nlbc = abi.make_nlbc(radiation={(1, 1): (0.0, 0.0, 4.0)})  # a/dx - b/2 == 0
+    assert ws() == abi.ERR_ARG
+    nl.apply_derived_bc = 0  # the condition is not applied: nothing to check
+    assert ws() == 0
+    nl.apply_derived_bc = 1
+    nl.nlbc = abi.make_nlbc(radiation={(1, 1): (0.5, -1.0, 4.0)})
+    nl.derived_bc = abi.make_bc()
+    nl.phi_bc = abi.make_bc({(1, 1, 0): (mixed, -0.5)})  # on the (H, C) condition
+    assert ws() == abi.ERR_ARG
+    vc = abi.VCOp()
+    vc.grid = g
+    vc.bc = abi.make_bc({(1, 1, 0): (mixed, 0.0)})
+    lib.mlgpu_mg_default_options(C.byref(opts), 0)
+    assert lib.mlgpu_vc_solver_workspace(C.byref(vc), C.byref(opts), C.byref(nbytes)) == abi.ERR_ARG
+    st = abi.SolveStats()
+    buf = (C.c_double * 4)()
+    assert lib.mlgpu_hc_tga_step(None, buf, buf, None, None, 1e-3, buf, C.byref(st)) == abi.ERR_ARG
+
+
 def test_temperature_condition_large_residual_is_zeroed():
     """NonlinearTemperatureBCRobin zeroes a residual above 10 (the reference
     warns and leaves the ghost enthalpy at its guess): a fixed temperature 20
