@@ -266,6 +266,15 @@ cudaError_t launch_vcl_gsrb(const VCLeanT<T> &P, int pass, int zero, cudaStream_
 template <class T>
 cudaError_t launch_vcl_restrict(const VCLeanT<T> &P, const Geom &C, int csplit, int red, T *rc,
                                 T *ec, cudaStream_t s) {
+  constexpr int V = Vec16<T>::V;
+  if (red && ((P.G.n0 >> 1) % V) == 0 && C.n0 == (P.G.n0 >> 1)) {  // vector groups
+    const int nbv = blocks_for(C.ncell / V);
+    if (csplit)
+      MLGPU_DIM_SWITCH(P.G.dim, (vcl_restrict_vec_kernel<T, DIM, SplitIdx><<<nbv, kBlock, 0, s>>>(P, C, rc, ec)));
+    else
+      MLGPU_DIM_SWITCH(P.G.dim, (vcl_restrict_vec_kernel<T, DIM, NaturalIdx><<<nbv, kBlock, 0, s>>>(P, C, rc, ec)));
+    return cudaGetLastError();
+  }
   const int nb = blocks_for(C.ncell);
 #define MLGPU_VCL_RST(IDX, RED) \
   MLGPU_DIM_SWITCH(P.G.dim, (vcl_restrict_kernel<T, DIM, IDX, RED><<<nb, kBlock, 0, s>>>(P, C, rc, ec)))

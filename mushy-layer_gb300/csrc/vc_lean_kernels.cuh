@@ -125,75 +125,89 @@ __global__ void __launch_bounds__(kBlock) vcl_gsrb_kernel(VCLeanT<T> P, int pass
 // 1/diag, the y / z neighbours' e as 16-byte loads, the x neighbours' e as one
 // vector and one scalar, e stored as a vector); each cell's arithmetic in
 // vcl_gsrb_kernel's order (the same bits).  Needs n0 / 2 a multiple of V.
+// The neighbour sums of the V cells hh .. hh + V - 1 of colour `pass` in
+// row `row` = (j, k) of a split level (the other colour's e around them,
+// vcl_nbsum's order term by term: the same bits)
+template <class T, int DIM>
+__device__ __forceinline__ void vcl_vsum(const VCLeanT<T> &P, int pass, unsigned row, int hh,
+                                         int j, int k, T *s) {
+  constexpr int V = Vec16<T>::V;
+  const Geom &G = P.G;
+  const long long half = G.ncell >> 1;
+  const int h0 = G.n0 >> 1;
+  const long long obase = half - pass * half;
+  const long long pl = (long long)G.n0 * G.n1;
+  const T *e = P.e;
+  const int par = (j + k + pass) & 1;
+#pragma unroll
+  for (int v = 0; v < V; v++) s[v] = T(0);
+  {  // x: the other colour's e at hh - 1 + par .. hh + V - 1 + par of this row
+    const long long ob = obase + (long long)row * h0;
+    T wv[V];
+    ldv(e + ob + hh, wv);
+    int xe = par ? hh + V : hh - 1;
+    bool has_e = true;
+    if (xe < 0) {
+      xe = h0 - 1;
+      has_e = G.per0 != 0;
+    } else if (xe >= h0) {
+      xe = 0;
+      has_e = G.per0 != 0;
+    }
+    const T ev = has_e ? e[ob + xe] : T(0);
+    const long long f0 = (long long)row * (G.n0 + 1) + 2 * hh + par;
+#pragma unroll
+    for (int v = 0; v < V; v++) {
+      const long long f = f0 + 2 * v;
+      const int vl = v > 0 ? v - 1 : 0, vh = v < V - 1 ? v + 1 : V - 1;
+      const bool lo_e = par == 0 && v == 0;
+      if (!lo_e || has_e) s[v] = fmaT(P.b[0][f], lo_e ? ev : (par ? wv[v] : wv[vl]), s[v]);
+      const bool hi_e = par == 1 && v == V - 1;
+      if (!hi_e || has_e) s[v] = fmaT(P.b[0][f + 1], hi_e ? ev : (par ? wv[vh] : wv[v]), s[v]);
+    }
+  }
+#pragma unroll
+  for (int d = 1; d < DIM; d++) {
+    const int m = d == 1 ? G.n1 : G.n2, c = d == 1 ? j : k;
+    const bool per = d == 1 ? G.per1 != 0 : G.per2 != 0;
+    const long long step = d == 1 ? G.n0 : pl;
+    const long long fb = d == 1 ? ((long long)k * (G.n1 + 1) + j) * G.n0 + 2 * hh + par
+                                : (long long)row * G.n0 + 2 * hh + par;
+#pragma unroll
+    for (int side = 0; side < 2; side++) {
+      int cn = c + (side ? 1 : -1);
+      if (cn < 0 || cn >= m) {
+        if (!per || m == 1) continue;
+        cn = cn < 0 ? m - 1 : 0;
+      }
+      const unsigned nrow = d == 1 ? (unsigned)k * G.n1 + cn : (unsigned)cn * G.n1 + j;
+      T nb[V];
+      ldv(e + obase + (long long)nrow * h0 + hh, nb);
+#pragma unroll
+      for (int v = 0; v < V; v++)
+        s[v] = fmaT(P.b[d][fb + 2 * v + (side ? step : 0)], nb[v], s[v]);
+    }
+  }
+}
+
 template <class T, int DIM>
 __global__ void __launch_bounds__(kBlock) vcl_gsrb_vec_kernel(VCLeanT<T> P, int pass, int zero) {
   constexpr int V = Vec16<T>::V;
   const Geom &G = P.G;
-  const long long n = G.ncell, half = n >> 1;
+  const long long half = G.ncell >> 1;
   const int h0 = G.n0 >> 1;
-  const long long base = pass * half, obase = half - base;
+  const long long base = pass * half;
   const long long ngroups = half / V;
-  const long long pl = (long long)G.n0 * G.n1;
-  const T *e = P.e;
   for (long long t = gtid(); t < ngroups; t += gstride()) {
     const long long u = t * V;
     const unsigned row = (unsigned)u / (unsigned)h0;
     const int hh = (int)((unsigned)u - row * (unsigned)h0);
     const int k = (int)(row / (unsigned)G.n1), j = (int)(row - (unsigned)k * G.n1);
-    const int par = (j + k + pass) & 1;
     const long long q = base + u;
     T s[V];
 #pragma unroll
     for (int v = 0; v < V; v++) s[v] = T(0);
-    if (!zero) {
-      {  // x: the other colour's e at hh - 1 + par .. hh + V - 1 + par of this row
-        const long long ob = obase + (long long)row * h0;
-        T wv[V];
-        ldv(e + ob + hh, wv);
-        int xe = par ? hh + V : hh - 1;
-        bool has_e = true;
-        if (xe < 0) {
-          xe = h0 - 1;
-          has_e = G.per0 != 0;
-        } else if (xe >= h0) {
-          xe = 0;
-          has_e = G.per0 != 0;
-        }
-        const T ev = has_e ? e[ob + xe] : T(0);
-        const long long f0 = (long long)row * (G.n0 + 1) + 2 * hh + par;
-#pragma unroll
-        for (int v = 0; v < V; v++) {
-          const long long f = f0 + 2 * v;
-          const int vl = v > 0 ? v - 1 : 0, vh = v < V - 1 ? v + 1 : V - 1;
-          const bool lo_e = par == 0 && v == 0;
-          if (!lo_e || has_e) s[v] = fmaT(P.b[0][f], lo_e ? ev : (par ? wv[v] : wv[vl]), s[v]);
-          const bool hi_e = par == 1 && v == V - 1;
-          if (!hi_e || has_e) s[v] = fmaT(P.b[0][f + 1], hi_e ? ev : (par ? wv[vh] : wv[v]), s[v]);
-        }
-      }
-#pragma unroll
-      for (int d = 1; d < DIM; d++) {
-        const int m = d == 1 ? G.n1 : G.n2, c = d == 1 ? j : k;
-        const bool per = d == 1 ? G.per1 != 0 : G.per2 != 0;
-        const long long step = d == 1 ? G.n0 : pl;
-        const long long fb = d == 1 ? ((long long)k * (G.n1 + 1) + j) * G.n0 + 2 * hh + par
-                                    : (long long)row * G.n0 + 2 * hh + par;
-#pragma unroll
-        for (int side = 0; side < 2; side++) {
-          int cn = c + (side ? 1 : -1);
-          if (cn < 0 || cn >= m) {
-            if (!per || m == 1) continue;
-            cn = cn < 0 ? m - 1 : 0;
-          }
-          const unsigned nrow = d == 1 ? (unsigned)k * G.n1 + cn : (unsigned)cn * G.n1 + j;
-          T nb[V];
-          ldv(e + obase + (long long)nrow * h0 + hh, nb);
-#pragma unroll
-          for (int v = 0; v < V; v++)
-            s[v] = fmaT(P.b[d][fb + 2 * v + (side ? step : 0)], nb[v], s[v]);
-        }
-      }
-    }
+    if (!zero) vcl_vsum<T, DIM>(P, pass, row, hh, j, k, s);
     T r[V], id[V], out[V];
     ldv(P.r + q, r);
     ldv(P.idg + q, id);
@@ -233,6 +247,55 @@ __global__ void __launch_bounds__(kBlock) vcl_restrict_kernel(VCLeanT<T> P, Geom
     const long long o = CIDX()(C, I, J, K);
     rc[o] = a * wgt;
     ec[o] = T(0);
+  }
+}
+
+// vcl_restrict_kernel (RED) with V coarse cells of a coarse row per thread:
+// the red children of coarse cells I0 .. I0 + V - 1 in fine row (2J + jj,
+// 2K + kk) are that row's red cells I0 .. I0 + V - 1, one vector group per
+// child class (vcl_vsum), summed in the scalar kernel's order (the same bits)
+template <class T, int DIM, class CIDX>
+__global__ void __launch_bounds__(kBlock) vcl_restrict_vec_kernel(VCLeanT<T> P, Geom C,
+                                                                  T *__restrict__ rc,
+                                                                  T *__restrict__ ec) {
+  constexpr int V = Vec16<T>::V;
+  const Geom &G = P.G;
+  const int h0 = G.n0 >> 1;
+  const long long ngroups = C.ncell / V;
+  const T wgt = DIM == 3 ? T(0.125) : T(0.25);
+  const CIDX at;
+  for (long long t = gtid(); t < ngroups; t += gstride()) {
+    const long long U = t * V;
+    const unsigned crow = (unsigned)U / (unsigned)C.n0;
+    const int I0 = (int)((unsigned)U - crow * (unsigned)C.n0);
+    const int K = (int)(crow / (unsigned)C.n1), J = (int)(crow - (unsigned)K * C.n1);
+    T a[V];
+#pragma unroll
+    for (int v = 0; v < V; v++) a[v] = T(0);
+#pragma unroll
+    for (int kk = 0; kk < (DIM == 3 ? 2 : 1); kk++)
+#pragma unroll
+      for (int jj = 0; jj < 2; jj++)
+#pragma unroll
+        for (int ii = 0; ii < 2; ii++) {
+          if ((ii + jj + kk) & 1) continue;  // black child
+          const int j = 2 * J + jj, k = DIM == 3 ? 2 * K + kk : 0;
+          const unsigned row = (unsigned)k * G.n1 + j;
+          const long long q = (long long)row * h0 + I0;
+          T s[V], r[V], dg[V], e[V];
+          vcl_vsum<T, DIM>(P, 0, row, I0, j, k, s);
+          ldv(P.r + q, r);
+          ldv(P.dg + q, dg);
+          ldv(P.e + q, e);
+#pragma unroll
+          for (int v = 0; v < V; v++) a[v] += fmaT(P.bd, s[v], r[v]) - dg[v] * e[v];
+        }
+#pragma unroll
+    for (int v = 0; v < V; v++) {
+      const long long o = at(C, I0 + v, J, K);
+      rc[o] = a[v] * wgt;
+      ec[o] = T(0);
+    }
   }
 }
 
