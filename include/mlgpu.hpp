@@ -368,6 +368,19 @@ class Solver {
     mlgpu_grid g = {2, {1, 1, 1}, 1.0, {0, 0, 0}};
     ws_.reset(new DeviceField(g, 1, MLGPU_F64, bytes / 8 + 64));
   }
+  // mlgpu_hc_tga_step on solver h with its two-field scratch
+  static mlgpu_solve_stats tga_step(mlgpu_solver *h, DeviceField &phi_new,
+                                    const DeviceField &phi_old, double dt, const DeviceField *src,
+                                    const DeviceField *aCoef, const char *what) {
+    DeviceField scratch(phi_old.grid(), 2 * phi_old.ncomp(), phi_old.dtype());
+    mlgpu_solve_stats st;
+    int rc = mlgpu_hc_tga_step(h, (double *)phi_new.data(), (const double *)phi_old.data(),
+                               src ? (const double *)src->data() : nullptr,
+                               aCoef ? (const double *)aCoef->data() : nullptr, dt,
+                               (double *)scratch.data(), &st);
+    tolerate(rc, what);
+    return st;
+  }
   // the workspace must be 256-byte aligned, which every device allocation
   // made through the library (cudaMalloc) is
   void *ws() { return ws_->data(); }
@@ -405,6 +418,12 @@ class AMRFASMultiGrid : public Solver {
                                      (double *)scratch.data(), &st);
     tolerate(rc, "AMRFASMultiGrid::backwardEuler");
     return st;
+  }
+  // LevelTGA::updateSoln: (a - mu1 dt L) psi = (a + mu3 dt L) phi_old + dt src,
+  // (a - mu2 dt L) phi_new = a psi (mlgpu_hc_tga_step, FAS solves)
+  mlgpu_solve_stats tgaStep(DeviceField &phi_new, const DeviceField &phi_old, double dt,
+                            const DeviceField *src = nullptr, const DeviceField *aCoef = nullptr) {
+    return tga_step(h_, phi_new, phi_old, dt, src, aCoef, "AMRFASMultiGrid::tgaStep");
   }
 };
 
@@ -465,6 +484,11 @@ class AdjointMultiGrid : public Solver {
     int rc = mlgpu_hc_newton_solve(h_, (double *)phi.data(), (const double *)rhs.data(), &st);
     tolerate(rc, "AdjointMultiGrid::newtonSolve");
     return st;
+  }
+  // the TGA step with Newton's solves (mlgpu_hc_tga_step on this solver)
+  mlgpu_solve_stats tgaStep(DeviceField &phi_new, const DeviceField &phi_old, double dt,
+                            const DeviceField *src = nullptr, const DeviceField *aCoef = nullptr) {
+    return tga_step(h_, phi_new, phi_old, dt, src, aCoef, "AdjointMultiGrid::tgaStep");
   }
   // adjoint of AMRFASMultiGrid::backwardEuler: A^T mu = phi_new_bar, then
   // phi_old_bar = a mu, src_bar = dt mu and the wall-value gradient

@@ -1,8 +1,8 @@
 // host_classes.cpp -- drives the C++ host classes of include/mlgpu.hpp on one
 // GPU with the reference's method names: reads the fields written by
 // tests/test_cpp_host.py, runs residual / levelGSRB / MGnewOp + restrictR +
-// applyOp / an AMRFASMultiGrid solve / an AMRMultiGrid projection solve, and
-// writes each result for comparison with the oracle.
+// applyOp / an AMRFASMultiGrid solve and TGA step / an AMRMultiGrid projection
+// solve, and writes each result for comparison with the oracle.
 // Usage: host_classes <dir> <nx> <ny>
 #include <cstdio>
 #include <cstdlib>
@@ -93,6 +93,11 @@ int main(int argc, char **argv) {
     mlgpu::AMRFASMultiGrid fas(op);
     const mlgpu_solve_stats st = fas.solve(u, rhs);
     save(dir + "/out_fas.bin", fetch(u));
+    // one TGA step from phi (dt 1e-3) on the same solver
+    mlgpu::DeviceField ut(g, 2);
+    ut.copyFrom(phi);
+    fas.tgaStep(ut, phi, 1e-3);
+    save(dir + "/out_tga.bin", fetch(ut));
 
     // ---- projection operator: div(Pi grad p) = f, Neumann walls
     mlgpu::DeviceField p0(g, 1, MLGPU_F64, mlgpu::faces(g, 0));

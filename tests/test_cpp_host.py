@@ -77,6 +77,8 @@ def test_cpp_host_classes_match_oracle(tmp_path):
     sol, st, rc = O.hc_solve(ref, O.default_options(1), phi, rhs)
     assert stats["fas_iterations"] == st.iterations and stats["fas_status"] == st.exit_status
     assert np.array_equal(out("fas", phi.shape), sol)
+    tga, st_t, rc_t = O.hc_tga_step(ref, O.default_options(1), phi, phi, 1e-3)
+    assert np.array_equal(out("tga", phi.shape), tga)
     vref = O.VCOpHost(g, abi.make_bc(), 0.0, 1.0, None, vb)
     cvb = [O.coarsen_faces(g, 1, d, vb[d]) for d in range(2)]
     cvref = O.VCOpHost(cg, abi.make_bc(), 0.0, 1.0, None, cvb)
