@@ -402,6 +402,18 @@ class Inputs:
                 setattr(o, field, v)
         return o
 
+    def time_integration_order(self):
+        """main.time_integration_order (srcSubcycle/MushyLayerSubcycleUtils.cpp:
+        625-626, default 1): 1 takes the (H, C) step by backward Euler
+        (mlgpu_hc_backward_euler / backwardEuler), 2 by the TGA scheme
+        (mlgpu_hc_tga_step / tgaStep), as AMRLevelMushyLayer.cpp:1766-1779
+        chooses."""
+        order = self.get("main.time_integration_order", 1, int)
+        if order not in (1, 2):
+            raise ValueError("main.time_integration_order = %d: 1 (backward Euler) or 2 (TGA)"
+                             % order)
+        return order
+
     def hc_options(self):
         """HCMultigrid.* (srcSubcycle/MushyLayerSubcycleUtils.cpp:668-692)."""
         o = self._options(True, [

@@ -305,3 +305,19 @@ def test_poiseuille_inputs_give_the_pinned_coefficients():
     assert p.darcyCoeff == 1 / 0.01 == 100.0 and p.viscosityCoeff == 1.0
     g = inp.grid(2)
     assert list(g.n)[:2] == [64, 64] and g.dx == 1.0 / 64
+
+
+def test_time_integration_order():
+    """main.time_integration_order picks the (H, C) step: the reference's
+    unit-test and restart-regression inputs ask for TGA (2), its
+    diffusive-growth inputs for backward Euler (1); absent, 1."""
+    assert mi.Inputs.parse("main.num_cells = 8 8\n").time_integration_order() == 1
+    assert mi.Inputs.parse("main.time_integration_order = 2\n").time_integration_order() == 2
+    with pytest.raises(ValueError, match="time_integration_order"):
+        mi.Inputs.parse("main.time_integration_order = 3\n").time_integration_order()
+    cases = [(REF_INPUTS, 2),
+             (os.path.join(os.path.dirname(REG), "diffusiveGrowth", "inputs"), 1),
+             (os.path.join(REG, "AMRRestartDarcyBrinkman", "inputs"), 2)]
+    for path, order in cases:
+        if os.path.exists(path):
+            assert mi.Inputs.read(path).time_integration_order() == order, path
